@@ -1,0 +1,216 @@
+/*
+ * sem2d_gpu.h -- C-ABI of the GB300 spectral-element time step.
+ *
+ * This is the drop-in boundary for SEM2DPACK's explicit time step.  In the
+ * reference the step is the Fortran call chain
+ *     main.f90:54        call solve(pb)
+ *     solver.f90:140-161 solve_leapfrog  /  solver.f90:42-83 solve_Newmark
+ *     solver.f90:273-316 compute_Fint  (gather, MAT_Fint, scatter-add)
+ *     src_gen.f90:290    SO_add        (point forces x Ricker)
+ *     bc_gen.f90:256     BC_apply      (absorbing, then dynamic fault)
+ *     receivers.f90:309  REC_store     (seismogram sampling)
+ *     bc_dynflt.f90:751  BC_DYNFLT_write (fault time series)
+ * over the state held in problem_type (problem_class.f90:19-46).
+ *
+ * sem2d_gpu_create() receives the arrays exactly as the reference's
+ * init_main (init.f90:16-131) leaves them: Fortran column-major order,
+ * 1-based node numbers, the inverted mass already folded with the absorbing
+ * dashpots, the fault impedance Z and the snapshots invM1/invM2.  The
+ * library deep-copies everything to the device and keeps its own layout.
+ *
+ * All functions return 0 on success and a negative SEM2D_E_* code on
+ * failure; sem2d_gpu_last_error() then returns a message (the Fortran side
+ * maps a non-zero status to IO_abort, stdio.f90:205-213).  A handle is used
+ * by one host thread at a time and owns one CUDA stream.
+ */
+#ifndef SEM2D_GPU_H
+#define SEM2D_GPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEM2D_GPU_ABI_VERSION 1
+
+/* status codes */
+#define SEM2D_OK 0
+#define SEM2D_E_ARG (-1)         /* bad argument or inconsistent sizes        */
+#define SEM2D_E_CUDA (-2)        /* CUDA runtime error                        */
+#define SEM2D_E_UNSUPPORTED (-3) /* mesh or option outside the GPU path      */
+#define SEM2D_E_NR (-4)          /* rate-and-state Newton solver did not converge */
+#define SEM2D_E_NAN (-5)         /* non-finite field value detected           */
+#define SEM2D_E_STATE (-6)       /* call out of sequence                      */
+#define SEM2D_E_NOMEM (-7)       /* device or host allocation failed          */
+
+/* time schemes (time.f90:122-315) */
+#define SEM2D_TIME_LEAPFROG 0
+#define SEM2D_TIME_NEWMARK 1
+
+/* friction laws (bc_dynflt.f90:200-213) */
+#define SEM2D_FRICTION_SWF 1
+#define SEM2D_FRICTION_RSF 2
+
+/* arithmetic of the bulk fields */
+#define SEM2D_PRECISION_FP64 0  /* everything in FP64                       */
+#define SEM2D_PRECISION_MIXED 1 /* FP32 fields/forces, FP64 fault state     */
+
+typedef struct sem2d_problem_desc {
+  /* ---- sizes (spec_grid.f90:49-64, fields.f90:7-11) ---- */
+  int ngll;  /* GLL nodes per element edge                        */
+  int ndof;  /* 1 = SH (antiplane), 2 = P-SV (in-plane)           */
+  int nelem; /* number of spectral elements                       */
+  int npoin; /* number of global GLL nodes                        */
+
+  /* ---- grid ---- */
+  const int *ibool;      /* ibool(ngll,ngll,nelem), 1-based global node      */
+  const double *coord;   /* coord(2,npoin)                                   */
+  const double *hprime;  /* hprime(ngll,ngll), H(i,j) = h'_i(xgll(j))        */
+  const double *wgll;    /* wgll(ngll)                                       */
+
+  /* ---- elastic moduli at every element GLL point, (ngll,ngll,nelem) ----
+   * mat_elastic.f90:307-321: isotropic -> Kx=Kz=lambda+2mu, la=lambda,
+   * mu=mux=mu; VTI -> Kx=c11, Kz=c33, la=c13, mu=c55, mux=c66.          */
+  const double *Kx, *Kz, *la, *mu, *mux;
+  /* Kelvin-Voigt viscosity eta (already multiplied by dt when ETAxDT),
+   * (ngll,ngll,nelem); NULL when no element is Kelvin-Voigt
+   * (mat_kelvin_voigt.f90:117-151).                                     */
+  const double *kv_eta;
+  /* 1 selects the NGLL=5 specialised kernel ELAST_KD2_* of the reference
+   * (mat_elastic.f90:589-641), whose flat P-SV shear term uses a4 for both
+   * derivatives; 0 selects ELAST_KD1_* (mat_elastic.f90:464-518).       */
+  int kd2_form;
+
+  /* ---- inverted mass rmass(npoin,ndof), absorbing fold included ---- */
+  const double *rmass;
+
+  /* ---- absorbing boundaries (bc_abso.f90:115-336), one entry per
+   * (boundary, node); a node on two boundaries appears twice.          */
+  int nabs;
+  const int *abs_node;  /* [nabs], 1-based                                  */
+  const double *abs_C;  /* abs_C(nabs,ndof) dashpot rho*c*w*|J1D|           */
+
+  /* ---- time scheme (time.f90) ---- */
+  int time_scheme; /* SEM2D_TIME_*                                          */
+  double dt;
+  double beta, gamma; /* Newmark parameters (ignored by leapfrog)          */
+  int nt;             /* total number of steps the caller intends to run    */
+
+  /* ---- point-force sources with a Ricker time function
+   * (src_gen.f90:290-317, src_force.f90:77-92, stf_ricker.f90:89-103) */
+  int nsrc;
+  const int *src_node;      /* [nsrc], 1-based                               */
+  const double *src_dir;    /* src_dir(2,nsrc): (-sin a, cos a); SH uses 1   */
+  const double *src_f0;     /* [nsrc] Ricker centre frequency               */
+  const double *src_t0;     /* [nsrc] Ricker onset                          */
+  const double *src_ampli;  /* [nsrc] Ricker amplitude                      */
+  const double *src_relamp; /* [nsrc] relative amplitude (file column 4) or NULL */
+  const double *src_tdelay; /* [nsrc] time delay                            */
+
+  /* ---- receivers (receivers.f90:231-344) ---- */
+  int nrec;
+  char rec_field;          /* 'D', 'V' or 'A'                                */
+  int rec_isamp;           /* sampling stride in steps                       */
+  int rec_nsamp;           /* samples stored = nt/isamp + 1                  */
+  const int *rec_node;     /* [nrec] 1-based node (AtNode) or NULL           */
+  const int *rec_elem;     /* [nrec] 1-based element (interpolated) or NULL  */
+  const double *rec_interp;/* interp(ngll*ngll,nrec) Lagrange weights        */
+
+  /* ---- dynamic fault (bc_dynflt.f90:231-778); nflt = 0 if none ---- */
+  int nflt;
+  const int *flt_node1;    /* [nflt], 1-based, side 1                        */
+  const int *flt_node2;    /* [nflt], 1-based, side 2; NULL = one-sided      */
+  const double *flt_n1;    /* n1(nflt,2) normal of side 1                    */
+  const double *flt_B;     /* B(nflt) boundary weights                       */
+  const double *flt_invM1; /* invM1(nflt,ndof)                               */
+  const double *flt_invM2; /* invM2(nflt,ndof) or NULL                       */
+  const double *flt_Z;     /* Z(nflt,ndof) impedance                         */
+  const double *flt_T0;    /* T0(nflt,2) initial (tangent, normal) traction  */
+  const double *flt_cohesion; /* [nflt]                                      */
+  double flt_coefA2V, flt_coefA2D;
+  int flt_opening;         /* allow opening (T_n <= 0)                       */
+  int flt_friction;        /* SEM2D_FRICTION_*                               */
+  int swf_kind;            /* 1 linear, 2 exponential, 3 power law           */
+  int swf_healing;
+  const double *swf_dc, *swf_mus, *swf_mud, *swf_p, *swf_alpha; /* [nflt] */
+  int rsf_kind;            /* 1..4 (bc_dynflt_rsf.f90:40-48)                 */
+  const double *rsf_dc, *rsf_mus, *rsf_a, *rsf_b, *rsf_vstar, *rsf_vc;
+  const double *rsf_theta; /* [nflt] initial state                           */
+  const double *flt_V0;    /* [nflt] initial slip rate (RSF) or NULL         */
+  int normal_kind;         /* 0..3 (bc_dynflt_normal.f90)                    */
+  double normal_T, normal_L, normal_V;
+  /* output sampling (bc_dynflt.f90:436-440): first step oit, stride oitd,
+   * nodes oix1..oixn step oixd (1-based), flt_nsamp samples              */
+  int flt_oit, flt_oitd, flt_oix1, flt_oixn, flt_oixd, flt_nsamp;
+
+  /* ---- options ---- */
+  int precision; /* SEM2D_PRECISION_*                                      */
+} sem2d_problem_desc;
+
+typedef struct sem2d_handle sem2d_handle;
+
+/* Library ABI version (SEM2D_GPU_ABI_VERSION). */
+int sem2d_gpu_version(void);
+
+/* Number of visible CUDA devices, or a negative status. */
+int sem2d_gpu_device_count(void);
+
+/* Replaces the start of the time loop, init.f90:16-131 -> main.f90:51:
+ * uploads the problem and records the step-0 outputs (main.f90:35,
+ * bc_gen.f90:247).  *out receives a new handle. */
+int sem2d_gpu_create(const sem2d_problem_desc *desc, sem2d_handle **out);
+
+/* Replaces nsteps iterations of `do it=1,nt; call solve(pb); REC_store;
+ * BC_write` (main.f90:51-96).  Asynchronous on the handle's stream; the
+ * status of device-side checks is reported by the next call that
+ * synchronises (get_* / sync / destroy). */
+int sem2d_gpu_step(sem2d_handle *h, int nsteps);
+
+/* Waits for all queued steps; returns device-side error status. */
+int sem2d_gpu_sync(sem2d_handle *h);
+
+/* Steps completed so far. */
+int sem2d_gpu_current_step(sem2d_handle *h);
+
+/* Copies displ, veloc, accel (npoin,ndof) in the reference's global
+ * numbering into caller buffers; any pointer may be NULL. */
+int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc,
+                         double *accel);
+
+/* Copies seismograms sis(rec_nsamp,nrec,ndof) (receivers.f90:12) as FP64;
+ * samples not yet recorded are zero. */
+int sem2d_gpu_get_seismograms(sem2d_handle *h, double *sis);
+
+/* Copies the fault time series as FP64, laid out (onx, 6, flt_nsamp) with
+ * the 6 records of BC_DYNFLT_write: slip, slip rate, shear traction,
+ * normal traction, friction coefficient, T_stick (bc_dynflt.f90:760-767). */
+int sem2d_gpu_get_fault(sem2d_handle *h, double *out);
+
+/* Current fault state D(nflt,ndof), V(nflt,ndof), T(nflt,2), MU(nflt),
+ * state variable theta(nflt) (RSF, else zeros); any pointer may be NULL. */
+int sem2d_gpu_get_fault_state(sem2d_handle *h, double *D, double *V,
+                              double *T, double *MU, double *theta);
+
+/* Returns the handle to its state right after create (zero fields, step
+ * 0, initial fault state); the uploaded problem is kept.  Lets a caller
+ * rerun the same problem without a new upload. */
+int sem2d_gpu_reset(sem2d_handle *h);
+
+/* Kernels launched by this handle since creation (graph replays count
+ * every kernel node). */
+long long sem2d_gpu_kernel_launches(sem2d_handle *h);
+
+/* Element tile (TX x TZ elements per CTA) chosen for the bulk kernel. */
+int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz);
+
+/* Releases device memory; h becomes invalid. */
+int sem2d_gpu_destroy(sem2d_handle *h);
+
+/* Message of the last failed call on h (or of the last failed create when
+ * h is NULL). */
+const char *sem2d_gpu_last_error(sem2d_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEM2D_GPU_H */

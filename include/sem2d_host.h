@@ -1,0 +1,184 @@
+/*
+ * sem2d_host.h -- host-side problem builder (the reference's input and
+ * initialisation phases for the Cartesian solver path).
+ *
+ * The reference reads a Par.inp of Fortran NAMELIST blocks (input.f90:12-62)
+ * and builds the solver state in init_main (init.f90:16-131).  sem2d_deck
+ * carries the values of the blocks this path uses; the builder restates
+ *   MESH_CART  / MESH_CART_DOMAIN   mesh_cartesian.f90:86-314
+ *   element renumbering (RCM)       mesh_structured.f90:204-269, rcm.f90
+ *   GLL numbering, coordinates      spec_grid.f90:149-374
+ *   boundary node tables            spec_grid.f90:676-822
+ *   materials, CHECK_grid, TIME     mat_gen.f90:204-303, init.f90:145-289,
+ *                                   time.f90:323-341
+ *   mass, absorbing fold, fault     mat_mass.f90:29-61, bc_abso.f90:115-266,
+ *                                   bc_dynflt.f90:231-520
+ *   sources, receivers              src_gen.f90:216-262, receivers.f90:168-303
+ * and fills a sem2d_problem_desc for sem2d_gpu_create().
+ *
+ * Spatially variable inputs (the DIST_* blocks of the reference) are given
+ * as arrays already evaluated at the GLL points (materials) or at the fault
+ * nodes (fault parameters); sem2d_grid_* exposes the coordinates and the
+ * boundary node tables needed to evaluate them.
+ */
+#ifndef SEM2D_HOST_H
+#define SEM2D_HOST_H
+
+#include "sem2d_gpu.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SEM2D_MAX_DOMAINS 64
+#define SEM2D_MAX_MATS 64
+#define SEM2D_MAX_BCS 16
+
+/* &MESH_CART_DOMAIN tag, ex, ez (mesh_cartesian.f90:64-79), 1-based */
+typedef struct sem2d_domain {
+  int tag;
+  int ex[2];
+  int ez[2];
+} sem2d_domain;
+
+/* &MATERIAL tag + &MAT_ELASTIC (+ &MAT_KV) (mat_elastic.f90:69-189) */
+typedef struct sem2d_material {
+  int tag;
+  int aniso;  /* 0: rho, cp, cs;  1: rho, c11, c13, c33, c55, c66       */
+  double rho, cp, cs;
+  double c11, c13, c33, c55, c66;
+  int hetero; /* 1: the values of this tag come from the deck's h_* arrays */
+  int kv;     /* Kelvin-Voigt damping present                           */
+  double kv_eta;
+  int kv_etaxdt; /* eta given in units of dt (ETAxDT, default true)      */
+} sem2d_material;
+
+/* &BC_DEF kind, tag(s) (bc_gen.f90:84-186) */
+#define SEM2D_BC_ABSORB 1
+#define SEM2D_BC_DYNFLT 2
+typedef struct sem2d_bc {
+  int kind;
+  int tag[2];
+} sem2d_bc;
+
+/* Per-node fault inputs of &BC_DYNFLT, &BC_DYNFLT_SWF and &BC_DYNFLT_RSF */
+enum {
+  SEM2D_FP_TT = 0, SEM2D_FP_TN, SEM2D_FP_SXX, SEM2D_FP_SXY, SEM2D_FP_SXZ,
+  SEM2D_FP_SYZ, SEM2D_FP_SZZ, SEM2D_FP_COHESION, SEM2D_FP_V0,
+  SEM2D_FP_SWF_DC, SEM2D_FP_SWF_MUS, SEM2D_FP_SWF_MUD, SEM2D_FP_SWF_P,
+  SEM2D_FP_SWF_ALPHA,
+  SEM2D_FP_RSF_DC, SEM2D_FP_RSF_MUS, SEM2D_FP_RSF_A, SEM2D_FP_RSF_B,
+  SEM2D_FP_RSF_VSTAR, SEM2D_FP_RSF_THETA, SEM2D_FP_RSF_VC,
+  SEM2D_FP_NPARAM
+};
+
+typedef struct sem2d_deck {
+  /* &GENERAL (input.f90:101-169) */
+  int ngll, ndof;
+  double fmax;
+
+  /* &MESH_CART */
+  double xlim[2], zlim[2];
+  int nelem[2];
+  int ezflt;  /* 0 none, -1 middle, k>0 fault above element row k      */
+  int fztag, fznz;
+  int ndomains;
+  sem2d_domain domains[SEM2D_MAX_DOMAINS];
+
+  /* materials */
+  int nmats;
+  sem2d_material mats[SEM2D_MAX_MATS];
+  /* per element GLL point values (ngll,ngll,nelem) for hetero tags */
+  const double *h_rho, *h_cp, *h_cs;
+  const double *h_c11, *h_c13, *h_c33, *h_c55, *h_c66;
+  const double *h_kveta;
+
+  /* boundary conditions in &BC_DEF order (the order matters:
+   * bc_gen.f90:229-246) */
+  int nbcs;
+  sem2d_bc bcs[SEM2D_MAX_BCS];
+
+  /* the dynamic fault (at most one DYNFLT boundary) */
+  int flt_friction;   /* SEM2D_FRICTION_SWF or SEM2D_FRICTION_RSF          */
+  int swf_kind, swf_healing, rsf_kind;
+  int normal_kind;
+  double normal_T, normal_L, normal_V;
+  int flt_opening;
+  double flt_ot1, flt_otd;
+  int flt_oxi[3];     /* first, last (<=0: last fault node), stride        */
+  double flt_value[SEM2D_FP_NPARAM];        /* uniform values            */
+  const double *flt_array[SEM2D_FP_NPARAM]; /* or per fault node (NULL)   */
+
+  /* &TIME (time.f90:122-315) */
+  int time_kind;      /* SEM2D_TIME_*                                       */
+  double dt;          /* > 0: fixed timestep                                */
+  double courant;     /* used when dt == 0                                  */
+  double total_time;  /* > 0: sets nsteps                                   */
+  int nsteps;
+  double beta, gamma; /* &TIME_NEWMARK                                      */
+
+  /* &SRC_DEF (FORCE mechanism, RICKER time function) */
+  int nsrc;
+  const double *src_coord;  /* (2,nsrc) requested positions                */
+  const double *src_tdelay; /* [nsrc] or NULL                              */
+  const double *src_ampli;  /* [nsrc] or NULL                              */
+  double ricker_f0, ricker_onset, ricker_ampli; /* read as REAL (FP32)     */
+  double force_angle;       /* degrees, counterclockwise from z-up          */
+
+  /* &REC_LINE (receivers.f90:62-163) */
+  int rec_number;
+  double rec_first[2], rec_last[2];
+  const double *rec_coord;  /* (2,rec_number) explicit positions or NULL   */
+  int rec_atnode;
+  int rec_isamp;
+  char rec_field;
+
+  /* options passed through to the descriptor */
+  int precision;  /* SEM2D_PRECISION_*                                      */
+  int kd2_form;   /* -1: as the reference (ngll == 5), 0 or 1 to force     */
+} sem2d_deck;
+
+typedef struct sem2d_grid sem2d_grid;
+typedef struct sem2d_problem sem2d_problem;
+
+/* Mesh + spectral grid (MESH_build then SE_init, init.f90:53-54). */
+int sem2d_grid_build(const sem2d_deck *deck, sem2d_grid **out);
+int sem2d_grid_sizes(const sem2d_grid *g, int *nelem, int *npoin, int *ngll);
+/* ibool(ngll,ngll,nelem) 1-based, coord(2,npoin), tag(nelem) */
+int sem2d_grid_ibool(const sem2d_grid *g, int *ibool);
+int sem2d_grid_coord(const sem2d_grid *g, double *coord);
+int sem2d_grid_tags(const sem2d_grid *g, int *tag);
+/* Bulk nodes of boundary `tag` sorted along the boundary
+ * (BC_set_bulk_node, spec_grid.f90:676-822); *npoin receives the count,
+ * nodes (1-based) may be NULL to query the size. */
+int sem2d_grid_boundary(const sem2d_grid *g, int tag, int *npoin, int *nodes);
+/* GLL points, weights and H (gll.f90:19-36). */
+int sem2d_grid_gll(const sem2d_grid *g, double *xgll, double *wgll,
+                   double *hprime);
+void sem2d_grid_destroy(sem2d_grid *g);
+
+/* Everything else of init_main; the grid must outlive the problem. */
+int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck,
+                        sem2d_problem **out);
+/* Descriptor whose arrays point into the problem (valid until destroy). */
+int sem2d_problem_get_desc(const sem2d_problem *p, sem2d_problem_desc *out);
+/* Timestep and the Courant number obtained (TIME_init). */
+int sem2d_problem_time(const sem2d_problem *p, double *dt, int *nt,
+                       double *courant);
+/* Positions of receivers and sources after relocation, (2,n). */
+int sem2d_problem_rec_coord(const sem2d_problem *p, double *coord);
+int sem2d_problem_fault_coord(const sem2d_problem *p, double *coord);
+void sem2d_problem_destroy(sem2d_problem *p);
+
+/* Message of the last failed builder call (thread local). */
+const char *sem2d_host_last_error(void);
+
+/* sizeof(sem2d_problem_desc) and sizeof(sem2d_deck) as compiled, so that
+ * foreign-language bindings can check their struct layouts. */
+int sem2d_abi_struct_sizes(int *desc_size, int *deck_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SEM2D_HOST_H */

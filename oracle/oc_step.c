@@ -1,0 +1,734 @@
+/*
+ * ORACLE (test infrastructure only -- never part of the product path).
+ *
+ * FP64 restatement of SEM2DPACK's explicit time step, driven by the same
+ * sem2d_problem_desc the GPU library receives:
+ *   solve_leapfrog / solve_Newmark   solver.f90:42-83, 140-161
+ *   compute_Fint                      solver.f90:273-316, fields.f90:113-189
+ *   MAT_Fint -> MAT_KV_add_etav       mat_gen.f90:418-460,
+ *               MAT_ELAST_f            mat_kelvin_voigt.f90:137-151,
+ *               ELAST_KD1/KD2_PSV/SH   mat_elastic.f90:396-775
+ *   a coefficients (MAT_ELAST_init_a) mat_elastic.f90:290-360
+ *   SO_add + FORCE_add + ricker       src_gen.f90:290-317,
+ *                                     src_force.f90:77-92, stf_ricker.f90:89-103
+ *   BC_ABSO_apply                     bc_abso.f90:286-336
+ *   BC_DYNFLT_apply                   bc_dynflt.f90:569-739
+ *   swf_*                             bc_dynflt_swf.f90:142-194
+ *   rsf_*                             bc_dynflt_rsf.f90:165-568
+ *   normal_update                     bc_dynflt_normal.f90:106-133
+ *   REC_store                         receivers.f90:309-344
+ *   BC_DYNFLT_write                   bc_dynflt.f90:751-778
+ * Operation order follows the Fortran expressions; compile without FMA
+ * contraction.
+ */
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "sem2d_oracle.h"
+
+#define PI_REF 3.141592653589793
+#define V_HEALING 1.0e-14 /* bc_dynflt_swf.f90:27 */
+#define NR_MAXIT 200      /* bc_dynflt_rsf.f90:372 */
+#define NR_MAXBRACKET 200 /* the reference loop at :393-398 has no bound */
+
+struct oc_sim {
+  int ngll, ndof, nelem, npoin, nelast, kd2;
+  int *ibool;
+  double *H;
+  double *acoef; /* (ngll,ngll,nelast,nelem) */
+  double *kveta;
+  double *rmass;
+  int nabs;
+  int *abs_node;
+  double *abs_C;
+  int scheme;
+  double dt, beta, gamma;
+  int nt;
+  int nsrc;
+  int *src_node;
+  double *src_dir, *src_f0, *src_t0, *src_amp, *src_rel, *src_tdelay;
+  int nrec, rec_isamp, rec_nsamp;
+  char rec_field;
+  int *rec_node, *rec_elem;
+  double *rec_interp;
+  double *sis;
+  /* fault */
+  int nflt, two, friction, swf_kind, swf_healing, rsf_kind, normal_kind, opening;
+  int *node1, *node2;
+  double *n1, *B, *invM1, *invM2, *Z, *T0, *coh;
+  double coefA2V, coefA2D, nT, nL, nV, ncoef;
+  double *swf_dc, *swf_mus, *swf_mud, *swf_p, *swf_alpha, *theta;
+  double *rsf_dc, *rsf_mus, *rsf_a, *rsf_b, *rsf_vstar, *rsf_vc, *rsf_Tc, *rsf_coeft;
+  double *D, *V, *T, *Tstick, *MU, *sigma;
+  int oit, oitd, oix1, oixn, oixd, fnsamp, onx, fsamp;
+  double *fseries;
+  /* fields */
+  double *d, *v, *a;
+  int it;
+  int status;
+};
+
+static void *xcalloc(size_t n, size_t sz) {
+  void *p = calloc(n ? n : 1, sz);
+  if (!p) {
+    fprintf(stderr, "oracle: out of memory\n");
+    abort();
+  }
+  return p;
+}
+static double *dupd(const double *src, size_t n) {
+  if (!src) return NULL;
+  double *p = xcalloc(n, sizeof(double));
+  memcpy(p, src, n * sizeof(double));
+  return p;
+}
+static int *dupi(const int *src, size_t n) {
+  if (!src) return NULL;
+  int *p = xcalloc(n, sizeof(int));
+  memcpy(p, src, n * sizeof(int));
+  return p;
+}
+static double *dupd_or(const double *src, size_t n, double fill) {
+  double *p = xcalloc(n, sizeof(double));
+  for (size_t k = 0; k < n; k++) p[k] = src ? src[k] : fill;
+  return p;
+}
+
+/* ------------------------------------------------------------------ */
+/* MAT_ELAST_init_a for flat elements: Jacobian from the four corner
+ * nodes (Q4, elem_q4.f90), inverse Jacobian by invert2 (utils.f90:92-114),
+ * weights = det(J)*wgll(i)*wgll(j) (spec_grid.f90:590-602)             */
+static void init_acoef(oc_sim *s, const sem2d_problem_desc *dd) {
+  int n = s->ngll, ne = s->nelem, na = s->nelast;
+  double *xg = xcalloc((size_t)n, sizeof(double)), *wg = xcalloc((size_t)n, sizeof(double));
+  double *Hd = xcalloc((size_t)n * n, sizeof(double));
+  oc_gll_info(n, xg, wg, Hd);
+  free(Hd);
+  s->acoef = xcalloc((size_t)n * n * na * ne, sizeof(double));
+  for (int e = 0; e < ne; e++) {
+    int cidx[4][2] = {{0, 0}, {n - 1, 0}, {n - 1, n - 1}, {0, n - 1}};
+    double c[8];
+    for (int k = 0; k < 4; k++) {
+      int p = dd->ibool[cidx[k][0] + n * (cidx[k][1] + n * e)] - 1;
+      c[2 * k] = dd->coord[2 * p];
+      c[2 * k + 1] = dd->coord[2 * p + 1];
+    }
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        double s_ = xg[i], t = xg[j];
+        double sp = s_ + 1.0, sm = s_ - 1.0, tp = t + 1.0, tm = t - 1.0;
+        double ds[8] = {0.25 * tm, -(0.25 * tm), 0.25 * tp, -(0.25 * tp),
+                        0.25 * sm, -(0.25 * sp), 0.25 * sp, -(0.25 * sm)};
+        double jac[4];
+        for (int b = 0; b < 2; b++)
+          for (int a = 0; a < 2; a++) {
+            double acc = c[a] * ds[4 * b];
+            for (int k = 1; k < 4; k++) acc = acc + c[a + 2 * k] * ds[k + 4 * b];
+            jac[a + 2 * b] = acc;
+          }
+        double det = jac[0] * jac[3] - jac[2] * jac[1];
+        double DxiDx = jac[3] / det, DetaDz = jac[0] / det;
+        double w = det * (wg[i] * wg[j]);
+        size_t p = i + (size_t)n * j + (size_t)n * n * e;
+        double *A = s->acoef + (size_t)n * n * na * e + i + n * j;
+        size_t st = (size_t)n * n;
+        double Kx = dd->Kx[p], Kz = dd->Kz[p], la = dd->la[p], mu = dd->mu[p], mux = dd->mux[p];
+        if (na == 2) {
+          A[0] = -(w * ((mux * DxiDx) * DxiDx));
+          A[st] = -(w * ((mu * DetaDz) * DetaDz));
+        } else {
+          A[0] = -(w * ((Kx * DxiDx) * DxiDx));
+          A[st] = -(w * ((la * DxiDx) * DetaDz));
+          A[2 * st] = -(w * ((Kz * DetaDz) * DetaDz));
+          A[3 * st] = -(w * ((mu * DetaDz) * DetaDz));
+          A[4 * st] = -(w * ((mu * DxiDx) * DetaDz));
+          A[5 * st] = -(w * ((mu * DxiDx) * DxiDx));
+        }
+      }
+  }
+  free(xg);
+  free(wg);
+}
+
+/* C = A*B for n x n column-major matrices, c(i,j) = sum_k a(i,k)b(k,j) in
+ * increasing k (mxmlib.f90:12-31, My_MATMUL mat_elastic.f90:779-799) */
+static void mxm(const double *A, const double *B, double *C, int n) {
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) {
+      double acc = A[i] * B[n * j];
+      for (int k = 1; k < n; k++) acc = acc + A[i + n * k] * B[k + n * j];
+      C[i + n * j] = acc;
+    }
+}
+
+static void elem_forces(const oc_sim *s, int e, const double *dl, double *fl) {
+  int n = s->ngll, n2 = n * n;
+  const double *H = s->H;
+  double Ht[400], t1[400], t2[400], t3[400], t4[400], tmp[400], tmp2[400];
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) Ht[i + n * j] = H[j + n * i];
+  const double *A = s->acoef + (size_t)n2 * s->nelast * e;
+  if (s->ndof == 1) {
+    mxm(Ht, dl, t1, n); /* dU_dxi  */
+    mxm(dl, H, t2, n);  /* dU_deta */
+    for (int q = 0; q < n2; q++) tmp[q] = A[q] * t1[q];
+    mxm(H, tmp, fl, n);
+    for (int q = 0; q < n2; q++) tmp[q] = A[n2 + q] * t2[q];
+    mxm(tmp, Ht, tmp2, n);
+    for (int q = 0; q < n2; q++) fl[q] = fl[q] + tmp2[q];
+    return;
+  }
+  const double *ux = dl, *uz = dl + n2;
+  double *fx = fl, *fz = fl + n2;
+  mxm(Ht, ux, t1, n); /* dUx_dxi  */
+  mxm(Ht, uz, t2, n); /* dUz_dxi  */
+  mxm(ux, H, t3, n);  /* dUx_deta */
+  mxm(uz, H, t4, n);  /* dUz_deta */
+  const double *a1 = A, *a2 = A + n2, *a3 = A + 2 * n2, *a4 = A + 3 * n2, *a5 = A + 4 * n2,
+               *a6 = A + 5 * n2;
+  for (int q = 0; q < n2; q++) tmp[q] = a1[q] * t1[q] + a2[q] * t4[q];
+  mxm(H, tmp, fx, n);
+  if (s->kd2)
+    for (int q = 0; q < n2; q++) tmp[q] = a4[q] * (t3[q] + t2[q]);
+  else
+    for (int q = 0; q < n2; q++) tmp[q] = a4[q] * t3[q] + a5[q] * t2[q];
+  mxm(tmp, Ht, tmp2, n);
+  for (int q = 0; q < n2; q++) fx[q] = fx[q] + tmp2[q];
+  for (int q = 0; q < n2; q++) tmp[q] = a5[q] * t3[q] + a6[q] * t2[q];
+  mxm(H, tmp, fz, n);
+  for (int q = 0; q < n2; q++) tmp[q] = a2[q] * t1[q] + a3[q] * t4[q];
+  mxm(tmp, Ht, tmp2, n);
+  for (int q = 0; q < n2; q++) fz[q] = fz[q] + tmp2[q];
+}
+
+/* compute_Fint (solver.f90:273-316) */
+static void compute_fint(oc_sim *s, double *f, const double *d, const double *v) {
+  int n = s->ngll, n2 = n * n, nd = s->ndof, np = s->npoin;
+  double dl[800], fl[800];
+  memset(f, 0, (size_t)np * nd * sizeof(double));
+  for (int e = 0; e < s->nelem; e++) {
+    const int *ib = s->ibool + (size_t)n2 * e;
+    for (int k = 0; k < nd; k++)
+      for (int q = 0; q < n2; q++) dl[q + n2 * k] = d[(ib[q] - 1) + (size_t)np * k];
+    if (s->kveta) {
+      const double *eta = s->kveta + (size_t)n2 * e;
+      for (int k = 0; k < nd; k++)
+        for (int q = 0; q < n2; q++)
+          dl[q + n2 * k] = dl[q + n2 * k] + eta[q] * v[(ib[q] - 1) + (size_t)np * k];
+    }
+    elem_forces(s, e, dl, fl);
+    for (int q = 0; q < n2; q++)
+      for (int k = 0; k < nd; k++) {
+        size_t g = (ib[q] - 1) + (size_t)np * k;
+        f[g] = f[g] + fl[q + n2 * k];
+      }
+  }
+}
+
+static double ricker(double t, double f0, double t0, double ampli) {
+  double arg = PI_REF * f0 * (t - t0);
+  arg = arg * arg;
+  return -((ampli * (1.0 - 2.0 * arg)) * exp(-arg));
+}
+
+static void so_add(oc_sim *s, double t, double *f) {
+  for (int k = 0; k < s->nsrc; k++) {
+    double ampli = ricker(t - s->src_tdelay[k], s->src_f0[k], s->src_t0[k], s->src_amp[k]);
+    ampli = ampli * s->src_rel[k];
+    size_t g = s->src_node[k] - 1;
+    if (s->ndof == 1) {
+      f[g] = f[g] + ampli;
+    } else {
+      f[g] = f[g] + s->src_dir[2 * k] * ampli;
+      f[g + s->npoin] = f[g + s->npoin] + s->src_dir[2 * k + 1] * ampli;
+    }
+  }
+}
+
+static void abso_apply(oc_sim *s, double *f, const double *v) {
+  for (int k = 0; k < s->nabs; k++) {
+    size_t g = s->abs_node[k] - 1;
+    for (int d = 0; d < s->ndof; d++) {
+      size_t gg = g + (size_t)s->npoin * d;
+      f[gg] = f[gg] - s->abs_C[k + (size_t)s->nabs * d] * v[gg];
+    }
+  }
+}
+
+/* ---------------- friction laws ---------------- */
+static double swf_mu(const oc_sim *s, int k) {
+  double th = s->theta[k], mu;
+  if (s->swf_kind == 1) {
+    double r = th / s->swf_dc[k];
+    mu = s->swf_mus[k] - (s->swf_mus[k] - s->swf_mud[k]) * (r < 1.0 ? r : 1.0);
+  } else if (s->swf_kind == 2) {
+    mu = s->swf_mud[k] - (s->swf_mud[k] - s->swf_mus[k]) * exp(-th / s->swf_dc[k]);
+  } else {
+    mu = s->swf_mud[k] + (s->swf_mus[k] - s->swf_mud[k]) / pow(1.0 + th / s->swf_dc[k], s->swf_p[k]);
+  }
+  return mu + s->swf_alpha[k] * th;
+}
+
+static double rsf_mu(const oc_sim *s, int k, double v) {
+  double av = fabs(v), a = s->rsf_a[k], b = s->rsf_b[k], th = s->theta[k];
+  switch (s->rsf_kind) {
+    case 1:
+      return s->rsf_mus[k] + a * av / (av + s->rsf_vstar[k]) - b * th / (th + s->rsf_dc[k]);
+    case 4:
+      return a * asinh(av / (2.0 * s->rsf_vstar[k]) *
+                       exp((s->rsf_mus[k] + b * log(s->rsf_vc[k] * th / s->rsf_dc[k] + 1.0)) / a));
+    default:
+      return a * asinh(av / (2.0 * s->rsf_vstar[k]) *
+                       exp((s->rsf_mus[k] + b * log(s->rsf_vstar[k] * th / s->rsf_dc[k])) / a));
+  }
+}
+
+static double rsf_update_theta(const oc_sim *s, int k, double theta, double v) {
+  double th;
+  switch (s->rsf_kind) {
+    case 1:
+      th = theta * s->rsf_coeft[k] + s->rsf_Tc[k] * fabs(v) * (1.0 - s->rsf_coeft[k]);
+      if (th < 1.0e-12) th = 0.0;
+      return th;
+    case 3:
+      th = s->rsf_dc[k] / fabs(v);
+      return th * pow(theta / th, exp(-s->dt / th));
+    default: {
+      double x = fabs(v) / s->rsf_dc[k];
+      double ex = exp(-(s->dt * x));
+      if (s->dt * x > 1.0e-8) return theta * ex + (1.0 - ex) / x;
+      return theta * ex + s->dt * (1.0 - 0.5 * s->dt * x);
+    }
+  }
+}
+
+/* nr_fric_func_tau (bc_dynflt_rsf.f90:533-568) */
+static void nr_func(const oc_sim *s, int k, double theta, double tau, double tau_stick,
+                    double sigma, double Z, double *fn, double *dfn, double *v) {
+  double tmp;
+  if (s->rsf_kind == 4)
+    tmp = s->rsf_mus[k] + s->rsf_b[k] * log(s->rsf_vc[k] * theta / s->rsf_dc[k] + 1.0);
+  else
+    tmp = s->rsf_mus[k] + s->rsf_b[k] * log(s->rsf_vstar[k] * theta / s->rsf_dc[k]);
+  tmp = 2.0 * s->rsf_vstar[k] * exp(-tmp / s->rsf_a[k]);
+  double sa = -sigma * s->rsf_a[k];
+  *v = sinh(tau / sa) * tmp;
+  *fn = tau_stick - Z * (*v) - tau;
+  double dv = cosh(tau / sa) * tmp / sa;
+  *dfn = -Z * dv - 1.0;
+}
+
+/* nr_solver (bc_dynflt_rsf.f90:369-468): bracketed Newton-Raphson with
+ * bisection.  The value returned is the slip rate of the last function
+ * evaluation, exactly as in the reference. */
+static double nr_solver(oc_sim *s, int k, double xL, double xR, double xacc, double theta,
+                        double tau_stick, double sigma, double Z) {
+  double flo, fhi, dfn, v, xl = xL, xr = xR;
+  nr_func(s, k, theta, xL, tau_stick, sigma, Z, &flo, &dfn, &v);
+  nr_func(s, k, theta, xR, tau_stick, sigma, Z, &fhi, &dfn, &v);
+  int guard = 0;
+  while (flo * fhi > 0) {
+    if (++guard > NR_MAXBRACKET) {
+      s->status = SEM2D_E_NR;
+      return v;
+    }
+    xl = xl / 2.0;
+    xr = xr * 2.0;
+    nr_func(s, k, theta, xl, tau_stick, sigma, Z, &flo, &dfn, &v);
+    nr_func(s, k, theta, xr, tau_stick, sigma, Z, &fhi, &dfn, &v);
+  }
+  double xlow, xhigh;
+  if (flo == 0) return v;
+  if (fhi == 0) return v;
+  if (flo < 0) {
+    xlow = xl;
+    xhigh = xr;
+  } else {
+    xhigh = xl;
+    xlow = xr;
+  }
+  double xest = 0.5 * (xl + xr), dxold = fabs(xr - xl), dx = dxold, fx;
+  nr_func(s, k, theta, xest, tau_stick, sigma, Z, &fx, &dfn, &v);
+  for (int is = 1; is <= NR_MAXIT; is++) {
+    if (((xest - xhigh) * dfn - fx) * ((xest - xlow) * dfn - fx) > 0 ||
+        fabs(2 * fx) > fabs(dxold * dfn)) {
+      dxold = dx;
+      dx = 0.5 * (xhigh - xlow);
+      xest = xlow + dx;
+      if (xlow == xest) return v;
+    } else {
+      dxold = dx;
+      dx = fx / dfn;
+      double temp = xest;
+      xest = xest - dx;
+      if (temp == xest) return v;
+    }
+    if (fabs(dx) < fabs(xacc)) {
+      nr_func(s, k, theta, xest, tau_stick, sigma, Z, &fx, &dfn, &v);
+      return v;
+    }
+    nr_func(s, k, theta, xest, tau_stick, sigma, Z, &fx, &dfn, &v);
+    if (fx < 0)
+      xlow = xest;
+    else
+      xhigh = xest;
+  }
+  s->status = SEM2D_E_NR;
+  return v;
+}
+
+static double rsf_update_V(oc_sim *s, int k, double tau_stick, double sigma, double theta,
+                           double Z) {
+  if (s->rsf_kind == 1) {
+    /* rsf_mu_no_direct uses the stored (old) state variable */
+    double mnd = s->rsf_mus[k] - s->rsf_b[k] * s->theta[k] / (s->theta[k] + s->rsf_dc[k]);
+    double v = (tau_stick + sigma * mnd) / Z;
+    double tmp = v - s->rsf_vstar[k] + sigma * s->rsf_a[k] / Z;
+    v = 0.5 * (tmp + sqrt(tmp * tmp + 4.0 * v * s->rsf_vstar[k]));
+    v = v > 0.0 ? v : 0.0;
+    if (v < 1.0e-12) v = 0.0;
+    return v;
+  }
+  double tol = -0.001 * s->rsf_a[k] * sigma;
+  double lo = tau_stick < 0.0 ? tau_stick : 0.0, hi = tau_stick > 0.0 ? tau_stick : 0.0;
+  return nr_solver(s, k, lo, hi, tol, theta, tau_stick, sigma, Z);
+}
+
+/* BC_DYNFLT_apply (bc_dynflt.f90:569-689) */
+static void dynflt_apply(oc_sim *s, double *f, const double *v, const double *d) {
+  int nf = s->nflt, nd = s->ndof, np = s->npoin;
+  for (int k = 0; k < nf; k++) {
+    size_t g1 = s->node1[k] - 1, g2 = s->two ? (size_t)(s->node2[k] - 1) : 0;
+    double dD[2] = {0, 0}, dV[2] = {0, 0}, dA[2] = {0, 0}, T[2] = {0, 0}, Ts[2] = {0, 0};
+    for (int c = 0; c < nd; c++) {
+      size_t o = (size_t)np * c;
+      if (s->two) {
+        dD[c] = d[g2 + o] - d[g1 + o];
+        dV[c] = v[g2 + o] - v[g1 + o];
+        dA[c] = s->invM2[k + nf * c] * f[g2 + o] - s->invM1[k + nf * c] * f[g1 + o];
+      } else {
+        dD[c] = -2.0 * d[g1 + o];
+        dV[c] = -2.0 * v[g1 + o];
+        dA[c] = -2.0 * s->invM1[k + nf * c] * f[g1 + o];
+      }
+      T[c] = s->Z[k + nf * c] * (dV[c] + s->coefA2V * dA[c]);
+    }
+    double nx = s->n1[k], nz = s->n1[k + nf];
+    if (nd == 2) {
+      double r0, r1;
+      r0 = nz * dD[0] - nx * dD[1]; r1 = nx * dD[0] + nz * dD[1]; dD[0] = r0; dD[1] = r1;
+      r0 = nz * dV[0] - nx * dV[1]; r1 = nx * dV[0] + nz * dV[1]; dV[0] = r0; dV[1] = r1;
+      r0 = nz * dA[0] - nx * dA[1]; r1 = nx * dA[0] + nz * dA[1]; dA[0] = r0; dA[1] = r1;
+      r0 = nz * T[0] - nx * T[1]; r1 = nx * T[0] + nz * T[1]; T[0] = r0; T[1] = r1;
+    }
+    if (!s->two || nd == 1) T[1] = 0.0;
+    T[0] = T[0] + s->T0[k];
+    T[1] = T[1] + s->T0[k + nf];
+    if (s->opening) T[1] = T[1] < 0.0 ? T[1] : 0.0;
+    /* normal_update */
+    switch (s->normal_kind) {
+      case 1: s->sigma[k] = T[1]; break;
+      case 2: s->sigma[k] = T[1] + s->ncoef * (s->sigma[k] - T[1]); break;
+      case 3: s->sigma[k] = T[1] + exp(-(fabs(dV[0]) + s->nV) * s->ncoef) * (s->sigma[k] - T[1]); break;
+      default: break;
+    }
+    double sig = s->sigma[k];
+    if (s->friction == SEM2D_FRICTION_RSF) {
+      double vold = s->V[k];
+      double th1 = rsf_update_theta(s, k, s->theta[k], vold);
+      double vnew = rsf_update_V(s, k, T[0], sig, th1, s->Z[k]);
+      double th2 = rsf_update_theta(s, k, s->theta[k], 0.5 * (vold + vnew));
+      vnew = rsf_update_V(s, k, T[0], sig, th2, s->Z[k]);
+      s->theta[k] = th2;
+      s->V[k] = vnew;
+      s->MU[k] = rsf_mu(s, k, s->V[k]);
+      double strength = -s->MU[k] * sig;
+      T[0] = copysign(fabs(strength), T[0]);
+      /* T_stick is not defined on this branch of the reference
+       * (bc_dynflt.f90:581); record zero before the T0 shift */
+      Ts[0] = 0.0;
+      Ts[1] = 0.0;
+    } else {
+      if (s->coefA2D == 0.0) {
+        if (s->swf_healing) {
+          s->theta[k] = s->theta[k] + fabs(dV[0]) * s->dt;
+          if (fabs(dV[0]) < V_HEALING) s->theta[k] = 0.0;
+        } else {
+          s->theta[k] = fabs(dD[0]);
+        }
+      } else {
+        s->theta[k] = fabs(s->D[k]);
+      }
+      s->MU[k] = swf_mu(s, k);
+      double strength = s->coh[k] - s->MU[k] * sig;
+      Ts[0] = T[0];
+      Ts[1] = T[1];
+      double at = fabs(T[0]);
+      T[0] = copysign(fabs(at < strength ? at : strength), T[0]);
+    }
+    T[0] = T[0] - s->T0[k];
+    T[1] = T[1] - s->T0[k + nf];
+    Ts[0] = Ts[0] - s->T0[k];
+    Ts[1] = Ts[1] - s->T0[k + nf];
+    s->T[k] = T[0];
+    s->T[k + nf] = T[1];
+    s->Tstick[k] = Ts[0];
+    s->Tstick[k + nf] = Ts[1];
+    double Tx[2] = {T[0], T[1]};
+    if (nd == 2) {
+      Tx[0] = nz * T[0] + nx * T[1];
+      Tx[1] = -nx * T[0] + nz * T[1];
+    }
+    for (int c = 0; c < nd; c++) {
+      size_t o = (size_t)np * c;
+      f[g1 + o] = f[g1 + o] + s->B[k] * Tx[c];
+      if (s->two) f[g2 + o] = f[g2 + o] - s->B[k] * Tx[c];
+    }
+    for (int c = 0; c < nd; c++) {
+      double dAc = dA[c] - s->T[k + nf * c] / (s->Z[k + nf * c] * s->coefA2V);
+      s->D[k + nf * c] = dD[c] + s->coefA2D * dAc;
+      s->V[k + nf * c] = dV[c] + s->coefA2V * dAc;
+    }
+  }
+}
+
+static void rec_store(oc_sim *s) {
+  if (s->nrec == 0 || s->it % s->rec_isamp != 0) return;
+  int isamp = s->it / s->rec_isamp;
+  if (isamp >= s->rec_nsamp) return;
+  const double *fld = s->rec_field == 'D' ? s->d : (s->rec_field == 'A' ? s->a : s->v);
+  int n2 = s->ngll * s->ngll, np = s->npoin;
+  for (int r = 0; r < s->nrec; r++)
+    for (int c = 0; c < s->ndof; c++) {
+      double val;
+      if (s->rec_node) {
+        val = fld[(s->rec_node[r] - 1) + (size_t)np * c];
+      } else {
+        const int *ib = s->ibool + (size_t)n2 * (s->rec_elem[r] - 1);
+        const double *w = s->rec_interp + (size_t)n2 * r;
+        val = w[0] * fld[(ib[0] - 1) + (size_t)np * c];
+        for (int q = 1; q < n2; q++) val = val + w[q] * fld[(ib[q] - 1) + (size_t)np * c];
+      }
+      s->sis[isamp + (size_t)s->rec_nsamp * (r + (size_t)s->nrec * c)] = val;
+    }
+}
+
+static void flt_write(oc_sim *s) {
+  if (s->nflt == 0 || s->it < s->oit) return;
+  if (s->fsamp < s->fnsamp) {
+    int nf = s->nflt, q = 0;
+    double *o = s->fseries + (size_t)s->onx * 6 * s->fsamp;
+    for (int k = s->oix1 - 1; k <= s->oixn - 1; k += s->oixd, q++) {
+      o[q] = s->D[k];
+      o[q + s->onx] = s->V[k];
+      o[q + 2 * s->onx] = s->T[k];
+      o[q + 3 * s->onx] = s->T[k + nf];
+      o[q + 4 * s->onx] = s->MU[k];
+      o[q + 5 * s->onx] = s->Tstick[k];
+    }
+  }
+  s->fsamp++;
+  s->oit += s->oitd;
+}
+
+oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
+  if (!dd || dd->ngll < 2 || dd->ngll > 20 || (dd->ndof != 1 && dd->ndof != 2) || dd->nelem <= 0 ||
+      dd->npoin <= 0) {
+    if (err) snprintf(err, (size_t)el, "oc_sim_create: bad descriptor");
+    return NULL;
+  }
+  oc_sim *s = xcalloc(1, sizeof(oc_sim));
+  int n = dd->ngll, n2 = n * n, nd = dd->ndof, np = dd->npoin, ne = dd->nelem;
+  s->ngll = n;
+  s->ndof = nd;
+  s->nelem = ne;
+  s->npoin = np;
+  s->nelast = nd == 1 ? 2 : 6;
+  s->kd2 = dd->kd2_form;
+  s->ibool = dupi(dd->ibool, (size_t)n2 * ne);
+  s->H = dupd(dd->hprime, (size_t)n2);
+  init_acoef(s, dd);
+  s->kveta = dupd(dd->kv_eta, (size_t)n2 * ne);
+  s->rmass = dupd(dd->rmass, (size_t)np * nd);
+  s->nabs = dd->nabs;
+  s->abs_node = dupi(dd->abs_node, (size_t)dd->nabs);
+  s->abs_C = dupd(dd->abs_C, (size_t)dd->nabs * nd);
+  s->scheme = dd->time_scheme;
+  s->dt = dd->dt;
+  s->beta = dd->beta;
+  s->gamma = dd->gamma;
+  s->nt = dd->nt;
+  s->nsrc = dd->nsrc;
+  s->src_node = dupi(dd->src_node, (size_t)dd->nsrc);
+  s->src_dir = dupd(dd->src_dir, 2 * (size_t)dd->nsrc);
+  s->src_f0 = dupd(dd->src_f0, (size_t)dd->nsrc);
+  s->src_t0 = dupd(dd->src_t0, (size_t)dd->nsrc);
+  s->src_amp = dupd(dd->src_ampli, (size_t)dd->nsrc);
+  s->src_rel = dupd_or(dd->src_relamp, (size_t)dd->nsrc, 1.0);
+  s->src_tdelay = dupd_or(dd->src_tdelay, (size_t)dd->nsrc, 0.0);
+  s->nrec = dd->nrec;
+  s->rec_isamp = dd->rec_isamp > 0 ? dd->rec_isamp : 1;
+  s->rec_nsamp = dd->rec_nsamp;
+  s->rec_field = dd->rec_field;
+  s->rec_node = dupi(dd->rec_node, (size_t)dd->nrec);
+  s->rec_elem = dd->rec_node ? NULL : dupi(dd->rec_elem, (size_t)dd->nrec);
+  s->rec_interp = dd->rec_node ? NULL : dupd(dd->rec_interp, (size_t)n2 * dd->nrec);
+  s->sis = xcalloc((size_t)dd->rec_nsamp * dd->nrec * nd + 1, sizeof(double));
+  s->d = xcalloc((size_t)np * nd, sizeof(double));
+  s->v = xcalloc((size_t)np * nd, sizeof(double));
+  s->a = xcalloc((size_t)np * nd, sizeof(double));
+  int nf = dd->nflt;
+  s->nflt = nf;
+  if (nf > 0) {
+    s->two = dd->flt_node2 != NULL;
+    s->friction = dd->flt_friction;
+    s->swf_kind = dd->swf_kind;
+    s->swf_healing = dd->swf_healing;
+    s->rsf_kind = dd->rsf_kind;
+    s->normal_kind = dd->normal_kind;
+    s->opening = dd->flt_opening;
+    s->node1 = dupi(dd->flt_node1, (size_t)nf);
+    s->node2 = dupi(dd->flt_node2, (size_t)nf);
+    s->n1 = dupd(dd->flt_n1, 2 * (size_t)nf);
+    s->B = dupd(dd->flt_B, (size_t)nf);
+    s->invM1 = dupd(dd->flt_invM1, (size_t)nf * nd);
+    s->invM2 = dupd(dd->flt_invM2, (size_t)nf * nd);
+    s->Z = dupd(dd->flt_Z, (size_t)nf * nd);
+    s->T0 = dupd(dd->flt_T0, 2 * (size_t)nf);
+    s->coh = dupd_or(dd->flt_cohesion, (size_t)nf, 0.0);
+    s->coefA2V = dd->flt_coefA2V;
+    s->coefA2D = dd->flt_coefA2D;
+    s->nT = dd->normal_T;
+    s->nL = dd->normal_L;
+    s->nV = dd->normal_V;
+    if (s->normal_kind == 2) s->ncoef = exp(-s->dt / s->nT);
+    if (s->normal_kind == 3) s->ncoef = s->dt / s->nL;
+    s->D = xcalloc((size_t)nf * nd, sizeof(double));
+    s->V = xcalloc((size_t)nf * nd, sizeof(double));
+    s->T = xcalloc(2 * (size_t)nf, sizeof(double));
+    s->Tstick = xcalloc(2 * (size_t)nf, sizeof(double));
+    s->MU = xcalloc((size_t)nf, sizeof(double));
+    s->sigma = xcalloc((size_t)nf, sizeof(double));
+    s->theta = xcalloc((size_t)nf, sizeof(double));
+    for (int k = 0; k < nf; k++) s->sigma[k] = s->T0[k + nf];
+    if (s->friction == SEM2D_FRICTION_SWF) {
+      s->swf_dc = dupd(dd->swf_dc, nf);
+      s->swf_mus = dupd(dd->swf_mus, nf);
+      s->swf_mud = dupd(dd->swf_mud, nf);
+      s->swf_p = dupd_or(dd->swf_p, nf, 3.0);
+      s->swf_alpha = dupd_or(dd->swf_alpha, nf, 0.0);
+      for (int k = 0; k < nf; k++) s->MU[k] = swf_mu(s, k);
+    } else {
+      s->rsf_dc = dupd(dd->rsf_dc, nf);
+      s->rsf_mus = dupd(dd->rsf_mus, nf);
+      s->rsf_a = dupd(dd->rsf_a, nf);
+      s->rsf_b = dupd(dd->rsf_b, nf);
+      s->rsf_vstar = dupd(dd->rsf_vstar, nf);
+      s->rsf_vc = dupd_or(dd->rsf_vc, nf, 1e-6);
+      s->rsf_Tc = xcalloc((size_t)nf, sizeof(double));
+      s->rsf_coeft = xcalloc((size_t)nf, sizeof(double));
+      for (int k = 0; k < nf; k++) {
+        s->theta[k] = dd->rsf_theta ? dd->rsf_theta[k] : 0.0;
+        s->rsf_Tc[k] = s->rsf_dc[k] / s->rsf_vstar[k];
+        s->rsf_coeft[k] = exp(-s->dt / s->rsf_Tc[k]);
+        s->V[k] = dd->flt_V0 ? dd->flt_V0[k] : 1e-12;
+        s->MU[k] = rsf_mu(s, k, s->V[k]);
+      }
+    }
+    s->oit = dd->flt_oit;
+    s->oitd = dd->flt_oitd > 0 ? dd->flt_oitd : 1;
+    s->oix1 = dd->flt_oix1 > 0 ? dd->flt_oix1 : 1;
+    s->oixn = dd->flt_oixn > 0 ? dd->flt_oixn : nf;
+    s->oixd = dd->flt_oixd > 0 ? dd->flt_oixd : 1;
+    s->fnsamp = dd->flt_nsamp;
+    s->onx = (s->oixn - s->oix1) / s->oixd + 1;
+    s->fseries = xcalloc((size_t)s->onx * 6 * (s->fnsamp > 0 ? s->fnsamp : 1), sizeof(double));
+  }
+  /* step-0 outputs: REC_store(rec,0) (main.f90:35), BC_write(bc,0) (bc_gen.f90:247) */
+  s->it = 0;
+  flt_write(s);
+  rec_store(s);
+  return s;
+}
+
+int oc_sim_run(oc_sim *s, int nsteps) {
+  int nd = s->ndof;
+  size_t nn = (size_t)s->npoin * nd;
+  double *d = s->d, *v = s->v, *a = s->a;
+  for (int st = 0; st < nsteps; st++) {
+    s->it++;
+    double t = s->it * s->dt;
+    if (s->scheme == SEM2D_TIME_NEWMARK) {
+      double cd = (0.5 - s->beta) * s->dt * s->dt, cv = (1.0 - s->gamma) * s->dt;
+      for (size_t q = 0; q < nn; q++) {
+        d[q] = d[q] + s->dt * v[q] + cd * a[q];
+        v[q] = v[q] + cv * a[q];
+      }
+    } else {
+      for (size_t q = 0; q < nn; q++) d[q] = d[q] + s->dt * v[q];
+    }
+    compute_fint(s, a, d, v); /* f aliases accel */
+    so_add(s, t, a);
+    abso_apply(s, a, v);
+    if (s->nflt) dynflt_apply(s, a, v, d);
+    for (size_t q = 0; q < nn; q++) a[q] = s->rmass[q] * a[q];
+    if (s->scheme == SEM2D_TIME_NEWMARK) {
+      double cv = s->gamma * s->dt, cd = s->beta * s->dt * s->dt;
+      for (size_t q = 0; q < nn; q++) {
+        v[q] = v[q] + cv * a[q];
+        d[q] = d[q] + cd * a[q];
+      }
+    } else {
+      for (size_t q = 0; q < nn; q++) v[q] = v[q] + s->dt * a[q];
+    }
+    rec_store(s);
+    flt_write(s);
+    if (s->status) return s->status;
+  }
+  return s->status;
+}
+
+int oc_sim_step_count(const oc_sim *s) { return s->it; }
+
+void oc_sim_fields(const oc_sim *s, double *d, double *v, double *a) {
+  size_t nn = (size_t)s->npoin * s->ndof * sizeof(double);
+  if (d) memcpy(d, s->d, nn);
+  if (v) memcpy(v, s->v, nn);
+  if (a) memcpy(a, s->a, nn);
+}
+
+void oc_sim_seismograms(const oc_sim *s, double *sis) {
+  memcpy(sis, s->sis, (size_t)s->rec_nsamp * s->nrec * s->ndof * sizeof(double));
+}
+
+void oc_sim_fault_series(const oc_sim *s, double *out) {
+  if (s->nflt) memcpy(out, s->fseries, (size_t)s->onx * 6 * s->fnsamp * sizeof(double));
+}
+
+void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T, double *MU,
+                        double *theta) {
+  int nf = s->nflt, nd = s->ndof;
+  if (!nf) return;
+  if (D) memcpy(D, s->D, (size_t)nf * nd * sizeof(double));
+  if (V) memcpy(V, s->V, (size_t)nf * nd * sizeof(double));
+  if (T) memcpy(T, s->T, 2 * (size_t)nf * sizeof(double));
+  if (MU) memcpy(MU, s->MU, (size_t)nf * sizeof(double));
+  if (theta) memcpy(theta, s->theta, (size_t)nf * sizeof(double));
+}
+
+void oc_sim_free(oc_sim *s) {
+  if (!s) return;
+  void *ptrs[] = {s->ibool, s->H, s->acoef, s->kveta, s->rmass, s->abs_node, s->abs_C,
+                  s->src_node, s->src_dir, s->src_f0, s->src_t0, s->src_amp, s->src_rel,
+                  s->src_tdelay, s->rec_node, s->rec_elem, s->rec_interp, s->sis, s->node1,
+                  s->node2, s->n1, s->B, s->invM1, s->invM2, s->Z, s->T0, s->coh, s->swf_dc,
+                  s->swf_mus, s->swf_mud, s->swf_p, s->swf_alpha, s->theta, s->rsf_dc,
+                  s->rsf_mus, s->rsf_a, s->rsf_b, s->rsf_vstar, s->rsf_vc, s->rsf_Tc,
+                  s->rsf_coeft, s->D, s->V, s->T, s->Tstick, s->MU, s->sigma, s->fseries,
+                  s->d, s->v, s->a};
+  for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
+  free(s);
+}

@@ -1,0 +1,335 @@
+// fault_kernel.cuh -- split-node dynamic fault, run after the bulk kernel
+// of each step with one thread per fault node pair, entirely in FP64.
+//
+// Restates BC_DYNFLT_apply (bc_dynflt.f90:569-739): traction that keeps
+// the fault stuck (T = Z (dV + coefA2V dA)), rotation to the fault frame,
+// opening, normal-stress law (bc_dynflt_normal.f90:118-133), friction
+// (slip weakening bc_dynflt_swf.f90:142-183; rate and state
+// bc_dynflt_rsf.f90:165-568 with the bracketed Newton solver), boundary
+// term B T added to both sides, slip and slip-rate update; then finishes
+// the time update of the two split nodes (which the bulk kernel skipped)
+// and records the fault time series (bc_dynflt.f90:751-778).
+//
+// Each thread keeps FP64 copies of displacement, velocity and
+// acceleration of its two nodes, so slip, slip rate and the state
+// variable are accumulated in FP64 whatever the precision of the bulk.
+#pragma once
+
+#include "sem2d_common.cuh"
+
+namespace sem2d {
+
+constexpr int kNrMaxIt = 200;       // bc_dynflt_rsf.f90:372
+constexpr int kNrMaxBracket = 200;  // bound for the loop at bc_dynflt_rsf.f90:393-398
+constexpr int kErrNR = -4;          // SEM2D_E_NR
+
+template <typename real>
+__device__ double swf_mu(const FaultParams<real> &p, int k, double th) {
+  double mu;
+  if (p.swf_kind == 1) {
+    const double r = th / p.swf_dc[k];
+    mu = p.swf_mus[k] - (p.swf_mus[k] - p.swf_mud[k]) * (r < 1.0 ? r : 1.0);
+  } else if (p.swf_kind == 2) {
+    mu = p.swf_mud[k] - (p.swf_mud[k] - p.swf_mus[k]) * exp(-th / p.swf_dc[k]);
+  } else {
+    mu = p.swf_mud[k] + (p.swf_mus[k] - p.swf_mud[k]) / pow(1.0 + th / p.swf_dc[k], p.swf_p[k]);
+  }
+  return mu + p.swf_alpha[k] * th;
+}
+
+template <typename real>
+__device__ double rsf_mu(const FaultParams<real> &p, int k, double v, double th) {
+  const double av = fabs(v), a = p.rsf_a[k], b = p.rsf_b[k];
+  if (p.rsf_kind == 1)
+    return p.rsf_mus[k] + a * av / (av + p.rsf_vstar[k]) - b * th / (th + p.rsf_dc[k]);
+  const double lg = p.rsf_kind == 4 ? log(p.rsf_vc[k] * th / p.rsf_dc[k] + 1.0)
+                                    : log(p.rsf_vstar[k] * th / p.rsf_dc[k]);
+  return a * asinh(av / (2.0 * p.rsf_vstar[k]) * exp((p.rsf_mus[k] + b * lg) / a));
+}
+
+template <typename real>
+__device__ double rsf_theta(const FaultParams<real> &p, int k, double th, double v) {
+  if (p.rsf_kind == 1) {
+    double r = th * p.rsf_coeft[k] + p.rsf_Tc[k] * fabs(v) * (1.0 - p.rsf_coeft[k]);
+    return r < 1.0e-12 ? 0.0 : r;
+  }
+  if (p.rsf_kind == 3) {
+    const double r = p.rsf_dc[k] / fabs(v);
+    return r * pow(th / r, exp(-p.dt / r));
+  }
+  const double x = fabs(v) / p.rsf_dc[k];
+  const double ex = exp(-(p.dt * x));
+  if (p.dt * x > 1.0e-8) return th * ex + (1.0 - ex) / x;
+  return th * ex + p.dt * (1.0 - 0.5 * p.dt * x);
+}
+
+template <typename real>
+__device__ void nr_func(const FaultParams<real> &p, int k, double th, double tau, double ts,
+                        double sig, double Z, double &fn, double &dfn, double &v) {
+  double tmp = p.rsf_kind == 4
+                   ? p.rsf_mus[k] + p.rsf_b[k] * log(p.rsf_vc[k] * th / p.rsf_dc[k] + 1.0)
+                   : p.rsf_mus[k] + p.rsf_b[k] * log(p.rsf_vstar[k] * th / p.rsf_dc[k]);
+  tmp = 2.0 * p.rsf_vstar[k] * exp(-tmp / p.rsf_a[k]);
+  const double sa = -sig * p.rsf_a[k];
+  v = sinh(tau / sa) * tmp;
+  fn = ts - Z * v - tau;
+  dfn = -Z * (cosh(tau / sa) * tmp / sa) - 1.0;
+}
+
+// bracketed Newton-Raphson with bisection (bc_dynflt_rsf.f90:369-468);
+// returns the slip rate of its last function evaluation, as the reference
+template <typename real>
+__device__ double nr_solve(const FaultParams<real> &p, int k, double xL, double xR, double xacc,
+                           double th, double ts, double sig, double Z, bool &fail) {
+  double flo, fhi, dfn, v, xl = xL, xr = xR;
+  nr_func(p, k, th, xL, ts, sig, Z, flo, dfn, v);
+  nr_func(p, k, th, xR, ts, sig, Z, fhi, dfn, v);
+  int guard = 0;
+  while (flo * fhi > 0) {
+    if (++guard > kNrMaxBracket) {
+      fail = true;
+      return v;
+    }
+    xl = xl / 2.0;
+    xr = xr * 2.0;
+    nr_func(p, k, th, xl, ts, sig, Z, flo, dfn, v);
+    nr_func(p, k, th, xr, ts, sig, Z, fhi, dfn, v);
+  }
+  if (flo == 0 || fhi == 0) return v;
+  double xlow = flo < 0 ? xl : xr, xhigh = flo < 0 ? xr : xl;
+  double xest = 0.5 * (xl + xr), dxold = fabs(xr - xl), dx = dxold, fx;
+  nr_func(p, k, th, xest, ts, sig, Z, fx, dfn, v);
+  for (int is = 0; is < kNrMaxIt; ++is) {
+    if (((xest - xhigh) * dfn - fx) * ((xest - xlow) * dfn - fx) > 0 ||
+        fabs(2 * fx) > fabs(dxold * dfn)) {
+      dxold = dx;
+      dx = 0.5 * (xhigh - xlow);
+      xest = xlow + dx;
+      if (xlow == xest) return v;
+    } else {
+      dxold = dx;
+      dx = fx / dfn;
+      const double tmp = xest;
+      xest = xest - dx;
+      if (tmp == xest) return v;
+    }
+    if (fabs(dx) < fabs(xacc)) {
+      nr_func(p, k, th, xest, ts, sig, Z, fx, dfn, v);
+      return v;
+    }
+    nr_func(p, k, th, xest, ts, sig, Z, fx, dfn, v);
+    if (fx < 0) xlow = xest;
+    else xhigh = xest;
+  }
+  fail = true;
+  return v;
+}
+
+template <typename real>
+__device__ double rsf_V(const FaultParams<real> &p, int k, double ts, double sig, double th,
+                        double th_old, double Z, bool &fail) {
+  if (p.rsf_kind == 1) {
+    // rsf_mu_no_direct uses the state stored before this step
+    const double mnd = p.rsf_mus[k] - p.rsf_b[k] * th_old / (th_old + p.rsf_dc[k]);
+    double v = (ts + sig * mnd) / Z;
+    const double tmp = v - p.rsf_vstar[k] + sig * p.rsf_a[k] / Z;
+    v = 0.5 * (tmp + sqrt(tmp * tmp + 4.0 * v * p.rsf_vstar[k]));
+    v = v > 0.0 ? v : 0.0;
+    return v < 1.0e-12 ? 0.0 : v;
+  }
+  const double tol = -0.001 * p.rsf_a[k] * sig;
+  const double lo = ts < 0.0 ? ts : 0.0, hi = ts > 0.0 ? ts : 0.0;
+  return nr_solve(p, k, lo, hi, tol, th, ts, sig, Z, fail);
+}
+
+template <typename real>
+__device__ void fault_record(const FaultParams<real> &p, int k, int it) {
+  if (it < p.oit || (it - p.oit) % p.oitd != 0) return;
+  const int s = (it - p.oit) / p.oitd;
+  const int k1 = k + 1;
+  if (s >= p.nsamp || k1 < p.oix1 || (k1 - p.oix1) % p.oixd != 0) return;
+  const int q = (k1 - p.oix1) / p.oixd;
+  if (q >= p.onx) return;
+  const int nf = p.nflt;
+  double *o = p.series + (size_t)p.onx * 6 * s;
+  o[q] = p.D[k];
+  o[q + p.onx] = p.V[k];
+  o[q + 2 * p.onx] = p.T[k];
+  o[q + 3 * p.onx] = p.T[k + nf];
+  o[q + 4 * p.onx] = p.MU[k];
+  o[q + 5 * p.onx] = p.Tstick[k];
+}
+
+// initial friction and the step-0 record (bc_dynflt.f90:401-415, 247)
+template <typename real>
+__global__ void fault_init_kernel(FaultParams<real> p) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= p.nflt) return;
+  p.sigma[k] = p.T0[k + p.nflt];
+  if (p.friction == 2) p.MU[k] = rsf_mu(p, k, p.V[k], p.theta[k]);
+  else p.MU[k] = swf_mu(p, k, p.theta[k]);
+  fault_record(p, k, 0);
+}
+
+template <typename real>
+__global__ void fault_step_kernel(FaultParams<real> p) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int it = *p.step + 1;
+  if (k < p.nflt) {
+    const int nd = p.ndof, nf = p.nflt;
+    double f1[2] = {0, 0}, f2[2] = {0, 0}, d1[2] = {0, 0}, d2[2] = {0, 0};
+    double v1[2] = {0, 0}, v2[2] = {0, 0}, dD[2] = {0, 0}, dV[2] = {0, 0}, dA[2] = {0, 0};
+    double T[2] = {0, 0}, Ts[2] = {0, 0};
+    for (int c = 0; c < nd; ++c) {
+      const int o1 = (0 * nd + c) * nf + k, o2 = (1 * nd + c) * nf + k;
+      f1[c] = double(p.f_flt[(0 * nd + c) * p.LX + k]);
+      d1[c] = p.d64[o1];
+      v1[c] = p.v64[o1];
+      if (p.scheme == 1) v1[c] = v1[c] + p.cpred * p.a64[o1];
+      if (p.two) {
+        f2[c] = double(p.f_flt[(1 * nd + c) * p.LX + k]);
+        d2[c] = p.d64[o2];
+        v2[c] = p.v64[o2];
+        if (p.scheme == 1) v2[c] = v2[c] + p.cpred * p.a64[o2];
+        dD[c] = d2[c] - d1[c];
+        dV[c] = v2[c] - v1[c];
+        dA[c] = p.invM2[k + nf * c] * f2[c] - p.invM1[k + nf * c] * f1[c];
+      } else {
+        dD[c] = -2.0 * d1[c];
+        dV[c] = -2.0 * v1[c];
+        dA[c] = -2.0 * p.invM1[k + nf * c] * f1[c];
+      }
+      T[c] = p.Z[k + nf * c] * (dV[c] + p.coefA2V * dA[c]);
+    }
+    const double nx = p.n1[k], nz = p.n1[k + nf];
+    if (nd == 2) {
+      double r0, r1;
+      r0 = nz * dD[0] - nx * dD[1]; r1 = nx * dD[0] + nz * dD[1]; dD[0] = r0; dD[1] = r1;
+      r0 = nz * dV[0] - nx * dV[1]; r1 = nx * dV[0] + nz * dV[1]; dV[0] = r0; dV[1] = r1;
+      r0 = nz * dA[0] - nx * dA[1]; r1 = nx * dA[0] + nz * dA[1]; dA[0] = r0; dA[1] = r1;
+      r0 = nz * T[0] - nx * T[1];   r1 = nx * T[0] + nz * T[1];   T[0] = r0;  T[1] = r1;
+    }
+    if (!p.two || nd == 1) T[1] = 0.0;
+    T[0] = T[0] + p.T0[k];
+    T[1] = T[1] + p.T0[k + nf];
+    if (p.opening) T[1] = T[1] < 0.0 ? T[1] : 0.0;
+    double sig = p.sigma[k];
+    if (p.normal_kind == 1) sig = T[1];
+    else if (p.normal_kind == 2) sig = T[1] + p.normal_coef * (sig - T[1]);
+    else if (p.normal_kind == 3)
+      sig = T[1] + exp(-(fabs(dV[0]) + p.normal_V) * p.normal_coef) * (sig - T[1]);
+    p.sigma[k] = sig;
+    double mu;
+    if (p.friction == 2) {
+      bool fail = false;
+      const double vold = p.V[k], th0 = p.theta[k];
+      const double th1 = rsf_theta(p, k, th0, vold);
+      double vnew = rsf_V(p, k, T[0], sig, th1, th0, p.Z[k], fail);
+      const double th2 = rsf_theta(p, k, th0, 0.5 * (vold + vnew));
+      vnew = rsf_V(p, k, T[0], sig, th2, th0, p.Z[k], fail);
+      if (fail) atomicExch(p.error, kErrNR);
+      p.theta[k] = th2;
+      mu = rsf_mu(p, k, vnew, th2);
+      T[0] = copysign(fabs(-mu * sig), T[0]);
+      // T_stick is undefined on this branch of the reference (bc_dynflt.f90:581)
+      Ts[0] = 0.0;
+      Ts[1] = 0.0;
+    } else {
+      double th = p.theta[k];
+      if (p.coefA2D == 0.0) {
+        if (p.swf_healing) {
+          th = th + fabs(dV[0]) * p.dt;
+          if (fabs(dV[0]) < 1.0e-14) th = 0.0;
+        } else {
+          th = fabs(dD[0]);
+        }
+      } else {
+        th = fabs(p.D[k]);
+      }
+      p.theta[k] = th;
+      mu = swf_mu(p, k, th);
+      const double strength = p.coh[k] - mu * sig;
+      Ts[0] = T[0];
+      Ts[1] = T[1];
+      const double at = fabs(T[0]);
+      T[0] = copysign(fabs(at < strength ? at : strength), T[0]);
+    }
+    p.MU[k] = mu;
+    T[0] = T[0] - p.T0[k];
+    T[1] = T[1] - p.T0[k + nf];
+    p.T[k] = T[0];
+    p.T[k + nf] = T[1];
+    p.Tstick[k] = Ts[0] - p.T0[k];
+    p.Tstick[k + nf] = Ts[1] - p.T0[k + nf];
+    double Tx[2] = {T[0], T[1]};
+    if (nd == 2) {
+      Tx[0] = nz * T[0] + nx * T[1];
+      Tx[1] = -nx * T[0] + nz * T[1];
+    }
+    for (int c = 0; c < nd; ++c) {
+      const double dAc = dA[c] - T[c] / (p.Z[k + nf * c] * p.coefA2V);
+      p.D[k + nf * c] = dD[c] + p.coefA2D * dAc;
+      p.V[k + nf * c] = dV[c] + p.coefA2V * dAc;
+    }
+    // finish the two split nodes: boundary term, inverse mass, time update
+    for (int side = 0; side < 1 + p.two; ++side) {
+      const int J = side == 0 ? p.jf1 : p.jf2;
+      for (int c = 0; c < nd; ++c) {
+        const int o = (side * nd + c) * nf + k;
+        const double f = side == 0 ? f1[c] + p.B[k] * Tx[c] : f2[c] - p.B[k] * Tx[c];
+        const double vp = side == 0 ? v1[c] : v2[c];
+        const double dc = side == 0 ? d1[c] : d2[c];
+        const double a = p.rm[o] * f;
+        const double vn = vp + p.cv * a;
+        const double dn = p.scheme == 1 ? (dc + p.dt * vn) + p.cd2 * a : dc + p.dt * vn;
+        p.d64[o] = dn;
+        p.v64[o] = vn;
+        p.a64[o] = a;
+        const long long g = c * p.plane + (long long)J * p.pitch + k;
+        p.Dnext[g] = real(dn);
+        p.Vnext[g] = real(vn);
+        if (p.Anext) p.Anext[g] = real(a);
+      }
+    }
+    fault_record(p, k, it);
+  }
+  // the last block to finish advances the step counter
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(p.done, 1u);
+    if (prev == gridDim.x - 1) {
+      *p.done = 0u;
+      __threadfence();
+      *p.step = it;
+    }
+  }
+}
+
+// step counter only (no fault)
+__global__ void advance_kernel(int *step) { *step = *step + 1; }
+
+// seismograms (REC_store, receivers.f90:309-344), after the step counter moved
+template <typename real>
+__global__ void receiver_kernel(RecParams<real> p) {
+  const int it = *p.step;
+  if (it % p.isamp != 0) return;
+  const int s = it / p.isamp;
+  if (s >= p.nsamp) return;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= p.nrec * p.ndof) return;
+  const int r = q % p.nrec, c = q / p.nrec;
+  const real *f = p.field + c * p.plane;
+  double val;
+  if (p.npts == 1) {
+    val = double(f[p.lat[r]]);
+  } else {
+    const int *L = p.lat + (size_t)r * p.npts;
+    const double *W = p.w + (size_t)r * p.npts;
+    val = W[0] * double(f[L[0]]);
+    for (int k = 1; k < p.npts; ++k) val = val + W[k] * double(f[L[k]]);
+  }
+  p.sis[s + (size_t)p.nsamp * (r + (size_t)p.nrec * c)] = val;
+}
+
+}  // namespace sem2d

@@ -1,0 +1,1349 @@
+// host_builder.cpp -- Par.inp-level problem builder for the Cartesian path.
+//
+// Implements include/sem2d_host.h.  The reference builds a generic FEM
+// database (vertex/edge connectivity lists, fem_grid.f90:103-205) and then
+// numbers GLL nodes element by element (spec_grid.f90:198-314).  Here the
+// mesh is known to be a structured lattice of GLL nodes, possibly with one
+// duplicated row at a fault (mesh_structured.f90:78-80), so numbering,
+// coordinates and boundary tables are produced directly on that lattice.
+// The results are bit-identical to the reference's:
+//   * elements are visited in reverse Cuthill-McKee order (rcm.f90), and a
+//     node gets its number the first time an element in that order reaches
+//     it: interior nodes, then the unnumbered edges D,R,U,L in
+//     counterclockwise order, then the unnumbered vertices;
+//   * a node shared by several elements takes the coordinate computed by
+//     the last of them (spec_grid.f90:321-374);
+//   * boundary node tables are the lattice lines, i.e. the order of the
+//     stable coordinate sort of BC_set_bulk_node (spec_grid.f90:780-800).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <new>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sem2d_host.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+struct BuildError : std::runtime_error {
+  explicit BuildError(const std::string &m) : std::runtime_error(m) {}
+};
+
+constexpr double kPi = 3.141592653589793;  // constants.f90:34
+constexpr double kTinyXabs = 1.0e-3;       // constants.f90:30
+
+// --------------------------------------------------------------------
+// Gauss-Lobatto-Legendre quadrature: Gauss-Jacobi interior points by
+// Newton iteration with deflation, weights from the Jacobi recurrences
+// (the algorithm of gll.f90:300-684), derivative matrix from the Legendre
+// recurrence (gll.f90:230-265).  Same recurrences and operation order.
+struct Jacobi {
+  double p, pd, pm1, pdm1, pm2, pdm2;
+};
+
+Jacobi jacobi_eval(int n, double a, double b, double x) {
+  Jacobi r{1.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  if (n == 0) return r;
+  const double apb = a + b;
+  double pl = r.p, pdl = r.pd, ps = 0.0, pds = 0.0;
+  r.p = (a - b + (apb + 2.0) * x) / 2.0;
+  r.pd = (apb + 2.0) / 2.0;
+  if (n == 1) return r;
+  for (int k = 2; k <= n; ++k) {
+    const double dk = k;
+    const double a1 = 2.0 * dk * (dk + apb) * (2.0 * dk + apb - 2.0);
+    const double a2 = (2.0 * dk + apb - 1.0) * (a * a - b * b);
+    const double b3 = (2.0 * dk + apb - 2.0);
+    const double a3 = b3 * (b3 + 1.0) * (b3 + 2.0);
+    const double a4 = 2.0 * (dk + a - 1.0) * (dk + b - 1.0) * (2.0 * dk + apb);
+    const double pn = ((a2 + a3 * x) * r.p - a4 * pl) / a1;
+    const double pdn = ((a2 + a3 * x) * r.pd - a4 * pdl + a3 * r.p) / a1;
+    ps = pl;
+    pds = pdl;
+    pl = r.p;
+    r.p = pn;
+    pdl = r.pd;
+    r.pd = pdn;
+  }
+  r.pm1 = pl;
+  r.pdm1 = pdl;
+  r.pm2 = ps;
+  r.pdm2 = pds;
+  return r;
+}
+
+double gamma_small(double x) {  // exact values used by the GLL weights
+  const double sp = std::sqrt(kPi);
+  if (x == -0.5) return -2.0 * sp;
+  if (x == 0.5) return sp;
+  if (x == 1.5) return sp / 2.0;
+  if (x == 2.5) return 1.5 * sp / 2.0;
+  if (x == 3.5) return 2.5 * 1.5 * sp / 2.0;
+  if (x == 3.0) return 2.0;
+  if (x == 4.0) return 6.0;
+  if (x == 5.0) return 24.0;
+  if (x == 6.0) return 120.0;
+  return 1.0;
+}
+
+double end_weight(int n, double a, double b, bool right) {
+  const double apb = a + b;
+  if (n == 0) return 0.0;
+  double f1 = right ? gamma_small(a + 1.0) * gamma_small(b + 2.0) / gamma_small(apb + 3.0)
+                    : gamma_small(a + 2.0) * gamma_small(b + 1.0) / gamma_small(apb + 3.0);
+  f1 = f1 * (apb + 2.0) * std::pow(2.0, apb + 2.0) / 2.0;
+  if (n == 1) return f1;
+  double fint1 = right ? gamma_small(a + 1.0) * gamma_small(b + 2.0) / gamma_small(apb + 3.0)
+                       : gamma_small(a + 2.0) * gamma_small(b + 1.0) / gamma_small(apb + 3.0);
+  fint1 = fint1 * std::pow(2.0, apb + 2.0);
+  double fint2 = gamma_small(a + 2.0) * gamma_small(b + 2.0) / gamma_small(apb + 4.0);
+  fint2 = fint2 * std::pow(2.0, apb + 3.0);
+  double f2 = right ? (2.0 * (a + 2.0) * fint1 - (apb + 4.0) * fint2) * (apb + 3.0) / 4.0
+                    : (-2.0 * (b + 2.0) * fint1 + (apb + 4.0) * fint2) * (apb + 3.0) / 4.0;
+  if (n == 2) return f2;
+  double f3 = 0.0;
+  for (int i = 3; i <= n; ++i) {
+    const double di = i - 1, abn = a + b + di, abnn = abn + di;
+    const double a1 = -(2.0 * (di + a) * (di + b)) / (abn * abnn * (abnn + 1.0));
+    const double a2 = (2.0 * (a - b)) / (abnn * (abnn + 2.0));
+    const double a3 = (2.0 * (abn + 1.0)) / ((abnn + 2.0) * (abnn + 1.0));
+    f3 = -(a2 * f2 + a1 * f1) / a3;
+    f1 = f2;
+    f2 = f3;
+  }
+  return f3;
+}
+
+double jacobi_norm(int n, double a, double b) {
+  const double dn = n, c = a + b + 1.0;
+  double prod;
+  if (n <= 1) {
+    prod = gamma_small(dn + a) * gamma_small(dn + b);
+    prod = prod / (gamma_small(dn) * gamma_small(dn + a + b));
+    return prod * std::pow(2.0, c) / (2.0 * dn + c);
+  }
+  prod = gamma_small(a + 1.0) * gamma_small(b + 1.0);
+  prod = prod / (2.0 * (1.0 + c) * gamma_small(c + 1.0));
+  prod = prod * (1.0 + a) * (2.0 + a);
+  prod = prod * (1.0 + b) * (2.0 + b);
+  for (int i = 3; i <= n; ++i) {
+    const double di = i;
+    prod = prod * ((di + a) * (di + b) / (di * (di + a + b)));
+  }
+  return prod * std::pow(2.0, c) / (2.0 * dn + c);
+}
+
+void gauss_jacobi(double *z, double *w, int np, double a, double b) {
+  const double apb = a + b;
+  if (np == 1) {
+    z[0] = (b - a) / (apb + 2.0);
+    w[0] = gamma_small(a + 1.0) * gamma_small(b + 1.0) / gamma_small(apb + 2.0) *
+           std::pow(2.0, apb + 1.0);
+    return;
+  }
+  // roots, largest first, Newton with deflation of the roots already found
+  const int n = np - 1;
+  const double dth = 4.0 * std::atan(1.0) / (2.0 * n + 2.0);
+  double xlast = 0.0;
+  for (int j = 1; j <= np; ++j) {
+    double x = std::cos((2.0 * (j - 1.0) + 1.0) * dth);
+    if (j > 1) x = (x + xlast) / 2.0;
+    for (int k = 0; k < 10; ++k) {
+      const Jacobi J = jacobi_eval(np, a, b, x);
+      double rs = 0.0;
+      for (int i = 1; i <= j - 1; ++i) rs = rs + 1.0 / (x - z[np - i]);
+      const double dx = -J.p / (J.pd - rs * J.p);
+      x = x + dx;
+      if (std::fabs(dx) < 1.0e-12) break;
+    }
+    z[np - j] = x;
+    xlast = x;
+  }
+  // selection sort to ascending order (as gll.f90:370-381)
+  int jmin = 0;
+  for (int i = 0; i < np; ++i) {
+    double xm = 2.0;
+    for (int j = i; j < np; ++j)
+      if (z[j] < xm) {
+        xm = z[j];
+        jmin = j;
+      }
+    if (jmin != i) std::swap(z[i], z[jmin]);
+  }
+  const int np1 = n + 1, np2 = n + 2;
+  const double fac1 = np1 + a + b + 1.0, fac2 = fac1 + np1, fac3 = fac2 + 1.0;
+  const double rcoef = (jacobi_norm(np1, a, b) * fac2 * fac3) / (2.0 * fac1 * double(np2));
+  for (int i = 0; i < np; ++i) {
+    const Jacobi J = jacobi_eval(np2, a, b, z[i]);
+    w[i] = -rcoef / (J.p * J.pdm1);
+  }
+}
+
+double legendre(double z, int n) {
+  double p1 = 1.0, p2 = z, p3 = p2;
+  for (int k = 1; k <= n - 1; ++k) {
+    const double fk = k;
+    p3 = ((2.0 * fk + 1.0) * z * p2 - fk * p1) / (fk + 1.0);
+    p1 = p2;
+    p2 = p3;
+  }
+  return p3;
+}
+
+double legendre_deriv(double z, int n) {
+  double p1 = 1.0, p2 = z, p1d = 0.0, p2d = 1.0, p3d = 1.0;
+  for (int k = 1; k <= n - 1; ++k) {
+    const double fk = k;
+    const double p3 = ((2.0 * fk + 1.0) * z * p2 - fk * p1) / (fk + 1.0);
+    p3d = ((2.0 * fk + 1.0) * p2 + (2.0 * fk + 1.0) * z * p2d - fk * p1d) / (fk + 1.0);
+    p1 = p2;
+    p2 = p3;
+    p1d = p2d;
+    p2d = p3d;
+  }
+  return p3d;
+}
+
+struct Gll {
+  int n;
+  std::vector<double> x, w, H;  // H(i,j) = h'_i(x_j), column-major
+};
+
+Gll make_gll(int n) {
+  Gll g{n, std::vector<double>(n), std::vector<double>(n), std::vector<double>(n * n)};
+  if (n > 2) gauss_jacobi(&g.x[1], &g.w[1], n - 2, 1.0, 1.0);
+  g.x[0] = -1.0;
+  g.x[n - 1] = 1.0;
+  for (int i = 1; i < n - 1; ++i) g.w[i] = g.w[i] / (1.0 - g.x[i] * g.x[i]);
+  const int deg = n - 1;
+  g.w[0] = end_weight(deg, 0.0, 0.0, false) / (2.0 * jacobi_eval(deg, 0, 0, g.x[0]).pd);
+  g.w[n - 1] = end_weight(deg, 0.0, 0.0, true) / (2.0 * jacobi_eval(deg, 0, 0, g.x[n - 1]).pd);
+  if (n % 2) g.x[(n - 1) / 2] = 0.0;
+  const double dd = deg, al = dd * (dd + 1.0);
+  for (int j = 0; j < n; ++j)
+    for (int i = 0; i < n; ++i) {
+      double h;
+      if (i == 0 && j == 0) h = -dd * (dd + 1.0) / 4.0;
+      else if (i == deg && j == deg) h = dd * (dd + 1.0) / 4.0;
+      else if (i == j) h = 0.0;
+      else {
+        const double l1 = legendre(g.x[j], deg), l2 = legendre_deriv(g.x[j], deg);
+        const double l3 = legendre(g.x[i], deg), dz = g.x[j] - g.x[i];
+        h = l1 / (l3 * dz) + (1.0 - g.x[j] * g.x[j]) * l2 / (dd * (dd + 1.0) * l3 * dz * dz);
+      }
+      g.H[i + n * j] = h;
+    }
+  (void)al;
+  return g;
+}
+
+// Lagrange interpolant through the GLL points (gll.f90:269-296)
+double lagrange(int i, double z, const Gll &g) {
+  if (std::fabs(z - g.x[i]) < 1.0e-5) return 1.0;
+  const int n = g.n - 1;
+  const double al = double(n) * (double(n) + 1.0);
+  return -(1.0 - z * z) * legendre_deriv(z, n) / (al * legendre(g.x[i], n) * (z - g.x[i]));
+}
+
+// --------------------------------------------------------------------
+// Reverse Cuthill-McKee ordering of the 8-neighbour element graph of an
+// nx x nz box (mesh_structured.f90:204-269 with rcm.f90: root_find by
+// pseudo-peripheral search, level-by-level ordering with neighbours sorted
+// by increasing degree, then reversal).  Returns perm[new] = old (0-based).
+class ElementGraph {
+ public:
+  ElementGraph(int nx, int nz) : nx_(nx), nz_(nz), row_(size_t(nx) * nz + 1) {
+    static const int di[8] = {-1, 0, 1, -1, 1, -1, 0, 1};
+    static const int dj[8] = {-1, -1, -1, 0, 0, 1, 1, 1};
+    adj_.reserve(size_t(nx) * nz * 8);
+    for (int j = 0; j < nz; ++j)
+      for (int i = 0; i < nx; ++i) {
+        row_[size_t(j) * nx + i] = int(adj_.size());
+        for (int q = 0; q < 8; ++q) {
+          const int ii = i + di[q], jj = j + dj[q];
+          if (ii >= 0 && ii < nx && jj >= 0 && jj < nz) adj_.push_back(jj * nx + ii);
+        }
+      }
+    row_[size_t(nx) * nz] = int(adj_.size());
+  }
+  int size() const { return nx_ * nz_; }
+  int begin(int v) const { return row_[v]; }
+  int end(int v) const { return row_[v + 1]; }
+  int at(int k) const { return adj_[k]; }
+
+ private:
+  int nx_, nz_;
+  std::vector<int> row_, adj_;
+};
+
+// breadth-first level structure from root among unmasked vertices
+int level_structure(const ElementGraph &G, int root, std::vector<char> &mask,
+                    std::vector<int> &level, std::vector<int> &level_start) {
+  level.clear();
+  level_start.clear();
+  mask[root] = 0;
+  level.push_back(root);
+  size_t lbegin = 0;
+  while (true) {
+    const size_t lend = level.size();
+    level_start.push_back(int(lbegin));
+    for (size_t i = lbegin; i < lend; ++i) {
+      const int v = level[i];
+      for (int k = G.begin(v); k < G.end(v); ++k) {
+        const int u = G.at(k);
+        if (mask[u]) {
+          mask[u] = 0;
+          level.push_back(u);
+        }
+      }
+    }
+    if (level.size() == lend) break;
+    lbegin = lend;
+  }
+  for (int v : level) mask[v] = 1;
+  level_start.push_back(int(level.size()));
+  return int(level_start.size()) - 1;  // number of levels
+}
+
+std::vector<int> rcm_order(int nx, int nz) {
+  ElementGraph G(nx, nz);
+  const int n = G.size();
+  std::vector<char> mask(n, 1);
+  std::vector<int> perm;
+  perm.reserve(n);
+  std::vector<int> level, lstart, deg(n, 0);
+  for (int start = 0; start < n; ++start) {
+    if (!mask[start]) continue;
+    // pseudo-peripheral root
+    int root = start;
+    int nlev = level_structure(G, root, mask, level, lstart);
+    const int ncomp = int(level.size());
+    if (nlev != 1 && nlev != ncomp) {
+      while (true) {
+        int mindeg = ncomp;
+        const int last = lstart[nlev - 1];
+        root = level[last];
+        if (last < ncomp - 1) {
+          for (int j = last; j < ncomp; ++j) {
+            const int v = level[j];
+            int d = 0;
+            for (int k = G.begin(v); k < G.end(v); ++k) d += mask[G.at(k)] > 0;
+            if (d < mindeg) {
+              root = v;
+              mindeg = d;
+            }
+          }
+        }
+        const int nlev2 = level_structure(G, root, mask, level, lstart);
+        if (nlev2 <= nlev) break;
+        nlev = nlev2;
+        if (ncomp <= nlev) break;
+      }
+    }
+    // degrees within the component (counted over unmasked neighbours)
+    const size_t base = perm.size();
+    {
+      std::vector<char> seen(n, 0);
+      std::vector<int> q{root};
+      seen[root] = 1;
+      for (size_t i = 0; i < q.size(); ++i) {
+        const int v = q[i];
+        int d = 0;
+        for (int k = G.begin(v); k < G.end(v); ++k) {
+          const int u = G.at(k);
+          if (mask[u]) {
+            ++d;
+            if (!seen[u]) {
+              seen[u] = 1;
+              q.push_back(u);
+            }
+          }
+        }
+        deg[v] = d;
+      }
+    }
+    // Cuthill-McKee: children of each vertex, sorted by increasing degree
+    mask[root] = 0;
+    perm.push_back(root);
+    size_t lvl_end = base, lnbr = base + 1;
+    while (lvl_end < lnbr) {
+      const size_t lbegin = lvl_end;
+      lvl_end = lnbr;
+      for (size_t i = lbegin; i < lvl_end; ++i) {
+        const int v = perm[i];
+        const size_t first = lnbr;
+        for (int k = G.begin(v); k < G.end(v); ++k) {
+          const int u = G.at(k);
+          if (mask[u]) {
+            mask[u] = 0;
+            perm.push_back(u);
+            ++lnbr;
+          }
+        }
+        // stable insertion sort by degree of perm[first+1, lnbr); as in
+        // rcm.f90:571-590 the first child is never compared and stays first
+        for (size_t a = first + 2; a < lnbr; ++a) {
+          const int u = perm[a];
+          size_t b = a;
+          while (b > first + 1 && deg[perm[b - 1]] > deg[u]) {
+            perm[b] = perm[b - 1];
+            --b;
+          }
+          perm[b] = u;
+        }
+      }
+    }
+    std::reverse(perm.begin() + long(base), perm.end());
+  }
+  return perm;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+// Grid: control mesh, lattice, numbering, coordinates, boundary tables.
+struct sem2d_grid {
+  int ngll = 0, ndof = 0, nx = 0, nz = 0, ezflt = 0, npoin = 0, nelem = 0;
+  Gll gll;
+  std::vector<double> xc, zc;     // control-node coordinates
+  std::vector<int> elem_ex, elem_ez;  // structured position of element e (RCM order)
+  std::vector<int> tag;
+  std::vector<int> ibool;         // (ngll,ngll,nelem), 1-based
+  std::vector<double> coord;      // (2,npoin)
+  int LX = 0, LZ = 0;             // lattice size
+  std::vector<int> lattice;       // node number at lattice (I,J), 1-based
+  std::vector<int> row0;          // lattice row of local j=0 for element row ez
+  struct Boundary {
+    int tag;
+    std::vector<int> elem, edge;  // 1-based element, edge 1..4
+    std::vector<int> node;        // 1-based bulk nodes in boundary order
+    std::vector<int> ib;          // (ngll, nelem_b) boundary-node index, 1-based
+  };
+  std::vector<Boundary> bnds;
+  const Boundary *find(int t) const {
+    for (auto &b : bnds)
+      if (b.tag == t) return &b;
+    return nullptr;
+  }
+  // lattice index of GLL point (i,j) of element e
+  size_t lat(int e, int i, int j) const {
+    const int I = elem_ex[e] * (ngll - 1) + i;
+    const int J = row0[elem_ez[e]] + j;
+    return size_t(J) * LX + I;
+  }
+  // control-node corner coordinates of element e: (x1,z1,...,x4,z4), counterclockwise
+  void corners(int e, double *c) const {
+    const int i = elem_ex[e], j = elem_ez[e];
+    const int jr = j + (ezflt > 0 && j >= ezflt ? 1 : 0);  // control row with the split
+    c[0] = xc[i]; c[1] = zc[jr];
+    c[2] = xc[i + 1]; c[3] = zc[jr];
+    c[4] = xc[i + 1]; c[5] = zc[jr + 1];
+    c[6] = xc[i]; c[7] = zc[jr + 1];
+  }
+};
+
+namespace {
+
+// Q4 shape functions (elem_q4.f90:43-95)
+inline void q4_shape(double s, double t, double *sh) {
+  const double sp = s + 1.0, sm = s - 1.0, tp = t + 1.0, tm = t - 1.0;
+  sh[0] = 0.25 * sm * tm;
+  sh[1] = -(0.25 * sp * tm);
+  sh[2] = 0.25 * sp * tp;
+  sh[3] = -(0.25 * sm * tp);
+}
+inline void q4_dshape(double s, double t, double *d) {
+  const double sp = s + 1.0, sm = s - 1.0, tp = t + 1.0, tm = t - 1.0;
+  d[0] = 0.25 * tm; d[1] = -(0.25 * tm); d[2] = 0.25 * tp; d[3] = -(0.25 * tp);
+  d[4] = 0.25 * sm; d[5] = -(0.25 * sp); d[6] = 0.25 * sp; d[7] = -(0.25 * sm);
+}
+inline double interp4(const double *c, int a, const double *w) {
+  double acc = c[a] * w[0];
+  for (int k = 1; k < 4; ++k) acc = acc + c[a + 2 * k] * w[k];
+  return acc;
+}
+// Jacobian [dx/dxi dx/deta; dz/dxi dz/deta] at (s,t), column-major
+inline void jacobian(const double *c, double s, double t, double *J) {
+  double d[8];
+  q4_dshape(s, t, d);
+  for (int b = 0; b < 2; ++b)
+    for (int a = 0; a < 2; ++a) J[a + 2 * b] = interp4(c, a, d + 4 * b);
+}
+
+void edge_ij(int n, int edge, int k, int &i, int &j) {
+  switch (edge) {
+    case 1: i = k; j = 0; break;
+    case 2: i = n - 1; j = k; break;
+    case 3: i = n - 1 - k; j = n - 1; break;
+    default: i = 0; j = n - 1 - k; break;
+  }
+}
+
+void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
+  const int nx = dk.nelem[0], nz = dk.nelem[1];
+  if (nx <= 0 || nz <= 0) throw BuildError("CART_read: nelem must be positive");
+  if (dk.ngll < 2 || dk.ngll > 20) throw BuildError("ngll out of range");
+  if (dk.ndof != 1 && dk.ndof != 2) throw BuildError("ndof must be 1 or 2");
+  int ezflt = dk.ezflt;
+  if (ezflt >= nz) throw BuildError("CART_read: ezflt must be < nelem(2)");
+  if (ezflt == -1) ezflt = nz / 2;
+  if (ezflt < -1) throw BuildError("CART_read: ezflt must be >= -1");
+  g.ngll = dk.ngll;
+  g.ndof = dk.ndof;
+  g.nx = nx;
+  g.nz = nz;
+  g.ezflt = ezflt;
+  g.nelem = nx * nz;
+  g.gll = make_gll(dk.ngll);
+  const int N = g.ngll;
+  // control-node coordinates (mesh_cartesian.f90:248-263); the fault row is
+  // duplicated in zc
+  const double hx = (dk.xlim[1] - dk.xlim[0]) / double(nx);
+  const double hz = (dk.zlim[1] - dk.zlim[0]) / double(nz);
+  g.xc.resize(nx + 1);
+  for (int i = 0; i <= nx; ++i) g.xc[i] = dk.xlim[0] + hx * double(i);
+  for (int j = 0; j <= nz; ++j) {
+    g.zc.push_back(dk.zlim[0] + hz * double(j));
+    if (ezflt > 0 && j == ezflt) g.zc.push_back(dk.zlim[0] + hz * double(j));
+  }
+  // domain tags in structured order
+  std::vector<int> tag_s(size_t(nx) * nz, dk.ndomains == 0 ? 1 : 0);
+  for (int d = 0; d < dk.ndomains; ++d) {
+    const sem2d_domain &dm = dk.domains[d];
+    if (dm.tag < 1) throw BuildError("CART_read: tag null, negative or missing");
+    if (dm.ex[0] < 1 || dm.ex[0] > nx || dm.ex[1] < 1 || dm.ex[1] > nx || dm.ez[0] < 1 ||
+        dm.ez[0] > nz || dm.ez[1] < 1 || dm.ez[1] > nz)
+      throw BuildError("CART_read: domain index out of bounds");
+    for (int i = dm.ex[0]; i <= dm.ex[1]; ++i)
+      for (int j = dm.ez[0]; j <= dm.ez[1]; ++j) tag_s[size_t(j - 1) * nx + (i - 1)] = dm.tag;
+  }
+  if (dk.fztag > 0) {
+    const int fznz = dk.fznz > 0 ? dk.fznz : 1;
+    const int j1 = std::max(ezflt + 1 - fznz, 1), j2 = std::min(ezflt + fznz, nz);
+    for (int j = j1; j <= j2; ++j)
+      for (int i = 1; i <= nx; ++i) tag_s[size_t(j - 1) * nx + (i - 1)] = dk.fztag;
+  }
+  for (int t : tag_s)
+    if (t == 0) throw BuildError("CART_build: Domain tags not entirely set");
+  // element order
+  const std::vector<int> perm = rcm_order(nx, nz);
+  std::vector<int> inv(perm.size());
+  for (size_t k = 0; k < perm.size(); ++k) inv[perm[k]] = int(k);
+  g.elem_ex.resize(g.nelem);
+  g.elem_ez.resize(g.nelem);
+  g.tag.resize(g.nelem);
+  for (int e = 0; e < g.nelem; ++e) {
+    g.elem_ex[e] = perm[e] % nx;
+    g.elem_ez[e] = perm[e] / nx;
+    g.tag[e] = tag_s[perm[e]];
+  }
+  // GLL lattice with one extra row at the fault
+  g.LX = nx * (N - 1) + 1;
+  g.row0.resize(nz);
+  for (int j = 0; j < nz; ++j) g.row0[j] = j * (N - 1) + (ezflt > 0 && j >= ezflt ? 1 : 0);
+  g.LZ = g.row0[nz - 1] + N;
+  g.lattice.assign(size_t(g.LX) * g.LZ, 0);
+  // numbering (spec_grid.f90:198-314) on the lattice
+  int np = 0;
+  for (int e = 0; e < g.nelem; ++e) {
+    for (int j = 1; j < N - 1; ++j)
+      for (int i = 1; i < N - 1; ++i) g.lattice[g.lat(e, i, j)] = ++np;
+    for (int ed = 1; ed <= 4; ++ed) {
+      int i, j;
+      edge_ij(N, ed, 1, i, j);
+      if (g.lattice[g.lat(e, i, j)] > 0) continue;
+      for (int k = 1; k < N - 1; ++k) {
+        edge_ij(N, ed, k, i, j);
+        g.lattice[g.lat(e, i, j)] = ++np;
+      }
+    }
+    static const int vi[4] = {0, 1, 1, 0}, vj[4] = {0, 0, 1, 1};
+    for (int c = 0; c < 4; ++c) {
+      const size_t L = g.lat(e, vi[c] * (N - 1), vj[c] * (N - 1));
+      if (g.lattice[L] == 0) g.lattice[L] = ++np;
+    }
+  }
+  g.npoin = np;
+  g.ibool.resize(size_t(N) * N * g.nelem);
+  for (int e = 0; e < g.nelem; ++e)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) g.ibool[i + N * (j + size_t(N) * e)] = g.lattice[g.lat(e, i, j)];
+  // coordinates: the last element (in element order) writes a shared node
+  g.coord.assign(2 * size_t(np), 0.0);
+  std::vector<double> shp(4 * size_t(N) * N);
+  for (int j = 0; j < N; ++j)
+    for (int i = 0; i < N; ++i) q4_shape(g.gll.x[i], g.gll.x[j], &shp[4 * (i + N * j)]);
+  for (int e = 0; e < g.nelem; ++e) {
+    double c[8];
+    g.corners(e, c);
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        const int p = g.ibool[i + N * (j + size_t(N) * e)] - 1;
+        g.coord[2 * p] = interp4(c, 0, &shp[4 * (i + N * j)]);
+        g.coord[2 * p + 1] = interp4(c, 1, &shp[4 * (i + N * j)]);
+      }
+  }
+  // boundaries: tags 1..4 = bottom, right, top, left; 5/6 = fault sides
+  auto add_bnd = [&](int t, int edge, auto elem_of, int count, bool horizontal_line, int line) {
+    sem2d_grid::Boundary b;
+    b.tag = t;
+    for (int q = 0; q < count; ++q) {
+      b.elem.push_back(inv[elem_of(q)] + 1);
+      b.edge.push_back(edge);
+    }
+    // lattice line in increasing coordinate
+    if (horizontal_line)
+      for (int I = 0; I < g.LX; ++I) b.node.push_back(g.lattice[size_t(line) * g.LX + I]);
+    else
+      for (int J = 0; J < g.LZ; ++J) b.node.push_back(g.lattice[size_t(J) * g.LX + line]);
+    // position of each node of each boundary element in b.node
+    b.ib.resize(size_t(N) * count);
+    for (int q = 0; q < count; ++q) {
+      const int e = b.elem[q] - 1;
+      for (int k = 0; k < N; ++k) {
+        int i, j;
+        edge_ij(N, edge, k, i, j);
+        const size_t L = g.lat(e, i, j);
+        const int pos = horizontal_line ? int(L % g.LX) : int(L / g.LX);
+        b.ib[k + size_t(N) * q] = pos + 1;
+      }
+    }
+    g.bnds.push_back(std::move(b));
+  };
+  add_bnd(1, 1, [&](int q) { return q; }, nx, true, 0);
+  add_bnd(2, 2, [&](int q) { return q * nx + nx - 1; }, nz, false, g.LX - 1);
+  add_bnd(3, 3, [&](int q) { return (nz - 1) * nx + q; }, nx, true, g.LZ - 1);
+  add_bnd(4, 4, [&](int q) { return q * nx; }, nz, false, 0);
+  if (ezflt > 0) {
+    add_bnd(5, 3, [&](int q) { return (ezflt - 1) * nx + q; }, nx, true, g.row0[ezflt - 1] + N - 1);
+    add_bnd(6, 1, [&](int q) { return ezflt * nx + q; }, nx, true, g.row0[ezflt]);
+  }
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+struct sem2d_problem {
+  const sem2d_grid *g = nullptr;
+  int ndof = 0, time_kind = 0, nt = 0;
+  double dt = 0, courant = 0, beta = 0, gamma = 0.5;
+  std::vector<double> Kx, Kz, la, mu, mux, rho, cp, cs, kveta;
+  bool has_kv = false;
+  std::vector<double> mass;  // becomes rmass
+  std::vector<int> abs_node;
+  std::vector<double> abs_C;  // built per dof then transposed at export
+  std::vector<std::vector<double>> abs_Cd;
+  // fault
+  int nflt = 0;
+  bool two = false;
+  std::vector<int> node1, node2;
+  std::vector<double> fcoord, n1, B, invM1, invM2, Z, T0, coh;
+  double coefA2V = 0, coefA2D = 0;
+  std::vector<double> prm[SEM2D_FP_NPARAM];
+  int oit = 0, oitd = 1, oix1 = 1, oixn = 1, oixd = 1, fnsamp = 0;
+  // sources, receivers
+  std::vector<int> src_node;
+  std::vector<double> src_dir, src_f0, src_t0, src_amp, src_rel, src_tdelay;
+  int nrec = 0, rec_isamp = 1, rec_nsamp = 0;
+  char rec_field = 'V';
+  std::vector<int> rec_node, rec_elem;
+  std::vector<double> rec_interp, rec_coord;
+  std::vector<double> H, w;
+  sem2d_deck deck{};
+};
+
+namespace {
+
+const sem2d_material *find_mat(const sem2d_deck &dk, int tag) {
+  for (int m = 0; m < dk.nmats; ++m)
+    if (dk.mats[m].tag == tag) return &dk.mats[m];
+  return nullptr;
+}
+
+void build_materials(sem2d_problem &P, const sem2d_deck &dk) {
+  const sem2d_grid &g = *P.g;
+  const size_t n2 = size_t(g.ngll) * g.ngll, np = n2 * g.nelem;
+  for (auto *v : {&P.Kx, &P.Kz, &P.la, &P.mu, &P.mux, &P.rho, &P.cp, &P.cs}) v->assign(np, 0.0);
+  for (int m = 0; m < dk.nmats; ++m) P.has_kv |= dk.mats[m].kv != 0;
+  if (P.has_kv) P.kveta.assign(np, 0.0);
+  for (int e = 0; e < g.nelem; ++e) {
+    const sem2d_material *m = find_mat(dk, g.tag[e]);
+    if (!m) throw BuildError("element tag " + std::to_string(g.tag[e]) + " has no material");
+    if (!m->hetero && m->rho <= 0.0) throw BuildError("MAT_ELAST_read: undefined density (rho)");
+    if (m->hetero && (!dk.h_rho || (!m->aniso && (!dk.h_cp || !dk.h_cs)) ||
+                      (m->aniso && (!dk.h_c11 || !dk.h_c13 || !dk.h_c33 || !dk.h_c55 || !dk.h_c66))))
+      throw BuildError("heterogeneous material without per-point arrays");
+    if (!m->aniso && !m->hetero && m->cp > 0 && m->cs > 0) {
+      const double mu = m->rho * m->cs * m->cs, K = m->rho * m->cp * m->cp;
+      const double lam = m->rho * (m->cp * m->cp - 2.0 * m->cs * m->cs);
+      const double poiss = 0.5 * lam / (K - mu);
+      if (poiss < 0.0 || poiss > 0.5) throw BuildError("Poisson's ratio out of range !");
+    }
+    for (size_t q = 0; q < n2; ++q) {
+      const size_t p = q + n2 * e;
+      const double rho = m->hetero ? dk.h_rho[p] : m->rho;
+      P.rho[p] = rho;
+      if (!m->aniso) {
+        const double cp = m->hetero ? dk.h_cp[p] : m->cp, cs = m->hetero ? dk.h_cs[p] : m->cs;
+        const double lam = rho * (cp * cp - 2.0 * cs * cs), mu = rho * cs * cs;
+        P.cp[p] = cp;
+        P.cs[p] = cs;
+        P.la[p] = lam;
+        P.mu[p] = mu;
+        P.mux[p] = mu;
+        P.Kx[p] = lam + 2.0 * mu;
+        P.Kz[p] = P.Kx[p];
+      } else {
+        auto val = [&](double c, const double *h) { return m->hetero ? h[p] : c; };
+        const double c11 = val(m->c11, dk.h_c11), c13 = val(m->c13, dk.h_c13);
+        const double c33 = val(m->c33, dk.h_c33), c55 = val(m->c55, dk.h_c55);
+        const double c66 = val(m->c66, dk.h_c66);
+        P.la[p] = c13;
+        P.mu[p] = c55;
+        P.mux[p] = c66;
+        P.Kx[p] = c11;
+        P.Kz[p] = c33;
+        P.cp[p] = std::sqrt(c11 / rho);
+        P.cs[p] = std::sqrt(c55 / rho);
+      }
+      if (P.has_kv) P.kveta[p] = m->kv ? ((m->hetero && dk.h_kveta) ? dk.h_kveta[p] : m->kv_eta) : 0.0;
+    }
+  }
+}
+
+// CHECK_grid (init.f90:145-289) and TIME_read/TIME_init (time.f90:122-395)
+void build_time(sem2d_problem &P, const sem2d_deck &dk) {
+  const sem2d_grid &g = *P.g;
+  const int N = g.ngll;
+  const size_t n2 = size_t(N) * N;
+  double lam_min = 1e308, max_c_dx = 0.0;
+  for (int e = 0; e < g.nelem; ++e) {
+    double c[8];
+    g.corners(e, c);
+    double hsq[4] = {(c[2] - c[0]) * (c[2] - c[0]) + (c[3] - c[1]) * (c[3] - c[1]),
+                     (c[4] - c[2]) * (c[4] - c[2]) + (c[5] - c[3]) * (c[5] - c[3]),
+                     (c[6] - c[4]) * (c[6] - c[4]) + (c[7] - c[5]) * (c[7] - c[5]),
+                     (c[6] - c[0]) * (c[6] - c[0]) + (c[7] - c[1]) * (c[7] - c[1])};
+    const double hmax = std::sqrt(*std::max_element(hsq, hsq + 4));
+    const double *cs = &P.cs[n2 * e], *cp = &P.cp[n2 * e];
+    lam_min = std::min(lam_min, *std::min_element(cs, cs + n2) / hmax);
+    const double *cel = g.ndof == 2 ? cp : cs;
+    double rmax = 0.0;
+    for (int j = 0; j < N - 1; ++j)
+      for (int i = 0; i < N - 1; ++i) {
+        const int p0 = g.ibool[i + N * (j + size_t(N) * e)] - 1;
+        const int p1 = g.ibool[(i + 1) + N * (j + size_t(N) * e)] - 1;
+        const int p2 = g.ibool[i + N * ((j + 1) + size_t(N) * e)] - 1;
+        const double *c0 = &g.coord[2 * p0], *c1 = &g.coord[2 * p1], *c2 = &g.coord[2 * p2];
+        const double r1 = std::sqrt((c1[0] - c0[0]) * (c1[0] - c0[0]) + (c1[1] - c0[1]) * (c1[1] - c0[1]));
+        const double r2 = std::sqrt((c2[0] - c0[0]) * (c2[0] - c0[0]) + (c2[1] - c0[1]) * (c2[1] - c0[1]));
+        rmax = std::max(rmax, cel[i + N * j] / std::min(r1, r2));
+      }
+    max_c_dx = std::max(max_c_dx, rmax);
+  }
+  if (double(N) * lam_min / dk.fmax < 5.0)
+    throw BuildError("warning: low resolution at fmax (the reference aborts on warnings)");
+  int nsteps = dk.nsteps;
+  double dt = dk.dt, courant = dk.courant, total = dk.total_time;
+  if (nsteps < 0 || dt < 0 || total < 0) throw BuildError("TIME: negative setting");
+  if (courant < 0.0 || courant > 0.6) throw BuildError("TIME: Courant out of range [0,0.6]");
+  if (double(nsteps) * total != 0.0)
+    throw BuildError("TIME: bad combination of settings, NbSteps or TotalTime");
+  if (dt > 0.0) {
+    if (total > 0.0) nsteps = int(std::ceil(total / dt));
+    total = dt * nsteps;
+  }
+  P.time_kind = dk.time_kind;
+  double omega = 2.0;
+  if (dk.time_kind == SEM2D_TIME_NEWMARK) {
+    P.beta = dk.beta;
+    P.gamma = dk.gamma;
+    if (P.beta < 0 || P.beta > 1 || P.gamma < 0 || P.gamma > 1)
+      throw BuildError("TIME_NEWMARK: parameter out of range");
+    omega = std::sqrt(2.0 / P.gamma);
+  }
+  if (dt > 0.0) {
+    courant = max_c_dx * dt;
+  } else {
+    dt = courant / max_c_dx;
+    if (total > 0.0) nsteps = int(std::ceil(total / dt));
+  }
+  if (courant > omega * 3.0 / 7.0 / std::sqrt(2.0))
+    throw BuildError("warning: Courant number too high (the reference aborts on warnings)");
+  P.dt = dt;
+  P.courant = courant;
+  P.nt = nsteps;
+}
+
+double coefA2V(const sem2d_problem &P) { return P.time_kind == SEM2D_TIME_NEWMARK ? P.gamma * P.dt : P.dt; }
+double coefA2D(const sem2d_problem &P) { return P.time_kind == SEM2D_TIME_NEWMARK ? P.beta * P.dt * P.dt : 0.0; }
+double coefA2Vrhs(const sem2d_problem &P) {
+  return P.time_kind == SEM2D_TIME_NEWMARK ? 1.0 * coefA2V(P) : 0.5 * coefA2V(P);
+}
+
+// MAT_MASS_init (mat_mass.f90:29-61)
+void build_mass(sem2d_problem &P) {
+  const sem2d_grid &g = *P.g;
+  const int N = g.ngll;
+  P.mass.assign(size_t(g.npoin) * P.ndof, 0.0);
+  for (int e = 0; e < g.nelem; ++e) {
+    double c[8];
+    g.corners(e, c);
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        double J[4];
+        jacobian(c, g.gll.x[i], g.gll.x[j], J);
+        double dvol = J[0] * J[3] - J[2] * J[1];
+        dvol = dvol * (g.gll.w[i] * g.gll.w[j]);
+        const size_t q = i + N * (j + size_t(N) * e);
+        const int p = g.ibool[q] - 1;
+        P.mass[p] = P.mass[p] + P.rho[q] * dvol;
+      }
+  }
+  if (P.ndof == 2) std::copy(P.mass.begin(), P.mass.begin() + g.npoin, P.mass.begin() + g.npoin);
+}
+
+// BC_get_normal_and_weights (spec_grid.f90:961-1011)
+void normals(const sem2d_grid &g, const sem2d_grid::Boundary &b, std::vector<double> &nrm,
+             std::vector<double> &w) {
+  const int N = g.ngll, np = int(b.node.size());
+  nrm.assign(2 * size_t(np), 0.0);
+  w.assign(np, 0.0);
+  for (size_t q = 0; q < b.elem.size(); ++q) {
+    const int e = b.elem[q] - 1, ed = b.edge[q];
+    const int ld = (ed == 1 || ed == 3) ? 0 : 1;
+    const double sg = (ed == 3 || ed == 4) ? -1.0 : 1.0;
+    double c[8];
+    g.corners(e, c);
+    for (int k = 0; k < N; ++k) {
+      int i, j;
+      edge_ij(N, ed, k, i, j);
+      double J[4];
+      jacobian(c, g.gll.x[i], g.gll.x[j], J);
+      const double dx = J[0 + 2 * ld], dz = J[1 + 2 * ld];
+      const double j1 = std::sqrt(dx * dx + dz * dz);
+      const double tx = sg * dx / j1, tz = sg * dz / j1;
+      const int bn = b.ib[k + size_t(N) * q] - 1;
+      nrm[bn] = nrm[bn] + tz;
+      nrm[bn + np] = nrm[bn + np] + (-tx);
+      w[bn] = w[bn] + g.gll.w[k] * j1;
+    }
+  }
+  for (size_t q = 0; q < b.elem.size(); ++q)
+    for (int k : {0, N - 1}) {
+      const int bn = b.ib[k + size_t(N) * q] - 1;
+      const double r = std::sqrt(nrm[bn] * nrm[bn] + nrm[bn + np] * nrm[bn + np]);
+      nrm[bn] = nrm[bn] / r;
+      nrm[bn + np] = nrm[bn + np] / r;
+    }
+}
+
+// BC_ABSO_init (bc_abso.f90:115-266), Clayton-Engquist on flat sides
+void abso_init(sem2d_problem &P, int tag) {
+  const sem2d_grid &g = *P.g;
+  const sem2d_grid::Boundary *b = g.find(tag);
+  if (!b) return;  // the reference ignores a BC whose tag is absent (bc_gen.f90:214-219)
+  const int N = g.ngll, np = int(b->node.size()), nd = P.ndof;
+  std::vector<double> nrm, w;
+  normals(g, *b, nrm, w);
+  bool horiz = true, vert = true;
+  for (int k = 0; k < np; ++k) {
+    horiz &= std::fabs(nrm[k]) < kTinyXabs;
+    vert &= std::fabs(nrm[k + np]) < kTinyXabs;
+  }
+  if (!horiz && !vert) throw BuildError("absorbing boundary is not flat");
+  const int gtan = horiz ? 0 : 1, gnor = horiz ? 1 : 0;
+  std::vector<double> Cb(size_t(np) * nd, 0.0);
+  for (size_t q = 0; q < b->elem.size(); ++q) {
+    const int e = b->elem[q] - 1, ed = b->edge[q];
+    const int ld = (ed == 1 || ed == 3) ? 0 : 1;
+    double c8[8];
+    g.corners(e, c8);
+    for (int k = 0; k < N; ++k) {
+      int i, j;
+      edge_ij(N, ed, k, i, j);
+      const size_t p = i + N * (j + size_t(N) * e);
+      double cv[2];
+      cv[gnor] = P.cp[p];
+      cv[gtan] = P.cs[p];
+      double J[4];
+      jacobian(c8, g.gll.x[i], g.gll.x[j], J);
+      const double ci = g.gll.w[k] * std::sqrt(J[0 + 2 * ld] * J[0 + 2 * ld] + J[1 + 2 * ld] * J[1 + 2 * ld]);
+      const int bk = b->ib[k + size_t(N) * q] - 1;
+      if (nd == 1) {
+        Cb[bk] = Cb[bk] + P.rho[p] * cv[gtan] * ci;
+      } else {
+        Cb[bk] = Cb[bk] + P.rho[p] * cv[0] * ci;
+        Cb[bk + np] = Cb[bk + np] + P.rho[p] * cv[1] * ci;
+      }
+    }
+  }
+  const double cf = coefA2Vrhs(P);
+  for (int d = 0; d < nd; ++d)
+    for (int k = 0; k < np; ++k) {
+      const size_t p = size_t(b->node[k] - 1) + size_t(g.npoin) * d;
+      P.mass[p] = P.mass[p] + cf * Cb[k + size_t(np) * d];
+    }
+  if (P.abs_Cd.empty()) P.abs_Cd.resize(nd);
+  for (int k = 0; k < np; ++k) {
+    P.abs_node.push_back(b->node[k]);
+    for (int d = 0; d < nd; ++d) P.abs_Cd[d].push_back(Cb[k + size_t(np) * d]);
+  }
+}
+
+long nint_ref(double x) { return long(x >= 0 ? std::floor(x + 0.5) : -std::floor(-x + 0.5)); }
+
+// BC_DYNFLT_init (bc_dynflt.f90:231-520)
+void dynflt_init(sem2d_problem &P, const sem2d_deck &dk, const int *tags) {
+  const sem2d_grid &g = *P.g;
+  if (P.nflt) throw BuildError("only one DYNFLT boundary is supported");
+  const sem2d_grid::Boundary *b1 = g.find(tags[0]);
+  const sem2d_grid::Boundary *b2 = tags[1] > 0 ? g.find(tags[1]) : nullptr;
+  if (!b1 || (tags[1] > 0 && !b2)) return;
+  const int nd = P.ndof, nb = int(b1->node.size());
+  P.two = tags[1] > 0;
+  if (P.two && (b1->elem.size() != b2->elem.size() || b2->node.size() != b1->node.size()))
+    throw BuildError("bc_dynflt_init: boundaries do not match");
+  std::vector<double> nrm, w;
+  normals(g, *b1, nrm, w);
+  for (int k = 0; k < nb; ++k) {
+    if (P.two && b1->node[k] == b2->node[k]) continue;  // non-split nodes are dropped
+    P.node1.push_back(b1->node[k]);
+    P.node2.push_back(P.two ? b2->node[k] : 0);
+    P.B.push_back(w[k]);
+    P.n1.push_back(nrm[k]);
+  }
+  const int nf = int(P.node1.size());
+  P.nflt = nf;
+  {
+    std::vector<double> nz;
+    int q = 0;
+    for (int k = 0; k < nb; ++k) {
+      if (P.two && b1->node[k] == b2->node[k]) continue;
+      nz.push_back(nrm[k + nb]);
+      ++q;
+    }
+    P.n1.insert(P.n1.end(), nz.begin(), nz.end());
+  }
+  for (int k = 0; k < nf; ++k) {
+    const double *c1 = &g.coord[2 * size_t(P.node1[k] - 1)];
+    P.fcoord.push_back(c1[0]);
+    P.fcoord.push_back(c1[1]);
+    if (P.two) {
+      const double *c2 = &g.coord[2 * size_t(P.node2[k] - 1)];
+      if (std::fabs(c1[0] - c2[0]) > kTinyXabs || std::fabs(c1[1] - c2[1]) > kTinyXabs)
+        throw BuildError("bc_dynflt_init: coordinates on boundaries do not match properly");
+    }
+  }
+  P.coefA2V = coefA2V(P);
+  P.coefA2D = coefA2D(P);
+  P.invM1.assign(size_t(nf) * nd, 0.0);
+  P.invM2.assign(size_t(nf) * nd, 0.0);
+  P.Z.assign(size_t(nf) * nd, 0.0);
+  for (int d = 0; d < nd; ++d)
+    for (int k = 0; k < nf; ++k) {
+      const size_t o = size_t(k) + size_t(nf) * d;
+      P.invM1[o] = 1.0 / P.mass[size_t(P.node1[k] - 1) + size_t(g.npoin) * d];
+      if (P.two) {
+        P.invM2[o] = 1.0 / P.mass[size_t(P.node2[k] - 1) + size_t(g.npoin) * d];
+        P.Z[o] = 1.0 / (P.coefA2V * P.B[k] * (P.invM1[o] + P.invM2[o]));
+      } else {
+        P.Z[o] = 0.5 / (P.coefA2V * P.B[k] * P.invM1[o]);
+      }
+    }
+  for (int q = 0; q < SEM2D_FP_NPARAM; ++q) {
+    P.prm[q].resize(nf);
+    for (int k = 0; k < nf; ++k) P.prm[q][k] = dk.flt_array[q] ? dk.flt_array[q][k] : dk.flt_value[q];
+  }
+  P.T0.assign(2 * size_t(nf), 0.0);
+  P.coh.resize(nf);
+  for (int k = 0; k < nf; ++k) {
+    const double nx = P.n1[k], nz = P.n1[k + nf];
+    const double Sxx = P.prm[SEM2D_FP_SXX][k], Sxy = P.prm[SEM2D_FP_SXY][k];
+    const double Sxz = P.prm[SEM2D_FP_SXZ][k], Syz = P.prm[SEM2D_FP_SYZ][k];
+    const double Szz = P.prm[SEM2D_FP_SZZ][k];
+    const double Tx = Sxx * nx + Sxz * nz, Ty = Sxy * nx + Syz * nz, Tz = Sxz * nx + Szz * nz;
+    P.T0[k] = nd == 1 ? P.prm[SEM2D_FP_TT][k] + Ty : P.prm[SEM2D_FP_TT][k] + Tx * nz - Tz * nx;
+    P.T0[k + nf] = P.prm[SEM2D_FP_TN][k] + Tx * nx + Tz * nz;
+    P.coh[k] = P.prm[SEM2D_FP_COHESION][k];
+    if (P.coh[k] < 0.0) throw BuildError("bc_dynflt_init: cohesion must be positive");
+  }
+  P.oix1 = std::max(dk.flt_oxi[0], 1);
+  P.oixn = (dk.flt_oxi[1] > 0 && dk.flt_oxi[1] < nf) ? dk.flt_oxi[1] : nf;
+  P.oixd = dk.flt_oxi[2] > 0 ? dk.flt_oxi[2] : 1;
+  P.oitd = int(std::max(1L, nint_ref(dk.flt_otd / P.dt)));
+  P.oit = int(nint_ref(dk.flt_ot1 / P.dt));
+  P.fnsamp = (P.nt - P.oit) / P.oitd + 1;
+}
+
+// SE_find_nearest_node (spec_grid.f90:410-435): last node at the minimum
+int nearest_node(const sem2d_grid &g, const double *xz) {
+  double d2min = 1.7976931348623157e308;
+  int ig = 0;
+  for (int p = 0; p < g.npoin; ++p) {
+    const double dx = xz[0] - g.coord[2 * size_t(p)], dz = xz[1] - g.coord[2 * size_t(p) + 1];
+    const double d2 = dx * dx + dz * dz;
+    if (d2 <= d2min) {
+      d2min = d2;
+      ig = p + 1;
+    }
+  }
+  return ig;
+}
+
+// SE_find_point / FE_find_point (spec_grid.f90:471-497, fem_grid.f90:451-501):
+// Newton iteration for (xi,eta) in the first element holding the nearest node
+void find_point(const sem2d_grid &g, const double *xz, int &e_out, double &xi, double &eta,
+                double *newc) {
+  const int ig = nearest_node(g, xz), N = g.ngll;
+  for (int e = 0; e < g.nelem; ++e)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        if (g.ibool[i + N * (j + size_t(N) * e)] != ig) continue;
+        double c[8];
+        g.corners(e, c);
+        const double x1 = c[0] - c[4], x2 = c[1] - c[5], y1 = c[2] - c[6], y2 = c[3] - c[7];
+        const double area = 0.5 * std::fabs(x1 * y2 - x2 * y1);
+        const double tolf = kTinyXabs * std::sqrt(area / kPi), tolx = kTinyXabs;
+        double X[2] = {g.gll.x[i], g.gll.x[j]};
+        int it;
+        for (it = 1; it <= 100; ++it) {
+          double sh[4], J[4];
+          q4_shape(X[0], X[1], sh);
+          const double f0 = interp4(c, 0, sh) - xz[0], f1 = interp4(c, 1, sh) - xz[1];
+          jacobian(c, X[0], X[1], J);
+          if (std::fabs(f0) + std::fabs(f1) <= tolf) break;
+          const double det = J[0] * J[3] - J[2] * J[1];
+          const double i00 = J[3] / det, i10 = -J[1] / det, i01 = -J[2] / det, i11 = J[0] / det;
+          const double p0 = -f0, p1 = -f1;
+          const double q0 = i00 * p0 + i01 * p1, q1 = i10 * p0 + i11 * p1;
+          X[0] = X[0] + q0;
+          X[1] = X[1] + q1;
+          if (std::fabs(q0) + std::fabs(q1) <= tolx) break;
+        }
+        if (it >= 100) throw BuildError("FE_find_point: did not converge");
+        e_out = e + 1;
+        xi = X[0];
+        eta = X[1];
+        double sh[4];
+        q4_shape(xi, eta, sh);
+        newc[0] = interp4(c, 0, sh);
+        newc[1] = interp4(c, 1, sh);
+        return;
+      }
+  throw BuildError("SE_find_point: point not found");
+}
+
+void rec_init(sem2d_problem &P, const sem2d_deck &dk) {
+  const sem2d_grid &g = *P.g;
+  const int nx = dk.rec_number;
+  if (nx <= 0) return;
+  std::vector<double> rc(2 * size_t(nx));
+  if (dk.rec_coord) {
+    std::copy(dk.rec_coord, dk.rec_coord + 2 * nx, rc.begin());
+  } else if (nx > 1) {
+    for (int i = 0; i < nx; ++i)
+      for (int a = 0; a < 2; ++a)
+        rc[2 * i + a] = dk.rec_first[a] + (double(i) / double(nx - 1)) * (dk.rec_last[a] - dk.rec_first[a]);
+  } else {
+    rc[0] = dk.rec_first[0];
+    rc[1] = dk.rec_first[1];
+  }
+  P.rec_isamp = dk.rec_isamp > 0 ? dk.rec_isamp : 1;
+  P.rec_field = dk.rec_field ? dk.rec_field : 'V';
+  if (P.rec_field != 'D' && P.rec_field != 'V' && P.rec_field != 'A')
+    throw BuildError("REC_read: parameter field has wrong value [D,V,A]");
+  const int n2 = g.ngll * g.ngll;
+  if (dk.rec_atnode) {
+    for (int k = 0; k < nx; ++k) {
+      const int ip = nearest_node(g, &rc[2 * k]);
+      // receivers.f90:255 only de-duplicates from the third kept receiver on
+      if (P.rec_node.size() > 1 && std::find(P.rec_node.begin(), P.rec_node.end(), ip) != P.rec_node.end())
+        continue;
+      P.rec_node.push_back(ip);
+    }
+    P.nrec = int(P.rec_node.size());
+    for (int ip : P.rec_node) {
+      P.rec_coord.push_back(g.coord[2 * size_t(ip - 1)]);
+      P.rec_coord.push_back(g.coord[2 * size_t(ip - 1) + 1]);
+    }
+  } else {
+    P.nrec = nx;
+    for (int k = 0; k < nx; ++k) {
+      int e;
+      double xi, eta, nc[2];
+      find_point(g, &rc[2 * k], e, xi, eta, nc);
+      P.rec_elem.push_back(e);
+      for (int j = 0; j < g.ngll; ++j) {
+        const double fj = lagrange(j, eta, g.gll);
+        for (int i = 0; i < g.ngll; ++i) P.rec_interp.push_back(lagrange(i, xi, g.gll) * fj);
+      }
+      P.rec_coord.push_back(nc[0]);
+      P.rec_coord.push_back(nc[1]);
+    }
+    (void)n2;
+  }
+  P.rec_nsamp = P.nt / P.rec_isamp + 1;
+}
+
+void src_init(sem2d_problem &P, const sem2d_deck &dk) {
+  const int ns = dk.nsrc;
+  if (ns <= 0) return;
+  // &STF_RICKER reads f0, onset and ampli as REAL (stf_ricker.f90:49-51)
+  const float f0 = float(dk.ricker_f0), onset = float(dk.ricker_onset), amp = float(dk.ricker_ampli);
+  if (f0 <= 0.0f) throw BuildError("RICKER_read: f0 must be positive");
+  if (onset < 1.0f / f0) throw BuildError("warning: RICKER_read: Onset time too small");
+  const double ang = dk.force_angle * kPi / 180.0;
+  for (int k = 0; k < ns; ++k) {
+    P.src_node.push_back(nearest_node(*P.g, dk.src_coord + 2 * k));
+    P.src_dir.push_back(-std::sin(ang));
+    P.src_dir.push_back(std::cos(ang));
+    P.src_f0.push_back(double(f0));
+    P.src_t0.push_back(double(onset));
+    P.src_amp.push_back(double(amp));
+    P.src_rel.push_back(dk.src_ampli ? dk.src_ampli[k] : 1.0);
+    P.src_tdelay.push_back(dk.src_tdelay ? dk.src_tdelay[k] : 0.0);
+  }
+}
+
+int fail(const std::exception &e) {
+  g_err = e.what();
+  return SEM2D_E_ARG;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------
+extern "C" {
+
+int sem2d_grid_build(const sem2d_deck *deck, sem2d_grid **out) {
+  if (!deck || !out) return g_err = "null argument", SEM2D_E_ARG;
+  try {
+    auto g = std::make_unique<sem2d_grid>();
+    build_grid(*g, *deck);
+    *out = g.release();
+    return SEM2D_OK;
+  } catch (const std::bad_alloc &) {
+    g_err = "out of host memory";
+    return SEM2D_E_NOMEM;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+int sem2d_grid_sizes(const sem2d_grid *g, int *nelem, int *npoin, int *ngll) {
+  if (!g) return SEM2D_E_ARG;
+  if (nelem) *nelem = g->nelem;
+  if (npoin) *npoin = g->npoin;
+  if (ngll) *ngll = g->ngll;
+  return SEM2D_OK;
+}
+
+int sem2d_grid_ibool(const sem2d_grid *g, int *ibool) {
+  if (!g || !ibool) return SEM2D_E_ARG;
+  std::copy(g->ibool.begin(), g->ibool.end(), ibool);
+  return SEM2D_OK;
+}
+
+int sem2d_grid_coord(const sem2d_grid *g, double *coord) {
+  if (!g || !coord) return SEM2D_E_ARG;
+  std::copy(g->coord.begin(), g->coord.end(), coord);
+  return SEM2D_OK;
+}
+
+int sem2d_grid_tags(const sem2d_grid *g, int *tag) {
+  if (!g || !tag) return SEM2D_E_ARG;
+  std::copy(g->tag.begin(), g->tag.end(), tag);
+  return SEM2D_OK;
+}
+
+int sem2d_grid_boundary(const sem2d_grid *g, int tag, int *npoin, int *nodes) {
+  if (!g || !npoin) return SEM2D_E_ARG;
+  const sem2d_grid::Boundary *b = g->find(tag);
+  *npoin = b ? int(b->node.size()) : 0;
+  if (b && nodes) std::copy(b->node.begin(), b->node.end(), nodes);
+  return SEM2D_OK;
+}
+
+int sem2d_grid_gll(const sem2d_grid *g, double *x, double *w, double *H) {
+  if (!g) return SEM2D_E_ARG;
+  if (x) std::copy(g->gll.x.begin(), g->gll.x.end(), x);
+  if (w) std::copy(g->gll.w.begin(), g->gll.w.end(), w);
+  if (H) std::copy(g->gll.H.begin(), g->gll.H.end(), H);
+  return SEM2D_OK;
+}
+
+void sem2d_grid_destroy(sem2d_grid *g) { delete g; }
+
+int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_problem **out) {
+  if (!g || !deck || !out) return g_err = "null argument", SEM2D_E_ARG;
+  try {
+    auto P = std::make_unique<sem2d_problem>();
+    P->g = g;
+    P->deck = *deck;
+    P->ndof = g->ndof;
+    if (deck->ndof != g->ndof || deck->ngll != g->ngll) throw BuildError("deck does not match the grid");
+    build_materials(*P, *deck);
+    build_time(*P, *deck);
+    if (P->has_kv) {
+      const size_t n2 = size_t(g->ngll) * g->ngll;
+      for (int e = 0; e < g->nelem; ++e) {
+        const sem2d_material *m = find_mat(*deck, g->tag[e]);
+        if (m->kv && m->kv_etaxdt)
+          for (size_t q = 0; q < n2; ++q) P->kveta[q + n2 * e] = P->dt * P->kveta[q + n2 * e];
+      }
+    }
+    build_mass(*P);
+    for (int b = 0; b < deck->nbcs; ++b) {
+      const sem2d_bc &bc = deck->bcs[b];
+      if (bc.kind == SEM2D_BC_ABSORB) abso_init(*P, bc.tag[0]);
+      else if (bc.kind == SEM2D_BC_DYNFLT) dynflt_init(*P, *deck, bc.tag);
+      else throw BuildError("unsupported boundary condition kind");
+    }
+    rec_init(*P, *deck);
+    src_init(*P, *deck);
+    for (double &m : P->mass) m = 1.0 / m;  // init.f90:112-116
+    const int nd = P->ndof;
+    const size_t na = P->abs_node.size();
+    P->abs_C.resize(na * nd);
+    for (int d = 0; d < nd && na; ++d)
+      for (size_t k = 0; k < na; ++k) P->abs_C[k + na * d] = P->abs_Cd[d][k];
+    *out = P.release();
+    return SEM2D_OK;
+  } catch (const std::bad_alloc &) {
+    g_err = "out of host memory";
+    return SEM2D_E_NOMEM;
+  } catch (const std::exception &e) {
+    return fail(e);
+  }
+}
+
+#define VPTR(v) ((v).empty() ? nullptr : (v).data())
+
+int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
+  if (!P || !d) return SEM2D_E_ARG;
+  const sem2d_grid &g = *P->g;
+  std::memset(d, 0, sizeof(*d));
+  d->ngll = g.ngll;
+  d->ndof = P->ndof;
+  d->nelem = g.nelem;
+  d->npoin = g.npoin;
+  d->ibool = g.ibool.data();
+  d->coord = g.coord.data();
+  d->hprime = g.gll.H.data();
+  d->wgll = g.gll.w.data();
+  d->Kx = P->Kx.data();
+  d->Kz = P->Kz.data();
+  d->la = P->la.data();
+  d->mu = P->mu.data();
+  d->mux = P->mux.data();
+  d->kv_eta = P->has_kv ? P->kveta.data() : nullptr;
+  d->kd2_form = P->deck.kd2_form >= 0 ? P->deck.kd2_form : (g.ngll == 5);
+  d->rmass = P->mass.data();
+  d->nabs = int(P->abs_node.size());
+  d->abs_node = VPTR(P->abs_node);
+  d->abs_C = VPTR(P->abs_C);
+  d->time_scheme = P->time_kind;
+  d->dt = P->dt;
+  d->beta = P->beta;
+  d->gamma = P->gamma;
+  d->nt = P->nt;
+  d->nsrc = int(P->src_node.size());
+  d->src_node = VPTR(P->src_node);
+  d->src_dir = VPTR(P->src_dir);
+  d->src_f0 = VPTR(P->src_f0);
+  d->src_t0 = VPTR(P->src_t0);
+  d->src_ampli = VPTR(P->src_amp);
+  d->src_relamp = VPTR(P->src_rel);
+  d->src_tdelay = VPTR(P->src_tdelay);
+  d->nrec = P->nrec;
+  d->rec_field = P->rec_field;
+  d->rec_isamp = P->rec_isamp;
+  d->rec_nsamp = P->rec_nsamp;
+  d->rec_node = VPTR(P->rec_node);
+  d->rec_elem = VPTR(P->rec_elem);
+  d->rec_interp = VPTR(P->rec_interp);
+  d->nflt = P->nflt;
+  if (P->nflt) {
+    const sem2d_deck &dk = P->deck;
+    d->flt_node1 = P->node1.data();
+    d->flt_node2 = P->two ? P->node2.data() : nullptr;
+    d->flt_n1 = P->n1.data();
+    d->flt_B = P->B.data();
+    d->flt_invM1 = P->invM1.data();
+    d->flt_invM2 = P->two ? P->invM2.data() : nullptr;
+    d->flt_Z = P->Z.data();
+    d->flt_T0 = P->T0.data();
+    d->flt_cohesion = P->coh.data();
+    d->flt_coefA2V = P->coefA2V;
+    d->flt_coefA2D = P->coefA2D;
+    d->flt_opening = dk.flt_opening;
+    d->flt_friction = dk.flt_friction;
+    d->swf_kind = dk.swf_kind;
+    d->swf_healing = dk.swf_healing;
+    d->swf_dc = P->prm[SEM2D_FP_SWF_DC].data();
+    d->swf_mus = P->prm[SEM2D_FP_SWF_MUS].data();
+    d->swf_mud = P->prm[SEM2D_FP_SWF_MUD].data();
+    d->swf_p = P->prm[SEM2D_FP_SWF_P].data();
+    d->swf_alpha = P->prm[SEM2D_FP_SWF_ALPHA].data();
+    d->rsf_kind = dk.rsf_kind;
+    d->rsf_dc = P->prm[SEM2D_FP_RSF_DC].data();
+    d->rsf_mus = P->prm[SEM2D_FP_RSF_MUS].data();
+    d->rsf_a = P->prm[SEM2D_FP_RSF_A].data();
+    d->rsf_b = P->prm[SEM2D_FP_RSF_B].data();
+    d->rsf_vstar = P->prm[SEM2D_FP_RSF_VSTAR].data();
+    d->rsf_vc = P->prm[SEM2D_FP_RSF_VC].data();
+    d->rsf_theta = P->prm[SEM2D_FP_RSF_THETA].data();
+    d->flt_V0 = P->prm[SEM2D_FP_V0].data();
+    d->normal_kind = dk.normal_kind;
+    d->normal_T = dk.normal_T;
+    d->normal_L = dk.normal_L;
+    d->normal_V = dk.normal_V;
+    d->flt_oit = P->oit;
+    d->flt_oitd = P->oitd;
+    d->flt_oix1 = P->oix1;
+    d->flt_oixn = P->oixn;
+    d->flt_oixd = P->oixd;
+    d->flt_nsamp = P->fnsamp;
+  }
+  d->precision = P->deck.precision;
+  return SEM2D_OK;
+}
+
+int sem2d_problem_time(const sem2d_problem *P, double *dt, int *nt, double *courant) {
+  if (!P) return SEM2D_E_ARG;
+  if (dt) *dt = P->dt;
+  if (nt) *nt = P->nt;
+  if (courant) *courant = P->courant;
+  return SEM2D_OK;
+}
+
+int sem2d_problem_rec_coord(const sem2d_problem *P, double *coord) {
+  if (!P) return SEM2D_E_ARG;
+  if (coord) std::copy(P->rec_coord.begin(), P->rec_coord.end(), coord);
+  return P->nrec;
+}
+
+int sem2d_problem_fault_coord(const sem2d_problem *P, double *coord) {
+  if (!P) return SEM2D_E_ARG;
+  if (coord) std::copy(P->fcoord.begin(), P->fcoord.end(), coord);
+  return P->nflt;
+}
+
+void sem2d_problem_destroy(sem2d_problem *P) { delete P; }
+
+const char *sem2d_host_last_error(void) { return g_err.c_str(); }
+
+int sem2d_abi_struct_sizes(int *desc_size, int *deck_size) {
+  if (desc_size) *desc_size = int(sizeof(sem2d_problem_desc));
+  if (deck_size) *deck_size = int(sizeof(sem2d_deck));
+  return SEM2D_OK;
+}
+
+}  // extern "C"

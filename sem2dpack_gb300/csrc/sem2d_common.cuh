@@ -1,0 +1,127 @@
+// sem2d_common.cuh -- device layout and launch parameters shared by the
+// kernels and the host side of the GB300 time step.
+//
+// Device layout.  The Cartesian mesh of SEM2DPACK (mesh_cartesian.f90) is a
+// structured lattice of GLL nodes: LX = nx*(N-1)+1 columns and LZ rows, with
+// one extra row where a fault splits the mesh (mesh_structured.f90:78-80).
+// Element (ex,ez) covers columns ex*(N-1) .. ex*(N-1)+N-1 and rows
+// row0[ez] .. row0[ez]+N-1.  Every nodal field is stored as one plane per
+// degree of freedom, row-major with a padded row pitch:
+//     field[c*plane + J*pitch + I].
+// The reference's global numbering (ibool, RCM element order) is mapped to
+// this lattice once at upload and back at download.
+#pragma once
+
+#include <cstdint>
+
+namespace sem2d {
+
+constexpr int kMaxN = 9;          // largest NGLL compiled
+constexpr int kBulkThreads = 256; // threads of the bulk kernel
+constexpr int kMaxSrc = 64;
+
+// Parameters of the fused element-force + assembly + update kernel.
+template <typename real, int N>
+struct BulkParams {
+  // lattice
+  int LX, LZ, pitch;
+  long long plane;
+  int nx, nz;
+  const int *row0;  // [nz+1]; row0[nz] = LZ
+  int TX, TZ;       // tile of elements per CTA
+  // GLL operator
+  real H[N * N];    // H(i,j) = h'_i(x_j), column-major
+  real w[N];
+  // state (ping-pong buffers chosen by the host)
+  const real *Dcur;
+  real *Dnext;
+  const real *Vcur;
+  real *Vnext;
+  const real *Acur;
+  real *Anext;      // null unless accelerations are kept
+  // material
+  int mat_iso;      // isotropic: planes (la, mu) [P-SV] or (mu) [SH]
+  const real *mat[4];
+  int mat_elem;     // 1: per element GLL point (structured element order)
+  const real *kveta;// per element GLL point or null
+  const real *rmass;// lattice plane (both dofs equal away from the perimeter)
+  // element geometry (rectilinear): per column / per row
+  const real *xix;    // dxi/dx  of element column
+  const real *etaz;   // deta/dz of element row
+  const real *dxdxi;  // dx/dxi  of element column
+  const real *dzdeta; // dz/deta of element row
+  // perimeter table: slot -> rmass(dof), dashpots Ca(dof), Cb(dof)
+  const real *per_rm, *per_Ca, *per_Cb;
+  // fault rows (lattice rows of side 1 and side 2, -1 if none)
+  int jf1, jf2;
+  real *f_flt;      // [(side*ndof + c)*LX + I] raw forces for the fault kernel
+  // point sources
+  int nsrc;
+  const int *src_I, *src_J;
+  const double *src_amp;  // [(s*ndof + c)*(nt+1) + it]
+  int nt;
+  const int *step;        // completed steps (device counter)
+  // time scheme
+  int scheme;             // 0 leapfrog, 1 Newmark (beta = 0)
+  real dt, cv, cpred, cd2;// cv: coef a->v, cpred: (1-gamma)dt, cd2: (0.5-beta)dt^2
+  int kd2;
+};
+
+// Perimeter slot of lattice node (I,J): bottom row, top row, left column,
+// right column (corners belong to the rows).
+__host__ __device__ inline int perimeter_slot(int I, int J, int LX, int LZ) {
+  if (J == 0) return I;
+  if (J == LZ - 1) return LX + I;
+  if (I == 0) return 2 * LX + (J - 1);
+  if (I == LX - 1) return 2 * LX + (LZ - 2) + (J - 1);
+  return -1;
+}
+__host__ __device__ inline int perimeter_slots(int LX, int LZ) { return 2 * LX + 2 * (LZ - 2); }
+
+// Parameters of the per-step fault + bookkeeping kernel (FP64 fault state).
+template <typename real>
+struct FaultParams {
+  int ndof, LX, pitch;
+  long long plane;
+  int nflt, two, jf1, jf2;
+  const real *f_flt;
+  const real *Dcur;
+  real *Dnext, *Vnext, *Anext;
+  // FP64 shadow of the fault-node fields: [(side*ndof + c)*nflt + k]
+  double *d64, *v64, *a64;
+  const double *rm;     // [(side*ndof + c)*nflt + k] inverse mass
+  const double *n1;     // (nflt,2)
+  const double *B;      // [nflt]
+  const double *invM1, *invM2, *Z;  // (nflt,ndof)
+  const double *T0;     // (nflt,2)
+  const double *coh;
+  double coefA2V, coefA2D;
+  int opening, friction, swf_kind, swf_healing, rsf_kind, normal_kind;
+  double normal_V, normal_coef;
+  const double *swf_dc, *swf_mus, *swf_mud, *swf_p, *swf_alpha;
+  const double *rsf_dc, *rsf_mus, *rsf_a, *rsf_b, *rsf_vstar, *rsf_vc, *rsf_Tc, *rsf_coeft;
+  // state
+  double *D, *V, *T, *Tstick, *MU, *theta, *sigma;
+  // outputs: series[(q + onx*(rec + 6*sample))]
+  int oit, oitd, oix1, oixd, onx, nsamp;
+  double *series;
+  // time scheme
+  int scheme;
+  double dt, cv, cpred, cd2;
+  int *step;            // incremented by the last block
+  unsigned int *done;   // block completion counter (reset by the last block)
+  int *error;           // sticky device error flag (SEM2D_E_*)
+};
+
+template <typename real>
+struct RecParams {
+  int nrec, ndof, nsamp, isamp, npts;  // npts = 1 (at node) or N*N
+  long long plane;
+  const int *lat;       // [r*npts + q] lattice offset J*pitch+I
+  const double *w;      // [r*npts + q] weights (1 at node)
+  const real *field;
+  double *sis;          // sis(nsamp,nrec,ndof)
+  const int *step;
+};
+
+}  // namespace sem2d

@@ -1,0 +1,975 @@
+// sem2d_gpu.cu -- C-ABI of include/sem2d_gpu.h: upload, layout, launches.
+//
+// create():  validates the descriptor, recovers the structured GLL lattice
+//            behind the reference's global numbering (ibool + coord), picks
+//            the material layout, uploads everything.
+// step():    per time step launches (1) the fused bulk kernel, (2) the fault
+//            kernel -- or a counter bump when there is no fault -- and (3) the
+//            receiver kernel; runs of 2*kGraphPairs steps are captured once in
+//            a CUDA graph and replayed.
+// get_*():   synchronise and map results back to the reference numbering.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/sem2d_gpu.h"
+#include "bulk_launch.h"
+#include "fault_kernel.cuh"
+#include "sem2d_common.cuh"
+
+using namespace sem2d;
+
+namespace {
+
+std::string g_create_err;
+constexpr int kGraphPairs = 8;  // a captured graph covers 16 steps
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t n = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+};
+
+}  // namespace
+
+struct FaultScalars {
+  double coefA2V = 0, coefA2D = 0, normal_V = 0, normal_T = 1, normal_L = 1;
+  int opening = 0, swf_kind = 1, swf_healing = 0, rsf_kind = 1, normal_kind = 1;
+  int oit = 0, oitd = 1, oix1 = 1, oixd = 1;
+};
+
+struct sem2d_handle {
+  // problem
+  std::vector<double> H, w;          // GLL derivative matrix and weights
+  int kd2 = 0;
+  FaultScalars fs;
+  int N = 0, ndof = 0, nelem = 0, npoin = 0, nt = 0, mixed = 0, scheme = 0;
+  double dt = 0, beta = 0, gamma = 0.5;
+  int nx = 0, nz = 0, LX = 0, LZ = 0, pitch = 0;
+  long long plane = 0;
+  std::vector<int> row0;             // [nz+1]
+  std::vector<long long> glob2lat;   // global node -> J*pitch + I
+  std::vector<int> elem_ex, elem_ez; // reference element -> structured position
+  int TX = 8, TZ = 8, tile_nodes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
+  bool keep_accel = false;
+  // device memory
+  cudaStream_t stream = nullptr;
+  std::vector<void *> allocs;
+  void *D[2] = {nullptr, nullptr}, *V[2] = {nullptr, nullptr}, *A[2] = {nullptr, nullptr};
+  void *mat[4] = {nullptr, nullptr, nullptr, nullptr};
+  void *kveta = nullptr, *rmass = nullptr, *geo[4] = {nullptr, nullptr, nullptr, nullptr};
+  void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr, *f_flt = nullptr;
+  int *d_row0 = nullptr, *d_step = nullptr, *d_error = nullptr;
+  unsigned *d_done = nullptr;
+  // sources
+  int nsrc = 0;
+  int *src_I = nullptr, *src_J = nullptr;
+  double *src_amp = nullptr;
+  // receivers
+  int nrec = 0, rec_isamp = 1, rec_nsamp = 0, rec_npts = 1;
+  char rec_field = 'V';
+  int *rec_lat = nullptr;
+  double *rec_w = nullptr, *sis = nullptr;
+  // fault
+  int nflt = 0, two = 0, jf1 = -1, jf2 = -1, onx = 0, fnsamp = 0, friction = 0;
+  std::vector<double> h_fault_init;  // V0, theta for reset
+  double *fd[64] = {nullptr};        // fault arrays, see enum below
+  // time stepping
+  int cur = 0;       // ping-pong index of the current displacement predictor
+  int steps = 0;     // steps queued
+  long long launches = 0;
+  cudaGraphExec_t graph_exec = nullptr;
+  std::string err;
+};
+
+namespace {
+
+enum FaultArr {
+  F_D64, F_V64, F_A64, F_RM, F_N1, F_B, F_INVM1, F_INVM2, F_Z, F_T0, F_COH,
+  F_SWF_DC, F_SWF_MUS, F_SWF_MUD, F_SWF_P, F_SWF_ALPHA,
+  F_RSF_DC, F_RSF_MUS, F_RSF_A, F_RSF_B, F_RSF_VSTAR, F_RSF_VC, F_RSF_TC, F_RSF_COEFT,
+  F_D, F_V, F_T, F_TSTICK, F_MU, F_THETA, F_SIGMA, F_SERIES, F_COUNT
+};
+
+#define CK(call)                                                                       \
+  do {                                                                                 \
+    cudaError_t e_ = (call);                                                           \
+    if (e_ != cudaSuccess) {                                                           \
+      h->err = std::string(#call) + ": " + cudaGetErrorString(e_);                     \
+      return SEM2D_E_CUDA;                                                             \
+    }                                                                                  \
+  } while (0)
+
+int set_err(sem2d_handle *h, int code, const std::string &m) {
+  h->err = m;
+  return code;
+}
+
+template <typename T>
+int dalloc(sem2d_handle *h, T **out, size_t n, bool zero = true) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) return set_err(h, SEM2D_E_NOMEM, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+  h->allocs.push_back(p);
+  if (zero) {
+    e = cudaMemset(p, 0, n * sizeof(T));
+    if (e != cudaSuccess) return set_err(h, SEM2D_E_CUDA, cudaGetErrorString(e));
+  }
+  *out = static_cast<T *>(p);
+  return SEM2D_OK;
+}
+
+template <typename T>
+int dupload(sem2d_handle *h, T **out, const std::vector<T> &v) {
+  int st = dalloc(h, out, v.size(), false);
+  if (st) return st;
+  if (!v.empty()) CK(cudaMemcpy(*out, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return SEM2D_OK;
+}
+
+// real-typed upload of a double vector
+int upload_real(sem2d_handle *h, void **out, const std::vector<double> &v) {
+  if (h->mixed) {
+    std::vector<float> f(v.begin(), v.end());
+    float *p;
+    int st = dupload(h, &p, f);
+    *out = p;
+    return st;
+  }
+  double *p;
+  int st = dupload(h, &p, v);
+  *out = p;
+  return st;
+}
+
+double ricker(double t, double f0, double t0, double ampli) {
+  const double kPi = 3.141592653589793;
+  double arg = kPi * f0 * (t - t0);
+  arg = arg * arg;
+  return -((ampli * (1.0 - 2.0 * arg)) * std::exp(-arg));
+}
+
+// ---------------------------------------------------------------------
+// Recover the lattice: element columns/rows from the element corner
+// coordinates, shared or split rows from ibool.
+int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int N = d->ngll, ne = d->nelem;
+  auto ib = [&](int i, int j, int e) { return d->ibool[i + N * (j + (size_t)N * e)] - 1; };
+  std::vector<double> x0(ne), z0(ne), x1(ne), z1(ne);
+  for (int e = 0; e < ne; ++e) {
+    const int a = ib(0, 0, e), b = ib(N - 1, N - 1, e);
+    if (a < 0 || a >= d->npoin || b < 0 || b >= d->npoin)
+      return set_err(h, SEM2D_E_ARG, "ibool out of range");
+    x0[e] = d->coord[2 * (size_t)a];
+    z0[e] = d->coord[2 * (size_t)a + 1];
+    x1[e] = d->coord[2 * (size_t)b];
+    z1[e] = d->coord[2 * (size_t)b + 1];
+  }
+  std::vector<double> xs(x0), zs(z0);
+  std::sort(xs.begin(), xs.end());
+  xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
+  std::sort(zs.begin(), zs.end());
+  zs.erase(std::unique(zs.begin(), zs.end()), zs.end());
+  const int nx = int(xs.size()), nz = int(zs.size());
+  if ((long long)nx * nz != ne)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "mesh is not a structured rectilinear grid of elements");
+  h->nx = nx;
+  h->nz = nz;
+  h->elem_ex.resize(ne);
+  h->elem_ez.resize(ne);
+  std::vector<int> grid((size_t)nx * nz, -1);
+  for (int e = 0; e < ne; ++e) {
+    const int ex = int(std::lower_bound(xs.begin(), xs.end(), x0[e]) - xs.begin());
+    const int ez = int(std::lower_bound(zs.begin(), zs.end(), z0[e]) - zs.begin());
+    if (grid[(size_t)ez * nx + ex] >= 0)
+      return set_err(h, SEM2D_E_UNSUPPORTED, "two elements at one lattice position");
+    grid[(size_t)ez * nx + ex] = e;
+    h->elem_ex[e] = ex;
+    h->elem_ez[e] = ez;
+  }
+  // rows: shared (no fault) or split (fault) between consecutive element rows
+  h->row0.assign(nz + 1, 0);
+  for (int ez = 1; ez < nz; ++ez) {
+    int shared = -1;
+    for (int ex = 0; ex < nx; ++ex) {
+      const int lo = grid[(size_t)(ez - 1) * nx + ex], up = grid[(size_t)ez * nx + ex];
+      const int s = ib(0, N - 1, lo) == ib(0, 0, up) ? 1 : 0;
+      if (shared < 0) shared = s;
+      if (s != shared) return set_err(h, SEM2D_E_UNSUPPORTED, "partially split element row");
+    }
+    h->row0[ez] = h->row0[ez - 1] + (shared ? N - 1 : N);
+  }
+  for (int ez = 0; ez < nz; ++ez)
+    for (int ex = 1; ex < nx; ++ex)
+      if (ib(N - 1, 0, grid[(size_t)ez * nx + ex - 1]) != ib(0, 0, grid[(size_t)ez * nx + ex]))
+        return set_err(h, SEM2D_E_UNSUPPORTED, "vertically split element columns are not supported");
+  h->LX = nx * (N - 1) + 1;
+  h->LZ = h->row0[nz - 1] + N;
+  h->row0[nz] = h->LZ;
+  h->pitch = (h->LX + 7) / 8 * 8;
+  h->plane = (long long)h->pitch * h->LZ;
+  if ((long long)h->LX * h->LZ != d->npoin)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "node count does not match a structured lattice");
+  h->glob2lat.assign(d->npoin, -1);
+  for (int e = 0; e < ne; ++e)
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        const long long L = (long long)(h->row0[h->elem_ez[e]] + j) * h->pitch + h->elem_ex[e] * (N - 1) + i;
+        long long &slot = h->glob2lat[ib(i, j, e)];
+        if (slot >= 0 && slot != L) return set_err(h, SEM2D_E_UNSUPPORTED, "inconsistent ibool on the lattice");
+        slot = L;
+      }
+  for (int p = 0; p < d->npoin; ++p)
+    if (h->glob2lat[p] < 0) return set_err(h, SEM2D_E_ARG, "global node not referenced by ibool");
+  // rectilinear geometry: one width per column, one height per row
+  std::vector<double> dxdxi(nx), dzdeta(nz);
+  for (int e = 0; e < ne; ++e) {
+    const double ddx = 0.5 * (x1[e] - x0[e]), ddz = 0.5 * (z1[e] - z0[e]);
+    if (!(ddx > 0) || !(ddz > 0)) return set_err(h, SEM2D_E_ARG, "degenerate element");
+    dxdxi[h->elem_ex[e]] = ddx;
+    dzdeta[h->elem_ez[e]] = ddz;
+  }
+  for (int e = 0; e < ne; ++e)
+    if (0.5 * (x1[e] - x0[e]) != dxdxi[h->elem_ex[e]] || 0.5 * (z1[e] - z0[e]) != dzdeta[h->elem_ez[e]])
+      return set_err(h, SEM2D_E_UNSUPPORTED, "elements are not rectilinear");
+  std::vector<double> xix(nx), etaz(nz);
+  for (int i = 0; i < nx; ++i) xix[i] = 1.0 / dxdxi[i];
+  for (int j = 0; j < nz; ++j) etaz[j] = 1.0 / dzdeta[j];
+  int st;
+  if ((st = upload_real(h, &h->geo[0], xix)) || (st = upload_real(h, &h->geo[1], etaz)) ||
+      (st = upload_real(h, &h->geo[2], dxdxi)) || (st = upload_real(h, &h->geo[3], dzdeta)))
+    return st;
+  return SEM2D_OK;
+}
+
+int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int N = d->ngll, NN = N * N, ne = d->nelem;
+  const size_t npt = (size_t)NN * ne;
+  // isotropic?  Kx = Kz = la + 2 mu and mux = mu everywhere
+  bool iso = true;
+  for (size_t q = 0; q < npt && iso; ++q)
+    iso = d->Kx[q] == d->la[q] + 2.0 * d->mu[q] && d->Kz[q] == d->Kx[q] && d->mux[q] == d->mu[q];
+  std::vector<const double *> src;
+  if (d->ndof == 2) src = iso ? std::vector<const double *>{d->la, d->mu}
+                              : std::vector<const double *>{d->Kx, d->Kz, d->la, d->mu};
+  else src = iso ? std::vector<const double *>{d->mu} : std::vector<const double *>{d->mu, d->mux};
+  h->nmat = int(src.size());
+  h->mat_iso = iso;
+  // node layout when every shared node carries one value
+  bool node = true;
+  std::vector<std::vector<double>> planes(src.size(), std::vector<double>(h->plane, 0.0));
+  std::vector<char> seen(h->plane, 0);
+  for (int e = 0; e < ne && node; ++e)
+    for (int q = 0; q < NN && node; ++q) {
+      const long long L = h->glob2lat[d->ibool[q + (size_t)NN * e] - 1];
+      for (size_t m = 0; m < src.size(); ++m) {
+        const double v = src[m][q + (size_t)NN * e];
+        if (seen[L] && planes[m][L] != v) {
+          node = false;
+          break;
+        }
+        planes[m][L] = v;
+      }
+      seen[L] = 1;
+    }
+  h->mat_elem = node ? 0 : 1;
+  int st;
+  for (size_t m = 0; m < src.size(); ++m) {
+    if (node) {
+      st = upload_real(h, &h->mat[m], planes[m]);
+    } else {
+      std::vector<double> el(npt);
+      for (int e = 0; e < ne; ++e) {
+        const size_t eo = ((size_t)h->elem_ez[e] * h->nx + h->elem_ex[e]) * NN;
+        for (int q = 0; q < NN; ++q) el[eo + q] = src[m][q + (size_t)NN * e];
+      }
+      st = upload_real(h, &h->mat[m], el);
+    }
+    if (st) return st;
+  }
+  if (d->kv_eta) {
+    h->has_kv = 1;
+    std::vector<double> el(npt);
+    for (int e = 0; e < ne; ++e) {
+      const size_t eo = ((size_t)h->elem_ez[e] * h->nx + h->elem_ex[e]) * NN;
+      for (int q = 0; q < NN; ++q) el[eo + q] = d->kv_eta[q + (size_t)NN * e];
+    }
+    if ((st = upload_real(h, &h->kveta, el))) return st;
+  }
+  return SEM2D_OK;
+}
+
+int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int nd = d->ndof, np = d->npoin;
+  const int nslot = perimeter_slots(h->LX, h->LZ);
+  std::vector<double> rm(h->plane, 1.0), prm((size_t)nslot * nd, 0.0), pca((size_t)nslot * nd, 0.0),
+      pcb((size_t)nslot * nd, 0.0);
+  std::vector<int> used(nslot, 0);
+  for (int p = 0; p < np; ++p) {
+    const long long L = h->glob2lat[p];
+    const int I = int(L % h->pitch), J = int(L / h->pitch);
+    const int s = perimeter_slot(I, J, h->LX, h->LZ);
+    if (s >= 0) {
+      for (int c = 0; c < nd; ++c) prm[(size_t)c * nslot + s] = d->rmass[p + (size_t)np * c];
+    } else {
+      if (nd == 2 && d->rmass[p] != d->rmass[p + np] &&
+          !(h->nflt && (J == h->jf1 || J == h->jf2)))
+        return set_err(h, SEM2D_E_UNSUPPORTED, "dof-dependent mass away from the boundary");
+    }
+    rm[L] = d->rmass[p];
+  }
+  for (int k = 0; k < d->nabs; ++k) {
+    const int p = d->abs_node[k] - 1;
+    if (p < 0 || p >= np) return set_err(h, SEM2D_E_ARG, "absorbing node out of range");
+    const long long L = h->glob2lat[p];
+    const int s = perimeter_slot(int(L % h->pitch), int(L / h->pitch), h->LX, h->LZ);
+    if (s < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "absorbing node inside the domain");
+    if (used[s] >= 2) return set_err(h, SEM2D_E_UNSUPPORTED, "node on more than two absorbing boundaries");
+    std::vector<double> &dst = used[s] == 0 ? pca : pcb;
+    for (int c = 0; c < nd; ++c) dst[(size_t)c * nslot + s] = d->abs_C[k + (size_t)d->nabs * c];
+    used[s]++;
+  }
+  int st;
+  if ((st = upload_real(h, &h->rmass, rm)) || (st = upload_real(h, &h->per_rm, prm)) ||
+      (st = upload_real(h, &h->per_Ca, pca)) || (st = upload_real(h, &h->per_Cb, pcb)))
+    return st;
+  return SEM2D_OK;
+}
+
+int upload_fault(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int nf = d->nflt, nd = d->ndof, np = d->npoin;
+  h->nflt = nf;
+  if (!nf) return SEM2D_OK;
+  if (!d->flt_node1 || !d->flt_n1 || !d->flt_B || !d->flt_invM1 || !d->flt_Z || !d->flt_T0)
+    return set_err(h, SEM2D_E_ARG, "incomplete fault description");
+  h->two = d->flt_node2 != nullptr;
+  if (h->two && !d->flt_invM2) return set_err(h, SEM2D_E_ARG, "two-sided fault without invM2");
+  if (nf != h->LX) return set_err(h, SEM2D_E_UNSUPPORTED, "fault must span a full lattice row");
+  for (int side = 0; side < 1 + h->two; ++side) {
+    const int *nodes = side == 0 ? d->flt_node1 : d->flt_node2;
+    int J = -1;
+    for (int k = 0; k < nf; ++k) {
+      const int p = nodes[k] - 1;
+      if (p < 0 || p >= np) return set_err(h, SEM2D_E_ARG, "fault node out of range");
+      const long long L = h->glob2lat[p];
+      const int I = int(L % h->pitch), Jk = int(L / h->pitch);
+      if (k == 0) J = Jk;
+      if (I != k || Jk != J) return set_err(h, SEM2D_E_UNSUPPORTED, "fault nodes are not a lattice row");
+    }
+    (side == 0 ? h->jf1 : h->jf2) = J;
+  }
+  if (d->flt_friction == SEM2D_FRICTION_SWF) {
+    if (!d->swf_dc || !d->swf_mus || !d->swf_mud) return set_err(h, SEM2D_E_ARG, "missing SWF parameters");
+  } else if (d->flt_friction == SEM2D_FRICTION_RSF) {
+    if (!d->rsf_dc || !d->rsf_mus || !d->rsf_a || !d->rsf_b || !d->rsf_vstar)
+      return set_err(h, SEM2D_E_ARG, "missing RSF parameters");
+    if (d->rsf_kind < 1 || d->rsf_kind > 4) return set_err(h, SEM2D_E_ARG, "rsf_kind out of range");
+  } else {
+    return set_err(h, SEM2D_E_UNSUPPORTED, "fault without SWF or RSF friction");
+  }
+  h->friction = d->flt_friction;
+  auto vec = [&](const double *p, size_t n, double fill) {
+    std::vector<double> v(n, fill);
+    if (p) std::copy(p, p + n, v.begin());
+    return v;
+  };
+  std::vector<double> rmf((size_t)2 * nd * nf, 0.0);
+  for (int side = 0; side < 1 + h->two; ++side)
+    for (int c = 0; c < nd; ++c)
+      for (int k = 0; k < nf; ++k) {
+        const int p = (side == 0 ? d->flt_node1 : d->flt_node2)[k] - 1;
+        rmf[((size_t)side * nd + c) * nf + k] = d->rmass[p + (size_t)np * c];
+      }
+  int st;
+  auto up = [&](int idx, const std::vector<double> &v) { return dupload(h, &h->fd[idx], v); };
+  const size_t nfd = (size_t)nf * nd;
+  if ((st = dalloc(h, &h->fd[F_D64], 2 * nfd)) || (st = dalloc(h, &h->fd[F_V64], 2 * nfd)) ||
+      (st = dalloc(h, &h->fd[F_A64], 2 * nfd)) || (st = up(F_RM, rmf)) ||
+      (st = up(F_N1, vec(d->flt_n1, 2 * (size_t)nf, 0))) || (st = up(F_B, vec(d->flt_B, nf, 0))) ||
+      (st = up(F_INVM1, vec(d->flt_invM1, nfd, 0))) || (st = up(F_INVM2, vec(d->flt_invM2, nfd, 0))) ||
+      (st = up(F_Z, vec(d->flt_Z, nfd, 0))) || (st = up(F_T0, vec(d->flt_T0, 2 * (size_t)nf, 0))) ||
+      (st = up(F_COH, vec(d->flt_cohesion, nf, 0))))
+    return st;
+  if ((st = up(F_SWF_DC, vec(d->swf_dc, nf, 0.5))) || (st = up(F_SWF_MUS, vec(d->swf_mus, nf, 0.6))) ||
+      (st = up(F_SWF_MUD, vec(d->swf_mud, nf, 0.5))) || (st = up(F_SWF_P, vec(d->swf_p, nf, 3.0))) ||
+      (st = up(F_SWF_ALPHA, vec(d->swf_alpha, nf, 0.0))))
+    return st;
+  std::vector<double> rdc = vec(d->rsf_dc, nf, 0.5), rvs = vec(d->rsf_vstar, nf, 1.0);
+  std::vector<double> tc(nf), ct(nf);
+  for (int k = 0; k < nf; ++k) {
+    tc[k] = rdc[k] / rvs[k];
+    ct[k] = std::exp(-d->dt / tc[k]);
+  }
+  if ((st = up(F_RSF_DC, rdc)) || (st = up(F_RSF_MUS, vec(d->rsf_mus, nf, 0.6))) ||
+      (st = up(F_RSF_A, vec(d->rsf_a, nf, 0.01))) || (st = up(F_RSF_B, vec(d->rsf_b, nf, 0.02))) ||
+      (st = up(F_RSF_VSTAR, rvs)) || (st = up(F_RSF_VC, vec(d->rsf_vc, nf, 1e-6))) ||
+      (st = up(F_RSF_TC, tc)) || (st = up(F_RSF_COEFT, ct)))
+    return st;
+  // state
+  std::vector<double> V0(nfd, 0.0), th0(nf, 0.0);
+  if (h->friction == SEM2D_FRICTION_RSF) {
+    for (int k = 0; k < nf; ++k) {
+      V0[k] = d->flt_V0 ? d->flt_V0[k] : 1e-12;
+      th0[k] = d->rsf_theta ? d->rsf_theta[k] : 0.0;
+    }
+  }
+  h->h_fault_init = V0;
+  h->h_fault_init.insert(h->h_fault_init.end(), th0.begin(), th0.end());
+  if ((st = dalloc(h, &h->fd[F_D], nfd)) || (st = up(F_V, V0)) || (st = dalloc(h, &h->fd[F_T], 2 * (size_t)nf)) ||
+      (st = dalloc(h, &h->fd[F_TSTICK], 2 * (size_t)nf)) || (st = dalloc(h, &h->fd[F_MU], nf)) ||
+      (st = up(F_THETA, th0)) || (st = dalloc(h, &h->fd[F_SIGMA], nf)))
+    return st;
+  const int oix1 = d->flt_oix1 > 0 ? d->flt_oix1 : 1;
+  const int oixn = d->flt_oixn > 0 ? d->flt_oixn : nf;
+  const int oixd = d->flt_oixd > 0 ? d->flt_oixd : 1;
+  h->onx = (oixn - oix1) / oixd + 1;
+  h->fnsamp = std::max(d->flt_nsamp, 0);
+  if ((st = dalloc(h, &h->fd[F_SERIES], (size_t)h->onx * 6 * std::max(h->fnsamp, 1)))) return st;
+  return SEM2D_OK;
+}
+
+template <typename real>
+FaultParams<real> fault_params(sem2d_handle *h, int cur) {
+  const FaultScalars &s = h->fs;
+  FaultParams<real> f{};
+  f.ndof = h->ndof;
+  f.LX = h->LX;
+  f.pitch = h->pitch;
+  f.plane = h->plane;
+  f.nflt = h->nflt;
+  f.two = h->two;
+  f.jf1 = h->jf1;
+  f.jf2 = h->jf2;
+  f.f_flt = (const real *)h->f_flt;
+  f.Dcur = (const real *)h->D[cur];
+  f.Dnext = (real *)h->D[1 - cur];
+  f.Vnext = (real *)h->V[1 - cur];
+  f.Anext = h->keep_accel ? (real *)h->A[1 - cur] : nullptr;
+  f.d64 = h->fd[F_D64];
+  f.v64 = h->fd[F_V64];
+  f.a64 = h->fd[F_A64];
+  f.rm = h->fd[F_RM];
+  f.n1 = h->fd[F_N1];
+  f.B = h->fd[F_B];
+  f.invM1 = h->fd[F_INVM1];
+  f.invM2 = h->fd[F_INVM2];
+  f.Z = h->fd[F_Z];
+  f.T0 = h->fd[F_T0];
+  f.coh = h->fd[F_COH];
+  f.coefA2V = s.coefA2V;
+  f.coefA2D = s.coefA2D;
+  f.opening = s.opening;
+  f.friction = h->friction == SEM2D_FRICTION_RSF ? 2 : 1;
+  f.swf_kind = s.swf_kind;
+  f.swf_healing = s.swf_healing;
+  f.rsf_kind = s.rsf_kind;
+  f.normal_kind = s.normal_kind;
+  f.normal_V = s.normal_V;
+  f.normal_coef = 0;
+  if (s.normal_kind == 2) f.normal_coef = std::exp(-h->dt / s.normal_T);
+  if (s.normal_kind == 3) f.normal_coef = h->dt / s.normal_L;
+  f.swf_dc = h->fd[F_SWF_DC];
+  f.swf_mus = h->fd[F_SWF_MUS];
+  f.swf_mud = h->fd[F_SWF_MUD];
+  f.swf_p = h->fd[F_SWF_P];
+  f.swf_alpha = h->fd[F_SWF_ALPHA];
+  f.rsf_dc = h->fd[F_RSF_DC];
+  f.rsf_mus = h->fd[F_RSF_MUS];
+  f.rsf_a = h->fd[F_RSF_A];
+  f.rsf_b = h->fd[F_RSF_B];
+  f.rsf_vstar = h->fd[F_RSF_VSTAR];
+  f.rsf_vc = h->fd[F_RSF_VC];
+  f.rsf_Tc = h->fd[F_RSF_TC];
+  f.rsf_coeft = h->fd[F_RSF_COEFT];
+  f.D = h->fd[F_D];
+  f.V = h->fd[F_V];
+  f.T = h->fd[F_T];
+  f.Tstick = h->fd[F_TSTICK];
+  f.MU = h->fd[F_MU];
+  f.theta = h->fd[F_THETA];
+  f.sigma = h->fd[F_SIGMA];
+  f.oit = s.oit;
+  f.oitd = s.oitd;
+  f.oix1 = s.oix1;
+  f.oixd = s.oixd;
+  f.onx = h->onx;
+  f.nsamp = h->fnsamp;
+  f.series = h->fd[F_SERIES];
+  f.scheme = h->scheme;
+  f.dt = h->dt;
+  f.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
+  f.cpred = (1.0 - h->gamma) * h->dt;
+  f.cd2 = (0.5 - h->beta) * h->dt * h->dt;
+  f.step = h->d_step;
+  f.done = h->d_done;
+  f.error = h->d_error;
+  return f;
+}
+
+template <typename real>
+int launch_fault_init(sem2d_handle *h) {
+  if (!h->nflt) return SEM2D_OK;
+  FaultParams<real> f = fault_params<real>(h, h->cur);
+  fault_init_kernel<real><<<(h->nflt + 127) / 128, 128, 0, h->stream>>>(f);
+  CK(cudaGetLastError());
+  h->launches++;
+  return SEM2D_OK;
+}
+
+template <typename real>
+int launch_one_step(sem2d_handle *h, int cur) {
+  BulkConfig bc;
+  bc.N = h->N;
+  bc.ndof = h->ndof;
+  bc.mixed = h->mixed;
+  bc.tile_nodes = h->tile_nodes;
+  bc.nmat = h->nmat;
+  bc.has_kv = h->has_kv;
+  bc.mat_elem = h->mat_elem;
+  bc.mat_iso = h->mat_iso;
+  bc.grid_x = (h->nx + h->TX - 1) / h->TX;
+  bc.grid_y = (h->nz + h->TZ - 1) / h->TZ;
+  bc.LX = h->LX;
+  bc.LZ = h->LZ;
+  bc.pitch = h->pitch;
+  bc.plane = h->plane;
+  bc.nx = h->nx;
+  bc.nz = h->nz;
+  bc.row0 = h->d_row0;
+  bc.TX = h->TX;
+  bc.TZ = h->TZ;
+  bc.Dcur = h->D[cur];
+  bc.Dnext = h->D[1 - cur];
+  bc.Vcur = h->V[cur];
+  bc.Vnext = h->V[1 - cur];
+  bc.Acur = h->A[cur];
+  bc.Anext = h->keep_accel ? h->A[1 - cur] : nullptr;
+  for (int m = 0; m < 4; ++m) bc.mat[m] = h->mat[m];
+  bc.kveta = h->kveta;
+  bc.rmass = h->rmass;
+  for (int g = 0; g < 4; ++g) bc.geo[g] = h->geo[g];
+  bc.per_rm = h->per_rm;
+  bc.per_Ca = h->per_Ca;
+  bc.per_Cb = h->per_Cb;
+  bc.jf1 = h->nflt ? h->jf1 : -1;
+  bc.jf2 = h->nflt ? h->jf2 : -1;
+  bc.f_flt = h->f_flt;
+  bc.nsrc = h->nsrc;
+  bc.src_I = h->src_I;
+  bc.src_J = h->src_J;
+  bc.src_amp = h->src_amp;
+  bc.nt = h->nt;
+  bc.step = h->d_step;
+  bc.scheme = h->scheme;
+  bc.dt = h->dt;
+  bc.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
+  bc.cpred = (1.0 - h->gamma) * h->dt;
+  bc.cd2 = (0.5 - h->beta) * h->dt * h->dt;
+  bc.kd2 = h->kd2;
+  bc.H = h->H.data();
+  bc.w = h->w.data();
+  bc.stream = h->stream;
+  int st = launch_bulk(bc);
+  if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+  h->launches++;
+  if (h->nflt) {
+    FaultParams<real> f = fault_params<real>(h, cur);
+    fault_step_kernel<real><<<(h->nflt + 127) / 128, 128, 0, h->stream>>>(f);
+  } else {
+    advance_kernel<<<1, 1, 0, h->stream>>>(h->d_step);
+  }
+  CK(cudaGetLastError());
+  h->launches++;
+  if (h->nrec) {
+    RecParams<real> r{};
+    r.nrec = h->nrec;
+    r.ndof = h->ndof;
+    r.nsamp = h->rec_nsamp;
+    r.isamp = h->rec_isamp;
+    r.npts = h->rec_npts;
+    r.plane = h->plane;
+    r.lat = h->rec_lat;
+    r.w = h->rec_w;
+    // after the step: d^n is the buffer read (cur), v and a the ones written
+    r.field = (const real *)(h->rec_field == 'D' ? h->D[cur] : (h->rec_field == 'A' ? h->A[1 - cur] : h->V[1 - cur]));
+    r.sis = h->sis;
+    r.step = h->d_step;
+    const int nthr = h->nrec * h->ndof;
+    receiver_kernel<real><<<(nthr + 127) / 128, 128, 0, h->stream>>>(r);
+    CK(cudaGetLastError());
+    h->launches++;
+  }
+  return SEM2D_OK;
+}
+
+int launch_steps(sem2d_handle *h, int n) {
+  for (int k = 0; k < n; ++k) {
+    const int st = h->mixed ? launch_one_step<float>(h, h->cur) : launch_one_step<double>(h, h->cur);
+    if (st) return st;
+    h->cur = 1 - h->cur;
+    h->steps++;
+  }
+  return SEM2D_OK;
+}
+
+int kernels_per_step(const sem2d_handle *h) { return 2 + (h->nrec ? 1 : 0); }
+
+int ensure_graph(sem2d_handle *h) {
+  if (h->graph_exec) return SEM2D_OK;
+  const int cur0 = h->cur, steps0 = h->steps;
+  const long long l0 = h->launches;
+  cudaGraph_t graph;
+  CK(cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal));
+  int st = launch_steps(h, 2 * kGraphPairs);
+  cudaError_t e = cudaStreamEndCapture(h->stream, &graph);
+  h->cur = cur0;
+  h->steps = steps0;
+  h->launches = l0;
+  if (st) return st;
+  if (e != cudaSuccess) return set_err(h, SEM2D_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph_exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return set_err(h, SEM2D_E_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  return SEM2D_OK;
+}
+
+int reset_state(sem2d_handle *h) {
+  const size_t rs = h->mixed ? sizeof(float) : sizeof(double);
+  for (int b = 0; b < 2; ++b) {
+    CK(cudaMemsetAsync(h->D[b], 0, rs * h->plane * h->ndof, h->stream));
+    CK(cudaMemsetAsync(h->V[b], 0, rs * h->plane * h->ndof, h->stream));
+    if (h->A[b]) CK(cudaMemsetAsync(h->A[b], 0, rs * h->plane * h->ndof, h->stream));
+  }
+  CK(cudaMemsetAsync(h->d_step, 0, sizeof(int), h->stream));
+  CK(cudaMemsetAsync(h->d_done, 0, sizeof(unsigned), h->stream));
+  CK(cudaMemsetAsync(h->d_error, 0, sizeof(int), h->stream));
+  if (h->sis) CK(cudaMemsetAsync(h->sis, 0, sizeof(double) * (size_t)h->rec_nsamp * h->nrec * h->ndof, h->stream));
+  if (h->nflt) {
+    const size_t nfd = (size_t)h->nflt * h->ndof;
+    for (int a : {F_D64, F_V64, F_A64}) CK(cudaMemsetAsync(h->fd[a], 0, sizeof(double) * 2 * nfd, h->stream));
+    for (int a : {F_D}) CK(cudaMemsetAsync(h->fd[a], 0, sizeof(double) * nfd, h->stream));
+    for (int a : {F_T, F_TSTICK}) CK(cudaMemsetAsync(h->fd[a], 0, sizeof(double) * 2 * h->nflt, h->stream));
+    CK(cudaMemcpyAsync(h->fd[F_V], h->h_fault_init.data(), sizeof(double) * nfd, cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(h->fd[F_THETA], h->h_fault_init.data() + nfd, sizeof(double) * h->nflt,
+                       cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemsetAsync(h->fd[F_SERIES], 0, sizeof(double) * (size_t)h->onx * 6 * std::max(h->fnsamp, 1), h->stream));
+  }
+  h->cur = 0;
+  h->steps = 0;
+  int st = h->mixed ? launch_fault_init<float>(h) : launch_fault_init<double>(h);
+  return st;
+}
+
+int check_device_error(sem2d_handle *h) {
+  int e = 0;
+  CK(cudaStreamSynchronize(h->stream));
+  CK(cudaMemcpy(&e, h->d_error, sizeof(int), cudaMemcpyDeviceToHost));
+  if (e == SEM2D_E_NR) return set_err(h, SEM2D_E_NR, "rate-and-state Newton solver did not converge");
+  if (e) return set_err(h, e, "device error");
+  return SEM2D_OK;
+}
+
+int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
+  if (d->ngll != 5 && d->ngll != 6 && d->ngll != 9)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "GPU kernels are compiled for ngll in {5, 6, 9}");
+  if (d->ndof != 1 && d->ndof != 2) return set_err(h, SEM2D_E_ARG, "ndof must be 1 or 2");
+  if (d->nelem <= 0 || d->npoin <= 0 || !d->ibool || !d->coord || !d->hprime || !d->wgll || !d->rmass ||
+      !d->Kx || !d->Kz || !d->la || !d->mu || !d->mux)
+    return set_err(h, SEM2D_E_ARG, "incomplete descriptor");
+  if (!(d->dt > 0) || d->nt < 0) return set_err(h, SEM2D_E_ARG, "bad time step settings");
+  if (d->time_scheme == SEM2D_TIME_NEWMARK && d->beta != 0.0)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "Newmark with beta != 0 is not supported on the GPU path");
+  if (d->precision != SEM2D_PRECISION_FP64 && d->precision != SEM2D_PRECISION_MIXED)
+    return set_err(h, SEM2D_E_ARG, "unknown precision");
+  h->N = d->ngll;
+  h->ndof = d->ndof;
+  h->nelem = d->nelem;
+  h->npoin = d->npoin;
+  h->nt = d->nt;
+  h->mixed = d->precision == SEM2D_PRECISION_MIXED;
+  h->scheme = d->time_scheme == SEM2D_TIME_NEWMARK ? 1 : 0;
+  h->dt = d->dt;
+  h->beta = d->beta;
+  h->gamma = h->scheme ? d->gamma : 0.5;
+  h->keep_accel = h->scheme == 1 || d->rec_field == 'A';
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  int st;
+  if ((st = detect_lattice(h, d))) return st;
+  if ((st = upload_fault(h, d))) return st;
+  if ((st = upload_material(h, d))) return st;
+  if ((st = upload_mass_and_boundaries(h, d))) return st;
+  {
+    FaultScalars &fs = h->fs;
+    fs.coefA2V = d->flt_coefA2V;
+    fs.coefA2D = d->flt_coefA2D;
+    fs.normal_V = d->normal_V;
+    fs.normal_T = d->normal_T;
+    fs.normal_L = d->normal_L;
+    fs.opening = d->flt_opening;
+    fs.swf_kind = d->swf_kind;
+    fs.swf_healing = d->swf_healing;
+    fs.rsf_kind = d->rsf_kind;
+    fs.normal_kind = d->normal_kind;
+    fs.oit = d->flt_oit;
+    fs.oitd = d->flt_oitd > 0 ? d->flt_oitd : 1;
+    fs.oix1 = d->flt_oix1 > 0 ? d->flt_oix1 : 1;
+    fs.oixd = d->flt_oixd > 0 ? d->flt_oixd : 1;
+  }
+  const size_t rs = h->mixed ? sizeof(float) : sizeof(double);
+  for (int b = 0; b < 2; ++b) {
+    char *p;
+    if ((st = dalloc(h, &p, rs * h->plane * h->ndof))) return st;
+    h->D[b] = p;
+    if ((st = dalloc(h, &p, rs * h->plane * h->ndof))) return st;
+    h->V[b] = p;
+    if (h->keep_accel) {
+      if ((st = dalloc(h, &p, rs * h->plane * h->ndof))) return st;
+      h->A[b] = p;
+    }
+  }
+  {
+    char *p;
+    if ((st = dalloc(h, &p, rs * 2 * h->ndof * std::max(h->LX, 1)))) return st;
+    h->f_flt = p;
+  }
+  if ((st = dupload(h, &h->d_row0, h->row0))) return st;
+  if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)))
+    return st;
+  h->H.assign(d->hprime, d->hprime + h->N * h->N);
+  h->w.assign(d->wgll, d->wgll + h->N);
+  h->kd2 = d->kd2_form ? 1 : 0;
+  // sources: lattice position and per-step amplitude (SO_add, src_gen.f90:290-317)
+  h->nsrc = d->nsrc;
+  if (h->nsrc > kMaxSrc) return set_err(h, SEM2D_E_UNSUPPORTED, "too many sources");
+  if (h->nsrc) {
+    std::vector<int> sI(h->nsrc), sJ(h->nsrc);
+    std::vector<double> amp((size_t)h->nsrc * h->ndof * (h->nt + 1), 0.0);
+    for (int s = 0; s < h->nsrc; ++s) {
+      const int p = d->src_node[s] - 1;
+      if (p < 0 || p >= d->npoin) return set_err(h, SEM2D_E_ARG, "source node out of range");
+      sI[s] = int(h->glob2lat[p] % h->pitch);
+      sJ[s] = int(h->glob2lat[p] / h->pitch);
+      const double td = d->src_tdelay ? d->src_tdelay[s] : 0.0, rel = d->src_relamp ? d->src_relamp[s] : 1.0;
+      for (int it = 1; it <= h->nt; ++it) {
+        const double t = it * d->dt;
+        double a = ricker(t - td, d->src_f0[s], d->src_t0[s], d->src_ampli[s]);
+        a = a * rel;
+        for (int c = 0; c < h->ndof; ++c)
+          amp[((size_t)s * h->ndof + c) * (h->nt + 1) + it] = h->ndof == 1 ? a : d->src_dir[2 * s + c] * a;
+      }
+    }
+    if ((st = dupload(h, &h->src_I, sI)) || (st = dupload(h, &h->src_J, sJ)) || (st = dupload(h, &h->src_amp, amp)))
+      return st;
+  }
+  // receivers
+  h->nrec = d->nrec;
+  if (h->nrec) {
+    h->rec_isamp = d->rec_isamp > 0 ? d->rec_isamp : 1;
+    h->rec_nsamp = d->rec_nsamp;
+    h->rec_field = d->rec_field;
+    if (h->rec_field != 'D' && h->rec_field != 'V' && h->rec_field != 'A')
+      return set_err(h, SEM2D_E_ARG, "rec_field must be D, V or A");
+    std::vector<int> lat;
+    std::vector<double> w;
+    if (d->rec_node) {
+      h->rec_npts = 1;
+      for (int r = 0; r < h->nrec; ++r) {
+        const int p = d->rec_node[r] - 1;
+        if (p < 0 || p >= d->npoin) return set_err(h, SEM2D_E_ARG, "receiver node out of range");
+        lat.push_back(int(h->glob2lat[p]));
+        w.push_back(1.0);
+      }
+    } else {
+      if (!d->rec_elem || !d->rec_interp) return set_err(h, SEM2D_E_ARG, "receivers need nodes or interpolation");
+      const int NN = h->N * h->N;
+      h->rec_npts = NN;
+      for (int r = 0; r < h->nrec; ++r) {
+        const int e = d->rec_elem[r] - 1;
+        if (e < 0 || e >= d->nelem) return set_err(h, SEM2D_E_ARG, "receiver element out of range");
+        for (int q = 0; q < NN; ++q) {
+          lat.push_back(int(h->glob2lat[d->ibool[q + (size_t)NN * e] - 1]));
+          w.push_back(d->rec_interp[q + (size_t)NN * r]);
+        }
+      }
+    }
+    if ((st = dupload(h, &h->rec_lat, lat)) || (st = dupload(h, &h->rec_w, w)) ||
+        (st = dalloc(h, &h->sis, (size_t)h->rec_nsamp * h->nrec * h->ndof)))
+      return st;
+  }
+  // tile shape
+  if ((st = choose_tiles(h->N, h->ndof, h->mixed, h->nx, h->nz, h->row0.data(), h->nmat, h->has_kv,
+                         h->mat_elem, &h->TX, &h->TZ, &h->tile_nodes)))
+    return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no tile shape fits: ") + bulk_last_error());
+  if ((st = reset_state(h))) return st;
+  CK(cudaStreamSynchronize(h->stream));
+  return SEM2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sem2d_gpu_version(void) { return SEM2D_GPU_ABI_VERSION; }
+
+int sem2d_gpu_device_count(void) {
+  int n = 0;
+  if (cudaGetDeviceCount(&n) != cudaSuccess) return SEM2D_E_CUDA;
+  return n;
+}
+
+int sem2d_gpu_create(const sem2d_problem_desc *desc, sem2d_handle **out) {
+  if (!desc || !out) {
+    g_create_err = "null argument";
+    return SEM2D_E_ARG;
+  }
+  *out = nullptr;
+  auto h = new (std::nothrow) sem2d_handle();
+  if (!h) {
+    g_create_err = "out of host memory";
+    return SEM2D_E_NOMEM;
+  }
+  int st;
+  try {
+    st = create_impl(h, desc);
+  } catch (const std::bad_alloc &) {
+    h->err = "out of host memory";
+    st = SEM2D_E_NOMEM;
+  }
+  if (st) {
+    g_create_err = h->err;
+    sem2d_gpu_destroy(h);
+    return st;
+  }
+  *out = h;
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
+  if (!h) return SEM2D_E_ARG;
+  if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
+  if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
+  int st;
+  int left = nsteps;
+  const char *nog = std::getenv("SEM2D_NO_GRAPH");
+  const bool use_graph = !(nog && nog[0] == '1');
+  // align to even parity, then replay captured runs
+  if (use_graph && left >= 2 * kGraphPairs) {
+    if (h->cur != 0) {
+      if ((st = launch_steps(h, 1))) return st;
+      --left;
+    }
+    if ((st = ensure_graph(h))) return st;
+    while (left >= 2 * kGraphPairs) {
+      CK(cudaGraphLaunch(h->graph_exec, h->stream));
+      h->steps += 2 * kGraphPairs;
+      h->launches += (long long)2 * kGraphPairs * kernels_per_step(h);
+      left -= 2 * kGraphPairs;
+    }
+  }
+  if (left && (st = launch_steps(h, left))) return st;
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_sync(sem2d_handle *h) {
+  if (!h) return SEM2D_E_ARG;
+  return check_device_error(h);
+}
+
+int sem2d_gpu_current_step(sem2d_handle *h) { return h ? h->steps : SEM2D_E_ARG; }
+
+int sem2d_gpu_reset(sem2d_handle *h) {
+  if (!h) return SEM2D_E_ARG;
+  int st = reset_state(h);
+  if (st) return st;
+  return check_device_error(h);
+}
+
+int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc, double *accel) {
+  if (!h) return SEM2D_E_ARG;
+  int st = check_device_error(h);
+  if (st) return st;
+  if (accel && !h->keep_accel) return set_err(h, SEM2D_E_STATE, "accelerations are not kept (leapfrog without field 'A')");
+  const size_t n = (size_t)h->plane * h->ndof;
+  // after n >= 1 steps: displacement d^n is the buffer not current; v and a are current
+  void *src[3] = {h->steps > 0 ? h->D[1 - h->cur] : h->D[h->cur], h->V[h->cur], h->A[h->cur]};
+  double *dst[3] = {displ, veloc, accel};
+  std::vector<double> tmp(n);
+  std::vector<float> tmpf(h->mixed ? n : 0);
+  for (int k = 0; k < 3; ++k) {
+    if (!dst[k]) continue;
+    if (h->mixed) {
+      CK(cudaMemcpy(tmpf.data(), src[k], n * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < n; ++q) tmp[q] = tmpf[q];
+    } else {
+      CK(cudaMemcpy(tmp.data(), src[k], n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    for (int c = 0; c < h->ndof; ++c)
+      for (int p = 0; p < h->npoin; ++p) dst[k][p + (size_t)h->npoin * c] = tmp[c * h->plane + h->glob2lat[p]];
+  }
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_get_seismograms(sem2d_handle *h, double *sis) {
+  if (!h || !sis) return SEM2D_E_ARG;
+  int st = check_device_error(h);
+  if (st) return st;
+  if (h->nrec)
+    CK(cudaMemcpy(sis, h->sis, sizeof(double) * (size_t)h->rec_nsamp * h->nrec * h->ndof, cudaMemcpyDeviceToHost));
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_get_fault(sem2d_handle *h, double *out) {
+  if (!h || !out) return SEM2D_E_ARG;
+  int st = check_device_error(h);
+  if (st) return st;
+  if (h->nflt && h->fnsamp > 0)
+    CK(cudaMemcpy(out, h->fd[F_SERIES], sizeof(double) * (size_t)h->onx * 6 * h->fnsamp, cudaMemcpyDeviceToHost));
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_get_fault_state(sem2d_handle *h, double *D, double *V, double *T, double *MU, double *theta) {
+  if (!h) return SEM2D_E_ARG;
+  int st = check_device_error(h);
+  if (st) return st;
+  if (!h->nflt) return SEM2D_OK;
+  const size_t nfd = (size_t)h->nflt * h->ndof;
+  if (D) CK(cudaMemcpy(D, h->fd[F_D], nfd * sizeof(double), cudaMemcpyDeviceToHost));
+  if (V) CK(cudaMemcpy(V, h->fd[F_V], nfd * sizeof(double), cudaMemcpyDeviceToHost));
+  if (T) CK(cudaMemcpy(T, h->fd[F_T], 2 * h->nflt * sizeof(double), cudaMemcpyDeviceToHost));
+  if (MU) CK(cudaMemcpy(MU, h->fd[F_MU], h->nflt * sizeof(double), cudaMemcpyDeviceToHost));
+  if (theta) CK(cudaMemcpy(theta, h->fd[F_THETA], h->nflt * sizeof(double), cudaMemcpyDeviceToHost));
+  return SEM2D_OK;
+}
+
+long long sem2d_gpu_kernel_launches(sem2d_handle *h) { return h ? h->launches : 0; }
+
+int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz) {
+  if (!h) return SEM2D_E_ARG;
+  if (tx) *tx = h->TX;
+  if (tz) *tz = h->TZ;
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_destroy(sem2d_handle *h) {
+  if (!h) return SEM2D_E_ARG;
+  if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
+  for (void *p : h->allocs) cudaFree(p);
+  if (h->stream) cudaStreamDestroy(h->stream);
+  delete h;
+  return SEM2D_OK;
+}
+
+const char *sem2d_gpu_last_error(sem2d_handle *h) { return h ? h->err.c_str() : g_create_err.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,216 @@
+"""Par.inp-shaped problem description.
+
+Each class mirrors one NAMELIST block of the reference input file
+(doc/doc.txt; the *_read routines cited below) for the Cartesian solver
+path.  ``ParDeck.to_c()`` packs the values into the ``sem2d_deck`` C struct
+of include/sem2d_host.h and keeps the numpy arrays it points to alive.
+"""
+from dataclasses import dataclass, field
+from typing import Dict, List, Optional, Sequence, Tuple, Union
+
+import ctypes as C
+import numpy as np
+
+from . import abi
+
+ArrayLike = Union[float, np.ndarray]
+
+
+def _dptr(a):
+    return a.ctypes.data_as(abi.P_double) if a is not None else abi.P_double()
+
+
+@dataclass
+class Material:
+    """&MATERIAL tag + &MAT_ELASTIC (mat_elastic.f90:69-189) [+ &MAT_KV]."""
+    tag: int = 1
+    rho: float = 0.0
+    cp: float = 0.0
+    cs: float = 0.0
+    c11: float = 0.0
+    c13: float = 0.0
+    c33: float = 0.0
+    c55: float = 0.0
+    c66: float = 0.0
+    aniso: bool = False
+    hetero: bool = False      # values taken from ParDeck.hetero arrays
+    kv_eta: Optional[float] = None
+    kv_etaxdt: bool = True
+
+
+@dataclass
+class Fault:
+    """&BC_DEF kind='DYNFLT' + &BC_DYNFLT/_SWF/_RSF/_NOR (bc_dynflt.f90:100-178)."""
+    tags: Tuple[int, int] = (5, 6)
+    friction: str = "SWF"
+    swf_kind: int = 1
+    healing: bool = False
+    rsf_kind: int = 1
+    normal_kind: int = 1
+    normal_T: float = 1.0
+    normal_L: float = 1.0
+    normal_V: float = 1.0
+    opening: bool = True
+    ot1: float = 0.0
+    otd: float = 0.0
+    oxi: Tuple[int, int, int] = (1, 0, 1)
+    # name (abi.FP_NAMES) -> scalar, or an array over the fault nodes
+    values: Dict[str, ArrayLike] = field(default_factory=dict)
+
+
+@dataclass
+class Time:
+    """&TIME (+ &TIME_NEWMARK) (time.f90:122-315)."""
+    kind: str = "leapfrog"
+    dt: float = 0.0
+    courant: float = 0.5
+    total_time: float = 0.0
+    nsteps: int = 0
+    beta: float = 0.0
+    gamma: float = 0.5
+
+
+@dataclass
+class Sources:
+    """&SRC_DEF mechanism='FORCE' stf='RICKER' + &STF_RICKER + &SRC_FORCE."""
+    coords: Sequence[Sequence[float]] = ((0.0, 0.0),)
+    f0: float = 1.0
+    onset: float = 1.0
+    ampli: float = 1.0
+    angle: float = 0.0
+    tdelay: Optional[Sequence[float]] = None
+    relamp: Optional[Sequence[float]] = None
+
+
+@dataclass
+class Receivers:
+    """&REC_LINE (receivers.f90:62-163)."""
+    number: int = 0
+    first: Tuple[float, float] = (0.0, 0.0)
+    last: Tuple[float, float] = (0.0, 0.0)
+    coords: Optional[np.ndarray] = None
+    atnode: bool = True
+    isamp: int = 1
+    field: str = "V"
+
+
+@dataclass
+class ParDeck:
+    """The blocks of one Par.inp for the Cartesian solver path."""
+    ngll: int = 5
+    ndof: int = 2
+    fmax: float = 1.0
+    xlim: Tuple[float, float] = (0.0, 1.0)
+    zlim: Tuple[float, float] = (0.0, 1.0)
+    nelem: Tuple[int, int] = (1, 1)
+    ezflt: int = 0
+    fztag: int = 0
+    fznz: int = 1
+    domains: List[Tuple[int, Tuple[int, int], Tuple[int, int]]] = field(default_factory=list)
+    materials: List[Material] = field(default_factory=list)
+    absorbing: List[int] = field(default_factory=list)   # tags with kind='ABSORB'
+    fault: Optional[Fault] = None
+    fault_first: bool = False  # &BC_DEF order: DYNFLT block before the ABSORB blocks
+    time: Time = field(default_factory=Time)
+    sources: Optional[Sources] = None
+    receivers: Optional[Receivers] = None
+    precision: int = abi.PRECISION_FP64
+    kd2_form: int = -1
+    # per element GLL point arrays (ngll,ngll,nelem) for hetero materials
+    hetero: Dict[str, np.ndarray] = field(default_factory=dict)
+
+    def to_c(self):
+        """Return (abi.Deck, keepalive) for the C builders."""
+        keep = []
+        d = abi.Deck()
+        d.ngll, d.ndof, d.fmax = self.ngll, self.ndof, float(self.fmax)
+        d.xlim[:] = [float(v) for v in self.xlim]
+        d.zlim[:] = [float(v) for v in self.zlim]
+        d.nelem[:] = [int(v) for v in self.nelem]
+        d.ezflt, d.fztag, d.fznz = self.ezflt, self.fztag, self.fznz
+        if len(self.domains) > abi.MAX_DOMAINS or len(self.materials) > abi.MAX_MATS:
+            raise ValueError("too many domains or materials")
+        d.ndomains = len(self.domains)
+        for k, (tag, ex, ez) in enumerate(self.domains):
+            d.domains[k].tag = tag
+            d.domains[k].ex[:] = list(ex)
+            d.domains[k].ez[:] = list(ez)
+        d.nmats = len(self.materials)
+        for k, m in enumerate(self.materials):
+            cm = d.mats[k]
+            cm.tag, cm.aniso, cm.hetero = m.tag, int(m.aniso), int(m.hetero)
+            cm.rho, cm.cp, cm.cs = m.rho, m.cp, m.cs
+            cm.c11, cm.c13, cm.c33, cm.c55, cm.c66 = m.c11, m.c13, m.c33, m.c55, m.c66
+            cm.kv = int(m.kv_eta is not None)
+            cm.kv_eta = float(m.kv_eta or 0.0)
+            cm.kv_etaxdt = int(m.kv_etaxdt)
+        for name in ("rho", "cp", "cs", "c11", "c13", "c33", "c55", "c66", "kveta"):
+            arr = self.hetero.get(name)
+            if arr is not None:
+                arr = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).ravel(order="F"))
+                keep.append(arr)
+            setattr(d, "h_" + name, _dptr(arr))
+        bcs = []
+        if self.fault is not None and self.fault_first:
+            bcs.append((abi.BC_DYNFLT, self.fault.tags))
+        bcs += [(abi.BC_ABSORB, (t, 0)) for t in self.absorbing]
+        if self.fault is not None and not self.fault_first:
+            bcs.append((abi.BC_DYNFLT, self.fault.tags))
+        if len(bcs) > abi.MAX_BCS:
+            raise ValueError("too many boundary conditions")
+        d.nbcs = len(bcs)
+        for k, (kind, tags) in enumerate(bcs):
+            d.bcs[k].kind = kind
+            d.bcs[k].tag[:] = [int(tags[0]), int(tags[1])]
+        f = self.fault
+        for i, name in enumerate(abi.FP_NAMES):
+            d.flt_value[i] = abi.FP_DEFAULTS[name]
+            d.flt_array[i] = abi.P_double()
+        if f is not None:
+            d.flt_friction = abi.FRICTION_RSF if f.friction.upper() == "RSF" else abi.FRICTION_SWF
+            d.swf_kind, d.swf_healing, d.rsf_kind = f.swf_kind, int(f.healing), f.rsf_kind
+            d.normal_kind = f.normal_kind
+            d.normal_T, d.normal_L, d.normal_V = f.normal_T, f.normal_L, f.normal_V
+            d.flt_opening = int(f.opening)
+            d.flt_ot1, d.flt_otd = f.ot1, f.otd
+            d.flt_oxi[:] = list(f.oxi)
+            for name, val in f.values.items():
+                i = abi.FP_INDEX[name]
+                if np.isscalar(val):
+                    d.flt_value[i] = float(val)
+                else:
+                    arr = np.ascontiguousarray(np.asarray(val, dtype=np.float64))
+                    keep.append(arr)
+                    d.flt_array[i] = _dptr(arr)
+        t = self.time
+        d.time_kind = abi.TIME_NEWMARK if t.kind.lower() == "newmark" else abi.TIME_LEAPFROG
+        d.dt, d.courant, d.total_time, d.nsteps = t.dt, t.courant, t.total_time, t.nsteps
+        d.beta, d.gamma = t.beta, t.gamma
+        s = self.sources
+        if s is not None:
+            xy = np.ascontiguousarray(np.asarray(s.coords, dtype=np.float64).reshape(-1, 2))
+            keep.append(xy)
+            d.nsrc = xy.shape[0]
+            d.src_coord = _dptr(xy)
+            for attr, val in (("src_tdelay", s.tdelay), ("src_ampli", s.relamp)):
+                if val is not None:
+                    arr = np.ascontiguousarray(np.asarray(val, dtype=np.float64))
+                    keep.append(arr)
+                    setattr(d, attr, _dptr(arr))
+            d.ricker_f0, d.ricker_onset, d.ricker_ampli = s.f0, s.onset, s.ampli
+            d.force_angle = s.angle
+        r = self.receivers
+        if r is not None:
+            if r.coords is not None:
+                rc = np.ascontiguousarray(np.asarray(r.coords, dtype=np.float64).reshape(-1, 2))
+                keep.append(rc)
+                d.rec_number = rc.shape[0]
+                d.rec_coord = _dptr(rc)
+            else:
+                d.rec_number = r.number
+            d.rec_first[:] = list(r.first)
+            d.rec_last[:] = list(r.last)
+            d.rec_atnode, d.rec_isamp = int(r.atnode), r.isamp
+            d.rec_field = r.field.encode()[:1]
+        d.precision, d.kd2_form = self.precision, self.kd2_form
+        return d, keep

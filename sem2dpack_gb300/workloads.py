@@ -1,0 +1,107 @@
+"""Synthetic workloads: the benchmark configurations as Par.inp-shaped decks.
+
+All inputs are seeded (numpy PCG64, base seed 20261203 + configuration
+index); no external data set is involved.
+
+  plain_psv        P-SV elastic, 100 x 100 elements of 100 m, NGLL=5,
+                   rho 2700, vp 5000, vs 2887, vertical Ricker force
+                   (f0 = 10 Hz) at the centre, absorbing on all sides, CFL 0.5,
+                   2000 steps, 16 receivers on a seeded random line.
+  sh_rupture       SH dynamic rupture, 400 x 200 elements of 100 m, NGLL=5,
+                   rho 2670, vs 3464; split-node fault at mid depth along
+                   300 elements (friction 1e4 outside), linear slip weakening
+                   mu_s 0.68, mu_d 0.52, Dc 0.4 m, normal stress -120 MPa,
+                   shear stress 70 MPa plus Gaussian-correlated noise
+                   (correlation 500 m, max 2 MPa), 3 km nucleation patch at
+                   81 MPa, absorbing on all sides, 6000 steps.
+  psv_rsf          P-SV rate-and-state rupture in a random medium (aging law).
+Each builder takes ``scale`` to shrink the mesh (and steps) for tests.
+"""
+import numpy as np
+
+from . import abi
+from .api import Grid, Problem
+from .deck import Fault, Material, ParDeck, Receivers, Sources, Time
+
+BASE_SEED = 20261203
+
+
+def _rng(config_index):
+    return np.random.default_rng(BASE_SEED + config_index)
+
+
+def plain_psv(scale=1.0, nsteps=2000, precision=abi.PRECISION_FP64, nrec=16):
+    """Plain P-SV elastic box (the reference's CPU-runnable case)."""
+    n = max(2, int(round(100 * scale)))
+    L = 100.0 * n
+    rng = _rng(0)
+    first = rng.uniform(0.1 * L, 0.9 * L, size=2)
+    last = rng.uniform(0.1 * L, 0.9 * L, size=2)
+    return ParDeck(
+        ngll=5, ndof=2, fmax=25.0, xlim=(0.0, L), zlim=(0.0, L), nelem=(n, n),
+        materials=[Material(tag=1, rho=2700.0, cp=5000.0, cs=2887.0)],
+        absorbing=[1, 2, 3, 4],
+        time=Time(kind="leapfrog", courant=0.5, nsteps=nsteps),
+        sources=Sources(coords=[(0.5 * L, 0.5 * L)], f0=10.0, onset=0.12, ampli=1.0, angle=0.0),
+        receivers=Receivers(number=nrec, first=tuple(first), last=tuple(last), field="V"),
+        precision=precision,
+    )
+
+
+def _correlated_noise(rng, x, corr, amp, dx=25.0):
+    """Gaussian-filtered white noise sampled at x, scaled to max |.| = amp."""
+    x0, x1 = float(np.min(x)) - 4 * corr, float(np.max(x)) + 4 * corr
+    xs = np.arange(x0, x1 + dx, dx)
+    white = rng.standard_normal(xs.size)
+    k = np.arange(-int(4 * corr / dx), int(4 * corr / dx) + 1) * dx
+    kern = np.exp(-0.5 * (k / corr) ** 2)
+    smooth = np.convolve(white, kern / kern.sum(), mode="same")
+    vals = np.interp(x, xs, smooth)
+    return vals * (amp / np.max(np.abs(vals)))
+
+
+def sh_rupture(scale=1.0, nsteps=6000, precision=abi.PRECISION_MIXED, out_every=10):
+    """SH antiplane rupture on a split-node fault with slip weakening.
+
+    The nucleation patch (81 MPa) must exceed the static strength to start
+    the rupture; with mu_s = 0.68 (81.6 MPa under 120 MPa) it would not, so
+    mu_s is 0.67 (80.4 MPa) inside the patch.
+    """
+    nx, nz = max(4, int(round(400 * scale))), max(4, int(round(200 * scale)))
+    h = 100.0
+    Lx, Lz = nx * h, nz * h
+    half = 0.5 * min(300 * h * scale if scale < 1 else 300 * h, 0.9 * Lx)
+    patch = 1500.0 * min(1.0, scale * 4) if scale < 1 else 1500.0
+    deck = ParDeck(
+        ngll=5, ndof=1, fmax=10.0, xlim=(0.0, Lx), zlim=(0.0, Lz), nelem=(nx, nz), ezflt=-1,
+        materials=[Material(tag=1, rho=2670.0, cp=6000.0, cs=3464.0)],
+        absorbing=[1, 2, 3, 4],
+        fault=Fault(tags=(5, 6), friction="SWF", swf_kind=1, normal_kind=1, opening=True),
+        time=Time(kind="leapfrog", courant=0.5, nsteps=nsteps),
+        receivers=Receivers(number=16, first=(0.1 * Lx, 0.5 * Lz + 2000.0 * min(scale * 4, 1.0)),
+                            last=(0.9 * Lx, 0.5 * Lz + 2000.0 * min(scale * 4, 1.0)), field="V"),
+        precision=precision,
+    )
+    grid = Grid(deck)
+    n1, _ = grid.fault_nodes()
+    x = grid.coord()[0, n1 - 1]
+    xc = 0.5 * Lx
+    rng = _rng(1)
+    tt = 70.0e6 + _correlated_noise(rng, x, 500.0, 2.0e6)
+    inpatch = np.abs(x - xc) <= patch
+    tt[inpatch] = 81.0e6
+    mus = np.where(np.abs(x - xc) <= half, 0.68, 1.0e4)
+    mus[inpatch] = 0.67
+    deck.fault.values = {"Tn": -120.0e6, "Tt": tt, "swf_mus": mus, "swf_mud": 0.52, "swf_dc": 0.4}
+    # output every out_every steps, every node
+    dt_est = 0.5 * (h * (1.0 - np.sqrt(3.0 / 7.0)) / 2.0) / 3464.0
+    deck.fault.otd = out_every * dt_est
+    return deck, grid
+
+
+def build(deck_or_pair):
+    """Problem for a deck (or a (deck, grid) pair from a builder)."""
+    if isinstance(deck_or_pair, tuple):
+        deck, grid = deck_or_pair
+        return Problem(deck, grid)
+    return Problem(deck_or_pair)

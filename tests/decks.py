@@ -1,0 +1,66 @@
+"""Input decks of the reference's own examples, restated as ParDeck objects.
+
+Each function cites the Par.inp it restates (EXAMPLES/<name>/Par.inp of the
+reference).  Used by the tests only.
+"""
+import os
+import sys
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+
+from sem2dpack_gb300.deck import (Fault, Material, ParDeck, Receivers,  # noqa: E402
+                                  Sources, Time)
+
+
+def lambs_problem():
+    """EXAMPLES/LambsProblem/Par.inp:1-44.  The &TIME namelist ends at the
+    first '/', so kind stays at its default 'leapfrog' (time.f90:138)."""
+    return ParDeck(
+        ngll=9, ndof=2, fmax=25.0, xlim=(0.0, 4.0e3), zlim=(-2.0e3, 0.0), nelem=(40, 20),
+        materials=[Material(tag=1, rho=2000.0, cp=3200.0, cs=1847.5)],
+        absorbing=[1, 2, 4],
+        time=Time(kind="leapfrog", total_time=1.5, dt=0.5e-3, courant=0.5),
+        sources=Sources(coords=[(1500.0, -50.0)], f0=10.0, onset=0.15, ampli=1.0, angle=0.0),
+        receivers=Receivers(number=2, first=(2200.0, 0.0), last=(2700.0, 0.0), field="D"),
+    )
+
+
+def test_sh():
+    """EXAMPLES/TestSH/Par.inp:1-33."""
+    return ParDeck(
+        ngll=6, ndof=1, fmax=1.25, xlim=(0.0, 30.0), zlim=(0.0, 30.0), nelem=(60, 60),
+        materials=[Material(tag=1, rho=1.0, cp=1.7321, cs=1.0)],
+        absorbing=[2, 3],
+        time=Time(kind="leapfrog", total_time=35.0, courant=0.3),
+        sources=Sources(coords=[(0.0, 0.0)], f0=0.5, onset=3.0, ampli=0.25, angle=0.0),
+        receivers=Receivers(number=7, first=(0.0, 0.0), last=(30.0, 0.0), field="D", isamp=1),
+    )
+
+
+def anisotropic():
+    """EXAMPLES/Anisotropic/Par.inp (Komatitsch, Barnes and Tromp 2000 fig. 7)."""
+    return ParDeck(
+        ngll=6, ndof=2, fmax=400.0e3, xlim=(-0.325, 0.325), zlim=(-0.325, 0.325),
+        nelem=(130, 130),
+        domains=[(1, (1, 65), (1, 130)), (2, (66, 130), (1, 130))],
+        materials=[Material(tag=1, aniso=True, rho=7100.0, c11=16.5e10, c13=5.0e10,
+                            c33=6.2e10, c55=3.96e10),
+                   Material(tag=2, rho=7100.0, cp=4820.729884542206, cs=2361.665680982894)],
+        absorbing=[],
+        time=Time(kind="leapfrog", total_time=1.0e-4, dt=5.0e-8),
+        sources=Sources(coords=[(-0.02, 0.0)], f0=170.0e3, onset=6.0e-6, ampli=1.0e13,
+                        angle=180.0),
+        receivers=Receivers(number=49, first=(-12.0e-2, -8.0e-2), last=(12.0e-2, -8.0e-2),
+                            field="D", isamp=1),
+    )
+
+
+def inabox():
+    """EXAMPLES/InaBox/Par.inp:1-60 (example 1, homogeneous box)."""
+    return ParDeck(
+        ngll=5, ndof=2, fmax=25.0, xlim=(-1.0e3, 1.0e3), zlim=(-1.0e3, 1.0e3), nelem=(40, 40),
+        materials=[Material(tag=1, rho=2400.0, cp=3800.0, cs=2000.0)],
+        absorbing=[1, 2, 3, 4],
+        time=Time(kind="newmark", total_time=2.0, courant=0.3, beta=0.0, gamma=0.5),
+        sources=Sources(coords=[(0.0, 0.0)], f0=1.0, onset=1.0, ampli=1.0),
+    )

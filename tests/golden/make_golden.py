@@ -1,0 +1,59 @@
+"""Generate the golden fixtures in this folder from SEM2DPACK's examples.
+
+Run in a container where the reference checkout is available:
+
+    python tests/golden/make_golden.py /path/to/sem2dpack
+
+It reads the reference's own test data (nothing is written from memory):
+  EXAMPLES/LambsProblem/{Ux,Uz}_file_ascii   analytic traces (EX2DDIR),
+                                              pass threshold 0.005
+                                              (LambsProblem/analyze_test.m:21-22)
+  EXAMPLES/LambsProblem/test.out             recorded misfits of the reference
+  EXAMPLES/TestSH/uyref.mat                   analytic SH trace (SEMLAB),
+                                              threshold 0.02 (TestSH/analyze_test.m:14-15)
+  EXAMPLES/Anisotropic/p{1..4}.tab            reference output at stations
+                                              4, 18, 23, 46 (Anisotropic/write_seis.m)
+  EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
+and writes golden.npz.  The GPU machine and the test suite only read the npz.
+"""
+import os
+import re
+import sys
+
+import numpy as np
+
+
+def main(ref):
+    ex = os.path.join(ref, "EXAMPLES")
+    out = {}
+    lamb = os.path.join(ex, "LambsProblem")
+    out["lamb_ux"] = np.loadtxt(os.path.join(lamb, "Ux_file_ascii"))
+    out["lamb_uz"] = np.loadtxt(os.path.join(lamb, "Uz_file_ascii"))
+    txt = open(os.path.join(lamb, "test.out")).read()
+    m = re.search(r"misfit ux1 ux2 uz1 uz2 = ([0-9.eE+\- ]+)", txt)
+    out["lamb_recorded_misfit"] = np.array([float(v) for v in m.group(1).split()])
+
+    from scipy.io import loadmat
+    sh = loadmat(os.path.join(ex, "TestSH", "uyref.mat"))
+    out["sh_tref"] = np.asarray(sh["tref"], dtype=np.float64).ravel()
+    out["sh_uref"] = np.asarray(sh["uref"], dtype=np.float64).ravel()
+
+    for k in range(1, 5):
+        out["aniso_p%d" % k] = np.loadtxt(os.path.join(ex, "Anisotropic", "p%d.tab" % k))
+    out["aniso_stations"] = np.array([4, 18, 23, 46])
+
+    info = open(os.path.join(ex, "InaBox", "info")).read()
+    out["inabox_npoin"] = np.array(int(re.search(r"Total number of GLL points[ .]*= *(\d+)", info).group(1)))
+    out["inabox_nelem"] = np.array(int(re.search(r"Total number of elements[ .]*= *(\d+)", info).group(1)))
+    out["inabox_dt"] = np.array(float(re.search(r"Time step \(secs\) *= *([0-9.E+\-]+)", info).group(1)))
+    out["inabox_nt"] = np.array(int(re.search(r"Number of time steps *= *(\d+)", info).group(1)))
+
+    dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
+    np.savez_compressed(dst, **out)
+    for k, v in out.items():
+        print(k, np.shape(v))
+    print("wrote", dst)
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")

@@ -1,0 +1,120 @@
+"""Product host builder (C++) against the oracle's restated init_main.
+
+Integer data (ibool, boundary tables, node pairs) must be bit-exact; the
+floating-point arrays of the descriptor are compared bit-exactly too, since
+both follow the reference's operation order in FP64 without contraction.
+"""
+import numpy as np
+import pytest
+
+import decks
+from oracle import pyoracle as po
+from sem2dpack_gb300 import Grid, Problem, workloads
+
+INT_FIELDS = ["ibool", "abs_node", "src_node", "rec_node", "rec_elem", "flt_node1", "flt_node2"]
+
+
+def _arr(d, name, n):
+    p = getattr(d, name)
+    if not p:
+        return None
+    return np.ctypeslib.as_array(p, shape=(n,)).copy()
+
+
+def _sizes(d):
+    n2, ne, npn, nd = d.ngll * d.ngll, d.nelem, d.npoin, d.ndof
+    return {"ibool": n2 * ne, "coord": 2 * npn, "hprime": n2, "wgll": d.ngll, "Kx": n2 * ne,
+            "Kz": n2 * ne, "la": n2 * ne, "mu": n2 * ne, "mux": n2 * ne, "rmass": npn * nd,
+            "abs_node": d.nabs, "abs_C": d.nabs * nd, "src_node": d.nsrc, "src_dir": 2 * d.nsrc,
+            "src_f0": d.nsrc, "src_t0": d.nsrc, "src_ampli": d.nsrc, "src_relamp": d.nsrc,
+            "rec_node": d.nrec, "rec_elem": d.nrec, "rec_interp": n2 * d.nrec,
+            "flt_node1": d.nflt, "flt_node2": d.nflt, "flt_n1": 2 * d.nflt, "flt_B": d.nflt,
+            "flt_invM1": d.nflt * nd, "flt_invM2": d.nflt * nd, "flt_Z": d.nflt * nd,
+            "flt_T0": 2 * d.nflt, "flt_cohesion": d.nflt, "swf_dc": d.nflt, "swf_mus": d.nflt,
+            "swf_mud": d.nflt, "rsf_a": d.nflt, "rsf_b": d.nflt, "rsf_theta": d.nflt,
+            "flt_V0": d.nflt}
+
+
+def assert_same_desc(a, b):
+    for attr in ("ngll", "ndof", "nelem", "npoin", "nabs", "nt", "nsrc", "nrec", "rec_nsamp",
+                 "rec_isamp", "nflt", "flt_nsamp", "flt_oit", "flt_oitd", "flt_oix1", "flt_oixn",
+                 "kd2_form", "time_scheme"):
+        assert getattr(a, attr) == getattr(b, attr), attr
+    assert a.dt == b.dt and a.flt_coefA2V == b.flt_coefA2V
+    for name, n in _sizes(a).items():
+        x, y = _arr(a, name, n), _arr(b, name, n)
+        assert (x is None) == (y is None), name
+        if x is not None:
+            assert np.array_equal(x, y), name
+
+
+@pytest.mark.parametrize("name", ["lambs_problem", "test_sh", "inabox", "anisotropic"])
+def test_grid_bit_exact(name):
+    dk = getattr(decks, name)()
+    g, o = Grid(dk), po.OracleSetup(dk, grid_only=True)
+    assert (g.nelem, g.npoin) == (o.nelem, o.npoin)
+    assert np.array_equal(g.ibool(), o.ibool())
+    assert np.array_equal(g.coord(), o.coord())
+    assert np.array_equal(g.tags(), o.tags())
+    for t in (1, 2, 3, 4):
+        assert np.array_equal(g.boundary(t), o.boundary(t))
+
+
+@pytest.mark.parametrize("name", ["lambs_problem", "test_sh", "inabox"])
+def test_problem_bit_exact(name):
+    dk = getattr(decks, name)()
+    P, O = Problem(dk), po.OracleSetup(dk)
+    assert_same_desc(P.desc(), O.desc())
+
+
+def test_fault_problem_bit_exact():
+    dk, g = workloads.sh_rupture(scale=0.1, nsteps=200)
+    P = Problem(dk, g)
+    O = po.OracleSetup(dk)
+    assert_same_desc(P.desc(), O.desc())
+    # split rows: every fault node pair is distinct and sorted along x
+    d = P.desc()
+    n1 = _arr(d, "flt_node1", d.nflt)
+    n2 = _arr(d, "flt_node2", d.nflt)
+    assert np.all(n1 != n2)
+    x = g.coord()[0, n1 - 1]
+    assert np.all(np.diff(x) > 0)
+
+
+def test_fault_before_absorbing_order():
+    """&BC_DEF order decides whether the fault snapshots the mass before or
+    after the absorbing fold (bc_gen.f90:229-246)."""
+    dk, g = workloads.sh_rupture(scale=0.1, nsteps=50)
+    Pa = Problem(dk, g)
+    a = Pa.desc()
+    dk.fault_first = True
+    Pb = Problem(dk, g)
+    b = Pb.desc()
+    inv_a, inv_b = _arr(a, "flt_invM1", a.nflt), _arr(b, "flt_invM1", b.nflt)
+    # the end nodes lie on the absorbing sides: only they differ
+    diff = np.nonzero(inv_a != inv_b)[0]
+    assert set(diff.tolist()) == {0, a.nflt - 1}
+    O = po.OracleSetup(dk)
+    assert_same_desc(b, O.desc())
+
+
+@pytest.mark.parametrize("atnode", [True, False])
+def test_receivers(atnode):
+    dk = workloads.plain_psv(scale=0.1, nsteps=10, nrec=5)
+    dk.receivers.atnode = atnode
+    P, O = Problem(dk), po.OracleSetup(dk)
+    assert_same_desc(P.desc(), O.desc())
+    np.testing.assert_array_equal(P.rec_coord(), O.rec_coord())
+
+
+def test_reference_warnings_abort():
+    """Warnings abort by default in the reference (stdio.f90:13,218-227)."""
+    from sem2dpack_gb300 import Sem2dError
+    dk = workloads.plain_psv(scale=0.1, nsteps=10)
+    dk.fmax = 1000.0  # resolution warning (init.f90:271-281)
+    with pytest.raises(Sem2dError):
+        Problem(dk)
+    dk = workloads.plain_psv(scale=0.1, nsteps=10)
+    dk.sources.onset = 0.05  # onset < 1/f0 (stf_ricker.f90:63-68)
+    with pytest.raises(Sem2dError):
+        Problem(dk)
