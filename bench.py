@@ -1,0 +1,336 @@
+"""Benchmark of the GB300 spectral-element time step.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload sh_rupture|plain_psv|psv_rsf]
+
+A benchmark step is one complete solve of the workload (all its time steps,
+fields reset and L2 flushed before it).  The default workload is the SH
+dynamic rupture (400 x 200 elements, NGLL=5, 6000 steps, FP32 fields with
+FP64 fault state).  The metric is GLL node-steps per second.
+
+Reported on one JSON line (rank 0):
+  value      node-steps/s of the solves, device-timed with CUDA events on the
+             solver's own stream, inputs resident on the device
+  e2e        the same metric through the C-ABI from host arrays: create
+             (host->device copies), all steps, seismograms and fault series
+             back to the host, destroy
+  roofline   the bulk kernel: algorithmic bytes per launch / average launch
+             duration (CUDA events around every launch, a second pass)
+  cpu_baseline  the FP64 oracle (CPU port of the reference path, 1 thread)
+             on a bounded sample of the same workload
+
+--impl reference times the CPU restatement of the reference path (the
+reference itself is Fortran and cannot be built here) on the same workload.
+Under torchrun every rank runs its own replica (no data exchange); rank 0
+prints the line and `value` is the sum over ranks of work / the slowest rank.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BYTES_PER_NODE_STEP = {  # algorithmic bytes per GLL node-step
+    # read+write displacement and velocity (ndof words each), read inverse
+    # mass (1 word), read the elastic moduli (SH: mu; P-SV: lambda, mu)
+    (1, "f32"): 4 * (2 + 2 + 1 + 1),
+    (2, "f32"): 4 * (4 + 4 + 1 + 2),
+    (1, "f64"): 8 * (2 + 2 + 1 + 1),
+    (2, "f64"): 8 * (4 + 4 + 1 + 2),
+}
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--workload", default="sh_rupture", choices=["sh_rupture", "plain_psv", "psv_rsf"])
+    p.add_argument("--scale", type=float, default=1.0)
+    p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    p.add_argument("--cpu-seconds", type=float, default=15.0)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def make_workload(args):
+    from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, workloads
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    if args.workload == "sh_rupture":
+        pair = workloads.sh_rupture(scale=args.scale, precision=prec)
+        name = "SH antiplane rupture, SWF, 400x200 elements of 100 m, NGLL=5, 6000 steps"
+    elif args.workload == "psv_rsf":
+        pair = workloads.psv_rsf(scale=args.scale, precision=prec)
+        name = "P-SV rate-and-state rupture (aging), von Karman medium, 1024x512 elements, NGLL=5"
+    else:
+        pair = workloads.plain_psv(scale=args.scale, precision=prec)
+        name = "plain P-SV elastic, 100x100 elements of 100 m, NGLL=5, 2000 steps"
+    if args.scale != 1.0:
+        name += " (scale %.3g)" % args.scale
+    return workloads.build(pair), name
+
+
+def desc_bytes(d):
+    """Bytes of every host array the descriptor hands to sem2d_gpu_create."""
+    n2, ne, npn, nd, nf = d.ngll * d.ngll, d.nelem, d.npoin, d.ndof, d.nflt
+    sizes = {"ibool": 4 * n2 * ne, "coord": 16 * npn, "hprime": 8 * n2, "wgll": 8 * d.ngll,
+             "rmass": 8 * npn * nd, "abs_node": 4 * d.nabs, "abs_C": 8 * d.nabs * nd,
+             "src_node": 4 * d.nsrc, "src_dir": 16 * d.nsrc, "rec_node": 4 * d.nrec}
+    for f in ("Kx", "Kz", "la", "mu", "mux"):
+        sizes[f] = 8 * n2 * ne
+    if nf:
+        sizes["fault"] = 8 * nf * (2 + 2 + 1 + 3 * nd + 2 + 1 + 5) + 8 * nf
+    return sum(sizes.values())
+
+
+class ClockSampler:
+    """nvidia-smi clock and throttle-reason samples during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % index)
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    for path in (os.path.join(ROOT, "MEASURED_PEAKS.json"),):
+        if os.path.exists(path):
+            with open(path) as f:
+                return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def ncu_traffic(workload):
+    """DRAM bytes per bulk-kernel launch from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "bulk_kernel_%s.txt" % workload)
+    if not os.path.exists(path):
+        return None
+    for line in open(path):
+        if line.startswith("dram_bytes_per_launch:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+def cpu_baseline(desc, owner, npoin, seconds):
+    """FP64 oracle (single thread) on a bounded sample of the workload."""
+    from oracle import pyoracle as po
+    sim = po.OracleSim(desc, owner=owner)
+    t0 = time.perf_counter()
+    sim.run(2)
+    rate = 2 / max(time.perf_counter() - t0, 1e-9)
+    n = max(2, min(int(rate * seconds), desc.nt - 2))
+    t0 = time.perf_counter()
+    sim.run(n)
+    dt = time.perf_counter() - t0
+    return npoin * n / dt, n
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    from oracle import pyoracle as po
+    prob, name = make_workload(args)
+    d = prob.desc()
+    d.precision = 0
+    sim = po.OracleSim(d, owner=prob)
+    t0 = time.perf_counter()
+    sim.run(2)
+    rate = 2 / max(time.perf_counter() - t0, 1e-9)
+    # one benchmark step = a bounded sample of the workload's time steps
+    per = max(1, min(int(rate * 2.0), (d.nt - 2) // max(1, args.steps + args.warmup)))
+    for _ in range(args.warmup):
+        sim.run(per)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        sim.run(per)
+    el = time.perf_counter() - t0
+    value = d.npoin * per * args.steps / el
+    sample = "%d time steps per benchmark step of %s (%d GLL nodes), FP64, 1 thread" % (per, name, d.npoin)
+    print(json.dumps({
+        "impl": "reference", "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000 * el / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": name, "global_batch": 1, "seq_len": 0, "parallelism": "replicas",
+                   "reference_build": "CPU restatement (oracle); the Fortran reference needs a Fortran compiler"},
+        "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": 1, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    import torch
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    from sem2dpack_gb300 import Solver
+    prob, name = make_workload(args)
+    desc = prob.desc()
+    npoin, nt, ndof = desc.npoin, desc.nt, desc.ndof
+    dtype = "f32" if desc.precision == 1 else "f64"
+    sim = Solver(desc, owner=prob)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > L2 (129 MB)
+
+    def one_solve(timed):
+        sim.reset()
+        flush.fill_(1.0)
+        barrier()
+        if not timed:
+            sim.step(nt)
+            sim.sync()
+            return 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(nt)
+        e1.record(stream)
+        e1.synchronize()
+        sim.sync()
+        return e0.elapsed_time(e1)
+
+    for _ in range(args.warmup):
+        one_solve(False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = sim.launches
+    ms = [one_solve(True) for _ in range(args.steps)]
+    launches = sim.launches - l0
+    clk = clocks.stop()
+    total = sum(ms)
+    if dist is not None:
+        t = torch.tensor([total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = world * npoin * nt * args.steps / (total / 1000.0)
+
+    # per-kernel durations (events around every launch) for the roofline
+    sim.reset()
+    kms = sim.step_timed(nt)
+    bulk_ms = kms[0] / nt
+    bpn = BYTES_PER_NODE_STEP[(ndof, dtype)]
+    achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
+    peaks, peak_kind = measured_peaks()
+    traffic = ncu_traffic(args.workload)
+
+    # end to end through the C-ABI from host buffers
+    sim.close()
+    del stream
+    h2d = desc_bytes(desc)
+    nflt_onx = (desc.flt_oixn - desc.flt_oix1) // max(desc.flt_oixd, 1) + 1 if desc.nflt else 0
+    d2h = 8 * desc.rec_nsamp * desc.nrec * ndof + 8 * nflt_onx * 6 * desc.flt_nsamp
+    e2e_times = []
+    for _ in range(2):
+        barrier()
+        t0 = time.perf_counter()
+        s2 = Solver(desc, owner=prob)
+        s2.step(nt)
+        s2.seismograms()
+        if desc.nflt:
+            s2.fault_series()
+        s2.close()
+        e2e_times.append(time.perf_counter() - t0)
+    e2e_value = world * npoin * nt / min(e2e_times)
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, n = cpu_baseline(desc, prob, npoin, args.cpu_seconds)
+        base = {"value": v, "unit": "node-steps/s", "cores": 1, "kind": "port",
+                "sample": "%d of %d time steps of the same workload in FP64 on 1 host thread" % (n, nt)}
+
+    if rank == 0:
+        line = {
+            "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic",
+            "config": {"workload": name, "global_batch": 1, "seq_len": 0, "parallelism": "replicas",
+                       "npoin": npoin, "time_steps_per_step": nt,
+                       "precision": "FP32 fields, FP64 fault state" if dtype == "f32" else "FP64",
+                       "l2": "512 MB buffer written before every timed solve; the solve's working set "
+                             "then stays L2-resident across its time steps"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
+                         "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "bulk_step_kernel", "bytes_per_node_step": bpn,
+                         "bulk_ms_per_launch": bulk_ms, "fault_ms_per_launch": kms[1] / nt,
+                         "receiver_ms_per_launch": kms[2] / nt},
+            "cpu_baseline": base,
+            "e2e": {"value": e2e_value, "unit": "node-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "clocks": clk,
+            "gpu_launches": launches,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

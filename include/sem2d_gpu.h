@@ -165,6 +165,17 @@ int sem2d_gpu_create(const sem2d_problem_desc *desc, sem2d_handle **out);
  * synchronises (get_* / sync / destroy). */
 int sem2d_gpu_step(sem2d_handle *h, int nsteps);
 
+/* Measurement variant of sem2d_gpu_step: runs nsteps steps with direct
+ * launches and a CUDA event pair around each kernel on the handle's
+ * stream, waits, and stores the summed kernel durations in milliseconds:
+ * ms[0] bulk kernel, ms[1] fault kernel (or step-counter kernel), ms[2]
+ * receiver kernel.  Results are identical to sem2d_gpu_step. */
+int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms);
+
+/* The CUDA stream (a cudaStream_t) the handle launches on, so that a
+ * caller can order its own work after the steps or record events on it. */
+void *sem2d_gpu_stream(sem2d_handle *h);
+
 /* Waits for all queued steps; returns device-side error status. */
 int sem2d_gpu_sync(sem2d_handle *h);
 

@@ -19,6 +19,8 @@ PROTOTYPES = [
     ("sem2d_gpu_device_count", C.c_int, []),
     ("sem2d_gpu_create", C.c_int, [C.POINTER(abi.ProblemDesc), PP]),
     ("sem2d_gpu_step", C.c_int, [vp, C.c_int]),
+    ("sem2d_gpu_step_timed", C.c_int, [vp, C.c_int, dp]),
+    ("sem2d_gpu_stream", C.c_void_p, [vp]),
     ("sem2d_gpu_sync", C.c_int, [vp]),
     ("sem2d_gpu_current_step", C.c_int, [vp]),
     ("sem2d_gpu_get_fields", C.c_int, [vp, dp, dp, dp]),

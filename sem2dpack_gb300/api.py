@@ -163,6 +163,13 @@ class Solver:
     def step(self, nsteps):
         self._check(lib().sem2d_gpu_step(self.h, int(nsteps)))
 
+    def step_timed(self, nsteps):
+        """Like step(), with per-kernel CUDA-event timing; returns the summed
+        milliseconds of (bulk, fault/counter, receiver) kernels."""
+        ms = np.zeros(3)
+        self._check(lib().sem2d_gpu_step_timed(self.h, int(nsteps), _p(ms)))
+        return ms
+
     def run(self):
         """All remaining steps up to nt."""
         self.step(self.desc.nt - self.current_step)
@@ -172,6 +179,11 @@ class Solver:
 
     def reset(self):
         self._check(lib().sem2d_gpu_reset(self.h))
+
+    @property
+    def stream(self):
+        """The cudaStream_t (as an int) the solver launches on."""
+        return lib().sem2d_gpu_stream(self.h)
 
     @property
     def current_step(self):

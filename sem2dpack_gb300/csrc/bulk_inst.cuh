@@ -11,6 +11,18 @@ namespace sem2d {
 extern thread_local std::string g_bulk_err;
 
 template <typename real, int N, int NDOF>
+int configure_typed(const BulkConfig &c) {
+  const size_t smem = bulk_smem_bytes<real, N, NDOF>(c.tile_nodes, c.nmat, c.has_kv, c.mat_elem);
+  cudaError_t e = cudaFuncSetAttribute(bulk_step_kernel<real, N, NDOF>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) {
+    g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
+}
+
+template <typename real, int N, int NDOF>
 int launch_typed(const BulkConfig &c) {
   BulkParams<real, N> p{};
   p.LX = c.LX;
@@ -59,15 +71,6 @@ int launch_typed(const BulkConfig &c) {
   p.kd2 = c.kd2;
   const size_t smem = bulk_smem_bytes<real, N, NDOF>(c.tile_nodes, c.nmat, c.has_kv, c.mat_elem);
   auto kern = bulk_step_kernel<real, N, NDOF>;
-  static thread_local size_t configured = 0;
-  if (smem > configured) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-    if (e != cudaSuccess) {
-      g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
-      return 1;
-    }
-    configured = smem;
-  }
   kern<<<dim3(c.grid_x, c.grid_y), kBulkThreads, smem, c.stream>>>(p, c.tile_nodes, c.nmat, c.has_kv);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -75,6 +78,12 @@ int launch_typed(const BulkConfig &c) {
     return 1;
   }
   return 0;
+}
+
+template <int N>
+int configure_for_n(const BulkConfig &c) {
+  if (c.ndof == 1) return c.mixed ? configure_typed<float, N, 1>(c) : configure_typed<double, N, 1>(c);
+  return c.mixed ? configure_typed<float, N, 2>(c) : configure_typed<double, N, 2>(c);
 }
 
 template <int N>

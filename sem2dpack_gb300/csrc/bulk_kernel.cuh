@@ -86,10 +86,14 @@ __global__ void __launch_bounds__(kBulkThreads)
     for (int c = 0; c < NDOF; ++c) {
       sD[c * tile_nodes + idx] = p.Dcur[c * p.plane + g];
       sF[c * tile_nodes + idx] = real(0);
-      if (has_kv) sV[c * tile_nodes + idx] = p.Vcur[c * p.plane + g];
+      if (has_kv) {
+        real v = p.Vcur[c * p.plane + g];
+        if (p.scheme == 1) v = v + p.cpred * p.Acur[c * p.plane + g];
+        sV[c * tile_nodes + idx] = v;
+      }
     }
     if (!p.mat_elem)
-      for (int m = 0; m < nmat; ++m) sM[m * tile_nodes + idx] = p.mat[m][m * 0 + g];
+      for (int m = 0; m < nmat; ++m) sM[m * tile_nodes + idx] = p.mat[m][g];
   }
   __syncthreads();
 
@@ -118,13 +122,11 @@ __global__ void __launch_bounds__(kBulkThreads)
       }
       // material / geometry of this element
       real xix = 0, etaz = 0, det = 0;
-      const real *me = nullptr;
       const real *kve = nullptr;
       if (act) {
         xix = p.xix[ex];
         etaz = p.etaz[ez];
         det = p.dxdxi[ex] * p.dzdeta[ez];
-        if (p.mat_elem) me = nullptr;
         if (has_kv) kve = p.kveta + ((long long)ez * p.nx + ex) * NN;
       }
       const long long eoff = ((long long)ez * p.nx + ex) * NN;

@@ -20,6 +20,15 @@ int launch_bulk(const BulkConfig &c) {
   }
 }
 
+int configure_bulk(const BulkConfig &c) {
+  switch (c.N) {
+    case 5: return configure_bulk_n5(c);
+    case 6: return configure_bulk_n6(c);
+    case 9: return configure_bulk_n9(c);
+    default: g_bulk_err = "NGLL not compiled"; return 1;
+  }
+}
+
 size_t bulk_smem(int N, int ndof, int mixed, int tn, int nmat, int kv, int me) {
   switch (N) {
     case 5: return bulk_smem_n5(ndof, mixed, tn, nmat, kv, me);

@@ -37,6 +37,9 @@ struct BulkConfig {
 
 // launches one time step of the bulk kernel; 0 or non-zero on error
 int launch_bulk(const BulkConfig &c);
+// sets the kernel's dynamic shared-memory limit (once per handle, before
+// any launch or stream capture)
+int configure_bulk(const BulkConfig &c);
 const char *bulk_last_error();
 
 // largest shared-memory tile over all CTAs for a TX x TZ tiling
@@ -52,6 +55,9 @@ int choose_tiles(int N, int ndof, int mixed, int nx, int nz, const int *row0, in
 int launch_bulk_n5(const BulkConfig &c);
 int launch_bulk_n6(const BulkConfig &c);
 int launch_bulk_n9(const BulkConfig &c);
+int configure_bulk_n5(const BulkConfig &c);
+int configure_bulk_n6(const BulkConfig &c);
+int configure_bulk_n9(const BulkConfig &c);
 size_t bulk_smem_n5(int ndof, int mixed, int tile_nodes, int nmat, int has_kv, int mat_elem);
 size_t bulk_smem_n6(int ndof, int mixed, int tile_nodes, int nmat, int has_kv, int mat_elem);
 size_t bulk_smem_n9(int ndof, int mixed, int tile_nodes, int nmat, int has_kv, int mat_elem);

@@ -31,14 +31,6 @@ namespace {
 std::string g_create_err;
 constexpr int kGraphPairs = 8;  // a captured graph covers 16 steps
 
-struct DevBuf {
-  void *p = nullptr;
-  size_t n = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-};
-
 }  // namespace
 
 struct FaultScalars {
@@ -527,7 +519,7 @@ int launch_fault_init(sem2d_handle *h) {
 }
 
 template <typename real>
-int launch_one_step(sem2d_handle *h, int cur) {
+int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
@@ -579,9 +571,11 @@ int launch_one_step(sem2d_handle *h, int cur) {
   bc.H = h->H.data();
   bc.w = h->w.data();
   bc.stream = h->stream;
+  if (ev) CK(cudaEventRecord(ev[0], h->stream));
   int st = launch_bulk(bc);
   if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
   h->launches++;
+  if (ev) CK(cudaEventRecord(ev[1], h->stream));
   if (h->nflt) {
     FaultParams<real> f = fault_params<real>(h, cur);
     fault_step_kernel<real><<<(h->nflt + 127) / 128, 128, 0, h->stream>>>(f);
@@ -590,6 +584,7 @@ int launch_one_step(sem2d_handle *h, int cur) {
   }
   CK(cudaGetLastError());
   h->launches++;
+  if (ev) CK(cudaEventRecord(ev[2], h->stream));
   if (h->nrec) {
     RecParams<real> r{};
     r.nrec = h->nrec;
@@ -609,6 +604,7 @@ int launch_one_step(sem2d_handle *h, int cur) {
     CK(cudaGetLastError());
     h->launches++;
   }
+  if (ev) CK(cudaEventRecord(ev[3], h->stream));
   return SEM2D_OK;
 }
 
@@ -810,6 +806,17 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
   if ((st = choose_tiles(h->N, h->ndof, h->mixed, h->nx, h->nz, h->row0.data(), h->nmat, h->has_kv,
                          h->mat_elem, &h->TX, &h->TZ, &h->tile_nodes)))
     return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no tile shape fits: ") + bulk_last_error());
+  {
+    BulkConfig bc;
+    bc.N = h->N;
+    bc.ndof = h->ndof;
+    bc.mixed = h->mixed;
+    bc.tile_nodes = h->tile_nodes;
+    bc.nmat = h->nmat;
+    bc.has_kv = h->has_kv;
+    bc.mat_elem = h->mat_elem;
+    if (configure_bulk(bc)) return set_err(h, SEM2D_E_CUDA, bulk_last_error());
+  }
   if ((st = reset_state(h))) return st;
   CK(cudaStreamSynchronize(h->stream));
   return SEM2D_OK;
@@ -879,6 +886,43 @@ int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
   if (left && (st = launch_steps(h, left))) return st;
   return SEM2D_OK;
 }
+
+int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms) {
+  if (!h || !ms) return SEM2D_E_ARG;
+  if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
+  if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
+  ms[0] = ms[1] = ms[2] = 0.0;
+  constexpr int kBatch = 64;
+  std::vector<cudaEvent_t> ev(4 * kBatch);
+  for (auto &e : ev) CK(cudaEventCreate(&e));
+  int st = SEM2D_OK;
+  for (int done = 0; done < nsteps && !st;) {
+    const int nb = std::min(kBatch, nsteps - done);
+    for (int k = 0; k < nb && !st; ++k) {
+      st = h->mixed ? launch_one_step<float>(h, h->cur, &ev[4 * k]) : launch_one_step<double>(h, h->cur, &ev[4 * k]);
+      h->cur = 1 - h->cur;
+      h->steps++;
+    }
+    if (st) break;
+    cudaError_t e = cudaStreamSynchronize(h->stream);
+    if (e != cudaSuccess) {
+      st = set_err(h, SEM2D_E_CUDA, cudaGetErrorString(e));
+      break;
+    }
+    for (int k = 0; k < nb; ++k)
+      for (int q = 0; q < 3; ++q) {
+        float t = 0.f;
+        cudaEventElapsedTime(&t, ev[4 * k + q], ev[4 * k + q + 1]);
+        ms[q] += t;
+      }
+    done += nb;
+  }
+  for (auto &e : ev) cudaEventDestroy(e);
+  if (st) return st;
+  return check_device_error(h);
+}
+
+void *sem2d_gpu_stream(sem2d_handle *h) { return h ? (void *)h->stream : nullptr; }
 
 int sem2d_gpu_sync(sem2d_handle *h) {
   if (!h) return SEM2D_E_ARG;

@@ -99,6 +99,85 @@ def sh_rupture(scale=1.0, nsteps=6000, precision=abi.PRECISION_MIXED, out_every=
     return deck, grid
 
 
+def von_karman_field(rng, nx, nz, dx, corr, hurst, std):
+    """Seeded 2-D von Karman random field on a regular grid (FFT synthesis,
+    PSD ~ (1 + k^2 a^2)^-(H+1)), zero mean, given standard deviation."""
+    kx = np.fft.fftfreq(nx, d=dx) * 2 * np.pi
+    kz = np.fft.fftfreq(nz, d=dx) * 2 * np.pi
+    k2 = kz[:, None] ** 2 + kx[None, :] ** 2
+    amp = (1.0 + k2 * corr * corr) ** (-(hurst + 1.0) / 2.0)
+    spec = np.fft.fft2(rng.standard_normal((nz, nx))) * amp
+    f = np.real(np.fft.ifft2(spec))
+    f -= f.mean()
+    return f * (std / f.std())
+
+
+def _bilinear(field, x0, z0, dx, x, z):
+    """Bilinear interpolation on a regular grid, as DIST_HETE1 samples its
+    table (distribution_hete1.f90:100-146)."""
+    nz, nx = field.shape
+    fx = np.clip((x - x0) / dx, 0, nx - 1 - 1e-9)
+    fz = np.clip((z - z0) / dx, 0, nz - 1 - 1e-9)
+    i, j = np.floor(fx).astype(int), np.floor(fz).astype(int)
+    tx, tz = fx - i, fz - j
+    return ((1 - tx) * (1 - tz) * field[j, i] + tx * (1 - tz) * field[j, i + 1]
+            + (1 - tx) * tz * field[j + 1, i] + tx * tz * field[j + 1, i + 1])
+
+
+def psv_rsf(scale=1.0, nsteps=10000, precision=abi.PRECISION_MIXED, rsf_kind=2, out_every=10):
+    """In-plane rupture with rate-and-state friction in a random medium.
+
+    Background vp/vs/rho 6000/3464/2670 perturbed by one von Karman field
+    (5 % std, 1 km correlation, Hurst 0.3) given at the GLL points; fault at
+    mid depth, aging law a=0.008, b=0.012, Dc=0.02 m, V*=1e-6 m/s, f0=0.6 on
+    800 elements (velocity strengthening a=0.02, b=0 outside); initial slip
+    rate 1e-12 m/s with the state at steady state, shear stress at steady
+    state plus a 25 MPa Gaussian perturbation (radius 1.5 km) for nucleation.
+    """
+    nx, nz = max(4, int(round(1024 * scale))), max(4, int(round(512 * scale)))
+    h = 100.0
+    Lx, Lz = nx * h, nz * h
+    seg = 0.5 * min(800 * h * max(scale, 0.05), 0.9 * Lx)
+    deck = ParDeck(
+        ngll=5, ndof=2, fmax=10.0, xlim=(0.0, Lx), zlim=(0.0, Lz), nelem=(nx, nz), ezflt=-1,
+        materials=[Material(tag=1, hetero=True)],
+        absorbing=[1, 2, 3, 4],
+        fault=Fault(tags=(5, 6), friction="RSF", rsf_kind=rsf_kind, normal_kind=1, opening=True),
+        time=Time(kind="leapfrog", courant=0.5, nsteps=nsteps),
+        receivers=Receivers(number=16, first=(0.1 * Lx, 0.5 * Lz + 1500.0),
+                            last=(0.9 * Lx, 0.5 * Lz + 1500.0), field="V"),
+        precision=precision,
+    )
+    grid = Grid(deck)
+    rng = _rng(2)
+    dxg = 25.0
+    gx, gz = int(Lx / dxg) + 2, int(Lz / dxg) + 2
+    xi = von_karman_field(rng, gx, gz, dxg, 1000.0, 0.3, 0.05)
+    coord = grid.coord()
+    pert = _bilinear(xi, 0.0, 0.0, dxg, coord[0], coord[1])
+    ib = grid.ibool() - 1
+    pe = pert[ib]  # (ngll, ngll, nelem)
+    deck.hetero = {"rho": 2670.0 * (1 + pe), "cp": 6000.0 * (1 + pe), "cs": 3464.0 * (1 + pe)}
+    n1, _ = grid.fault_nodes()
+    x = coord[0, n1 - 1]
+    xc = 0.5 * Lx
+    inside = np.abs(x - xc) <= seg
+    a = np.where(inside, 0.008, 0.02)
+    b = np.where(inside, 0.012, 0.0)
+    dc, vstar, f0, v0, sigma = 0.02, 1.0e-6, 0.6, 1.0e-12, -120.0e6
+    theta = np.full(x.shape, dc / v0)
+    if rsf_kind == 1:
+        theta = np.zeros(x.shape)
+    mu0 = a * np.arcsinh(v0 / (2 * vstar) * np.exp((f0 + b * np.log(vstar * theta / dc)) / a)) \
+        if rsf_kind != 1 else f0 + a * v0 / (v0 + vstar)
+    tau = -sigma * mu0 + 25.0e6 * np.exp(-0.5 * ((x - xc) / 1500.0) ** 2)
+    deck.fault.values = {"Tn": sigma, "Tt": tau, "V": v0, "rsf_a": a, "rsf_b": b, "rsf_dc": dc,
+                         "rsf_vstar": vstar, "rsf_mus": f0, "rsf_theta": theta}
+    dt_est = 0.5 * (h * (1.0 - np.sqrt(3.0 / 7.0)) / 2.0) / (6000.0 * 1.25)
+    deck.fault.otd = out_every * dt_est
+    return deck, grid
+
+
 def build(deck_or_pair):
     """Problem for a deck (or a (deck, grid) pair from a builder)."""
     if isinstance(deck_or_pair, tuple):

@@ -1,0 +1,195 @@
+"""GPU time step (through the C-ABI) against the FP64 oracle.
+
+Tolerances (relative L2 over the whole compared array):
+  FP64 path   <= 1e-10   (the oracle evaluates without FMA, the GPU with)
+  mixed path  <= 1e-4    (FP32 fields and forces, FP64 fault state)
+Integer/layout properties (step counters, sample counts) are exact.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import decks
+from oracle import pyoracle as po
+from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Problem, Solver, workloads
+
+pytestmark = pytest.mark.gpu
+
+TOL = {PRECISION_FP64: 1e-10, PRECISION_MIXED: 1e-4}
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def make(deck_or_pair, precision):
+    P = workloads.build(deck_or_pair)
+    d = P.desc()
+    d.precision = precision
+    return P, d
+
+
+def run_both(deck_or_pair, nsteps, precision):
+    P, d = make(deck_or_pair, precision)
+    g = Solver(d, owner=P)
+    g.step(nsteps)
+    o = po.OracleSim(d, owner=P)
+    o.run(nsteps)
+    return P, g, o
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+def test_plain_psv(precision):
+    P, g, o = run_both(workloads.plain_psv(scale=0.2, nsteps=300), 300, precision)
+    assert g.current_step == 300
+    s_g, s_o = g.seismograms(), o.seismograms()
+    assert np.abs(s_o).max() > 0
+    assert rel_l2(s_g, s_o) <= TOL[precision]
+    dg, vg = g.fields()
+    do, vo, _ = o.fields()
+    assert rel_l2(dg, do) <= TOL[precision]
+    assert rel_l2(vg, vo) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+def test_sh_rupture_swf(precision):
+    pair = workloads.sh_rupture(scale=0.1, nsteps=400)
+    P, g, o = run_both(pair, 400, precision)
+    fg, fo = g.fault_series(), o.fault_series()
+    assert fo[:, 0, -1].max() > 0.1  # the rupture slipped
+    for rec, name in ((0, "slip"), (1, "slip rate"), (2, "shear"), (4, "friction")):
+        assert rel_l2(fg[:, rec, :], fo[:, rec, :]) <= TOL[precision], name
+    assert rel_l2(g.seismograms(), o.seismograms()) <= TOL[precision]
+    Dg, Vg, Tg, MUg, _ = g.fault_state()
+    Do, Vo, To, MUo, _ = o.fault_state()
+    assert rel_l2(Dg, Do) <= TOL[precision]
+
+
+@pytest.mark.parametrize("kind", [1, 2, 3, 4])
+def test_psv_rsf_fp64(kind):
+    pair = workloads.psv_rsf(scale=0.05, nsteps=300, rsf_kind=kind)
+    P, g, o = run_both(pair, 300, PRECISION_FP64)
+    fg, fo = g.fault_series(), o.fault_series()
+    for rec in (0, 1, 2, 3, 4):  # record 6 (T_stick) is undefined for RSF in the reference
+        assert rel_l2(fg[:, rec, :], fo[:, rec, :]) <= 1e-9, rec
+    assert rel_l2(g.seismograms(), o.seismograms()) <= 1e-9
+    _, _, _, _, thg = g.fault_state()
+    _, _, _, _, tho = o.fault_state()
+    assert rel_l2(thg, tho) <= 1e-9
+
+
+def test_psv_rsf_mixed():
+    pair = workloads.psv_rsf(scale=0.05, nsteps=300, rsf_kind=2)
+    P, g, o = run_both(pair, 300, PRECISION_MIXED)
+    fg, fo = g.fault_series(), o.fault_series()
+    for rec in (0, 1):
+        assert rel_l2(fg[:, rec, :], fo[:, rec, :]) <= 1e-4, rec
+
+
+def test_lamb_ngll9(golden):
+    """Lamb's problem (NGLL=9, KD1) on the GPU against the oracle and the
+    analytic solution with the reference's criterion."""
+    P = Problem(decks.lambs_problem())
+    g = Solver(P)
+    g.run()
+    sis = g.seismograms()
+    uxa = np.vstack([np.zeros((1, 2)), golden["lamb_ux"].reshape(3000, 2, order="F")])
+    uza = np.vstack([np.zeros((1, 2)), golden["lamb_uz"].reshape(3000, 2, order="F")])
+    A = np.hstack([uxa, uza])
+    U = np.hstack([sis[:, :, 0], sis[:, :, 1]])
+    err = np.abs(U - A).max(0) / np.abs(A).max(0)
+    np.testing.assert_allclose(err, golden["lamb_recorded_misfit"], rtol=2e-4)
+    # the whole record: before the P wave arrives (~740 steps) the traces
+    # are round-off-level precursors, so only the full record is compared
+    o = po.OracleSim(P.desc(), owner=P)
+    o.run(P.nt)
+    assert rel_l2(sis, o.seismograms()) <= 1e-10
+
+
+def test_testsh_ngll6(golden):
+    P = Problem(decks.test_sh())
+    g = Solver(P)
+    g.run()
+    u = g.seismograms()[:, 4, 0]
+    uref = golden["sh_uref"]
+    assert np.abs(u - uref).max() / np.abs(uref).max() < 0.02
+
+
+def test_anisotropic_element_material(golden):
+    """VTI + isotropic domains: the material is discontinuous at the domain
+    interface, so the per-element-point layout is used."""
+    P = Problem(decks.anisotropic())
+    g = Solver(P)
+    g.step(1000)
+    sis = g.seismograms()
+    for k, st in enumerate(golden["aniso_stations"]):
+        p = golden["aniso_p%d" % (k + 1)]
+        for c in (0, 1):
+            scale = np.abs(p[:, 1 + c]).max()
+            assert np.abs(sis[1:1001, st - 1, c] - p[:1000, 1 + c]).max() / scale < 2e-6
+
+
+def test_kelvin_voigt_and_interpolated_receivers():
+    dk = workloads.plain_psv(scale=0.2, nsteps=200)
+    dk.materials[0].kv_eta = 0.2
+    dk.receivers.atnode = False
+    P, g, o = run_both(dk, 200, PRECISION_FP64)
+    assert rel_l2(g.seismograms(), o.seismograms()) <= 1e-10
+
+
+def test_newmark_inabox():
+    dk = decks.inabox()
+    dk.time.total_time = 0.0
+    dk.time.nsteps = 200
+    dk.receivers = workloads.plain_psv(scale=0.4).receivers
+    dk.receivers.first, dk.receivers.last = (-800.0, -700.0), (800.0, 600.0)
+    dk.receivers.field = "A"
+    P, g, o = run_both(dk, 200, PRECISION_FP64)
+    assert rel_l2(g.seismograms(), o.seismograms()) <= 1e-10
+    d, v, a = g.fields(accel=True)
+    do, vo, ao = o.fields()
+    assert rel_l2(a, ao) <= 1e-10
+
+
+def test_reset_is_deterministic_and_tiles_agree(monkeypatch):
+    pair = workloads.sh_rupture(scale=0.1, nsteps=200)
+    P, d = make(pair, PRECISION_FP64)
+    g = Solver(d, owner=P)
+    g.step(200)
+    a = g.seismograms().copy()
+    fa = g.fault_series().copy()
+    g.reset()
+    g.step(200)
+    assert np.array_equal(a, g.seismograms())        # bitwise
+    assert np.array_equal(fa, g.fault_series())
+    for tile in ("1x1", "4x2", "3x5"):
+        monkeypatch.setenv("SEM2D_TILE", tile)
+        h = Solver(d, owner=P)
+        assert h.tile == tuple(int(v) for v in tile.split("x"))
+        h.step(200)
+        assert np.array_equal(a, h.seismograms()), tile  # same per-node summation order
+    monkeypatch.delenv("SEM2D_TILE")
+
+
+def test_graph_and_direct_launches_agree(monkeypatch):
+    P, d = make(workloads.plain_psv(scale=0.2, nsteps=100), PRECISION_MIXED)
+    g = Solver(d, owner=P)
+    g.step(37)
+    g.step(63)
+    monkeypatch.setenv("SEM2D_NO_GRAPH", "1")
+    h = Solver(d, owner=P)
+    h.step(100)
+    assert np.array_equal(g.seismograms(), h.seismograms())
+    assert g.launches == h.launches == 100 * 3
+
+
+def test_errors_are_reported():
+    from sem2dpack_gb300 import Sem2dError
+    P, d = make(workloads.plain_psv(scale=0.1, nsteps=10), PRECISION_FP64)
+    g = Solver(d, owner=P)
+    with pytest.raises(Sem2dError):
+        g.step(11)  # beyond nt
+    with pytest.raises(Sem2dError):
+        g.fields(accel=True)  # leapfrog keeps no accelerations unless asked
