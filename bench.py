@@ -56,6 +56,8 @@ def parse():
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--time-steps", type=int, default=0,
+                   help="time steps per solve (default: all of the workload); for short profiling runs")
     return p.parse_args()
 
 
@@ -234,6 +236,8 @@ def main():
     prob, name = make_workload(args)
     desc = prob.desc()
     npoin, nt, ndof = desc.npoin, desc.nt, desc.ndof
+    if args.time_steps:
+        nt = min(nt, args.time_steps)
     dtype = "f32" if desc.precision == 1 else "f64"
     sim = Solver(desc, owner=prob)
     stream = torch.cuda.ExternalStream(sim.stream)
