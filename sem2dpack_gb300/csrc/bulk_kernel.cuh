@@ -1,25 +1,31 @@
-// bulk_kernel.cuh -- the fused spectral-element step for one tile of
-// elements per CTA.
+// bulk_kernel.cuh -- one fused launch per time step.
 //
-// One launch performs, for every lattice node a CTA owns, what the
-// reference does in one pass of solve_leapfrog / solve_Newmark
-// (solver.f90:42-83, 140-161):
+// For every lattice node a CTA owns, one launch performs what the reference
+// does in one pass of solve_leapfrog / solve_Newmark (solver.f90:42-83,
+// 140-161):
 //   f = -K d            compute_Fint (solver.f90:273-316) with MAT_Fint ->
 //                       ELAST_KD1/KD2 (mat_elastic.f90:464-775) and the
 //                       Kelvin-Voigt term (mat_kelvin_voigt.f90:137-151)
 //   f += sources        SO_add (src_gen.f90:290-317)
 //   f -= C v            BC_ABSO_apply (bc_abso.f90:286-319)
+//   dynamic fault       BC_DYNFLT_apply (bc_dynflt.f90:569-739), FP64
 //   a = rmass f, v += c a, next displacement predictor
-// Fault-row nodes only get f; the fault kernel finishes them.
+//   seismograms         REC_store (receivers.f90:309-344) for the receivers
+//                       the CTA owns
+// and the last CTA to finish advances the device step counter, so a time
+// step is a single kernel node in the captured CUDA graph.
 //
-// Work decomposition.  A CTA owns the lattice nodes of a TX x TZ tile of
-// elements (lower-left convention).  Nodes on its left/bottom edges also
-// receive forces from the neighbouring element column/row, so those
-// elements are recomputed (a one-element halo).  Displacements of the tile
-// (with halo) are staged in shared memory once; elements are processed in
-// the four parity colours of the element lattice, so elements of one
-// colour never share a node and add into the shared force tile without
-// atomics; the per-node sum is therefore in a fixed order.
+// Work decomposition.  A CTA owns the lattice nodes of a tile of TX element
+// columns by ztile[y]..ztile[y+1] element rows (lower-left convention).
+// Nodes on its left/bottom edges also receive forces from the neighbouring
+// element column/row, so those elements are recomputed (a one-element
+// halo).  The host places tile-row boundaries away from a fault split, so
+// both split rows of a fault belong to the same CTA.  Displacement (and the
+// material when it is stored per node) of the tile with its halo, and the
+// velocity and inverse mass of the owned nodes, are staged in shared memory
+// up front; elements are processed in the four parity colours of the
+// element lattice, so elements of one colour never share a node and add
+// into the shared force tile without atomics, in a fixed order per node.
 //
 // Element operator.  For an N x N element the gradients dU/dxi = H^T U and
 // dU/deta = U H and the divergence H tmp + tmp H^T are computed with N
@@ -29,6 +35,7 @@
 // exchanged through a per-warp scratch area.
 #pragma once
 
+#include "fault_kernel.cuh"
 #include "sem2d_common.cuh"
 
 namespace sem2d {
@@ -41,20 +48,27 @@ struct BulkShape {
 
 // shared-memory footprint (bytes) of one CTA, same arithmetic as the kernel
 template <typename real, int N, int NDOF>
-__host__ __device__ inline size_t bulk_smem_bytes(int tile_nodes, int nmat_planes, int has_kv,
-                                                  int mat_elem) {
+__host__ __device__ inline size_t bulk_smem_bytes(int tile_nodes, int own_nodes, int nmat_planes,
+                                                  int has_kv, int mat_elem) {
   const int nwarps = kBulkThreads / 32;
   size_t n = size_t(tile_nodes) * NDOF * 2;                 // D, F
   if (!mat_elem) n += size_t(tile_nodes) * nmat_planes;     // material
-  if (has_kv) n += size_t(tile_nodes) * NDOF;               // V for Kelvin-Voigt
+  if (has_kv) n += size_t(tile_nodes) * NDOF;               // V of the tile (Kelvin-Voigt)
+  n += size_t(own_nodes) * (NDOF + 1);                      // owned V, rmass
   n += size_t(nwarps) * BulkShape<N, NDOF>::kSlots * BulkShape<N, NDOF>::kScr * N * N;
   return n * sizeof(real);
 }
 
-template <typename real, int N, int NDOF>
-__global__ void __launch_bounds__(kBulkThreads)
-    bulk_step_kernel(const BulkParams<real, N> p, const int tile_nodes, const int nmat,
-                     const int has_kv) {
+// minimum resident CTAs per SM the register allocation is sized for
+template <typename real>
+struct BulkOccupancy {
+  static constexpr int kMinBlocks = sizeof(real) == 4 ? 4 : 2;
+};
+
+template <typename real, int N, int NDOF, bool MELEM>
+__global__ void __launch_bounds__(kBulkThreads, BulkOccupancy<real>::kMinBlocks)
+    bulk_step_kernel(const BulkParams<real, N> p, const int tile_nodes, const int own_nodes,
+                     const int nmat, const int has_kv) {
   constexpr int NN = N * N;
   constexpr int SLOTS = BulkShape<N, NDOF>::kSlots;
   constexpr int NSCR = BulkShape<N, NDOF>::kScr;
@@ -62,13 +76,16 @@ __global__ void __launch_bounds__(kBulkThreads)
   real *sD = reinterpret_cast<real *>(smem_raw);
   real *sF = sD + size_t(tile_nodes) * NDOF;
   real *sM = sF + size_t(tile_nodes) * NDOF;
-  real *sV = sM + (p.mat_elem ? 0 : size_t(tile_nodes) * nmat);
-  real *sS = sV + (has_kv ? size_t(tile_nodes) * NDOF : 0);
+  real *sV = sM + (MELEM ? 0 : size_t(tile_nodes) * nmat);
+  real *sVo = sV + (has_kv ? size_t(tile_nodes) * NDOF : 0);
+  real *sRm = sVo + size_t(own_nodes) * NDOF;
+  real *sS = sRm + own_nodes;
 
+  const int it = *p.step + 1;  // the step this launch computes
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nwarps = blockDim.x >> 5;
-  const int ex0 = blockIdx.x * p.TX, ez0 = blockIdx.y * p.TZ;
-  const int ex1 = min(ex0 + p.TX, p.nx), ez1 = min(ez0 + p.TZ, p.nz);
+  const int ex0 = blockIdx.x * p.TX, ex1 = min(ex0 + p.TX, p.nx);
+  const int ez0 = p.ztile[blockIdx.y], ez1 = p.ztile[blockIdx.y + 1];
   const int hx = ex0 > 0 ? 1 : 0;
   const int hz = (ez0 > 0 && p.row0[ez0] == p.row0[ez0 - 1] + (N - 1)) ? 1 : 0;
   const int exa = ex0 - hx, eza = ez0 - hz;
@@ -77,23 +94,41 @@ __global__ void __launch_bounds__(kBulkThreads)
   const int TW = Ib - Ia, TH = Jb - Ja;
   const int I0 = ex0 * (N - 1), I1 = (ex1 == p.nx) ? p.LX : ex1 * (N - 1);
   const int J0 = p.row0[ez0], J1 = p.row0[ez1];  // row0[nz] == LZ
+  const int OW = I1 - I0, OH = J1 - J0;
 
-  // ---- 1. stage the tile: displacement (+velocity for KV), material ----
-  for (int idx = tid; idx < TW * TH; idx += blockDim.x) {
-    const int I = Ia + idx % TW, J = Ja + idx / TW;
-    const long long g = (long long)J * p.pitch + I;
+  // ---- 1. stage the tile (with halo) and the owned nodes ----
+  for (int j = warp; j < TH; j += nwarps) {
+    const long long rowg = (long long)(Ja + j) * p.pitch + Ia;
+    for (int i = lane; i < TW; i += 32) {
+      const int idx = j * TW + i;
+      const long long g = rowg + i;
 #pragma unroll
-    for (int c = 0; c < NDOF; ++c) {
-      sD[c * tile_nodes + idx] = p.Dcur[c * p.plane + g];
-      sF[c * tile_nodes + idx] = real(0);
-      if (has_kv) {
+      for (int c = 0; c < NDOF; ++c) {
+        sD[c * tile_nodes + idx] = p.Dcur[c * p.plane + g];
+        sF[c * tile_nodes + idx] = real(0);
+        if (has_kv) {
+          real v = p.Vcur[c * p.plane + g];
+          if (p.scheme == 1) v = v + p.cpred * p.Acur[c * p.plane + g];
+          sV[c * tile_nodes + idx] = v;
+        }
+      }
+      if (!MELEM)
+        for (int m = 0; m < nmat; ++m) sM[m * tile_nodes + idx] = p.mat[m][g];
+    }
+  }
+  for (int j = warp; j < OH; j += nwarps) {
+    const long long rowg = (long long)(J0 + j) * p.pitch + I0;
+    for (int i = lane; i < OW; i += 32) {
+      const int o = j * OW + i;
+      const long long g = rowg + i;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) {
         real v = p.Vcur[c * p.plane + g];
         if (p.scheme == 1) v = v + p.cpred * p.Acur[c * p.plane + g];
-        sV[c * tile_nodes + idx] = v;
+        sVo[c * own_nodes + o] = v;  // velocity predictor
       }
+      sRm[o] = p.rmass[g];
     }
-    if (!p.mat_elem)
-      for (int m = 0; m < nmat; ++m) sM[m * tile_nodes + idx] = p.mat[m][g];
   }
   __syncthreads();
 
@@ -114,24 +149,21 @@ __global__ void __launch_bounds__(kBulkThreads)
       const int k = base + slot;
       const bool act = lane_ok && k < ncol;
       int ex = 0, ez = 0, eb = 0;
-      if (act) {
-        const int lx = fx + 2 * (k % nxc), lz = fz + 2 * (k / nxc);
-        ex = exa + lx;
-        ez = eza + lz;
-        eb = (p.row0[ez] - Ja) * TW + (ex * (N - 1) - Ia);
-      }
-      // material / geometry of this element
       real xix = 0, etaz = 0, det = 0;
-      const real *kve = nullptr;
       if (act) {
+        const int kz = k / nxc;
+        ex = exa + fx + 2 * (k - kz * nxc);
+        ez = eza + fz + 2 * kz;
+        eb = (p.row0[ez] - Ja) * TW + (ex * (N - 1) - Ia);
         xix = p.xix[ex];
         etaz = p.etaz[ez];
         det = p.dxdxi[ex] * p.dzdeta[ez];
-        if (has_kv) kve = p.kveta + ((long long)ez * p.nx + ex) * NN;
       }
       const long long eoff = ((long long)ez * p.nx + ex) * NN;
+      const real *kve = has_kv ? p.kveta + eoff : nullptr;
       auto matv = [&](int m, int i, int j) -> real {
-        return p.mat_elem ? p.mat[m][eoff + i + N * j] : sM[m * tile_nodes + eb + j * TW + i];
+        if (MELEM) return p.mat[m][eoff + i + N * j];
+        return sM[m * tile_nodes + eb + j * TW + i];
       };
       auto uval = [&](int c, int i, int j) -> real {
         real u = sD[c * tile_nodes + eb + j * TW + i];
@@ -161,15 +193,21 @@ __global__ void __launch_bounds__(kBulkThreads)
             for (int q = 1; q < N; ++q) a = a + row[q] * p.H[q + N * j];
             geta[j] = a;
           }
-          // column part: points (q,t); row part: points (t,q)
+          // column part at points (q,t), row part at points (t,q)
+          if (p.mat_iso) {
 #pragma unroll
-          for (int q = 0; q < N; ++q) {
-            const real mux = p.mat_iso ? matv(0, q, t) : matv(1, q, t);
-            const real W1 = det * (p.w[q] * p.w[t]);
-            col[q] = -(W1 * ((mux * xix) * xix)) * gxi[q];
-            const real mu = matv(0, t, q);
-            const real W2 = det * (p.w[t] * p.w[q]);
-            row[q] = -(W2 * ((mu * etaz) * etaz)) * geta[q];
+            for (int q = 0; q < N; ++q) {
+              const real mux = matv(0, q, t), mu = matv(0, t, q);
+              col[q] = -((det * (p.w[q] * p.w[t])) * ((mux * xix) * xix)) * gxi[q];
+              row[q] = -((det * (p.w[t] * p.w[q])) * ((mu * etaz) * etaz)) * geta[q];
+            }
+          } else {
+#pragma unroll
+            for (int q = 0; q < N; ++q) {
+              const real mux = matv(1, q, t), mu = matv(0, t, q);
+              col[q] = -((det * (p.w[q] * p.w[t])) * ((mux * xix) * xix)) * gxi[q];
+              row[q] = -((det * (p.w[t] * p.w[q])) * ((mu * etaz) * etaz)) * geta[q];
+            }
           }
 #pragma unroll
           for (int i = 0; i < N; ++i) {
@@ -186,13 +224,12 @@ __global__ void __launch_bounds__(kBulkThreads)
             real a = row[0] * p.H[j + N * 0];
 #pragma unroll
             for (int q = 1; q < N; ++q) a = a + row[q] * p.H[j + N * q];
-            const real fl = scr[t + N * j] + a;
-            sF[eb + j * TW + t] += fl;
+            sF[eb + j * TW + t] += scr[t + N * j] + a;
           }
         }
         __syncwarp();
       } else {
-        real cx[N], cz[N], rx[N], rz[N];  // loads, then reused
+        real cx[N], cz[N], rx[N], rz[N];
         real gxx[N], gxz[N], gex[N], gez[N];
         real *SXX = scr, *SXZ = scr + NN, *SEX = scr + 2 * NN, *SEZ = scr + 3 * NN;
         if (act) {
@@ -235,10 +272,10 @@ __global__ void __launch_bounds__(kBulkThreads)
         }
         __syncwarp();
         if (act) {
-          // column part at points (q,t) and row part at points (t,q)
 #pragma unroll
           for (int q = 0; q < N; ++q) {
-            real la, mu, Kx, Kz;
+            // column part at point (q,t)
+            real la, mu, Kx;
             if (p.mat_iso) {
               la = matv(0, q, t);
               mu = matv(1, q, t);
@@ -258,6 +295,7 @@ __global__ void __launch_bounds__(kBulkThreads)
           }
 #pragma unroll
           for (int q = 0; q < N; ++q) {
+            // row part at point (t,q)
             real la, mu, Kz;
             if (p.mat_iso) {
               la = matv(0, t, q);
@@ -280,7 +318,6 @@ __global__ void __launch_bounds__(kBulkThreads)
         }
         __syncwarp();
         if (act) {
-          // divergence: column part -> scratch, row part summed by row owner
 #pragma unroll
           for (int i = 0; i < N; ++i) {
             real a = p.H[i + N * 0] * cx[0], b = p.H[i + N * 0] * cz[0];
@@ -315,11 +352,10 @@ __global__ void __launch_bounds__(kBulkThreads)
   }
 
   // ---- 3. point sources at owned nodes (in source order) ----
-  const int it = *p.step + 1;
-  if (tid == 0 && p.nsrc > 0) {
+  if (tid == 0 && p.nsrc > 0 && it <= p.nt) {
     for (int s = 0; s < p.nsrc; ++s) {
       const int I = p.src_I[s], J = p.src_J[s];
-      if (I >= I0 && I < I1 && J >= J0 && J < J1 && it <= p.nt) {
+      if (I >= I0 && I < I1 && J >= J0 && J < J1) {
         const int ti = (J - Ja) * TW + (I - Ia);
         for (int c = 0; c < NDOF; ++c)
           sF[c * tile_nodes + ti] += real(p.src_amp[((long long)s * NDOF + c) * (p.nt + 1) + it]);
@@ -329,45 +365,97 @@ __global__ void __launch_bounds__(kBulkThreads)
   __syncthreads();
 
   // ---- 4. absorbing dashpots, inverse mass, time update of owned nodes ----
-  const int OW = I1 - I0, OH = J1 - J0;
-  for (int idx = tid; idx < OW * OH; idx += blockDim.x) {
-    const int I = I0 + idx % OW, J = J0 + idx / OW;
-    const int ti = (J - Ja) * TW + (I - Ia);
-    const long long g = (long long)J * p.pitch + I;
-    const int slot_p = perimeter_slot(I, J, p.LX, p.LZ);
-    const int nslot = perimeter_slots(p.LX, p.LZ);
+  const int nslot = perimeter_slots(p.LX, p.LZ);
+  for (int j = warp; j < OH; j += nwarps) {
+    const int J = J0 + j;
     const bool fault_row = (J == p.jf1 || J == p.jf2);
+    const bool edge_row = (J == 0 || J == p.LZ - 1);
+    for (int i = lane; i < OW; i += 32) {
+      const int I = I0 + i;
+      const int o = j * OW + i;
+      const int ti = (J - Ja) * TW + (I - Ia);
+      const long long g = (long long)J * p.pitch + I;
+      const int sp = (edge_row || I == 0 || I == p.LX - 1) ? perimeter_slot(I, J, p.LX, p.LZ) : -1;
 #pragma unroll
-    for (int c = 0; c < NDOF; ++c) {
-      real f = sF[c * tile_nodes + ti];
-      const real vold = p.Vcur[c * p.plane + g];
-      real vpred = vold;
-      if (p.scheme == 1) vpred = vold + p.cpred * p.Acur[c * p.plane + g];
-      real rm;
-      if (slot_p >= 0) {
-        const int so = c * nslot + slot_p;
-        f = f - p.per_Ca[so] * vpred;
-        f = f - p.per_Cb[so] * vpred;
-        rm = p.per_rm[so];
-      } else {
-        rm = p.rmass[g];
+      for (int c = 0; c < NDOF; ++c) {
+        real f = sF[c * tile_nodes + ti];
+        const real vpred = sVo[c * own_nodes + o];
+        real rm;
+        if (sp >= 0) {
+          const int so = c * nslot + sp;
+          f = f - p.per_Ca[so] * vpred;
+          f = f - p.per_Cb[so] * vpred;
+          rm = p.per_rm[so];
+        } else {
+          rm = sRm[o];
+        }
+        if (fault_row) {  // finished by the fault phase below
+          sF[c * tile_nodes + ti] = f;
+          continue;
+        }
+        const real a = rm * f;
+        const real vnew = vpred + p.cv * a;
+        const real dcur = sD[c * tile_nodes + ti];
+        const real dnext = p.scheme == 1 ? (dcur + p.dt * vnew) + p.cd2 * a : dcur + p.dt * vnew;
+        p.Vnext[c * p.plane + g] = vnew;
+        p.Dnext[c * p.plane + g] = dnext;
+        if (p.Anext) p.Anext[c * p.plane + g] = a;
       }
-      if (fault_row) {
-        const int side = (J == p.jf1) ? 0 : 1;
-        p.f_flt[(side * NDOF + c) * p.LX + I] = f;
-        continue;
+    }
+  }
+
+  // ---- 5. fault nodes of this tile (FP64) ----
+  const bool fault_here = p.has_fault && p.jf1 >= J0 && p.jf1 < J1;
+  const int nrec_here = p.rec_tile_start ? p.rec_tile_start[blockIdx.y * gridDim.x + blockIdx.x + 1] -
+                                               p.rec_tile_start[blockIdx.y * gridDim.x + blockIdx.x]
+                                         : 0;
+  if (fault_here || nrec_here) __syncthreads();
+  if (fault_here) {
+    for (int I = I0 + tid; I < I1; I += blockDim.x) {
+      double f1[2] = {0, 0}, f2[2] = {0, 0};
+      for (int c = 0; c < NDOF; ++c) {
+        f1[c] = double(sF[c * tile_nodes + (p.jf1 - Ja) * TW + (I - Ia)]);
+        if (p.flt.two) f2[c] = double(sF[c * tile_nodes + (p.jf2 - Ja) * TW + (I - Ia)]);
       }
-      const real a = rm * f;
-      const real vnew = vpred + p.cv * a;
-      const real dcur = sD[c * tile_nodes + ti];
-      real dnext;
-      if (p.scheme == 1)
-        dnext = (dcur + p.dt * vnew) + p.cd2 * a;
-      else
-        dnext = dcur + p.dt * vnew;
-      p.Vnext[c * p.plane + g] = vnew;
-      p.Dnext[c * p.plane + g] = dnext;
-      if (p.Anext) p.Anext[c * p.plane + g] = a;
+      fault_node_update(p.flt, I, it, f1, f2);
+    }
+  }
+
+  // ---- 6. seismograms of the receivers owned by this tile ----
+  if (nrec_here) {
+    if (fault_here) __syncthreads();
+    const int s = it / p.rec_isamp;
+    if (it % p.rec_isamp == 0 && s < p.rec_nsamp) {
+      const int r0 = p.rec_tile_start[blockIdx.y * gridDim.x + blockIdx.x];
+      for (int q = tid; q < nrec_here * NDOF; q += blockDim.x) {
+        const int r = p.rec_ids[r0 + q % nrec_here], c = q / nrec_here;
+        double val;
+        if (p.rec_npts == 1) {  // receiver at a node: D, V or A
+          const int I = p.rec_I[r], J = p.rec_J[r];
+          val = p.rec_field == 'D' ? double(sD[c * tile_nodes + (J - Ja) * TW + (I - Ia)])
+                : p.rec_field == 'V' ? double(p.Vnext[c * p.plane + (long long)J * p.pitch + I])
+                                     : double(p.Anext[c * p.plane + (long long)J * p.pitch + I]);
+        } else {  // interpolated displacement; the element lies in this tile
+          const int *RI = p.rec_I + (size_t)r * p.rec_npts, *RJ = p.rec_J + (size_t)r * p.rec_npts;
+          const double *W = p.rec_w + (size_t)r * p.rec_npts;
+          val = W[0] * double(sD[c * tile_nodes + (RJ[0] - Ja) * TW + (RI[0] - Ia)]);
+          for (int k = 1; k < p.rec_npts; ++k)
+            val = val + W[k] * double(sD[c * tile_nodes + (RJ[k] - Ja) * TW + (RI[k] - Ia)]);
+        }
+        p.sis[s + (size_t)p.rec_nsamp * (r + (size_t)p.rec_nrec * c)] = val;
+      }
+    }
+  }
+
+  // ---- 7. the last CTA to finish advances the step counter ----
+  __syncthreads();
+  if (tid == 0) {
+    __threadfence();
+    const unsigned prev = atomicAdd(p.done, 1u);
+    if (prev == gridDim.x * gridDim.y - 1) {
+      *p.done = 0u;
+      __threadfence();
+      *p.step = it;
     }
   }
 }

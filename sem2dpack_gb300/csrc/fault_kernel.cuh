@@ -1,5 +1,6 @@
-// fault_kernel.cuh -- split-node dynamic fault, run after the bulk kernel
-// of each step with one thread per fault node pair, entirely in FP64.
+// fault_kernel.cuh -- split-node dynamic fault, one thread per fault node
+// pair, entirely in FP64 (called from the bulk kernel by the CTA that owns
+// the fault rows).
 //
 // Restates BC_DYNFLT_apply (bc_dynflt.f90:569-739): traction that keeps
 // the fault stuck (T = Z (dV + coefA2V dA)), rotation to the fault frame,
@@ -171,145 +172,131 @@ __global__ void fault_init_kernel(FaultParams<real> p) {
   fault_record(p, k, 0);
 }
 
+// One fault node pair k at step it, given the raw nodal forces f1, f2 of
+// both sides (internal + sources + absorbing terms).  Finishes the time
+// update of the two split nodes, which the bulk update skips.
 template <typename real>
-__global__ void fault_step_kernel(FaultParams<real> p) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int it = *p.step + 1;
-  if (k < p.nflt) {
-    const int nd = p.ndof, nf = p.nflt;
-    double f1[2] = {0, 0}, f2[2] = {0, 0}, d1[2] = {0, 0}, d2[2] = {0, 0};
-    double v1[2] = {0, 0}, v2[2] = {0, 0}, dD[2] = {0, 0}, dV[2] = {0, 0}, dA[2] = {0, 0};
-    double T[2] = {0, 0}, Ts[2] = {0, 0};
-    for (int c = 0; c < nd; ++c) {
-      const int o1 = (0 * nd + c) * nf + k, o2 = (1 * nd + c) * nf + k;
-      f1[c] = double(p.f_flt[(0 * nd + c) * p.LX + k]);
-      d1[c] = p.d64[o1];
-      v1[c] = p.v64[o1];
-      if (p.scheme == 1) v1[c] = v1[c] + p.cpred * p.a64[o1];
-      if (p.two) {
-        f2[c] = double(p.f_flt[(1 * nd + c) * p.LX + k]);
-        d2[c] = p.d64[o2];
-        v2[c] = p.v64[o2];
-        if (p.scheme == 1) v2[c] = v2[c] + p.cpred * p.a64[o2];
-        dD[c] = d2[c] - d1[c];
-        dV[c] = v2[c] - v1[c];
-        dA[c] = p.invM2[k + nf * c] * f2[c] - p.invM1[k + nf * c] * f1[c];
-      } else {
-        dD[c] = -2.0 * d1[c];
-        dV[c] = -2.0 * v1[c];
-        dA[c] = -2.0 * p.invM1[k + nf * c] * f1[c];
-      }
-      T[c] = p.Z[k + nf * c] * (dV[c] + p.coefA2V * dA[c]);
-    }
-    const double nx = p.n1[k], nz = p.n1[k + nf];
-    if (nd == 2) {
-      double r0, r1;
-      r0 = nz * dD[0] - nx * dD[1]; r1 = nx * dD[0] + nz * dD[1]; dD[0] = r0; dD[1] = r1;
-      r0 = nz * dV[0] - nx * dV[1]; r1 = nx * dV[0] + nz * dV[1]; dV[0] = r0; dV[1] = r1;
-      r0 = nz * dA[0] - nx * dA[1]; r1 = nx * dA[0] + nz * dA[1]; dA[0] = r0; dA[1] = r1;
-      r0 = nz * T[0] - nx * T[1];   r1 = nx * T[0] + nz * T[1];   T[0] = r0;  T[1] = r1;
-    }
-    if (!p.two || nd == 1) T[1] = 0.0;
-    T[0] = T[0] + p.T0[k];
-    T[1] = T[1] + p.T0[k + nf];
-    if (p.opening) T[1] = T[1] < 0.0 ? T[1] : 0.0;
-    double sig = p.sigma[k];
-    if (p.normal_kind == 1) sig = T[1];
-    else if (p.normal_kind == 2) sig = T[1] + p.normal_coef * (sig - T[1]);
-    else if (p.normal_kind == 3)
-      sig = T[1] + exp(-(fabs(dV[0]) + p.normal_V) * p.normal_coef) * (sig - T[1]);
-    p.sigma[k] = sig;
-    double mu;
-    if (p.friction == 2) {
-      bool fail = false;
-      const double vold = p.V[k], th0 = p.theta[k];
-      const double th1 = rsf_theta(p, k, th0, vold);
-      double vnew = rsf_V(p, k, T[0], sig, th1, th0, p.Z[k], fail);
-      const double th2 = rsf_theta(p, k, th0, 0.5 * (vold + vnew));
-      vnew = rsf_V(p, k, T[0], sig, th2, th0, p.Z[k], fail);
-      if (fail) atomicExch(p.error, kErrNR);
-      p.theta[k] = th2;
-      mu = rsf_mu(p, k, vnew, th2);
-      T[0] = copysign(fabs(-mu * sig), T[0]);
-      // T_stick is undefined on this branch of the reference (bc_dynflt.f90:581)
-      Ts[0] = 0.0;
-      Ts[1] = 0.0;
+__device__ void fault_node_update(const FaultParams<real> &p, int k, int it, const double *f1in,
+                                  const double *f2in) {
+  const int nd = p.ndof, nf = p.nflt;
+  double f1[2] = {0, 0}, f2[2] = {0, 0}, d1[2] = {0, 0}, d2[2] = {0, 0};
+  double v1[2] = {0, 0}, v2[2] = {0, 0}, dD[2] = {0, 0}, dV[2] = {0, 0}, dA[2] = {0, 0};
+  double T[2] = {0, 0}, Ts[2] = {0, 0};
+  for (int c = 0; c < nd; ++c) {
+    const int o1 = (0 * nd + c) * nf + k, o2 = (1 * nd + c) * nf + k;
+    f1[c] = f1in[c];
+    d1[c] = p.d64[o1];
+    v1[c] = p.v64[o1];
+    if (p.scheme == 1) v1[c] = v1[c] + p.cpred * p.a64[o1];
+    if (p.two) {
+      f2[c] = f2in[c];
+      d2[c] = p.d64[o2];
+      v2[c] = p.v64[o2];
+      if (p.scheme == 1) v2[c] = v2[c] + p.cpred * p.a64[o2];
+      dD[c] = d2[c] - d1[c];
+      dV[c] = v2[c] - v1[c];
+      dA[c] = p.invM2[k + nf * c] * f2[c] - p.invM1[k + nf * c] * f1[c];
     } else {
-      double th = p.theta[k];
-      if (p.coefA2D == 0.0) {
-        if (p.swf_healing) {
-          th = th + fabs(dV[0]) * p.dt;
-          if (fabs(dV[0]) < 1.0e-14) th = 0.0;
-        } else {
-          th = fabs(dD[0]);
-        }
+      dD[c] = -2.0 * d1[c];
+      dV[c] = -2.0 * v1[c];
+      dA[c] = -2.0 * p.invM1[k + nf * c] * f1[c];
+    }
+    T[c] = p.Z[k + nf * c] * (dV[c] + p.coefA2V * dA[c]);
+  }
+  const double nx = p.n1[k], nz = p.n1[k + nf];
+  if (nd == 2) {
+    double r0, r1;
+    r0 = nz * dD[0] - nx * dD[1]; r1 = nx * dD[0] + nz * dD[1]; dD[0] = r0; dD[1] = r1;
+    r0 = nz * dV[0] - nx * dV[1]; r1 = nx * dV[0] + nz * dV[1]; dV[0] = r0; dV[1] = r1;
+    r0 = nz * dA[0] - nx * dA[1]; r1 = nx * dA[0] + nz * dA[1]; dA[0] = r0; dA[1] = r1;
+    r0 = nz * T[0] - nx * T[1];   r1 = nx * T[0] + nz * T[1];   T[0] = r0;  T[1] = r1;
+  }
+  if (!p.two || nd == 1) T[1] = 0.0;
+  T[0] = T[0] + p.T0[k];
+  T[1] = T[1] + p.T0[k + nf];
+  if (p.opening) T[1] = T[1] < 0.0 ? T[1] : 0.0;
+  double sig = p.sigma[k];
+  if (p.normal_kind == 1) sig = T[1];
+  else if (p.normal_kind == 2) sig = T[1] + p.normal_coef * (sig - T[1]);
+  else if (p.normal_kind == 3)
+    sig = T[1] + exp(-(fabs(dV[0]) + p.normal_V) * p.normal_coef) * (sig - T[1]);
+  p.sigma[k] = sig;
+  double mu;
+  if (p.friction == 2) {
+    bool fail = false;
+    const double vold = p.V[k], th0 = p.theta[k];
+    const double th1 = rsf_theta(p, k, th0, vold);
+    double vnew = rsf_V(p, k, T[0], sig, th1, th0, p.Z[k], fail);
+    const double th2 = rsf_theta(p, k, th0, 0.5 * (vold + vnew));
+    vnew = rsf_V(p, k, T[0], sig, th2, th0, p.Z[k], fail);
+    if (fail) atomicExch(p.error, kErrNR);
+    p.theta[k] = th2;
+    mu = rsf_mu(p, k, vnew, th2);
+    T[0] = copysign(fabs(-mu * sig), T[0]);
+    // T_stick is undefined on this branch of the reference (bc_dynflt.f90:581)
+    Ts[0] = 0.0;
+    Ts[1] = 0.0;
+  } else {
+    double th = p.theta[k];
+    if (p.coefA2D == 0.0) {
+      if (p.swf_healing) {
+        th = th + fabs(dV[0]) * p.dt;
+        if (fabs(dV[0]) < 1.0e-14) th = 0.0;
       } else {
-        th = fabs(p.D[k]);
+        th = fabs(dD[0]);
       }
-      p.theta[k] = th;
-      mu = swf_mu(p, k, th);
-      const double strength = p.coh[k] - mu * sig;
-      Ts[0] = T[0];
-      Ts[1] = T[1];
-      const double at = fabs(T[0]);
-      T[0] = copysign(fabs(at < strength ? at : strength), T[0]);
+    } else {
+      th = fabs(p.D[k]);
     }
-    p.MU[k] = mu;
-    T[0] = T[0] - p.T0[k];
-    T[1] = T[1] - p.T0[k + nf];
-    p.T[k] = T[0];
-    p.T[k + nf] = T[1];
-    p.Tstick[k] = Ts[0] - p.T0[k];
-    p.Tstick[k + nf] = Ts[1] - p.T0[k + nf];
-    double Tx[2] = {T[0], T[1]};
-    if (nd == 2) {
-      Tx[0] = nz * T[0] + nx * T[1];
-      Tx[1] = -nx * T[0] + nz * T[1];
-    }
+    p.theta[k] = th;
+    mu = swf_mu(p, k, th);
+    const double strength = p.coh[k] - mu * sig;
+    Ts[0] = T[0];
+    Ts[1] = T[1];
+    const double at = fabs(T[0]);
+    T[0] = copysign(fabs(at < strength ? at : strength), T[0]);
+  }
+  p.MU[k] = mu;
+  T[0] = T[0] - p.T0[k];
+  T[1] = T[1] - p.T0[k + nf];
+  p.T[k] = T[0];
+  p.T[k + nf] = T[1];
+  p.Tstick[k] = Ts[0] - p.T0[k];
+  p.Tstick[k + nf] = Ts[1] - p.T0[k + nf];
+  double Tx[2] = {T[0], T[1]};
+  if (nd == 2) {
+    Tx[0] = nz * T[0] + nx * T[1];
+    Tx[1] = -nx * T[0] + nz * T[1];
+  }
+  for (int c = 0; c < nd; ++c) {
+    const double dAc = dA[c] - T[c] / (p.Z[k + nf * c] * p.coefA2V);
+    p.D[k + nf * c] = dD[c] + p.coefA2D * dAc;
+    p.V[k + nf * c] = dV[c] + p.coefA2V * dAc;
+  }
+  for (int side = 0; side < 1 + p.two; ++side) {
+    const int J = side == 0 ? p.jf1 : p.jf2;
     for (int c = 0; c < nd; ++c) {
-      const double dAc = dA[c] - T[c] / (p.Z[k + nf * c] * p.coefA2V);
-      p.D[k + nf * c] = dD[c] + p.coefA2D * dAc;
-      p.V[k + nf * c] = dV[c] + p.coefA2V * dAc;
-    }
-    // finish the two split nodes: boundary term, inverse mass, time update
-    for (int side = 0; side < 1 + p.two; ++side) {
-      const int J = side == 0 ? p.jf1 : p.jf2;
-      for (int c = 0; c < nd; ++c) {
-        const int o = (side * nd + c) * nf + k;
-        const double f = side == 0 ? f1[c] + p.B[k] * Tx[c] : f2[c] - p.B[k] * Tx[c];
-        const double vp = side == 0 ? v1[c] : v2[c];
-        const double dc = side == 0 ? d1[c] : d2[c];
-        const double a = p.rm[o] * f;
-        const double vn = vp + p.cv * a;
-        const double dn = p.scheme == 1 ? (dc + p.dt * vn) + p.cd2 * a : dc + p.dt * vn;
-        p.d64[o] = dn;
-        p.v64[o] = vn;
-        p.a64[o] = a;
-        const long long g = c * p.plane + (long long)J * p.pitch + k;
-        p.Dnext[g] = real(dn);
-        p.Vnext[g] = real(vn);
-        if (p.Anext) p.Anext[g] = real(a);
-      }
-    }
-    fault_record(p, k, it);
-  }
-  // the last block to finish advances the step counter
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    const unsigned prev = atomicAdd(p.done, 1u);
-    if (prev == gridDim.x - 1) {
-      *p.done = 0u;
-      __threadfence();
-      *p.step = it;
+      const int o = (side * nd + c) * nf + k;
+      const double f = side == 0 ? f1[c] + p.B[k] * Tx[c] : f2[c] - p.B[k] * Tx[c];
+      const double vp = side == 0 ? v1[c] : v2[c];
+      const double dc = side == 0 ? d1[c] : d2[c];
+      const double a = p.rm[o] * f;
+      const double vn = vp + p.cv * a;
+      const double dn = p.scheme == 1 ? (dc + p.dt * vn) + p.cd2 * a : dc + p.dt * vn;
+      p.d64[o] = dn;
+      p.v64[o] = vn;
+      p.a64[o] = a;
+      const long long g = c * p.plane + (long long)J * p.pitch + k;
+      p.Dnext[g] = real(dn);
+      p.Vnext[g] = real(vn);
+      if (p.Anext) p.Anext[g] = real(a);
     }
   }
+  fault_record(p, k, it);
 }
 
-// step counter only (no fault)
-__global__ void advance_kernel(int *step) { *step = *step + 1; }
-
-// seismograms (REC_store, receivers.f90:309-344), after the step counter moved
+// interpolated seismograms of velocity or acceleration (REC_store,
+// receivers.f90:309-344), after the bulk kernel moved the step counter
 template <typename real>
 __global__ void receiver_kernel(RecParams<real> p) {
   const int it = *p.step;

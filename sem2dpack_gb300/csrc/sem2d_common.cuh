@@ -20,65 +20,7 @@ constexpr int kMaxN = 9;          // largest NGLL compiled
 constexpr int kBulkThreads = 256; // threads of the bulk kernel
 constexpr int kMaxSrc = 64;
 
-// Parameters of the fused element-force + assembly + update kernel.
-template <typename real, int N>
-struct BulkParams {
-  // lattice
-  int LX, LZ, pitch;
-  long long plane;
-  int nx, nz;
-  const int *row0;  // [nz+1]; row0[nz] = LZ
-  int TX, TZ;       // tile of elements per CTA
-  // GLL operator
-  real H[N * N];    // H(i,j) = h'_i(x_j), column-major
-  real w[N];
-  // state (ping-pong buffers chosen by the host)
-  const real *Dcur;
-  real *Dnext;
-  const real *Vcur;
-  real *Vnext;
-  const real *Acur;
-  real *Anext;      // null unless accelerations are kept
-  // material
-  int mat_iso;      // isotropic: planes (la, mu) [P-SV] or (mu) [SH]
-  const real *mat[4];
-  int mat_elem;     // 1: per element GLL point (structured element order)
-  const real *kveta;// per element GLL point or null
-  const real *rmass;// lattice plane (both dofs equal away from the perimeter)
-  // element geometry (rectilinear): per column / per row
-  const real *xix;    // dxi/dx  of element column
-  const real *etaz;   // deta/dz of element row
-  const real *dxdxi;  // dx/dxi  of element column
-  const real *dzdeta; // dz/deta of element row
-  // perimeter table: slot -> rmass(dof), dashpots Ca(dof), Cb(dof)
-  const real *per_rm, *per_Ca, *per_Cb;
-  // fault rows (lattice rows of side 1 and side 2, -1 if none)
-  int jf1, jf2;
-  real *f_flt;      // [(side*ndof + c)*LX + I] raw forces for the fault kernel
-  // point sources
-  int nsrc;
-  const int *src_I, *src_J;
-  const double *src_amp;  // [(s*ndof + c)*(nt+1) + it]
-  int nt;
-  const int *step;        // completed steps (device counter)
-  // time scheme
-  int scheme;             // 0 leapfrog, 1 Newmark (beta = 0)
-  real dt, cv, cpred, cd2;// cv: coef a->v, cpred: (1-gamma)dt, cd2: (0.5-beta)dt^2
-  int kd2;
-};
-
-// Perimeter slot of lattice node (I,J): bottom row, top row, left column,
-// right column (corners belong to the rows).
-__host__ __device__ inline int perimeter_slot(int I, int J, int LX, int LZ) {
-  if (J == 0) return I;
-  if (J == LZ - 1) return LX + I;
-  if (I == 0) return 2 * LX + (J - 1);
-  if (I == LX - 1) return 2 * LX + (LZ - 2) + (J - 1);
-  return -1;
-}
-__host__ __device__ inline int perimeter_slots(int LX, int LZ) { return 2 * LX + 2 * (LZ - 2); }
-
-// Parameters of the per-step fault + bookkeeping kernel (FP64 fault state).
+// Parameters of the per-node fault update (FP64 fault state).
 template <typename real>
 struct FaultParams {
   int ndof, LX, pitch;
@@ -108,10 +50,81 @@ struct FaultParams {
   // time scheme
   int scheme;
   double dt, cv, cpred, cd2;
-  int *step;            // incremented by the last block
+  int *step;            // incremented by the last block (stand-alone kernel)
   unsigned int *done;   // block completion counter (reset by the last block)
   int *error;           // sticky device error flag (SEM2D_E_*)
 };
+
+// Parameters of the fused element-force + assembly + update kernel.
+template <typename real, int N>
+struct BulkParams {
+  // lattice
+  int LX, LZ, pitch;
+  long long plane;
+  int nx, nz;
+  const int *row0;  // [nz+1]; row0[nz] = LZ
+  int TX;           // element columns per CTA tile
+  const int *ztile; // [ntz+1] element-row boundaries of the tile rows
+  // GLL operator
+  real H[N * N];    // H(i,j) = h'_i(x_j), column-major
+  real w[N];
+  // state (ping-pong buffers chosen by the host)
+  const real *Dcur;
+  real *Dnext;
+  const real *Vcur;
+  real *Vnext;
+  const real *Acur;
+  real *Anext;      // null unless accelerations are kept
+  // material
+  int mat_iso;      // isotropic: planes (la, mu) [P-SV] or (mu) [SH]
+  const real *mat[4];
+  int mat_elem;     // 1: per element GLL point (structured element order)
+  const real *kveta;// per element GLL point or null
+  const real *rmass;// lattice plane (both dofs equal away from the perimeter)
+  // element geometry (rectilinear): per column / per row
+  const real *xix;    // dxi/dx  of element column
+  const real *etaz;   // deta/dz of element row
+  const real *dxdxi;  // dx/dxi  of element column
+  const real *dzdeta; // dz/deta of element row
+  // perimeter table: slot -> rmass(dof), dashpots Ca(dof), Cb(dof)
+  const real *per_rm, *per_Ca, *per_Cb;
+  // fault rows (lattice rows of side 1 and side 2, -1 if none); a tile row
+  // always holds both rows, so the owning CTA finishes the fault nodes
+  int jf1, jf2;
+  int has_fault;
+  FaultParams<real> flt;
+  // point sources
+  int nsrc;
+  const int *src_I, *src_J;
+  const double *src_amp;  // [(s*ndof + c)*(nt+1) + it]
+  int nt;
+  int *step;              // completed steps (device counter, bumped by the last CTA)
+  unsigned int *done;     // CTA completion counter
+  // receivers sampled by the CTA that owns them: node receivers (D, V or A)
+  // and interpolated receivers of D
+  int rec_nsamp, rec_isamp, rec_nrec, rec_npts;
+  char rec_field;
+  const int *rec_tile_start;  // [ntiles+1] into rec_ids
+  const int *rec_ids;         // receiver numbers grouped by tile
+  const int *rec_I, *rec_J;   // [r*npts + q] lattice position
+  const double *rec_w;        // [r*npts + q] weight
+  double *sis;
+  // time scheme
+  int scheme;             // 0 leapfrog, 1 Newmark (beta = 0)
+  real dt, cv, cpred, cd2;// cv: coef a->v, cpred: (1-gamma)dt, cd2: (0.5-beta)dt^2
+  int kd2;
+};
+
+// Perimeter slot of lattice node (I,J): bottom row, top row, left column,
+// right column (corners belong to the rows).
+__host__ __device__ inline int perimeter_slot(int I, int J, int LX, int LZ) {
+  if (J == 0) return I;
+  if (J == LZ - 1) return LX + I;
+  if (I == 0) return 2 * LX + (J - 1);
+  if (I == LX - 1) return 2 * LX + (LZ - 2) + (J - 1);
+  return -1;
+}
+__host__ __device__ inline int perimeter_slots(int LX, int LZ) { return 2 * LX + 2 * (LZ - 2); }
 
 template <typename real>
 struct RecParams {

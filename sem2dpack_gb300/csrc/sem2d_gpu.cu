@@ -51,7 +51,9 @@ struct sem2d_handle {
   std::vector<int> row0;             // [nz+1]
   std::vector<long long> glob2lat;   // global node -> J*pitch + I
   std::vector<int> elem_ex, elem_ez; // reference element -> structured position
-  int TX = 8, TZ = 8, tile_nodes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
+  int TX = 8, TZ = 8, tile_nodes = 0, own_nodes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
+  std::vector<int> ztile;            // tile-row boundaries (element rows)
+  int *d_ztile = nullptr;
   bool keep_accel = false;
   // device memory
   cudaStream_t stream = nullptr;
@@ -59,7 +61,7 @@ struct sem2d_handle {
   void *D[2] = {nullptr, nullptr}, *V[2] = {nullptr, nullptr}, *A[2] = {nullptr, nullptr};
   void *mat[4] = {nullptr, nullptr, nullptr, nullptr};
   void *kveta = nullptr, *rmass = nullptr, *geo[4] = {nullptr, nullptr, nullptr, nullptr};
-  void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr, *f_flt = nullptr;
+  void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
   int *d_row0 = nullptr, *d_step = nullptr, *d_error = nullptr;
   unsigned *d_done = nullptr;
   // sources
@@ -69,8 +71,10 @@ struct sem2d_handle {
   // receivers
   int nrec = 0, rec_isamp = 1, rec_nsamp = 0, rec_npts = 1;
   char rec_field = 'V';
+  bool rec_separate = false;          // interpolated V/A: own kernel after the step
   int *rec_lat = nullptr;
   double *rec_w = nullptr, *sis = nullptr;
+  int *rec_tile_start = nullptr, *rec_ids = nullptr, *rec_I = nullptr, *rec_J = nullptr;
   // fault
   int nflt = 0, two = 0, jf1 = -1, jf2 = -1, onx = 0, fnsamp = 0, friction = 0;
   std::vector<double> h_fault_init;  // V0, theta for reset
@@ -442,7 +446,7 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.two = h->two;
   f.jf1 = h->jf1;
   f.jf2 = h->jf2;
-  f.f_flt = (const real *)h->f_flt;
+  f.f_flt = nullptr;
   f.Dcur = (const real *)h->D[cur];
   f.Dnext = (real *)h->D[1 - cur];
   f.Vnext = (real *)h->V[1 - cur];
@@ -525,12 +529,13 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   bc.ndof = h->ndof;
   bc.mixed = h->mixed;
   bc.tile_nodes = h->tile_nodes;
+  bc.own_nodes = h->own_nodes;
   bc.nmat = h->nmat;
   bc.has_kv = h->has_kv;
   bc.mat_elem = h->mat_elem;
   bc.mat_iso = h->mat_iso;
   bc.grid_x = (h->nx + h->TX - 1) / h->TX;
-  bc.grid_y = (h->nz + h->TZ - 1) / h->TZ;
+  bc.grid_y = int(h->ztile.size()) - 1;
   bc.LX = h->LX;
   bc.LZ = h->LZ;
   bc.pitch = h->pitch;
@@ -539,7 +544,7 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   bc.nz = h->nz;
   bc.row0 = h->d_row0;
   bc.TX = h->TX;
-  bc.TZ = h->TZ;
+  bc.ztile = h->d_ztile;
   bc.Dcur = h->D[cur];
   bc.Dnext = h->D[1 - cur];
   bc.Vcur = h->V[cur];
@@ -555,13 +560,32 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   bc.per_Cb = h->per_Cb;
   bc.jf1 = h->nflt ? h->jf1 : -1;
   bc.jf2 = h->nflt ? h->jf2 : -1;
-  bc.f_flt = h->f_flt;
+  bc.has_fault = h->nflt ? 1 : 0;
+  FaultParams<real> f{};
+  if (h->nflt) {
+    f = fault_params<real>(h, cur);
+    bc.flt = &f;
+  }
   bc.nsrc = h->nsrc;
   bc.src_I = h->src_I;
   bc.src_J = h->src_J;
   bc.src_amp = h->src_amp;
   bc.nt = h->nt;
   bc.step = h->d_step;
+  bc.done = h->d_done;
+  if (h->nrec && !h->rec_separate) {
+    bc.rec_nsamp = h->rec_nsamp;
+    bc.rec_isamp = h->rec_isamp;
+    bc.rec_nrec = h->nrec;
+    bc.rec_npts = h->rec_npts;
+    bc.rec_field = h->rec_field;
+    bc.rec_tile_start = h->rec_tile_start;
+    bc.rec_ids = h->rec_ids;
+    bc.rec_I = h->rec_I;
+    bc.rec_J = h->rec_J;
+    bc.rec_w = h->rec_w;
+    bc.sis = h->sis;
+  }
   bc.scheme = h->scheme;
   bc.dt = h->dt;
   bc.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
@@ -576,16 +600,8 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
   h->launches++;
   if (ev) CK(cudaEventRecord(ev[1], h->stream));
-  if (h->nflt) {
-    FaultParams<real> f = fault_params<real>(h, cur);
-    fault_step_kernel<real><<<(h->nflt + 127) / 128, 128, 0, h->stream>>>(f);
-  } else {
-    advance_kernel<<<1, 1, 0, h->stream>>>(h->d_step);
-  }
-  CK(cudaGetLastError());
-  h->launches++;
   if (ev) CK(cudaEventRecord(ev[2], h->stream));
-  if (h->nrec) {
+  if (h->nrec && h->rec_separate) {
     RecParams<real> r{};
     r.nrec = h->nrec;
     r.ndof = h->ndof;
@@ -595,8 +611,8 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     r.plane = h->plane;
     r.lat = h->rec_lat;
     r.w = h->rec_w;
-    // after the step: d^n is the buffer read (cur), v and a the ones written
-    r.field = (const real *)(h->rec_field == 'D' ? h->D[cur] : (h->rec_field == 'A' ? h->A[1 - cur] : h->V[1 - cur]));
+    // after the step: velocity and acceleration are the buffers just written
+    r.field = (const real *)(h->rec_field == 'A' ? h->A[1 - cur] : h->V[1 - cur]);
     r.sis = h->sis;
     r.step = h->d_step;
     const int nthr = h->nrec * h->ndof;
@@ -618,7 +634,7 @@ int launch_steps(sem2d_handle *h, int n) {
   return SEM2D_OK;
 }
 
-int kernels_per_step(const sem2d_handle *h) { return 2 + (h->nrec ? 1 : 0); }
+int kernels_per_step(const sem2d_handle *h) { return 1 + (h->nrec && h->rec_separate ? 1 : 0); }
 
 int ensure_graph(sem2d_handle *h) {
   if (h->graph_exec) return SEM2D_OK;
@@ -733,11 +749,6 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
       h->A[b] = p;
     }
   }
-  {
-    char *p;
-    if ((st = dalloc(h, &p, rs * 2 * h->ndof * std::max(h->LX, 1)))) return st;
-    h->f_flt = p;
-  }
   if ((st = dupload(h, &h->d_row0, h->row0))) return st;
   if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)))
     return st;
@@ -775,43 +786,76 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
     h->rec_field = d->rec_field;
     if (h->rec_field != 'D' && h->rec_field != 'V' && h->rec_field != 'A')
       return set_err(h, SEM2D_E_ARG, "rec_field must be D, V or A");
-    std::vector<int> lat;
+    if (!d->rec_node && (!d->rec_elem || !d->rec_interp))
+      return set_err(h, SEM2D_E_ARG, "receivers need nodes or interpolation");
+    h->rec_npts = d->rec_node ? 1 : h->N * h->N;
+    // interpolated velocity/acceleration reads nodes owned by several CTAs:
+    // sampled by a separate kernel after the step; everything else is
+    // sampled inside the bulk kernel by the CTA that owns the receiver
+    h->rec_separate = !d->rec_node && h->rec_field != 'D';
+  }
+  if ((st = dalloc(h, &h->sis, (size_t)std::max(h->rec_nsamp, 1) * std::max(h->nrec, 1) * h->ndof))) return st;
+  // tile shape: TX element columns by ztile rows, fault split kept inside a tile
+  if (choose_tiles(h->N, h->ndof, h->mixed, h->nx, h->nz, h->row0.data(), h->nmat, h->has_kv,
+                   h->mat_elem, &h->TX, &h->TZ))
+    return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no tile shape fits: ") + bulk_last_error());
+  h->ztile = tile_rows(h->N, h->nz, h->row0.data(), h->TZ);
+  tile_sizes(h->N, h->nx, h->row0.data(), h->TX, h->ztile, &h->tile_nodes, &h->own_nodes);
+  if ((st = dupload(h, &h->d_ztile, h->ztile))) return st;
+  if (h->nrec) {
+    // receiver lattice positions; for the fused path, grouped by owning tile
+    const int gx = (h->nx + h->TX - 1) / h->TX, gy = int(h->ztile.size()) - 1;
+    std::vector<int> tileJ(h->LZ, -1);  // lattice row -> tile row owning it
+    for (int y = 0; y < gy; ++y)
+      for (int J = h->row0[h->ztile[y]]; J < h->row0[h->ztile[y + 1]]; ++J) tileJ[J] = y;
+    std::vector<int> etile(h->nz, -1);
+    for (int y = 0; y < gy; ++y)
+      for (int z = h->ztile[y]; z < h->ztile[y + 1]; ++z) etile[z] = y;
+    std::vector<int> rI, rJ, lat, owner(h->nrec);
     std::vector<double> w;
-    if (d->rec_node) {
-      h->rec_npts = 1;
-      for (int r = 0; r < h->nrec; ++r) {
+    const int NN = h->N * h->N;
+    for (int r = 0; r < h->nrec; ++r) {
+      if (d->rec_node) {
         const int p = d->rec_node[r] - 1;
         if (p < 0 || p >= d->npoin) return set_err(h, SEM2D_E_ARG, "receiver node out of range");
-        lat.push_back(int(h->glob2lat[p]));
+        const long long L = h->glob2lat[p];
+        const int I = int(L % h->pitch), J = int(L / h->pitch);
+        rI.push_back(I);
+        rJ.push_back(J);
+        lat.push_back(int(L));
         w.push_back(1.0);
-      }
-    } else {
-      if (!d->rec_elem || !d->rec_interp) return set_err(h, SEM2D_E_ARG, "receivers need nodes or interpolation");
-      const int NN = h->N * h->N;
-      h->rec_npts = NN;
-      for (int r = 0; r < h->nrec; ++r) {
+        const int x = std::min(I / (h->TX * (h->N - 1)), gx - 1);
+        owner[r] = tileJ[J] * gx + x;
+      } else {
         const int e = d->rec_elem[r] - 1;
         if (e < 0 || e >= d->nelem) return set_err(h, SEM2D_E_ARG, "receiver element out of range");
         for (int q = 0; q < NN; ++q) {
-          lat.push_back(int(h->glob2lat[d->ibool[q + (size_t)NN * e] - 1]));
+          const long long L = h->glob2lat[d->ibool[q + (size_t)NN * e] - 1];
+          rI.push_back(int(L % h->pitch));
+          rJ.push_back(int(L / h->pitch));
+          lat.push_back(int(L));
           w.push_back(d->rec_interp[q + (size_t)NN * r]);
         }
+        owner[r] = etile[h->elem_ez[e]] * gx + h->elem_ex[e] / h->TX;
       }
     }
+    std::vector<int> start(gx * gy + 1, 0), ids(h->nrec);
+    for (int r = 0; r < h->nrec; ++r) start[owner[r] + 1]++;
+    for (int k = 0; k < gx * gy; ++k) start[k + 1] += start[k];
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int r = 0; r < h->nrec; ++r) ids[fill[owner[r]]++] = r;
     if ((st = dupload(h, &h->rec_lat, lat)) || (st = dupload(h, &h->rec_w, w)) ||
-        (st = dalloc(h, &h->sis, (size_t)h->rec_nsamp * h->nrec * h->ndof)))
+        (st = dupload(h, &h->rec_I, rI)) || (st = dupload(h, &h->rec_J, rJ)) ||
+        (st = dupload(h, &h->rec_tile_start, start)) || (st = dupload(h, &h->rec_ids, ids)))
       return st;
   }
-  // tile shape
-  if ((st = choose_tiles(h->N, h->ndof, h->mixed, h->nx, h->nz, h->row0.data(), h->nmat, h->has_kv,
-                         h->mat_elem, &h->TX, &h->TZ, &h->tile_nodes)))
-    return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no tile shape fits: ") + bulk_last_error());
   {
     BulkConfig bc;
     bc.N = h->N;
     bc.ndof = h->ndof;
     bc.mixed = h->mixed;
     bc.tile_nodes = h->tile_nodes;
+    bc.own_nodes = h->own_nodes;
     bc.nmat = h->nmat;
     bc.has_kv = h->has_kv;
     bc.mat_elem = h->mat_elem;
