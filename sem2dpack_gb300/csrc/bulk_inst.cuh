@@ -93,6 +93,28 @@ int launch_typed(const BulkConfig &c) {
   return 0;
 }
 
+template <typename real, int N, int NDOF, bool MELEM>
+int occupancy_typed(const BulkConfig &c) {
+  const size_t smem = bulk_smem_bytes<real, N, NDOF>(c.tile_nodes, c.own_nodes, c.nmat, c.has_kv, c.mat_elem);
+  if (configure_typed<real, N, NDOF, MELEM>(c)) return 0;
+  int nb = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, bulk_step_kernel<real, N, NDOF, MELEM>, kBulkThreads,
+                                                    smem) != cudaSuccess)
+    return 0;
+  return nb;
+}
+
+template <typename real, int N, int NDOF>
+int occupancy_m(const BulkConfig &c) {
+  return c.mat_elem ? occupancy_typed<real, N, NDOF, true>(c) : occupancy_typed<real, N, NDOF, false>(c);
+}
+
+template <int N>
+int occupancy_for_n(const BulkConfig &c) {
+  if (c.ndof == 1) return c.mixed ? occupancy_m<float, N, 1>(c) : occupancy_m<double, N, 1>(c);
+  return c.mixed ? occupancy_m<float, N, 2>(c) : occupancy_m<double, N, 2>(c);
+}
+
 template <typename real, int N, int NDOF>
 int configure_m(const BulkConfig &c) {
   return c.mat_elem ? configure_typed<real, N, NDOF, true>(c) : configure_typed<real, N, NDOF, false>(c);

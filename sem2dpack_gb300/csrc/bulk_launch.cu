@@ -31,6 +31,15 @@ int configure_bulk(const BulkConfig &c) {
   }
 }
 
+int occupancy_bulk(const BulkConfig &c) {
+  switch (c.N) {
+    case 5: return occupancy_bulk_n5(c);
+    case 6: return occupancy_bulk_n6(c);
+    case 9: return occupancy_bulk_n9(c);
+    default: return 0;
+  }
+}
+
 size_t bulk_smem(int N, int ndof, int mixed, int tn, int on, int nmat, int kv, int me) {
   switch (N) {
     case 5: return bulk_smem_n5(ndof, mixed, tn, on, nmat, kv, me);
@@ -81,42 +90,63 @@ void tile_sizes(int N, int nx, const int *row0, int TX, const std::vector<int> &
 
 int choose_tiles(int N, int ndof, int mixed, int nx, int nz, const int *row0, int nmat, int has_kv,
                  int mat_elem, int *TX, int *TZ) {
-  const size_t kSmemCap = 113 * 1024;  // two CTAs per SM
-  auto fits = [&](int tx, int tz, size_t cap) {
-    int tn, on;
-    tile_sizes(N, nx, row0, tx, tile_rows(N, nz, row0, tz), &tn, &on);
-    return bulk_smem(N, ndof, mixed, tn, on, nmat, has_kv, mat_elem) <= cap;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
+  auto eval = [&](int tx, int tz, double *cost) -> bool {
+    const std::vector<int> zt = tile_rows(N, nz, row0, tz);
+    BulkConfig c;
+    c.N = N;
+    c.ndof = ndof;
+    c.mixed = mixed;
+    c.nmat = nmat;
+    c.has_kv = has_kv;
+    c.mat_elem = mat_elem;
+    tile_sizes(N, nx, row0, tx, zt, &c.tile_nodes, &c.own_nodes);
+    if (bulk_smem(N, ndof, mixed, c.tile_nodes, c.own_nodes, nmat, has_kv, mat_elem) > 227 * 1024) return false;
+    const int per_sm = occupancy_bulk(c);
+    if (per_sm <= 0) return false;
+    const long long ntiles = (long long)((nx + tx - 1) / tx) * (long long)(zt.size() - 1);
+    const long long waves = (ntiles + (long long)per_sm * nsm - 1) / ((long long)per_sm * nsm);
+    // work of the slowest SM: waves x elements computed per tile (with halo)
+    const double per_tile = double(std::min(tx, nx) + (nx > tx ? 1 : 0)) * double(std::min(tz, nz) + (nz > tz ? 1 : 0));
+    *cost = double(waves) * per_tile + 1e-3 * per_tile;
+    return true;
   };
   const char *env = std::getenv("SEM2D_TILE");
   if (env) {
     int tx = 0, tz = 0;
+    double cost;
     if (std::sscanf(env, "%dx%d", &tx, &tz) == 2 && tx > 0 && tz > 0) {
-      if (fits(tx, tz, 227 * 1024)) {
+      if (eval(tx, tz, &cost)) {
         *TX = tx;
         *TZ = tz;
         return 0;
       }
-      g_bulk_err = "SEM2D_TILE does not fit in shared memory";
+      g_bulk_err = "SEM2D_TILE does not fit";
       return 1;
     }
   }
-  static const int cand[][2] = {{16, 8}, {8, 8}, {8, 4}, {4, 4}, {4, 2}, {2, 2}, {1, 1}};
-  for (const auto &c : cand) {
-    const long long ntiles = (long long)((nx + c[0] - 1) / c[0]) * ((nz + c[1] - 1) / c[1]);
-    if (!fits(c[0], c[1], kSmemCap)) continue;
-    if (ntiles < 2 * 152 && !(c[0] == 1 && c[1] == 1)) continue;  // keep every SM busy
-    *TX = c[0];
-    *TZ = c[1];
-    return 0;
-  }
-  for (int k = int(sizeof(cand) / sizeof(cand[0])) - 1; k >= 0; --k)
-    if (fits(cand[k][0], cand[k][1], kSmemCap)) {
-      *TX = cand[k][0];
-      *TZ = cand[k][1];
-      return 0;
+  double best = 1e300;
+  int bx = 0, bz = 0;
+  for (int tx = 1; tx <= 32; ++tx)
+    for (int tz = 1; tz <= 16; ++tz) {
+      if (tx > nx || tz > nz) continue;
+      double cost;
+      if (!eval(tx, tz, &cost)) continue;
+      if (cost < best) {
+        best = cost;
+        bx = tx;
+        bz = tz;
+      }
     }
-  g_bulk_err = "no tile fits in shared memory";
-  return 1;
+  if (bx == 0) {
+    g_bulk_err = "no tile fits in shared memory";
+    return 1;
+  }
+  *TX = bx;
+  *TZ = bz;
+  return 0;
 }
 
 }  // namespace sem2d

@@ -62,7 +62,9 @@ void tile_sizes(int N, int nx, const int *row0, int TX, const std::vector<int> &
 size_t bulk_smem(int N, int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv,
                  int mat_elem);
 
-// picks the tile shape (SEM2D_TILE=TXxTZ overrides); 0 on success
+// picks the tile shape minimising (waves x recomputed elements per tile)
+// for the device's SM count and the kernel's occupancy; SEM2D_TILE=TXxTZ
+// overrides.  0 on success.
 int choose_tiles(int N, int ndof, int mixed, int nx, int nz, const int *row0, int nmat, int has_kv,
                  int mat_elem, int *TX, int *TZ);
 
@@ -73,6 +75,11 @@ int launch_bulk_n9(const BulkConfig &c);
 int configure_bulk_n5(const BulkConfig &c);
 int configure_bulk_n6(const BulkConfig &c);
 int configure_bulk_n9(const BulkConfig &c);
+int occupancy_bulk_n5(const BulkConfig &c);
+int occupancy_bulk_n6(const BulkConfig &c);
+int occupancy_bulk_n9(const BulkConfig &c);
+// resident CTAs per SM for the configuration's shared memory (0 if none)
+int occupancy_bulk(const BulkConfig &c);
 size_t bulk_smem_n5(int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv, int mat_elem);
 size_t bulk_smem_n6(int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv, int mat_elem);
 size_t bulk_smem_n9(int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv, int mat_elem);
