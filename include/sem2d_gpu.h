@@ -220,6 +220,64 @@ int sem2d_gpu_destroy(sem2d_handle *h);
  * h is NULL). */
 const char *sem2d_gpu_last_error(sem2d_handle *h);
 
+/* ---- stepping caller-owned device arrays without allocating ----------
+ *
+ * Device lattice layout.  The library stores a Cartesian problem on the
+ * structured lattice of GLL nodes: LX = nx*(ngll-1)+1 columns and LZ rows,
+ * element row ez starting at lattice row row0[ez] (row0[nz] = LZ).  A nodal
+ * field is ndof planes of pitch*LZ values, value (I,J) of dof c at
+ * [c*pitch*LZ + J*pitch + I].  Values are double for SEM2D_PRECISION_FP64
+ * and float for SEM2D_PRECISION_MIXED.  The state between steps is the
+ * displacement of the next step (the reference's displ + dt*veloc for
+ * leapfrog) and the velocity (the reference's veloc). */
+typedef struct sem2d_lattice_args {
+  int ngll, ndof, precision;
+  int nx, nz, LX, LZ, pitch;
+  const int *row0;            /* device, [nz+1]                              */
+  const double *hprime, *wgll;/* host, H(ngll,ngll) and the GLL weights      */
+  void *d, *v;                /* device state, updated in place              */
+  const void *rmass;          /* device plane: inverse mass                  */
+  const void *per_rm, *per_Ca, *per_Cb; /* device perimeter tables
+                                 [c*nslot + s]: inverse mass and the dashpots
+                                 of up to two absorbing sides at slot s; node
+                                 (I,J) has slot I (J=0), LX+I (J=LZ-1),
+                                 2LX+J-1 (I=0), 2LX+LZ-2+J-1 (I=LX-1), and
+                                 nslot = 2LX + 2(LZ-2)                        */
+  int mat_iso;                /* 1: planes (lambda, mu) [P-SV] or (mu) [SH];
+                                 0: (Kx, Kz, lambda, mu) [P-SV] or (mu, mux) */
+  const void *mat[4];         /* device material planes                      */
+  const void *xix, *etaz, *dxdxi, *dzdeta; /* device, per element column (x)
+                                 and row (z): dxi/dx, deta/dz, dx/dxi, dz/deta */
+  int nsrc;
+  const int *src_I, *src_J;   /* device lattice positions of the sources     */
+  const double *src_amp;      /* device ((s*ndof + c)*(nt+1) + it) amplitudes */
+  int nt;                     /* last step covered by src_amp                */
+  int step0;                  /* steps already done before this call         */
+  double dt;
+  int kd2_form;
+} sem2d_lattice_args;
+
+/* Advances nsteps leapfrog steps of the elastic bulk (element forces,
+ * sources, absorbing dashpots, inverse mass, update) on the caller's device
+ * arrays a->d, a->v, queued on `stream` (a cudaStream_t, NULL = default
+ * stream), without allocating any device memory.
+ *
+ * For callers that cannot call cudaMalloc -- code running inside another
+ * framework's memory pool (a PyTorch caching allocator that owns all device
+ * memory), inside a CUDA graph being captured, or under a fixed memory
+ * budget.  This entry point has no counterpart in the reference.  It is the
+ * bulk step kernel of sem2d_gpu_step with its scratch (the partner
+ * displacement and velocity buffers of the double-buffered update and the
+ * step and CTA counters) in one file-scope device array of
+ * SEM2D_NOALLOC_SCRATCH_BYTES that every GPU loading the library keeps until
+ * the process exits; problems whose partner buffers do not fit are rejected
+ * with SEM2D_E_ARG.  The first call on a device looks up that array's
+ * address, so make it before any stream capture.  All calls share the one
+ * array: calls that overlap on the GPU (other streams, other threads) race
+ * and must be ordered by the caller. */
+#define SEM2D_NOALLOC_SCRATCH_BYTES (8u << 20)
+int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,7 @@ PROTOTYPES = [
     ("sem2d_gpu_tile_shape", C.c_int, [vp, ip, ip]),
     ("sem2d_gpu_destroy", C.c_int, [vp]),
     ("sem2d_gpu_last_error", C.c_char_p, [vp]),
+    ("sem2d_gpu_step_noalloc", C.c_int, [C.POINTER(abi.LatticeArgs), C.c_int, vp]),
     # sem2d_host.h
     ("sem2d_grid_build", C.c_int, [C.POINTER(abi.Deck), PP]),
     ("sem2d_grid_sizes", C.c_int, [vp, ip, ip, ip]),

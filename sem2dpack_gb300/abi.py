@@ -128,3 +128,18 @@ class Deck(C.Structure):
         ("rec_field", c_char),
         ("precision", c_int), ("kd2_form", c_int),
     ]
+
+
+class LatticeArgs(C.Structure):
+    """sem2d_lattice_args: caller-owned device arrays in the lattice layout."""
+    _fields_ = [
+        ("ngll", c_int), ("ndof", c_int), ("precision", c_int),
+        ("nx", c_int), ("nz", c_int), ("LX", c_int), ("LZ", c_int), ("pitch", c_int),
+        ("row0", C.c_void_p), ("hprime", P_double), ("wgll", P_double),
+        ("d", C.c_void_p), ("v", C.c_void_p), ("rmass", C.c_void_p),
+        ("per_rm", C.c_void_p), ("per_Ca", C.c_void_p), ("per_Cb", C.c_void_p),
+        ("mat_iso", c_int), ("mat", C.c_void_p * 4),
+        ("xix", C.c_void_p), ("etaz", C.c_void_p), ("dxdxi", C.c_void_p), ("dzdeta", C.c_void_p),
+        ("nsrc", c_int), ("src_I", C.c_void_p), ("src_J", C.c_void_p), ("src_amp", C.c_void_p),
+        ("nt", c_int), ("step0", c_int), ("dt", c_double), ("kd2_form", c_int),
+    ]
