@@ -1,10 +1,11 @@
 """Benchmark of the GB300 spectral-element time step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload sh_rupture|plain_psv|psv_rsf]
+                    [--workload sh_rupture|plain_psv|psv_rsf|batch_shots]
 
 A benchmark step is one complete solve of the workload (all its time steps,
-fields reset and L2 flushed before it).  The default workload is the SH
+fields reset and L2 flushed before it; for batch_shots, 200 of the 3000 time
+steps of all 256 problems, one launch per time step for the whole batch).  The default workload is the SH
 dynamic rupture (400 x 200 elements, NGLL=5, 6000 steps, FP32 fields with
 FP64 fault state).  The metric is GLL node-steps per second.
 
@@ -51,13 +52,15 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="sh_rupture", choices=["sh_rupture", "plain_psv", "psv_rsf"])
+    p.add_argument("--workload", default="sh_rupture",
+                   choices=["sh_rupture", "plain_psv", "psv_rsf", "batch_shots"])
+    p.add_argument("--nsim", type=int, default=256, help="problems of the batch_shots workload")
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--time-steps", type=int, default=0,
-                   help="time steps per solve (default: all of the workload); for short profiling runs")
+                   help="time steps per solve (default: all of the workload, 200 for batch_shots)")
     return p.parse_args()
 
 
@@ -212,6 +215,111 @@ def run_reference(args, rank):
     }), flush=True)
 
 
+def run_batch(args, rank, world, local, torch, dist, barrier):
+    """The batched-shot configuration: many uneven P-SV problems stepped by
+    one launch per time step (sem2d_gpu_create_batch path)."""
+    from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, BatchSolver, workloads
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    nt_full = 3000
+    nt = args.time_steps or 200
+    decks = workloads.batch_shots(nsim=args.nsim, scale=args.scale, nsteps=nt_full, precision=prec)
+    sizes = {"npoin": 0, "h2d": 0, "d2h": 0}
+
+    def problems():
+        for dk in decks:
+            P = workloads.build(dk)
+            d = P.desc()
+            sizes["npoin"] += d.npoin
+            sizes["h2d"] += desc_bytes(d)
+            sizes["d2h"] += 8 * d.rec_nsamp * d.nrec * d.ndof
+            yield d
+            del P
+
+    sim = BatchSolver(problems())
+    npoin = sizes["npoin"]
+    dtype = "f32" if prec == PRECISION_MIXED else "f64"
+    name = ("batched P-SV shots: %d problems of 64^2..512^2 elements (25 m), NGLL=5, layered media, "
+            "%d GLL nodes in total" % (len(sim), npoin))
+    if args.scale != 1.0:
+        name += " (scale %.3g)" % args.scale
+    stream = torch.cuda.ExternalStream(sim.stream)
+
+    def one_solve(timed):
+        sim.reset()
+        barrier()
+        if not timed:
+            sim.step(nt)
+            sim.sync()
+            return 0.0
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(nt)
+        e1.record(stream)
+        e1.synchronize()
+        sim.sync()
+        return e0.elapsed_time(e1)
+
+    for _ in range(args.warmup):
+        one_solve(False)
+    clocks = ClockSampler(local)
+    clocks.start()
+    l0 = sim.launches
+    ms = [one_solve(True) for _ in range(args.steps)]
+    launches = sim.launches - l0
+    clk = clocks.stop()
+    total = sum(ms)
+    if dist is not None:
+        t = torch.tensor([total], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total = float(t.item())
+    value = world * npoin * nt * args.steps / (total / 1000.0)
+    sim.reset()
+    kms = sim.step_timed(nt)
+    bulk_ms = kms[0] / nt
+    bpn = BYTES_PER_NODE_STEP[(2, dtype)]
+    achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
+    peaks, peak_kind = measured_peaks()
+    traffic = ncu_traffic("batch_shots")
+    # end to end: uploads of every problem (the host arrays of the
+    # descriptors), the time steps, all seismograms back, destroy
+    barrier()
+    t0 = time.perf_counter()
+    sim.reset()
+    sim.step(nt)
+    for m in sim.members:
+        m.seismograms()
+    t_run = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sim.close()
+    t_close = time.perf_counter() - t0
+    e2e_value = world * npoin * nt / (sim.upload_seconds + t_run + t_close)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
+            "data": "synthetic",
+            "config": {"workload": name, "global_batch": len(sim.members), "seq_len": 0,
+                       "parallelism": "replicas", "npoin": npoin, "time_steps_per_step": nt,
+                       "precision": "FP32 fields" if dtype == "f32" else "FP64",
+                       "l2": "inputs larger than L2 (the batch's fields are %.1f GB)"
+                             % (npoin * bpn / 1e9)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
+                         "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
+                         "traffic": traffic, "peak_kind": peak_kind,
+                         "kernel": "strip_batch_kernel", "bytes_per_node_step": bpn,
+                         "bulk_ms_per_launch": bulk_ms},
+            "cpu_baseline": None,
+            "e2e": {"value": e2e_value, "unit": "node-steps/s", "h2d_bytes_per_step": sizes["h2d"],
+                    "d2h_bytes_per_step": sizes["d2h"],
+                    "upload_s": sim.upload_seconds, "run_s": t_run},
+            "clocks": clk,
+            "gpu_launches": launches,
+        }), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -232,6 +340,9 @@ def main():
             dist.barrier()
         torch.cuda.synchronize()
 
+    if args.workload == "batch_shots":
+        run_batch(args, rank, world, local, torch, dist, barrier)
+        return
     from sem2dpack_gb300 import Solver
     prob, name = make_workload(args)
     desc = prob.desc()
@@ -322,7 +433,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "bulk_step_kernel", "bytes_per_node_step": bpn,
+                         "kernel": "strip_step_kernel", "bytes_per_node_step": bpn,
                          "bulk_ms_per_launch": bulk_ms, "fault_ms_per_launch": kms[1] / nt,
                          "receiver_ms_per_launch": kms[2] / nt},
             "cpu_baseline": base,

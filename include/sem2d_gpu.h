@@ -41,6 +41,7 @@ extern "C" {
 #define SEM2D_E_NAN (-5)         /* non-finite field value detected           */
 #define SEM2D_E_STATE (-6)       /* call out of sequence                      */
 #define SEM2D_E_NOMEM (-7)       /* device or host allocation failed          */
+#define SEM2D_E_TIMEOUT (-8)     /* a bounded device wait expired             */
 
 /* time schemes (time.f90:122-315) */
 #define SEM2D_TIME_LEAPFROG 0
@@ -49,6 +50,7 @@ extern "C" {
 /* friction laws (bc_dynflt.f90:200-213) */
 #define SEM2D_FRICTION_SWF 1
 #define SEM2D_FRICTION_RSF 2
+#define SEM2D_FRICTION_TWF 3 /* time weakening alone (bc_dynflt.f90:656-657) */
 
 /* arithmetic of the bulk fields */
 #define SEM2D_PRECISION_FP64 0  /* everything in FP64                       */
@@ -144,6 +146,21 @@ typedef struct sem2d_problem_desc {
 
   /* ---- options ---- */
   int precision; /* SEM2D_PRECISION_*                                      */
+
+  /* ---- 2.5D crustal-plane term f -= beta d, beta = dvol mu (pi/W)^2
+   * (SH) or dvol mu (pi (1-nu)/W)^2 (P-SV), nu = lambda/(lambda+mu)/2
+   * (mat_elastic.f90:363-383, 447-459; mat_gen.f90:440).  width is W of
+   * &GENERAL; width <= 0 (the reference's huge(1d0)) is a 2D problem.
+   * Isotropic materials only.                                           */
+  double width;
+
+  /* ---- time-weakening friction (bc_dynflt_twf.f90:117-184), alone
+   * (flt_friction = SEM2D_FRICTION_TWF) or superimposed on SWF/RSF as
+   * mu = min(mu, mu_twf) (bc_dynflt.f90:405-412, 632, 653-657).
+   * twf_kind 0 = none, 1..3 = kind of &BC_DYNFLT_TWF; the node positions
+   * are those of flt_node1 (bc_dynflt.f90:302).                         */
+  int twf_kind;
+  double twf_mus, twf_mud, twf_mu0, twf_X, twf_Z, twf_V, twf_L, twf_T, twf_Dc;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;
@@ -158,6 +175,27 @@ int sem2d_gpu_device_count(void);
  * uploads the problem and records the step-0 outputs (main.f90:35,
  * bc_gen.f90:247).  *out receives a new handle. */
 int sem2d_gpu_create(const sem2d_problem_desc *desc, sem2d_handle **out);
+
+/* Many independent problems advanced together: one launch per time step
+ * walks the work units (strip x chunk) of all of them.  The reference runs
+ * one problem per process; this replaces nsim runs of init_main + the time
+ * loop (main.f90:16-96) with one handle.  Every member must share NGLL,
+ * ndof, precision, time scheme, nt and material layout (homogeneous
+ * elements, GLL-point values or continuous node values); mesh sizes,
+ * materials, sources and receivers may differ.  *out receives the batch;
+ * step / step_timed / sync / reset / destroy act on all members. */
+int sem2d_gpu_create_batch(const sem2d_problem_desc *descs, int nsim, sem2d_handle **out);
+/* The same batch built one member at a time, so that a caller holds one
+ * problem description at a time: open an empty batch, add members (each is
+ * uploaded at once), close it (units and parameter blocks are built). */
+int sem2d_gpu_batch_open(sem2d_handle **out);
+int sem2d_gpu_batch_add(sem2d_handle *h, const sem2d_problem_desc *desc);
+int sem2d_gpu_batch_close(sem2d_handle *h);
+/* Number of members of a batch (0 for a single problem). */
+int sem2d_gpu_batch_size(sem2d_handle *h);
+/* Member i of a batch (owned by the batch, valid until it is destroyed),
+ * for the get_* calls; NULL if out of range. */
+sem2d_handle *sem2d_gpu_batch_member(sem2d_handle *h, int i);
 
 /* Replaces nsteps iterations of `do it=1,nt; call solve(pb); REC_store;
  * BC_write` (main.f90:51-96).  Asynchronous on the handle's stream; the
@@ -210,7 +248,9 @@ int sem2d_gpu_reset(sem2d_handle *h);
  * every kernel node). */
 long long sem2d_gpu_kernel_launches(sem2d_handle *h);
 
-/* Element tile (TX x TZ elements per CTA) chosen for the bulk kernel. */
+/* Work unit of one CTA of the step kernel: a strip of TX element columns
+ * and a chunk of (about) TZ element rows; SEM2D_CHUNK=TZ in the
+ * environment overrides the chunk height chosen at create time. */
 int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz);
 
 /* Releases device memory; h becomes invalid. */
@@ -227,7 +267,9 @@ const char *sem2d_gpu_last_error(sem2d_handle *h);
  * element row ez starting at lattice row row0[ez] (row0[nz] = LZ).  A nodal
  * field is ndof planes of pitch*LZ values, value (I,J) of dof c at
  * [c*pitch*LZ + J*pitch + I].  Values are double for SEM2D_PRECISION_FP64
- * and float for SEM2D_PRECISION_MIXED.  The state between steps is the
+ * and float for SEM2D_PRECISION_MIXED.  Rows are fetched with 16-byte bulk
+ * copies: pitch times the value size is a multiple of 16 bytes and every
+ * device plane starts 16-byte aligned.  The state between steps is the
  * displacement of the next step (the reference's displ + dt*veloc for
  * leapfrog) and the velocity (the reference's veloc). */
 typedef struct sem2d_lattice_args {

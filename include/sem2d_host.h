@@ -136,6 +136,15 @@ typedef struct sem2d_deck {
   /* options passed through to the descriptor */
   int precision;  /* SEM2D_PRECISION_*                                      */
   int kd2_form;   /* -1: as the reference (ngll == 5), 0 or 1 to force     */
+
+  /* W of &GENERAL (2.5D term); <= 0 for a 2D problem                     */
+  double width;
+  /* &BC_DYNFLT_TWF (bc_dynflt_twf.f90:52-100); twf_kind 0 = absent.  With
+   * flt_friction = SEM2D_FRICTION_TWF it is the only friction law,
+   * otherwise it is superimposed on SWF/RSF.  Defaults of the reference:
+   * kind 1, MuS 0.6, MuD 0.5, Mu0 0.6, X = Z = 0, V 1e3, L 1, T = Dc = huge */
+  int twf_kind;
+  double twf_mus, twf_mud, twf_mu0, twf_X, twf_Z, twf_V, twf_L, twf_T, twf_Dc;
 } sem2d_deck;
 
 typedef struct sem2d_grid sem2d_grid;

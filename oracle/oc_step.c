@@ -21,6 +21,7 @@
  * Operation order follows the Fortran expressions; compile without FMA
  * contraction.
  */
+#include <float.h>
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
@@ -39,6 +40,7 @@ struct oc_sim {
   int *ibool;
   double *H;
   double *acoef; /* (ngll,ngll,nelast,nelem) */
+  double *beta25; /* (ngll,ngll,nelem) 2.5D coefficients or NULL */
   double *kveta;
   double *rmass;
   int nabs;
@@ -63,6 +65,9 @@ struct oc_sim {
   double *swf_dc, *swf_mus, *swf_mud, *swf_p, *swf_alpha, *theta;
   double *rsf_dc, *rsf_mus, *rsf_a, *rsf_b, *rsf_vstar, *rsf_vc, *rsf_Tc, *rsf_coeft;
   double *D, *V, *T, *Tstick, *MU, *sigma;
+  int twf_kind;
+  double twf_mus, twf_mud, twf_mu0, twf_X, twf_Z, twf_V, twf_L, twf_T, twf_Dc;
+  double *fcoord; /* (2,nflt) positions of node1 (bc_dynflt.f90:302) */
   int oit, oitd, oix1, oixn, oixd, fnsamp, onx, fsamp;
   double *fseries;
   /* fields */
@@ -108,6 +113,7 @@ static void init_acoef(oc_sim *s, const sem2d_problem_desc *dd) {
   oc_gll_info(n, xg, wg, Hd);
   free(Hd);
   s->acoef = xcalloc((size_t)n * n * na * ne, sizeof(double));
+  s->beta25 = dd->width > 0.0 ? xcalloc((size_t)n * n * ne, sizeof(double)) : NULL;
   for (int e = 0; e < ne; e++) {
     int cidx[4][2] = {{0, 0}, {n - 1, 0}, {n - 1, n - 1}, {0, n - 1}};
     double c[8];
@@ -136,6 +142,17 @@ static void init_acoef(oc_sim *s, const sem2d_problem_desc *dd) {
         double *A = s->acoef + (size_t)n * n * na * e + i + n * j;
         size_t st = (size_t)n * n;
         double Kx = dd->Kx[p], Kz = dd->Kz[p], la = dd->la[p], mu = dd->mu[p], mux = dd->mux[p];
+        if (s->beta25) {
+          /* MAT_ELAST_init_25D (mat_elastic.f90:363-383), dvol = w */
+          double pw;
+          if (s->ndof == 1) {
+            pw = PI_REF / dd->width;
+          } else {
+            double nu = (la / (la + mu)) / 2.0;
+            pw = (PI_REF * (1.0 - nu)) / dd->width;
+          }
+          s->beta25[p] = (w * mu) * (pw * pw);
+        }
         if (na == 2) {
           A[0] = -(w * ((mux * DxiDx) * DxiDx));
           A[st] = -(w * ((mu * DetaDz) * DetaDz));
@@ -220,6 +237,11 @@ static void compute_fint(oc_sim *s, double *f, const double *d, const double *v)
           dl[q + n2 * k] = dl[q + n2 * k] + eta[q] * v[(ib[q] - 1) + (size_t)np * k];
     }
     elem_forces(s, e, dl, fl);
+    if (s->beta25) { /* MAT_ELAST_add_25D_f (mat_elastic.f90:447-459) */
+      const double *b = s->beta25 + (size_t)n2 * e;
+      for (int k = 0; k < nd; k++)
+        for (int q = 0; q < n2; q++) fl[q + n2 * k] = fl[q + n2 * k] - b[q] * dl[q + n2 * k];
+    }
     for (int q = 0; q < n2; q++)
       for (int k = 0; k < nd; k++) {
         size_t g = (ib[q] - 1) + (size_t)np * k;
@@ -397,6 +419,45 @@ static double rsf_update_V(oc_sim *s, int k, double tau_stick, double sigma, dou
   return nr_solver(s, k, lo, hi, tol, theta, tau_stick, sigma, Z);
 }
 
+/* twf_mu (bc_dynflt_twf.f90:117-184) at fault node k, time t, slip d.
+ * Kind 3 leaves mu undefined beyond r > V T in the reference; here it is
+ * the large value, so the other law (or sticking) decides there.        */
+static double twf_mu(const oc_sim *s, int k, double time, double d) {
+  const double big = DBL_MAX;
+  double x = s->fcoord[2 * k] - s->twf_X, z = s->fcoord[2 * k + 1] - s->twf_Z;
+  double dist = sqrt(x * x + z * z);
+  if (s->twf_kind == 1 || s->twf_kind == 2) {
+    double t, r;
+    if (s->twf_kind == 1) {
+      t = time + ((s->twf_mus - s->twf_mu0) * s->twf_L) / ((s->twf_mus - s->twf_mud) * s->twf_V);
+      if (t > s->twf_T) t = 0.0;
+      r = s->twf_V * t;
+    } else {
+      t = time + (0.5 * s->twf_T) *
+                     (1.0 - sqrt(1.0 - ((4.0 * (s->twf_mus - s->twf_mu0)) * s->twf_L) /
+                                           (((s->twf_mus - s->twf_mud) * s->twf_T) * s->twf_V)));
+      if (t > s->twf_T) t = s->twf_T;
+      r = (s->twf_V * t) * (1.0 - t / s->twf_T);
+    }
+    r = dist - r;
+    if (r < -s->twf_L) return s->twf_mud;
+    if (r <= s->twf_L) return s->twf_mus + ((s->twf_mus - s->twf_mud) / s->twf_L) * r;
+    return big;
+  }
+  /* kind 3: cohesive nucleation front at V t */
+  double vt = s->twf_V * time;
+  if (dist <= s->twf_V * s->twf_T) {
+    if (d <= s->twf_Dc) {
+      if (dist < vt - s->twf_L) return s->twf_mud;
+      if (dist >= vt - s->twf_L && dist <= vt)
+        return s->twf_mus + ((s->twf_mus - s->twf_mud) / s->twf_L) * (dist - vt);
+      return big;
+    }
+    return big;
+  }
+  return big;
+}
+
 /* BC_DYNFLT_apply (bc_dynflt.f90:569-689) */
 static void dynflt_apply(oc_sim *s, double *f, const double *v, const double *d) {
   int nf = s->nflt, nd = s->ndof, np = s->npoin;
@@ -445,6 +506,10 @@ static void dynflt_apply(oc_sim *s, double *f, const double *v, const double *d)
       s->theta[k] = th2;
       s->V[k] = vnew;
       s->MU[k] = rsf_mu(s, k, s->V[k]);
+      if (s->twf_kind) {
+        double mt = twf_mu(s, k, s->it * s->dt, s->D[k]);
+        if (mt < s->MU[k]) s->MU[k] = mt;
+      }
       double strength = -s->MU[k] * sig;
       T[0] = copysign(fabs(strength), T[0]);
       /* T_stick is not defined on this branch of the reference
@@ -452,17 +517,25 @@ static void dynflt_apply(oc_sim *s, double *f, const double *v, const double *d)
       Ts[0] = 0.0;
       Ts[1] = 0.0;
     } else {
-      if (s->coefA2D == 0.0) {
-        if (s->swf_healing) {
-          s->theta[k] = s->theta[k] + fabs(dV[0]) * s->dt;
-          if (fabs(dV[0]) < V_HEALING) s->theta[k] = 0.0;
+      if (s->friction == SEM2D_FRICTION_SWF) {
+        if (s->coefA2D == 0.0) {
+          if (s->swf_healing) {
+            s->theta[k] = s->theta[k] + fabs(dV[0]) * s->dt;
+            if (fabs(dV[0]) < V_HEALING) s->theta[k] = 0.0;
+          } else {
+            s->theta[k] = fabs(dD[0]);
+          }
         } else {
-          s->theta[k] = fabs(dD[0]);
+          s->theta[k] = fabs(s->D[k]);
         }
-      } else {
-        s->theta[k] = fabs(s->D[k]);
+        s->MU[k] = swf_mu(s, k);
+        if (s->twf_kind) {
+          double mt = twf_mu(s, k, s->it * s->dt, s->D[k]);
+          if (mt < s->MU[k]) s->MU[k] = mt;
+        }
+      } else { /* time weakening alone */
+        s->MU[k] = twf_mu(s, k, s->it * s->dt, s->D[k]);
       }
-      s->MU[k] = swf_mu(s, k);
       double strength = s->coh[k] - s->MU[k] * sig;
       Ts[0] = T[0];
       Ts[1] = T[1];
@@ -621,7 +694,7 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
       s->swf_p = dupd_or(dd->swf_p, nf, 3.0);
       s->swf_alpha = dupd_or(dd->swf_alpha, nf, 0.0);
       for (int k = 0; k < nf; k++) s->MU[k] = swf_mu(s, k);
-    } else {
+    } else if (s->friction == SEM2D_FRICTION_RSF) {
       s->rsf_dc = dupd(dd->rsf_dc, nf);
       s->rsf_mus = dupd(dd->rsf_mus, nf);
       s->rsf_a = dupd(dd->rsf_a, nf);
@@ -636,6 +709,29 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
         s->rsf_coeft[k] = exp(-s->dt / s->rsf_Tc[k]);
         s->V[k] = dd->flt_V0 ? dd->flt_V0[k] : 1e-12;
         s->MU[k] = rsf_mu(s, k, s->V[k]);
+      }
+    }
+    s->twf_kind = dd->twf_kind;
+    if (s->friction == SEM2D_FRICTION_TWF && s->twf_kind == 0) s->twf_kind = 1;
+    if (s->twf_kind) {
+      s->twf_mus = dd->twf_mus;
+      s->twf_mud = dd->twf_mud;
+      s->twf_mu0 = dd->twf_mu0;
+      s->twf_X = dd->twf_X;
+      s->twf_Z = dd->twf_Z;
+      s->twf_V = dd->twf_V;
+      s->twf_L = dd->twf_L;
+      s->twf_T = dd->twf_T;
+      s->twf_Dc = dd->twf_Dc;
+      s->fcoord = xcalloc(2 * (size_t)nf, sizeof(double));
+      for (int k = 0; k < nf; k++) {
+        s->fcoord[2 * k] = dd->coord[2 * (size_t)(dd->flt_node1[k] - 1)];
+        s->fcoord[2 * k + 1] = dd->coord[2 * (size_t)(dd->flt_node1[k] - 1) + 1];
+      }
+      /* initial friction (bc_dynflt.f90:405-413), time 0, slip 0 */
+      for (int k = 0; k < nf; k++) {
+        double mt = twf_mu(s, k, 0.0, 0.0);
+        if (s->friction == SEM2D_FRICTION_TWF || mt < s->MU[k]) s->MU[k] = mt;
       }
     }
     s->oit = dd->flt_oit;
@@ -728,7 +824,7 @@ void oc_sim_free(oc_sim *s) {
                   s->swf_mus, s->swf_mud, s->swf_p, s->swf_alpha, s->theta, s->rsf_dc,
                   s->rsf_mus, s->rsf_a, s->rsf_b, s->rsf_vstar, s->rsf_vc, s->rsf_Tc,
                   s->rsf_coeft, s->D, s->V, s->T, s->Tstick, s->MU, s->sigma, s->fseries,
-                  s->d, s->v, s->a};
+                  s->d, s->v, s->a, s->beta25, s->fcoord};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(s);
 }

@@ -6,8 +6,8 @@ binding, the Par.inp-shaped deck and the host problem builder binding.
 """
 from .abi import (FRICTION_RSF, FRICTION_SWF, PRECISION_FP64, PRECISION_MIXED,  # noqa: F401
                   TIME_LEAPFROG, TIME_NEWMARK)
-from .api import Grid, Problem, Sem2dError, Solver  # noqa: F401
+from .api import BatchSolver, Grid, Problem, Sem2dError, Solver  # noqa: F401
 from .deck import Fault, Material, ParDeck, Receivers, Sources, Time  # noqa: F401
 
-__all__ = ["Grid", "Problem", "Solver", "Sem2dError", "ParDeck", "Material", "Fault", "Time",
+__all__ = ["Grid", "Problem", "Solver", "BatchSolver", "Sem2dError", "ParDeck", "Material", "Fault", "Time",
            "Sources", "Receivers"]

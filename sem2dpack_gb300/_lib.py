@@ -18,6 +18,12 @@ PROTOTYPES = [
     ("sem2d_gpu_version", C.c_int, []),
     ("sem2d_gpu_device_count", C.c_int, []),
     ("sem2d_gpu_create", C.c_int, [C.POINTER(abi.ProblemDesc), PP]),
+    ("sem2d_gpu_create_batch", C.c_int, [C.POINTER(abi.ProblemDesc), C.c_int, PP]),
+    ("sem2d_gpu_batch_open", C.c_int, [PP]),
+    ("sem2d_gpu_batch_add", C.c_int, [vp, C.POINTER(abi.ProblemDesc)]),
+    ("sem2d_gpu_batch_close", C.c_int, [vp]),
+    ("sem2d_gpu_batch_size", C.c_int, [vp]),
+    ("sem2d_gpu_batch_member", C.c_void_p, [vp, C.c_int]),
     ("sem2d_gpu_step", C.c_int, [vp, C.c_int]),
     ("sem2d_gpu_step_timed", C.c_int, [vp, C.c_int, dp]),
     ("sem2d_gpu_stream", C.c_void_p, [vp]),

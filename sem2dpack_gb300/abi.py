@@ -18,11 +18,13 @@ SEM2D_E_NR = -4
 SEM2D_E_NAN = -5
 SEM2D_E_STATE = -6
 SEM2D_E_NOMEM = -7
+SEM2D_E_TIMEOUT = -8
 
 TIME_LEAPFROG = 0
 TIME_NEWMARK = 1
 FRICTION_SWF = 1
 FRICTION_RSF = 2
+FRICTION_TWF = 3
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
@@ -81,6 +83,11 @@ class ProblemDesc(C.Structure):
         ("flt_oit", c_int), ("flt_oitd", c_int), ("flt_oix1", c_int), ("flt_oixn", c_int),
         ("flt_oixd", c_int), ("flt_nsamp", c_int),
         ("precision", c_int),
+        ("width", c_double),
+        ("twf_kind", c_int),
+        ("twf_mus", c_double), ("twf_mud", c_double), ("twf_mu0", c_double),
+        ("twf_X", c_double), ("twf_Z", c_double), ("twf_V", c_double), ("twf_L", c_double),
+        ("twf_T", c_double), ("twf_Dc", c_double),
     ]
 
 
@@ -127,6 +134,11 @@ class Deck(C.Structure):
         ("rec_coord", P_double), ("rec_atnode", c_int), ("rec_isamp", c_int),
         ("rec_field", c_char),
         ("precision", c_int), ("kd2_form", c_int),
+        ("width", c_double),
+        ("twf_kind", c_int),
+        ("twf_mus", c_double), ("twf_mud", c_double), ("twf_mu0", c_double),
+        ("twf_X", c_double), ("twf_Z", c_double), ("twf_V", c_double), ("twf_L", c_double),
+        ("twf_T", c_double), ("twf_Dc", c_double),
     ]
 
 

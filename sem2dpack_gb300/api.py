@@ -10,6 +10,7 @@ There is no CPU execution path: Solver needs the compiled library and a
 CUDA device and raises Sem2dError otherwise.
 """
 import ctypes as C
+import time
 
 import numpy as np
 
@@ -233,3 +234,111 @@ class Solver:
         self._check(lib().sem2d_gpu_get_fault_state(self.h, _p(D), _p(V), _p(T), _p(MU), _p(th)))
         return (D.reshape(nf, nd, order="F"), V.reshape(nf, nd, order="F"),
                 T.reshape(nf, 2, order="F"), MU, th)
+
+
+class _Member(Solver):
+    """Read access to one problem of a batch (outputs only; the batch steps,
+    resets and destroys it)."""
+
+    def __init__(self, batch, h, desc):
+        self._owner = batch
+        self.desc = desc
+        self.h = h
+
+    def close(self):
+        self.h = None
+
+
+class BatchSolver:
+    """Independent problems advanced together by one launch per step
+    (sem2d_gpu_batch_open / add / close).  ``problems`` may be an iterator:
+    each Problem (or deck, or (deck, grid) pair) is built, uploaded and
+    released before the next one, so host memory holds one problem at a
+    time.  ``batch[i]`` reads the outputs of problem i."""
+
+    def __init__(self, problems, owners=None):
+        h = C.c_void_p()
+        st = lib().sem2d_gpu_batch_open(C.byref(h))
+        if st != 0:
+            raise Sem2dError(st, lib().sem2d_gpu_last_error(None).decode())
+        self.h = h
+        self._keep = list(owners or [])
+        self.upload_seconds = 0.0  # time spent in batch_add / batch_close
+        descs = []
+        try:
+            for p in problems:
+                if isinstance(p, abi.ProblemDesc):
+                    d = p
+                else:
+                    if not isinstance(p, Problem):
+                        p = Problem(*p) if isinstance(p, tuple) else Problem(p)
+                    d = p.desc()
+                t0 = time.perf_counter()
+                self._check(lib().sem2d_gpu_batch_add(h, C.byref(d)))
+                self.upload_seconds += time.perf_counter() - t0
+                # only the sizes of the description are used from now on
+                descs.append(abi.ProblemDesc.from_buffer_copy(d))
+            t0 = time.perf_counter()
+            self._check(lib().sem2d_gpu_batch_close(h))
+            self.upload_seconds += time.perf_counter() - t0
+        except Exception:
+            self.close()
+            raise
+        self.members = [_Member(self, C.c_void_p(lib().sem2d_gpu_batch_member(h, i)), descs[i])
+                        for i in range(len(descs))]
+        self.nt = descs[0].nt
+
+    def _check(self, st):
+        if st != 0:
+            raise Sem2dError(st, lib().sem2d_gpu_last_error(self.h).decode())
+
+    def __len__(self):
+        return len(self.members)
+
+    def __getitem__(self, i):
+        return self.members[i]
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in getattr(self, "members", []):
+                m.h = None
+            lib().sem2d_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def step(self, nsteps):
+        self._check(lib().sem2d_gpu_step(self.h, int(nsteps)))
+
+    def step_timed(self, nsteps):
+        ms = np.zeros(3)
+        self._check(lib().sem2d_gpu_step_timed(self.h, int(nsteps), _p(ms)))
+        return ms
+
+    def run(self):
+        self.step(self.nt - self.current_step)
+
+    def sync(self):
+        self._check(lib().sem2d_gpu_sync(self.h))
+
+    def reset(self):
+        self._check(lib().sem2d_gpu_reset(self.h))
+
+    @property
+    def stream(self):
+        return lib().sem2d_gpu_stream(self.h)
+
+    @property
+    def current_step(self):
+        return lib().sem2d_gpu_current_step(self.h)
+
+    @property
+    def launches(self):
+        return lib().sem2d_gpu_kernel_launches(self.h)

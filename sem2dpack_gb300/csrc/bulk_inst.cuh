@@ -1,30 +1,19 @@
-// bulk_inst.cuh -- instantiation of the bulk kernel for one NGLL.
+// bulk_inst.cuh -- instantiation of the step kernels for one NGLL.
 #pragma once
 
 #include <string>
 
-#include "bulk_kernel.cuh"
 #include "bulk_launch.h"
+#include "strip_kernel.cuh"
 
 namespace sem2d {
 
 extern thread_local std::string g_bulk_err;
 
-template <typename real, int N, int NDOF, bool MELEM>
-int configure_typed(const BulkConfig &c) {
-  const size_t smem = bulk_smem_bytes<real, N, NDOF>(c.tile_nodes, c.own_nodes, c.nmat, c.has_kv, c.mat_elem);
-  cudaError_t e = cudaFuncSetAttribute(bulk_step_kernel<real, N, NDOF, MELEM>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) {
-    g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
-    return 1;
-  }
-  return 0;
-}
-
-template <typename real, int N, int NDOF, bool MELEM>
-int launch_typed(const BulkConfig &c) {
-  BulkParams<real, N> p{};
+// the typed parameter block of a problem from its type-erased description
+template <typename real, int N>
+void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
+  p = BulkParams<real, N>{};
   p.LX = c.LX;
   p.LZ = c.LZ;
   p.pitch = c.pitch;
@@ -78,13 +67,38 @@ int launch_typed(const BulkConfig &c) {
   p.sis = c.sis;
   p.scheme = c.scheme;
   p.dt = real(c.dt);
+  p.width = real(c.width);
   p.cv = real(c.cv);
   p.cpred = real(c.cpred);
   p.cd2 = real(c.cd2);
   p.kd2 = c.kd2;
-  const size_t smem = bulk_smem_bytes<real, N, NDOF>(c.tile_nodes, c.own_nodes, c.nmat, c.has_kv, c.mat_elem);
-  bulk_step_kernel<real, N, NDOF, MELEM><<<dim3(c.grid_x, c.grid_y), kBulkThreads, smem, c.stream>>>(
-      p, c.tile_nodes, c.own_nodes, c.nmat, c.has_kv);
+  p.nmat = c.nmat;
+  p.has_kv = c.has_kv;
+  p.nplanes = c.nplanes;
+  p.error = c.error;
+}
+
+template <typename real, int N, int NDOF, int MAT, bool FAST>
+int configure_typed(const BulkConfig &c) {
+  const size_t smem = strip_smem_bytes<real, N, NDOF>(c.nplanes);
+  cudaError_t e = cudaFuncSetAttribute(strip_step_kernel<real, N, NDOF, MAT, FAST>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(strip_batch_kernel<real, N, NDOF, MAT, FAST>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) {
+    g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
+}
+
+template <typename real, int N, int NDOF, int MAT, bool FAST>
+int launch_typed(const BulkConfig &c) {
+  BulkParams<real, N> p;
+  fill_params<real, N>(c, p);
+  const size_t smem = strip_smem_bytes<real, N, NDOF>(c.nplanes);
+  strip_step_kernel<real, N, NDOF, MAT, FAST><<<dim3(c.grid_x, c.grid_y), kStripThreads, smem, c.stream>>>(p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -93,54 +107,109 @@ int launch_typed(const BulkConfig &c) {
   return 0;
 }
 
-template <typename real, int N, int NDOF, bool MELEM>
+template <typename real, int N, int NDOF, int MAT, bool FAST>
+int launch_batch_typed(const BulkConfig &c, const BatchLaunch &b) {
+  BatchParams<real, N> bp{};
+  for (int k = 0; k < N * N; ++k) bp.H[k] = real(c.H[k]);
+  for (int k = 0; k < N; ++k) bp.w[k] = real(c.w[k]);
+  bp.sims = static_cast<const BulkParams<real, N> *>(b.params);
+  bp.units = static_cast<const int4 *>(b.units);
+  bp.nunits = b.nunits;
+  bp.step = b.step;
+  bp.done = b.done;
+  const size_t smem = strip_smem_bytes<real, N, NDOF>(c.nplanes);
+  strip_batch_kernel<real, N, NDOF, MAT, FAST><<<b.grid, kStripThreads, smem, c.stream>>>(bp);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_bulk_err = cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
+}
+
+template <typename real, int N, int NDOF, int MAT, bool FAST>
 int occupancy_typed(const BulkConfig &c) {
-  const size_t smem = bulk_smem_bytes<real, N, NDOF>(c.tile_nodes, c.own_nodes, c.nmat, c.has_kv, c.mat_elem);
-  if (configure_typed<real, N, NDOF, MELEM>(c)) return 0;
+  const size_t smem = strip_smem_bytes<real, N, NDOF>(c.nplanes);
+  if (configure_typed<real, N, NDOF, MAT, FAST>(c)) return 0;
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, bulk_step_kernel<real, N, NDOF, MELEM>, kBulkThreads,
-                                                    smem) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, strip_step_kernel<real, N, NDOF, MAT, FAST>,
+                                                    kStripThreads, smem) != cudaSuccess)
     return 0;
   return nb;
 }
 
-template <typename real, int N, int NDOF>
-int occupancy_m(const BulkConfig &c) {
-  return c.mat_elem ? occupancy_typed<real, N, NDOF, true>(c) : occupancy_typed<real, N, NDOF, false>(c);
+// dispatch over the material layout and the fast path (NGLL = 5 only)
+template <typename real, int N, int NDOF, typename F>
+int dispatch_m(const BulkConfig &c, F &&f) {
+  const bool fast = N == 5 && c.fast;
+  if (c.mat_elem == kMatPoint)
+    return fast ? f.template operator()<real, N, NDOF, kMatPoint, (N == 5)>()
+                : f.template operator()<real, N, NDOF, kMatPoint, false>();
+  if (c.mat_elem == kMatElement)
+    return fast ? f.template operator()<real, N, NDOF, kMatElement, (N == 5)>()
+                : f.template operator()<real, N, NDOF, kMatElement, false>();
+  return fast ? f.template operator()<real, N, NDOF, kMatNode, (N == 5)>()
+              : f.template operator()<real, N, NDOF, kMatNode, false>();
 }
+
+template <int N, typename F>
+int dispatch_all(const BulkConfig &c, F &&f) {
+  if (c.ndof == 1) return c.mixed ? dispatch_m<float, N, 1>(c, f) : dispatch_m<double, N, 1>(c, f);
+  return c.mixed ? dispatch_m<float, N, 2>(c, f) : dispatch_m<double, N, 2>(c, f);
+}
+
+struct ConfigureOp {
+  const BulkConfig &c;
+  template <typename real, int N, int NDOF, int MAT, bool FAST>
+  int operator()() const { return configure_typed<real, N, NDOF, MAT, FAST>(c); }
+};
+struct LaunchOp {
+  const BulkConfig &c;
+  template <typename real, int N, int NDOF, int MAT, bool FAST>
+  int operator()() const { return launch_typed<real, N, NDOF, MAT, FAST>(c); }
+};
+struct OccupancyOp {
+  const BulkConfig &c;
+  template <typename real, int N, int NDOF, int MAT, bool FAST>
+  int operator()() const { return occupancy_typed<real, N, NDOF, MAT, FAST>(c); }
+};
+struct BatchOp {
+  const BulkConfig &c;
+  const BatchLaunch &b;
+  template <typename real, int N, int NDOF, int MAT, bool FAST>
+  int operator()() const { return launch_batch_typed<real, N, NDOF, MAT, FAST>(c, b); }
+};
 
 template <int N>
-int occupancy_for_n(const BulkConfig &c) {
-  if (c.ndof == 1) return c.mixed ? occupancy_m<float, N, 1>(c) : occupancy_m<double, N, 1>(c);
-  return c.mixed ? occupancy_m<float, N, 2>(c) : occupancy_m<double, N, 2>(c);
-}
-
-template <typename real, int N, int NDOF>
-int configure_m(const BulkConfig &c) {
-  return c.mat_elem ? configure_typed<real, N, NDOF, true>(c) : configure_typed<real, N, NDOF, false>(c);
-}
-template <typename real, int N, int NDOF>
-int launch_m(const BulkConfig &c) {
-  return c.mat_elem ? launch_typed<real, N, NDOF, true>(c) : launch_typed<real, N, NDOF, false>(c);
-}
+int configure_for_n(const BulkConfig &c) { return dispatch_all<N>(c, ConfigureOp{c}); }
+template <int N>
+int launch_for_n(const BulkConfig &c) { return dispatch_all<N>(c, LaunchOp{c}); }
+template <int N>
+int occupancy_for_n(const BulkConfig &c) { return dispatch_all<N>(c, OccupancyOp{c}); }
+template <int N>
+int launch_batch_for_n(const BulkConfig &c, const BatchLaunch &b) { return dispatch_all<N>(c, BatchOp{c, b}); }
 
 template <int N>
-int configure_for_n(const BulkConfig &c) {
-  if (c.ndof == 1) return c.mixed ? configure_m<float, N, 1>(c) : configure_m<double, N, 1>(c);
-  return c.mixed ? configure_m<float, N, 2>(c) : configure_m<double, N, 2>(c);
-}
-
-template <int N>
-int launch_for_n(const BulkConfig &c) {
-  if (c.ndof == 1) return c.mixed ? launch_m<float, N, 1>(c) : launch_m<double, N, 1>(c);
-  return c.mixed ? launch_m<float, N, 2>(c) : launch_m<double, N, 2>(c);
-}
-
-template <int N>
-size_t smem_for_n(int ndof, int mixed, int tn, int on, int nmat, int kv, int me) {
+size_t smem_for_n(int ndof, int mixed, int nplanes) {
   if (ndof == 1)
-    return mixed ? bulk_smem_bytes<float, N, 1>(tn, on, nmat, kv, me) : bulk_smem_bytes<double, N, 1>(tn, on, nmat, kv, me);
-  return mixed ? bulk_smem_bytes<float, N, 2>(tn, on, nmat, kv, me) : bulk_smem_bytes<double, N, 2>(tn, on, nmat, kv, me);
+    return mixed ? strip_smem_bytes<float, N, 1>(nplanes) : strip_smem_bytes<double, N, 1>(nplanes);
+  return mixed ? strip_smem_bytes<float, N, 2>(nplanes) : strip_smem_bytes<double, N, 2>(nplanes);
+}
+
+template <int N>
+int strip_width_for_n() {
+  return StripShape<float, N>::SW1 - 1;
+}
+
+// the parameter block of one problem, written to `out` (params_bytes)
+template <int N>
+size_t params_bytes_for_n(int mixed) {
+  return mixed ? sizeof(BulkParams<float, N>) : sizeof(BulkParams<double, N>);
+}
+template <int N>
+void fill_params_for_n(const BulkConfig &c, void *out) {
+  if (c.mixed) fill_params<float, N>(c, *static_cast<BulkParams<float, N> *>(out));
+  else fill_params<double, N>(c, *static_cast<BulkParams<double, N> *>(out));
 }
 
 }  // namespace sem2d

@@ -1,4 +1,4 @@
-// bulk_launch.cu -- NGLL dispatch and tile-shape selection for the bulk kernel.
+// bulk_launch.cu -- NGLL dispatch and chunk selection for the step kernel.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
@@ -40,13 +40,54 @@ int occupancy_bulk(const BulkConfig &c) {
   }
 }
 
-size_t bulk_smem(int N, int ndof, int mixed, int tn, int on, int nmat, int kv, int me) {
+size_t bulk_smem(int N, int ndof, int mixed, int nplanes) {
   switch (N) {
-    case 5: return bulk_smem_n5(ndof, mixed, tn, on, nmat, kv, me);
-    case 6: return bulk_smem_n6(ndof, mixed, tn, on, nmat, kv, me);
-    case 9: return bulk_smem_n9(ndof, mixed, tn, on, nmat, kv, me);
+    case 5: return bulk_smem_n5(ndof, mixed, nplanes);
+    case 6: return bulk_smem_n6(ndof, mixed, nplanes);
+    case 9: return bulk_smem_n9(ndof, mixed, nplanes);
     default: return size_t(-1);
   }
+}
+
+int launch_batch(const BulkConfig &c, const BatchLaunch &b) {
+  switch (c.N) {
+    case 5: return launch_batch_n5(c, b);
+    case 6: return launch_batch_n6(c, b);
+    case 9: return launch_batch_n9(c, b);
+    default: g_bulk_err = "NGLL not compiled"; return 1;
+  }
+}
+
+size_t params_bytes(int N, int mixed) {
+  switch (N) {
+    case 5: return params_bytes_n5(mixed);
+    case 6: return params_bytes_n6(mixed);
+    case 9: return params_bytes_n9(mixed);
+    default: return 0;
+  }
+}
+
+int fill_params_block(const BulkConfig &c, void *out) {
+  switch (c.N) {
+    case 5: fill_params_n5(c, out); return 0;
+    case 6: fill_params_n6(c, out); return 0;
+    case 9: fill_params_n9(c, out); return 0;
+    default: g_bulk_err = "NGLL not compiled"; return 1;
+  }
+}
+
+int strip_width(int N) {
+  switch (N) {
+    case 5: return strip_width_n5();
+    case 6: return strip_width_n6();
+    case 9: return strip_width_n9();
+    default: return 0;
+  }
+}
+
+int strip_plane_count(int ndof, int nmat, int mat_elem, int scheme) {
+  // displacement, node material, velocity, acceleration (Newmark), inverse mass
+  return ndof + (mat_elem == 0 ? nmat : 0) + ndof + (scheme == 1 ? ndof : 0) + 1;
 }
 
 std::vector<int> tile_rows(int N, int nz, const int *row0, int TZ) {
@@ -56,9 +97,9 @@ std::vector<int> tile_rows(int N, int nz, const int *row0, int TZ) {
   auto split = [&](int z) { return z > 0 && z < nz && row0[z] == row0[z - 1] + N; };
   for (size_t k = 1; k + 1 < b.size(); ++k) {
     if (!split(b[k])) continue;
-    if (b[k] + 1 < b[k + 1] && !split(b[k] + 1)) b[k] += 1;        // lower tile takes the row
-    else if (b[k] - 1 > b[k - 1] && !split(b[k] - 1)) b[k] -= 1;   // upper tile takes the row
-    else {                                                          // merge the two tiles
+    if (b[k] + 1 < b[k + 1] && !split(b[k] + 1)) b[k] += 1;        // lower chunk takes the row
+    else if (b[k] - 1 > b[k - 1] && !split(b[k] - 1)) b[k] -= 1;   // upper chunk takes the row
+    else {                                                          // merge the two chunks
       b.erase(b.begin() + long(k));
       --k;
     }
@@ -66,85 +107,62 @@ std::vector<int> tile_rows(int N, int nz, const int *row0, int TZ) {
   return b;
 }
 
-void tile_sizes(int N, int nx, const int *row0, int TX, const std::vector<int> &zt, int *tile_nodes,
-                int *own_nodes) {
-  int best = 0, own = 0;
-  const int LX = nx * (N - 1) + 1;
-  for (size_t y = 0; y + 1 < zt.size(); ++y) {
-    const int ez0 = zt[y], ez1 = zt[y + 1];
-    const int hz = (ez0 > 0 && row0[ez0] == row0[ez0 - 1] + (N - 1)) ? 1 : 0;
-    const int TH = row0[ez1 - 1] + N - row0[ez0 - hz];
-    const int OH = row0[ez1] - row0[ez0];
-    for (int ex0 = 0; ex0 < nx; ex0 += TX) {
-      const int ex1 = ex0 + TX < nx ? ex0 + TX : nx;
-      const int hx = ex0 > 0 ? 1 : 0;
-      const int TW = (ex1 - 1) * (N - 1) + N - (ex0 - hx) * (N - 1);
-      const int OW = (ex1 == nx ? LX : ex1 * (N - 1)) - ex0 * (N - 1);
-      best = std::max(best, TW * TH);
-      own = std::max(own, OW * OH);
-    }
-  }
-  *tile_nodes = best;
-  *own_nodes = own;
-}
-
-int choose_tiles(int N, int ndof, int mixed, int nx, int nz, const int *row0, int nmat, int has_kv,
-                 int mat_elem, int *TX, int *TZ) {
+int choose_tiles(const BulkConfig &c, const int *row0, int *TZ) {
   int dev = 0, nsm = 0;
   cudaGetDevice(&dev);
   if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || nsm <= 0) nsm = 1;
-  auto eval = [&](int tx, int tz, double *cost) -> bool {
+  const int N = c.N, nx = c.nx, nz = c.nz, SW = strip_width(N);
+  if (SW <= 0) {
+    g_bulk_err = "NGLL not compiled";
+    return 1;
+  }
+  if (bulk_smem(N, c.ndof, c.mixed, c.nplanes) > 227 * 1024) {
+    g_bulk_err = "the stage buffers do not fit in shared memory";
+    return 1;
+  }
+  const int per_sm = occupancy_bulk(c);
+  if (per_sm <= 0) {
+    g_bulk_err = std::string("no resident CTA: ") + g_bulk_err;
+    return 1;
+  }
+  // batch rows of the step kernel: the slots per batch over the strip width
+  const int slots = 8 * (32 / N), R = slots / (SW + 1);
+  const long long nstrips = (nx + SW - 1) / SW;
+  auto eval = [&](int tz) {
     const std::vector<int> zt = tile_rows(N, nz, row0, tz);
-    BulkConfig c;
-    c.N = N;
-    c.ndof = ndof;
-    c.mixed = mixed;
-    c.nmat = nmat;
-    c.has_kv = has_kv;
-    c.mat_elem = mat_elem;
-    tile_sizes(N, nx, row0, tx, zt, &c.tile_nodes, &c.own_nodes);
-    if (bulk_smem(N, ndof, mixed, c.tile_nodes, c.own_nodes, nmat, has_kv, mat_elem) > 227 * 1024) return false;
-    const int per_sm = occupancy_bulk(c);
-    if (per_sm <= 0) return false;
-    const long long ntiles = (long long)((nx + tx - 1) / tx) * (long long)(zt.size() - 1);
-    const long long waves = (ntiles + (long long)per_sm * nsm - 1) / ((long long)per_sm * nsm);
-    // work of the slowest SM: waves x elements computed per tile (with halo)
-    const double per_tile = double(std::min(tx, nx) + (nx > tx ? 1 : 0)) * double(std::min(tz, nz) + (nz > tz ? 1 : 0));
-    *cost = double(waves) * per_tile + 1e-3 * per_tile;
-    return true;
+    const long long nchunks = (long long)zt.size() - 1;
+    long long batches = 0;  // the slowest chunk
+    for (size_t y = 0; y + 1 < zt.size(); ++y) {
+      const int ez0 = zt[y], ez1 = zt[y + 1];
+      const int hz = (ez0 > 0 && row0[ez0] == row0[ez0 - 1] + (N - 1)) ? 1 : 0;
+      batches = std::max(batches, (long long)((ez1 - ez0 + hz + R - 1) / R));
+    }
+    const long long ctas = nstrips * nchunks;
+    const long long conc = (long long)per_sm * nsm;
+    const long long waves = (ctas + conc - 1) / conc;
+    // time ~ waves x batches per CTA, plus the pipeline fill of each CTA
+    return double(waves) * (double(batches) + 1.0);
   };
-  const char *env = std::getenv("SEM2D_TILE");
+  // chunks of at most kMaxChunkRows element rows (two merged around a fault
+  // split plus the halo row stay within the kernel's row tables)
+  const int tzmax = std::min(nz, kMaxChunkRows);
+  const char *env = std::getenv("SEM2D_CHUNK");
   if (env) {
-    int tx = 0, tz = 0;
-    double cost;
-    if (std::sscanf(env, "%dx%d", &tx, &tz) == 2 && tx > 0 && tz > 0) {
-      if (eval(tx, tz, &cost)) {
-        *TX = tx;
-        *TZ = tz;
-        return 0;
-      }
-      g_bulk_err = "SEM2D_TILE does not fit";
-      return 1;
+    const int tz = std::atoi(env);
+    if (tz > 0) {
+      *TZ = std::min(tz, tzmax);
+      return 0;
     }
   }
   double best = 1e300;
-  int bx = 0, bz = 0;
-  for (int tx = 1; tx <= 32; ++tx)
-    for (int tz = 1; tz <= 16; ++tz) {
-      if (tx > nx || tz > nz) continue;
-      double cost;
-      if (!eval(tx, tz, &cost)) continue;
-      if (cost < best) {
-        best = cost;
-        bx = tx;
-        bz = tz;
-      }
+  int bz = tzmax;
+  for (int tz = 1; tz <= tzmax; ++tz) {
+    const double cost = eval(tz);
+    if (cost <= best + 1e-9) {  // ties: the taller chunk (less halo work)
+      best = cost;
+      bz = tz;
     }
-  if (bx == 0) {
-    g_bulk_err = "no tile fits in shared memory";
-    return 1;
   }
-  *TX = bx;
   *TZ = bz;
   return 0;
 }

@@ -1,4 +1,4 @@
-// bulk_launch.h -- host interface of the bulk kernel instantiations.
+// bulk_launch.h -- host interface of the step-kernel instantiations.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -7,18 +7,23 @@
 
 namespace sem2d {
 
+// largest chunk height the host picks (the kernel holds the row tables of
+// up to 256 element rows: two chunks merged around a fault split + a halo)
+constexpr int kMaxChunkRows = 120;
+
 // Everything the bulk kernel needs, type-erased; the launcher for the
 // (NGLL, ndof, precision) of the problem fills the typed parameter block.
 struct BulkConfig {
   int N = 0, ndof = 0, mixed = 0;
-  int tile_nodes = 0, own_nodes = 0, nmat = 0, has_kv = 0, mat_elem = 0, mat_iso = 0;
+  int nplanes = 0, nmat = 0, has_kv = 0, mat_elem = 0, mat_iso = 0;
+  int fast = 0;  // isotropic, leapfrog, no Kelvin-Voigt, no 2.5D term
   int grid_x = 0, grid_y = 0;
   int LX = 0, LZ = 0, pitch = 0;
   long long plane = 0;
   int nx = 0, nz = 0;
   const int *row0 = nullptr;
-  int TX = 0;
-  const int *ztile = nullptr;  // device [grid_y+1]
+  int TX = 0;                  // element columns per strip (strip_width)
+  const int *ztile = nullptr;  // device [grid_y+1] element-row chunk boundaries
   const double *H = nullptr, *w = nullptr;  // host arrays
   void *Dcur = nullptr, *Dnext = nullptr, *Vcur = nullptr, *Vnext = nullptr;
   void *Acur = nullptr, *Anext = nullptr;
@@ -42,31 +47,49 @@ struct BulkConfig {
   double *sis = nullptr;
   int scheme = 0, kd2 = 0;
   double dt = 0, cv = 0, cpred = 0, cd2 = 0;
+  double width = 0;  // 2.5D seismogenic width, 0 = 2D
+  int *error = nullptr;  // device error flag
   cudaStream_t stream = nullptr;
 };
 
-// launches one time step of the bulk kernel; 0 or non-zero on error
+// a batched step: device array of per-problem parameter blocks for this
+// step's buffer parity, the work units and the batch's counters
+struct BatchLaunch {
+  const void *params = nullptr;  // [nsim] parameter blocks (params_bytes each)
+  const void *units = nullptr;   // [nunits] int4 (problem, strip, chunk, strips per row)
+  int nunits = 0, grid = 0;
+  int *step = nullptr;
+  unsigned *done = nullptr;
+};
+
+// launches one time step of the step kernel; 0 or non-zero on error
 int launch_bulk(const BulkConfig &c);
+// launches one time step of a batch (c describes the shared kernel shape:
+// N, ndof, precision, material layout, planes, fast path, H, w, stream)
+int launch_batch(const BulkConfig &c, const BatchLaunch &b);
+// size of one parameter block and the block of a problem
+size_t params_bytes(int N, int mixed);
+int fill_params_block(const BulkConfig &c, void *out);
 // sets the kernel's dynamic shared-memory limit (once per handle, before
 // any launch or stream capture)
 int configure_bulk(const BulkConfig &c);
 const char *bulk_last_error();
 
-// tile-row boundaries (element rows) of height TZ, moved off split rows
-// (row0[b] == row0[b-1] + N) so that both rows of a fault stay in one tile
-std::vector<int> tile_rows(int N, int nz, const int *row0, int TZ);
-// largest staged tile and largest owned block over all CTAs
-void tile_sizes(int N, int nx, const int *row0, int TX, const std::vector<int> &zt,
-                int *tile_nodes, int *own_nodes);
-// dynamic shared memory (bytes) of one CTA
-size_t bulk_smem(int N, int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv,
-                 int mat_elem);
+// element columns per strip for NGLL N (0 if N is not compiled)
+int strip_width(int N);
+// lattice planes staged per batch
+int strip_plane_count(int ndof, int nmat, int mat_elem, int scheme);
 
-// picks the tile shape minimising (waves x recomputed elements per tile)
-// for the device's SM count and the kernel's occupancy; SEM2D_TILE=TXxTZ
-// overrides.  0 on success.
-int choose_tiles(int N, int ndof, int mixed, int nx, int nz, const int *row0, int nmat, int has_kv,
-                 int mat_elem, int *TX, int *TZ);
+// chunk boundaries (element rows) of height TZ, moved off split rows
+// (row0[b] == row0[b-1] + N) so that both rows of a fault stay in one chunk
+std::vector<int> tile_rows(int N, int nz, const int *row0, int TZ);
+// dynamic shared memory (bytes) of one CTA
+size_t bulk_smem(int N, int ndof, int mixed, int nplanes);
+
+// picks the chunk height minimising (waves x batches per chunk) for the
+// device's SM count and the kernel's occupancy; SEM2D_CHUNK=TZ overrides.
+// 0 on success.
+int choose_tiles(const BulkConfig &c, const int *row0, int *TZ);
 
 // per-NGLL launchers
 int launch_bulk_n5(const BulkConfig &c);
@@ -80,8 +103,20 @@ int occupancy_bulk_n6(const BulkConfig &c);
 int occupancy_bulk_n9(const BulkConfig &c);
 // resident CTAs per SM for the configuration's shared memory (0 if none)
 int occupancy_bulk(const BulkConfig &c);
-size_t bulk_smem_n5(int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv, int mat_elem);
-size_t bulk_smem_n6(int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv, int mat_elem);
-size_t bulk_smem_n9(int ndof, int mixed, int tile_nodes, int own_nodes, int nmat, int has_kv, int mat_elem);
+size_t bulk_smem_n5(int ndof, int mixed, int nplanes);
+size_t bulk_smem_n6(int ndof, int mixed, int nplanes);
+size_t bulk_smem_n9(int ndof, int mixed, int nplanes);
+int strip_width_n5();
+int strip_width_n6();
+int strip_width_n9();
+int launch_batch_n5(const BulkConfig &c, const BatchLaunch &b);
+int launch_batch_n6(const BulkConfig &c, const BatchLaunch &b);
+int launch_batch_n9(const BulkConfig &c, const BatchLaunch &b);
+size_t params_bytes_n5(int mixed);
+size_t params_bytes_n6(int mixed);
+size_t params_bytes_n9(int mixed);
+void fill_params_n5(const BulkConfig &c, void *out);
+void fill_params_n6(const BulkConfig &c, void *out);
+void fill_params_n9(const BulkConfig &c, void *out);
 
 }  // namespace sem2d

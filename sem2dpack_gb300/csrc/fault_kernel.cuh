@@ -161,6 +161,41 @@ __device__ void fault_record(const FaultParams<real> &p, int k, int it) {
   o[q + 5 * p.onx] = p.Tstick[k];
 }
 
+// time-weakening friction coefficient (twf_mu, bc_dynflt_twf.f90:117-184)
+// of node k at time `time` with slip d.  Kind 3 leaves mu undefined for
+// r > V T in the reference; the large value is returned there, so the
+// other law (or sticking) decides.
+template <typename real>
+__device__ double twf_mu(const FaultParams<real> &p, int k, double time, double d) {
+  const double big = 1.7976931348623157e308;  // huge(1d0)
+  const double x = p.fxz[2 * k] - p.twf_X, z = p.fxz[2 * k + 1] - p.twf_Z;
+  const double dist = sqrt(x * x + z * z);
+  if (p.twf_kind == 1 || p.twf_kind == 2) {
+    double t, r;
+    if (p.twf_kind == 1) {
+      t = time + ((p.twf_mus - p.twf_mu0) * p.twf_L) / ((p.twf_mus - p.twf_mud) * p.twf_V);
+      if (t > p.twf_T) t = 0.0;
+      r = p.twf_V * t;
+    } else {
+      t = time + (0.5 * p.twf_T) *
+                     (1.0 - sqrt(1.0 - ((4.0 * (p.twf_mus - p.twf_mu0)) * p.twf_L) /
+                                           (((p.twf_mus - p.twf_mud) * p.twf_T) * p.twf_V)));
+      if (t > p.twf_T) t = p.twf_T;
+      r = (p.twf_V * t) * (1.0 - t / p.twf_T);
+    }
+    r = dist - r;
+    if (r < -p.twf_L) return p.twf_mud;
+    if (r <= p.twf_L) return p.twf_mus + ((p.twf_mus - p.twf_mud) / p.twf_L) * r;
+    return big;
+  }
+  const double vt = p.twf_V * time;
+  if (dist <= p.twf_V * p.twf_T && d <= p.twf_Dc) {
+    if (dist < vt - p.twf_L) return p.twf_mud;
+    if (dist <= vt) return p.twf_mus + ((p.twf_mus - p.twf_mud) / p.twf_L) * (dist - vt);
+  }
+  return big;
+}
+
 // initial friction and the step-0 record (bc_dynflt.f90:401-415, 247)
 template <typename real>
 __global__ void fault_init_kernel(FaultParams<real> p) {
@@ -168,7 +203,11 @@ __global__ void fault_init_kernel(FaultParams<real> p) {
   if (k >= p.nflt) return;
   p.sigma[k] = p.T0[k + p.nflt];
   if (p.friction == 2) p.MU[k] = rsf_mu(p, k, p.V[k], p.theta[k]);
-  else p.MU[k] = swf_mu(p, k, p.theta[k]);
+  else if (p.friction == 1) p.MU[k] = swf_mu(p, k, p.theta[k]);
+  if (p.twf_kind) {
+    const double mt = twf_mu(p, k, 0.0, 0.0);
+    if (p.friction == 3 || mt < p.MU[k]) p.MU[k] = mt;
+  }
   fault_record(p, k, 0);
 }
 
@@ -232,24 +271,36 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     if (fail) atomicExch(p.error, kErrNR);
     p.theta[k] = th2;
     mu = rsf_mu(p, k, vnew, th2);
+    if (p.twf_kind) {
+      const double mt = twf_mu(p, k, it * p.dt, p.D[k]);
+      if (mt < mu) mu = mt;
+    }
     T[0] = copysign(fabs(-mu * sig), T[0]);
     // T_stick is undefined on this branch of the reference (bc_dynflt.f90:581)
     Ts[0] = 0.0;
     Ts[1] = 0.0;
   } else {
-    double th = p.theta[k];
-    if (p.coefA2D == 0.0) {
-      if (p.swf_healing) {
-        th = th + fabs(dV[0]) * p.dt;
-        if (fabs(dV[0]) < 1.0e-14) th = 0.0;
+    if (p.friction == 1) {
+      double th = p.theta[k];
+      if (p.coefA2D == 0.0) {
+        if (p.swf_healing) {
+          th = th + fabs(dV[0]) * p.dt;
+          if (fabs(dV[0]) < 1.0e-14) th = 0.0;
+        } else {
+          th = fabs(dD[0]);
+        }
       } else {
-        th = fabs(dD[0]);
+        th = fabs(p.D[k]);
       }
-    } else {
-      th = fabs(p.D[k]);
+      p.theta[k] = th;
+      mu = swf_mu(p, k, th);
+      if (p.twf_kind) {
+        const double mt = twf_mu(p, k, it * p.dt, p.D[k]);
+        if (mt < mu) mu = mt;
+      }
+    } else {  // time weakening alone
+      mu = twf_mu(p, k, it * p.dt, p.D[k]);
     }
-    p.theta[k] = th;
-    mu = swf_mu(p, k, th);
     const double strength = p.coh[k] - mu * sig;
     Ts[0] = T[0];
     Ts[1] = T[1];

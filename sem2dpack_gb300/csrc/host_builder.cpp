@@ -1313,6 +1313,20 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
     d->flt_nsamp = P->fnsamp;
   }
   d->precision = P->deck.precision;
+  d->width = P->deck.width;
+  if (P->nflt) {
+    const sem2d_deck &dk = P->deck;
+    d->twf_kind = dk.flt_friction == SEM2D_FRICTION_TWF && dk.twf_kind == 0 ? 1 : dk.twf_kind;
+    d->twf_mus = dk.twf_mus;
+    d->twf_mud = dk.twf_mud;
+    d->twf_mu0 = dk.twf_mu0;
+    d->twf_X = dk.twf_X;
+    d->twf_Z = dk.twf_Z;
+    d->twf_V = dk.twf_V;
+    d->twf_L = dk.twf_L;
+    d->twf_T = dk.twf_T;
+    d->twf_Dc = dk.twf_Dc;
+  }
   return SEM2D_OK;
 }
 

@@ -3,7 +3,8 @@
 //
 // The handle-based path allocates the partner buffers of its double-buffered
 // update and two counters with cudaMalloc.  Here they live in g_scratch:
-//   [0, 64)         step counter (int) and CTA completion counter (unsigned)
+//   [0, 64)         step counter (int), CTA completion counter (unsigned),
+//                   device error flag (int)
 //   [64, 16384)     tile-row boundaries, nz+1 ints
 //   [16384, ...)    partner displacement plane(s), then partner velocity
 // Host code never dereferences g_scratch: its device address is looked up
@@ -11,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <mutex>
 
 #include "../../include/sem2d_gpu.h"
@@ -34,6 +36,7 @@ __global__ void noalloc_setup_kernel(unsigned char *scratch, int step0, int nz, 
   int *ztile = reinterpret_cast<int *>(scratch + kHeaderBytes);
   *step = step0;
   *done = 0u;
+  *reinterpret_cast<int *>(scratch + 8) = 0;
   int k = 0;
   for (int z = 0; z < nz; z += TZ) ztile[k++] = z;
   ztile[k] = nz;
@@ -56,6 +59,16 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
   if (!a->d || !a->v || !a->row0 || !a->hprime || !a->wgll || !a->rmass || !a->per_rm || !a->per_Ca ||
       !a->per_Cb || !a->mat[0] || !a->xix || !a->etaz || !a->dxdxi || !a->dzdeta)
     return fail(SEM2D_E_ARG, "missing array");
+  {
+    // rows are fetched with 16-byte bulk copies: 16-byte aligned planes and
+    // a row pitch of a multiple of 16 bytes
+    const size_t rs = a->precision == SEM2D_PRECISION_MIXED ? sizeof(float) : sizeof(double);
+    const size_t al = 16 / rs;
+    if (a->pitch % al != 0) return fail(SEM2D_E_ARG, "the row pitch must be a multiple of 16 bytes");
+    const void *ptrs[] = {a->d, a->v, a->rmass, a->mat[0], a->mat[1], a->mat[2], a->mat[3]};
+    for (const void *q : ptrs)
+      if (reinterpret_cast<uintptr_t>(q) % 16 != 0) return fail(SEM2D_E_ARG, "arrays must be 16-byte aligned");
+  }
   if (a->nsrc > 0 && (!a->src_I || !a->src_J || !a->src_amp)) return fail(SEM2D_E_ARG, "missing source arrays");
   if (a->step0 < 0 || a->step0 + nsteps > a->nt) return fail(SEM2D_E_ARG, "steps beyond nt");
   const size_t rs = a->precision == SEM2D_PRECISION_MIXED ? sizeof(float) : sizeof(double);
@@ -82,7 +95,8 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const int N = a->ngll;
-  int TX = std::min(8, a->nx), TZ = std::min(8, a->nz);
+  const int TX = strip_width(N), TZ = std::min(16, a->nz);
+  if (TX <= 0) return fail(SEM2D_E_UNSUPPORTED, "NGLL not compiled");
   BulkConfig c;
   c.N = N;
   c.ndof = a->ndof;
@@ -93,16 +107,10 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
   c.has_kv = 0;
   c.mat_elem = 0;
   c.mat_iso = a->mat_iso;
-  // uniform tile rows: bound the staged tile by a split at every element row;
-  // shrink the tile until it fits in shared memory
-  for (;;) {
-    c.tile_nodes = ((TX + 1) * (N - 1) + 1) * ((TZ + 1) * N + 1);
-    c.own_nodes = (TX * (N - 1) + 1) * (TZ * N + 1);
-    if (bulk_smem(N, c.ndof, c.mixed, c.tile_nodes, c.own_nodes, c.nmat, 0, 0) <= 200 * 1024) break;
-    if (TX == 1 && TZ == 1) return fail(SEM2D_E_UNSUPPORTED, "no tile fits in shared memory");
-    if (TX >= TZ) TX = std::max(1, TX / 2);
-    else TZ = std::max(1, TZ / 2);
-  }
+  c.fast = a->mat_iso ? 1 : 0;
+  c.nplanes = strip_plane_count(c.ndof, c.nmat, 0, 0);
+  if (bulk_smem(N, c.ndof, c.mixed, c.nplanes) > 227 * 1024)
+    return fail(SEM2D_E_UNSUPPORTED, "the stage buffers do not fit in shared memory");
   if (configure_bulk(c)) return fail(SEM2D_E_CUDA, bulk_last_error());
   c.grid_x = (a->nx + TX - 1) / TX;
   c.grid_y = (a->nz + TZ - 1) / TZ;
@@ -133,6 +141,7 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
   c.nt = a->nt;
   c.step = reinterpret_cast<int *>(scratch);
   c.done = reinterpret_cast<unsigned *>(scratch + 4);
+  c.error = reinterpret_cast<int *>(scratch + 8);
   c.scheme = 0;
   c.dt = a->dt;
   c.cv = a->dt;

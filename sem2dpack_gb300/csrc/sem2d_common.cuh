@@ -17,8 +17,14 @@
 namespace sem2d {
 
 constexpr int kMaxN = 9;          // largest NGLL compiled
-constexpr int kBulkThreads = 256; // threads of the bulk kernel
 constexpr int kMaxSrc = 64;
+
+// material layouts: lattice planes (continuous material), one value per
+// element GLL point, or one value per element (homogeneous elements); the
+// element layouts are in structured element order (ez*nx + ex)
+constexpr int kMatNode = 0;
+constexpr int kMatPoint = 1;
+constexpr int kMatElement = 2;
 
 // Parameters of the per-node fault update (FP64 fault state).
 template <typename real>
@@ -42,6 +48,10 @@ struct FaultParams {
   double normal_V, normal_coef;
   const double *swf_dc, *swf_mus, *swf_mud, *swf_p, *swf_alpha;
   const double *rsf_dc, *rsf_mus, *rsf_a, *rsf_b, *rsf_vstar, *rsf_vc, *rsf_Tc, *rsf_coeft;
+  // time weakening (0 = none), alone when friction == 3
+  int twf_kind;
+  double twf_mus, twf_mud, twf_mu0, twf_X, twf_Z, twf_V, twf_L, twf_T, twf_Dc;
+  const double *fxz;    // (2,nflt) positions of the side-1 nodes
   // state
   double *D, *V, *T, *Tstick, *MU, *theta, *sigma;
   // outputs: series[(q + onx*(rec + 6*sample))]
@@ -78,7 +88,7 @@ struct BulkParams {
   // material
   int mat_iso;      // isotropic: planes (la, mu) [P-SV] or (mu) [SH]
   const real *mat[4];
-  int mat_elem;     // 1: per element GLL point (structured element order)
+  int mat_elem;     // material layout: kMatNode, kMatPoint or kMatElement
   const real *kveta;// per element GLL point or null
   const real *rmass;// lattice plane (both dofs equal away from the perimeter)
   // element geometry (rectilinear): per column / per row
@@ -113,6 +123,11 @@ struct BulkParams {
   int scheme;             // 0 leapfrog, 1 Newmark (beta = 0)
   real dt, cv, cpred, cd2;// cv: coef a->v, cpred: (1-gamma)dt, cd2: (0.5-beta)dt^2
   int kd2;
+  real width;             // 2.5D seismogenic width W, 0 for a 2D problem
+  int nmat;               // material planes (node layout) or arrays (element layout)
+  int has_kv;             // Kelvin-Voigt viscosity present
+  int nplanes;            // lattice planes staged per batch (strip_planes)
+  int *error;             // sticky device error flag (SEM2D_E_*)
 };
 
 // Perimeter slot of lattice node (I,J): bottom row, top row, left column,

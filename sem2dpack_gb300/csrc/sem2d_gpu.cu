@@ -37,12 +37,16 @@ struct FaultScalars {
   double coefA2V = 0, coefA2D = 0, normal_V = 0, normal_T = 1, normal_L = 1;
   int opening = 0, swf_kind = 1, swf_healing = 0, rsf_kind = 1, normal_kind = 1;
   int oit = 0, oitd = 1, oix1 = 1, oixd = 1;
+  int twf_kind = 0;
+  double twf_mus = 0.6, twf_mud = 0.5, twf_mu0 = 0.6, twf_X = 0, twf_Z = 0, twf_V = 1e3, twf_L = 1,
+         twf_T = 0, twf_Dc = 0;
 };
 
 struct sem2d_handle {
   // problem
   std::vector<double> H, w;          // GLL derivative matrix and weights
   int kd2 = 0;
+  double width = 0;  // 2.5D seismogenic width, 0 = 2D
   FaultScalars fs;
   int N = 0, ndof = 0, nelem = 0, npoin = 0, nt = 0, mixed = 0, scheme = 0;
   double dt = 0, beta = 0, gamma = 0.5;
@@ -51,7 +55,7 @@ struct sem2d_handle {
   std::vector<int> row0;             // [nz+1]
   std::vector<long long> glob2lat;   // global node -> J*pitch + I
   std::vector<int> elem_ex, elem_ez; // reference element -> structured position
-  int TX = 8, TZ = 8, tile_nodes = 0, own_nodes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
+  int TX = 8, TZ = 8, nplanes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
   std::vector<int> ztile;            // tile-row boundaries (element rows)
   int *d_ztile = nullptr;
   bool keep_accel = false;
@@ -85,6 +89,16 @@ struct sem2d_handle {
   long long launches = 0;
   cudaGraphExec_t graph_exec = nullptr;
   std::string err;
+  // a batch of independent problems advanced by one launch per step: the
+  // members hold the problems, the batch holds their parameter blocks (by
+  // buffer parity), the work units and the step counters
+  std::vector<sem2d_handle *> subs;
+  sem2d_handle *owner = nullptr;    // the batch a member belongs to
+  bool owns_stream = true;
+  void *d_params[2] = {nullptr, nullptr};
+  void *d_units = nullptr;
+  int nunits = 0, batch_grid = 0;
+  bool batch_open = false;          // members may still be added
 };
 
 namespace {
@@ -93,7 +107,7 @@ enum FaultArr {
   F_D64, F_V64, F_A64, F_RM, F_N1, F_B, F_INVM1, F_INVM2, F_Z, F_T0, F_COH,
   F_SWF_DC, F_SWF_MUS, F_SWF_MUD, F_SWF_P, F_SWF_ALPHA,
   F_RSF_DC, F_RSF_MUS, F_RSF_A, F_RSF_B, F_RSF_VSTAR, F_RSF_VC, F_RSF_TC, F_RSF_COEFT,
-  F_D, F_V, F_T, F_TSTICK, F_MU, F_THETA, F_SIGMA, F_SERIES, F_COUNT
+  F_D, F_V, F_T, F_TSTICK, F_MU, F_THETA, F_SIGMA, F_SERIES, F_XZ, F_COUNT
 };
 
 #define CK(call)                                                                       \
@@ -104,6 +118,12 @@ enum FaultArr {
       return SEM2D_E_CUDA;                                                             \
     }                                                                                  \
   } while (0)
+
+// the common case the step kernel compiles separately: isotropic material,
+// leapfrog, no Kelvin-Voigt, no 2.5D term
+bool fast_path(const sem2d_handle *h) {
+  return h->mat_iso && h->scheme == 0 && !h->has_kv && !(h->width > 0);
+}
 
 int set_err(sem2d_handle *h, int code, const std::string &m) {
   h->err = m;
@@ -261,8 +281,31 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
   else src = iso ? std::vector<const double *>{d->mu} : std::vector<const double *>{d->mu, d->mux};
   h->nmat = int(src.size());
   h->mat_iso = iso;
+  if (d->width > 0 && !iso)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "the 2.5D term needs an isotropic material");
+  // one value per element when every element is homogeneous (the
+  // reference then shares one coefficient set per tag, mat_gen.f90:358-361)
+  bool elem_const = true;
+  for (int e = 0; e < ne && elem_const; ++e)
+    for (size_t m = 0; m < src.size() && elem_const; ++m) {
+      const double *v = src[m] + (size_t)NN * e;
+      for (int q = 1; q < NN; ++q)
+        if (v[q] != v[0]) {
+          elem_const = false;
+          break;
+        }
+    }
+  if (elem_const) {
+    h->mat_elem = kMatElement;
+    for (size_t m = 0; m < src.size(); ++m) {
+      std::vector<double> el((size_t)ne);
+      for (int e = 0; e < ne; ++e) el[(size_t)h->elem_ez[e] * h->nx + h->elem_ex[e]] = src[m][(size_t)NN * e];
+      int st = upload_real(h, &h->mat[m], el);
+      if (st) return st;
+    }
+  }
   // node layout when every shared node carries one value
-  bool node = true;
+  bool node = !elem_const;
   std::vector<std::vector<double>> planes(src.size(), std::vector<double>(h->plane, 0.0));
   std::vector<char> seen(h->plane, 0);
   for (int e = 0; e < ne && node; ++e)
@@ -278,9 +321,9 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
       }
       seen[L] = 1;
     }
-  h->mat_elem = node ? 0 : 1;
+  if (!elem_const) h->mat_elem = node ? kMatNode : kMatPoint;
   int st;
-  for (size_t m = 0; m < src.size(); ++m) {
+  for (size_t m = 0; m < src.size() && !elem_const; ++m) {
     if (node) {
       st = upload_real(h, &h->mat[m], planes[m]);
     } else {
@@ -370,9 +413,12 @@ int upload_fault(sem2d_handle *h, const sem2d_problem_desc *d) {
     if (!d->rsf_dc || !d->rsf_mus || !d->rsf_a || !d->rsf_b || !d->rsf_vstar)
       return set_err(h, SEM2D_E_ARG, "missing RSF parameters");
     if (d->rsf_kind < 1 || d->rsf_kind > 4) return set_err(h, SEM2D_E_ARG, "rsf_kind out of range");
-  } else {
-    return set_err(h, SEM2D_E_UNSUPPORTED, "fault without SWF or RSF friction");
+  } else if (d->flt_friction != SEM2D_FRICTION_TWF) {
+    return set_err(h, SEM2D_E_UNSUPPORTED, "fault without SWF, RSF or TWF friction");
   }
+  if (d->twf_kind < 0 || d->twf_kind > 3) return set_err(h, SEM2D_E_ARG, "twf_kind out of range");
+  if ((d->twf_kind || d->flt_friction == SEM2D_FRICTION_TWF) && (!(d->twf_L > 0) || !(d->twf_V > 0)))
+    return set_err(h, SEM2D_E_ARG, "time weakening needs L > 0 and V > 0");
   h->friction = d->flt_friction;
   auto vec = [&](const double *p, size_t n, double fill) {
     std::vector<double> v(n, fill);
@@ -431,6 +477,13 @@ int upload_fault(sem2d_handle *h, const sem2d_problem_desc *d) {
   h->onx = (oixn - oix1) / oixd + 1;
   h->fnsamp = std::max(d->flt_nsamp, 0);
   if ((st = dalloc(h, &h->fd[F_SERIES], (size_t)h->onx * 6 * std::max(h->fnsamp, 1)))) return st;
+  std::vector<double> xz(2 * (size_t)nf);
+  for (int k = 0; k < nf; ++k) {
+    const int p = d->flt_node1[k] - 1;
+    xz[2 * k] = d->coord[2 * (size_t)p];
+    xz[2 * k + 1] = d->coord[2 * (size_t)p + 1];
+  }
+  if ((st = up(F_XZ, xz))) return st;
   return SEM2D_OK;
 }
 
@@ -465,7 +518,18 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.coefA2V = s.coefA2V;
   f.coefA2D = s.coefA2D;
   f.opening = s.opening;
-  f.friction = h->friction == SEM2D_FRICTION_RSF ? 2 : 1;
+  f.friction = h->friction == SEM2D_FRICTION_RSF ? 2 : h->friction == SEM2D_FRICTION_TWF ? 3 : 1;
+  f.twf_kind = s.twf_kind;
+  f.twf_mus = s.twf_mus;
+  f.twf_mud = s.twf_mud;
+  f.twf_mu0 = s.twf_mu0;
+  f.twf_X = s.twf_X;
+  f.twf_Z = s.twf_Z;
+  f.twf_V = s.twf_V;
+  f.twf_L = s.twf_L;
+  f.twf_T = s.twf_T;
+  f.twf_Dc = s.twf_Dc;
+  f.fxz = h->fd[F_XZ];
   f.swf_kind = s.swf_kind;
   f.swf_healing = s.swf_healing;
   f.rsf_kind = s.rsf_kind;
@@ -522,18 +586,21 @@ int launch_fault_init(sem2d_handle *h) {
   return SEM2D_OK;
 }
 
+// the type-erased description of one step of problem h from buffer parity
+// cur; f holds the fault parameters the description points to
 template <typename real>
-int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
+BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
   bc.mixed = h->mixed;
-  bc.tile_nodes = h->tile_nodes;
-  bc.own_nodes = h->own_nodes;
+  bc.nplanes = h->nplanes;
   bc.nmat = h->nmat;
   bc.has_kv = h->has_kv;
   bc.mat_elem = h->mat_elem;
   bc.mat_iso = h->mat_iso;
+  bc.fast = fast_path(h);
+  bc.error = h->d_error;
   bc.grid_x = (h->nx + h->TX - 1) / h->TX;
   bc.grid_y = int(h->ztile.size()) - 1;
   bc.LX = h->LX;
@@ -561,7 +628,7 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   bc.jf1 = h->nflt ? h->jf1 : -1;
   bc.jf2 = h->nflt ? h->jf2 : -1;
   bc.has_fault = h->nflt ? 1 : 0;
-  FaultParams<real> f{};
+  f = FaultParams<real>{};
   if (h->nflt) {
     f = fault_params<real>(h, cur);
     bc.flt = &f;
@@ -592,9 +659,17 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   bc.cpred = (1.0 - h->gamma) * h->dt;
   bc.cd2 = (0.5 - h->beta) * h->dt * h->dt;
   bc.kd2 = h->kd2;
+  bc.width = h->width;
   bc.H = h->H.data();
   bc.w = h->w.data();
   bc.stream = h->stream;
+  return bc;
+}
+
+template <typename real>
+int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
+  FaultParams<real> f;
+  BulkConfig bc = make_config<real>(h, cur, f);
   if (ev) CK(cudaEventRecord(ev[0], h->stream));
   int st = launch_bulk(bc);
   if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
@@ -624,7 +699,45 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   return SEM2D_OK;
 }
 
+template <typename real>
+int launch_batch_step(sem2d_handle *h, cudaEvent_t *ev = nullptr) {
+  FaultParams<real> f;
+  BulkConfig bc = make_config<real>(h->subs[0], h->cur, f);
+  bc.stream = h->stream;
+  BatchLaunch b;
+  b.params = h->d_params[h->cur];
+  b.units = h->d_units;
+  b.nunits = h->nunits;
+  b.grid = h->batch_grid;
+  b.step = h->d_step;
+  b.done = h->d_done;
+  if (ev) CK(cudaEventRecord(ev[0], h->stream));
+  if (launch_batch(bc, b)) return set_err(h, SEM2D_E_CUDA, std::string("batch launch: ") + bulk_last_error());
+  h->launches++;
+  if (ev)
+    for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ev[q], h->stream));
+  return SEM2D_OK;
+}
+
+// members follow the batch's step count and buffer parity
+void sync_members(sem2d_handle *h) {
+  for (sem2d_handle *m : h->subs) {
+    m->cur = h->cur;
+    m->steps = h->steps;
+  }
+}
+
 int launch_steps(sem2d_handle *h, int n) {
+  if (!h->subs.empty()) {
+    for (int k = 0; k < n; ++k) {
+      const int st = h->mixed ? launch_batch_step<float>(h) : launch_batch_step<double>(h);
+      if (st) return st;
+      h->cur = 1 - h->cur;
+      h->steps++;
+    }
+    sync_members(h);
+    return SEM2D_OK;
+  }
   for (int k = 0; k < n; ++k) {
     const int st = h->mixed ? launch_one_step<float>(h, h->cur) : launch_one_step<double>(h, h->cur);
     if (st) return st;
@@ -634,7 +747,10 @@ int launch_steps(sem2d_handle *h, int n) {
   return SEM2D_OK;
 }
 
-int kernels_per_step(const sem2d_handle *h) { return 1 + (h->nrec && h->rec_separate ? 1 : 0); }
+int kernels_per_step(const sem2d_handle *h) {
+  if (!h->subs.empty()) return 1;
+  return 1 + (h->nrec && h->rec_separate ? 1 : 0);
+}
 
 int ensure_graph(sem2d_handle *h) {
   if (h->graph_exec) return SEM2D_OK;
@@ -656,6 +772,19 @@ int ensure_graph(sem2d_handle *h) {
 }
 
 int reset_state(sem2d_handle *h) {
+  if (!h->subs.empty()) {
+    for (sem2d_handle *m : h->subs) {
+      const int st = reset_state(m);
+      if (st) return set_err(h, st, m->err);
+    }
+    CK(cudaMemsetAsync(h->d_step, 0, sizeof(int), h->stream));
+    CK(cudaMemsetAsync(h->d_done, 0, sizeof(unsigned), h->stream));
+    CK(cudaMemsetAsync(h->d_error, 0, sizeof(int), h->stream));
+    h->cur = 0;
+    h->steps = 0;
+    sync_members(h);
+    return SEM2D_OK;
+  }
   const size_t rs = h->mixed ? sizeof(float) : sizeof(double);
   for (int b = 0; b < 2; ++b) {
     CK(cudaMemsetAsync(h->D[b], 0, rs * h->plane * h->ndof, h->stream));
@@ -685,13 +814,21 @@ int reset_state(sem2d_handle *h) {
 int check_device_error(sem2d_handle *h) {
   int e = 0;
   CK(cudaStreamSynchronize(h->stream));
+  for (sem2d_handle *m : h->subs) {
+    const int st = check_device_error(m);
+    if (st) return set_err(h, st, m->err);
+  }
   CK(cudaMemcpy(&e, h->d_error, sizeof(int), cudaMemcpyDeviceToHost));
   if (e == SEM2D_E_NR) return set_err(h, SEM2D_E_NR, "rate-and-state Newton solver did not converge");
+  if (e == SEM2D_E_TIMEOUT) return set_err(h, SEM2D_E_TIMEOUT, "a bounded wait for shared-memory copies expired");
   if (e) return set_err(h, e, "device error");
   return SEM2D_OK;
 }
 
-int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
+// force_tz > 0 sets the chunk height (batch members share one);
+// `shared` is a stream owned by a batch
+int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t shared = nullptr,
+                int force_tz = 0) {
   if (d->ngll != 5 && d->ngll != 6 && d->ngll != 9)
     return set_err(h, SEM2D_E_UNSUPPORTED, "GPU kernels are compiled for ngll in {5, 6, 9}");
   if (d->ndof != 1 && d->ndof != 2) return set_err(h, SEM2D_E_ARG, "ndof must be 1 or 2");
@@ -714,7 +851,12 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
   h->beta = d->beta;
   h->gamma = h->scheme ? d->gamma : 0.5;
   h->keep_accel = h->scheme == 1 || d->rec_field == 'A';
-  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  if (shared) {
+    h->stream = shared;
+    h->owns_stream = false;
+  } else {
+    CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  }
   int st;
   if ((st = detect_lattice(h, d))) return st;
   if ((st = upload_fault(h, d))) return st;
@@ -736,6 +878,17 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
     fs.oitd = d->flt_oitd > 0 ? d->flt_oitd : 1;
     fs.oix1 = d->flt_oix1 > 0 ? d->flt_oix1 : 1;
     fs.oixd = d->flt_oixd > 0 ? d->flt_oixd : 1;
+    fs.twf_kind = d->twf_kind;
+    if (d->nflt > 0 && d->flt_friction == SEM2D_FRICTION_TWF && fs.twf_kind == 0) fs.twf_kind = 1;
+    fs.twf_mus = d->twf_mus;
+    fs.twf_mud = d->twf_mud;
+    fs.twf_mu0 = d->twf_mu0;
+    fs.twf_X = d->twf_X;
+    fs.twf_Z = d->twf_Z;
+    fs.twf_V = d->twf_V;
+    fs.twf_L = d->twf_L;
+    fs.twf_T = d->twf_T;
+    fs.twf_Dc = d->twf_Dc;
   }
   const size_t rs = h->mixed ? sizeof(float) : sizeof(double);
   for (int b = 0; b < 2; ++b) {
@@ -755,6 +908,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
   h->H.assign(d->hprime, d->hprime + h->N * h->N);
   h->w.assign(d->wgll, d->wgll + h->N);
   h->kd2 = d->kd2_form ? 1 : 0;
+  h->width = d->width > 0 ? d->width : 0.0;
   // sources: lattice position and per-step amplitude (SO_add, src_gen.f90:290-317)
   h->nsrc = d->nsrc;
   if (h->nsrc > kMaxSrc) return set_err(h, SEM2D_E_UNSUPPORTED, "too many sources");
@@ -795,12 +949,31 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
     h->rec_separate = !d->rec_node && h->rec_field != 'D';
   }
   if ((st = dalloc(h, &h->sis, (size_t)std::max(h->rec_nsamp, 1) * std::max(h->nrec, 1) * h->ndof))) return st;
-  // tile shape: TX element columns by ztile rows, fault split kept inside a tile
-  if (choose_tiles(h->N, h->ndof, h->mixed, h->nx, h->nz, h->row0.data(), h->nmat, h->has_kv,
-                   h->mat_elem, &h->TX, &h->TZ))
-    return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no tile shape fits: ") + bulk_last_error());
+  // strips of TX element columns by chunks of element rows, fault split kept inside a chunk
+  h->TX = strip_width(h->N);
+  if (h->TX <= 0) return set_err(h, SEM2D_E_UNSUPPORTED, "NGLL not compiled");
+  h->nplanes = strip_plane_count(h->ndof, h->nmat, h->mat_elem, h->scheme);
+  {
+    BulkConfig bc;
+    bc.N = h->N;
+    bc.ndof = h->ndof;
+    bc.mixed = h->mixed;
+    bc.nplanes = h->nplanes;
+    bc.nmat = h->nmat;
+    bc.has_kv = h->has_kv;
+    bc.mat_elem = h->mat_elem;
+    bc.mat_iso = h->mat_iso;
+    bc.fast = fast_path(h);
+    bc.nx = h->nx;
+    bc.nz = h->nz;
+    if (force_tz > 0) h->TZ = std::min(std::min(force_tz, kMaxChunkRows), h->nz);
+    else if (choose_tiles(bc, h->row0.data(), &h->TZ))
+      return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no strip configuration fits: ") + bulk_last_error());
+  }
   h->ztile = tile_rows(h->N, h->nz, h->row0.data(), h->TZ);
-  tile_sizes(h->N, h->nx, h->row0.data(), h->TX, h->ztile, &h->tile_nodes, &h->own_nodes);
+  for (size_t y = 0; y + 1 < h->ztile.size(); ++y)
+    if (h->ztile[y + 1] - h->ztile[y] + 1 > 2 * kMaxChunkRows + 1)
+      return set_err(h, SEM2D_E_UNSUPPORTED, "element-row chunk too tall");
   if ((st = dupload(h, &h->d_ztile, h->ztile))) return st;
   if (h->nrec) {
     // receiver lattice positions; for the fused path, grouped by owning tile
@@ -854,11 +1027,12 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
     bc.N = h->N;
     bc.ndof = h->ndof;
     bc.mixed = h->mixed;
-    bc.tile_nodes = h->tile_nodes;
-    bc.own_nodes = h->own_nodes;
+    bc.nplanes = h->nplanes;
     bc.nmat = h->nmat;
     bc.has_kv = h->has_kv;
     bc.mat_elem = h->mat_elem;
+    bc.mat_iso = h->mat_iso;
+    bc.fast = fast_path(h);
     if (configure_bulk(bc)) return set_err(h, SEM2D_E_CUDA, bulk_last_error());
   }
   if ((st = reset_state(h))) return st;
@@ -868,9 +1042,183 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
 
 }  // namespace
 
+namespace {
+
+constexpr int kBatchChunk = 16;  // element rows per chunk of a batch member
+
+int batch_open_impl(sem2d_handle *h) {
+  CK(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+  h->batch_open = true;
+  return SEM2D_OK;
+}
+
+int batch_add_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
+  auto m = new (std::nothrow) sem2d_handle();
+  if (!m) return set_err(h, SEM2D_E_NOMEM, "out of host memory");
+  m->owner = h;
+  h->subs.push_back(m);
+  int st;
+  try {
+    st = create_impl(m, d, h->stream, kBatchChunk);
+  } catch (const std::bad_alloc &) {
+    m->err = "out of host memory";
+    st = SEM2D_E_NOMEM;
+  }
+  if (st) {
+    const std::string e = m->err;
+    h->subs.pop_back();
+    m->owner = nullptr;
+    sem2d_gpu_destroy(m);
+    return set_err(h, st, "problem " + std::to_string(h->subs.size()) + ": " + e);
+  }
+  // the members' host-side copies of the mesh numbering are not needed again
+  std::vector<int>().swap(m->elem_ex);
+  std::vector<int>().swap(m->elem_ez);
+  return SEM2D_OK;
+}
+
+int batch_close_impl(sem2d_handle *h) {
+  const int nsim = int(h->subs.size());
+  if (nsim <= 0) return set_err(h, SEM2D_E_ARG, "empty batch");
+  const sem2d_handle *a = h->subs[0];
+  for (const sem2d_handle *m : h->subs) {
+    if (m->N != a->N || m->ndof != a->ndof || m->mixed != a->mixed || m->mat_elem != a->mat_elem ||
+        m->nplanes != a->nplanes || fast_path(m) != fast_path(a) || m->mat_iso != a->mat_iso ||
+        m->has_kv != a->has_kv || m->scheme != a->scheme)
+      return set_err(h, SEM2D_E_UNSUPPORTED,
+                     "batch members differ in NGLL, dof count, precision, scheme or material layout");
+    if (m->nt != a->nt) return set_err(h, SEM2D_E_UNSUPPORTED, "batch members differ in the number of steps");
+    if (m->nrec && m->rec_separate)
+      return set_err(h, SEM2D_E_UNSUPPORTED, "interpolated velocity/acceleration receivers in a batch");
+  }
+  h->N = a->N;
+  h->ndof = a->ndof;
+  h->mixed = a->mixed;
+  h->nt = a->nt;
+  h->scheme = a->scheme;
+  h->TX = a->TX;
+  h->TZ = a->TZ;
+  int st;
+  if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)))
+    return st;
+  // parameter blocks of every member for both buffer parities
+  const size_t pb = params_bytes(h->N, h->mixed);
+  for (int cur = 0; cur < 2; ++cur) {
+    std::vector<unsigned char> blk(pb * nsim);
+    for (int i = 0; i < nsim; ++i) {
+      sem2d_handle *m = h->subs[i];
+      if (h->mixed) {
+        FaultParams<float> f;
+        BulkConfig bc = make_config<float>(m, cur, f);
+        fill_params_block(bc, blk.data() + pb * i);
+      } else {
+        FaultParams<double> f;
+        BulkConfig bc = make_config<double>(m, cur, f);
+        fill_params_block(bc, blk.data() + pb * i);
+      }
+    }
+    if ((st = dupload(h, reinterpret_cast<unsigned char **>(&h->d_params[cur]), blk))) return st;
+  }
+  // work units, member by member
+  std::vector<int> units;
+  for (int i = 0; i < nsim; ++i) {
+    const sem2d_handle *m = h->subs[i];
+    const int gx = (m->nx + m->TX - 1) / m->TX, gy = int(m->ztile.size()) - 1;
+    for (int y = 0; y < gy; ++y)
+      for (int x = 0; x < gx; ++x) units.insert(units.end(), {i, x, y, gx});
+  }
+  h->nunits = int(units.size() / 4);
+  if ((st = dupload(h, reinterpret_cast<int **>(&h->d_units), units))) return st;
+  BulkConfig bc;
+  bc.N = h->N;
+  bc.ndof = h->ndof;
+  bc.mixed = h->mixed;
+  bc.nplanes = a->nplanes;
+  bc.nmat = a->nmat;
+  bc.has_kv = a->has_kv;
+  bc.mat_elem = a->mat_elem;
+  bc.mat_iso = a->mat_iso;
+  bc.fast = fast_path(a);
+  const int per_sm = occupancy_bulk(bc);
+  if (per_sm <= 0) return set_err(h, SEM2D_E_CUDA, std::string("no resident CTA: ") + bulk_last_error());
+  int dev = 0, nsm = 1;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  h->batch_grid = std::min(h->nunits, per_sm * nsm);
+  if ((st = reset_state(h))) return st;
+  CK(cudaStreamSynchronize(h->stream));
+  h->batch_open = false;
+  return SEM2D_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int sem2d_gpu_version(void) { return SEM2D_GPU_ABI_VERSION; }
+
+int sem2d_gpu_batch_open(sem2d_handle **out) {
+  if (!out) {
+    g_create_err = "null argument";
+    return SEM2D_E_ARG;
+  }
+  *out = nullptr;
+  auto h = new (std::nothrow) sem2d_handle();
+  if (!h) {
+    g_create_err = "out of host memory";
+    return SEM2D_E_NOMEM;
+  }
+  const int st = batch_open_impl(h);
+  if (st) {
+    g_create_err = h->err;
+    sem2d_gpu_destroy(h);
+    return st;
+  }
+  *out = h;
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_batch_add(sem2d_handle *h, const sem2d_problem_desc *desc) {
+  if (!h || !desc) return SEM2D_E_ARG;
+  if (!h->batch_open) return set_err(h, SEM2D_E_STATE, "not an open batch");
+  return batch_add_impl(h, desc);
+}
+
+int sem2d_gpu_batch_close(sem2d_handle *h) {
+  if (!h) return SEM2D_E_ARG;
+  if (!h->batch_open) return set_err(h, SEM2D_E_STATE, "not an open batch");
+  int st;
+  try {
+    st = batch_close_impl(h);
+  } catch (const std::bad_alloc &) {
+    st = set_err(h, SEM2D_E_NOMEM, "out of host memory");
+  }
+  return st;
+}
+
+int sem2d_gpu_create_batch(const sem2d_problem_desc *descs, int nsim, sem2d_handle **out) {
+  if (!descs || !out || nsim <= 0) {
+    g_create_err = "null argument or empty batch";
+    return SEM2D_E_ARG;
+  }
+  int st = sem2d_gpu_batch_open(out);
+  if (st) return st;
+  for (int i = 0; i < nsim && !st; ++i) st = sem2d_gpu_batch_add(*out, &descs[i]);
+  if (!st) st = sem2d_gpu_batch_close(*out);
+  if (st) {
+    g_create_err = (*out)->err;
+    sem2d_gpu_destroy(*out);
+    *out = nullptr;
+  }
+  return st;
+}
+
+int sem2d_gpu_batch_size(sem2d_handle *h) { return h ? int(h->subs.size()) : SEM2D_E_ARG; }
+
+sem2d_handle *sem2d_gpu_batch_member(sem2d_handle *h, int i) {
+  if (!h || i < 0 || i >= int(h->subs.size())) return nullptr;
+  return h->subs[i];
+}
 
 int sem2d_gpu_device_count(void) {
   int n = 0;
@@ -907,6 +1255,8 @@ int sem2d_gpu_create(const sem2d_problem_desc *desc, sem2d_handle **out) {
 
 int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
   if (!h) return SEM2D_E_ARG;
+  if (h->owner) return set_err(h, SEM2D_E_STATE, "a batch member is stepped through its batch");
+  if (h->batch_open) return set_err(h, SEM2D_E_STATE, "the batch is still open");
   if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
   if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
   int st;
@@ -928,11 +1278,14 @@ int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
     }
   }
   if (left && (st = launch_steps(h, left))) return st;
+  sync_members(h);
   return SEM2D_OK;
 }
 
 int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms) {
   if (!h || !ms) return SEM2D_E_ARG;
+  if (h->owner) return set_err(h, SEM2D_E_STATE, "a batch member is stepped through its batch");
+  if (h->batch_open) return set_err(h, SEM2D_E_STATE, "the batch is still open");
   if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
   if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
   ms[0] = ms[1] = ms[2] = 0.0;
@@ -943,10 +1296,15 @@ int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms) {
   for (int done = 0; done < nsteps && !st;) {
     const int nb = std::min(kBatch, nsteps - done);
     for (int k = 0; k < nb && !st; ++k) {
-      st = h->mixed ? launch_one_step<float>(h, h->cur, &ev[4 * k]) : launch_one_step<double>(h, h->cur, &ev[4 * k]);
+      if (!h->subs.empty())
+        st = h->mixed ? launch_batch_step<float>(h, &ev[4 * k]) : launch_batch_step<double>(h, &ev[4 * k]);
+      else
+        st = h->mixed ? launch_one_step<float>(h, h->cur, &ev[4 * k])
+                      : launch_one_step<double>(h, h->cur, &ev[4 * k]);
       h->cur = 1 - h->cur;
       h->steps++;
     }
+    sync_members(h);
     if (st) break;
     cudaError_t e = cudaStreamSynchronize(h->stream);
     if (e != cudaSuccess) {
@@ -977,6 +1335,7 @@ int sem2d_gpu_current_step(sem2d_handle *h) { return h ? h->steps : SEM2D_E_ARG;
 
 int sem2d_gpu_reset(sem2d_handle *h) {
   if (!h) return SEM2D_E_ARG;
+  if (h->owner) return set_err(h, SEM2D_E_STATE, "a batch member is reset through its batch");
   int st = reset_state(h);
   if (st) return st;
   return check_device_error(h);
@@ -984,6 +1343,7 @@ int sem2d_gpu_reset(sem2d_handle *h) {
 
 int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc, double *accel) {
   if (!h) return SEM2D_E_ARG;
+  if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
   int st = check_device_error(h);
   if (st) return st;
   if (accel && !h->keep_accel) return set_err(h, SEM2D_E_STATE, "accelerations are not kept (leapfrog without field 'A')");
@@ -1009,6 +1369,7 @@ int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc, double *
 
 int sem2d_gpu_get_seismograms(sem2d_handle *h, double *sis) {
   if (!h || !sis) return SEM2D_E_ARG;
+  if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
   int st = check_device_error(h);
   if (st) return st;
   if (h->nrec)
@@ -1018,6 +1379,7 @@ int sem2d_gpu_get_seismograms(sem2d_handle *h, double *sis) {
 
 int sem2d_gpu_get_fault(sem2d_handle *h, double *out) {
   if (!h || !out) return SEM2D_E_ARG;
+  if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
   int st = check_device_error(h);
   if (st) return st;
   if (h->nflt && h->fnsamp > 0)
@@ -1027,6 +1389,7 @@ int sem2d_gpu_get_fault(sem2d_handle *h, double *out) {
 
 int sem2d_gpu_get_fault_state(sem2d_handle *h, double *D, double *V, double *T, double *MU, double *theta) {
   if (!h) return SEM2D_E_ARG;
+  if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
   int st = check_device_error(h);
   if (st) return st;
   if (!h->nflt) return SEM2D_OK;
@@ -1050,10 +1413,21 @@ int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz) {
 
 int sem2d_gpu_destroy(sem2d_handle *h) {
   if (!h) return SEM2D_E_ARG;
+  if (h->owner && h->owner->subs.size()) {
+    // members are destroyed with their batch
+    bool member = false;
+    for (sem2d_handle *m : h->owner->subs) member = member || m == h;
+    if (member) return set_err(h, SEM2D_E_STATE, "a batch member is destroyed with its batch");
+  }
   if (h->stream) cudaStreamSynchronize(h->stream);
+  for (sem2d_handle *m : h->subs) {
+    m->owner = nullptr;
+    sem2d_gpu_destroy(m);
+  }
+  h->subs.clear();
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   for (void *p : h->allocs) cudaFree(p);
-  if (h->stream) cudaStreamDestroy(h->stream);
+  if (h->stream && h->owns_stream) cudaStreamDestroy(h->stream);
   delete h;
   return SEM2D_OK;
 }

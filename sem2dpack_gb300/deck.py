@@ -39,10 +39,30 @@ class Material:
 
 
 @dataclass
+class TimeWeakening:
+    """&BC_DYNFLT_TWF (bc_dynflt_twf.f90:52-100), reference defaults."""
+    kind: int = 1
+    mus: float = 0.6
+    mud: float = 0.5
+    mu0: float = 0.6
+    X: float = 0.0
+    Z: float = 0.0
+    V: float = 1e3
+    L: float = 1.0
+    T: float = float(np.finfo(np.float64).max)
+    Dc: float = float(np.finfo(np.float64).max)
+
+
+@dataclass
 class Fault:
-    """&BC_DEF kind='DYNFLT' + &BC_DYNFLT/_SWF/_RSF/_NOR (bc_dynflt.f90:100-178)."""
+    """&BC_DEF kind='DYNFLT' + &BC_DYNFLT/_SWF/_RSF/_TWF/_NOR (bc_dynflt.f90:100-178).
+
+    ``friction`` is 'SWF', 'RSF' or 'TWF'; ``twf`` adds a time-weakening law,
+    superimposed on SWF/RSF (friction='SWF','TWF' in Par.inp) or alone.
+    """
     tags: Tuple[int, int] = (5, 6)
     friction: str = "SWF"
+    twf: Optional[TimeWeakening] = None
     swf_kind: int = 1
     healing: bool = False
     rsf_kind: int = 1
@@ -116,6 +136,7 @@ class ParDeck:
     receivers: Optional[Receivers] = None
     precision: int = abi.PRECISION_FP64
     kd2_form: int = -1
+    width: float = 0.0   # W of &GENERAL; 0 = 2D (the reference's huge)
     # per element GLL point arrays (ngll,ngll,nelem) for hetero materials
     hetero: Dict[str, np.ndarray] = field(default_factory=dict)
 
@@ -167,7 +188,16 @@ class ParDeck:
             d.flt_value[i] = abi.FP_DEFAULTS[name]
             d.flt_array[i] = abi.P_double()
         if f is not None:
-            d.flt_friction = abi.FRICTION_RSF if f.friction.upper() == "RSF" else abi.FRICTION_SWF
+            d.flt_friction = {"RSF": abi.FRICTION_RSF, "TWF": abi.FRICTION_TWF}.get(
+                f.friction.upper(), abi.FRICTION_SWF)
+            tw = f.twf
+            if tw is None and d.flt_friction == abi.FRICTION_TWF:
+                tw = TimeWeakening()
+            if tw is not None:
+                d.twf_kind = tw.kind
+                d.twf_mus, d.twf_mud, d.twf_mu0 = tw.mus, tw.mud, tw.mu0
+                d.twf_X, d.twf_Z, d.twf_V, d.twf_L = tw.X, tw.Z, tw.V, tw.L
+                d.twf_T, d.twf_Dc = tw.T, tw.Dc
             d.swf_kind, d.swf_healing, d.rsf_kind = f.swf_kind, int(f.healing), f.rsf_kind
             d.normal_kind = f.normal_kind
             d.normal_T, d.normal_L, d.normal_V = f.normal_T, f.normal_L, f.normal_V
@@ -213,4 +243,5 @@ class ParDeck:
             d.rec_atnode, d.rec_isamp = int(r.atnode), r.isamp
             d.rec_field = r.field.encode()[:1]
         d.precision, d.kd2_form = self.precision, self.kd2_form
+        d.width = float(self.width)
         return d, keep

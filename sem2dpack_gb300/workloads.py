@@ -15,6 +15,11 @@ index); no external data set is involved.
                    (correlation 500 m, max 2 MPa), 3 km nucleation patch at
                    81 MPa, absorbing on all sides, 6000 steps.
   psv_rsf          P-SV rate-and-state rupture in a random medium (aging law).
+  batch_shots      independent P-SV shots of uneven size (64^2..512^2
+                   elements of 25 m, NGLL=5), each with its own 3-8 layer
+                   model (vs 1500-4000 m/s, vp = 1.73 vs, rho = 1700 +
+                   0.2 vp), a vertical Ricker force (f0 5-20 Hz) at a
+                   random interior point and 32 receivers, 3000 steps.
 Each builder takes ``scale`` to shrink the mesh (and steps) for tests.
 """
 import numpy as np
@@ -176,6 +181,48 @@ def psv_rsf(scale=1.0, nsteps=10000, precision=abi.PRECISION_MIXED, rsf_kind=2, 
     dt_est = 0.5 * (h * (1.0 - np.sqrt(3.0 / 7.0)) / 2.0) / (6000.0 * 1.25)
     deck.fault.otd = out_every * dt_est
     return deck, grid
+
+
+def batch_shots(nsim=256, scale=1.0, nsteps=3000, precision=abi.PRECISION_MIXED, seed_index=3):
+    """Decks of the batched-shot configuration.
+
+    Element side 25 m, fmax 40 Hz (the resolution check of CHECK_grid holds
+    for vs >= 1500 m/s); layer boundaries on element rows (&MESH_CART_DOMAIN
+    tags, velocity increasing with depth); absorbing on all four sides; CFL
+    0.5; receivers on a line 5 elements below the top.  ``scale`` shrinks
+    the element counts (64..512 -> 64*scale..512*scale, at least 4).
+    """
+    rng = _rng(seed_index)
+    h = 25.0
+    lo, hi = max(4, int(round(64 * scale))), max(4, int(round(512 * scale)))
+    decks = []
+    for _ in range(nsim):
+        n = int(rng.integers(lo, hi + 1))
+        L = n * h
+        nl = int(rng.integers(3, 9))
+        cuts = np.sort(rng.choice(np.arange(1, n), size=min(nl - 1, n - 1), replace=False))
+        bounds = [0] + [int(c) for c in cuts] + [n]
+        vs = np.sort(rng.uniform(1500.0, 4000.0, size=len(bounds) - 1))  # slowest at the top
+        domains, mats = [], []
+        for k in range(len(bounds) - 1):
+            # element rows counted from the bottom (1-based): layer 0 at the top
+            ez_top = n - bounds[k]
+            ez_bot = n - bounds[k + 1] + 1
+            domains.append((k + 1, (1, n), (ez_bot, ez_top)))
+            vp = 1.73 * vs[k]
+            mats.append(Material(tag=k + 1, rho=1700.0 + 0.2 * vp, cp=vp, cs=float(vs[k])))
+        f0 = float(rng.uniform(5.0, 20.0))
+        src = (float(rng.uniform(0.1, 0.9) * L), float(rng.uniform(0.1, 0.9) * L))
+        depth = L - 5 * h
+        decks.append(ParDeck(
+            ngll=5, ndof=2, fmax=40.0, xlim=(0.0, L), zlim=(0.0, L), nelem=(n, n),
+            domains=domains, materials=mats, absorbing=[1, 2, 3, 4],
+            time=Time(kind="leapfrog", courant=0.5, nsteps=nsteps),
+            sources=Sources(coords=[src], f0=f0, onset=1.2 / f0, ampli=1.0, angle=0.0),
+            receivers=Receivers(number=32, first=(0.05 * L, depth), last=(0.95 * L, depth), field="V"),
+            precision=precision,
+        ))
+    return decks
 
 
 def build(deck_or_pair):

@@ -158,7 +158,7 @@ def test_newmark_inabox():
     assert rel_l2(a, ao) <= 1e-10
 
 
-def test_reset_is_deterministic_and_tiles_agree(monkeypatch):
+def test_reset_is_deterministic_and_chunks_agree(monkeypatch):
     pair = workloads.sh_rupture(scale=0.1, nsteps=200)
     P, d = make(pair, PRECISION_FP64)
     g = Solver(d, owner=P)
@@ -169,13 +169,14 @@ def test_reset_is_deterministic_and_tiles_agree(monkeypatch):
     g.step(200)
     assert np.array_equal(a, g.seismograms())        # bitwise
     assert np.array_equal(fa, g.fault_series())
-    for tile in ("1x1", "4x2", "3x5"):
-        monkeypatch.setenv("SEM2D_TILE", tile)
+    for chunk in (1, 2, 5, 13):
+        monkeypatch.setenv("SEM2D_CHUNK", str(chunk))
         h = Solver(d, owner=P)
-        assert h.tile == tuple(int(v) for v in tile.split("x"))
+        assert h.tile[1] == chunk
         h.step(200)
-        assert np.array_equal(a, h.seismograms()), tile  # same per-node summation order
-    monkeypatch.delenv("SEM2D_TILE")
+        assert np.array_equal(a, h.seismograms()), chunk  # same per-node summation order
+        assert np.array_equal(fa, h.fault_series()), chunk
+    monkeypatch.delenv("SEM2D_CHUNK")
 
 
 def test_graph_and_direct_launches_agree(monkeypatch):
