@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="sh_rupture",
-                   choices=["sh_rupture", "plain_psv", "psv_rsf", "batch_shots"])
+                   choices=["sh_rupture", "plain_psv", "psv_rsf", "batch_shots", "gradient_shots"])
     p.add_argument("--nsim", type=int, default=256, help="problems of the batch_shots workload")
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -320,6 +320,91 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
         dist.destroy_process_group()
 
 
+def run_gradient(args, rank, world, local, torch, dist, barrier):
+    """Gradient workflow (8 shots on 512^2 elements): forward solves against
+    forward-with-checkpoints + adjoint; reports the cost ratio."""
+    import ctypes as C
+
+    import numpy as np
+
+    from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Solver, workloads
+    from sem2dpack_gb300._lib import lib
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    nt = args.time_steps or 400
+    models, start, true = workloads.gradient_shots(scale=args.scale, nsteps=nt, precision=prec)
+    every = max(1, int(round(np.sqrt(nt))))
+    pp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+    sims, obs = [], []
+    for m in models:
+        Pt = workloads.build(m.deck_for(*true))
+        st = Solver(Pt)
+        st.step(nt)
+        obs.append(st.seismograms())
+        st.close()
+        P = workloads.build(m.deck_for(*start))
+        d = P.desc()
+        d.precision = prec
+        d.adjoint = 1
+        sims.append((Solver(d, owner=P), d))
+    npoin = sims[0][1].npoin
+    grads = [np.zeros(npoin) for _ in range(3)]
+
+    def forward_only():
+        for s, _ in sims:
+            s._check(lib().sem2d_gpu_checkpoint_every(s.h, 0))
+            s.reset()
+        barrier()
+        t0 = time.perf_counter()
+        for s, _ in sims:
+            s.step(nt)
+        for s, _ in sims:
+            s.sync()
+        return time.perf_counter() - t0
+
+    def gradient():
+        for s, _ in sims:
+            s.reset()
+            s._check(lib().sem2d_gpu_checkpoint_every(s.h, every))
+        barrier()
+        t0 = time.perf_counter()
+        for k, (s, d) in enumerate(sims):
+            s.step(nt)
+            r = np.asfortranarray(s.seismograms() - obs[k])
+            s._check(lib().sem2d_gpu_adjoint(s.h, pp(r), pp(grads[0]), pp(grads[1]), pp(grads[2])))
+        return time.perf_counter() - t0
+
+    for _ in range(max(1, args.warmup)):
+        forward_only()
+        gradient()
+    clocks = ClockSampler(local)
+    clocks.start()
+    tf = [forward_only() for _ in range(args.steps)]
+    tg = [gradient() for _ in range(args.steps)]
+    clk = clocks.stop()
+    l0 = sum(s.launches for s, _ in sims)
+    fwd = min(tf)
+    grd = min(tg)
+    value = len(sims) * npoin * nt / fwd
+    name = ("gradient workflow: %d P-SV shots on %dx%d elements of 25 m, NGLL=5, %d of 4000 steps, "
+            "checkpoint every %d steps" % (len(sims), models[0].deck.nelem[0], models[0].deck.nelem[1], nt, every))
+    if rank == 0:
+        print(json.dumps({
+            "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * fwd,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32" if prec == PRECISION_MIXED else "f64", "data": "synthetic",
+            "config": {"workload": name, "global_batch": len(sims), "seq_len": 0, "parallelism": "replicas",
+                       "npoin": npoin, "time_steps_per_step": nt},
+            "gradient_cost": {"forward_s": fwd, "forward_and_adjoint_s": grd, "ratio": grd / fwd,
+                              "note": "forward with checkpoints + segment recomputation + adjoint, "
+                                      "over the plain forward solves of the same shots"},
+            "roofline": None, "cpu_baseline": None,
+            "e2e": None, "clocks": clk, "gpu_launches": l0,
+        }), flush=True)
+    for s, _ in sims:
+        s.close()
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -342,6 +427,9 @@ def main():
 
     if args.workload == "batch_shots":
         run_batch(args, rank, world, local, torch, dist, barrier)
+        return
+    if args.workload == "gradient_shots":
+        run_gradient(args, rank, world, local, torch, dist, barrier)
         return
     from sem2dpack_gb300 import Solver
     prob, name = make_workload(args)

@@ -161,6 +161,14 @@ typedef struct sem2d_problem_desc {
    * are those of flt_node1 (bc_dynflt.f90:302).                         */
   int twf_kind;
   double twf_mus, twf_mud, twf_mu0, twf_X, twf_Z, twf_V, twf_L, twf_T, twf_Dc;
+
+  /* ---- density at every element GLL point (ngll,ngll,nelem) ---- */
+  const double *rho;
+  /* 1 prepares the handle for sem2d_gpu_adjoint (gradients with respect
+   * to density and wave speeds at every node, mat_elastic.f90:189-321
+   * defines the moduli from rho, cp, cs): rho is required and the material
+   * must be continuous at nodes. */
+  int adjoint;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;
@@ -196,6 +204,24 @@ int sem2d_gpu_batch_size(sem2d_handle *h);
 /* Member i of a batch (owned by the batch, valid until it is destroyed),
  * for the get_* calls; NULL if out of range. */
 sem2d_handle *sem2d_gpu_batch_member(sem2d_handle *h, int i);
+
+/* ---- gradient of a seismogram misfit (no counterpart in the reference:
+ * SEM2DPACK has no adjoint) ----------------------------------------------
+ * For a handle created with desc->adjoint = 1: keep the forward state every
+ * `every` steps during the next run from step 0 (every <= 0 disables).
+ * Memory: (nt/every + 1) x 2 x ndof lattice planes. */
+int sem2d_gpu_checkpoint_every(sem2d_handle *h, int every);
+/* After all nt steps with checkpoints: the gradient of a misfit J with
+ * respect to density, P and S wave speed at every global node (npoin
+ * values each, NULL to skip), given resid = dJ/dsis laid out like the
+ * seismograms (rec_nsamp, nrec, ndof).  Discrete adjoint of the leapfrog
+ * step (reverse steps of the same element operator, the inverse mass and
+ * dashpot terms) with segment-wise recomputation from the checkpoints; the
+ * gradient covers the moduli, the mass and the absorbing dashpots.  NGLL=5,
+ * isotropic material continuous at nodes, leapfrog, no fault, Kelvin-Voigt
+ * or 2.5D term, receivers at nodes recording V or D. */
+int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, double *grad_vp,
+                      double *grad_vs);
 
 /* Replaces nsteps iterations of `do it=1,nt; call solve(pb); REC_store;
  * BC_write` (main.f90:51-96).  Asynchronous on the handle's stream; the

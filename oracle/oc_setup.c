@@ -1380,6 +1380,7 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
   }
   d->precision = dk->precision;
   d->width = dk->width;
+  d->rho = s->rho;
   if (s->nflt) {
     d->twf_kind = dk->flt_friction == SEM2D_FRICTION_TWF && dk->twf_kind == 0 ? 1 : dk->twf_kind;
     d->twf_mus = dk->twf_mus;

@@ -24,6 +24,8 @@ PROTOTYPES = [
     ("sem2d_gpu_batch_close", C.c_int, [vp]),
     ("sem2d_gpu_batch_size", C.c_int, [vp]),
     ("sem2d_gpu_batch_member", C.c_void_p, [vp, C.c_int]),
+    ("sem2d_gpu_checkpoint_every", C.c_int, [vp, C.c_int]),
+    ("sem2d_gpu_adjoint", C.c_int, [vp, dp, dp, dp, dp]),
     ("sem2d_gpu_step", C.c_int, [vp, C.c_int]),
     ("sem2d_gpu_step_timed", C.c_int, [vp, C.c_int, dp]),
     ("sem2d_gpu_stream", C.c_void_p, [vp]),

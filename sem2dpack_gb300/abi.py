@@ -88,6 +88,8 @@ class ProblemDesc(C.Structure):
         ("twf_mus", c_double), ("twf_mud", c_double), ("twf_mu0", c_double),
         ("twf_X", c_double), ("twf_Z", c_double), ("twf_V", c_double), ("twf_L", c_double),
         ("twf_T", c_double), ("twf_Dc", c_double),
+        ("rho", P_double),
+        ("adjoint", c_int),
     ]
 
 

@@ -76,6 +76,7 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.has_kv = c.has_kv;
   p.nplanes = c.nplanes;
   p.error = c.error;
+  p.chunk_shift = c.chunk_shift;
 }
 
 template <typename real, int N, int NDOF, int MAT, bool FAST>

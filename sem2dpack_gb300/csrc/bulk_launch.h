@@ -49,6 +49,7 @@ struct BulkConfig {
   double dt = 0, cv = 0, cpred = 0, cd2 = 0;
   double width = 0;  // 2.5D seismogenic width, 0 = 2D
   int *error = nullptr;  // device error flag
+  int chunk_shift = 0;   // chunk scheduled first (the fault's)
   cudaStream_t stream = nullptr;
 };
 
@@ -61,6 +62,46 @@ struct BatchLaunch {
   int *step = nullptr;
   unsigned *done = nullptr;
 };
+
+// one reverse step of the adjoint (adjoint_kernel.cuh), type-erased
+struct AdjConfig {
+  int ndof = 0, mixed = 0, grid_x = 0, grid_y = 0;
+  int LX = 0, LZ = 0, pitch = 0;
+  long long plane = 0;
+  int nx = 0, nz = 0;
+  const int *row0 = nullptr, *ztile = nullptr;
+  const double *H = nullptr, *w = nullptr;  // host
+  void *geo[4] = {nullptr, nullptr, nullptr, nullptr};
+  int nmat = 0;
+  void *mat[2] = {nullptr, nullptr};
+  void *rmass = nullptr, *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
+  void *Db = nullptr, *Vb = nullptr, *Dbn = nullptr, *Vbn = nullptr;
+  void *d = nullptr, *vprev = nullptr, *a = nullptr;
+  void *g_la = nullptr, *g_mu = nullptr, *g_M = nullptr, *g_C = nullptr;
+  int nrec = 0, nsamp = 0, isamp = 1;
+  char field = 'V';
+  const int *rec_I = nullptr, *rec_J = nullptr;
+  const double *resid = nullptr;
+  double dt = 0;
+  int kd2 = 0, it = 0;
+  int *error = nullptr;
+  cudaStream_t stream = nullptr;
+};
+int configure_adjoint(const AdjConfig &c);
+int launch_adjoint(const AdjConfig &c);
+// acc64[k] += (double)part[k]; part[k] = 0, for n values
+int launch_fold(void *part, double *acc64, long long n, int mixed, cudaStream_t s);
+// node gradients from the accumulated terms (see adjoint.cu)
+struct ChainConfig {
+  int ndof = 0, mixed = 0, LX = 0, LZ = 0, pitch = 0;
+  double dt = 0;
+  const void *rho = nullptr, *la = nullptr, *mu = nullptr, *rmass = nullptr;
+  const void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
+  const double *g_la = nullptr, *g_mu = nullptr, *g_M = nullptr, *g_C = nullptr;
+  double *grad_rho = nullptr, *grad_vp = nullptr, *grad_vs = nullptr;  // lattice planes
+  cudaStream_t stream = nullptr;
+};
+int launch_chain(const ChainConfig &c);
 
 // launches one time step of the step kernel; 0 or non-zero on error
 int launch_bulk(const BulkConfig &c);

@@ -1314,6 +1314,7 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
   }
   d->precision = P->deck.precision;
   d->width = P->deck.width;
+  d->rho = P->rho.data();
   if (P->nflt) {
     const sem2d_deck &dk = P->deck;
     d->twf_kind = dk.flt_friction == SEM2D_FRICTION_TWF && dk.twf_kind == 0 ? 1 : dk.twf_kind;

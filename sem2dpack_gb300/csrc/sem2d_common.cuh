@@ -128,6 +128,8 @@ struct BulkParams {
   int has_kv;             // Kelvin-Voigt viscosity present
   int nplanes;            // lattice planes staged per batch (strip_planes)
   int *error;             // sticky device error flag (SEM2D_E_*)
+  int chunk_shift;        // chunk of CTA row y is (y + chunk_shift) % rows: the
+                          // fault's chunk (long FP64 work) is scheduled first
 };
 
 // Perimeter slot of lattice node (I,J): bottom row, top row, left column,

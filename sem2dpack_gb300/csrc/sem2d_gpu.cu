@@ -56,7 +56,8 @@ struct sem2d_handle {
   std::vector<long long> glob2lat;   // global node -> J*pitch + I
   std::vector<int> elem_ex, elem_ez; // reference element -> structured position
   int TX = 8, TZ = 8, nplanes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
-  std::vector<int> ztile;            // tile-row boundaries (element rows)
+  std::vector<int> ztile;            // chunk boundaries (element rows)
+  int fault_chunk = 0;               // chunk holding the fault rows
   int *d_ztile = nullptr;
   bool keep_accel = false;
   // device memory
@@ -99,6 +100,12 @@ struct sem2d_handle {
   void *d_units = nullptr;
   int nunits = 0, batch_grid = 0;
   bool batch_open = false;          // members may still be added
+  // gradient workflow (sem2d_gpu_adjoint)
+  int adjoint = 0;
+  void *rho_plane = nullptr;        // density at the nodes
+  int ckpt_every = 0;               // forward states kept every ckpt_every steps
+  std::vector<void *> ckpt;         // [slot] D then V (ndof planes each)
+  int ckpt_saved = -1;              // last slot written
 };
 
 namespace {
@@ -283,9 +290,13 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
   h->mat_iso = iso;
   if (d->width > 0 && !iso)
     return set_err(h, SEM2D_E_UNSUPPORTED, "the 2.5D term needs an isotropic material");
+  if (d->adjoint) {
+    if (!d->rho) return set_err(h, SEM2D_E_ARG, "the gradient workflow needs the density (rho)");
+    if (!iso) return set_err(h, SEM2D_E_UNSUPPORTED, "the gradient workflow needs an isotropic material");
+  }
   // one value per element when every element is homogeneous (the
   // reference then shares one coefficient set per tag, mat_gen.f90:358-361)
-  bool elem_const = true;
+  bool elem_const = !d->adjoint;
   for (int e = 0; e < ne && elem_const; ++e)
     for (size_t m = 0; m < src.size() && elem_const; ++m) {
       const double *v = src[m] + (size_t)NN * e;
@@ -322,6 +333,22 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
       seen[L] = 1;
     }
   if (!elem_const) h->mat_elem = node ? kMatNode : kMatPoint;
+  if (d->adjoint) {
+    if (!node) return set_err(h, SEM2D_E_UNSUPPORTED, "the gradient workflow needs a material continuous at nodes");
+    std::vector<double> rp(h->plane, 0.0);
+    std::vector<char> seen2(h->plane, 0);
+    for (int e = 0; e < ne; ++e)
+      for (int q = 0; q < NN; ++q) {
+        const long long L = h->glob2lat[d->ibool[q + (size_t)NN * e] - 1];
+        const double v = d->rho[q + (size_t)NN * e];
+        if (seen2[L] && rp[L] != v) return set_err(h, SEM2D_E_UNSUPPORTED, "density not continuous at nodes");
+        rp[L] = v;
+        seen2[L] = 1;
+      }
+    h->adjoint = 1;
+    const int st2 = upload_real(h, &h->rho_plane, rp);
+    if (st2) return st2;
+  }
   int st;
   for (size_t m = 0; m < src.size() && !elem_const; ++m) {
     if (node) {
@@ -660,6 +687,7 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.cd2 = (0.5 - h->beta) * h->dt * h->dt;
   bc.kd2 = h->kd2;
   bc.width = h->width;
+  bc.chunk_shift = h->fault_chunk;
   bc.H = h->H.data();
   bc.w = h->w.data();
   bc.stream = h->stream;
@@ -807,6 +835,7 @@ int reset_state(sem2d_handle *h) {
   }
   h->cur = 0;
   h->steps = 0;
+  h->ckpt_saved = -1;
   int st = h->mixed ? launch_fault_init<float>(h) : launch_fault_init<double>(h);
   return st;
 }
@@ -971,6 +1000,10 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
       return set_err(h, SEM2D_E_UNSUPPORTED, std::string("no strip configuration fits: ") + bulk_last_error());
   }
   h->ztile = tile_rows(h->N, h->nz, h->row0.data(), h->TZ);
+  h->fault_chunk = 0;
+  if (h->nflt)
+    for (size_t y = 0; y + 1 < h->ztile.size(); ++y)
+      if (h->row0[h->ztile[y]] <= h->jf1 && h->jf1 < h->row0[h->ztile[y + 1]]) h->fault_chunk = int(y);
   for (size_t y = 0; y + 1 < h->ztile.size(); ++y)
     if (h->ztile[y + 1] - h->ztile[y] + 1 > 2 * kMaxChunkRows + 1)
       return set_err(h, SEM2D_E_UNSUPPORTED, "element-row chunk too tall");
@@ -1124,8 +1157,10 @@ int batch_close_impl(sem2d_handle *h) {
   for (int i = 0; i < nsim; ++i) {
     const sem2d_handle *m = h->subs[i];
     const int gx = (m->nx + m->TX - 1) / m->TX, gy = int(m->ztile.size()) - 1;
-    for (int y = 0; y < gy; ++y)
+    for (int yy = 0; yy < gy; ++yy) {
+      const int y = (yy + m->fault_chunk) % gy;  // the fault's chunk first
       for (int x = 0; x < gx; ++x) units.insert(units.end(), {i, x, y, gx});
+    }
   }
   h->nunits = int(units.size() / 4);
   if ((st = dupload(h, reinterpret_cast<int **>(&h->d_units), units))) return st;
@@ -1253,12 +1288,11 @@ int sem2d_gpu_create(const sem2d_problem_desc *desc, sem2d_handle **out) {
   return SEM2D_OK;
 }
 
-int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
-  if (!h) return SEM2D_E_ARG;
-  if (h->owner) return set_err(h, SEM2D_E_STATE, "a batch member is stepped through its batch");
-  if (h->batch_open) return set_err(h, SEM2D_E_STATE, "the batch is still open");
-  if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
-  if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
+}  // extern "C"
+
+namespace {
+
+int step_impl(sem2d_handle *h, int nsteps) {
   int st;
   int left = nsteps;
   const char *nog = std::getenv("SEM2D_NO_GRAPH");
@@ -1280,6 +1314,261 @@ int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
   if (left && (st = launch_steps(h, left))) return st;
   sync_members(h);
   return SEM2D_OK;
+}
+
+// copies the current state (next displacement predictor, velocity) into
+// checkpoint slot k
+int save_checkpoint(sem2d_handle *h, int k) {
+  const size_t n = (h->mixed ? sizeof(float) : sizeof(double)) * (size_t)h->plane * h->ndof;
+  char *slot = static_cast<char *>(h->ckpt[k]);
+  CK(cudaMemcpyAsync(slot, h->D[h->cur], n, cudaMemcpyDeviceToDevice, h->stream));
+  CK(cudaMemcpyAsync(slot + n, h->V[h->cur], n, cudaMemcpyDeviceToDevice, h->stream));
+  h->ckpt_saved = k;
+  return SEM2D_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
+  if (!h) return SEM2D_E_ARG;
+  if (h->owner) return set_err(h, SEM2D_E_STATE, "a batch member is stepped through its batch");
+  if (h->batch_open) return set_err(h, SEM2D_E_STATE, "the batch is still open");
+  if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
+  if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
+  if (h->ckpt_every <= 0) return step_impl(h, nsteps);
+  // keep the state of every ckpt_every-th step for the adjoint
+  int st, left = nsteps;
+  if (h->steps == 0 && (st = save_checkpoint(h, 0))) return st;
+  while (left > 0) {
+    const int to_next = h->ckpt_every - h->steps % h->ckpt_every;
+    const int n = std::min(left, to_next);
+    if ((st = step_impl(h, n))) return st;
+    left -= n;
+    if (h->steps % h->ckpt_every == 0 && (st = save_checkpoint(h, h->steps / h->ckpt_every))) return st;
+  }
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_checkpoint_every(sem2d_handle *h, int every) {
+  if (!h) return SEM2D_E_ARG;
+  if (!h->adjoint) return set_err(h, SEM2D_E_STATE, "the handle was not created for the gradient workflow");
+  if (h->steps != 0) return set_err(h, SEM2D_E_STATE, "checkpoints are set before the first step");
+  for (void *q : h->ckpt) {
+    cudaFree(q);
+    h->allocs.erase(std::remove(h->allocs.begin(), h->allocs.end(), q), h->allocs.end());
+  }
+  h->ckpt.clear();
+  h->ckpt_every = every > 0 ? every : 0;
+  h->ckpt_saved = -1;
+  if (!h->ckpt_every) return SEM2D_OK;
+  const size_t n = (h->mixed ? sizeof(float) : sizeof(double)) * (size_t)h->plane * h->ndof;
+  for (int k = 0; k <= h->nt / h->ckpt_every; ++k) {
+    char *q = nullptr;
+    const int st = dalloc(h, &q, 2 * n, false);
+    if (st) return st;
+    h->ckpt.push_back(q);
+  }
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, double *grad_vp,
+                      double *grad_vs) {
+  if (!h || !resid) return SEM2D_E_ARG;
+  if (!h->adjoint || !h->rho_plane) return set_err(h, SEM2D_E_STATE, "the handle was not created for the gradient workflow");
+  if (h->ckpt_every <= 0 || h->steps != h->nt || h->ckpt_saved != h->nt / h->ckpt_every)
+    return set_err(h, SEM2D_E_STATE, "run all nt steps with checkpoints first (sem2d_gpu_checkpoint_every)");
+  if (h->N != 5 || h->nflt || h->scheme != 0 || h->has_kv || h->width > 0 || !h->mat_iso ||
+      h->mat_elem != kMatNode)
+    return set_err(h, SEM2D_E_UNSUPPORTED,
+                   "the adjoint covers NGLL=5, isotropic node material, leapfrog, no fault, KV or 2.5D");
+  if (h->nrec && (h->rec_npts != 1 || (h->rec_field != 'V' && h->rec_field != 'D')))
+    return set_err(h, SEM2D_E_UNSUPPORTED, "the adjoint needs receivers at nodes recording V or D");
+  int st = check_device_error(h);
+  if (st) return st;
+  const size_t rs = h->mixed ? sizeof(float) : sizeof(double);
+  const size_t fbytes = rs * (size_t)h->plane * h->ndof;
+  const int k = h->ckpt_every, nd = h->ndof, nslot = perimeter_slots(h->LX, h->LZ);
+  std::vector<void *> tmp;
+  auto alloc = [&](size_t bytes) -> void * {
+    void *q = nullptr;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) return nullptr;
+    tmp.push_back(q);
+    cudaMemsetAsync(q, 0, bytes, h->stream);
+    return q;
+  };
+  auto release = [&]() {
+    cudaStreamSynchronize(h->stream);
+    for (void *q : tmp) cudaFree(q);
+    tmp.clear();
+  };
+  // ring of recomputed forward states: slot j holds (after step n0+j) the
+  // displacement predictor, velocity and acceleration
+  std::vector<void *> RD(k + 1), RV(k + 1), RA(k + 1);
+  for (int j = 1; j <= k; ++j) {
+    RD[j] = alloc(fbytes);
+    RV[j] = alloc(fbytes);
+    RA[j] = alloc(fbytes);
+    if (!RD[j] || !RV[j] || !RA[j]) {
+      release();
+      return set_err(h, SEM2D_E_NOMEM, "no device memory for the recomputed segment");
+    }
+  }
+  void *Dbar[2] = {alloc(fbytes), alloc(fbytes)}, *Vbar[2] = {alloc(fbytes), alloc(fbytes)};
+  void *g_la = alloc(rs * h->plane), *g_mu = alloc(rs * h->plane), *g_M = alloc(rs * h->plane);
+  void *g_C = alloc(rs * (size_t)nd * nslot);
+  double *a_la = (double *)alloc(8 * h->plane), *a_mu = (double *)alloc(8 * h->plane);
+  double *a_M = (double *)alloc(8 * h->plane), *a_C = (double *)alloc(8 * (size_t)nd * nslot);
+  double *grads = (double *)alloc(8 * 3 * (size_t)h->plane);
+  const size_t nres = (size_t)std::max(h->rec_nsamp, 1) * std::max(h->nrec, 1) * nd;
+  double *d_resid = (double *)alloc(8 * nres);
+  if (!Dbar[0] || !Dbar[1] || !Vbar[0] || !Vbar[1] || !g_la || !g_mu || !g_M || !g_C || !a_la || !a_mu ||
+      !a_M || !a_C || !grads || !d_resid) {
+    release();
+    return set_err(h, SEM2D_E_NOMEM, "no device memory for the adjoint");
+  }
+  if (h->nrec)
+    CK(cudaMemcpyAsync(d_resid, resid, 8 * (size_t)h->rec_nsamp * h->nrec * nd, cudaMemcpyHostToDevice, h->stream));
+  AdjConfig ac;
+  ac.ndof = nd;
+  ac.mixed = h->mixed;
+  ac.grid_x = (h->nx + h->TX - 1) / h->TX;
+  ac.grid_y = int(h->ztile.size()) - 1;
+  ac.LX = h->LX;
+  ac.LZ = h->LZ;
+  ac.pitch = h->pitch;
+  ac.plane = h->plane;
+  ac.nx = h->nx;
+  ac.nz = h->nz;
+  ac.row0 = h->d_row0;
+  ac.ztile = h->d_ztile;
+  ac.H = h->H.data();
+  ac.w = h->w.data();
+  for (int q = 0; q < 4; ++q) ac.geo[q] = h->geo[q];
+  ac.nmat = h->nmat;
+  ac.mat[0] = h->mat[0];
+  ac.mat[1] = h->nmat > 1 ? h->mat[1] : nullptr;
+  ac.rmass = h->rmass;
+  ac.per_rm = h->per_rm;
+  ac.per_Ca = h->per_Ca;
+  ac.per_Cb = h->per_Cb;
+  ac.g_la = g_la;
+  ac.g_mu = g_mu;
+  ac.g_M = g_M;
+  ac.g_C = g_C;
+  ac.nrec = h->nrec;
+  ac.nsamp = h->rec_nsamp;
+  ac.isamp = h->rec_isamp;
+  ac.field = h->rec_field;
+  ac.rec_I = h->rec_I;
+  ac.rec_J = h->rec_J;
+  ac.resid = d_resid;
+  ac.dt = h->dt;
+  ac.kd2 = h->kd2;
+  ac.error = h->d_error;
+  ac.stream = h->stream;
+  if (configure_adjoint(ac)) {
+    release();
+    return set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
+  }
+  int ca = 0;
+  const int nseg = (h->nt + k - 1) / k;
+  for (int seg = nseg - 1; seg >= 0 && !st; --seg) {
+    const int n0 = seg * k, n1 = std::min(n0 + k, h->nt);
+    const size_t half = fbytes;
+    RD[0] = h->ckpt[seg];
+    RV[0] = static_cast<char *>(h->ckpt[seg]) + half;
+    // recompute the forward steps n0+1 .. n1 of the segment
+    const int s0 = n0;
+    CK(cudaMemcpyAsync(h->d_step, &s0, sizeof(int), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    for (int n = n0 + 1; n <= n1 && !st; ++n) {
+      const int j = n - n0;
+      if (h->mixed) {
+        FaultParams<float> f;
+        BulkConfig bc = make_config<float>(h, h->cur, f);
+        bc.Dcur = RD[j - 1];
+        bc.Vcur = RV[j - 1];
+        bc.Dnext = RD[j];
+        bc.Vnext = RV[j];
+        bc.Anext = RA[j];
+        bc.rec_tile_start = nullptr;
+        st = launch_bulk(bc) ? set_err(h, SEM2D_E_CUDA, bulk_last_error()) : SEM2D_OK;
+      } else {
+        FaultParams<double> f;
+        BulkConfig bc = make_config<double>(h, h->cur, f);
+        bc.Dcur = RD[j - 1];
+        bc.Vcur = RV[j - 1];
+        bc.Dnext = RD[j];
+        bc.Vnext = RV[j];
+        bc.Anext = RA[j];
+        bc.rec_tile_start = nullptr;
+        st = launch_bulk(bc) ? set_err(h, SEM2D_E_CUDA, bulk_last_error()) : SEM2D_OK;
+      }
+      h->launches++;
+    }
+    // reverse steps n1 .. n0+1
+    for (int n = n1; n > n0 && !st; --n) {
+      const int j = n - n0;
+      ac.Db = Dbar[ca];
+      ac.Vb = Vbar[ca];
+      ac.Dbn = Dbar[1 - ca];
+      ac.Vbn = Vbar[1 - ca];
+      ac.d = RD[j - 1];
+      ac.vprev = RV[j - 1];
+      ac.a = RA[j];
+      ac.it = n;
+      if (launch_adjoint(ac)) st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
+      h->launches++;
+      ca = 1 - ca;
+    }
+    if (!st && (launch_fold(g_la, a_la, h->plane, h->mixed, h->stream) ||
+                launch_fold(g_mu, a_mu, h->plane, h->mixed, h->stream) ||
+                launch_fold(g_M, a_M, h->plane, h->mixed, h->stream) ||
+                launch_fold(g_C, a_C, (long long)nd * nslot, h->mixed, h->stream)))
+      st = set_err(h, SEM2D_E_CUDA, bulk_last_error());
+  }
+  if (!st) {
+    ChainConfig cc;
+    cc.ndof = nd;
+    cc.mixed = h->mixed;
+    cc.LX = h->LX;
+    cc.LZ = h->LZ;
+    cc.pitch = h->pitch;
+    cc.dt = h->dt;
+    cc.rho = h->rho_plane;
+    cc.la = nd == 2 ? h->mat[0] : nullptr;
+    cc.mu = nd == 2 ? h->mat[1] : h->mat[0];
+    cc.rmass = h->rmass;
+    cc.per_rm = h->per_rm;
+    cc.per_Ca = h->per_Ca;
+    cc.per_Cb = h->per_Cb;
+    cc.g_la = a_la;
+    cc.g_mu = a_mu;
+    cc.g_M = a_M;
+    cc.g_C = a_C;
+    cc.grad_rho = grads;
+    cc.grad_vp = grads + h->plane;
+    cc.grad_vs = grads + 2 * h->plane;
+    cc.stream = h->stream;
+    if (launch_chain(cc)) st = set_err(h, SEM2D_E_CUDA, bulk_last_error());
+  }
+  const int s_now = h->steps;
+  if (!st) {
+    std::vector<double> hg(3 * (size_t)h->plane);
+    if (cudaMemcpyAsync(hg.data(), grads, 8 * hg.size(), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
+        cudaMemcpyAsync(h->d_step, &s_now, sizeof(int), cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+      st = set_err(h, SEM2D_E_CUDA, "adjoint: copy back failed");
+    double *out[3] = {grad_rho, grad_vp, grad_vs};
+    for (int q = 0; q < 3 && !st; ++q)
+      if (out[q])
+        for (int pnode = 0; pnode < h->npoin; ++pnode) out[q][pnode] = hg[(size_t)q * h->plane + h->glob2lat[pnode]];
+  }
+  release();
+  if (st) return st;
+  return check_device_error(h);
 }
 
 int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms) {

@@ -32,9 +32,9 @@
 //
 // Data movement.  The lattice rows a batch touches (displacement, node
 // material, velocity predictor, inverse mass) are fetched with one
-// cp.async.bulk per (row, plane) into one of two stage buffers; the copies
-// of batch b+1 are in flight while batch b computes, and those of batch b+2
-// are issued by all threads as soon as batch b has released its stage.
+// cp.async.bulk per (row, plane) into one of three stage buffers; the copies
+// of batches b+1 and b+2 are in flight while batch b computes (b+2 is
+// issued by all threads as soon as batch b-1 has released its stage).
 // Every mbarrier wait is bounded: a CTA that times out raises
 // SEM2D_E_TIMEOUT, lets its own copies drain and returns.
 //
@@ -62,6 +62,7 @@ namespace sem2d {
 constexpr int kStripThreads = 256;
 constexpr int kErrTimeout = -8;  // SEM2D_E_TIMEOUT
 constexpr int kMaxChunk = 256;   // element rows of one chunk (host-enforced)
+constexpr int kMaxStages = 3;    // stage buffers of the batch pipeline (at most)
 
 template <typename real, int N>
 struct StripShape {
@@ -71,6 +72,9 @@ struct StripShape {
   static constexpr int R = kNSlot / SW1;                         // element rows per batch
   static constexpr int HR = (N - 1) * R + 2;                     // lattice rows per stage (max)
   static constexpr int AL = 16 / int(sizeof(real));              // copy alignment in words
+  // stage buffers: three (batches b+1 and b+2 in flight) unless the FP64
+  // stages of NGLL 6 / 9 would not fit, then two
+  static constexpr int kStages = (sizeof(real) == 8 && N != 5) ? 2 : kMaxStages;
   static_assert(SW1 * R == kNSlot, "a batch fills every element slot");
 };
 
@@ -96,7 +100,7 @@ __host__ __device__ inline size_t strip_smem_bytes(int nplanes) {
   using S = StripShape<real, N>;
   constexpr int tw = strip_row_stride<real, N>();
   const int nscr = NDOF == 2 ? 4 : 1;
-  size_t n = 2 * size_t(nplanes) * S::HR * tw;   // two stages
+  size_t n = size_t(S::kStages) * nplanes * S::HR * tw;  // stage buffers
   n += size_t(S::kNSlot) * nscr * N * N;        // element scratch / nodal forces
   n += 2 * size_t(NDOF) * tw;                   // carry rows (double-buffered)
   n += 2 * size_t(NDOF) * tw;                   // fault-row forces, both sides
@@ -130,7 +134,8 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
   const int NP = p.nplanes;
   const size_t stage_sz = size_t(NP) * PS;
   real *stg = reinterpret_cast<real *>(smem_raw);
-  real *scr = stg + 2 * stage_sz;
+  constexpr int NST = S::kStages;
+  real *scr = stg + NST * stage_sz;
   real *carry = scr + size_t(S::kNSlot) * NSCR * NN;
   real *fbuf = carry + 2 * NDOF * TWp;
 
@@ -188,10 +193,10 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
     if (pl == pR) return p.rmass;
     return p.Acur + (pl - pA) * p.plane;
   };
-  // fetch the lattice rows of batch bb into stage bb & 1; every thread
+  // fetch the lattice rows of batch bb into stage bb % NST; every thread
   // issues at most one of the copies, thread 0 announces the byte count
   auto issue = [&](int bb) {
-    const int st = bb & 1;
+    const int st = bb % NST;
     const int eb0 = eza + bb * R, eb1 = min(eb0 + R, ez1);
     const int Jlo = rw(eb0), nr = rw(eb1 - 1) + N - Jlo;
     const uint32_t rowbytes = uint32_t(cw) * sizeof(real);
@@ -224,7 +229,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
   const real wt = w[t < N ? t : 0];
 
   for (int b = 0; b < nb; ++b) {
-    const int st = b & 1;
+    const int st = b % NST;
     const int eb0 = eza + b * R, eb1 = min(eb0 + R, ez1), nre = eb1 - eb0;
     const int Jlo = rw(eb0), nr = rw(eb1 - 1) + N - Jlo;
     const bool from_carry = b > 0 && rw(eb0) == rw(eb0 - 1) + (N - 1);
@@ -263,11 +268,14 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
       if (tid == 0) {
         if (p.error) atomicExch(p.error, kErrTimeout);
         mbar_wait(&bar[st], ph[st] ^ 1u);  // let this CTA's copies drain
-        if (b + 1 < nb) mbar_wait(&bar[st ^ 1], ph[st ^ 1]);
+        const int s1 = (b + 1) % NST;
+        if (b + 1 < nb) mbar_wait(&bar[s1], ph[s1]);
       }
       __syncthreads();
       return false;
     }
+    // three stages: batch b-1 has released its stage, fetch batch b+2 into it
+    if (NST == 3 && b + 2 < nb) issue(b + 2);
 
     const real *sg = stg + st * stage_sz;
     const real *sD = sg;
@@ -546,14 +554,17 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
     __syncthreads();
 
     // ---- assembly, sources, dashpots, inverse mass, time update ----
-    real *cin = carry + (st ^ 1) * NDOF * TWp, *cout = carry + st * NDOF * TWp;
-    for (int jj = warp; jj < nr; jj += NW) {
+    real *cin = carry + ((b & 1) ^ 1) * NDOF * TWp, *cout = carry + (b & 1) * NDOF * TWp;
+    // (row, column) pairs over all threads; OWS >= the owned width of a strip
+    constexpr int OWS = SW * (N - 1) + 1;
+    for (int q = tid; q < nr * OWS; q += kStripThreads) {
+      const int jj = q / OWS, io = q - jj * OWS;
       const int fate = s_stat[jj];
-      if (fate == 0) continue;
+      if (fate == 0 || io >= OWc) continue;
       const int ra = s_r[0][jj], ja = s_j[0][jj], rb = s_r[1][jj], jb = s_j[1][jj];
       const int J = Jlo + jj;
       const bool cin_row = jj == 0 && from_carry;
-      for (int io = lane; io < OWc; io += 32) {
+      {
         const int ii = ii0 + io;
         real f[NDOF];
 #pragma unroll
@@ -662,8 +673,8 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
         p.sis[s + (size_t)p.rec_nsamp * (r + (size_t)p.rec_nrec * c)] = val;
       }
     }
-    __syncthreads();  // the stage and the scratch areas are free again
-    if (b + 2 < nb) issue(b + 2);
+    __syncthreads();  // the stage, the scratch areas and the row tables are free again
+    if (NST == 2 && b + 2 < nb) issue(b + 2);
   }
 
   return true;
@@ -684,8 +695,7 @@ __device__ __forceinline__ void strip_step_done(int *step, unsigned *done, int i
 
 __device__ __forceinline__ void strip_init_bars(uint64_t *bar) {
   if (threadIdx.x == 0) {
-    mbar_init(&bar[0], 1);
-    mbar_init(&bar[1], 1);
+    for (int k = 0; k < kMaxStages; ++k) mbar_init(&bar[k], 1);
     mbar_fence_init();
   }
   __syncthreads();
@@ -696,12 +706,12 @@ template <typename real, int N, int NDOF, int MAT, bool FAST>
 __global__ void __launch_bounds__(kStripThreads, StripOcc<real, NDOF>::kMinBlocks)
     strip_step_kernel(const __grid_constant__ BulkParams<real, N> p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ __align__(8) uint64_t bar[kMaxStages];
   strip_init_bars(bar);
-  uint32_t ph[2] = {0u, 0u};
+  uint32_t ph[kMaxStages] = {0u, 0u, 0u};
   const int it = *p.step + 1;  // the step this launch computes
-  if (!strip_unit<real, N, NDOF, MAT, FAST>(p, p.H, p.w, blockIdx.x, blockIdx.y, gridDim.x, it, bar, ph,
-                                             smem_raw))
+  const int chunk = (blockIdx.y + p.chunk_shift) % gridDim.y;
+  if (!strip_unit<real, N, NDOF, MAT, FAST>(p, p.H, p.w, blockIdx.x, chunk, gridDim.x, it, bar, ph, smem_raw))
     return;
   strip_step_done(p.step, p.done, it);
 }
@@ -724,10 +734,10 @@ template <typename real, int N, int NDOF, int MAT, bool FAST>
 __global__ void __launch_bounds__(kStripThreads, StripOcc<real, NDOF>::kMinBlocks)
     strip_batch_kernel(const __grid_constant__ BatchParams<real, N> bp) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  __shared__ __align__(8) uint64_t bar[2];
+  __shared__ __align__(8) uint64_t bar[kMaxStages];
   __shared__ __align__(16) BulkParams<real, N> sp;
   strip_init_bars(bar);
-  uint32_t ph[2] = {0u, 0u};
+  uint32_t ph[kMaxStages] = {0u, 0u, 0u};
   const int it = *bp.step + 1;
   int cur = -1;
   for (int u = blockIdx.x; u < bp.nunits; u += gridDim.x) {

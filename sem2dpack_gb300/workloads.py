@@ -15,6 +15,12 @@ index); no external data set is involved.
                    (correlation 500 m, max 2 MPa), 3 km nucleation patch at
                    81 MPa, absorbing on all sides, 6000 steps.
   psv_rsf          P-SV rate-and-state rupture in a random medium (aging law).
+  gradient_shots   P-SV gradient workflow: 512 x 512 elements of 25 m,
+                   NGLL=5, homogeneous start model 2700/6000/3464, true
+                   model with a seeded Gaussian anomaly (+-10 % on vp, vs,
+                   rho), 8 Ricker shots (f0 = 8 Hz) near the surface, 128
+                   receivers on the free surface, absorbing elsewhere, 4000
+                   steps, L2 waveform misfit.
   batch_shots      independent P-SV shots of uneven size (64^2..512^2
                    elements of 25 m, NGLL=5), each with its own 3-8 layer
                    model (vs 1500-4000 m/s, vp = 1.73 vs, rho = 1700 +
@@ -223,6 +229,36 @@ def batch_shots(nsim=256, scale=1.0, nsteps=3000, precision=abi.PRECISION_MIXED,
             precision=precision,
         ))
     return decks
+
+
+def gradient_shots(scale=1.0, nsteps=4000, precision=abi.PRECISION_MIXED, nshots=8, seed_index=4):
+    """(NodeModel of shot k, start model, true model) for the gradient
+    workflow; the node models are (LZ, LX) arrays of rho, vp, vs."""
+    from .gradient import NodeModel
+    rng = _rng(seed_index)
+    n = max(8, int(round(512 * scale)))
+    h = 25.0
+    L = n * h
+    xs = np.linspace(0.1 * L, 0.9 * L, nshots)
+    models = []
+    for k in range(nshots):
+        deck = ParDeck(
+            ngll=5, ndof=2, fmax=20.0, xlim=(0.0, L), zlim=(0.0, L), nelem=(n, n),
+            materials=[Material(tag=1, rho=2700.0, cp=6000.0, cs=3464.0)], absorbing=[1, 2, 4],
+            time=Time(kind="leapfrog", dt=0.3e-3, nsteps=nsteps),
+            sources=Sources(coords=[(float(xs[k]), L - 4 * h)], f0=8.0, onset=0.15, ampli=1.0e10, angle=0.0),
+            receivers=Receivers(number=128, first=(0.02 * L, L), last=(0.98 * L, L), field="V"),
+            precision=precision,
+        )
+        models.append(NodeModel(deck))
+    m0 = models[0]
+    X, Z = np.meshgrid(np.linspace(0, L, m0.LX), np.linspace(0, L, m0.LZ))
+    xc, zc = rng.uniform(0.35 * L, 0.65 * L), rng.uniform(0.35 * L, 0.6 * L)
+    g = np.exp(-((X - xc) ** 2 + (Z - zc) ** 2) / (2 * (0.08 * L) ** 2))
+    start = [np.full(X.shape, v) for v in (2700.0, 6000.0, 3464.0)]
+    signs = rng.choice([-1.0, 1.0], size=3)
+    true = [b * (1.0 + 0.1 * sg * g) for b, sg in zip(start, signs)]
+    return models, start, true
 
 
 def build(deck_or_pair):
