@@ -351,8 +351,8 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
 
     def forward_only():
         for s, _ in sims:
-            s._check(lib().sem2d_gpu_checkpoint_every(s.h, 0))
             s.reset()
+            s._check(lib().sem2d_gpu_checkpoint_every(s.h, 0))
         barrier()
         t0 = time.perf_counter()
         for s, _ in sims:

@@ -517,14 +517,40 @@ __global__ void __launch_bounds__(kStripThreads, sizeof(real) == 4 ? 2 : 1) adjo
       return k == 0 ? 0 : 3;             // F, d/dmu
     };
     real *cin = carry + (st ^ 1) * NC * TWp, *cout = carry + st * NC * TWp;
-    for (int q = tid; q < nr * OWc; q += kStripThreads) {
+    // A thread's nodes: the global reads of all of them (forward
+    // acceleration, gradient partial sums) are issued first, so that their
+    // latencies overlap, then the nodes are assembled and updated in turn.
+    constexpr int OWS = SW * (N - 1) + 1;  // >= OWc
+    constexpr int NQI = (HR * OWS + kStripThreads - 1) / kStripThreads;
+    constexpr int NG = NDOF + 1 + (NDOF == 2 ? 2 : 1);  // a (NDOF), g_M, g_la, g_mu
+    real pre[NQI][NG];
+#pragma unroll
+    for (int k = 0; k < NQI; ++k) {
+      const int q = tid + k * kStripThreads;
+      const int jj = q / OWc, io = q - jj * OWc;
+      const bool upd = q < nr * OWc && s_stat[jj < HR ? jj : 0] == 1;
+      const long long g = (long long)(Jlo + jj) * p.pitch + I0 + io;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) pre[k][c] = upd ? p.a[c * p.plane + g] : real(0);
+      pre[k][NDOF] = upd ? p.g_M[g] : real(0);
+      if (NDOF == 2) {
+        pre[k][NDOF + 1] = upd ? p.g_la[g] : real(0);
+        pre[k][NDOF + 2] = upd ? p.g_mu[g] : real(0);
+      } else {
+        pre[k][NDOF + 1] = upd ? p.g_mu[g] : real(0);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < NQI; ++k) {
+      const int q = tid + k * kStripThreads;
+      if (q >= nr * OWc) break;
       const int jj = q / OWc, io = q - jj * OWc;
       const int fate = s_stat[jj];
       if (fate == 0) continue;
       const int ii = ii0 + io;
       real f[NQ];
 #pragma unroll
-      for (int k = 0; k < NQ; ++k) f[k] = (jj == 0 && from_carry) ? cin[k * TWp + io] : real(0);
+      for (int k2 = 0; k2 < NQ; ++k2) f[k2] = (jj == 0 && from_carry) ? cin[k2 * TWp + io] : real(0);
       const int ce = ii / (N - 1), il0 = ii - ce * (N - 1);
 #pragma unroll
       for (int kk = 0; kk < 2; ++kk) {
@@ -533,17 +559,17 @@ __global__ void __launch_bounds__(kStripThreads, sizeof(real) == 4 ? 2 : 1) adjo
         if (il0 == 0 && ce > 0) {
           const real *sl = scr + size_t(rr * SW1 + ce - 1) * NSC * NN + (N - 1) + N * jl;
 #pragma unroll
-          for (int k = 0; k < NQ; ++k) f[k] = f[k] + sl[qplane(k) * NN];
+          for (int k2 = 0; k2 < NQ; ++k2) f[k2] = f[k2] + sl[qplane(k2) * NN];
         }
         if (ce < ncol) {
           const real *sl = scr + size_t(rr * SW1 + ce) * NSC * NN + il0 + N * jl;
 #pragma unroll
-          for (int k = 0; k < NQ; ++k) f[k] = f[k] + sl[qplane(k) * NN];
+          for (int k2 = 0; k2 < NQ; ++k2) f[k2] = f[k2] + sl[qplane(k2) * NN];
         }
       }
       if (fate == 2) {
 #pragma unroll
-        for (int k = 0; k < NQ; ++k) cout[k * TWp + io] = f[k];
+        for (int k2 = 0; k2 < NQ; ++k2) cout[k2 * TWp + io] = f[k2];
         continue;
       }
       const int I = I0 + io, J = Jlo + jj;
@@ -555,7 +581,7 @@ __global__ void __launch_bounds__(kStripThreads, sizeof(real) == 4 ? 2 : 1) adjo
 #pragma unroll
       for (int c = 0; c < NDOF; ++c) {
         const real lam = sL[c * PS + si];
-        const real an = p.a[c * p.plane + g];
+        const real an = pre[k][c];
         const real gd = p.field == 'D' ? sG[c * PS + si] : real(0);
         p.Vbn[c * p.plane + g] = sVb[c * PS + si];
         p.Dbn[c * p.plane + g] = (gd + sDb[c * PS + si]) + f[c];
@@ -565,12 +591,12 @@ __global__ void __launch_bounds__(kStripThreads, sizeof(real) == 4 ? 2 : 1) adjo
           p.g_C[c * nslot + sp] += -lam * (vp + (real(0.5) * dt) * an);
         }
       }
-      p.g_M[g] += gm;
+      p.g_M[g] = pre[k][NDOF] + gm;
       if (NDOF == 2) {
-        p.g_la[g] += f[2];
-        p.g_mu[g] += f[3];
+        p.g_la[g] = pre[k][NDOF + 1] + f[2];
+        p.g_mu[g] = pre[k][NDOF + 2] + f[3];
       } else {
-        p.g_mu[g] += f[1];
+        p.g_mu[g] = pre[k][NDOF + 1] + f[1];
       }
     }
     __syncthreads();

@@ -201,6 +201,10 @@ template <int N>
 int strip_width_for_n() {
   return StripShape<float, N>::SW1 - 1;
 }
+template <int N>
+int strip_batch_rows_for_n() {
+  return StripShape<float, N>::R;
+}
 
 // the parameter block of one problem, written to `out` (params_bytes)
 template <int N>

@@ -76,6 +76,15 @@ int fill_params_block(const BulkConfig &c, void *out) {
   }
 }
 
+int strip_batch_rows(int N) {
+  switch (N) {
+    case 5: return strip_batch_rows_n5();
+    case 6: return strip_batch_rows_n6();
+    case 9: return strip_batch_rows_n9();
+    default: return 1;
+  }
+}
+
 int strip_width(int N) {
   switch (N) {
     case 5: return strip_width_n5();
@@ -125,8 +134,7 @@ int choose_tiles(const BulkConfig &c, const int *row0, int *TZ) {
     g_bulk_err = std::string("no resident CTA: ") + g_bulk_err;
     return 1;
   }
-  // batch rows of the step kernel: the slots per batch over the strip width
-  const int slots = 8 * (32 / N), R = slots / (SW + 1);
+  const int R = strip_batch_rows(N);
   const long long nstrips = (nx + SW - 1) / SW;
   auto eval = [&](int tz) {
     const std::vector<int> zt = tile_rows(N, nz, row0, tz);

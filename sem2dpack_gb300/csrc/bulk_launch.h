@@ -116,8 +116,9 @@ int fill_params_block(const BulkConfig &c, void *out);
 int configure_bulk(const BulkConfig &c);
 const char *bulk_last_error();
 
-// element columns per strip for NGLL N (0 if N is not compiled)
+// element columns per strip and element rows per batch for NGLL N
 int strip_width(int N);
+int strip_batch_rows(int N);
 // lattice planes staged per batch
 int strip_plane_count(int ndof, int nmat, int mat_elem, int scheme);
 
@@ -150,6 +151,9 @@ size_t bulk_smem_n9(int ndof, int mixed, int nplanes);
 int strip_width_n5();
 int strip_width_n6();
 int strip_width_n9();
+int strip_batch_rows_n5();
+int strip_batch_rows_n6();
+int strip_batch_rows_n9();
 int launch_batch_n5(const BulkConfig &c, const BatchLaunch &b);
 int launch_batch_n6(const BulkConfig &c, const BatchLaunch &b);
 int launch_batch_n9(const BulkConfig &c, const BatchLaunch &b);

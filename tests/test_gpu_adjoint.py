@@ -98,3 +98,32 @@ def test_adjoint_preconditions():
     pp = lambda a: a.ctypes.data_as(__import__("ctypes").POINTER(__import__("ctypes").c_double))
     with pytest.raises(Sem2dError):
         h._check(lib().sem2d_gpu_adjoint(h.h, pp(res), None, None, None))
+
+
+def test_adjoint_twenty_directions():
+    """Central finite differences of the FP64 forward along 20 seeded smooth
+    directions."""
+    m, start, obs = case(2, nsteps=100, nx=8)
+    J, sis, gr, gp, gs = forward_and_gradient(m, *start, obs=obs, checkpoint_every=10)
+    worst = 0.0
+    for seed in range(20):
+        dr, dp, ds = ac.smooth_direction(m, seed)
+        eps = 1e-3
+        Jp = forward_and_gradient(m, start[0] + eps * dr, start[1] + eps * dp, start[2] + eps * ds,
+                                  obs=obs, checkpoint_every=10)[0]
+        Jm = forward_and_gradient(m, start[0] - eps * dr, start[1] - eps * dp, start[2] - eps * ds,
+                                  obs=obs, checkpoint_every=10)[0]
+        fd = (Jp - Jm) / (2 * eps)
+        an = np.sum(gr * dr) + np.sum(gp * dp) + np.sum(gs * ds)
+        worst = max(worst, abs(an - fd) / abs(fd))
+    assert worst <= 1e-6, worst
+
+
+def test_adjoint_32x32_matches_autograd():
+    """The FP64 autograd-through-time reference on a 32 x 32 element copy."""
+    m, start, obs = case(2, nsteps=120, nx=32)
+    J, sis, gr, gp, gs = forward_and_gradient(m, *start, obs=obs, checkpoint_every=24)
+    Jt, sist, tr, tp, ts = ac.torch_misfit_grad(m, *start, obs)
+    assert J == pytest.approx(Jt, rel=1e-10)
+    for g, t in ((gr, tr), (gp, tp), (gs, ts)):
+        assert rel(g, t) <= 1e-8
