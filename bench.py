@@ -153,15 +153,16 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0}, "fallback"
 
 
-def ncu_traffic(workload):
-    """DRAM bytes per bulk-kernel launch from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "bulk_kernel_%s.txt" % workload)
+def ncu_traffic(kernel, workload, npoin):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary of a
+    (possibly smaller) capture of the workload, scaled by the node count."""
+    path = os.path.join(ROOT, "profiles", "%s_%s.txt" % (kernel, workload))
     if not os.path.exists(path):
         return None
     for line in open(path):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith("dram_bytes_per_node:"):
             try:
-                return float(line.split(":", 1)[1].split()[0])
+                return float(line.split(":", 1)[1].split()[0]) * npoin
             except ValueError:
                 return None
     return None
@@ -279,7 +280,7 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     bpn = BYTES_PER_NODE_STEP[(2, dtype)]
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
-    traffic = ncu_traffic("batch_shots")
+    traffic = ncu_traffic("strip_batch_kernel", "batch_shots", npoin)
     # end to end: uploads of every problem (the host arrays of the
     # descriptors), the time steps, all seismograms back, destroy
     barrier()
@@ -480,7 +481,7 @@ def main():
     bpn = BYTES_PER_NODE_STEP[(ndof, dtype)]
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
-    traffic = ncu_traffic(args.workload)
+    traffic = ncu_traffic("strip_step_kernel", args.workload, npoin)
 
     # end to end through the C-ABI from host buffers
     sim.close()
