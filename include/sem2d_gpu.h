@@ -274,9 +274,14 @@ int sem2d_gpu_reset(sem2d_handle *h);
  * every kernel node). */
 long long sem2d_gpu_kernel_launches(sem2d_handle *h);
 
-/* Work unit of one CTA of the step kernel: a strip of TX element columns
- * and a chunk of (about) TZ element rows; SEM2D_CHUNK=TZ in the
- * environment overrides the chunk height chosen at create time. */
+/* Work unit of the step kernel: a strip of TX element columns and a chunk
+ * of (about) TZ element rows.  FP32 problems with NGLL = 5, isotropic
+ * material per node or per element, leapfrog and no Kelvin-Voigt or 2.5D
+ * term run the one-element-per-thread kernel: a warp per unit, TX = 31
+ * (SEM2D_MARCH_CZ=TZ overrides its chunk height, SEM2D_MARCH=0 selects the
+ * strip kernel).  Every other problem runs the strip kernel: a CTA per
+ * unit (SEM2D_CHUNK=TZ overrides its chunk height).  The environment is
+ * read at create time. */
 int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz);
 
 /* Releases device memory; h becomes invalid. */

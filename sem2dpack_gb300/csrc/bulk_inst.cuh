@@ -47,6 +47,7 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.jf2 = c.jf2;
   p.has_fault = c.has_fault;
   if (c.has_fault) p.flt = *static_cast<const FaultParams<real> *>(c.flt);
+  p.fault_force = static_cast<real *>(c.fault_force);
   p.nsrc = c.nsrc;
   p.src_I = c.src_I;
   p.src_J = c.src_J;

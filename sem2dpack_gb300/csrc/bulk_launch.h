@@ -34,6 +34,7 @@ struct BulkConfig {
   int jf1 = -1, jf2 = -1;
   int has_fault = 0;
   const void *flt = nullptr;  // host FaultParams<real> of the problem's precision
+  void *fault_force = nullptr;  // march kernel: forces of the fault rows
   int nsrc = 0;
   const int *src_I = nullptr, *src_J = nullptr;
   const double *src_amp = nullptr;
@@ -157,6 +158,26 @@ int strip_batch_rows_n9();
 int launch_batch_n5(const BulkConfig &c, const BatchLaunch &b);
 int launch_batch_n6(const BulkConfig &c, const BatchLaunch &b);
 int launch_batch_n9(const BulkConfig &c, const BatchLaunch &b);
+// The FP32 NGLL=5 fast path with one element per thread (march_kernel.cuh).
+// Units are MarchUnit records {problem, strip, z0, z1, rec0, rec1}.
+constexpr int kMarchColsHost = 31;   // element columns owned by one unit
+constexpr int kMarchUnitInts = 6;    // ints per unit record
+struct MarchLaunch {
+  const void *units = nullptr;  // [nunits] unit records
+  int nunits = 0;
+  const void *sims = nullptr;   // [nsim] BulkParams<float, 5> (batch launches)
+  int *step = nullptr;          // batch launches
+  unsigned *done = nullptr;
+};
+// true when the march kernel covers the configuration
+bool march_supported(const BulkConfig &c);
+int launch_march(const BulkConfig &c, const MarchLaunch &m);
+int launch_march_batch(const BulkConfig &c, const MarchLaunch &m);
+// the fault node pairs of a march step (one thread per pair, after the step)
+int launch_march_fault(const BulkConfig &c);
+// resident warps per SM of the march kernel for the configuration
+int march_warps_per_sm(const BulkConfig &c);
+
 size_t params_bytes_n5(int mixed);
 size_t params_bytes_n6(int mixed);
 size_t params_bytes_n9(int mixed);

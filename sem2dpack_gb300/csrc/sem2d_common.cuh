@@ -103,6 +103,7 @@ struct BulkParams {
   int jf1, jf2;
   int has_fault;
   FaultParams<real> flt;
+  real *fault_force;      // march kernel: forces of the fault rows [(side*ndof + c)*nflt + I]
   // point sources
   int nsrc;
   const int *src_I, *src_J;

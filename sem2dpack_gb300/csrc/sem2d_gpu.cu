@@ -98,6 +98,14 @@ struct sem2d_handle {
   bool owns_stream = true;
   void *d_params[2] = {nullptr, nullptr};
   void *d_units = nullptr;
+  // the one-element-per-thread kernel (FP32, NGLL = 5 fast path): work
+  // units (strip, chunk) and the receivers each unit samples
+  bool march = false;
+  int march_cz = 0, march_nunits = 0;
+  void *d_march_units = nullptr;
+  int *d_march_rec = nullptr;
+  std::vector<int> march_units_host;
+  float *d_fault_force = nullptr;   // forces of the fault rows, finished by the fault kernel
   int nunits = 0, batch_grid = 0;
   bool batch_open = false;          // members may still be added
   // gradient workflow (sem2d_gpu_adjoint)
@@ -688,10 +696,25 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.kd2 = h->kd2;
   bc.width = h->width;
   bc.chunk_shift = h->fault_chunk;
+  bc.fault_force = h->d_fault_force;
   bc.H = h->H.data();
   bc.w = h->w.data();
   bc.stream = h->stream;
   return bc;
+}
+
+// one step of problem h: the march kernel when it covers the problem, else
+// the strip kernel; `receivers` false skips the in-kernel seismograms
+int launch_step_kernel(sem2d_handle *h, BulkConfig &bc, bool receivers) {
+  if (h->march) {
+    bc.rec_ids = receivers ? h->d_march_rec : nullptr;
+    MarchLaunch m;
+    m.units = h->d_march_units;
+    m.nunits = h->march_nunits;
+    return launch_march(bc, m);
+  }
+  if (!receivers) bc.rec_tile_start = nullptr;
+  return launch_bulk(bc);
 }
 
 template <typename real>
@@ -699,9 +722,13 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   FaultParams<real> f;
   BulkConfig bc = make_config<real>(h, cur, f);
   if (ev) CK(cudaEventRecord(ev[0], h->stream));
-  int st = launch_bulk(bc);
+  int st = launch_step_kernel(h, bc, h->nrec && !h->rec_separate);
   if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
   h->launches++;
+  if (h->march && h->nflt) {
+    if (launch_march_fault(bc)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
+    h->launches++;
+  }
   if (ev) CK(cudaEventRecord(ev[1], h->stream));
   if (ev) CK(cudaEventRecord(ev[2], h->stream));
   if (h->nrec && h->rec_separate) {
@@ -740,7 +767,18 @@ int launch_batch_step(sem2d_handle *h, cudaEvent_t *ev = nullptr) {
   b.step = h->d_step;
   b.done = h->d_done;
   if (ev) CK(cudaEventRecord(ev[0], h->stream));
-  if (launch_batch(bc, b)) return set_err(h, SEM2D_E_CUDA, std::string("batch launch: ") + bulk_last_error());
+  if (h->march) {
+    MarchLaunch ml;
+    ml.units = h->d_march_units;
+    ml.nunits = h->march_nunits;
+    ml.sims = h->d_params[h->cur];
+    ml.step = h->d_step;
+    ml.done = h->d_done;
+    if (launch_march_batch(bc, ml))
+      return set_err(h, SEM2D_E_CUDA, std::string("batch launch: ") + bulk_last_error());
+  } else if (launch_batch(bc, b)) {
+    return set_err(h, SEM2D_E_CUDA, std::string("batch launch: ") + bulk_last_error());
+  }
   h->launches++;
   if (ev)
     for (int q = 1; q < 4; ++q) CK(cudaEventRecord(ev[q], h->stream));
@@ -777,7 +815,7 @@ int launch_steps(sem2d_handle *h, int n) {
 
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
-  return 1 + (h->nrec && h->rec_separate ? 1 : 0);
+  return 1 + (h->march && h->nflt ? 1 : 0) + (h->nrec && h->rec_separate ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -856,6 +894,110 @@ int check_device_error(sem2d_handle *h) {
 
 // force_tz > 0 sets the chunk height (batch members share one);
 // `shared` is a stream owned by a batch
+// element row owning lattice row J (lower-left ownership): the highest
+// element row starting at or below J
+int owner_row(const sem2d_handle *h, int J) {
+  const int ez = int(std::upper_bound(h->row0.begin(), h->row0.begin() + h->nz, J) - h->row0.begin()) - 1;
+  return std::max(0, std::min(ez, h->nz - 1));
+}
+
+// Work units of the march kernel: strips of 31 element columns by chunks of
+// element rows.  The chunk height gives about two units per resident warp
+// (SEM2D_MARCH_CZ overrides it); a two-sided fault's rows stay in one chunk,
+// whose units come first (their FP64 fault work is the longest).
+// SEM2D_MARCH=0 keeps the strip kernel.
+int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vector<int> &rec_ez,
+                const std::vector<int> &rec_jn, int force_cz) {
+  h->march = false;
+  const char *env = std::getenv("SEM2D_MARCH");
+  if (env && std::atoi(env) == 0) return SEM2D_OK;
+  BulkConfig bc;
+  bc.N = h->N;
+  bc.ndof = h->ndof;
+  bc.mixed = h->mixed;
+  bc.fast = fast_path(h);
+  bc.mat_iso = h->mat_iso;
+  bc.mat_elem = h->mat_elem;
+  bc.pitch = h->pitch;
+  bc.plane = h->plane;
+  if (!march_supported(bc)) return SEM2D_OK;
+  int st;
+  if (h->nflt) {
+    // the fault kernel finishes the fault rows after the step: velocity or
+    // acceleration receivers there are sampled after it, by the receiver
+    // kernel
+    for (size_t r = 0; r < rec_jn.size(); ++r)
+      if (h->rec_field != 'D' && (rec_jn[r] == h->jf1 || rec_jn[r] == h->jf2)) h->rec_separate = true;
+    if ((st = dalloc(h, &h->d_fault_force, (size_t)2 * h->ndof * h->nflt))) return st;
+  }
+  const int nstrips = (h->nx + kMarchColsHost - 1) / kMarchColsHost;
+  int cz = 0;
+  if (const char *e = std::getenv("SEM2D_MARCH_CZ")) cz = std::atoi(e);
+  if (cz <= 0) cz = force_cz;
+  if (cz <= 0) {
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const long long target = 2LL * nsm * std::max(march_warps_per_sm(bc), 1);
+    cz = int(((long long)nstrips * h->nz + target - 1) / target);
+  }
+  cz = std::max(1, std::min(cz, h->nz));
+  std::vector<int> zb;
+  for (int z = 0; z < h->nz; z += cz)
+    if (!(h->nflt && h->two && z > 0 && h->row0[z] == h->jf2)) zb.push_back(z);
+  zb.push_back(h->nz);
+  const int nch = int(zb.size()) - 1;
+  int fch = -1;
+  if (h->nflt)
+    for (int y = 0; y < nch; ++y)
+      if (h->row0[zb[y]] <= h->jf1 && h->jf1 < (zb[y + 1] < h->nz ? h->row0[zb[y + 1]] : h->LZ)) fch = y;
+  std::vector<int> order, pos(nch);
+  if (fch >= 0) order.push_back(fch);
+  for (int y = 0; y < nch; ++y)
+    if (y != fch) order.push_back(y);
+  for (int k = 0; k < nch; ++k) pos[order[k]] = k;
+  std::vector<int> chunk_of(h->nz);
+  for (int y = 0; y < nch; ++y)
+    for (int z = zb[y]; z < zb[y + 1]; ++z) chunk_of[z] = y;
+  const int nu = nch * nstrips;
+  // receivers sampled inside the kernel, grouped by unit
+  std::vector<int> cnt(nu + 1, 0), ids;
+  std::vector<int> unit_of;
+  if (h->nrec && !h->rec_separate) {
+    unit_of.resize(h->nrec);
+    for (int r = 0; r < h->nrec; ++r) {
+      unit_of[r] = pos[chunk_of[rec_ez[r]]] * nstrips + rec_ex[r] / kMarchColsHost;
+      cnt[unit_of[r] + 1]++;
+    }
+  }
+  for (int k = 0; k < nu; ++k) cnt[k + 1] += cnt[k];
+  ids.resize(std::max(cnt[nu], 1));
+  {
+    std::vector<int> fill(cnt.begin(), cnt.end() - 1);
+    for (size_t r = 0; r < unit_of.size(); ++r) ids[fill[unit_of[r]]++] = int(r);
+  }
+  std::vector<int> units((size_t)nu * kMarchUnitInts);
+  for (int k = 0; k < nch; ++k)
+    for (int sx = 0; sx < nstrips; ++sx) {
+      const int u = k * nstrips + sx, y = order[k];
+      int *U = &units[(size_t)u * kMarchUnitInts];
+      U[0] = 0;
+      U[1] = sx;
+      U[2] = zb[y];
+      U[3] = zb[y + 1];
+      U[4] = cnt[u];
+      U[5] = cnt[u + 1];
+    }
+  int *du = nullptr;
+  if ((st = dupload(h, &du, units)) || (st = dupload(h, &h->d_march_rec, ids))) return st;
+  h->d_march_units = du;
+  h->march_units_host = units;
+  h->march_nunits = nu;
+  h->march_cz = cz;
+  h->march = true;
+  return SEM2D_OK;
+}
+
 int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t shared = nullptr,
                 int force_tz = 0) {
   if (d->ngll != 5 && d->ngll != 6 && d->ngll != 9)
@@ -978,6 +1120,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     h->rec_separate = !d->rec_node && h->rec_field != 'D';
   }
   if ((st = dalloc(h, &h->sis, (size_t)std::max(h->rec_nsamp, 1) * std::max(h->nrec, 1) * h->ndof))) return st;
+  std::vector<int> rec_ex, rec_ez, rec_jn;  // element owning each receiver (march units), node row
   // strips of TX element columns by chunks of element rows, fault split kept inside a chunk
   h->TX = strip_width(h->N);
   if (h->TX <= 0) return set_err(h, SEM2D_E_UNSUPPORTED, "NGLL not compiled");
@@ -1019,6 +1162,9 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
       for (int z = h->ztile[y]; z < h->ztile[y + 1]; ++z) etile[z] = y;
     std::vector<int> rI, rJ, lat, owner(h->nrec);
     std::vector<double> w;
+    rec_ex.assign(h->nrec, 0);
+    rec_ez.assign(h->nrec, 0);
+    rec_jn.assign(h->nrec, -1);
     const int NN = h->N * h->N;
     for (int r = 0; r < h->nrec; ++r) {
       if (d->rec_node) {
@@ -1032,6 +1178,9 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
         w.push_back(1.0);
         const int x = std::min(I / (h->TX * (h->N - 1)), gx - 1);
         owner[r] = tileJ[J] * gx + x;
+        rec_ex[r] = std::min(I / (h->N - 1), h->nx - 1);
+        rec_ez[r] = owner_row(h, J);
+        rec_jn[r] = J;
       } else {
         const int e = d->rec_elem[r] - 1;
         if (e < 0 || e >= d->nelem) return set_err(h, SEM2D_E_ARG, "receiver element out of range");
@@ -1043,6 +1192,8 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
           w.push_back(d->rec_interp[q + (size_t)NN * r]);
         }
         owner[r] = etile[h->elem_ez[e]] * gx + h->elem_ex[e] / h->TX;
+        rec_ex[r] = h->elem_ex[e];
+        rec_ez[r] = h->elem_ez[e];
       }
     }
     std::vector<int> start(gx * gy + 1, 0), ids(h->nrec);
@@ -1068,6 +1219,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     bc.fast = fast_path(h);
     if (configure_bulk(bc)) return set_err(h, SEM2D_E_CUDA, bulk_last_error());
   }
+  if ((st = setup_march(h, rec_ex, rec_ez, rec_jn, force_tz))) return st;
   if ((st = reset_state(h))) return st;
   CK(cudaStreamSynchronize(h->stream));
   return SEM2D_OK;
@@ -1131,6 +1283,10 @@ int batch_close_impl(sem2d_handle *h) {
   h->scheme = a->scheme;
   h->TX = a->TX;
   h->TZ = a->TZ;
+  // the march kernel runs the batch when it covers every member and none
+  // has a fault (the fault kernel is per problem)
+  h->march = true;
+  for (const sem2d_handle *m : h->subs) h->march = h->march && m->march && !m->nflt;
   int st;
   if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)))
     return st;
@@ -1143,6 +1299,7 @@ int batch_close_impl(sem2d_handle *h) {
       if (h->mixed) {
         FaultParams<float> f;
         BulkConfig bc = make_config<float>(m, cur, f);
+        if (h->march) bc.rec_ids = m->nrec ? m->d_march_rec : nullptr;
         fill_params_block(bc, blk.data() + pb * i);
       } else {
         FaultParams<double> f;
@@ -1164,6 +1321,21 @@ int batch_close_impl(sem2d_handle *h) {
   }
   h->nunits = int(units.size() / 4);
   if ((st = dupload(h, reinterpret_cast<int **>(&h->d_units), units))) return st;
+  if (h->march) {
+    std::vector<int> mu;
+    for (int i = 0; i < nsim; ++i) {
+      const std::vector<int> &src = h->subs[i]->march_units_host;
+      for (size_t k = 0; k < src.size(); k += kMarchUnitInts) {
+        mu.insert(mu.end(), src.begin() + k, src.begin() + k + kMarchUnitInts);
+        mu[mu.size() - kMarchUnitInts] = i;
+      }
+    }
+    h->march_nunits = int(mu.size() / kMarchUnitInts);
+    int *du = nullptr;
+    if ((st = dupload(h, &du, mu))) return st;
+    h->d_march_units = du;
+    h->march_cz = a->march_cz;
+  }
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
@@ -1493,8 +1665,7 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
         bc.Dnext = RD[j];
         bc.Vnext = RV[j];
         bc.Anext = RA[j];
-        bc.rec_tile_start = nullptr;
-        st = launch_bulk(bc) ? set_err(h, SEM2D_E_CUDA, bulk_last_error()) : SEM2D_OK;
+        st = launch_step_kernel(h, bc, false) ? set_err(h, SEM2D_E_CUDA, bulk_last_error()) : SEM2D_OK;
       } else {
         FaultParams<double> f;
         BulkConfig bc = make_config<double>(h, h->cur, f);
@@ -1503,8 +1674,7 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
         bc.Dnext = RD[j];
         bc.Vnext = RV[j];
         bc.Anext = RA[j];
-        bc.rec_tile_start = nullptr;
-        st = launch_bulk(bc) ? set_err(h, SEM2D_E_CUDA, bulk_last_error()) : SEM2D_OK;
+        st = launch_step_kernel(h, bc, false) ? set_err(h, SEM2D_E_CUDA, bulk_last_error()) : SEM2D_OK;
       }
       h->launches++;
     }
@@ -1695,8 +1865,8 @@ long long sem2d_gpu_kernel_launches(sem2d_handle *h) { return h ? h->launches : 
 
 int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz) {
   if (!h) return SEM2D_E_ARG;
-  if (tx) *tx = h->TX;
-  if (tz) *tz = h->TZ;
+  if (tx) *tx = h->march ? kMarchColsHost : h->TX;
+  if (tz) *tz = h->march ? h->march_cz : h->TZ;
   return SEM2D_OK;
 }
 
