@@ -64,17 +64,23 @@ __device__ double rsf_theta(const FaultParams<real> &p, int k, double th, double
   return th * ex + p.dt * (1.0 - 0.5 * p.dt * x);
 }
 
+// the factor 2 V* exp(-(f0 + b ln(V* theta/Dc))/a) of the slip-rate law,
+// fixed during one solve (theta does not change)
 template <typename real>
-__device__ void nr_func(const FaultParams<real> &p, int k, double th, double tau, double ts,
-                        double sig, double Z, double &fn, double &dfn, double &v) {
+__device__ double nr_rate_factor(const FaultParams<real> &p, int k, double th) {
   double tmp = p.rsf_kind == 4
                    ? p.rsf_mus[k] + p.rsf_b[k] * log(p.rsf_vc[k] * th / p.rsf_dc[k] + 1.0)
                    : p.rsf_mus[k] + p.rsf_b[k] * log(p.rsf_vstar[k] * th / p.rsf_dc[k]);
-  tmp = 2.0 * p.rsf_vstar[k] * exp(-tmp / p.rsf_a[k]);
-  const double sa = -sig * p.rsf_a[k];
-  v = sinh(tau / sa) * tmp;
+  return 2.0 * p.rsf_vstar[k] * exp(-tmp / p.rsf_a[k]);
+}
+
+// tau_stick - Z v(tau) - tau and its derivative (nr_fric_func_tau,
+// bc_dynflt_rsf.f90:533-568); rf = nr_rate_factor, sa = -sigma a
+__device__ __forceinline__ void nr_func(double rf, double sa, double tau, double ts, double Z, double &fn,
+                                        double &dfn, double &v) {
+  v = sinh(tau / sa) * rf;
   fn = ts - Z * v - tau;
-  dfn = -Z * (cosh(tau / sa) * tmp / sa) - 1.0;
+  dfn = -Z * (cosh(tau / sa) * rf / sa) - 1.0;
 }
 
 // bracketed Newton-Raphson with bisection (bc_dynflt_rsf.f90:369-468);
@@ -82,9 +88,10 @@ __device__ void nr_func(const FaultParams<real> &p, int k, double th, double tau
 template <typename real>
 __device__ double nr_solve(const FaultParams<real> &p, int k, double xL, double xR, double xacc,
                            double th, double ts, double sig, double Z, bool &fail) {
+  const double rf = nr_rate_factor(p, k, th), sa = -sig * p.rsf_a[k];
   double flo, fhi, dfn, v, xl = xL, xr = xR;
-  nr_func(p, k, th, xL, ts, sig, Z, flo, dfn, v);
-  nr_func(p, k, th, xR, ts, sig, Z, fhi, dfn, v);
+  nr_func(rf, sa, xL, ts, Z, flo, dfn, v);
+  nr_func(rf, sa, xR, ts, Z, fhi, dfn, v);
   int guard = 0;
   while (flo * fhi > 0) {
     if (++guard > kNrMaxBracket) {
@@ -93,13 +100,13 @@ __device__ double nr_solve(const FaultParams<real> &p, int k, double xL, double 
     }
     xl = xl / 2.0;
     xr = xr * 2.0;
-    nr_func(p, k, th, xl, ts, sig, Z, flo, dfn, v);
-    nr_func(p, k, th, xr, ts, sig, Z, fhi, dfn, v);
+    nr_func(rf, sa, xl, ts, Z, flo, dfn, v);
+    nr_func(rf, sa, xr, ts, Z, fhi, dfn, v);
   }
   if (flo == 0 || fhi == 0) return v;
   double xlow = flo < 0 ? xl : xr, xhigh = flo < 0 ? xr : xl;
   double xest = 0.5 * (xl + xr), dxold = fabs(xr - xl), dx = dxold, fx;
-  nr_func(p, k, th, xest, ts, sig, Z, fx, dfn, v);
+  nr_func(rf, sa, xest, ts, Z, fx, dfn, v);
   for (int is = 0; is < kNrMaxIt; ++is) {
     if (((xest - xhigh) * dfn - fx) * ((xest - xlow) * dfn - fx) > 0 ||
         fabs(2 * fx) > fabs(dxold * dfn)) {
@@ -115,10 +122,10 @@ __device__ double nr_solve(const FaultParams<real> &p, int k, double xL, double 
       if (tmp == xest) return v;
     }
     if (fabs(dx) < fabs(xacc)) {
-      nr_func(p, k, th, xest, ts, sig, Z, fx, dfn, v);
+      nr_func(rf, sa, xest, ts, Z, fx, dfn, v);
       return v;
     }
-    nr_func(p, k, th, xest, ts, sig, Z, fx, dfn, v);
+    nr_func(rf, sa, xest, ts, Z, fx, dfn, v);
     if (fx < 0) xlow = xest;
     else xhigh = xest;
   }

@@ -1,5 +1,6 @@
 // march.cu -- instantiation and launch of the march kernels (FP32, NGLL = 5,
 // isotropic, leapfrog; material per node or per element).
+#include <algorithm>
 #include <string>
 
 #include "bulk_inst.cuh"
@@ -18,7 +19,7 @@ template <int NDOF, int MAT>
 int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
-  const int grid = (m.nunits + kMarchWarps - 1) / kMarchWarps;
+  const int grid = std::max(1, (m.nunits + kMarchWarps - 1) / kMarchWarps);  // an empty set still counts the step
   march_step_kernel<NDOF, MAT><<<grid, kThreads, 0, c.stream>>>(p, static_cast<const MarchUnit *>(m.units),
                                                                 m.nunits);
   const cudaError_t e = cudaGetLastError();
@@ -39,7 +40,7 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   b.nunits = m.nunits;
   b.step = m.step;
   b.done = m.done;
-  const int grid = (m.nunits + kMarchWarps - 1) / kMarchWarps;
+  const int grid = std::max(1, (m.nunits + kMarchWarps - 1) / kMarchWarps);  // an empty set still counts the step
   march_batch_kernel<NDOF, MAT><<<grid, kThreads, 0, c.stream>>>(b);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -78,7 +79,9 @@ int launch_march_batch(const BulkConfig &c, const MarchLaunch &m) {
 
 int launch_march_fault(const BulkConfig &c) {
   const FaultParams<float> &f = *static_cast<const FaultParams<float> *>(c.flt);
-  march_fault_kernel<<<(f.nflt + 127) / 128, 128, 0, c.stream>>>(f, static_cast<const float *>(c.fault_force));
+  // one warp per block: the node pairs spread over the SMs (the FP64 pipe
+  // of an SM is shared by its warps)
+  march_fault_kernel<<<(f.nflt + 31) / 32, 32, 0, c.stream>>>(f, static_cast<const float *>(c.fault_force));
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);

@@ -96,6 +96,13 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   const int nslot = perimeter_slots(p.LX, p.LZ);
   const float dt = p.dt, cv = p.cv;
   const bool src_on = it <= p.nt && p.nsrc > 0;
+  // the node update reads the step's inputs and writes other buffers
+  const float *__restrict__ Vc = p.Vcur;
+  const float *__restrict__ Dc = p.Dcur;
+  const float *__restrict__ Rm = p.rmass;
+  float *__restrict__ Vn = p.Vnext;
+  float *__restrict__ Dn = p.Dnext;
+  float *__restrict__ An = p.Anext;
 
   // first element row walked: one below the chunk when they share nodes
   int zs = u.z0;
@@ -108,17 +115,26 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     for (int i = 0; i < N; ++i) carry[c][i] = 0.f;
   bool have_carry = false;
 
-  // one node row of a field: this lane's 4 columns and the next lane's first
-  auto load_row = [&](const float *base, long long off, float *v) {
-    float4 q = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (ld) q = ldg4(base + off + I0);
-    v[0] = q.x;
-    v[1] = q.y;
-    v[2] = q.z;
-    v[3] = q.w;
-    const float nx4 = __shfl_down_sync(0xffffffffu, q.x, 1);
-    v[4] = lane < 31 ? nx4 : (act ? __ldg(base + off + I0 + 4) : 0.f);
+  // the displacement rows of the next element row are requested while the
+  // current row's nodes are updated: 16-byte parts here, the fifth column
+  // (shuffled or, for lane 31, loaded) when the row starts
+  // (P-SV: requested at the row start instead; carrying them through the
+  // node update costs more registers than P-SV has)
+  constexpr bool kPrefetch = NDOF == 1;
+  float4 nq[NDOF][N];
+  float n5[NDOF][N];
+  auto fetch_u = [&](int ezn) {
+    const long long o = (long long)p.row0[ezn] * p.pitch;
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c)
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const float *b = p.Dcur + c * pl + o + (long long)j * p.pitch + I0;
+        nq[c][j] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
+        n5[c][j] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
+      }
   };
+  if (kPrefetch) fetch_u(zs);
 
   for (int ez = zs; ez < u.z1; ++ez) {
     const bool halo = ez < u.z0;
@@ -129,10 +145,18 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
 
     // ---- element forces: A holds u, then d/deta; B holds d/dxi ----
     float A[NDOF][N][N], B[NDOF][N][N];
+    if (!kPrefetch) fetch_u(ez);
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
 #pragma unroll
-      for (int j = 0; j < N; ++j) load_row(p.Dcur + c * pl, (long long)(J0 + j) * p.pitch, A[c][j]);
+      for (int j = 0; j < N; ++j) {
+        A[c][j][0] = nq[c][j].x;
+        A[c][j][1] = nq[c][j].y;
+        A[c][j][2] = nq[c][j].z;
+        A[c][j][3] = nq[c][j].w;
+        const float nx4 = __shfl_down_sync(0xffffffffu, nq[c][j].x, 1);
+        A[c][j][4] = lane < 31 ? nx4 : n5[c][j];
+      }
     // d/dxi at (i,j): sum_q H[q + N i] u(q,j)
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
@@ -168,12 +192,36 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
       em0 = p.mat[0][eidx];
       if (NDOF == 2) em1 = p.mat[1][eidx];
     }
+    // node material: the 16-byte parts of row j+1 are requested before row
+    // j is used
+    float4 mq[2][2];
+    float m5[2][2];
+    auto fetch_m = [&](int j, int slot) {
+      if (MAT != kMatNode) return;
+#pragma unroll
+      for (int m = 0; m < NDOF; ++m) {
+        const float *b = p.mat[m] + (long long)(J0 + j) * p.pitch + I0;
+        mq[slot][m] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
+        m5[slot][m] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
+      }
+    };
+    fetch_m(0, 0);
 #pragma unroll
     for (int j = 0; j < N; ++j) {
       float m0[N], m1[N];
       if (MAT == kMatNode) {
-        load_row(p.mat[0], (long long)(J0 + j) * p.pitch, m0);
-        if (NDOF == 2) load_row(p.mat[1], (long long)(J0 + j) * p.pitch, m1);
+        if (j + 1 < N) fetch_m(j + 1, (j + 1) & 1);
+#pragma unroll
+        for (int m = 0; m < NDOF; ++m) {
+          const float4 q = mq[j & 1][m];
+          float *v = m == 0 ? m0 : m1;
+          v[0] = q.x;
+          v[1] = q.y;
+          v[2] = q.z;
+          v[3] = q.w;
+          const float nx4 = __shfl_down_sync(0xffffffffu, q.x, 1);
+          v[4] = lane < 31 ? nx4 : m5[j & 1][m];
+        }
       } else {
 #pragma unroll
         for (int i = 0; i < N; ++i) {
@@ -242,6 +290,8 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
 #pragma unroll
       for (int j = 0; j < N; ++j) L[c][j] = __shfl_up_sync(0xffffffffu, B[c][j][N - 1], 1);
 
+    if (kPrefetch && ez + 1 < u.z1) fetch_u(ez + 1);
+
     // the top node row: shared with the next element row (carry), the
     // lattice's top row, a fault side-1 row, or the next chunk's
     const int Jt = J0 + N - 1;
@@ -302,20 +352,20 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float vv[NDOF][N], rmv[N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = ldg4(p.Vcur + c * pl + g);
+          const float4 q = ldg4(Vc + c * pl + g);
           vv[c][0] = q.x;
           vv[c][1] = q.y;
           vv[c][2] = q.z;
           vv[c][3] = q.w;
-          vv[c][4] = last_col ? __ldg(p.Vcur + c * pl + g + 4) : 0.f;
+          vv[c][4] = last_col ? __ldg(Vc + c * pl + g + 4) : 0.f;
         }
         {
-          const float4 q = ldg4(p.rmass + g);
+          const float4 q = ldg4(Rm + g);
           rmv[0] = q.x;
           rmv[1] = q.y;
           rmv[2] = q.z;
           rmv[3] = q.w;
-          rmv[4] = last_col ? __ldg(p.rmass + g + 4) : 0.f;
+          rmv[4] = last_col ? __ldg(Rm + g + 4) : 0.f;
         }
         // dashpots and the perimeter inverse mass
 #pragma unroll
@@ -347,12 +397,12 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float dv[NDOF][N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = ldg4(p.Dcur + c * pl + g);
+          const float4 q = ldg4(Dc + c * pl + g);
           dv[c][0] = q.x;
           dv[c][1] = q.y;
           dv[c][2] = q.z;
           dv[c][3] = q.w;
-          dv[c][4] = last_col ? __ldg(p.Dcur + c * pl + g + 4) : 0.f;
+          dv[c][4] = last_col ? __ldg(Dc + c * pl + g + 4) : 0.f;
         }
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
@@ -368,13 +418,13 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
             vn[i] = vv[c][i] + cv * a;
             dn[i] = dv[c][i] + dt * vn[i];
           }
-          *reinterpret_cast<float4 *>(p.Vnext + c * pl + g) = make_float4(vn[0], vn[1], vn[2], vn[3]);
-          *reinterpret_cast<float4 *>(p.Dnext + c * pl + g) = make_float4(dn[0], dn[1], dn[2], dn[3]);
-          if (p.Anext) *reinterpret_cast<float4 *>(p.Anext + c * pl + g) = make_float4(an[0], an[1], an[2], an[3]);
+          *reinterpret_cast<float4 *>(Vn + c * pl + g) = make_float4(vn[0], vn[1], vn[2], vn[3]);
+          *reinterpret_cast<float4 *>(Dn + c * pl + g) = make_float4(dn[0], dn[1], dn[2], dn[3]);
+          if (An) *reinterpret_cast<float4 *>(An + c * pl + g) = make_float4(an[0], an[1], an[2], an[3]);
           if (last_col) {
-            p.Vnext[c * pl + g + 4] = vn[4];
-            p.Dnext[c * pl + g + 4] = dn[4];
-            if (p.Anext) p.Anext[c * pl + g + 4] = an[4];
+            Vn[c * pl + g + 4] = vn[4];
+            Dn[c * pl + g + 4] = dn[4];
+            if (An) An[c * pl + g + 4] = an[4];
           }
         }
       }

@@ -105,7 +105,17 @@ struct sem2d_handle {
   void *d_march_units = nullptr;
   int *d_march_rec = nullptr;
   std::vector<int> march_units_host;
-  float *d_fault_force = nullptr;   // forces of the fault rows, finished by the fault kernel
+  float *d_fault_force = nullptr;
+  // with a fault: the first march_fault_units units are the fault chunk's,
+  // launched as their own kernel with their own step/done counters; the
+  // fault chunk and the fault kernel run on fstream, overlapping the next
+  // step's other units (march_overlap)
+  int march_fault_units = 0;
+  int *d_step_c = nullptr;
+  unsigned *d_done_c = nullptr;
+  bool march_overlap = false;
+  cudaStream_t fstream = nullptr;
+  cudaEvent_t ev_m[2] = {nullptr, nullptr}, ev_c[2] = {nullptr, nullptr}, ev_f = nullptr;   // forces of the fault rows, finished by the fault kernel
   int nunits = 0, batch_grid = 0;
   bool batch_open = false;          // members may still be added
   // gradient workflow (sem2d_gpu_adjoint)
@@ -711,6 +721,17 @@ int launch_step_kernel(sem2d_handle *h, BulkConfig &bc, bool receivers) {
     MarchLaunch m;
     m.units = h->d_march_units;
     m.nunits = h->march_nunits;
+    if (h->march_fault_units) {
+      // the fault chunk's units, then the others
+      BulkConfig bf = bc;
+      bf.step = h->d_step_c;
+      bf.done = h->d_done_c;
+      MarchLaunch mf = m;
+      mf.nunits = h->march_fault_units;
+      m.units = static_cast<const int *>(h->d_march_units) + kMarchUnitInts * h->march_fault_units;
+      m.nunits = h->march_nunits - h->march_fault_units;
+      if (launch_march(bf, mf)) return 1;
+    }
     return launch_march(bc, m);
   }
   if (!receivers) bc.rec_tile_start = nullptr;
@@ -726,8 +747,9 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
   h->launches++;
   if (h->march && h->nflt) {
+    f.step = h->d_step_c;
     if (launch_march_fault(bc)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
-    h->launches++;
+    h->launches += 2;  // the fault chunk's kernel and the fault kernel
   }
   if (ev) CK(cudaEventRecord(ev[1], h->stream));
   if (ev) CK(cudaEventRecord(ev[2], h->stream));
@@ -793,6 +815,53 @@ void sync_members(sem2d_handle *h) {
   }
 }
 
+// Steps of a problem with a fault on two streams.  Step k: the fault
+// chunk's units (C_k) and then the fault kernel (Q_k) on fstream, the other
+// units (M_k) on the main stream.  C_k follows M_{k-1} (it reads the rows
+// M_{k-1} wrote) and Q_{k-1} (stream order); M_k follows C_{k-1} but not
+// Q_{k-1}: the fault kernel writes only the fault rows, which the chunk
+// layout keeps away from every other unit.  So the FP64 fault update of
+// step k runs while M_{k+1} computes.
+int launch_steps_overlap(sem2d_handle *h, int n) {
+  cudaStream_t S = h->stream, F = h->fstream;
+  CK(cudaEventRecord(h->ev_m[1], S));
+  CK(cudaEventRecord(h->ev_c[1], S));
+  for (int k = 0; k < n; ++k) {
+    const int q = k & 1;
+    FaultParams<float> f;
+    BulkConfig bc = make_config<float>(h, h->cur, f);
+    const bool rec = h->nrec && !h->rec_separate;
+    bc.rec_ids = rec ? h->d_march_rec : nullptr;
+    // C_k and Q_k
+    CK(cudaStreamWaitEvent(F, h->ev_m[q ^ 1], 0));
+    BulkConfig bf = bc;
+    bf.step = h->d_step_c;
+    bf.done = h->d_done_c;
+    bf.stream = F;
+    MarchLaunch mf;
+    mf.units = h->d_march_units;
+    mf.nunits = h->march_fault_units;
+    if (launch_march(bf, mf)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    CK(cudaEventRecord(h->ev_c[q], F));
+    f.step = h->d_step_c;
+    if (launch_march_fault(bf)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
+    // M_k
+    CK(cudaStreamWaitEvent(S, h->ev_c[q ^ 1], 0));
+    MarchLaunch mm;
+    mm.units = static_cast<const int *>(h->d_march_units) + kMarchUnitInts * h->march_fault_units;
+    mm.nunits = h->march_nunits - h->march_fault_units;
+    if (launch_march(bc, mm)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    CK(cudaEventRecord(h->ev_m[q], S));
+    h->launches += 3;
+    h->cur = 1 - h->cur;
+    h->steps++;
+  }
+  // the main stream ends after the last fault kernel
+  CK(cudaEventRecord(h->ev_f, F));
+  CK(cudaStreamWaitEvent(S, h->ev_f, 0));
+  return SEM2D_OK;
+}
+
 int launch_steps(sem2d_handle *h, int n) {
   if (!h->subs.empty()) {
     for (int k = 0; k < n; ++k) {
@@ -804,6 +873,7 @@ int launch_steps(sem2d_handle *h, int n) {
     sync_members(h);
     return SEM2D_OK;
   }
+  if (h->march_overlap) return launch_steps_overlap(h, n);
   for (int k = 0; k < n; ++k) {
     const int st = h->mixed ? launch_one_step<float>(h, h->cur) : launch_one_step<double>(h, h->cur);
     if (st) return st;
@@ -815,7 +885,7 @@ int launch_steps(sem2d_handle *h, int n) {
 
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
-  return 1 + (h->march && h->nflt ? 1 : 0) + (h->nrec && h->rec_separate ? 1 : 0);
+  return 1 + (h->march && h->nflt ? 2 : 0) + (h->nrec && h->rec_separate ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -860,6 +930,8 @@ int reset_state(sem2d_handle *h) {
   CK(cudaMemsetAsync(h->d_step, 0, sizeof(int), h->stream));
   CK(cudaMemsetAsync(h->d_done, 0, sizeof(unsigned), h->stream));
   CK(cudaMemsetAsync(h->d_error, 0, sizeof(int), h->stream));
+  if (h->d_step_c) CK(cudaMemsetAsync(h->d_step_c, 0, sizeof(int), h->stream));
+  if (h->d_done_c) CK(cudaMemsetAsync(h->d_done_c, 0, sizeof(unsigned), h->stream));
   if (h->sis) CK(cudaMemsetAsync(h->sis, 0, sizeof(double) * (size_t)h->rec_nsamp * h->nrec * h->ndof, h->stream));
   if (h->nflt) {
     const size_t nfd = (size_t)h->nflt * h->ndof;
@@ -942,19 +1014,38 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
     cz = int(((long long)nstrips * h->nz + target - 1) / target);
   }
   cz = std::max(1, std::min(cz, h->nz));
-  std::vector<int> zb;
-  for (int z = 0; z < h->nz; z += cz)
-    if (!(h->nflt && h->two && z > 0 && h->row0[z] == h->jf2)) zb.push_back(z);
+  // element rows touching a fault row; no chunk boundary inside them or
+  // right above them, so that only the fault chunk reads fault rows
+  int t0 = h->nz, t1 = -1;
+  if (h->nflt)
+    for (int z = 0; z < h->nz; ++z) {
+      const int a = h->row0[z], b = a + h->N - 1;
+      if ((h->jf1 >= a && h->jf1 <= b) || (h->two && h->jf2 >= a && h->jf2 <= b)) {
+        t0 = std::min(t0, z);
+        t1 = std::max(t1, z);
+      }
+    }
+  // chunks: the element rows reading a fault row (those touching one and
+  // the row above them, which reads the upper fault row as its halo) are
+  // chunks of one row each and come first; the others are cut every cz rows
+  std::vector<int> zb, order;
+  int nfch = 0;
+  if (t1 >= 0) {
+    const int f0 = t0, f1 = std::min(t1 + 2, h->nz);
+    for (int z = 0; z < f0; z += cz) zb.push_back(z);
+    for (int z = f0; z < f1; ++z) zb.push_back(z);
+    for (int z = f1; z < h->nz; z += cz) zb.push_back(z);
+    nfch = f1 - f0;
+  } else {
+    for (int z = 0; z < h->nz; z += cz) zb.push_back(z);
+  }
   zb.push_back(h->nz);
   const int nch = int(zb.size()) - 1;
-  int fch = -1;
-  if (h->nflt)
-    for (int y = 0; y < nch; ++y)
-      if (h->row0[zb[y]] <= h->jf1 && h->jf1 < (zb[y + 1] < h->nz ? h->row0[zb[y + 1]] : h->LZ)) fch = y;
-  std::vector<int> order, pos(nch);
-  if (fch >= 0) order.push_back(fch);
+  std::vector<int> pos(nch);
   for (int y = 0; y < nch; ++y)
-    if (y != fch) order.push_back(y);
+    if (t1 >= 0 && zb[y] >= t0 && zb[y] < t1 + 2) order.push_back(y);
+  for (int y = 0; y < nch; ++y)
+    if (!(t1 >= 0 && zb[y] >= t0 && zb[y] < t1 + 2)) order.push_back(y);
   for (int k = 0; k < nch; ++k) pos[order[k]] = k;
   std::vector<int> chunk_of(h->nz);
   for (int y = 0; y < nch; ++y)
@@ -995,6 +1086,20 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   h->march_nunits = nu;
   h->march_cz = cz;
   h->march = true;
+  if (nfch > 0) {
+    h->march_fault_units = nfch * nstrips;
+    if ((st = dalloc(h, &h->d_step_c, 1)) || (st = dalloc(h, &h->d_done_c, 1))) return st;
+    const char *ov = std::getenv("SEM2D_OVERLAP");
+    h->march_overlap = !h->rec_separate && !(ov && std::atoi(ov) == 0);
+    if (h->march_overlap) {
+      CK(cudaStreamCreateWithFlags(&h->fstream, cudaStreamNonBlocking));
+      for (int q = 0; q < 2; ++q) {
+        CK(cudaEventCreateWithFlags(&h->ev_m[q], cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&h->ev_c[q], cudaEventDisableTiming));
+      }
+      CK(cudaEventCreateWithFlags(&h->ev_f, cudaEventDisableTiming));
+    }
+  }
   return SEM2D_OK;
 }
 
@@ -1887,6 +1992,9 @@ int sem2d_gpu_destroy(sem2d_handle *h) {
   if (h->graph_exec) cudaGraphExecDestroy(h->graph_exec);
   for (void *p : h->allocs) cudaFree(p);
   if (h->stream && h->owns_stream) cudaStreamDestroy(h->stream);
+  if (h->fstream) cudaStreamDestroy(h->fstream);
+  for (cudaEvent_t e : {h->ev_m[0], h->ev_m[1], h->ev_c[0], h->ev_c[1], h->ev_f})
+    if (e) cudaEventDestroy(e);
   delete h;
   return SEM2D_OK;
 }
