@@ -153,6 +153,9 @@ def measured_peaks():
     return {"hbm_gbs": 6800.0}, "fallback"
 
 
+MARCH_TX = 31  # element columns of a unit of the march kernels
+
+
 def ncu_traffic(kernel, workload, npoin):
     """DRAM bytes per launch of `kernel` from the committed ncu summary of a
     (possibly smaller) capture of the workload, scaled by the node count."""
@@ -280,7 +283,9 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     bpn = BYTES_PER_NODE_STEP[(2, dtype)]
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
-    traffic = ncu_traffic("strip_batch_kernel", "batch_shots", npoin)
+    # the one-element-per-thread kernel covers FP32 NGLL=5 isotropic problems
+    kernel = "march_batch_kernel" if sim.tile[0] == MARCH_TX else "strip_batch_kernel"
+    traffic = ncu_traffic(kernel, "batch_shots", npoin)
     # end to end: uploads of every problem (the host arrays of the
     # descriptors), the time steps, all seismograms back, destroy
     barrier()
@@ -308,7 +313,7 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "strip_batch_kernel", "bytes_per_node_step": bpn,
+                         "kernel": kernel, "bytes_per_node_step": bpn,
                          "bulk_ms_per_launch": bulk_ms},
             "cpu_baseline": None,
             "e2e": {"value": e2e_value, "unit": "node-steps/s", "h2d_bytes_per_step": sizes["h2d"],
@@ -481,7 +486,8 @@ def main():
     bpn = BYTES_PER_NODE_STEP[(ndof, dtype)]
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
-    traffic = ncu_traffic("strip_step_kernel", args.workload, npoin)
+    kernel = "march_step_kernel" if sim.tile[0] == MARCH_TX else "strip_step_kernel"
+    traffic = ncu_traffic(kernel, args.workload, npoin)
 
     # end to end through the C-ABI from host buffers
     sim.close()
@@ -522,7 +528,7 @@ def main():
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
                          "traffic": traffic, "peak_kind": peak_kind,
-                         "kernel": "strip_step_kernel", "bytes_per_node_step": bpn,
+                         "kernel": kernel, "bytes_per_node_step": bpn,
                          "bulk_ms_per_launch": bulk_ms, "fault_ms_per_launch": kms[1] / nt,
                          "receiver_ms_per_launch": kms[2] / nt},
             "cpu_baseline": base,

@@ -342,3 +342,9 @@ class BatchSolver:
     @property
     def launches(self):
         return lib().sem2d_gpu_kernel_launches(self.h)
+
+    @property
+    def tile(self):
+        tx, tz = C.c_int(), C.c_int()
+        self._check(lib().sem2d_gpu_tile_shape(self.h, C.byref(tx), C.byref(tz)))
+        return tx.value, tz.value

@@ -54,11 +54,12 @@ namespace sem2d {
 
 constexpr int kMarchWarps = 4;     // warps per CTA
 constexpr int kMarchCols = 31;     // element columns owned by a warp
-// resident CTAs per SM the register budget allows: 128 registers per
-// thread for SH, 168 for P-SV
+// resident CTAs per SM the register budget allows: 102 registers per
+// thread for SH (20 warps per SM), 168 for P-SV (12 warps; fewer registers
+// spill the node-material variant)
 template <int NDOF>
 struct MarchOcc {
-  static constexpr int kMinBlocks = NDOF == 1 ? 4 : 3;
+  static constexpr int kMinBlocks = NDOF == 1 ? 5 : 3;
 };
 
 // one unit of work: a strip of element columns and a chunk of element rows

@@ -742,16 +742,34 @@ template <typename real>
 int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   FaultParams<real> f;
   BulkConfig bc = make_config<real>(h, cur, f);
-  if (ev) CK(cudaEventRecord(ev[0], h->stream));
-  int st = launch_step_kernel(h, bc, h->nrec && !h->rec_separate);
-  if (st) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
-  h->launches++;
-  if (h->march && h->nflt) {
+  const bool rec = h->nrec && !h->rec_separate;
+  if (h->march && h->march_fault_units) {
+    // the units reading fault rows, then the others (the timed bulk), then
+    // the fault kernel
+    bc.rec_ids = rec ? h->d_march_rec : nullptr;
+    BulkConfig bf = bc;
+    bf.step = h->d_step_c;
+    bf.done = h->d_done_c;
+    MarchLaunch mf;
+    mf.units = h->d_march_units;
+    mf.nunits = h->march_fault_units;
+    if (launch_march(bf, mf)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    if (ev) CK(cudaEventRecord(ev[0], h->stream));
+    MarchLaunch mm;
+    mm.units = static_cast<const int *>(h->d_march_units) + kMarchUnitInts * h->march_fault_units;
+    mm.nunits = h->march_nunits - h->march_fault_units;
+    if (launch_march(bc, mm)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    if (ev) CK(cudaEventRecord(ev[1], h->stream));
     f.step = h->d_step_c;
     if (launch_march_fault(bc)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
-    h->launches += 2;  // the fault chunk's kernel and the fault kernel
+    h->launches += 3;
+  } else {
+    if (ev) CK(cudaEventRecord(ev[0], h->stream));
+    if (launch_step_kernel(h, bc, rec))
+      return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    h->launches++;
+    if (ev) CK(cudaEventRecord(ev[1], h->stream));
   }
-  if (ev) CK(cudaEventRecord(ev[1], h->stream));
   if (ev) CK(cudaEventRecord(ev[2], h->stream));
   if (h->nrec && h->rec_separate) {
     RecParams<real> r{};
