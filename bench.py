@@ -443,6 +443,12 @@ def main():
     npoin, nt, ndof = desc.npoin, desc.nt, desc.ndof
     if args.time_steps:
         nt = min(nt, args.time_steps)
+    elif args.workload == "psv_rsf":
+        # the synthetic rate-and-state rupture runs away after about 5000
+        # steps (slip rates above 30 m/s, then the Newton solver exceeds the
+        # reference's 200 iterations in every precision and kernel): the
+        # first 4000 of its 10000 steps are timed
+        nt = min(nt, 4000)
     dtype = "f32" if desc.precision == 1 else "f64"
     sim = Solver(desc, owner=prob)
     stream = torch.cuda.ExternalStream(sim.stream)

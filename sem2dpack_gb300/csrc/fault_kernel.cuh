@@ -24,18 +24,32 @@ constexpr int kNrMaxIt = 200;       // bc_dynflt_rsf.f90:372
 constexpr int kNrMaxBracket = 200;  // bound for the loop at bc_dynflt_rsf.f90:393-398
 constexpr int kErrNR = -4;          // SEM2D_E_NR
 
+// slip-weakening parameters of one node (read together, before any store)
+struct SwfNode {
+  double dc, mus, mud, p, alpha;
+};
+
+template <typename real>
+__device__ __forceinline__ SwfNode swf_node(const FaultParams<real> &p, int k) {
+  return SwfNode{p.swf_dc[k], p.swf_mus[k], p.swf_mud[k], p.swf_kind == 3 ? p.swf_p[k] : 0.0, p.swf_alpha[k]};
+}
+
+__device__ __forceinline__ double swf_mu_of(int kind, const SwfNode &w, double th) {
+  double mu;
+  if (kind == 1) {
+    const double r = th / w.dc;
+    mu = w.mus - (w.mus - w.mud) * (r < 1.0 ? r : 1.0);
+  } else if (kind == 2) {
+    mu = w.mud - (w.mud - w.mus) * exp(-th / w.dc);
+  } else {
+    mu = w.mud + (w.mus - w.mud) / pow(1.0 + th / w.dc, w.p);
+  }
+  return mu + w.alpha * th;
+}
+
 template <typename real>
 __device__ double swf_mu(const FaultParams<real> &p, int k, double th) {
-  double mu;
-  if (p.swf_kind == 1) {
-    const double r = th / p.swf_dc[k];
-    mu = p.swf_mus[k] - (p.swf_mus[k] - p.swf_mud[k]) * (r < 1.0 ? r : 1.0);
-  } else if (p.swf_kind == 2) {
-    mu = p.swf_mud[k] - (p.swf_mud[k] - p.swf_mus[k]) * exp(-th / p.swf_dc[k]);
-  } else {
-    mu = p.swf_mud[k] + (p.swf_mus[k] - p.swf_mud[k]) / pow(1.0 + th / p.swf_dc[k], p.swf_p[k]);
-  }
-  return mu + p.swf_alpha[k] * th;
+  return swf_mu_of(p.swf_kind, swf_node(p, k), th);
 }
 
 template <typename real>
@@ -250,6 +264,12 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     T[c] = p.Z[k + nf * c] * (dV[c] + p.coefA2V * dA[c]);
   }
   const double nx = p.n1[k], nz = p.n1[k + nf];
+  // the node's other inputs, read before any of its stores so that their
+  // latencies overlap
+  const double T00 = p.T0[k], T01 = p.T0[k + nf], sig_old = p.sigma[k], th_old = p.theta[k];
+  const double Dk = p.D[k], Vk = p.V[k], cohk = p.coh[k], Zk = p.Z[k];
+  SwfNode swn{0, 0, 0, 0, 0};
+  if (p.friction == 1) swn = swf_node(p, k);
   if (nd == 2) {
     double r0, r1;
     r0 = nz * dD[0] - nx * dD[1]; r1 = nx * dD[0] + nz * dD[1]; dD[0] = r0; dD[1] = r1;
@@ -258,28 +278,27 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     r0 = nz * T[0] - nx * T[1];   r1 = nx * T[0] + nz * T[1];   T[0] = r0;  T[1] = r1;
   }
   if (!p.two || nd == 1) T[1] = 0.0;
-  T[0] = T[0] + p.T0[k];
-  T[1] = T[1] + p.T0[k + nf];
+  T[0] = T[0] + T00;
+  T[1] = T[1] + T01;
   if (p.opening) T[1] = T[1] < 0.0 ? T[1] : 0.0;
-  double sig = p.sigma[k];
+  double sig = sig_old;
   if (p.normal_kind == 1) sig = T[1];
   else if (p.normal_kind == 2) sig = T[1] + p.normal_coef * (sig - T[1]);
   else if (p.normal_kind == 3)
     sig = T[1] + exp(-(fabs(dV[0]) + p.normal_V) * p.normal_coef) * (sig - T[1]);
-  p.sigma[k] = sig;
-  double mu;
+  double mu, th_new = th_old;
   if (p.friction == 2) {
     bool fail = false;
-    const double vold = p.V[k], th0 = p.theta[k];
+    const double vold = Vk, th0 = th_old;
     const double th1 = rsf_theta(p, k, th0, vold);
-    double vnew = rsf_V(p, k, T[0], sig, th1, th0, p.Z[k], fail);
+    double vnew = rsf_V(p, k, T[0], sig, th1, th0, Zk, fail);
     const double th2 = rsf_theta(p, k, th0, 0.5 * (vold + vnew));
-    vnew = rsf_V(p, k, T[0], sig, th2, th0, p.Z[k], fail);
+    vnew = rsf_V(p, k, T[0], sig, th2, th0, Zk, fail);
     if (fail) atomicExch(p.error, kErrNR);
-    p.theta[k] = th2;
+    th_new = th2;
     mu = rsf_mu(p, k, vnew, th2);
     if (p.twf_kind) {
-      const double mt = twf_mu(p, k, it * p.dt, p.D[k]);
+      const double mt = twf_mu(p, k, it * p.dt, Dk);
       if (mt < mu) mu = mt;
     }
     T[0] = copysign(fabs(-mu * sig), T[0]);
@@ -288,7 +307,7 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     Ts[1] = 0.0;
   } else {
     if (p.friction == 1) {
-      double th = p.theta[k];
+      double th = th_old;
       if (p.coefA2D == 0.0) {
         if (p.swf_healing) {
           th = th + fabs(dV[0]) * p.dt;
@@ -297,30 +316,32 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
           th = fabs(dD[0]);
         }
       } else {
-        th = fabs(p.D[k]);
+        th = fabs(Dk);
       }
-      p.theta[k] = th;
-      mu = swf_mu(p, k, th);
+      th_new = th;
+      mu = swf_mu_of(p.swf_kind, swn, th);
       if (p.twf_kind) {
-        const double mt = twf_mu(p, k, it * p.dt, p.D[k]);
+        const double mt = twf_mu(p, k, it * p.dt, Dk);
         if (mt < mu) mu = mt;
       }
     } else {  // time weakening alone
-      mu = twf_mu(p, k, it * p.dt, p.D[k]);
+      mu = twf_mu(p, k, it * p.dt, Dk);
     }
-    const double strength = p.coh[k] - mu * sig;
+    const double strength = cohk - mu * sig;
     Ts[0] = T[0];
     Ts[1] = T[1];
     const double at = fabs(T[0]);
     T[0] = copysign(fabs(at < strength ? at : strength), T[0]);
   }
+  p.sigma[k] = sig;
+  if (p.friction == 1 || p.friction == 2) p.theta[k] = th_new;
   p.MU[k] = mu;
-  T[0] = T[0] - p.T0[k];
-  T[1] = T[1] - p.T0[k + nf];
+  T[0] = T[0] - T00;
+  T[1] = T[1] - T01;
   p.T[k] = T[0];
   p.T[k + nf] = T[1];
-  p.Tstick[k] = Ts[0] - p.T0[k];
-  p.Tstick[k + nf] = Ts[1] - p.T0[k + nf];
+  p.Tstick[k] = Ts[0] - T00;
+  p.Tstick[k + nf] = Ts[1] - T01;
   double Tx[2] = {T[0], T[1]};
   if (nd == 2) {
     Tx[0] = nz * T[0] + nx * T[1];
