@@ -169,6 +169,10 @@ typedef struct sem2d_problem_desc {
    * defines the moduli from rho, cp, cs): rho is required and the material
    * must be continuous at nodes. */
   int adjoint;
+  /* 1 records the fault potency of the displacement and the velocity at
+   * every step (BC_DYNFLT_potency, bc_dynflt.f90:757,832-855), read with
+   * sem2d_gpu_get_fault_potency.  Single problems only (not in a batch). */
+  int flt_potency;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;
@@ -259,6 +263,15 @@ int sem2d_gpu_get_seismograms(sem2d_handle *h, double *sis);
  * the 6 records of BC_DYNFLT_write: slip, slip rate, shear traction,
  * normal traction, friction coefficient, T_stick (bc_dynflt.f90:760-767). */
 int sem2d_gpu_get_fault(sem2d_handle *h, double *out);
+
+/* Copies the fault potency series of a handle created with
+ * desc->flt_potency = 1 (the FltXX_potency_sem2d.tab records of
+ * BC_DYNFLT_write, bc_dynflt.f90:757 with BC_DYNFLT_potency :832-855):
+ * out[6*it + q], it = 0..nt, q = 0..2 the potency of the displacement
+ * (P-SV: p11, p22, p12; SH: p13, p23, 0) and q = 3..5 that of the velocity,
+ * after step it (row 0: the initial state).  Rows of steps not yet run are
+ * zero. */
+int sem2d_gpu_get_fault_potency(sem2d_handle *h, double *out);
 
 /* Current fault state D(nflt,ndof), V(nflt,ndof), T(nflt,2), MU(nflt),
  * state variable theta(nflt) (RSF, else zeros); any pointer may be NULL. */

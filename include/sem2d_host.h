@@ -145,6 +145,9 @@ typedef struct sem2d_deck {
    * kind 1, MuS 0.6, MuD 0.5, Mu0 0.6, X = Z = 0, V 1e3, L 1, T = Dc = huge */
   int twf_kind;
   double twf_mus, twf_mud, twf_mu0, twf_X, twf_Z, twf_V, twf_L, twf_T, twf_Dc;
+  /* 1: record the fault potency every step (the FltXX_potency_sem2d.tab
+   * file of the reference, bc_dynflt.f90:436,757)                        */
+  int flt_potency;
 } sem2d_deck;
 
 typedef struct sem2d_grid sem2d_grid;

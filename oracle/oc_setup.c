@@ -1392,6 +1392,7 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
     d->twf_L = dk->twf_L;
     d->twf_T = dk->twf_T;
     d->twf_Dc = dk->twf_Dc;
+    d->flt_potency = dk->flt_potency;
   }
   return 0;
 }

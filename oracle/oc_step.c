@@ -70,6 +70,8 @@ struct oc_sim {
   double *fcoord; /* (2,nflt) positions of node1 (bc_dynflt.f90:302) */
   int oit, oitd, oix1, oixn, oixd, fnsamp, onx, fsamp;
   double *fseries;
+  int pot_rows;   /* nt + 1 */
+  double *pseries; /* [6*it + q]: potency of d (q < 3) and v (q >= 3) */
   /* fields */
   double *d, *v, *a;
   int it;
@@ -589,6 +591,46 @@ static void rec_store(oc_sim *s) {
     }
 }
 
+/* BC_DYNFLT_potency (bc_dynflt.f90:832-855) of the displacement and the
+ * velocity after the step, written every step (bc_dynflt.f90:757); the
+ * jump is get_jump (bc_dynflt.f90:692-704).  P-SV: p11, p22, p12; SH: p13,
+ * p23 (third entry zero). */
+static void flt_potency(oc_sim *s) {
+  if (s->nflt == 0 || s->it >= s->pot_rows) return;
+  const int nf = s->nflt, nd = s->ndof;
+  const size_t np = (size_t)s->npoin;
+  double *o = s->pseries + 6 * (size_t)s->it;
+  for (int f = 0; f < 2; f++) {
+    const double *x = f == 0 ? s->d : s->v;
+    double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+    for (int k = 0; k < nf; k++) {
+      double dl[2] = {0.0, 0.0};
+      for (int c = 0; c < nd; c++) {
+        const double x1 = x[(size_t)(s->node1[k] - 1) + np * c];
+        dl[c] = s->two ? x[(size_t)(s->node2[k] - 1) + np * c] - x1 : -2.0 * x1;
+      }
+      const double nx = s->n1[k], nz = s->n1[k + nf], b = s->B[k];
+      if (nd == 2) {
+        p0 = p0 + nx * dl[0] * b;
+        p1 = p1 + nz * dl[1] * b;
+        p2 = p2 + (nx * dl[1] + nz * dl[0]) * b;
+      } else {
+        p0 = p0 + nx * dl[0] * b;
+        p1 = p1 + nz * dl[0] * b;
+      }
+    }
+    if (nd == 2) {
+      o[3 * f] = p0;
+      o[3 * f + 1] = p1;
+      o[3 * f + 2] = 0.5 * p2;
+    } else {
+      o[3 * f] = 0.5 * p0;
+      o[3 * f + 1] = 0.5 * p1;
+      o[3 * f + 2] = 0.0;
+    }
+  }
+}
+
 static void flt_write(oc_sim *s) {
   if (s->nflt == 0 || s->it < s->oit) return;
   if (s->fsamp < s->fnsamp) {
@@ -742,10 +784,13 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
     s->fnsamp = dd->flt_nsamp;
     s->onx = (s->oixn - s->oix1) / s->oixd + 1;
     s->fseries = xcalloc((size_t)s->onx * 6 * (s->fnsamp > 0 ? s->fnsamp : 1), sizeof(double));
+    s->pot_rows = (dd->nt > 0 ? dd->nt : 0) + 1;
+    s->pseries = xcalloc((size_t)6 * s->pot_rows, sizeof(double));
   }
   /* step-0 outputs: REC_store(rec,0) (main.f90:35), BC_write(bc,0) (bc_gen.f90:247) */
   s->it = 0;
   flt_write(s);
+  flt_potency(s);
   rec_store(s);
   return s;
 }
@@ -782,6 +827,7 @@ int oc_sim_run(oc_sim *s, int nsteps) {
     }
     rec_store(s);
     flt_write(s);
+    flt_potency(s);
     if (s->status) return s->status;
   }
   return s->status;
@@ -804,6 +850,10 @@ void oc_sim_fault_series(const oc_sim *s, double *out) {
   if (s->nflt) memcpy(out, s->fseries, (size_t)s->onx * 6 * s->fnsamp * sizeof(double));
 }
 
+void oc_sim_fault_potency(const oc_sim *s, double *out) {
+  if (s->nflt) memcpy(out, s->pseries, (size_t)6 * s->pot_rows * sizeof(double));
+}
+
 void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T, double *MU,
                         double *theta) {
   int nf = s->nflt, nd = s->ndof;
@@ -824,7 +874,7 @@ void oc_sim_free(oc_sim *s) {
                   s->swf_mus, s->swf_mud, s->swf_p, s->swf_alpha, s->theta, s->rsf_dc,
                   s->rsf_mus, s->rsf_a, s->rsf_b, s->rsf_vstar, s->rsf_vc, s->rsf_Tc,
                   s->rsf_coeft, s->D, s->V, s->T, s->Tstick, s->MU, s->sigma, s->fseries,
-                  s->d, s->v, s->a, s->beta25, s->fcoord};
+                  s->d, s->v, s->a, s->beta25, s->fcoord, s->pseries};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(s);
 }

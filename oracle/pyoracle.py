@@ -46,6 +46,7 @@ def lib():
         L.oc_sim_fields.argtypes = [vp, dp, dp, dp]
         L.oc_sim_seismograms.argtypes = [vp, dp]
         L.oc_sim_fault_series.argtypes = [vp, dp]
+        L.oc_sim_fault_potency.argtypes = [vp, dp]
         L.oc_sim_fault_state.argtypes = [vp, dp, dp, dp, dp, dp]
         L.oc_sim_free.argtypes = [vp]
         L.oc_gll_info.argtypes = [C.c_int, dp, dp, dp]
@@ -176,6 +177,14 @@ class OracleSim:
         a = np.zeros(max(onx * 6 * d.flt_nsamp, 1))
         lib().oc_sim_fault_series(self.h, _p(a))
         return a[: onx * 6 * d.flt_nsamp].reshape(onx, 6, d.flt_nsamp, order="F")
+
+    def fault_potency(self):
+        """(nt+1, 2, 3): potency of displacement and velocity at every step."""
+        d = self.desc
+        a = np.zeros(6 * (d.nt + 1))
+        if d.nflt:
+            lib().oc_sim_fault_potency(self.h, _p(a))
+        return a.reshape(d.nt + 1, 2, 3)
 
     def fault_state(self):
         d = self.desc

@@ -59,6 +59,8 @@ int oc_sim_step_count(const oc_sim *s);
 void oc_sim_fields(const oc_sim *s, double *displ, double *veloc, double *accel);
 void oc_sim_seismograms(const oc_sim *s, double *sis);
 void oc_sim_fault_series(const oc_sim *s, double *out);
+/* [6*it + q], it = 0..nt: fault potency of d (q = 0..2) and v (q = 3..5) */
+void oc_sim_fault_potency(const oc_sim *s, double *out);
 void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T,
                         double *MU, double *theta);
 void oc_sim_free(oc_sim *s);

@@ -90,6 +90,7 @@ class ProblemDesc(C.Structure):
         ("twf_T", c_double), ("twf_Dc", c_double),
         ("rho", P_double),
         ("adjoint", c_int),
+        ("flt_potency", c_int),
     ]
 
 
@@ -141,6 +142,7 @@ class Deck(C.Structure):
         ("twf_mus", c_double), ("twf_mud", c_double), ("twf_mu0", c_double),
         ("twf_X", c_double), ("twf_Z", c_double), ("twf_V", c_double), ("twf_L", c_double),
         ("twf_T", c_double), ("twf_Dc", c_double),
+        ("flt_potency", c_int),
     ]
 
 

@@ -226,6 +226,13 @@ class Solver:
         self._check(lib().sem2d_gpu_get_fault(self.h, _p(a)))
         return a[:n].reshape(onx, 6, d.flt_nsamp, order="F")
 
+    def fault_potency(self):
+        """(nt+1, 2, 3): potency of the displacement and of the velocity after
+        every step (a handle created with desc.flt_potency = 1)."""
+        a = np.zeros(6 * (self.desc.nt + 1))
+        self._check(lib().sem2d_gpu_get_fault_potency(self.h, _p(a)))
+        return a.reshape(self.desc.nt + 1, 2, 3)
+
     def fault_state(self):
         d = self.desc
         nf, nd = d.nflt, d.ndof

@@ -352,6 +352,7 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     p.D[k + nf * c] = dD[c] + p.coefA2D * dAc;
     p.V[k + nf * c] = dV[c] + p.coefA2V * dAc;
   }
+  double vnew[2][2] = {{0, 0}, {0, 0}};
   for (int side = 0; side < 1 + p.two; ++side) {
     const int J = side == 0 ? p.jf1 : p.jf2;
     for (int c = 0; c < nd; ++c) {
@@ -365,10 +366,37 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
       p.d64[o] = dn;
       p.v64[o] = vn;
       p.a64[o] = a;
+      vnew[side][c] = vn;
       const long long g = c * p.plane + (long long)J * p.pitch + k;
       p.Dnext[g] = real(dn);
       p.Vnext[g] = real(vn);
       if (p.Anext) p.Anext[g] = real(a);
+    }
+  }
+  if (p.pot) {
+    // this pair's terms of BC_DYNFLT_potency (bc_dynflt.f90:832-855) for
+    // the displacement d^n and the velocity v^n of the step (get_jump,
+    // bc_dynflt.f90:692-704): P-SV p11, p22, p12; SH p13, p23
+    const double b = p.B[k];
+    for (int f = 0; f < 2; ++f) {
+      double dl[2] = {0, 0};
+      for (int c = 0; c < nd; ++c) {
+        const double x1 = f == 0 ? d1[c] : vnew[0][c];
+        dl[c] = p.two ? (f == 0 ? d2[c] : vnew[1][c]) - x1 : -2.0 * x1;
+      }
+      double t0, t1, t2;
+      if (nd == 2) {
+        t0 = nx * dl[0] * b;
+        t1 = nz * dl[1] * b;
+        t2 = 0.5 * ((nx * dl[1] + nz * dl[0]) * b);
+      } else {
+        t0 = 0.5 * (nx * dl[0] * b);
+        t1 = 0.5 * (nz * dl[0] * b);
+        t2 = 0.0;
+      }
+      p.pot[(3 * f) * nf + k] = t0;
+      p.pot[(3 * f + 1) * nf + k] = t1;
+      p.pot[(3 * f + 2) * nf + k] = t2;
     }
   }
   fault_record(p, k, it);

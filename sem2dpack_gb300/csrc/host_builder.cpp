@@ -1327,6 +1327,7 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
     d->twf_L = dk.twf_L;
     d->twf_T = dk.twf_T;
     d->twf_Dc = dk.twf_Dc;
+    d->flt_potency = dk.flt_potency;
   }
   return SEM2D_OK;
 }

@@ -54,6 +54,8 @@ struct FaultParams {
   const double *fxz;    // (2,nflt) positions of the side-1 nodes
   // state
   double *D, *V, *T, *Tstick, *MU, *theta, *sigma;
+  // potency terms of this step per node pair, [q*nflt + k] (null: not kept)
+  double *pot;
   // outputs: series[(q + onx*(rec + 6*sample))]
   int oit, oitd, oix1, oixd, onx, nsamp;
   double *series;

@@ -82,6 +82,7 @@ struct sem2d_handle {
   int *rec_tile_start = nullptr, *rec_ids = nullptr, *rec_I = nullptr, *rec_J = nullptr;
   // fault
   int nflt = 0, two = 0, jf1 = -1, jf2 = -1, onx = 0, fnsamp = 0, friction = 0;
+  bool potency = false;              // fault potency recorded every step
   std::vector<double> h_fault_init;  // V0, theta for reset
   double *fd[64] = {nullptr};        // fault arrays, see enum below
   // time stepping
@@ -132,7 +133,7 @@ enum FaultArr {
   F_D64, F_V64, F_A64, F_RM, F_N1, F_B, F_INVM1, F_INVM2, F_Z, F_T0, F_COH,
   F_SWF_DC, F_SWF_MUS, F_SWF_MUD, F_SWF_P, F_SWF_ALPHA,
   F_RSF_DC, F_RSF_MUS, F_RSF_A, F_RSF_B, F_RSF_VSTAR, F_RSF_VC, F_RSF_TC, F_RSF_COEFT,
-  F_D, F_V, F_T, F_TSTICK, F_MU, F_THETA, F_SIGMA, F_SERIES, F_XZ, F_COUNT
+  F_D, F_V, F_T, F_TSTICK, F_MU, F_THETA, F_SIGMA, F_SERIES, F_XZ, F_POT, F_POTSERIES, F_COUNT
 };
 
 #define CK(call)                                                                       \
@@ -522,6 +523,10 @@ int upload_fault(sem2d_handle *h, const sem2d_problem_desc *d) {
   h->onx = (oixn - oix1) / oixd + 1;
   h->fnsamp = std::max(d->flt_nsamp, 0);
   if ((st = dalloc(h, &h->fd[F_SERIES], (size_t)h->onx * 6 * std::max(h->fnsamp, 1)))) return st;
+  h->potency = d->flt_potency != 0;
+  if (h->potency && ((st = dalloc(h, &h->fd[F_POT], (size_t)6 * nf)) ||
+                     (st = dalloc(h, &h->fd[F_POTSERIES], (size_t)6 * (std::max(d->nt, 0) + 1)))))
+    return st;
   std::vector<double> xz(2 * (size_t)nf);
   for (int k = 0; k < nf; ++k) {
     const int p = d->flt_node1[k] - 1;
@@ -610,6 +615,7 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.onx = h->onx;
   f.nsamp = h->fnsamp;
   f.series = h->fd[F_SERIES];
+  f.pot = h->potency ? h->fd[F_POT] : nullptr;
   f.scheme = h->scheme;
   f.dt = h->dt;
   f.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
@@ -713,6 +719,33 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   return bc;
 }
 
+// Sum of the potency terms of the fault node pairs of the step just
+// completed (step counter `step`) into row `it` of the potency series: one
+// block, a fixed summation order (strided partial sums, then a tree).
+__global__ void potency_kernel(const double *pot, int nflt, double *series, const int *step, int rows) {
+  __shared__ double part[6][256];
+  const int t = threadIdx.x;
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int k = t; k < nflt; k += 256)
+    for (int q = 0; q < 6; ++q) acc[q] += pot[(size_t)q * nflt + k];
+  for (int q = 0; q < 6; ++q) part[q][t] = acc[q];
+  __syncthreads();
+  for (int w = 128; w > 0; w >>= 1) {
+    if (t < w)
+      for (int q = 0; q < 6; ++q) part[q][t] += part[q][t + w];
+    __syncthreads();
+  }
+  const int it = *step;
+  if (t < 6 && it >= 0 && it < rows) series[(size_t)6 * it + t] = part[t][0];
+}
+
+int launch_potency(sem2d_handle *h, cudaStream_t s, const int *step) {
+  potency_kernel<<<1, 256, 0, s>>>(h->fd[F_POT], h->nflt, h->fd[F_POTSERIES], step, h->nt + 1);
+  CK(cudaGetLastError());
+  h->launches++;
+  return SEM2D_OK;
+}
+
 // one step of problem h: the march kernel when it covers the problem, else
 // the strip kernel; `receivers` false skips the in-kernel seismograms
 int launch_step_kernel(sem2d_handle *h, BulkConfig &bc, bool receivers) {
@@ -763,12 +796,14 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     f.step = h->d_step_c;
     if (launch_march_fault(bc)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
     h->launches += 3;
+    if (h->potency && launch_potency(h, h->stream, h->d_step_c)) return SEM2D_E_CUDA;
   } else {
     if (ev) CK(cudaEventRecord(ev[0], h->stream));
     if (launch_step_kernel(h, bc, rec))
       return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
     h->launches++;
     if (ev) CK(cudaEventRecord(ev[1], h->stream));
+    if (h->nflt && h->potency && launch_potency(h, h->stream, h->d_step)) return SEM2D_E_CUDA;
   }
   if (ev) CK(cudaEventRecord(ev[2], h->stream));
   if (h->nrec && h->rec_separate) {
@@ -863,6 +898,7 @@ int launch_steps_overlap(sem2d_handle *h, int n) {
     CK(cudaEventRecord(h->ev_c[q], F));
     f.step = h->d_step_c;
     if (launch_march_fault(bf)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
+    if (h->potency && launch_potency(h, F, h->d_step_c)) return SEM2D_E_CUDA;
     // M_k
     CK(cudaStreamWaitEvent(S, h->ev_c[q ^ 1], 0));
     MarchLaunch mm;
@@ -903,7 +939,7 @@ int launch_steps(sem2d_handle *h, int n) {
 
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
-  return 1 + (h->march && h->nflt ? 2 : 0) + (h->nrec && h->rec_separate ? 1 : 0);
+  return 1 + (h->march && h->nflt ? 2 : 0) + (h->nflt && h->potency ? 1 : 0) + (h->nrec && h->rec_separate ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -960,6 +996,7 @@ int reset_state(sem2d_handle *h) {
     CK(cudaMemcpyAsync(h->fd[F_THETA], h->h_fault_init.data() + nfd, sizeof(double) * h->nflt,
                        cudaMemcpyHostToDevice, h->stream));
     CK(cudaMemsetAsync(h->fd[F_SERIES], 0, sizeof(double) * (size_t)h->onx * 6 * std::max(h->fnsamp, 1), h->stream));
+    if (h->potency) CK(cudaMemsetAsync(h->fd[F_POTSERIES], 0, sizeof(double) * 6 * ((size_t)h->nt + 1), h->stream));
   }
   h->cur = 0;
   h->steps = 0;
@@ -1398,6 +1435,7 @@ int batch_close_impl(sem2d_handle *h) {
     if (m->nt != a->nt) return set_err(h, SEM2D_E_UNSUPPORTED, "batch members differ in the number of steps");
     if (m->nrec && m->rec_separate)
       return set_err(h, SEM2D_E_UNSUPPORTED, "interpolated velocity/acceleration receivers in a batch");
+    if (m->potency) return set_err(h, SEM2D_E_UNSUPPORTED, "fault potency records in a batch");
   }
   h->N = a->N;
   h->ndof = a->ndof;
@@ -1966,6 +2004,16 @@ int sem2d_gpu_get_fault(sem2d_handle *h, double *out) {
   if (st) return st;
   if (h->nflt && h->fnsamp > 0)
     CK(cudaMemcpy(out, h->fd[F_SERIES], sizeof(double) * (size_t)h->onx * 6 * h->fnsamp, cudaMemcpyDeviceToHost));
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_get_fault_potency(sem2d_handle *h, double *out) {
+  if (!h || !out) return SEM2D_E_ARG;
+  if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
+  if (!h->nflt || !h->potency) return set_err(h, SEM2D_E_STATE, "the handle does not record the fault potency");
+  int st = check_device_error(h);
+  if (st) return st;
+  CK(cudaMemcpy(out, h->fd[F_POTSERIES], sizeof(double) * 6 * ((size_t)h->nt + 1), cudaMemcpyDeviceToHost));
   return SEM2D_OK;
 }
 

@@ -74,6 +74,8 @@ class Fault:
     ot1: float = 0.0
     otd: float = 0.0
     oxi: Tuple[int, int, int] = (1, 0, 1)
+    # record the potency of displacement and velocity every step
+    potency: bool = False
     # name (abi.FP_NAMES) -> scalar, or an array over the fault nodes
     values: Dict[str, ArrayLike] = field(default_factory=dict)
 
@@ -202,6 +204,7 @@ class ParDeck:
             d.normal_kind = f.normal_kind
             d.normal_T, d.normal_L, d.normal_V = f.normal_T, f.normal_L, f.normal_V
             d.flt_opening = int(f.opening)
+            d.flt_potency = int(f.potency)
             d.flt_ot1, d.flt_otd = f.ot1, f.otd
             d.flt_oxi[:] = list(f.oxi)
             for name, val in f.values.items():
