@@ -273,6 +273,15 @@ int sem2d_gpu_get_fault(sem2d_handle *h, double *out);
  * zero. */
 int sem2d_gpu_get_fault_potency(sem2d_handle *h, double *out);
 
+/* Strain and stress at every element GLL point from the displacement that
+ * sem2d_gpu_get_fields returns, laid out e(ngll,ngll,ndof+1,nelem) in the
+ * reference's element order: MAT_strain_PSV/SH (mat_gen.f90:727-774) --
+ * P-SV e11, e22, e12; SH e13, e23 -- and MAT_ELAST_stress
+ * (mat_elastic.f90:804-862): P-SV sigma11, sigma22, sigma12 (isotropic or
+ * VTI), SH sigma13, sigma23.  Either pointer may be NULL.  Single problems
+ * (a batch member reads its own). */
+int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress);
+
 /* Current fault state D(nflt,ndof), V(nflt,ndof), T(nflt,2), MU(nflt),
  * state variable theta(nflt) (RSF, else zeros); any pointer may be NULL. */
 int sem2d_gpu_get_fault_state(sem2d_handle *h, double *D, double *V,

@@ -40,6 +40,8 @@ struct oc_sim {
   int *ibool;
   double *H;
   double *acoef; /* (ngll,ngll,nelast,nelem) */
+  double *dxidx, *detadz;      /* (ngll,ngll,nelem) inverse Jacobian (flat elements) */
+  double *mKx, *mKz, *mla, *mmu; /* (ngll,ngll,nelem) moduli for MAT_ELAST_stress */
   double *beta25; /* (ngll,ngll,nelem) 2.5D coefficients or NULL */
   double *kveta;
   double *rmass;
@@ -115,6 +117,12 @@ static void init_acoef(oc_sim *s, const sem2d_problem_desc *dd) {
   oc_gll_info(n, xg, wg, Hd);
   free(Hd);
   s->acoef = xcalloc((size_t)n * n * na * ne, sizeof(double));
+  s->dxidx = xcalloc((size_t)n * n * ne, sizeof(double));
+  s->detadz = xcalloc((size_t)n * n * ne, sizeof(double));
+  s->mKx = xcalloc((size_t)n * n * ne, sizeof(double));
+  s->mKz = xcalloc((size_t)n * n * ne, sizeof(double));
+  s->mla = xcalloc((size_t)n * n * ne, sizeof(double));
+  s->mmu = xcalloc((size_t)n * n * ne, sizeof(double));
   s->beta25 = dd->width > 0.0 ? xcalloc((size_t)n * n * ne, sizeof(double)) : NULL;
   for (int e = 0; e < ne; e++) {
     int cidx[4][2] = {{0, 0}, {n - 1, 0}, {n - 1, n - 1}, {0, n - 1}};
@@ -144,6 +152,12 @@ static void init_acoef(oc_sim *s, const sem2d_problem_desc *dd) {
         double *A = s->acoef + (size_t)n * n * na * e + i + n * j;
         size_t st = (size_t)n * n;
         double Kx = dd->Kx[p], Kz = dd->Kz[p], la = dd->la[p], mu = dd->mu[p], mux = dd->mux[p];
+        s->dxidx[p] = DxiDx;
+        s->detadz[p] = DetaDz;
+        s->mKx[p] = Kx;
+        s->mKz[p] = Kz;
+        s->mla[p] = la;
+        s->mmu[p] = mu;
         if (s->beta25) {
           /* MAT_ELAST_init_25D (mat_elastic.f90:363-383), dvol = w */
           double pw;
@@ -835,6 +849,11 @@ int oc_sim_run(oc_sim *s, int nsteps) {
 
 int oc_sim_step_count(const oc_sim *s) { return s->it; }
 
+/* test hook: overwrite the displacement field (npoin, ndof) */
+void oc_sim_set_displacement(oc_sim *s, const double *d) {
+  memcpy(s->d, d, (size_t)s->npoin * s->ndof * sizeof(double));
+}
+
 void oc_sim_fields(const oc_sim *s, double *d, double *v, double *a) {
   size_t nn = (size_t)s->npoin * s->ndof * sizeof(double);
   if (d) memcpy(d, s->d, nn);
@@ -848,6 +867,45 @@ void oc_sim_seismograms(const oc_sim *s, double *sis) {
 
 void oc_sim_fault_series(const oc_sim *s, double *out) {
   if (s->nflt) memcpy(out, s->fseries, (size_t)s->onx * 6 * s->fnsamp * sizeof(double));
+}
+
+/* MAT_strain_PSV/SH (mat_gen.f90:727-774) and MAT_ELAST_stress
+ * (mat_elastic.f90:804-862) of the current displacement at every element
+ * GLL point, e/sig(ngll,ngll,ndof+1,nelem); flat elements (dxi/dy =
+ * deta/dx = 0).  Isotropic: Kx = Kz = lambda + 2 mu. */
+void oc_sim_strain_stress(const oc_sim *s, double *eo, double *so) {
+  int n = s->ngll, n2 = n * n, nd = s->ndof, nc = nd + 1;
+  double Ht[400], dl[400], gx[400], ge[400];
+  for (int j = 0; j < n; j++)
+    for (int i = 0; i < n; i++) Ht[i + n * j] = s->H[j + n * i];
+  for (int e = 0; e < s->nelem; e++) {
+    double g[2][2][400];
+    for (int c = 0; c < nd; c++) {
+      for (int q = 0; q < n2; q++) dl[q] = s->d[(size_t)(s->ibool[q + (size_t)n2 * e] - 1) + (size_t)s->npoin * c];
+      mxm(Ht, dl, gx, n);
+      mxm(dl, s->H, ge, n);
+      memcpy(g[c][0], gx, sizeof(double) * n2);
+      memcpy(g[c][1], ge, sizeof(double) * n2);
+    }
+    for (int q = 0; q < n2; q++) {
+      size_t p = q + (size_t)n2 * e;
+      double *ev = eo + q + (size_t)n2 * nc * e, *sv = so + q + (size_t)n2 * nc * e;
+      double dx = s->dxidx[p], dz = s->detadz[p];
+      if (nd == 1) {
+        ev[0] = 0.5 * (g[0][0][q] * dx);
+        ev[n2] = 0.5 * (g[0][1][q] * dz);
+        sv[0] = 2.0 * s->mmu[p] * ev[0];
+        sv[n2] = 2.0 * s->mmu[p] * ev[n2];
+      } else {
+        ev[0] = g[0][0][q] * dx;
+        ev[n2] = g[1][1][q] * dz;
+        ev[2 * n2] = 0.5 * (g[0][1][q] * dz + g[1][0][q] * dx);
+        sv[0] = s->mKx[p] * ev[0] + s->mla[p] * ev[n2];
+        sv[n2] = s->mla[p] * ev[0] + s->mKz[p] * ev[n2];
+        sv[2 * n2] = 2.0 * s->mmu[p] * ev[2 * n2];
+      }
+    }
+  }
 }
 
 void oc_sim_fault_potency(const oc_sim *s, double *out) {
@@ -874,7 +932,8 @@ void oc_sim_free(oc_sim *s) {
                   s->swf_mus, s->swf_mud, s->swf_p, s->swf_alpha, s->theta, s->rsf_dc,
                   s->rsf_mus, s->rsf_a, s->rsf_b, s->rsf_vstar, s->rsf_vc, s->rsf_Tc,
                   s->rsf_coeft, s->D, s->V, s->T, s->Tstick, s->MU, s->sigma, s->fseries,
-                  s->d, s->v, s->a, s->beta25, s->fcoord, s->pseries};
+                  s->d, s->v, s->a, s->beta25, s->fcoord, s->pseries, s->dxidx, s->detadz,
+                  s->mKx, s->mKz, s->mla, s->mmu};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(s);
 }

@@ -47,6 +47,8 @@ def lib():
         L.oc_sim_seismograms.argtypes = [vp, dp]
         L.oc_sim_fault_series.argtypes = [vp, dp]
         L.oc_sim_fault_potency.argtypes = [vp, dp]
+        L.oc_sim_strain_stress.argtypes = [vp, dp, dp]
+        L.oc_sim_set_displacement.argtypes = [vp, dp]
         L.oc_sim_fault_state.argtypes = [vp, dp, dp, dp, dp, dp]
         L.oc_sim_free.argtypes = [vp]
         L.oc_gll_info.argtypes = [C.c_int, dp, dp, dp]
@@ -177,6 +179,17 @@ class OracleSim:
         a = np.zeros(max(onx * 6 * d.flt_nsamp, 1))
         lib().oc_sim_fault_series(self.h, _p(a))
         return a[: onx * 6 * d.flt_nsamp].reshape(onx, 6, d.flt_nsamp, order="F")
+
+    def set_displacement(self, d):
+        a = np.asfortranarray(d, dtype=np.float64).reshape(-1, order="F")
+        lib().oc_sim_set_displacement(self.h, _p(a))
+
+    def strain_stress(self):
+        d = self.desc
+        sh = (d.ngll, d.ngll, d.ndof + 1, d.nelem)
+        e, s = np.zeros(int(np.prod(sh))), np.zeros(int(np.prod(sh)))
+        lib().oc_sim_strain_stress(self.h, _p(e), _p(s))
+        return e.reshape(sh, order="F"), s.reshape(sh, order="F")
 
     def fault_potency(self):
         """(nt+1, 2, 3): potency of displacement and velocity at every step."""

@@ -61,6 +61,10 @@ void oc_sim_seismograms(const oc_sim *s, double *sis);
 void oc_sim_fault_series(const oc_sim *s, double *out);
 /* [6*it + q], it = 0..nt: fault potency of d (q = 0..2) and v (q = 3..5) */
 void oc_sim_fault_potency(const oc_sim *s, double *out);
+/* strain and stress e/sig(ngll,ngll,ndof+1,nelem) of the current displacement */
+void oc_sim_strain_stress(const oc_sim *s, double *strain, double *stress);
+/* test hook: overwrite the displacement field d(npoin, ndof) */
+void oc_sim_set_displacement(oc_sim *s, const double *d);
 void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T,
                         double *MU, double *theta);
 void oc_sim_free(oc_sim *s);

@@ -35,6 +35,7 @@ PROTOTYPES = [
     ("sem2d_gpu_get_seismograms", C.c_int, [vp, dp]),
     ("sem2d_gpu_get_fault", C.c_int, [vp, dp]),
     ("sem2d_gpu_get_fault_potency", C.c_int, [vp, dp]),
+    ("sem2d_gpu_get_strain_stress", C.c_int, [vp, dp, dp]),
     ("sem2d_gpu_get_fault_state", C.c_int, [vp, dp, dp, dp, dp, dp]),
     ("sem2d_gpu_reset", C.c_int, [vp]),
     ("sem2d_gpu_kernel_launches", C.c_longlong, [vp]),

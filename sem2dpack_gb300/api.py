@@ -226,6 +226,16 @@ class Solver:
         self._check(lib().sem2d_gpu_get_fault(self.h, _p(a)))
         return a[:n].reshape(onx, 6, d.flt_nsamp, order="F")
 
+    def strain_stress(self):
+        """(strain, stress), each (ngll, ngll, ndof+1, nelem) in the
+        reference's element order, from the current displacement."""
+        d = self.desc
+        n = d.ngll * d.ngll * (d.ndof + 1) * d.nelem
+        e, s = np.zeros(n), np.zeros(n)
+        self._check(lib().sem2d_gpu_get_strain_stress(self.h, _p(e), _p(s)))
+        sh = (d.ngll, d.ngll, d.ndof + 1, d.nelem)
+        return e.reshape(sh, order="F"), s.reshape(sh, order="F")
+
     def fault_potency(self):
         """(nt+1, 2, 3): potency of the displacement and of the velocity after
         every step (a handle created with desc.flt_potency = 1)."""

@@ -1521,6 +1521,73 @@ int batch_close_impl(sem2d_handle *h) {
 
 }  // namespace
 
+namespace sem2d_detail {
+// Strain and stress at the element GLL points (MAT_strain_PSV/SH,
+// mat_gen.f90:727-774; MAT_ELAST_stress, mat_elastic.f90:804-862) on the
+// rectilinear lattice: dxi/dy = deta/dx = 0, so e11 = dUx/dxi dxi/dx,
+// e22 = dUz/deta deta/dz, e12 = (dUx/deta deta/dz + dUz/dxi dxi/dx)/2
+// (SH: e13 = dU/dxi dxi/dx / 2, e23 = dU/deta deta/dz / 2).  One thread per
+// element point; out[((ez*nx + ex)*N*N + i + N*j)*(ndof+1) + c].
+template <typename real>
+__global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int nz, int pitch, long long plane,
+                                     const int *row0, const real *xix, const real *etaz, const double *H,
+                                     int mat_elem, int iso, const real *m0, const real *m1, const real *m2,
+                                     const real *m3, double *eo, double *so) {
+  const long long npt = (long long)nx * nz * N * N;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < npt;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int pt = int(q % (N * N));
+    const long long el = q / (N * N);
+    const int i = pt % N, j = pt / N, ex = int(el % nx), ez = int(el / nx);
+    const long long base = (long long)row0[ez] * pitch + (long long)ex * (N - 1);
+    const double dxi = double(xix[ex]), deta = double(etaz[ez]);
+    double gx[2] = {0, 0}, ge[2] = {0, 0};
+    for (int c = 0; c < ndof; ++c) {
+      const real *u = D + c * plane + base;
+      double a = H[0 + N * i] * double(u[(long long)j * pitch + 0]);
+      for (int k = 1; k < N; ++k) a = a + H[k + N * i] * double(u[(long long)j * pitch + k]);
+      double b = double(u[(long long)0 * pitch + i]) * H[0 + N * j];
+      for (int k = 1; k < N; ++k) b = b + double(u[(long long)k * pitch + i]) * H[k + N * j];
+      gx[c] = a;
+      ge[c] = b;
+    }
+    auto mat = [&](const real *m) -> double {
+      if (!m) return 0.0;
+      if (mat_elem == kMatElement) return double(m[el]);
+      if (mat_elem == kMatPoint) return double(m[el * N * N + pt]);
+      return double(m[base + (long long)j * pitch + i]);
+    };
+    double *e = eo + q * (ndof + 1), *s = so + q * (ndof + 1);
+    if (ndof == 1) {
+      const double mu = mat(m0);  // SH: mu (the reference has no anisotropic SH stress)
+      e[0] = 0.5 * (gx[0] * dxi);
+      e[1] = 0.5 * (ge[0] * deta);
+      s[0] = 2.0 * mu * e[0];
+      s[1] = 2.0 * mu * e[1];
+    } else {
+      double Kx, Kz, la, mu;
+      if (iso) {
+        la = mat(m0);
+        mu = mat(m1);
+        Kx = la + 2.0 * mu;
+        Kz = Kx;
+      } else {
+        Kx = mat(m0);
+        Kz = mat(m1);
+        la = mat(m2);
+        mu = mat(m3);
+      }
+      e[0] = gx[0] * dxi;
+      e[1] = ge[1] * deta;
+      e[2] = 0.5 * (ge[0] * deta + gx[1] * dxi);
+      s[0] = Kx * e[0] + la * e[1];
+      s[1] = la * e[0] + Kz * e[1];
+      s[2] = 2.0 * mu * e[2];
+    }
+  }
+}
+}  // namespace sem2d_detail
+
 extern "C" {
 
 int sem2d_gpu_version(void) { return SEM2D_GPU_ABI_VERSION; }
@@ -1983,6 +2050,54 @@ int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc, double *
     }
     for (int c = 0; c < h->ndof; ++c)
       for (int p = 0; p < h->npoin; ++p) dst[k][p + (size_t)h->npoin * c] = tmp[c * h->plane + h->glob2lat[p]];
+  }
+  return SEM2D_OK;
+}
+
+
+int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress) {
+  if (!h) return SEM2D_E_ARG;
+  if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
+  if (h->elem_ex.empty()) return set_err(h, SEM2D_E_STATE, "element numbering not kept (batch member)");
+  int st = check_device_error(h);
+  if (st) return st;
+  const int N = h->N, NN = N * N, nc = h->ndof + 1;
+  const long long npt = (long long)h->nx * h->nz * NN;
+  double *dev = nullptr, *dH = nullptr;
+  CK(cudaMalloc(&dev, sizeof(double) * (size_t)npt * nc * 2));
+  if (cudaMalloc(&dH, sizeof(double) * NN) != cudaSuccess) {
+    cudaFree(dev);
+    return set_err(h, SEM2D_E_NOMEM, "cudaMalloc");
+  }
+  cudaMemcpy(dH, h->H.data(), sizeof(double) * NN, cudaMemcpyHostToDevice);
+  const void *D = h->steps > 0 ? h->D[1 - h->cur] : h->D[h->cur];
+  const int blocks = int(std::min<long long>((npt + 255) / 256, 4096));
+  if (h->mixed)
+    sem2d_detail::strain_stress_kernel<float><<<blocks, 256, 0, h->stream>>>(
+        (const float *)D, h->ndof, N, h->nx, h->nz, h->pitch, h->plane, h->d_row0, (const float *)h->geo[0],
+        (const float *)h->geo[1], dH, h->mat_elem, h->mat_iso, (const float *)h->mat[0], (const float *)h->mat[1],
+        (const float *)h->mat[2], (const float *)h->mat[3], dev, dev + npt * nc);
+  else
+    sem2d_detail::strain_stress_kernel<double><<<blocks, 256, 0, h->stream>>>(
+        (const double *)D, h->ndof, N, h->nx, h->nz, h->pitch, h->plane, h->d_row0, (const double *)h->geo[0],
+        (const double *)h->geo[1], dH, h->mat_elem, h->mat_iso, (const double *)h->mat[0],
+        (const double *)h->mat[1], (const double *)h->mat[2], (const double *)h->mat[3], dev, dev + npt * nc);
+  std::vector<double> host((size_t)npt * nc * 2);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), dev, sizeof(double) * host.size(), cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(dev);
+  cudaFree(dH);
+  if (e != cudaSuccess) return set_err(h, SEM2D_E_CUDA, std::string("strain/stress: ") + cudaGetErrorString(e));
+  // lattice element (ex, ez) -> the reference's element e
+  for (int el = 0; el < h->nelem; ++el) {
+    const long long L = (long long)h->elem_ez[el] * h->nx + h->elem_ex[el];
+    for (int pt = 0; pt < NN; ++pt)
+      for (int c = 0; c < nc; ++c) {
+        const size_t src = ((size_t)L * NN + pt) * nc + c, dst = pt + (size_t)NN * (c + (size_t)nc * el);
+        if (strain) strain[dst] = host[src];
+        if (stress) stress[dst] = host[(size_t)npt * nc + src];
+      }
   }
   return SEM2D_OK;
 }
