@@ -175,6 +175,31 @@ int launch_march(const BulkConfig &c, const MarchLaunch &m);
 int launch_march_batch(const BulkConfig &c, const MarchLaunch &m);
 // the fault node pairs of a march step (one thread per pair, after the step)
 int launch_march_fault(const BulkConfig &c);
+// one reverse step of the adjoint with the march kernels (FP32, NGLL=5,
+// isotropic node material): the forces pass, then the moduli pass
+struct MarchAdjConfig {
+  int ndof = 0, LX = 0, LZ = 0, pitch = 0, nx = 0, nz = 0;
+  long long plane = 0;
+  const int *row0 = nullptr;
+  const double *H = nullptr, *w = nullptr;
+  const void *geo[4] = {nullptr, nullptr, nullptr, nullptr};
+  const void *mat[2] = {nullptr, nullptr};
+  const void *rmass = nullptr, *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
+  const void *Db = nullptr, *Vb = nullptr;
+  void *Dbn = nullptr, *Vbn = nullptr;
+  const void *d = nullptr, *vprev = nullptr, *a = nullptr;
+  void *g_la = nullptr, *g_mu = nullptr, *g_M = nullptr, *g_C = nullptr;
+  int nrec = 0, nsamp = 0, isamp = 1;
+  char field = 'V';
+  const int *rec_I = nullptr, *rec_row = nullptr, *rec_ids_row = nullptr;
+  const double *resid = nullptr;
+  double dt = 0;
+  int kd2 = 0, it = 0;
+  const void *units = nullptr;
+  int nunits = 0;
+  cudaStream_t stream = nullptr;
+};
+int launch_march_adjoint(const MarchAdjConfig &c);
 // resident warps per SM of the march kernel for the configuration
 int march_warps_per_sm(const BulkConfig &c);
 

@@ -5,6 +5,7 @@
 
 #include "bulk_inst.cuh"
 #include "bulk_launch.h"
+#include "march_adjoint.cuh"
 #include "march_kernel.cuh"
 
 namespace sem2d {
@@ -82,6 +83,66 @@ int launch_march_fault(const BulkConfig &c) {
   // one warp per block: the node pairs spread over the SMs (the FP64 pipe
   // of an SM is shared by its warps)
   march_fault_kernel<<<(f.nflt + 31) / 32, 32, 0, c.stream>>>(f, static_cast<const float *>(c.fault_force));
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_bulk_err = cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
+}
+
+int launch_march_adjoint(const MarchAdjConfig &c) {
+  MarchAdjParams p{};
+  p.LX = c.LX;
+  p.LZ = c.LZ;
+  p.pitch = c.pitch;
+  p.plane = c.plane;
+  p.nx = c.nx;
+  p.nz = c.nz;
+  p.row0 = c.row0;
+  for (int k = 0; k < 25; ++k) p.H[k] = float(c.H[k]);
+  for (int k = 0; k < 5; ++k) p.w[k] = float(c.w[k]);
+  p.xix = static_cast<const float *>(c.geo[0]);
+  p.etaz = static_cast<const float *>(c.geo[1]);
+  p.dxdxi = static_cast<const float *>(c.geo[2]);
+  p.dzdeta = static_cast<const float *>(c.geo[3]);
+  p.mat[0] = static_cast<const float *>(c.mat[0]);
+  p.mat[1] = static_cast<const float *>(c.mat[1]);
+  p.rmass = static_cast<const float *>(c.rmass);
+  p.per_rm = static_cast<const float *>(c.per_rm);
+  p.per_Ca = static_cast<const float *>(c.per_Ca);
+  p.per_Cb = static_cast<const float *>(c.per_Cb);
+  p.Db = static_cast<const float *>(c.Db);
+  p.Vb = static_cast<const float *>(c.Vb);
+  p.Dbn = static_cast<float *>(c.Dbn);
+  p.Vbn = static_cast<float *>(c.Vbn);
+  p.d = static_cast<const float *>(c.d);
+  p.vprev = static_cast<const float *>(c.vprev);
+  p.a = static_cast<const float *>(c.a);
+  p.g_la = static_cast<float *>(c.g_la);
+  p.g_mu = static_cast<float *>(c.g_mu);
+  p.g_M = static_cast<float *>(c.g_M);
+  p.g_C = static_cast<float *>(c.g_C);
+  p.nrec = c.nrec;
+  p.nsamp = c.nsamp;
+  p.isamp = c.isamp > 0 ? c.isamp : 1;
+  p.field = c.field;
+  p.rec_I = c.rec_I;
+  p.rec_row = c.rec_row;
+  p.rec_ids_row = c.rec_ids_row;
+  p.resid = c.resid;
+  p.dt = float(c.dt);
+  p.kd2 = c.kd2;
+  p.it = c.it;
+  const MarchUnit *u = static_cast<const MarchUnit *>(c.units);
+  const int grid = std::max(1, (c.nunits + kMarchWarps - 1) / kMarchWarps);
+  if (c.ndof == 1) {
+    adj_march_forces<1><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
+    adj_march_moduli<1><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
+  } else {
+    adj_march_forces<2><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
+    adj_march_moduli<2><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
+  }
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);

@@ -1872,6 +1872,62 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
     release();
     return set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
   }
+  // the march passes find the receivers of a lattice row through a CSR index
+  MarchAdjConfig mc;
+  if (h->march) {
+    std::vector<int> rI(std::max(h->nrec, 1)), rJ(std::max(h->nrec, 1));
+    if (h->nrec) {
+      CK(cudaMemcpy(rI.data(), h->rec_I, sizeof(int) * h->nrec, cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(rJ.data(), h->rec_J, sizeof(int) * h->nrec, cudaMemcpyDeviceToHost));
+    }
+    std::vector<int> row(h->LZ + 1, 0), ids(std::max(h->nrec, 1));
+    for (int r = 0; r < h->nrec; ++r) row[rJ[r] + 1]++;
+    for (int J = 0; J < h->LZ; ++J) row[J + 1] += row[J];
+    std::vector<int> fill(row.begin(), row.end() - 1);
+    for (int r = 0; r < h->nrec; ++r) ids[fill[rJ[r]]++] = r;
+    int *d_row = (int *)alloc(sizeof(int) * row.size()), *d_ids = (int *)alloc(sizeof(int) * ids.size());
+    if (!d_row || !d_ids) {
+      release();
+      return set_err(h, SEM2D_E_NOMEM, "no device memory for the adjoint");
+    }
+    CK(cudaMemcpyAsync(d_row, row.data(), sizeof(int) * row.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaMemcpyAsync(d_ids, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, h->stream));
+    CK(cudaStreamSynchronize(h->stream));
+    mc.ndof = nd;
+    mc.LX = h->LX;
+    mc.LZ = h->LZ;
+    mc.pitch = h->pitch;
+    mc.nx = h->nx;
+    mc.nz = h->nz;
+    mc.plane = h->plane;
+    mc.row0 = h->d_row0;
+    mc.H = h->H.data();
+    mc.w = h->w.data();
+    for (int q = 0; q < 4; ++q) mc.geo[q] = h->geo[q];
+    mc.mat[0] = h->mat[0];
+    mc.mat[1] = nd == 2 ? h->mat[1] : nullptr;
+    mc.rmass = h->rmass;
+    mc.per_rm = h->per_rm;
+    mc.per_Ca = h->per_Ca;
+    mc.per_Cb = h->per_Cb;
+    mc.g_la = g_la;
+    mc.g_mu = g_mu;
+    mc.g_M = g_M;
+    mc.g_C = g_C;
+    mc.nrec = h->nrec;
+    mc.nsamp = h->rec_nsamp;
+    mc.isamp = h->rec_isamp;
+    mc.field = h->rec_field;
+    mc.rec_I = h->rec_I;
+    mc.rec_row = d_row;
+    mc.rec_ids_row = d_ids;
+    mc.resid = d_resid;
+    mc.dt = h->dt;
+    mc.kd2 = h->kd2;
+    mc.units = h->d_march_units;
+    mc.nunits = h->march_nunits;
+    mc.stream = h->stream;
+  }
   int ca = 0;
   const int nseg = (h->nt + k - 1) / k;
   for (int seg = nseg - 1; seg >= 0 && !st; --seg) {
@@ -1917,8 +1973,21 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
       ac.vprev = RV[j - 1];
       ac.a = RA[j];
       ac.it = n;
-      if (launch_adjoint(ac)) st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
-      h->launches++;
+      if (h->march) {
+        mc.Db = ac.Db;
+        mc.Vb = ac.Vb;
+        mc.Dbn = ac.Dbn;
+        mc.Vbn = ac.Vbn;
+        mc.d = ac.d;
+        mc.vprev = ac.vprev;
+        mc.a = ac.a;
+        mc.it = n;
+        if (launch_march_adjoint(mc)) st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
+        h->launches += 2;
+      } else {
+        if (launch_adjoint(ac)) st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
+        h->launches++;
+      }
       ca = 1 - ca;
     }
     if (!st && (launch_fold(g_la, a_la, h->plane, h->mixed, h->stream) ||

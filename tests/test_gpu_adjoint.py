@@ -127,3 +127,21 @@ def test_adjoint_32x32_matches_autograd():
     assert J == pytest.approx(Jt, rel=1e-10)
     for g, t in ((gr, tr), (gp, tp), (gs, ts)):
         assert rel(g, t) <= 1e-8
+
+
+@pytest.mark.parametrize("ndof", [1, 2])
+def test_adjoint_march_matches_strip_kernels(ndof, monkeypatch):
+    """FP32: the march passes (one element per thread) against the strip
+    adjoint kernel, and both against the FP64 autograd reference."""
+    m, start, obs = case(ndof)
+    J1, s1, *g1 = forward_and_gradient(m, *start, obs=obs, checkpoint_every=16, precision=PRECISION_MIXED)
+    monkeypatch.setenv("SEM2D_MARCH", "0")
+    J2, s2, *g2 = forward_and_gradient(m, *start, obs=obs, checkpoint_every=16, precision=PRECISION_MIXED)
+    monkeypatch.delenv("SEM2D_MARCH")
+    assert J1 == pytest.approx(J2, rel=1e-5)
+    Jt, sist, *gt = ac.torch_misfit_grad(m, *start, obs)
+    for a, b, t in zip(g1, g2, gt):
+        if ndof == 1 and not np.any(t):
+            continue  # SH has no vp gradient
+        assert rel(a, b) <= 1e-4
+        assert rel(a, t) <= 1e-3
