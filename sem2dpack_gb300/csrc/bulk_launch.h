@@ -162,6 +162,7 @@ int launch_batch_n9(const BulkConfig &c, const BatchLaunch &b);
 // Units are MarchUnit records {problem, strip, z0, z1, rec0, rec1}.
 constexpr int kMarchColsHost = 31;   // element columns owned by one unit
 constexpr int kMarchUnitInts = 6;    // ints per unit record
+constexpr int kMarchWarpsHost = 4;   // warps per CTA of the march kernels
 struct MarchLaunch {
   const void *units = nullptr;  // [nunits] unit records
   int nunits = 0;
@@ -175,6 +176,9 @@ int launch_march(const BulkConfig &c, const MarchLaunch &m);
 int launch_march_batch(const BulkConfig &c, const MarchLaunch &m);
 // the fault node pairs of a march step (one thread per pair, after the step)
 int launch_march_fault(const BulkConfig &c);
+// the fault-side units of a march step and the fault node pairs in one
+// launch (a CTA per strip; nrows fault-side units per strip, at most 4)
+int launch_march_fault_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows);
 // one reverse step of the adjoint with the march kernels (FP32, NGLL=5,
 // isotropic node material): the forces pass, then the moduli pass
 struct MarchAdjConfig {

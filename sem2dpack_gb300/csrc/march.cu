@@ -15,6 +15,7 @@ extern thread_local std::string g_bulk_err;
 namespace {
 
 constexpr int kThreads = 32 * kMarchWarps;
+static_assert(kMarchWarpsHost == kMarchWarps, "host and device CTA shapes");
 
 template <int NDOF, int MAT>
 int launch_one(const BulkConfig &c, const MarchLaunch &m) {
@@ -76,6 +77,25 @@ int launch_march_batch(const BulkConfig &c, const MarchLaunch &m) {
   if (c.ndof == 1)
     return c.mat_elem == kMatNode ? launch_many<1, kMatNode>(c, m) : launch_many<1, kMatElement>(c, m);
   return c.mat_elem == kMatNode ? launch_many<2, kMatNode>(c, m) : launch_many<2, kMatElement>(c, m);
+}
+
+int launch_march_fault_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
+  BulkParams<float, 5> p;
+  fill_params<float, 5>(c, p);
+  const MarchUnit *u = static_cast<const MarchUnit *>(m.units);
+  if (c.ndof == 1) {
+    if (c.mat_elem == kMatNode) march_fault_side_kernel<1, kMatNode><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
+    else march_fault_side_kernel<1, kMatElement><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
+  } else {
+    if (c.mat_elem == kMatNode) march_fault_side_kernel<2, kMatNode><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
+    else march_fault_side_kernel<2, kMatElement><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_bulk_err = cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
 }
 
 int launch_march_fault(const BulkConfig &c) {

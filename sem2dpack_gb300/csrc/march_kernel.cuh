@@ -500,6 +500,34 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   march_done(b.step, b.done, it);
 }
 
+// The fault side of a step in one launch (slip- or time-weakening
+// friction): CTA s runs the fault-side units of strip s (unit w*nstrips + s
+// on warp w, w < nrows), then its threads finish the strip's fault node
+// pairs (columns 124 s .. 124 s + 123, and the last column on the last
+// strip) from the forces its warps wrote; the last CTA bumps the counter.
+template <int NDOF, int MAT>
+__global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
+    march_fault_side_kernel(const __grid_constant__ BulkParams<float, 5> p, const MarchUnit *units, int nstrips,
+                            int nrows) {
+  const int warp = threadIdx.x >> 5, s = blockIdx.x;
+  const int it = *p.step + 1;
+  if (warp < nrows) march_unit<NDOF, MAT>(p, p.H, p.w, units[warp * nstrips + s], it);
+  __syncthreads();  // the strip's fault-row forces are written (global memory, this block)
+  const int t = threadIdx.x, I = 4 * kMarchCols * s + t;
+  const bool mine = (t < 4 * kMarchCols && I < p.LX) || (t == 4 * kMarchCols && I == p.LX - 1);
+  if (mine) {
+    const float *ff = p.fault_force;
+    const int nf = p.flt.nflt;
+    double f1[2] = {0, 0}, f2[2] = {0, 0};
+    for (int c = 0; c < NDOF; ++c) {
+      f1[c] = double(ff[(0 * NDOF + c) * nf + I]);
+      if (p.flt.two) f2[c] = double(ff[(1 * NDOF + c) * nf + I]);
+    }
+    fault_node_update(p.flt, I, it, f1, f2);
+  }
+  march_done(p.step, p.done, it);
+}
+
 // the fault node pairs of the step the march kernel just completed
 __global__ void march_fault_kernel(const __grid_constant__ FaultParams<float> p, const float *ff) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;

@@ -112,6 +112,11 @@ struct sem2d_handle {
   // fault chunk and the fault kernel run on fstream, overlapping the next
   // step's other units (march_overlap)
   int march_fault_units = 0;
+  // slip/time weakening: the fault-side units and the fault node pairs in
+  // one launch (a CTA per strip); rate-and-state keeps the separate fault
+  // kernel, whose Newton solves want one warp per SM
+  bool march_fused = false;
+  int march_nstrips = 0, march_nfch = 0;
   int *d_step_c = nullptr;
   unsigned *d_done_c = nullptr;
   bool march_overlap = false;
@@ -786,7 +791,13 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     MarchLaunch mf;
     mf.units = h->d_march_units;
     mf.nunits = h->march_fault_units;
-    if (launch_march(bf, mf)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    if (h->march_fused) {
+      f.step = h->d_step_c;
+      if (launch_march_fault_side(bf, mf, h->march_nstrips, h->march_nfch))
+        return set_err(h, SEM2D_E_CUDA, std::string("fault side launch: ") + bulk_last_error());
+    } else if (launch_march(bf, mf)) {
+      return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+    }
     if (ev) CK(cudaEventRecord(ev[0], h->stream));
     MarchLaunch mm;
     mm.units = static_cast<const int *>(h->d_march_units) + kMarchUnitInts * h->march_fault_units;
@@ -794,8 +805,9 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     if (launch_march(bc, mm)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
     if (ev) CK(cudaEventRecord(ev[1], h->stream));
     f.step = h->d_step_c;
-    if (launch_march_fault(bc)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
-    h->launches += 3;
+    if (!h->march_fused && launch_march_fault(bc))
+      return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
+    h->launches += h->march_fused ? 2 : 3;
     if (h->potency && launch_potency(h, h->stream, h->d_step_c)) return SEM2D_E_CUDA;
   } else {
     if (ev) CK(cudaEventRecord(ev[0], h->stream));
@@ -894,10 +906,16 @@ int launch_steps_overlap(sem2d_handle *h, int n) {
     MarchLaunch mf;
     mf.units = h->d_march_units;
     mf.nunits = h->march_fault_units;
-    if (launch_march(bf, mf)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
-    CK(cudaEventRecord(h->ev_c[q], F));
     f.step = h->d_step_c;
-    if (launch_march_fault(bf)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
+    if (h->march_fused) {
+      if (launch_march_fault_side(bf, mf, h->march_nstrips, h->march_nfch))
+        return set_err(h, SEM2D_E_CUDA, std::string("fault side launch: ") + bulk_last_error());
+      CK(cudaEventRecord(h->ev_c[q], F));
+    } else {
+      if (launch_march(bf, mf)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
+      CK(cudaEventRecord(h->ev_c[q], F));
+      if (launch_march_fault(bf)) return set_err(h, SEM2D_E_CUDA, std::string("fault launch: ") + bulk_last_error());
+    }
     if (h->potency && launch_potency(h, F, h->d_step_c)) return SEM2D_E_CUDA;
     // M_k
     CK(cudaStreamWaitEvent(S, h->ev_c[q ^ 1], 0));
@@ -906,7 +924,7 @@ int launch_steps_overlap(sem2d_handle *h, int n) {
     mm.nunits = h->march_nunits - h->march_fault_units;
     if (launch_march(bc, mm)) return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
     CK(cudaEventRecord(h->ev_m[q], S));
-    h->launches += 3;
+    h->launches += h->march_fused ? 2 : 3;
     h->cur = 1 - h->cur;
     h->steps++;
   }
@@ -939,7 +957,8 @@ int launch_steps(sem2d_handle *h, int n) {
 
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
-  return 1 + (h->march && h->nflt ? 2 : 0) + (h->nflt && h->potency ? 1 : 0) + (h->nrec && h->rec_separate ? 1 : 0);
+  return 1 + (h->march && h->nflt ? (h->march_fused ? 1 : 2) : 0) + (h->nflt && h->potency ? 1 : 0) +
+         (h->nrec && h->rec_separate ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -1143,6 +1162,10 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   h->march = true;
   if (nfch > 0) {
     h->march_fault_units = nfch * nstrips;
+    h->march_nstrips = nstrips;
+    h->march_nfch = nfch;
+    const char *fu = std::getenv("SEM2D_FUSED_FAULT");
+    h->march_fused = nfch <= kMarchWarpsHost && h->friction != SEM2D_FRICTION_RSF && !(fu && std::atoi(fu) == 0);
     if ((st = dalloc(h, &h->d_step_c, 1)) || (st = dalloc(h, &h->d_done_c, 1))) return st;
     const char *ov = std::getenv("SEM2D_OVERLAP");
     h->march_overlap = !h->rec_separate && !(ov && std::atoi(ov) == 0);

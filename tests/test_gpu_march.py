@@ -122,3 +122,19 @@ def test_march_receivers(field, atnode, monkeypatch):
     assert rel_l2(g.seismograms(), o.seismograms()) <= 1e-4
     # interpolated velocity is sampled by the separate kernel after the step
     assert g.launches == 150 * (2 if (field != "D" and not atnode) else 1)
+
+
+def test_fused_fault_side_equals_separate_kernels(monkeypatch):
+    """Slip weakening: the fault-side units and the fault update in one
+    launch give the same bits as the two separate launches."""
+    build, nt = CASES["sh_rupture"]
+    case = build()
+    P, d, g = make(case, monkeypatch)
+    _, _, h = make(case, monkeypatch, {"SEM2D_FUSED_FAULT": 0})
+    lg, lh = g.launches, h.launches
+    g.step(nt)
+    h.step(nt)
+    assert g.launches - lg == 2 * nt and h.launches - lh == 3 * nt
+    a, b = outputs(g, True), outputs(h, True)
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
