@@ -1,0 +1,165 @@
+"""Output files in the reference's formats, so that its readers (the
+JUPYTER/POST scripts of SEM2DPACK, Seismic Unix) read a GPU run unchanged.
+
+  seismograms   Ux_sem2d.dat, Uz_sem2d.dat (P-SV) or Uy_sem2d.dat (SH):
+                direct-access FP32, record k = the nsamp samples of
+                receiver k (REC_write, receivers.f90:351-392);
+                SeisHeader_sem2d.hdr: 'DT NSAMP NSTA', values, 'XSTA ZSTA',
+                one coordinate pair per receiver (REC_init, receivers.f90:
+                212-221)
+  fault         FltXX_sem2d.dat: Fortran unformatted sequential, per output
+                time 6 records of NPTS FP32 values (slip, slip rate, shear
+                and normal stress, friction coefficient, T_stick), each
+                record framed by its 4-byte byte count (BC_DYNFLT_write,
+                bc_dynflt.f90:751-778); FltXX_sem2d.hdr (NPTS NDAT NSAMP
+                DELT, field names, node coordinates) and FltXX_sem2d.csh
+                (bc_dynflt.f90:455-518)
+  potency       FltXX_potency_sem2d.tab: one line per step, 6D24.16 (P-SV:
+                potency of d then v, 3 values each; SH: 2 each)
+                (bc_dynflt.f90:436,757)
+  fault init    FltXX_init_sem2d.tab: T0 shear, T0 normal, mu, B per output
+                node (bc_dynflt.f90:446-452)
+
+Values are written little-endian, as the reference built with gfortran on
+x86 or Arm writes them.
+"""
+import os
+
+import numpy as np
+
+__all__ = ["write_seismograms", "read_seismograms", "write_fault", "read_fault", "write_potency", "write_run",
+           "write_fault_init"]
+
+
+def _fmt_list(*vals):
+    """Fortran list-directed style line: values separated by blanks."""
+    out = []
+    for v in vals:
+        if isinstance(v, (int, np.integer)):
+            out.append("%12d" % int(v))
+        else:
+            out.append("%25.16E" % float(v))
+    return " " + " ".join(out)
+
+
+def write_seismograms(path, sis, tsamp, coords):
+    """sis (nsamp, nrec, ndof) as Solver.seismograms() returns it; tsamp the
+    sampling interval (isamp * dt); coords (2, nrec) receiver positions."""
+    sis = np.asarray(sis)
+    nsamp, nrec, ndof = sis.shape
+    os.makedirs(path, exist_ok=True)
+    names = ["Uy"] if ndof == 1 else ["Ux", "Uz"]
+    for c, name in enumerate(names):
+        data = np.ascontiguousarray(sis[:, :, c].T, dtype="<f4")  # record k = receiver k
+        data.tofile(os.path.join(path, name + "_sem2d.dat"))
+    with open(os.path.join(path, "SeisHeader_sem2d.hdr"), "w") as f:
+        f.write(" DT NSAMP NSTA\n")
+        f.write(_fmt_list(np.float32(tsamp), nsamp, nrec) + "\n")
+        f.write(" XSTA ZSTA\n")
+        for k in range(nrec):
+            f.write(_fmt_list(coords[0][k], coords[1][k]) + "\n")
+
+
+def read_seismograms(path, ndof):
+    """(sis (nsamp, nrec, ndof), tsamp, coords (2, nrec)) from a folder
+    written by the reference or by write_seismograms."""
+    with open(os.path.join(path, "SeisHeader_sem2d.hdr")) as f:
+        lines = f.read().split("\n")
+    dt, nsamp, nrec = lines[1].split()
+    nsamp, nrec = int(nsamp), int(nrec)
+    coords = np.array([[float(v) for v in lines[3 + k].split()] for k in range(nrec)]).T
+    names = ["Uy"] if ndof == 1 else ["Ux", "Uz"]
+    sis = np.zeros((nsamp, nrec, ndof))
+    for c, name in enumerate(names):
+        a = np.fromfile(os.path.join(path, name + "_sem2d.dat"), dtype="<f4")
+        sis[:, :, c] = a.reshape(nrec, nsamp).T
+    return sis, float(dt), coords
+
+
+def _record(f, values):
+    data = np.ascontiguousarray(values, dtype="<f4").tobytes()
+    n = np.array([len(data)], dtype="<i4").tobytes()
+    f.write(n + data + n)
+
+
+FAULT_FIELDS = "Slip:Slip_Rate:Shear_Stress:Normal_Stress:Friction:T_stick"
+
+
+def write_fault(path, tag, series, odt, coords):
+    """series (onx, 6, nsamp) as Solver.fault_series() returns it; odt the
+    output interval (oitd * dt); coords (2, onx) of the output nodes."""
+    series = np.asarray(series)
+    onx, ndat, nsamp = series.shape
+    os.makedirs(path, exist_ok=True)
+    name = os.path.join(path, "Flt%02d_sem2d" % int(tag))
+    with open(name + ".dat", "wb") as f:
+        for s in range(nsamp):
+            for q in range(ndat):
+                _record(f, series[:, q, s])
+    with open(name + ".hdr", "w") as f:
+        f.write(" NPTS NDAT NSAMP DELT\n")
+        f.write(_fmt_list(onx, ndat, nsamp, odt) + "\n")
+        f.write(" " + FAULT_FIELDS + "\n")
+        f.write(" XPTS ZPTS\n")
+        for k in range(onx):
+            f.write(_fmt_list(coords[0][k], coords[1][k]) + "\n")
+    base = os.path.basename(name)
+    with open(name + ".csh", "w") as f:
+        f.write(" #!/bin/csh -f\n")
+        f.write(" #USAGE: %s.csh node field\n" % base)
+        f.write(" @ ifs = $2 - 1\n")
+        f.write("subset <%s.dat n1=%d n2=%d n3=%d ix1s=$1 ix2s=$ifs | b2a n1=1 > %s.$1.$ifs.tab\n"
+                % (base, onx + 2, ndat, nsamp, base))
+
+
+def read_fault(path, tag):
+    """(series (onx, ndat, nsamp), odt, coords (2, onx)) of FltXX_sem2d.*"""
+    name = os.path.join(path, "Flt%02d_sem2d" % int(tag))
+    with open(name + ".hdr") as f:
+        lines = f.read().split("\n")
+    onx, ndat, nsamp, odt = lines[1].split()
+    onx, ndat, nsamp = int(onx), int(ndat), int(nsamp)
+    coords = np.array([[float(v) for v in lines[4 + k].split()] for k in range(onx)]).T
+    raw = np.fromfile(name + ".dat", dtype="<f4").reshape(nsamp, ndat, onx + 2)
+    head = raw[:, :, 0].view("<i4")
+    if np.any(head != 4 * onx):
+        raise ValueError("record markers do not match NPTS")
+    return np.transpose(raw[:, :, 1:-1], (2, 1, 0)).astype(np.float64), float(odt), coords
+
+
+def write_potency(path, tag, potency, ndof):
+    """potency (nt+1, 2, 3) as Solver.fault_potency() returns it."""
+    os.makedirs(path, exist_ok=True)
+    k = 3 if ndof == 2 else 2
+    with open(os.path.join(path, "Flt%02d_potency_sem2d.tab" % int(tag)), "w") as f:
+        for row in np.asarray(potency):
+            vals = list(row[0][:k]) + list(row[1][:k])
+            f.write("".join(("%24.16E" % v).replace("E", "D") for v in vals) + "\n")
+
+
+def write_fault_init(path, tag, T0, mu, B):
+    """T0 (onx, 2) initial shear and normal stress, mu (onx) initial friction
+    coefficient, B (onx) boundary weights of the output nodes."""
+    os.makedirs(path, exist_ok=True)
+    with open(os.path.join(path, "Flt%02d_init_sem2d.tab" % int(tag)), "w") as f:
+        for k in range(len(mu)):
+            f.write(_fmt_list(T0[k][0], T0[k][1], mu[k], B[k]) + "\n")
+
+
+def write_run(path, solver, problem):
+    """Every output file of a run the reference would have written for its
+    deck: seismograms, and for a fault its records (and the potency when the
+    handle keeps it).  `solver` a Solver (or an oracle run with the same
+    getters), `problem` the Problem it was created from."""
+    d = solver.desc
+    if d.nrec:
+        write_seismograms(path, solver.seismograms(), d.rec_isamp * d.dt, problem.rec_coord())
+    if d.nflt:
+        tag = problem.deck.fault.tags[0] if problem.deck.fault is not None else 5
+        xz = problem.fault_coord()
+        series = solver.fault_series()
+        if xz.shape[1] != series.shape[0]:
+            xz = xz[:, (d.flt_oix1 - 1):d.flt_oixn:d.flt_oixd]
+        write_fault(path, tag, series, d.flt_oitd * d.dt, xz)
+        if getattr(d, "flt_potency", 0):
+            write_potency(path, tag, solver.fault_potency(), d.ndof)

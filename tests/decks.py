@@ -62,5 +62,6 @@ def inabox():
         materials=[Material(tag=1, rho=2400.0, cp=3800.0, cs=2000.0)],
         absorbing=[1, 2, 3, 4],
         time=Time(kind="newmark", total_time=2.0, courant=0.3, beta=0.0, gamma=0.5),
-        sources=Sources(coords=[(0.0, 0.0)], f0=1.0, onset=1.0, ampli=1.0),
+        sources=Sources(coords=[(0.0, 0.0)], f0=5.0, onset=0.4, ampli=1.0, angle=0.0),
+        receivers=Receivers(number=21, first=(-500.0, -1000.0), last=(-500.0, 1000.0), field="V"),
     )

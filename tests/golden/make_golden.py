@@ -14,6 +14,8 @@ It reads the reference's own test data (nothing is written from memory):
   EXAMPLES/Anisotropic/p{1..4}.tab            reference output at stations
                                               4, 18, 23, 46 (Anisotropic/write_seis.m)
   EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
+  EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox}/Par.inp
+                                              the input decks, as text (parinp_*)
 and writes golden.npz.  The GPU machine and the test suite only read the npz.
 """
 import os
@@ -47,6 +49,9 @@ def main(ref):
     out["inabox_nelem"] = np.array(int(re.search(r"Total number of elements[ .]*= *(\d+)", info).group(1)))
     out["inabox_dt"] = np.array(float(re.search(r"Time step \(secs\) *= *([0-9.E+\-]+)", info).group(1)))
     out["inabox_nt"] = np.array(int(re.search(r"Number of time steps *= *(\d+)", info).group(1)))
+
+    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox"):
+        out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
 
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
     np.savez_compressed(dst, **out)

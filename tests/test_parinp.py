@@ -1,0 +1,144 @@
+"""Par.inp front end (sem2dpack_gb300.parinp) and the reference-format
+output writers (sem2dpack_gb300.outputs), on the CPU.
+
+The reference's own example decks (text fixtures from
+tests/golden/make_golden.py) parse to the decks tests/decks.py restates by
+hand; the writers' files read back bit-for-bit in the layout the
+reference's readers expect (direct-access FP32 traces, Fortran sequential
+records with 4-byte markers)."""
+import os
+
+import numpy as np
+import pytest
+
+import decks
+from oracle import pyoracle as po
+from sem2dpack_gb300 import PRECISION_FP64, Problem, workloads
+from sem2dpack_gb300 import outputs
+from sem2dpack_gb300.parinp import deck_from_parinp, read_namelists
+
+EXAMPLES = {"LambsProblem": decks.lambs_problem, "TestSH": decks.test_sh,
+            "Anisotropic": decks.anisotropic, "InaBox": decks.inabox}
+
+
+def same_deck(a, b):
+    for f in ("ngll", "ndof", "fmax", "xlim", "zlim", "nelem", "absorbing", "domains", "materials",
+              "ezflt", "width"):
+        assert getattr(a, f) == getattr(b, f), f
+    assert vars(a.time) == vars(b.time)
+    for f in ("sources", "receivers"):
+        x, y = getattr(a, f), getattr(b, f)
+        assert (x is None) == (y is None), f
+        if x is not None:
+            assert vars(x) == vars(y), f
+
+
+@pytest.mark.parametrize("name", list(EXAMPLES))
+def test_example_decks_parse_to_the_restated_decks(name, golden):
+    d = deck_from_parinp(str(golden["parinp_" + name]))
+    same_deck(d, EXAMPLES[name]())
+    assert all(s.startswith(("SNAP", "SRC_")) for s in d.skipped)
+
+
+def test_example_deck_builds_the_same_problem(golden):
+    pa, pb = Problem(deck_from_parinp(str(golden["parinp_TestSH"]))), Problem(decks.test_sh())
+    a, b = pa.desc(), pb.desc()  # the descriptors point into the problems' arrays
+    assert (a.nelem, a.npoin, a.nt, a.dt) == (b.nelem, b.npoin, b.nt, b.dt)
+    n = a.npoin
+    assert np.array_equal(np.ctypeslib.as_array(a.rmass, shape=(n,)), np.ctypeslib.as_array(b.rmass, shape=(n,)))
+
+
+def test_namelist_reader():
+    text = """
+    # comment &NOT_A_BLOCK x=1 /
+    &ONE a=1.5d3, b = -2.d-1 , s='x/y' , t=T, f=.false., v=1,2,3, r=3*0.5 / trailing, k='ignored' /
+    &TWO name = "q" ! comment
+         n=4 /
+    """
+    b = read_namelists(text)
+    assert [n for n, _ in b] == ["ONE", "TWO"]
+    one = b[0][1]
+    assert one == {"a": 1500.0, "b": -0.2, "s": "x/y", "t": True, "f": False, "v": [1, 2, 3],
+                   "r": [0.5, 0.5, 0.5]}
+    assert b[1][1] == {"name": "q", "n": 4}
+
+
+@pytest.mark.parametrize("bad", [
+    "&MESH_DEF method='MESH2D' /",
+    "&BC_DEF tag=1, kind='ABSORB' / &BC_ABSORB stacey=T /",
+    "&TIME kind='hhta' /",
+    "&SRC_DEF stf='RICKER', coord=0,0, mechanism='WAVE' /",
+    "&MATERIAL tag=1, kind='PLAST' /",
+    "&BC_DEF tags=5,6, kind='DYNFLT' / &BC_DYNFLT TtH='PWCONR' /",
+    "&BC_DEF tags=5,6, kind='DYNFLT' / &BC_DYNFLT_SWF MuSH='LINEAR' /",
+])
+def test_off_path_blocks_are_refused(bad):
+    with pytest.raises(ValueError):
+        deck_from_parinp(bad)
+
+
+FAULT_PARINP = """
+&GENERAL ngll=5, fmax=10d0, ndof=1 /
+&MESH_DEF method='CARTESIAN' /
+&MESH_CART xlim=0d0,4d3, zlim=0d0,2d3, nelem=40,20, ezflt=-1 /
+&MATERIAL tag=1, kind='ELAST' /
+&MAT_ELASTIC rho=2670d0, cp=6000d0, cs=3464d0 /
+&BC_DEF tags=5,6, kind='DYNFLT' /
+&BC_DYNFLT friction='SWF', Tn=-120d6, Tt=70d6, otd=0.01d0 /
+&BC_DYNFLT_SWF Dc=0.4d0, MuS=0.677d0, MuD=0.525d0 /
+&BC_DEF tag=1, kind='ABSORB' /
+&BC_DEF tag=3, kind='ABSORB' /
+&TIME TotalTime=0.2d0, courant=0.5d0 /
+&REC_LINE number=5, first=500d0,1500d0, last=3500d0,1500d0 /
+"""
+
+
+def test_fault_deck():
+    d = deck_from_parinp(FAULT_PARINP)
+    assert d.fault is not None and d.fault.friction == "SWF" and d.fault_first
+    assert d.fault.values == {"Tn": -120e6, "Tt": 70e6, "swf_dc": 0.4, "swf_mus": 0.677, "swf_mud": 0.525}
+    assert d.fault.otd == 0.01 and d.absorbing == [1, 3] and d.ezflt == -1
+    P = Problem(d)
+    desc = P.desc()
+    assert desc.nflt == 4 * 40 + 1 and desc.flt_node2
+
+
+def test_seismogram_files_round_trip(tmp_path):
+    P = Problem(workloads.plain_psv(scale=0.05, nsteps=40))
+    d = P.desc()
+    d.precision = PRECISION_FP64
+    o = po.OracleSim(d, owner=P)
+    o.run(40)
+    sis = o.seismograms()
+    coords = P.rec_coord()
+    outputs.write_seismograms(str(tmp_path), sis, d.rec_isamp * d.dt, coords)
+    assert os.path.getsize(tmp_path / "Ux_sem2d.dat") == 4 * sis.shape[0] * sis.shape[1]
+    back, tsamp, xz = outputs.read_seismograms(str(tmp_path), 2)
+    assert np.array_equal(back, sis.astype(np.float32))
+    assert tsamp == pytest.approx(d.rec_isamp * d.dt, rel=1e-6)
+    np.testing.assert_allclose(xz, coords, rtol=1e-15)
+    # record k holds receiver k's samples (the reference's direct access)
+    raw = np.fromfile(tmp_path / "Uz_sem2d.dat", dtype="<f4").reshape(sis.shape[1], sis.shape[0])
+    assert np.array_equal(raw[3], sis[:, 3, 1].astype(np.float32))
+
+
+def test_fault_files_round_trip(tmp_path):
+    P = Problem(deck_from_parinp(FAULT_PARINP))
+    d = P.desc()
+    o = po.OracleSim(d, owner=P)
+    o.run(60)
+    series = o.fault_series()
+    xz = P.fault_coord()
+    onx = series.shape[0]
+    cxz = xz[:, (d.flt_oix1 - 1):(d.flt_oixn):d.flt_oixd] if xz.shape[1] != onx else xz
+    outputs.write_fault(str(tmp_path), 5, series, d.flt_oitd * d.dt, cxz)
+    back, odt, bxz = outputs.read_fault(str(tmp_path), 5)
+    assert np.array_equal(back, series.astype(np.float32))
+    assert odt == pytest.approx(d.flt_oitd * d.dt, rel=1e-12)
+    assert (tmp_path / "Flt05_sem2d.csh").exists()
+    pot = o.fault_potency()
+    outputs.write_potency(str(tmp_path), 5, pot, 1)
+    lines = open(tmp_path / "Flt05_potency_sem2d.tab").read().splitlines()
+    assert len(lines) == d.nt + 1 and len(lines[0]) == 4 * 24
+    v = [float(x.replace("D", "E")) for x in lines[40].split()]
+    np.testing.assert_allclose(v, [pot[40, 0, 0], pot[40, 0, 1], pot[40, 1, 0], pot[40, 1, 1]], rtol=1e-15)
