@@ -72,6 +72,7 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.cv = real(c.cv);
   p.cpred = real(c.cpred);
   p.cd2 = real(c.cd2);
+  p.cb = real(c.cb);
   p.kd2 = c.kd2;
   p.nmat = c.nmat;
   p.has_kv = c.has_kv;

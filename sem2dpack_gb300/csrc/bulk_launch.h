@@ -47,7 +47,7 @@ struct BulkConfig {
   const double *rec_w = nullptr;
   double *sis = nullptr;
   int scheme = 0, kd2 = 0;
-  double dt = 0, cv = 0, cpred = 0, cd2 = 0;
+  double dt = 0, cv = 0, cpred = 0, cd2 = 0, cb = 0;
   double width = 0;  // 2.5D seismogenic width, 0 = 2D
   int *error = nullptr;  // device error flag
   int chunk_shift = 0;   // chunk scheduled first (the fault's)

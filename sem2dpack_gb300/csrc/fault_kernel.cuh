@@ -352,21 +352,25 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     p.D[k + nf * c] = dD[c] + p.coefA2D * dAc;
     p.V[k + nf * c] = dV[c] + p.coefA2V * dAc;
   }
-  double vnew[2][2] = {{0, 0}, {0, 0}};
+  double vnew[2][2] = {{0, 0}, {0, 0}}, dcor[2][2] = {{0, 0}, {0, 0}};
   for (int side = 0; side < 1 + p.two; ++side) {
     const int J = side == 0 ? p.jf1 : p.jf2;
     for (int c = 0; c < nd; ++c) {
       const int o = (side * nd + c) * nf + k;
       const double f = side == 0 ? f1[c] + p.B[k] * Tx[c] : f2[c] - p.B[k] * Tx[c];
       const double vp = side == 0 ? v1[c] : v2[c];
-      const double dc = side == 0 ? d1[c] : d2[c];
+      double dc = side == 0 ? d1[c] : d2[c];
       const double a = p.rm[o] * f;
       const double vn = vp + p.cv * a;
+      // Newmark corrector d += beta dt^2 a (solver.f90:82) before the next
+      // step's predictor
+      if (p.scheme == 1 && p.cb != 0.0) dc = dc + p.cb * a;
       const double dn = p.scheme == 1 ? (dc + p.dt * vn) + p.cd2 * a : dc + p.dt * vn;
       p.d64[o] = dn;
       p.v64[o] = vn;
       p.a64[o] = a;
       vnew[side][c] = vn;
+      dcor[side][c] = dc;
       const long long g = c * p.plane + (long long)J * p.pitch + k;
       p.Dnext[g] = real(dn);
       p.Vnext[g] = real(vn);
@@ -381,8 +385,8 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     for (int f = 0; f < 2; ++f) {
       double dl[2] = {0, 0};
       for (int c = 0; c < nd; ++c) {
-        const double x1 = f == 0 ? d1[c] : vnew[0][c];
-        dl[c] = p.two ? (f == 0 ? d2[c] : vnew[1][c]) - x1 : -2.0 * x1;
+        const double x1 = f == 0 ? dcor[0][c] : vnew[0][c];
+        dl[c] = p.two ? (f == 0 ? dcor[1][c] : vnew[1][c]) - x1 : -2.0 * x1;
       }
       double t0, t1, t2;
       if (nd == 2) {
@@ -402,7 +406,8 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
   fault_record(p, k, it);
 }
 
-// interpolated seismograms of velocity or acceleration (REC_store,
+// interpolated seismograms of velocity or acceleration, and of displacement
+// under the Newmark corrector (REC_store,
 // receivers.f90:309-344), after the bulk kernel moved the step counter
 template <typename real>
 __global__ void receiver_kernel(RecParams<real> p) {
@@ -414,14 +419,16 @@ __global__ void receiver_kernel(RecParams<real> p) {
   if (q >= p.nrec * p.ndof) return;
   const int r = q % p.nrec, c = q / p.nrec;
   const real *f = p.field + c * p.plane;
+  const real *ac = p.acc ? p.acc + c * p.plane : nullptr;
+  auto at = [&](int l) { return ac ? double(f[l] + p.cb * ac[l]) : double(f[l]); };
   double val;
   if (p.npts == 1) {
-    val = double(f[p.lat[r]]);
+    val = at(p.lat[r]);
   } else {
     const int *L = p.lat + (size_t)r * p.npts;
     const double *W = p.w + (size_t)r * p.npts;
-    val = W[0] * double(f[L[0]]);
-    for (int k = 1; k < p.npts; ++k) val = val + W[k] * double(f[L[k]]);
+    val = W[0] * at(L[0]);
+    for (int k = 1; k < p.npts; ++k) val = val + W[k] * at(L[k]);
   }
   p.sis[s + (size_t)p.nsamp * (r + (size_t)p.nrec * c)] = val;
 }

@@ -62,6 +62,7 @@ struct FaultParams {
   // time scheme
   int scheme;
   double dt, cv, cpred, cd2;
+  double cb;            // Newmark corrector beta dt^2
   int *step;            // incremented by the last block (stand-alone kernel)
   unsigned int *done;   // block completion counter (reset by the last block)
   int *error;           // sticky device error flag (SEM2D_E_*)
@@ -125,6 +126,7 @@ struct BulkParams {
   // time scheme
   int scheme;             // 0 leapfrog, 1 Newmark (beta = 0)
   real dt, cv, cpred, cd2;// cv: coef a->v, cpred: (1-gamma)dt, cd2: (0.5-beta)dt^2
+  real cb;                // Newmark corrector beta dt^2 (0: leapfrog or beta = 0)
   int kd2;
   real width;             // 2.5D seismogenic width W, 0 for a 2D problem
   int nmat;               // material planes (node layout) or arrays (element layout)
@@ -153,6 +155,8 @@ struct RecParams {
   const int *lat;       // [r*npts + q] lattice offset J*pitch+I
   const double *w;      // [r*npts + q] weights (1 at node)
   const real *field;
+  const real *acc;      // displacement with the Newmark corrector: field + cb * acc
+  real cb;
   double *sis;          // sis(nsamp,nrec,ndof)
   const int *step;
 };

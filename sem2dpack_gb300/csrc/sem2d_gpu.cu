@@ -626,6 +626,7 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
   f.cpred = (1.0 - h->gamma) * h->dt;
   f.cd2 = (0.5 - h->beta) * h->dt * h->dt;
+  f.cb = h->scheme == 1 ? h->beta * h->dt * h->dt : 0.0;
   f.step = h->d_step;
   f.done = h->d_done;
   f.error = h->d_error;
@@ -714,6 +715,7 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
   bc.cpred = (1.0 - h->gamma) * h->dt;
   bc.cd2 = (0.5 - h->beta) * h->dt * h->dt;
+  bc.cb = h->scheme == 1 ? h->beta * h->dt * h->dt : 0.0;
   bc.kd2 = h->kd2;
   bc.width = h->width;
   bc.chunk_shift = h->fault_chunk;
@@ -828,8 +830,14 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     r.plane = h->plane;
     r.lat = h->rec_lat;
     r.w = h->rec_w;
-    // after the step: velocity and acceleration are the buffers just written
-    r.field = (const real *)(h->rec_field == 'A' ? h->A[1 - cur] : h->V[1 - cur]);
+    // after the step: velocity and acceleration are the buffers just written;
+    // displacement is the step's predictor plus beta dt^2 times the new
+    // acceleration (solver.f90:82)
+    r.field = (const real *)(h->rec_field == 'A' ? h->A[1 - cur] : h->rec_field == 'V' ? h->V[1 - cur] : h->D[cur]);
+    if (h->rec_field == 'D') {
+      r.acc = (const real *)h->A[1 - cur];
+      r.cb = real(h->beta * h->dt * h->dt);
+    }
     r.sis = h->sis;
     r.step = h->d_step;
     const int nthr = h->nrec * h->ndof;
@@ -1070,10 +1078,13 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   int st;
   if (h->nflt) {
     // the fault kernel finishes the fault rows after the step: velocity or
-    // acceleration receivers there are sampled after it, by the receiver
+    // acceleration receivers there, and displacement ones when the Newmark
+    // corrector adds beta dt^2 a, are sampled after it, by the receiver
     // kernel
+    const bool corrected = h->scheme == 1 && h->beta != 0.0;
     for (size_t r = 0; r < rec_jn.size(); ++r)
-      if (h->rec_field != 'D' && (rec_jn[r] == h->jf1 || rec_jn[r] == h->jf2)) h->rec_separate = true;
+      if ((h->rec_field != 'D' || corrected) && (rec_jn[r] == h->jf1 || rec_jn[r] == h->jf2))
+        h->rec_separate = true;
     if ((st = dalloc(h, &h->d_fault_force, (size_t)2 * h->ndof * h->nflt))) return st;
   }
   const int nstrips = (h->nx + kMarchColsHost - 1) / kMarchColsHost;
@@ -1190,8 +1201,6 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
       !d->Kx || !d->Kz || !d->la || !d->mu || !d->mux)
     return set_err(h, SEM2D_E_ARG, "incomplete descriptor");
   if (!(d->dt > 0) || d->nt < 0) return set_err(h, SEM2D_E_ARG, "bad time step settings");
-  if (d->time_scheme == SEM2D_TIME_NEWMARK && d->beta != 0.0)
-    return set_err(h, SEM2D_E_UNSUPPORTED, "Newmark with beta != 0 is not supported on the GPU path");
   if (d->precision != SEM2D_PRECISION_FP64 && d->precision != SEM2D_PRECISION_MIXED)
     return set_err(h, SEM2D_E_ARG, "unknown precision");
   h->N = d->ngll;
@@ -1297,10 +1306,11 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     if (!d->rec_node && (!d->rec_elem || !d->rec_interp))
       return set_err(h, SEM2D_E_ARG, "receivers need nodes or interpolation");
     h->rec_npts = d->rec_node ? 1 : h->N * h->N;
-    // interpolated velocity/acceleration reads nodes owned by several CTAs:
-    // sampled by a separate kernel after the step; everything else is
-    // sampled inside the bulk kernel by the CTA that owns the receiver
-    h->rec_separate = !d->rec_node && h->rec_field != 'D';
+    // interpolated velocity/acceleration (and displacement with the Newmark
+    // corrector, which needs the new accelerations) reads nodes owned by
+    // several CTAs: sampled by a separate kernel after the step; everything
+    // else is sampled inside the bulk kernel by the CTA that owns the receiver
+    h->rec_separate = !d->rec_node && (h->rec_field != 'D' || (h->scheme == 1 && h->beta != 0.0));
   }
   if ((st = dalloc(h, &h->sis, (size_t)std::max(h->rec_nsamp, 1) * std::max(h->nrec, 1) * h->ndof))) return st;
   std::vector<int> rec_ex, rec_ez, rec_jn;  // element owning each receiver (march units), node row
@@ -1608,6 +1618,14 @@ __global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int
       s[2] = 2.0 * mu * e[2];
     }
   }
+}
+
+// out = d + cb a over n values: the Newmark corrector of the displacement
+// (solver.f90:82) for the outputs read between steps
+template <typename real>
+__global__ void corrector_kernel(real *out, const real *d, const real *a, real cb, long long n) {
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x)
+    out[q] = d[q] + cb * a[q];
 }
 }  // namespace sem2d_detail
 
@@ -2143,6 +2161,22 @@ int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc, double *
     for (int c = 0; c < h->ndof; ++c)
       for (int p = 0; p < h->npoin; ++p) dst[k][p + (size_t)h->npoin * c] = tmp[c * h->plane + h->glob2lat[p]];
   }
+  if (displ && h->steps > 0 && h->scheme == 1 && h->beta != 0.0) {
+    // the buffer holds the step's predictor: add the corrector beta dt^2 a^n
+    // (solver.f90:82)
+    const double cb = h->beta * h->dt * h->dt;
+    if (h->mixed) {
+      CK(cudaMemcpy(tmpf.data(), h->A[h->cur], n * sizeof(float), cudaMemcpyDeviceToHost));
+      for (size_t q = 0; q < n; ++q) tmp[q] = tmpf[q];
+    } else {
+      CK(cudaMemcpy(tmp.data(), h->A[h->cur], n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    for (int c = 0; c < h->ndof; ++c)
+      for (int p = 0; p < h->npoin; ++p) {
+        double &x = displ[p + (size_t)h->npoin * c];
+        x = x + cb * tmp[c * h->plane + h->glob2lat[p]];
+      }
+  }
   return SEM2D_OK;
 }
 
@@ -2163,6 +2197,25 @@ int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress)
   }
   cudaMemcpy(dH, h->H.data(), sizeof(double) * NN, cudaMemcpyHostToDevice);
   const void *D = h->steps > 0 ? h->D[1 - h->cur] : h->D[h->cur];
+  void *Dc = nullptr;
+  if (h->steps > 0 && h->scheme == 1 && h->beta != 0.0) {
+    // displacement d^n = the step's predictor + beta dt^2 a^n (solver.f90:82)
+    const long long n = (long long)h->plane * h->ndof;
+    const double cb = h->beta * h->dt * h->dt;
+    if (cudaMalloc(&Dc, (h->mixed ? sizeof(float) : sizeof(double)) * (size_t)n) != cudaSuccess) {
+      cudaFree(dev);
+      cudaFree(dH);
+      return set_err(h, SEM2D_E_NOMEM, "cudaMalloc");
+    }
+    const int b = int(std::min<long long>((n + 255) / 256, 4096));
+    if (h->mixed)
+      sem2d_detail::corrector_kernel<float><<<b, 256, 0, h->stream>>>((float *)Dc, (const float *)D,
+                                                                     (const float *)h->A[h->cur], float(cb), n);
+    else
+      sem2d_detail::corrector_kernel<double><<<b, 256, 0, h->stream>>>((double *)Dc, (const double *)D,
+                                                                      (const double *)h->A[h->cur], cb, n);
+    D = Dc;
+  }
   const int blocks = int(std::min<long long>((npt + 255) / 256, 4096));
   if (h->mixed)
     sem2d_detail::strain_stress_kernel<float><<<blocks, 256, 0, h->stream>>>(
@@ -2180,6 +2233,7 @@ int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress)
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
   cudaFree(dev);
   cudaFree(dH);
+  if (Dc) cudaFree(Dc);
   if (e != cudaSuccess) return set_err(h, SEM2D_E_CUDA, std::string("strain/stress: ") + cudaGetErrorString(e));
   // lattice element (ex, ez) -> the reference's element e
   for (int el = 0; el < h->nelem; ++el) {

@@ -624,7 +624,10 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           }
           const real a = rm * fc;
           const real vnew = vp + p.cv * a;
-          const real dcur = sD[c * PS + sidx];
+          real dcur = sD[c * PS + sidx];
+          // Newmark corrector d += beta dt^2 a (solver.f90:81-82), then the
+          // next step's predictor d + dt v + (1/2 - beta) dt^2 a (:59)
+          if (newmark && p.cb != real(0)) dcur = dcur + p.cb * a;
           const real dnext = newmark ? (dcur + p.dt * vnew) + p.cd2 * a : dcur + p.dt * vnew;
           p.Vnext[c * p.plane + g] = vnew;
           p.Dnext[c * p.plane + g] = dnext;
@@ -659,7 +662,12 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           const int I = p.rec_I[r], J = p.rec_J[r];
           const int jj = J - Jlo;
           if (jj < 0 || jj >= nr || s_stat[jj] != 1) continue;
-          val = p.rec_field == 'D' ? double(sD[c * PS + jj * TWp + xo + (I - Ia)])
+          // displacement after the step: the predictor plus the corrector
+          val = p.rec_field == 'D'
+                    ? (newmark && p.cb != real(0)
+                           ? double(sD[c * PS + jj * TWp + xo + (I - Ia)] +
+                                    p.cb * p.Anext[c * p.plane + (long long)J * p.pitch + I])
+                           : double(sD[c * PS + jj * TWp + xo + (I - Ia)]))
                 : p.rec_field == 'V' ? double(p.Vnext[c * p.plane + (long long)J * p.pitch + I])
                                      : double(p.Anext[c * p.plane + (long long)J * p.pitch + I]);
         } else {  // interpolated displacement over an element of this batch

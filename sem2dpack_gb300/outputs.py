@@ -19,6 +19,13 @@ JUPYTER/POST scripts of SEM2DPACK, Seismic Unix) read a GPU run unchanged.
                 (bc_dynflt.f90:436,757)
   fault init    FltXX_init_sem2d.tab: T0 shear, T0 normal, mu, B per output
                 node (bc_dynflt.f90:446-452)
+  grid          grid_sem2d.hdr: 'NELEM  NPGEO  NGNOD  NPOIN  NGLL', values
+                (SE_init, spec_grid.f90:136-141); ibool_sem2d.dat: direct
+                access, record e = the NGLL x NGLL global node numbers of
+                element e, int32, 1-based (SE_init_numbering,
+                spec_grid.f90:298-307); coord_sem2d.dat: direct access,
+                record i = (x, z) of node i in FP32 (SE_init_coord,
+                spec_grid.f90:363-371)
 
 Values are written little-endian, as the reference built with gfortran on
 x86 or Arm writes them.
@@ -28,7 +35,7 @@ import os
 import numpy as np
 
 __all__ = ["write_seismograms", "read_seismograms", "write_fault", "read_fault", "write_potency", "write_run",
-           "write_fault_init"]
+           "write_fault_init", "write_grid", "read_grid"]
 
 
 def _fmt_list(*vals):
@@ -146,12 +153,45 @@ def write_fault_init(path, tag, T0, mu, B):
             f.write(_fmt_list(T0[k][0], T0[k][1], mu[k], B[k]) + "\n")
 
 
+def write_grid(path, grid):
+    """grid_sem2d.hdr, ibool_sem2d.dat and coord_sem2d.dat of a Grid.  The
+    Cartesian mesher's geometric nodes are the (nx+1) x (nz+1) element
+    corners, one row more when a fault splits the mesh (nzp,
+    mesh_cartesian.f90:233-240), 4 per element."""
+    os.makedirs(path, exist_ok=True)
+    deck = grid.deck
+    nx, nz = deck.nelem
+    split = deck.ezflt > 0 or (deck.ezflt == -1 and nz // 2 > 0)
+    npgeo = (nx + 1) * (nz + (2 if split else 1))
+    with open(os.path.join(path, "grid_sem2d.hdr"), "w") as f:
+        f.write(" NELEM  NPGEO  NGNOD  NPOIN  NGLL\n")
+        f.write(_fmt_list(grid.nelem, npgeo, 4, grid.npoin, grid.ngll) + "\n")
+    ib = grid.ibool()  # (ngll, ngll, nelem), 1-based
+    np.ascontiguousarray(np.transpose(ib, (2, 1, 0)), dtype="<i4").tofile(os.path.join(path, "ibool_sem2d.dat"))
+    xz = grid.coord()  # (2, npoin)
+    np.ascontiguousarray(xz.T, dtype="<f4").tofile(os.path.join(path, "coord_sem2d.dat"))
+
+
+def read_grid(path):
+    """(sizes dict, ibool (ngll, ngll, nelem) 1-based, coord (2, npoin)
+    FP32) from grid_sem2d.hdr / ibool_sem2d.dat / coord_sem2d.dat."""
+    with open(os.path.join(path, "grid_sem2d.hdr")) as f:
+        lines = f.read().split("\n")
+    keys = lines[0].split()
+    sizes = dict(zip(keys, (int(v) for v in lines[1].split())))
+    n, ne, npn = sizes["NGLL"], sizes["NELEM"], sizes["NPOIN"]
+    ib = np.fromfile(os.path.join(path, "ibool_sem2d.dat"), dtype="<i4").reshape(ne, n, n)
+    xz = np.fromfile(os.path.join(path, "coord_sem2d.dat"), dtype="<f4").reshape(npn, 2)
+    return sizes, np.transpose(ib, (2, 1, 0)), xz.T
+
+
 def write_run(path, solver, problem):
     """Every output file of a run the reference would have written for its
-    deck: seismograms, and for a fault its records (and the potency when the
-    handle keeps it).  `solver` a Solver (or an oracle run with the same
+    deck: the grid files, seismograms, and for a fault its records (and the
+    potency when the handle keeps it).  `solver` a Solver (or an oracle run with the same
     getters), `problem` the Problem it was created from."""
     d = solver.desc
+    write_grid(path, problem.grid)
     if d.nrec:
         write_seismograms(path, solver.seismograms(), d.rec_isamp * d.dt, problem.rec_coord())
     if d.nflt:

@@ -65,7 +65,7 @@ def test_namelist_reader():
 
 @pytest.mark.parametrize("bad", [
     "&MESH_DEF method='MESH2D' /",
-    "&BC_DEF tag=1, kind='ABSORB' / &BC_ABSORB stacey=T /",
+    "&BC_DEF tags=1,3, kind='PERIOD' /",
     "&TIME kind='hhta' /",
     "&SRC_DEF stf='RICKER', coord=0,0, mechanism='WAVE' /",
     "&MATERIAL tag=1, kind='PLAST' /",
@@ -142,3 +142,18 @@ def test_fault_files_round_trip(tmp_path):
     assert len(lines) == d.nt + 1 and len(lines[0]) == 4 * 24
     v = [float(x.replace("D", "E")) for x in lines[40].split()]
     np.testing.assert_allclose(v, [pot[40, 0, 0], pot[40, 0, 1], pot[40, 1, 0], pot[40, 1, 1]], rtol=1e-15)
+
+
+def test_grid_files_round_trip(tmp_path):
+    P = Problem(deck_from_parinp(FAULT_PARINP))
+    g = P.grid
+    outputs.write_grid(str(tmp_path), g)
+    sizes, ib, xz = outputs.read_grid(str(tmp_path))
+    # 40 x 20 elements, the fault splits the corner rows: 41 x 22 geometric nodes
+    assert sizes == {"NELEM": 800, "NPGEO": 41 * 22, "NGNOD": 4, "NPOIN": g.npoin, "NGLL": 5}
+    assert np.array_equal(ib, g.ibool()) and ib.min() == 1 and ib.max() == g.npoin
+    assert np.array_equal(xz, g.coord().astype(np.float32))
+    # record e of ibool_sem2d.dat is element e's NGLL x NGLL table, i fastest
+    raw = np.fromfile(tmp_path / "ibool_sem2d.dat", dtype="<i4")
+    assert os.path.getsize(tmp_path / "ibool_sem2d.dat") == 4 * 25 * 800
+    assert np.array_equal(raw[25 * 7:25 * 8], g.ibool()[:, :, 7].ravel(order="F"))
