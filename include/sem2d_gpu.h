@@ -173,6 +173,31 @@ typedef struct sem2d_problem_desc {
    * every step (BC_DYNFLT_potency, bc_dynflt.f90:757,832-855), read with
    * sem2d_gpu_get_fault_potency.  Single problems only (not in a batch). */
   int flt_potency;
+
+  /* ---- Stacey P3 absorbing terms (BC_ABSO_init bc_abso.f90:174-218,
+   * BC_ABSO_apply :321-334) of the P-SV sides with stacey=T, one entry t
+   * per (boundary element, edge point k).  The force at node
+   * stacey_node[t] receives, for each component c,
+   *   - stacey_K[t + nstacey*c] * sum_l hprime(l, k_t) D(stacey_edge[l + ngll*t], c)
+   * with the element edge's nodes in the traversal order of SE_inquire
+   * (spec_grid.f90:876-881): counter-clockwise around the element, so the
+   * sum is the derivative along that direction. */
+  int nstacey;
+  const int *stacey_node;  /* [nstacey], 1-based                            */
+  const int *stacey_k;     /* [nstacey], edge point 0..ngll-1               */
+  const int *stacey_edge;  /* [ngll*nstacey], 1-based                       */
+  const double *stacey_K;  /* stacey_K(nstacey, 2)                          */
+
+  /* ---- zero-Dirichlet components of &BC_DIRNEU sides (bc_DIRNEU_apply,
+   * bc_dirneu.f90:148-169; traction time functions are not included): the
+   * force component dir_comp[k] at node dir_node[k] is set to zero after
+   * the absorbing terms (bc_gen.f90:271-281).  dir_after_fault[k] = 1 when
+   * the block follows the fault's in &BC_DEF order: at a node the two
+   * share, the zero then overrides the fault traction. */
+  int ndir;
+  const int *dir_node;        /* [ndir], 1-based                            */
+  const int *dir_comp;        /* [ndir], 0 horizontal (SH: the only one), 1 vertical */
+  const int *dir_after_fault; /* [ndir]                                     */
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;

@@ -56,9 +56,12 @@ typedef struct sem2d_material {
 /* &BC_DEF kind, tag(s) (bc_gen.f90:84-186) */
 #define SEM2D_BC_ABSORB 1
 #define SEM2D_BC_DYNFLT 2
+#define SEM2D_BC_DIRNEU 3
 typedef struct sem2d_bc {
   int kind;
   int tag[2];
+  int stacey; /* &BC_ABSORB stacey (bc_abso.f90:55-100); P-SV only        */
+  int dirichlet; /* &BC_DIRNEU: bit 0 h='D', bit 1 v='D' (bc_dirneu.f90:50-112) */
 } sem2d_bc;
 
 /* Per-node fault inputs of &BC_DYNFLT, &BC_DYNFLT_SWF and &BC_DYNFLT_RSF */

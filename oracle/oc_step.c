@@ -48,6 +48,11 @@ struct oc_sim {
   int nabs;
   int *abs_node;
   double *abs_C;
+  int nstacey;
+  int *st_node, *st_k, *st_edge;
+  double *st_K;
+  int ndir;
+  int *dir_node, *dir_comp, *dir_after;
   int scheme;
   double dt, beta, gamma;
   int nt;
@@ -294,6 +299,29 @@ static void abso_apply(oc_sim *s, double *f, const double *v) {
       f[gg] = f[gg] - s->abs_C[k + (size_t)s->nabs * d] * v[gg];
     }
   }
+  /* Stacey P3 (BC_ABSO_apply, bc_abso.f90:321-334): for each boundary
+   * element edge point k, K(k,c,e) times the derivative of D(:,c) along
+   * the edge's traversal order, sum_l Ht(k,l) D(node_l, c) with
+   * Ht(k,l) = hprime(l,k) */
+  for (int t = 0; t < s->nstacey; t++) {
+    const int n = s->ngll, k = s->st_k[t];
+    const size_t g = (size_t)s->st_node[t] - 1;
+    for (int c = 0; c < 2; c++) {
+      double dd = 0.0;
+      for (int l = 0; l < n; l++)
+        dd += s->H[l + (size_t)n * k] * s->d[(size_t)s->st_edge[l + (size_t)n * t] - 1 + (size_t)s->npoin * c];
+      f[g + (size_t)s->npoin * c] -= s->st_K[t + (size_t)s->nstacey * c] * dd;
+    }
+  }
+}
+
+/* zero-Dirichlet components of the &BC_DIRNEU sides that come before (after
+ * = 0) or after (after = 1) the fault in &BC_DEF order (bc_DIRNEU_apply,
+ * bc_dirneu.f90:148-169; bc_apply, bc_gen.f90:271-281) */
+static void dirneu_apply(oc_sim *s, double *f, int after) {
+  for (int k = 0; k < s->ndir; k++)
+    if (s->dir_after[k] == after)
+      f[(size_t)s->dir_node[k] - 1 + (size_t)s->npoin * s->dir_comp[k]] = 0.0;
 }
 
 /* ---------------- friction laws ---------------- */
@@ -685,6 +713,15 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
   s->nabs = dd->nabs;
   s->abs_node = dupi(dd->abs_node, (size_t)dd->nabs);
   s->abs_C = dupd(dd->abs_C, (size_t)dd->nabs * nd);
+  s->nstacey = dd->nstacey;
+  s->st_node = dupi(dd->stacey_node, (size_t)dd->nstacey);
+  s->st_k = dupi(dd->stacey_k, (size_t)dd->nstacey);
+  s->st_edge = dupi(dd->stacey_edge, (size_t)dd->nstacey * n);
+  s->st_K = dupd(dd->stacey_K, (size_t)dd->nstacey * 2);
+  s->ndir = dd->ndir;
+  s->dir_node = dupi(dd->dir_node, (size_t)dd->ndir);
+  s->dir_comp = dupi(dd->dir_comp, (size_t)dd->ndir);
+  s->dir_after = dupi(dd->dir_after_fault, (size_t)dd->ndir);
   s->scheme = dd->time_scheme;
   s->dt = dd->dt;
   s->beta = dd->beta;
@@ -828,7 +865,9 @@ int oc_sim_run(oc_sim *s, int nsteps) {
     compute_fint(s, a, d, v); /* f aliases accel */
     so_add(s, t, a);
     abso_apply(s, a, v);
+    dirneu_apply(s, a, 0);
     if (s->nflt) dynflt_apply(s, a, v, d);
+    dirneu_apply(s, a, 1);
     for (size_t q = 0; q < nn; q++) a[q] = s->rmass[q] * a[q];
     if (s->scheme == SEM2D_TIME_NEWMARK) {
       double cv = s->gamma * s->dt, cd = s->beta * s->dt * s->dt;
@@ -926,6 +965,7 @@ void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T, double
 void oc_sim_free(oc_sim *s) {
   if (!s) return;
   void *ptrs[] = {s->ibool, s->H, s->acoef, s->kveta, s->rmass, s->abs_node, s->abs_C,
+                  s->st_node, s->st_k, s->st_edge, s->st_K, s->dir_node, s->dir_comp, s->dir_after,
                   s->src_node, s->src_dir, s->src_f0, s->src_t0, s->src_amp, s->src_rel,
                   s->src_tdelay, s->rec_node, s->rec_elem, s->rec_interp, s->sis, s->node1,
                   s->node2, s->n1, s->B, s->invM1, s->invM2, s->Z, s->T0, s->coh, s->swf_dc,

@@ -30,6 +30,7 @@ PRECISION_MIXED = 1
 
 BC_ABSORB = 1
 BC_DYNFLT = 2
+BC_DIRNEU = 3
 
 MAX_DOMAINS = 64
 MAX_MATS = 64
@@ -91,6 +92,9 @@ class ProblemDesc(C.Structure):
         ("rho", P_double),
         ("adjoint", c_int),
         ("flt_potency", c_int),
+        ("nstacey", c_int), ("stacey_node", P_int), ("stacey_k", P_int), ("stacey_edge", P_int),
+        ("stacey_K", P_double),
+        ("ndir", c_int), ("dir_node", P_int), ("dir_comp", P_int), ("dir_after_fault", P_int),
     ]
 
 
@@ -107,7 +111,7 @@ class Material(C.Structure):
 
 
 class BC(C.Structure):
-    _fields_ = [("kind", c_int), ("tag", c_int * 2)]
+    _fields_ = [("kind", c_int), ("tag", c_int * 2), ("stacey", c_int), ("dirichlet", c_int)]
 
 
 class Deck(C.Structure):

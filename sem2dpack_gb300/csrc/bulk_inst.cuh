@@ -43,6 +43,8 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.per_rm = static_cast<const real *>(c.per_rm);
   p.per_Ca = static_cast<const real *>(c.per_Ca);
   p.per_Cb = static_cast<const real *>(c.per_Cb);
+  p.per_kd = static_cast<const real *>(c.per_kd);
+  p.per_dir = c.per_dir;
   p.jf1 = c.jf1;
   p.jf2 = c.jf2;
   p.has_fault = c.has_fault;

@@ -31,6 +31,8 @@ struct BulkConfig {
   void *kveta = nullptr, *rmass = nullptr;
   void *geo[4] = {nullptr, nullptr, nullptr, nullptr};  // xix, etaz, dxdxi, dzdeta
   void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
+  void *per_kd = nullptr;  // Stacey P3 forces [c*nslot + slot], or null
+  const int *per_dir = nullptr;  // zero-Dirichlet bits c by perimeter slot, or null
   int jf1 = -1, jf2 = -1;
   int has_fault = 0;
   const void *flt = nullptr;  // host FaultParams<real> of the problem's precision

@@ -357,7 +357,9 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     const int J = side == 0 ? p.jf1 : p.jf2;
     for (int c = 0; c < nd; ++c) {
       const int o = (side * nd + c) * nf + k;
-      const double f = side == 0 ? f1[c] + p.B[k] * Tx[c] : f2[c] - p.B[k] * Tx[c];
+      double f = side == 0 ? f1[c] + p.B[k] * Tx[c] : f2[c] - p.B[k] * Tx[c];
+      // a zero-Dirichlet side after the fault in &BC_DEF order (bc_gen.f90:279-281)
+      if (p.dir_zero && ((p.dir_zero[k] >> (side * 2 + c)) & 1)) f = 0.0;
       const double vp = side == 0 ? v1[c] : v2[c];
       double dc = side == 0 ? d1[c] : d2[c];
       const double a = p.rm[o] * f;

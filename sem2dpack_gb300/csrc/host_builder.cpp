@@ -639,6 +639,11 @@ struct sem2d_problem {
   std::vector<int> abs_node;
   std::vector<double> abs_C;  // built per dof then transposed at export
   std::vector<std::vector<double>> abs_Cd;
+  // Stacey P3 terms, one per (boundary element, edge point)
+  std::vector<int> st_node, st_k, st_edge;
+  std::vector<double> st_K0, st_K1;
+  // zero-Dirichlet components
+  std::vector<int> dir_node, dir_comp, dir_after;
   // fault
   int nflt = 0;
   bool two = false;
@@ -844,8 +849,11 @@ void normals(const sem2d_grid &g, const sem2d_grid::Boundary &b, std::vector<dou
     }
 }
 
-// BC_ABSO_init (bc_abso.f90:115-266), Clayton-Engquist on flat sides
-void abso_init(sem2d_problem &P, int tag) {
+// BC_ABSO_init (bc_abso.f90:115-266), Clayton-Engquist on flat sides, and
+// the Stacey P3 coefficients of a P-SV side with stacey=T
+// (bc_abso.f90:174-218): K(k,c,e) = w_k |dx/dloc_t| dloc_t/dx_t
+// rho cs (2 cs - cp), negated for the tangential component
+void abso_init(sem2d_problem &P, int tag, int stacey) {
   const sem2d_grid &g = *P.g;
   const sem2d_grid::Boundary *b = g.find(tag);
   if (!b) return;  // the reference ignores a BC whose tag is absent (bc_gen.f90:214-219)
@@ -882,6 +890,16 @@ void abso_init(sem2d_problem &P, int tag) {
         Cb[bk] = Cb[bk] + P.rho[p] * cv[0] * ci;
         Cb[bk + np] = Cb[bk + np] + P.rho[p] * cv[1] * ci;
       }
+      if (stacey && nd == 2) {
+        const double det = J[0] * J[3] - J[2] * J[1];
+        const double inv[2][2] = {{J[3] / det, -J[2] / det}, {-J[1] / det, J[0] / det}};
+        const double K0 = ci * inv[ld][gtan] * (P.rho[p] * cv[gtan] * (2.0 * cv[gtan] - cv[gnor]));
+        P.st_node.push_back(b->node[bk]);
+        P.st_k.push_back(k);
+        for (int l = 0; l < N; ++l) P.st_edge.push_back(b->node[b->ib[l + size_t(N) * q] - 1]);
+        P.st_K0.push_back(gtan == 0 ? -K0 : K0);
+        P.st_K1.push_back(gtan == 1 ? -K0 : K0);
+      }
     }
   }
   const double cf = coefA2Vrhs(P);
@@ -894,6 +912,31 @@ void abso_init(sem2d_problem &P, int tag) {
   for (int k = 0; k < np; ++k) {
     P.abs_node.push_back(b->node[k]);
     for (int d = 0; d < nd; ++d) P.abs_Cd[d].push_back(Cb[k + size_t(np) * d]);
+  }
+}
+
+// BC_DIRNEU_init (bc_dirneu.f90:117-143): a flat side whose components
+// flagged 'D' have their force set to zero (bc_DIRNEU_apply, :148-169)
+void dirneu_init(sem2d_problem &P, int tag, int mask, int after_fault) {
+  const sem2d_grid &g = *P.g;
+  const sem2d_grid::Boundary *b = g.find(tag);
+  if (!b) return;
+  const int np = int(b->node.size());
+  std::vector<double> nrm, w;
+  normals(g, *b, nrm, w);
+  bool horiz = true, vert = true;
+  for (int k = 0; k < np; ++k) {
+    horiz &= std::fabs(nrm[k]) < kTinyXabs;
+    vert &= std::fabs(nrm[k + np]) < kTinyXabs;
+  }
+  if (!horiz && !vert) throw BuildError("BC_DIRNEU_init: boundary is not vertical or horizontal");
+  for (int c = 0; c < P.ndof; ++c) {
+    if (!((mask >> c) & 1)) continue;
+    for (int k = 0; k < np; ++k) {
+      P.dir_node.push_back(b->node[k]);
+      P.dir_comp.push_back(c);
+      P.dir_after.push_back(after_fault);
+    }
   }
 }
 
@@ -1200,11 +1243,19 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
       }
     }
     build_mass(*P);
+    bool fault_seen = false;
     for (int b = 0; b < deck->nbcs; ++b) {
       const sem2d_bc &bc = deck->bcs[b];
-      if (bc.kind == SEM2D_BC_ABSORB) abso_init(*P, bc.tag[0]);
-      else if (bc.kind == SEM2D_BC_DYNFLT) dynflt_init(*P, *deck, bc.tag);
-      else throw BuildError("unsupported boundary condition kind");
+      if (bc.kind == SEM2D_BC_ABSORB) {
+        abso_init(*P, bc.tag[0], bc.stacey);
+      } else if (bc.kind == SEM2D_BC_DYNFLT) {
+        dynflt_init(*P, *deck, bc.tag);
+        fault_seen = true;
+      } else if (bc.kind == SEM2D_BC_DIRNEU) {
+        dirneu_init(*P, bc.tag[0], bc.dirichlet, fault_seen ? 1 : 0);
+      } else {
+        throw BuildError("unsupported boundary condition kind");
+      }
     }
     rec_init(*P, *deck);
     src_init(*P, *deck);
@@ -1214,6 +1265,7 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
     P->abs_C.resize(na * nd);
     for (int d = 0; d < nd && na; ++d)
       for (size_t k = 0; k < na; ++k) P->abs_C[k + na * d] = P->abs_Cd[d][k];
+    P->st_K0.insert(P->st_K0.end(), P->st_K1.begin(), P->st_K1.end());  // K(nstacey, 2)
     *out = P.release();
     return SEM2D_OK;
   } catch (const std::bad_alloc &) {
@@ -1249,6 +1301,15 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
   d->nabs = int(P->abs_node.size());
   d->abs_node = VPTR(P->abs_node);
   d->abs_C = VPTR(P->abs_C);
+  d->nstacey = int(P->st_node.size());
+  d->stacey_node = VPTR(P->st_node);
+  d->stacey_k = VPTR(P->st_k);
+  d->stacey_edge = VPTR(P->st_edge);
+  d->stacey_K = VPTR(P->st_K0);
+  d->ndir = int(P->dir_node.size());
+  d->dir_node = VPTR(P->dir_node);
+  d->dir_comp = VPTR(P->dir_comp);
+  d->dir_after_fault = VPTR(P->dir_after);
   d->time_scheme = P->time_kind;
   d->dt = P->dt;
   d->beta = P->beta;

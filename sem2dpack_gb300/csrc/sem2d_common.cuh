@@ -63,6 +63,7 @@ struct FaultParams {
   int scheme;
   double dt, cv, cpred, cd2;
   double cb;            // Newmark corrector beta dt^2
+  const unsigned char *dir_zero;  // [k] bits side*2+c: force zeroed after the fault, or null
   int *step;            // incremented by the last block (stand-alone kernel)
   unsigned int *done;   // block completion counter (reset by the last block)
   int *error;           // sticky device error flag (SEM2D_E_*)
@@ -101,6 +102,8 @@ struct BulkParams {
   const real *dzdeta; // dz/deta of element row
   // perimeter table: slot -> rmass(dof), dashpots Ca(dof), Cb(dof)
   const real *per_rm, *per_Ca, *per_Cb;
+  const real *per_kd;     // Stacey P3 forces [c*nslot + slot] of this step, or null
+  const int *per_dir;     // zero-Dirichlet bits c by perimeter slot, or null
   // fault rows (lattice rows of side 1 and side 2, -1 if none); a tile row
   // always holds both rows, so the owning CTA finishes the fault nodes
   int jf1, jf2;

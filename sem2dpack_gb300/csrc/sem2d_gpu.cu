@@ -67,6 +67,15 @@ struct sem2d_handle {
   void *mat[4] = {nullptr, nullptr, nullptr, nullptr};
   void *kveta = nullptr, *rmass = nullptr, *geo[4] = {nullptr, nullptr, nullptr, nullptr};
   void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
+  // Stacey P3 terms grouped by perimeter slot, and their forces
+  int st_nslot = 0, st_nterm = 0;
+  int *d_st_slot = nullptr, *d_st_ptr = nullptr, *d_st_k = nullptr, *d_st_lat = nullptr;
+  void *d_st_K = nullptr, *d_st_H = nullptr, *per_kd = nullptr;
+  // zero-Dirichlet force components: bits c of a perimeter slot, and bits
+  // (side*2 + c) of a fault node when the zero follows the fault
+  int ndir = 0;
+  int *per_dir = nullptr;
+  unsigned char *d_fdir = nullptr;
   int *d_row0 = nullptr, *d_step = nullptr, *d_error = nullptr;
   unsigned *d_done = nullptr;
   // sources
@@ -399,6 +408,84 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
   return SEM2D_OK;
 }
 
+// Stacey P3 terms (one per boundary element edge point) grouped by the
+// perimeter slot of the node they load, in the order of the descriptor
+int upload_stacey(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int nt = d->nstacey, N = h->N, np = d->npoin;
+  if (nt <= 0) return SEM2D_OK;
+  if (d->ndof != 2) return set_err(h, SEM2D_E_ARG, "Stacey terms need ndof = 2");
+  if (!d->stacey_node || !d->stacey_k || !d->stacey_edge || !d->stacey_K)
+    return set_err(h, SEM2D_E_ARG, "Stacey arrays missing");
+  const int nslot = perimeter_slots(h->LX, h->LZ);
+  std::vector<std::vector<int>> by_slot(nslot);
+  for (int t = 0; t < nt; ++t) {
+    const int p = d->stacey_node[t] - 1;
+    if (p < 0 || p >= np || d->stacey_k[t] < 0 || d->stacey_k[t] >= N)
+      return set_err(h, SEM2D_E_ARG, "Stacey term out of range");
+    const long long L = h->glob2lat[p];
+    const int sl = perimeter_slot(int(L % h->pitch), int(L / h->pitch), h->LX, h->LZ);
+    if (sl < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey node inside the domain");
+    by_slot[sl].push_back(t);
+  }
+  std::vector<int> slot, ptr(1, 0), kk, lat;
+  std::vector<double> K0, K1;
+  for (int sl = 0; sl < nslot; ++sl) {
+    if (by_slot[sl].empty()) continue;
+    slot.push_back(sl);
+    for (int t : by_slot[sl]) {
+      kk.push_back(d->stacey_k[t]);
+      for (int l = 0; l < N; ++l) {
+        const int q = d->stacey_edge[l + (size_t)N * t] - 1;
+        if (q < 0 || q >= np) return set_err(h, SEM2D_E_ARG, "Stacey edge node out of range");
+        lat.push_back(int(h->glob2lat[q]));
+      }
+      K0.push_back(d->stacey_K[t]);
+      K1.push_back(d->stacey_K[t + (size_t)nt]);
+    }
+    ptr.push_back(int(kk.size()));
+  }
+  K0.insert(K0.end(), K1.begin(), K1.end());
+  std::vector<double> H(d->hprime, d->hprime + (size_t)N * N);
+  h->st_nslot = int(slot.size());
+  h->st_nterm = nt;
+  int st;
+  if ((st = dupload(h, &h->d_st_slot, slot)) || (st = dupload(h, &h->d_st_ptr, ptr)) ||
+      (st = dupload(h, &h->d_st_k, kk)) || (st = dupload(h, &h->d_st_lat, lat)) ||
+      (st = upload_real(h, &h->d_st_K, K0)) || (st = upload_real(h, &h->d_st_H, H)) ||
+      (st = upload_real(h, &h->per_kd, std::vector<double>((size_t)2 * nslot, 0.0))))
+    return st;
+  return SEM2D_OK;
+}
+
+// &BC_DIRNEU zero-Dirichlet components by perimeter slot; at a fault node
+// the zero that follows the fault in &BC_DEF order is applied by the fault
+// update instead
+int upload_dirneu(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int n = d->ndir, np = d->npoin;
+  if (n <= 0) return SEM2D_OK;
+  if (!d->dir_node || !d->dir_comp || !d->dir_after_fault) return set_err(h, SEM2D_E_ARG, "Dirichlet arrays missing");
+  const int nslot = perimeter_slots(h->LX, h->LZ);
+  std::vector<int> slot(nslot, 0);
+  std::vector<unsigned char> fdir(h->nflt ? h->nflt : 1, 0);
+  for (int k = 0; k < n; ++k) {
+    const int p = d->dir_node[k] - 1, c = d->dir_comp[k];
+    if (p < 0 || p >= np || c < 0 || c >= d->ndof) return set_err(h, SEM2D_E_ARG, "Dirichlet entry out of range");
+    const long long L = h->glob2lat[p];
+    const int I = int(L % h->pitch), J = int(L / h->pitch);
+    const int sl = perimeter_slot(I, J, h->LX, h->LZ);
+    if (sl < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "Dirichlet node inside the domain");
+    const bool on_fault = h->nflt && (J == h->jf1 || (h->two && J == h->jf2));
+    if (on_fault && d->dir_after_fault[k])
+      fdir[I] |= (unsigned char)(1u << ((J == h->jf1 ? 0 : 1) * 2 + c));
+    else
+      slot[sl] |= 1 << c;
+  }
+  h->ndir = n;
+  int st;
+  if ((st = dupload(h, &h->per_dir, slot)) || (st = dupload(h, &h->d_fdir, fdir))) return st;
+  return SEM2D_OK;
+}
+
 int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
   const int nd = d->ndof, np = d->npoin;
   const int nslot = perimeter_slots(h->LX, h->LZ);
@@ -433,7 +520,8 @@ int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
   if ((st = upload_real(h, &h->rmass, rm)) || (st = upload_real(h, &h->per_rm, prm)) ||
       (st = upload_real(h, &h->per_Ca, pca)) || (st = upload_real(h, &h->per_Cb, pcb)))
     return st;
-  return SEM2D_OK;
+  if ((st = upload_stacey(h, d))) return st;
+  return upload_dirneu(h, d);
 }
 
 int upload_fault(sem2d_handle *h, const sem2d_problem_desc *d) {
@@ -559,6 +647,7 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.Dnext = (real *)h->D[1 - cur];
   f.Vnext = (real *)h->V[1 - cur];
   f.Anext = h->keep_accel ? (real *)h->A[1 - cur] : nullptr;
+  f.dir_zero = h->ndir ? h->d_fdir : nullptr;
   f.d64 = h->fd[F_D64];
   f.v64 = h->fd[F_V64];
   f.a64 = h->fd[F_A64];
@@ -682,6 +771,8 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.per_rm = h->per_rm;
   bc.per_Ca = h->per_Ca;
   bc.per_Cb = h->per_Cb;
+  bc.per_kd = h->per_kd;
+  bc.per_dir = h->ndir ? h->per_dir : nullptr;
   bc.jf1 = h->nflt ? h->jf1 : -1;
   bc.jf2 = h->nflt ? h->jf2 : -1;
   bc.has_fault = h->nflt ? 1 : 0;
@@ -724,6 +815,30 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.w = h->w.data();
   bc.stream = h->stream;
   return bc;
+}
+
+// Stacey P3 boundary forces of the step's predictor displacement
+// (BC_ABSO_apply, bc_abso.f90:321-334), one thread per (perimeter slot,
+// component): the sum over the slot's terms t of K(t,c) times the derivative
+// of D(:,c) along the element edge, sum_l hprime(l,k_t) D(edge node l, c).
+// The step kernel subtracts it at the slot together with the dashpots.
+template <typename real>
+__global__ void stacey_kernel(real *per_kd, const real *D, int nused, const int *slot, const int *ptr,
+                              const int *kk, const int *lat, const real *K, const real *H, int N, int nterm,
+                              int nslot, long long plane) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= 2 * nused) return;
+  const int i = q % nused, c = q / nused;
+  const real *Dc = D + c * plane;
+  real acc = real(0);
+  for (int t = ptr[i]; t < ptr[i + 1]; ++t) {
+    const int k = kk[t];
+    const int *L = lat + (size_t)t * N;
+    real dd = H[N * k] * Dc[L[0]];
+    for (int l = 1; l < N; ++l) dd = dd + H[l + N * k] * Dc[L[l]];
+    acc = acc + K[t + (size_t)nterm * c] * dd;
+  }
+  per_kd[(size_t)c * nslot + slot[i]] = acc;
 }
 
 // Sum of the potency terms of the fault node pairs of the step just
@@ -812,6 +927,15 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     h->launches += h->march_fused ? 2 : 3;
     if (h->potency && launch_potency(h, h->stream, h->d_step_c)) return SEM2D_E_CUDA;
   } else {
+    if (h->st_nslot) {
+      const int nthr = 2 * h->st_nslot;
+      stacey_kernel<real><<<(nthr + 127) / 128, 128, 0, h->stream>>>(
+          (real *)h->per_kd, (const real *)h->D[cur], h->st_nslot, h->d_st_slot, h->d_st_ptr, h->d_st_k,
+          h->d_st_lat, (const real *)h->d_st_K, (const real *)h->d_st_H, h->N, h->st_nterm,
+          perimeter_slots(h->LX, h->LZ), h->plane);
+      CK(cudaGetLastError());
+      h->launches++;
+    }
     if (ev) CK(cudaEventRecord(ev[0], h->stream));
     if (launch_step_kernel(h, bc, rec))
       return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
@@ -966,7 +1090,7 @@ int launch_steps(sem2d_handle *h, int n) {
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
   return 1 + (h->march && h->nflt ? (h->march_fused ? 1 : 2) : 0) + (h->nflt && h->potency ? 1 : 0) +
-         (h->nrec && h->rec_separate ? 1 : 0);
+         (h->nrec && h->rec_separate ? 1 : 0) + (h->st_nslot ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -1065,6 +1189,7 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   h->march = false;
   const char *env = std::getenv("SEM2D_MARCH");
   if (env && std::atoi(env) == 0) return SEM2D_OK;
+  if (h->st_nslot || h->ndir) return SEM2D_OK;  // Stacey or Dirichlet sides: the strip kernel
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
@@ -1469,6 +1594,8 @@ int batch_close_impl(sem2d_handle *h) {
     if (m->nrec && m->rec_separate)
       return set_err(h, SEM2D_E_UNSUPPORTED, "interpolated velocity/acceleration receivers in a batch");
     if (m->potency) return set_err(h, SEM2D_E_UNSUPPORTED, "fault potency records in a batch");
+    if (m->st_nslot) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey absorbing boundaries in a batch");
+    if (m->ndir) return set_err(h, SEM2D_E_UNSUPPORTED, "Dirichlet sides in a batch");
   }
   h->N = a->N;
   h->ndof = a->ndof;
@@ -1821,9 +1948,10 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
   if (h->ckpt_every <= 0 || h->steps != h->nt || h->ckpt_saved != h->nt / h->ckpt_every)
     return set_err(h, SEM2D_E_STATE, "run all nt steps with checkpoints first (sem2d_gpu_checkpoint_every)");
   if (h->N != 5 || h->nflt || h->scheme != 0 || h->has_kv || h->width > 0 || !h->mat_iso ||
-      h->mat_elem != kMatNode)
+      h->mat_elem != kMatNode || h->st_nslot || h->ndir)
     return set_err(h, SEM2D_E_UNSUPPORTED,
-                   "the adjoint covers NGLL=5, isotropic node material, leapfrog, no fault, KV or 2.5D");
+                   "the adjoint covers NGLL=5, isotropic node material, leapfrog, no fault, KV, 2.5D, Stacey "
+                   "or Dirichlet sides");
   if (h->nrec && (h->rec_npts != 1 || (h->rec_field != 'V' && h->rec_field != 'D')))
     return set_err(h, SEM2D_E_UNSUPPORTED, "the adjoint needs receivers at nodes recording V or D");
   int st = check_device_error(h);

@@ -131,6 +131,10 @@ class ParDeck:
     domains: List[Tuple[int, Tuple[int, int], Tuple[int, int]]] = field(default_factory=list)
     materials: List[Material] = field(default_factory=list)
     absorbing: List[int] = field(default_factory=list)   # tags with kind='ABSORB'
+    stacey: List[int] = field(default_factory=list)      # of those, the tags with &BC_ABSORB stacey=T
+    # &BC_DEF kind='DIRNEU' + &BC_DIRNEU h, v: (tag, h, v, before_fault), h and
+    # v 'N' or 'D'; before_fault when the block precedes the fault's in &BC_DEF
+    dirneu: List[Tuple[int, str, str, bool]] = field(default_factory=list)
     fault: Optional[Fault] = None
     fault_first: bool = False  # &BC_DEF order: DYNFLT block before the ABSORB blocks
     time: Time = field(default_factory=Time)
@@ -173,18 +177,32 @@ class ParDeck:
                 arr = np.ascontiguousarray(np.asarray(arr, dtype=np.float64).ravel(order="F"))
                 keep.append(arr)
             setattr(d, "h_" + name, _dptr(arr))
-        bcs = []
-        if self.fault is not None and self.fault_first:
-            bcs.append((abi.BC_DYNFLT, self.fault.tags))
-        bcs += [(abi.BC_ABSORB, (t, 0)) for t in self.absorbing]
-        if self.fault is not None and not self.fault_first:
-            bcs.append((abi.BC_DYNFLT, self.fault.tags))
+        for t in self.stacey:
+            if t not in self.absorbing:
+                raise ValueError("stacey tag %d is not an absorbing boundary" % t)
+        pre, post = [], []
+        for t, h, v, before in self.dirneu:
+            if h not in "ND" or v not in "ND" or len(h) != 1 or len(v) != 1:
+                raise ValueError("BC_DIRNEU h and v must be 'N' or 'D'")
+            (pre if before else post).append((abi.BC_DIRNEU, (t, (h == "D") | ((v == "D") << 1))))
+        absorb = [(abi.BC_ABSORB, (t, 0)) for t in self.absorbing]
+        if self.fault is None:
+            bcs = absorb + pre + post
+        elif self.fault_first:
+            bcs = pre + [(abi.BC_DYNFLT, self.fault.tags)] + absorb + post
+        else:
+            bcs = absorb + pre + [(abi.BC_DYNFLT, self.fault.tags)] + post
         if len(bcs) > abi.MAX_BCS:
             raise ValueError("too many boundary conditions")
         d.nbcs = len(bcs)
         for k, (kind, tags) in enumerate(bcs):
             d.bcs[k].kind = kind
+            if kind == abi.BC_DIRNEU:
+                d.bcs[k].tag[:] = [int(tags[0]), 0]
+                d.bcs[k].dirichlet = int(tags[1])
+                continue
             d.bcs[k].tag[:] = [int(tags[0]), int(tags[1])]
+            d.bcs[k].stacey = int(kind == abi.BC_ABSORB and tags[0] in self.stacey)
         f = self.fault
         for i, name in enumerate(abi.FP_NAMES):
             d.flt_value[i] = abi.FP_DEFAULTS[name]

@@ -16,7 +16,8 @@ between blocks (``#`` comments, anything after the ``/``) is ignored.
   &MATERIAL     tag, kind 'ELAST' [+ 'KV'] + &MAT_ELASTIC rho, cp, cs or
                 c11, c13, c33, c55, c66 (mat_elastic.f90:69-189),
                 &MAT_KV eta, ETAxDT (mat_kelvin_voigt.f90)
-  &BC_DEF       tag, kind 'ABSORB' + &BC_ABSORB stacey=F (bc_abso.f90),
+  &BC_DEF       tag, kind 'ABSORB' + &BC_ABSORB stacey (bc_abso.f90),
+                kind 'DIRNEU' + &BC_DIRNEU h, v (bc_dirneu.f90:50-112),
                 kind 'DYNFLT' + &BC_DYNFLT / _SWF / _RSF / _TWF / _NOR with
                 scalar values (bc_dynflt*.f90)
   &TIME         kind, Dt, Courant, TotalTime, NbSteps + &TIME_NEWMARK
@@ -186,14 +187,23 @@ def deck_from_parinp(text, precision=None):
             if kind == "ABSORB":
                 absorbing.extend(int(t) for t in tags)
                 if nxt[0] == "BC_ABSORB" and nxt[1].get("stacey", False):
-                    raise ValueError("&BC_ABSORB stacey=T is not on the GPU path")
+                    deck.stacey.extend(int(t) for t in tags)
             elif kind == "DYNFLT":
                 fault = fault or Fault()
-                fault.tags = (int(tags[0]), int(tags[1]) if len(tags) > 1 else int(tags[0]))
+                # a single tag is a one-sided fault: tags = (tag, 0) (bc_gen.f90:126-133)
+                fault.tags = (int(tags[0]), int(tags[1]) if len(tags) > 1 else 0)
                 deck.fault_first = not absorbing
+            elif kind == "DIRNEU":
+                b = nxt[1] if nxt[0] == "BC_DIRNEU" else {}
+                extra = set(b) - {"h", "v"}
+                if extra:
+                    raise ValueError("&BC_DIRNEU %s (traction time functions) is not on the GPU path"
+                                     % ", ".join(sorted(extra)))
+                h, v = str(b.get("h", "N")).upper(), str(b.get("v", "N")).upper()
+                deck.dirneu.extend((int(t), h, v, fault is None) for t in tags)
             else:
                 raise ValueError("boundary kind %s is not on the GPU path" % kind)
-        elif name == "BC_ABSORB":
+        elif name in ("BC_ABSORB", "BC_DIRNEU"):
             pass
         elif name == "BC_DYNFLT":
             fault = fault or Fault()

@@ -65,3 +65,20 @@ def inabox():
         sources=Sources(coords=[(0.0, 0.0)], f0=5.0, onset=0.4, ampli=1.0, angle=0.0),
         receivers=Receivers(number=21, first=(-500.0, -1000.0), last=(-500.0, 1000.0), field="V"),
     )
+
+
+def test_abso(zbottom, znel, stacey, ndof=2, total_time=1.5):
+    """EXAMPLES/TestAbso/Par.inp.template:1-53 with the substitutions of
+    EXAMPLES/TestAbso/run_test_PSV:1-9 (ZBOTTOM, ZNEL; NDOF=2, TT=1.5): a
+    vertical Ricker force in a 6 x (2 - zbottom) km box absorbing on all
+    four sides, 91 receivers on the line z = -1 km.  With zbottom = -1 km
+    that line is the bottom boundary; with zbottom = -3 km it is inside, and
+    the difference measures what the bottom boundary reflects."""
+    return ParDeck(
+        ngll=9, ndof=ndof, fmax=75.0, xlim=(-1.5e3, 4.5e3), zlim=(zbottom, 2.0e3), nelem=(120, znel),
+        materials=[Material(tag=1, rho=2500.0, cp=5000.0, cs=2887.0)],
+        absorbing=[1, 2, 3, 4], stacey=[1, 2, 3, 4] if stacey else [],
+        time=Time(kind="leapfrog", total_time=total_time, courant=0.6),
+        sources=Sources(coords=[(0.0, 0.0)], f0=30.0, onset=0.05, ampli=1.0e9, angle=90.0),
+        receivers=Receivers(number=91, first=(0.0, -1.0e3), last=(4.5e3, -1.0e3), isamp=1, field="V"),
+    )

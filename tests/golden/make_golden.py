@@ -16,6 +16,13 @@ It reads the reference's own test data (nothing is written from memory):
   EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
   EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox}/Par.inp
                                               the input decks, as text (parinp_*)
+  EXAMPLES/TestAbso/data_mat/{stacey,paraxial}_PSV.mat
+                                              the reference's misfits of the direct
+                                              P (errp) and S (errs) waves against
+                                              incidence angle (theta) on a bottom
+                                              boundary with Stacey P3 or
+                                              Clayton-Engquist P1 conditions
+                                              (TestAbso/test_abso_PSV.m:95-136)
 and writes golden.npz.  The GPU machine and the test suite only read the npz.
 """
 import os
@@ -49,6 +56,11 @@ def main(ref):
     out["inabox_nelem"] = np.array(int(re.search(r"Total number of elements[ .]*= *(\d+)", info).group(1)))
     out["inabox_dt"] = np.array(float(re.search(r"Time step \(secs\) *= *([0-9.E+\-]+)", info).group(1)))
     out["inabox_nt"] = np.array(int(re.search(r"Number of time steps *= *(\d+)", info).group(1)))
+
+    for kind in ("stacey", "paraxial"):
+        m = loadmat(os.path.join(ex, "TestAbso", "data_mat", kind + "_PSV.mat"))
+        for key in ("theta", "errp", "errs"):
+            out["abso_%s_%s" % (kind, key)] = np.asarray(m[key], dtype=np.float64).ravel()
 
     for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())

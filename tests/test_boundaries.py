@@ -1,0 +1,145 @@
+"""Stacey P3 and zero-Dirichlet (&BC_DIRNEU) boundary tables of the host
+builder, and the oracle's use of them, on the CPU.
+
+Stacey (BC_ABSO_init, bc_abso.f90:174-218): on the Cartesian mesher's flat
+rectangular elements |dx/dloc_t| dloc_t/dx_t = 1, so
+K(k,c,e) = w_k rho cs (2 cs - cp), negated for the tangential component;
+each term lists its element edge's nodes in SE_inquire's traversal order
+(spec_grid.f90:876-881).
+"""
+import numpy as np
+import pytest
+
+import decks
+from oracle import pyoracle as po
+from sem2dpack_gb300 import PRECISION_FP64, Problem
+from sem2dpack_gb300.deck import Time
+from sem2dpack_gb300.parinp import deck_from_parinp
+
+
+def arr(d, name, n):
+    return np.ctypeslib.as_array(getattr(d, name), shape=(n,)).copy()
+
+
+def small_box(stacey=True):
+    dk = decks.test_abso(-1.0e3, 12, stacey)
+    dk.ngll, dk.fmax, dk.nelem = 5, 20.0, (24, 15)
+    dk.xlim, dk.zlim = (-1.5e3, 0.9e3), (-1.0e3, 0.5e3)
+    dk.time = Time(kind="leapfrog", nsteps=200, courant=0.5)
+    dk.sources.coords = [(-1100.0, -700.0)]
+    dk.sources.f0, dk.sources.onset = 10.0, 0.1
+    dk.receivers.first, dk.receivers.last = (-1500.0, -1000.0), (900.0, -1000.0)
+    dk.receivers.number = 25
+    return dk
+
+
+def test_stacey_table():
+    P = Problem(small_box())
+    d = P.desc()
+    N, nt = d.ngll, d.nstacey
+    assert nt == (2 * 24 + 2 * 15) * N
+    K = arr(d, "stacey_K", 2 * nt).reshape(2, nt)
+    node = arr(d, "stacey_node", nt)
+    k = arr(d, "stacey_k", nt)
+    edge = arr(d, "stacey_edge", N * nt).reshape(nt, N)
+    _, w, _ = P.grid.gll()
+    rho, cp, cs = 2500.0, 5000.0, 2887.0
+    kmag = w[k] * rho * cs * (2 * cs - cp)
+    xz = P.grid.coord()
+    x, z = xz[0, node - 1], xz[1, node - 1]
+    horiz = np.isclose(z, -1.0e3) | np.isclose(z, 0.5e3)
+    # corner nodes belong to both sides: the side is the one the edge runs along
+    ex, ez = xz[0, edge - 1], xz[1, edge - 1]
+    along_x = np.ptp(ez, axis=1) < 1e-9
+    assert np.all(along_x[horiz & ~(np.isclose(x, -1.5e3) | np.isclose(x, 0.9e3))])
+    np.testing.assert_allclose(np.abs(K[0]), kmag, rtol=1e-13)
+    np.testing.assert_allclose(K[0][along_x], -kmag[along_x], rtol=1e-13)
+    np.testing.assert_allclose(K[1][along_x], kmag[along_x], rtol=1e-13)
+    np.testing.assert_allclose(K[0][~along_x], kmag[~along_x], rtol=1e-13)
+    np.testing.assert_allclose(K[1][~along_x], -kmag[~along_x], rtol=1e-13)
+    # the term's node is edge point k of its edge
+    assert np.array_equal(edge[np.arange(nt), k], node)
+    # counter-clockwise traversal: the bottom side runs in +x, the top in -x
+    bottom = along_x & np.isclose(ez[:, 0], -1.0e3)
+    top = along_x & np.isclose(ez[:, 0], 0.5e3)
+    assert np.all(np.diff(ex[bottom], axis=1) > 0) and np.all(np.diff(ex[top], axis=1) < 0)
+
+
+def test_stacey_needs_psv_and_is_absorbing():
+    dk = small_box()
+    dk.ndof = 1
+    P = Problem(dk)
+    assert P.desc().nstacey == 0  # bc_abso.f90:176: P-SV only
+    dk = small_box(False)
+    dk.stacey = [2]
+    dk.absorbing = [1, 3, 4]
+    with pytest.raises(ValueError):
+        Problem(dk)
+
+
+def test_oracle_stacey_changes_the_answer():
+    out = []
+    for st in (True, False):
+        P = Problem(small_box(st))
+        d = P.desc()
+        d.precision = PRECISION_FP64
+        o = po.OracleSim(d, owner=P)
+        o.run(200)
+        out.append(o.seismograms())
+    assert np.abs(out[0]).max() > 0
+    assert np.linalg.norm(out[0] - out[1]) > 1e-3 * np.linalg.norm(out[1])
+
+
+def dirneu_box(h="N", v="D", tag=4):
+    dk = small_box(False)
+    dk.absorbing = [t for t in dk.absorbing if t != tag]
+    dk.dirneu = [(tag, h, v, True)]
+    return dk
+
+
+def test_dirneu_table_and_oracle_zero():
+    P = Problem(dirneu_box())
+    d = P.desc()
+    assert d.ndir == 15 * 4 + 1  # the left side's nodes, vertical component
+    node = arr(d, "dir_node", d.ndir)
+    assert np.all(arr(d, "dir_comp", d.ndir) == 1)
+    assert np.all(arr(d, "dir_after_fault", d.ndir) == 0)
+    xz = P.grid.coord()
+    assert np.allclose(xz[0, node - 1], -1.5e3)
+    d.precision = PRECISION_FP64
+    o = po.OracleSim(d, owner=P)
+    o.run(200)
+    D, V, A = o.fields()
+    assert np.abs(D[:, 1]).max() > 0
+    assert np.all(D[node - 1, 1] == 0) and np.all(V[node - 1, 1] == 0)
+    assert np.abs(D[node - 1, 0]).max() > 0  # 'N' on the horizontal component
+
+
+def test_dirneu_order_against_the_fault():
+    text = """
+&GENERAL ngll=5, fmax=10d0, ndof=2 /
+&MESH_DEF method='CARTESIAN' /
+&MESH_CART xlim=0d0,4d3, zlim=0d0,2d3, nelem=40,20 /
+&MATERIAL tag=1, kind='ELAST' /
+&MAT_ELASTIC rho=2670d0, cp=6000d0, cs=3464d0 /
+&BC_DEF tag=4, kind='DIRNEU' /
+&BC_DIRNEU h='N', v='D' /
+&BC_DEF tag = 1, kind = 'DYNFLT' /
+&BC_DYNFLT friction='SWF', Tn=-120d6, Tt=70d6 /
+&BC_DYNFLT_SWF Dc=0.4d0, MuS=0.677d0, MuD=0.525d0 /
+&BC_DEF tag=2, kind='ABSORB' /
+&BC_DEF tag=3, kind='ABSORB' /
+&BC_DEF tag=4, kind='DIRNEU' /
+&BC_DIRNEU h='D' /
+&TIME TotalTime=0.1d0, courant=0.5d0, kind='newmark' /
+"""
+    dk = deck_from_parinp(text)
+    assert dk.fault.tags == (1, 0)  # one tag: a one-sided fault (bc_gen.f90:126-133)
+    assert dk.dirneu == [(4, "N", "D", True), (4, "D", "N", False)]
+    P = Problem(dk)
+    d = P.desc()  # points into P's arrays
+    n = d.ndir
+    comp, after = arr(d, "dir_comp", n), arr(d, "dir_after_fault", n)
+    assert set(zip(comp.tolist(), after.tolist())) == {(1, 0), (0, 1)}
+    with pytest.raises(ValueError):
+        deck_from_parinp(text.replace("&BC_DIRNEU h='D' /", "&BC_DIRNEU h='D', hsrc='RICKER' /"))
