@@ -26,6 +26,12 @@ JUPYTER/POST scripts of SEM2DPACK, Seismic Unix) read a GPU run unchanged.
                 spec_grid.f90:298-307); coord_sem2d.dat: direct access,
                 record i = (x, z) of node i in FP32 (SE_init_coord,
                 spec_grid.f90:363-371)
+  snapshots     {d,v,a}{x,z|y}_NNN_sem2d.dat: the node field in FP32, node
+                order (PLOT_FIELD, plot_gen.f90:180-214; IO_rw_field,
+                stdio.f90:113-139); e11/e22/e12 (SH e13/e23) and s11/s22/s12
+                (SH s13/s23)_NNN_sem2d.dat: direct access, record e = the
+                NGLL x NGLL values of element e in FP32 (plot_gen.f90:
+                220-300).  NNN = (it - it1) / itd, three digits
 
 Values are written little-endian, as the reference built with gfortran on
 x86 or Arm writes them.
@@ -35,7 +41,7 @@ import os
 import numpy as np
 
 __all__ = ["write_seismograms", "read_seismograms", "write_fault", "read_fault", "write_potency", "write_run",
-           "write_fault_init", "write_grid", "read_grid"]
+           "write_fault_init", "write_grid", "read_grid", "write_snapshot"]
 
 
 def _fmt_list(*vals):
@@ -183,6 +189,44 @@ def read_grid(path):
     ib = np.fromfile(os.path.join(path, "ibool_sem2d.dat"), dtype="<i4").reshape(ne, n, n)
     xz = np.fromfile(os.path.join(path, "coord_sem2d.dat"), dtype="<f4").reshape(npn, 2)
     return sizes, np.transpose(ib, (2, 1, 0)), xz.T
+
+
+def write_snapshot(path, solver, index, fields="V"):
+    """The binary snapshot files of one output time for the SNAP_DEF
+    `fields` letters D, V, A (node fields), E (strain) and S (stress);
+    `index` is the NNN of the file names.  The divergence and curl (d, c)
+    are not written; nor is S for Kelvin-Voigt materials, whose snapshot
+    stress the reference takes from d + eta v (MAT_stress_dv,
+    mat_gen.f90:626-641) while the GPU getter gives the elastic stress of d."""
+    d = solver.desc
+    fields = str(fields)
+    bad = set(fields) - set("DVAES")
+    if bad:
+        raise ValueError("snapshot fields %s are not written" % sorted(bad))
+    if "S" in fields and d.kv_eta:
+        raise ValueError("snapshot stress of a Kelvin-Voigt material is not written")
+    os.makedirs(path, exist_ok=True)
+    tag = "%03d" % int(index)
+    comps = ["y"] if d.ndof == 1 else ["x", "z"]
+    want = [c for c in "DVA" if c in fields]
+    if want:
+        got = solver.fields(accel="A" in want)
+        byname = {"D": got[0], "V": got[1]}
+        if "A" in want:
+            byname["A"] = got[2]
+        for c in want:
+            for k, comp in enumerate(comps):
+                np.ascontiguousarray(byname[c][:, k], dtype="<f4").tofile(
+                    os.path.join(path, "%s%s_%s_sem2d.dat" % (c.lower(), comp, tag)))
+    if "E" in fields or "S" in fields:
+        strain, stress = solver.strain_stress()  # (ngll, ngll, ndof+1, nelem)
+        names = (("13", "23") if d.ndof == 1 else ("11", "22", "12"))
+        for letter, arr, pre in (("E", strain, "e"), ("S", stress, "s")):
+            if letter not in fields:
+                continue
+            for k, nm in enumerate(names):
+                rec = np.transpose(arr[:, :, k, :], (2, 1, 0))  # record e, i fastest
+                np.ascontiguousarray(rec, dtype="<f4").tofile(os.path.join(path, "%s%s_%s_sem2d.dat" % (pre, nm, tag)))
 
 
 def write_run(path, solver, problem):

@@ -31,14 +31,23 @@ energies, and the option blocks the reference would not read for this deck
 (as it does, a &SRC_WAVE next to a mechanism='FORCE' source, or a
 &MESH_EMC2 under method='CARTESIAN', is ignored).  A selecting block that
 asks for something off the GPU path (another mesher, material kind,
-boundary kind, source mechanism or time scheme, Stacey absorption, a
-distribution of fault values) raises ValueError.
+boundary kind, source mechanism or time scheme, a traction time function,
+a SPLINE or HETE1 distribution) raises ValueError.
+
+Material and fault values given as distributions (rhoH, cpH, csH, etaH,
+TtH, TnH, MuSH, DcH, aH, ... followed by &DIST_* blocks) are evaluated on
+the host (sem2dpack_gb300.distributions) at the fault nodes and at the
+element GLL points once the grid is built.
 """
+import os
 import re
 
-from .deck import Fault, Material, ParDeck, Receivers, Sources, TimeWeakening, Time
+import numpy as np
 
-__all__ = ["read_namelists", "deck_from_parinp", "load_parinp"]
+from .deck import Fault, Material, ParDeck, Receivers, Sources, TimeWeakening, Time
+from .distributions import Dist
+
+__all__ = ["read_namelists", "read_blocks", "deck_from_parinp", "load_parinp"]
 
 TIME_KINDS = ("leapfrog", "newmark")
 
@@ -85,10 +94,19 @@ def _value(tok):
 
 def read_namelists(text):
     """[(NAME, {key: value or [values]})] in file order."""
+    return [(name, items) for name, items, _ in read_blocks(text)]
+
+
+def read_blocks(text):
+    """[(NAME, items, data)] in file order; data are the free-format values
+    between the block's closing '/' and the next '&' (the tables that
+    follow &DIST_PWCONR, &DIST_ORDER0 or &DIST_LINEAR)."""
     toks = _TOKEN.findall(_strip_comments(text))
     blocks, k = [], 0
     while k < len(toks):
         if toks[k] != "&" or k + 1 >= len(toks):
+            if blocks and toks[k] not in ",/":
+                blocks[-1][2].append(_value(toks[k]))
             k += 1
             continue
         name, k = toks[k + 1].upper(), k + 2
@@ -109,7 +127,7 @@ def read_namelists(text):
             k += 1
         if key is not None:
             items[key] = vals[0] if len(vals) == 1 else vals
-        blocks.append((name, items))
+        blocks.append((name, items, []))
         k += 1
     return blocks
 
@@ -118,9 +136,45 @@ def _pair(v):
     return (float(v[0]), float(v[1]))
 
 
-def deck_from_parinp(text, precision=None):
-    """ParDeck for the Par.inp text (see the module docstring)."""
-    blocks = read_namelists(text)
+# parameters that may be given as distributions (name + 'H'), in the order
+# the reference's read routines consume the &DIST_* blocks that follow
+_FAULT_DIST = (("cohesion", "cohesion"), ("tn", "Tn"), ("tt", "Tt"), ("sxx", "Sxx"), ("sxy", "Sxy"),
+               ("sxz", "Sxz"), ("syz", "Syz"), ("szz", "Szz"), ("v", "V"))   # bc_dynflt.f90:162-170
+_SWF_DIST = (("dc", "swf_dc"), ("mus", "swf_mus"), ("mud", "swf_mud"), ("alpha", "swf_alpha"),
+             ("p", "swf_p"))                                                  # bc_dynflt_swf.f90:99-103
+_RSF_DIST = (("dc", "rsf_dc"), ("mus", "rsf_mus"), ("a", "rsf_a"), ("b", "rsf_b"), ("vstar", "rsf_vstar"),
+             ("theta", "rsf_theta"), ("vc", "rsf_vc"))                         # bc_dynflt_rsf.f90:112-118
+
+
+def deck_from_parinp(text, precision=None, base=None):
+    """ParDeck for the Par.inp text (see the module docstring).  `base` is
+    the folder that `file=` names in &DIST_* blocks are relative to."""
+    blocks3 = read_blocks(text)
+    blocks = [(n, i) for n, i, _ in blocks3]
+    consumed = set()
+    fault_dists, mat_dists = {}, {}
+
+    def take_dists(j, it, keys):
+        """{name: Dist} for the keys of block j given as distributions: each
+        reads the next &DIST_<kind> block after the ones already read, as
+        the reference's namelist reads search forward (distribution_cd.f90
+        DIST_CD_Read)."""
+        out, pos = {}, j + 1
+        for key, name in keys:
+            v = it.get(key + "h")
+            if v is None or str(v).strip() == "":
+                continue
+            want = "DIST_" + str(v).strip().upper()
+            q = pos
+            while q < len(blocks3) and (q in consumed or blocks3[q][0] != want):
+                q += 1
+            if q >= len(blocks3):
+                raise ValueError("&%s %sH='%s': no &%s block follows" % (blocks3[j][0], key, v, want))
+            consumed.add(q)
+            out[name] = Dist(want[5:], blocks3[q][1], blocks3[q][2], base)
+            pos = q + 1
+        return out
+
     kw = {}
     if precision is not None:
         kw["precision"] = precision
@@ -134,6 +188,9 @@ def deck_from_parinp(text, precision=None):
     while k < len(blocks):
         name, it = blocks[k]
         nxt = blocks[k + 1] if k + 1 < len(blocks) else ("", {})
+        if k in consumed:
+            k += 1
+            continue
         if name == "GENERAL":
             deck.ngll = int(it.get("ngll", deck.ngll))
             deck.ndof = int(it.get("ndof", deck.ndof))
@@ -162,20 +219,26 @@ def deck_from_parinp(text, precision=None):
             if any(s not in ("ELAST", "KV") for s in kinds):
                 raise ValueError("material kind %s is not on the GPU path" % kinds)
             j = k + 1
-            while j < len(blocks) and blocks[j][0] in ("MAT_ELASTIC", "MAT_KV"):
+            md = {}
+            while j < len(blocks) and (blocks[j][0] in ("MAT_ELASTIC", "MAT_KV") or j in consumed):
                 bn, b = blocks[j]
-                if bn == "MAT_ELASTIC":
-                    if "c11" in b:
-                        m.aniso = True
-                        for c in ("c11", "c13", "c33", "c55", "c66"):
-                            setattr(m, c, float(b.get(c, 0.0)))
-                        m.rho = float(b.get("rho", 0.0))
-                    else:
-                        m.rho, m.cp, m.cs = float(b["rho"]), float(b["cp"]), float(b["cs"])
+                if j in consumed:
+                    pass
+                elif bn == "MAT_ELASTIC":
+                    # MAT_ELAST_read (mat_elastic.f90:102-135): rho, then cp, cs or the c_ij
+                    aniso = any(c in b or c + "h" in b for c in ("c11", "c55"))
+                    props = ("rho", "c11", "c13", "c33", "c55", "c66") if aniso else ("rho", "cp", "cs")
+                    md.update(take_dists(j, b, [(c, c) for c in props]))
+                    m.aniso = aniso
+                    for c in props:
+                        setattr(m, c, float(b.get(c, 0.0)))
                 else:
+                    md.update(take_dists(j, b, [("eta", "kveta")]))
                     m.kv_eta = float(b.get("eta", 0.0))
                     m.kv_etaxdt = bool(b.get("etaxdt", True))
                 j += 1
+            if md:
+                mat_dists[m.tag] = md
             mats.append(m)
             k = j
             continue
@@ -214,37 +277,33 @@ def deck_from_parinp(text, precision=None):
             if "TWF" in fr and fr[0] != "TWF":
                 fault.twf = fault.twf or TimeWeakening()
             fault.opening = bool(it.get("opening", True))
-            for key, fname in (("tn", "Tn"), ("tt", "Tt"), ("v", "V"), ("sxx", "Sxx"), ("sxy", "Sxy"),
-                               ("sxz", "Sxz"), ("syz", "Syz"), ("szz", "Szz"), ("cohesion", "cohesion")):
+            for key, fname in _FAULT_DIST:
                 if key in it:
                     fault.values[fname] = float(it[key])
+            fault_dists.update(take_dists(k, it, _FAULT_DIST))
             if "ot1" in it:
                 fault.ot1 = float(it["ot1"])
             if "otd" in it:
                 fault.otd = float(it["otd"])
             if "oxi" in it:
                 fault.oxi = tuple(int(v) for v in it["oxi"])
-            for key in it:
-                if key.endswith("h") and key[:-1] in ("tn", "tt", "v", "sxx", "sxy", "sxz", "syz", "szz"):
-                    raise ValueError("&BC_DYNFLT %s (distribution) is not supported by the front end" % key)
-        elif name in ("BC_DYNFLT_SWF", "BC_DYNFLT_RSF", "BC_DYNFLT_NOR") and \
-                any(key.endswith("h") and len(key) > 1 for key in it if key not in ("h",)):
-            bad = [key for key in it if key.endswith("h")]
-            raise ValueError("&%s %s (distribution) is not supported by the front end" % (name, bad))
+        elif name == "BC_DYNFLT_NOR" and any(key.endswith("h") for key in it):
+            raise ValueError("&BC_DYNFLT_NOR %s (distribution) is not supported by the front end"
+                             % [key for key in it if key.endswith("h")])
         elif name == "BC_DYNFLT_SWF":
             fault = fault or Fault()
             fault.swf_kind = int(it.get("kind", 1))
-            for key, fname in (("dc", "swf_dc"), ("mus", "swf_mus"), ("mud", "swf_mud"), ("p", "swf_p"),
-                               ("alpha", "swf_alpha")):
+            for key, fname in _SWF_DIST:
                 if key in it:
                     fault.values[fname] = float(it[key])
+            fault_dists.update(take_dists(k, it, _SWF_DIST))
         elif name == "BC_DYNFLT_RSF":
             fault = fault or Fault()
             fault.rsf_kind = int(it.get("kind", 1))
-            for key, fname in (("dc", "rsf_dc"), ("mus", "rsf_mus"), ("a", "rsf_a"), ("b", "rsf_b"),
-                               ("vstar", "rsf_vstar"), ("theta", "rsf_theta"), ("vc", "rsf_vc")):
+            for key, fname in _RSF_DIST:
                 if key in it:
                     fault.values[fname] = float(it[key])
+            fault_dists.update(take_dists(k, it, _RSF_DIST))
         elif name == "BC_DYNFLT_TWF":
             fault = fault or Fault()
             tw = fault.twf or TimeWeakening()
@@ -308,10 +367,47 @@ def deck_from_parinp(text, precision=None):
     deck.time = time
     deck.sources = src
     deck.receivers = rec
+    if fault_dists or mat_dists:
+        _evaluate(deck, fault_dists, mat_dists)
     return deck
 
 
+def _evaluate(deck, fault_dists, mat_dists):
+    """Distributions at the fault nodes (bc%coord = coord(:, node1),
+    bc_dynflt.f90:302) and at the GLL points of the elements of each
+    material tag (ngll, ngll, nelem arrays of the deck)."""
+    from .api import Grid
+    grid = Grid(deck)
+    xz = grid.coord()
+    if fault_dists:
+        if deck.fault is None:
+            raise ValueError("fault distributions without a fault")
+        n1, _ = grid.fault_nodes()
+        x, z = xz[0, n1 - 1], xz[1, n1 - 1]
+        for name, dist in fault_dists.items():
+            deck.fault.values[name] = dist(x, z)
+    if mat_dists:
+        ib = grid.ibool() - 1  # (ngll, ngll, nelem)
+        tags = grid.tags()
+        px, pz = xz[0][ib], xz[1][ib]
+        shape = ib.shape
+        for m in deck.materials:
+            md = mat_dists.get(m.tag)
+            if not md:
+                continue
+            sel = np.broadcast_to(tags == m.tag, shape)
+            props = ("rho", "c11", "c13", "c33", "c55", "c66") if m.aniso else ("rho", "cp", "cs")
+            for name in props + ("kveta",):
+                if name == "kveta" and "kveta" not in md:
+                    continue
+                arr = deck.hetero.setdefault(name, np.zeros(shape))
+                const = m.kv_eta if name == "kveta" else getattr(m, name)
+                arr[sel] = md[name](px[sel], pz[sel]) if name in md else const
+            m.hetero = True
+
+
 def load_parinp(path, precision=None):
-    """ParDeck for the Par.inp file at `path`."""
+    """ParDeck for the Par.inp file at `path` (tables named by `file=` in
+    &DIST_* blocks are read relative to its folder)."""
     with open(path) as f:
-        return deck_from_parinp(f.read(), precision)
+        return deck_from_parinp(f.read(), precision, base=os.path.dirname(os.path.abspath(path)))

@@ -14,7 +14,8 @@ It reads the reference's own test data (nothing is written from memory):
   EXAMPLES/Anisotropic/p{1..4}.tab            reference output at stations
                                               4, 18, 23, 46 (Anisotropic/write_seis.m)
   EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
-  EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox}/Par.inp
+  EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox,
+           TestFlt2D_SCEC_TPV3_inplane}/Par.inp
                                               the input decks, as text (parinp_*)
   EXAMPLES/TestAbso/data_mat/{stacey,paraxial}_PSV.mat
                                               the reference's misfits of the direct
@@ -62,7 +63,7 @@ def main(ref):
         for key in ("theta", "errp", "errs"):
             out["abso_%s_%s" % (kind, key)] = np.asarray(m[key], dtype=np.float64).ravel()
 
-    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox"):
+    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
 
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")

@@ -157,3 +157,86 @@ def test_grid_files_round_trip(tmp_path):
     raw = np.fromfile(tmp_path / "ibool_sem2d.dat", dtype="<i4")
     assert os.path.getsize(tmp_path / "ibool_sem2d.dat") == 4 * 25 * 800
     assert np.array_equal(raw[25 * 7:25 * 8], g.ibool()[:, :, 7].ravel(order="F"))
+
+
+def test_tpv3_inplane_deck_with_distributions(golden):
+    """EXAMPLES/TestFlt2D_SCEC_TPV3_inplane/Par.inp: TtH and MuSH as
+    &DIST_PWCONR rings, the Kelvin-Voigt eta as a &DIST_GAUSSIAN band along
+    the fault, a one-sided fault on the bottom side and v = 'D' on the left."""
+    d = deck_from_parinp(str(golden["parinp_TestFlt2D_SCEC_TPV3_inplane"]))
+    assert (d.ngll, d.ndof, d.nelem) == (6, 2, (70, 40))
+    assert d.fault.tags == (1, 0) and d.dirneu == [(4, "N", "D", False)] and d.absorbing == [2, 3]
+    assert d.time.kind == "newmark" and d.receivers.atnode is False and d.fault.oxi == (1, 65, 4)
+    from sem2dpack_gb300.api import Grid
+    g = Grid(d)
+    n1, _ = g.fault_nodes()
+    x = g.coord()[0, n1 - 1]
+    np.testing.assert_array_equal(d.fault.values["Tt"], np.where(x <= 1.5e3, 81.6e6, 70.0e6))
+    np.testing.assert_array_equal(d.fault.values["swf_mus"], np.where(x <= 15e3, 0.677, 1e4))
+    ib = g.ibool() - 1
+    z = g.coord()[1][ib]
+    xx = g.coord()[0][ib]
+    np.testing.assert_allclose(d.hetero["kveta"], 0.1 * np.exp(-((xx / 1e6) ** 2 + (z / 282.094) ** 2)), rtol=1e-15)
+    assert np.all(d.hetero["rho"] == 2670.0) and d.materials[0].hetero
+    P = Problem(d)
+    desc = P.desc()
+    assert desc.nflt == 70 * 5 + 1 and desc.ndir == 40 * 5 + 1
+
+
+def test_distributions(tmp_path):
+    from sem2dpack_gb300.distributions import Dist
+    x = np.array([-3.0, -1.0, 0.0, 0.5, 2.0, 5.0])
+    z = np.array([0.0, 1.0, -2.0, 0.5, 3.0, -1.0])
+    d = Dist("PWCONR", {"num": 3, "ref": [1.0, 0.0]}, [1.0, 3.0, 10.0, 20.0, 30.0])
+    r = np.hypot(x - 1.0, z)
+    np.testing.assert_array_equal(d(x, z), np.where(r <= 1, 10.0, np.where(r <= 3, 20.0, 30.0)))
+    d = Dist("ORDER0", {"xn": 2, "zn": 2}, [0.0, 0.5, 1.0, 2.0, 3.0, 4.0])
+    np.testing.assert_array_equal(d(x, z), np.where(z < 0.5, np.where(x < 0, 1.0, 2.0), np.where(x < 0, 3.0, 4.0)))
+    d = Dist("LINEAR", {"n": 3, "dim": 2}, [0.0, 1.0, 1.0, 3.0, 2.0, 4.0])
+    np.testing.assert_allclose(d(x, z), np.interp(z, [0, 1, 2], [1, 3, 4]) + np.where(z < 0, 2 * z, 0)
+                               + np.where(z > 2, (z - 2) * 1.0, 0), rtol=1e-15)
+    d = Dist("LINEAR", {"n": 2, "dim": 1, "length": 2.0}, [0.0, 0.0, 1.0, 1.0])
+    np.testing.assert_allclose(d(x, z), x, rtol=1e-13)  # the average of a line over a window is its centre value
+    d = Dist("GAUSSIAN", {"centered_at": [1.0, -1.0], "length": [2.0, 0.5], "offset": 3.0, "ampli": 2.0,
+                          "order": 2}, [])
+    np.testing.assert_allclose(d(x, z), 3 + 2 * np.exp(-(((x - 1) / 2) ** 2 + ((z + 1) / 0.5) ** 2) ** 2))
+    (tmp_path / "line.tab").write_text("-10 0\n10 0\n")
+    d = Dist("GRADIENT", {"file": "line.tab", "grad": -2.0, "valref": 5.0}, [], base=str(tmp_path))
+    np.testing.assert_allclose(d(x, z), 5.0 + 2.0 * (0.0 - z))
+    with pytest.raises(ValueError):
+        Dist("SPLINE", {}, [])
+
+
+def test_snapshot_files(tmp_path):
+    """Snapshot files of D, V, A, strain and stress written from an oracle
+    run, read back in the reference's layouts."""
+    P = Problem(workloads.plain_psv(scale=0.05, nsteps=40))
+    d = P.desc()
+    d.precision = PRECISION_FP64
+    o = po.OracleSim(d, owner=P)
+    o.run(40)
+
+    class Run:  # the getters write_snapshot calls, over the oracle
+        desc = d
+
+        def fields(self, accel=False):
+            f = o.fields()
+            return f if accel else f[:2]
+
+        def strain_stress(self):
+            return o.strain_stress()
+
+    outputs.write_snapshot(str(tmp_path), Run(), 3, "DVAES")
+    D, V, A = o.fields()
+    for c, arr in (("d", D), ("v", V), ("a", A)):
+        for k, comp in enumerate("xz"):
+            back = np.fromfile(tmp_path / ("%s%s_003_sem2d.dat" % (c, comp)), dtype="<f4")
+            assert np.array_equal(back, arr[:, k].astype(np.float32))
+    e, s = o.strain_stress()
+    N, ne = d.ngll, d.nelem
+    for pre, arr in (("e", e), ("s", s)):
+        for k, nm in enumerate(("11", "22", "12")):
+            raw = np.fromfile(tmp_path / ("%s%s_003_sem2d.dat" % (pre, nm)), dtype="<f4").reshape(ne, N * N)
+            assert np.array_equal(raw[5], arr[:, :, k, 5].ravel(order="F").astype(np.float32))
+    with pytest.raises(ValueError):
+        outputs.write_snapshot(str(tmp_path), Run(), 4, "Vc")
