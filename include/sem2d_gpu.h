@@ -46,6 +46,7 @@ extern "C" {
 /* time schemes (time.f90:122-315) */
 #define SEM2D_TIME_LEAPFROG 0
 #define SEM2D_TIME_NEWMARK 1
+#define SEM2D_TIME_HHT 2 /* explicit HHT-alpha (solver.f90:89-131)               */
 
 /* friction laws (bc_dynflt.f90:200-213) */
 #define SEM2D_FRICTION_SWF 1
@@ -198,6 +199,13 @@ typedef struct sem2d_problem_desc {
   const int *dir_node;        /* [ndir], 1-based                            */
   const int *dir_comp;        /* [ndir], 0 horizontal (SH: the only one), 1 vertical */
   const int *dir_after_fault; /* [ndir]                                     */
+
+  /* HHT-alpha (SEM2D_TIME_HHT): the forces, sources and boundary terms of
+   * a step are evaluated at d_alpha = alpha d_pred + (1-alpha) d_n,
+   * v_alpha likewise, and t + (alpha-1) dt (solve_HHT_alpha,
+   * solver.f90:89-131); beta and gamma hold the Newmark parameters the
+   * scheme derives from alpha and rho (time.f90:222-240).  1 otherwise. */
+  double alpha;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;

@@ -119,6 +119,7 @@ typedef struct sem2d_deck {
   double total_time;  /* > 0: sets nsteps                                   */
   int nsteps;
   double beta, gamma; /* &TIME_NEWMARK                                      */
+  double hht_alpha, hht_rho; /* &TIME_HHTA alpha, rho (time.f90:222-240)     */
 
   /* &SRC_DEF (FORCE mechanism, RICKER time function) */
   int nsrc;

@@ -42,7 +42,7 @@ struct oc_setup {
   int has_kv;
   /* time */
   int time_kind;
-  double dt, courant, total, beta, gamma;
+  double dt, courant, total, beta, gamma, alpha;
   int nt;
   /* mass -> inverse mass */
   double *rmass;     /* (npoin,ndof) */
@@ -788,12 +788,23 @@ static int build_time(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   double omega_max = 2.0;
   s->beta = 0.0;
   s->gamma = 0.5;
+  s->alpha = 1.0;
   if (dk->time_kind == SEM2D_TIME_NEWMARK) {
     s->beta = dk->beta;
     s->gamma = dk->gamma;
     if (s->beta < 0 || s->beta > 1 || s->gamma < 0 || s->gamma > 1)
       return seterr(err, el, "TIME_NEWMARK: parameter out of range"), -1;
     omega_max = sqrt(2.0 / s->gamma);
+  } else if (dk->time_kind == SEM2D_TIME_HHT) {
+    /* TIME_read, case 'HHT-alpha' (time.f90:222-240) */
+    double a = dk->hht_alpha, r = dk->hht_rho;
+    if (a < 0.0 || a > 1.0) return seterr(err, el, "TIME_HHTA: alpha is out of range [0,1]"), -1;
+    if (r < 0.5 || r > 1.0) return seterr(err, el, "TIME_HHTA: rho is out of range [0.5,1]"), -1;
+    s->alpha = a;
+    s->gamma = 1.5 - a;
+    double r2 = r * r, r3 = r2 * r, r4 = r3 * r, r5 = r4 * r, q = 1.0 + r;
+    s->beta = (a != 1.0) ? 1.0 - a - r * r * (r - 1.0) / ((1.0 - a) * (q * q * q)) : 0.0;
+    omega_max = sqrt(-4.0 * q * q * q * q * q / (r5 + 9.0 * r4 - 34.0 * r3 + 6.0 * r2 - 15.0 * r + 1.0));
   }
   /* TIME_init */
   double grid_cfl = max_c_dx;
@@ -814,15 +825,14 @@ static int build_time(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
 }
 
 /* ------------------------------------------------------------------ */
-static double coefA2V(const oc_setup *s) {
-  return s->time_kind == SEM2D_TIME_NEWMARK ? s->gamma * s->dt : s->dt;
+/* TIME_getCoefA2V/A2D/A2Vrhs (time.f90:426-486); alpha = 1 for Newmark */
+static int newmark_like(const oc_setup *s) {
+  return s->time_kind == SEM2D_TIME_NEWMARK || s->time_kind == SEM2D_TIME_HHT;
 }
-static double coefA2D(const oc_setup *s) {
-  return s->time_kind == SEM2D_TIME_NEWMARK ? s->beta * s->dt * s->dt : 0.0;
-}
+static double coefA2V(const oc_setup *s) { return newmark_like(s) ? s->gamma * s->dt : s->dt; }
+static double coefA2D(const oc_setup *s) { return newmark_like(s) ? s->beta * s->dt * s->dt : 0.0; }
 static double coefA2Vrhs(const oc_setup *s) {
-  /* alpha = 1 for Newmark (time.f90:476-484) */
-  return s->time_kind == SEM2D_TIME_NEWMARK ? 1.0 * coefA2V(s) : 0.5 * coefA2V(s);
+  return newmark_like(s) ? s->alpha * coefA2V(s) : 0.5 * coefA2V(s);
 }
 
 /* MAT_MASS_init (mat_mass.f90:29-61) */
@@ -1320,6 +1330,7 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
   d->dt = s->dt;
   d->beta = s->beta;
   d->gamma = s->gamma;
+  d->alpha = s->alpha;
   d->nt = s->nt;
   d->nsrc = s->nsrc;
   d->src_node = s->src_node;

@@ -81,6 +81,9 @@ struct oc_sim {
   double *pseries; /* [6*it + q]: potency of d (q < 3) and v (q >= 3) */
   /* fields */
   double *d, *v, *a;
+  double alpha;                /* HHT-alpha alpha */
+  double tshift;               /* (alpha-1) dt: the time of the boundary terms */
+  double *dal, *val;           /* HHT-alpha: d_alpha, v_alpha (NULL otherwise) */
   int it;
   int status;
 };
@@ -291,7 +294,7 @@ static void so_add(oc_sim *s, double t, double *f) {
   }
 }
 
-static void abso_apply(oc_sim *s, double *f, const double *v) {
+static void abso_apply(oc_sim *s, double *f, const double *v, const double *dsp) {
   for (int k = 0; k < s->nabs; k++) {
     size_t g = s->abs_node[k] - 1;
     for (int d = 0; d < s->ndof; d++) {
@@ -309,7 +312,7 @@ static void abso_apply(oc_sim *s, double *f, const double *v) {
     for (int c = 0; c < 2; c++) {
       double dd = 0.0;
       for (int l = 0; l < n; l++)
-        dd += s->H[l + (size_t)n * k] * s->d[(size_t)s->st_edge[l + (size_t)n * t] - 1 + (size_t)s->npoin * c];
+        dd += s->H[l + (size_t)n * k] * dsp[(size_t)s->st_edge[l + (size_t)n * t] - 1 + (size_t)s->npoin * c];
       f[g + (size_t)s->npoin * c] -= s->st_K[t + (size_t)s->nstacey * c] * dd;
     }
   }
@@ -551,7 +554,7 @@ static void dynflt_apply(oc_sim *s, double *f, const double *v, const double *d)
       s->V[k] = vnew;
       s->MU[k] = rsf_mu(s, k, s->V[k]);
       if (s->twf_kind) {
-        double mt = twf_mu(s, k, s->it * s->dt, s->D[k]);
+        double mt = twf_mu(s, k, s->it * s->dt + s->tshift, s->D[k]);
         if (mt < s->MU[k]) s->MU[k] = mt;
       }
       double strength = -s->MU[k] * sig;
@@ -574,11 +577,11 @@ static void dynflt_apply(oc_sim *s, double *f, const double *v, const double *d)
         }
         s->MU[k] = swf_mu(s, k);
         if (s->twf_kind) {
-          double mt = twf_mu(s, k, s->it * s->dt, s->D[k]);
+          double mt = twf_mu(s, k, s->it * s->dt + s->tshift, s->D[k]);
           if (mt < s->MU[k]) s->MU[k] = mt;
         }
       } else { /* time weakening alone */
-        s->MU[k] = twf_mu(s, k, s->it * s->dt, s->D[k]);
+        s->MU[k] = twf_mu(s, k, s->it * s->dt + s->tshift, s->D[k]);
       }
       double strength = s->coh[k] - s->MU[k] * sig;
       Ts[0] = T[0];
@@ -723,6 +726,7 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
   s->dir_comp = dupi(dd->dir_comp, (size_t)dd->ndir);
   s->dir_after = dupi(dd->dir_after_fault, (size_t)dd->ndir);
   s->scheme = dd->time_scheme;
+  s->alpha = dd->time_scheme == SEM2D_TIME_HHT ? dd->alpha : 1.0;
   s->dt = dd->dt;
   s->beta = dd->beta;
   s->gamma = dd->gamma;
@@ -850,26 +854,43 @@ int oc_sim_run(oc_sim *s, int nsteps) {
   int nd = s->ndof;
   size_t nn = (size_t)s->npoin * nd;
   double *d = s->d, *v = s->v, *a = s->a;
+  const int hht = s->scheme == SEM2D_TIME_HHT;
+  if (hht && !s->dal) {
+    s->dal = xcalloc(nn, sizeof(double));
+    s->val = xcalloc(nn, sizeof(double));
+  }
   for (int st = 0; st < nsteps; st++) {
     s->it++;
     double t = s->it * s->dt;
-    if (s->scheme == SEM2D_TIME_NEWMARK) {
+    if (s->scheme == SEM2D_TIME_NEWMARK || hht) {
+      /* predictors (solver.f90:59-60, 110-111); HHT-alpha keeps
+       * d_alpha = alpha d_pred + (1-alpha) d_n and v_alpha alike (:106-113) */
       double cd = (0.5 - s->beta) * s->dt * s->dt, cv = (1.0 - s->gamma) * s->dt;
       for (size_t q = 0; q < nn; q++) {
+        double d0 = d[q], v0 = v[q];
         d[q] = d[q] + s->dt * v[q] + cd * a[q];
         v[q] = v[q] + cv * a[q];
+        if (hht) {
+          s->dal[q] = s->alpha * d[q] + (1.0 - s->alpha) * d0;
+          s->val[q] = s->alpha * v[q] + (1.0 - s->alpha) * v0;
+        }
       }
     } else {
       for (size_t q = 0; q < nn; q++) d[q] = d[q] + s->dt * v[q];
     }
-    compute_fint(s, a, d, v); /* f aliases accel */
+    const double *df = hht ? s->dal : d, *vf = hht ? s->val : v;
+    /* HHT-alpha evaluates sources and boundaries at t + (alpha-1) dt
+     * (solver.f90:116-122) */
+    if (hht) t = t + (s->alpha - 1.0) * s->dt;
+    s->tshift = hht ? (s->alpha - 1.0) * s->dt : 0.0;
+    compute_fint(s, a, df, vf); /* f aliases accel */
     so_add(s, t, a);
-    abso_apply(s, a, v);
+    abso_apply(s, a, vf, df);
     dirneu_apply(s, a, 0);
     if (s->nflt) dynflt_apply(s, a, v, d);
     dirneu_apply(s, a, 1);
     for (size_t q = 0; q < nn; q++) a[q] = s->rmass[q] * a[q];
-    if (s->scheme == SEM2D_TIME_NEWMARK) {
+    if (s->scheme == SEM2D_TIME_NEWMARK || hht) {
       double cv = s->gamma * s->dt, cd = s->beta * s->dt * s->dt;
       for (size_t q = 0; q < nn; q++) {
         v[q] = v[q] + cv * a[q];
@@ -966,6 +987,7 @@ void oc_sim_free(oc_sim *s) {
   if (!s) return;
   void *ptrs[] = {s->ibool, s->H, s->acoef, s->kveta, s->rmass, s->abs_node, s->abs_C,
                   s->st_node, s->st_k, s->st_edge, s->st_K, s->dir_node, s->dir_comp, s->dir_after,
+                  s->dal, s->val,
                   s->src_node, s->src_dir, s->src_f0, s->src_t0, s->src_amp, s->src_rel,
                   s->src_tdelay, s->rec_node, s->rec_elem, s->rec_interp, s->sis, s->node1,
                   s->node2, s->n1, s->B, s->invM1, s->invM2, s->Z, s->T0, s->coh, s->swf_dc,

@@ -22,6 +22,7 @@ SEM2D_E_TIMEOUT = -8
 
 TIME_LEAPFROG = 0
 TIME_NEWMARK = 1
+TIME_HHT = 2
 FRICTION_SWF = 1
 FRICTION_RSF = 2
 FRICTION_TWF = 3
@@ -95,6 +96,7 @@ class ProblemDesc(C.Structure):
         ("nstacey", c_int), ("stacey_node", P_int), ("stacey_k", P_int), ("stacey_edge", P_int),
         ("stacey_K", P_double),
         ("ndir", c_int), ("dir_node", P_int), ("dir_comp", P_int), ("dir_after_fault", P_int),
+        ("alpha", c_double),
     ]
 
 
@@ -133,6 +135,7 @@ class Deck(C.Structure):
         ("flt_value", c_double * FP_NPARAM), ("flt_array", P_double * FP_NPARAM),
         ("time_kind", c_int), ("dt", c_double), ("courant", c_double),
         ("total_time", c_double), ("nsteps", c_int), ("beta", c_double), ("gamma", c_double),
+        ("hht_alpha", c_double), ("hht_rho", c_double),
         ("nsrc", c_int), ("src_coord", P_double), ("src_tdelay", P_double),
         ("src_ampli", P_double),
         ("ricker_f0", c_double), ("ricker_onset", c_double), ("ricker_ampli", c_double),

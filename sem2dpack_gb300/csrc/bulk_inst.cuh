@@ -75,6 +75,8 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.cpred = real(c.cpred);
   p.cd2 = real(c.cd2);
   p.cb = real(c.cb);
+  p.cal = real(c.cal);
+  p.cpa = real(c.cpa);
   p.kd2 = c.kd2;
   p.nmat = c.nmat;
   p.has_kv = c.has_kv;

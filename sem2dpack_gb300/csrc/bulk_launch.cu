@@ -96,7 +96,7 @@ int strip_width(int N) {
 
 int strip_plane_count(int ndof, int nmat, int mat_elem, int scheme) {
   // displacement, node material, velocity, acceleration (Newmark), inverse mass
-  return ndof + (mat_elem == 0 ? nmat : 0) + ndof + (scheme == 1 ? ndof : 0) + 1;
+  return ndof + (mat_elem == 0 ? nmat : 0) + ndof + (scheme != 0 ? ndof : 0) + 1;
 }
 
 std::vector<int> tile_rows(int N, int nz, const int *row0, int TZ) {

@@ -50,6 +50,7 @@ struct BulkConfig {
   double *sis = nullptr;
   int scheme = 0, kd2 = 0;
   double dt = 0, cv = 0, cpred = 0, cd2 = 0, cb = 0;
+  double cal = 0, cpa = 0;  // HHT-alpha: 1 - alpha; alpha (1 - gamma) dt
   double width = 0;  // 2.5D seismogenic width, 0 = 2D
   int *error = nullptr;  // device error flag
   int chunk_shift = 0;   // chunk scheduled first (the fault's)

@@ -298,7 +298,7 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
     th_new = th2;
     mu = rsf_mu(p, k, vnew, th2);
     if (p.twf_kind) {
-      const double mt = twf_mu(p, k, it * p.dt, Dk);
+      const double mt = twf_mu(p, k, it * p.dt + p.tshift, Dk);
       if (mt < mu) mu = mt;
     }
     T[0] = copysign(fabs(-mu * sig), T[0]);
@@ -321,11 +321,11 @@ __device__ void fault_node_update(const FaultParams<real> &p, int k, int it, con
       th_new = th;
       mu = swf_mu_of(p.swf_kind, swn, th);
       if (p.twf_kind) {
-        const double mt = twf_mu(p, k, it * p.dt, Dk);
+        const double mt = twf_mu(p, k, it * p.dt + p.tshift, Dk);
         if (mt < mu) mu = mt;
       }
     } else {  // time weakening alone
-      mu = twf_mu(p, k, it * p.dt, Dk);
+      mu = twf_mu(p, k, it * p.dt + p.tshift, Dk);
     }
     const double strength = cohk - mu * sig;
     Ts[0] = T[0];

@@ -632,7 +632,7 @@ void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
 struct sem2d_problem {
   const sem2d_grid *g = nullptr;
   int ndof = 0, time_kind = 0, nt = 0;
-  double dt = 0, courant = 0, beta = 0, gamma = 0.5;
+  double dt = 0, courant = 0, beta = 0, gamma = 0.5, alpha = 1.0;
   std::vector<double> Kx, Kz, la, mu, mux, rho, cp, cs, kveta;
   bool has_kv = false;
   std::vector<double> mass;  // becomes rmass
@@ -772,6 +772,19 @@ void build_time(sem2d_problem &P, const sem2d_deck &dk) {
     if (P.beta < 0 || P.beta > 1 || P.gamma < 0 || P.gamma > 1)
       throw BuildError("TIME_NEWMARK: parameter out of range");
     omega = std::sqrt(2.0 / P.gamma);
+  } else if (dk.time_kind == SEM2D_TIME_HHT) {
+    // TIME_read 'HHT-alpha' (time.f90:222-240): second order, gamma = 3/2 -
+    // alpha, beta from alpha and the spectral radius rho
+    const double a = dk.hht_alpha, r = dk.hht_rho;
+    if (a < 0.0 || a > 1.0) throw BuildError("TIME_HHTA: alpha is out of range [0,1]");
+    if (r < 0.5 || r > 1.0) throw BuildError("TIME_HHTA: rho is out of range [0.5,1]");
+    P.alpha = a;
+    P.gamma = 1.5 - a;
+    const double q = 1.0 + r, r2 = r * r, r3 = r2 * r, r4 = r3 * r, r5 = r4 * r;
+    P.beta = a != 1.0 ? 1.0 - a - r * r * (r - 1.0) / ((1.0 - a) * (q * q * q)) : 0.0;
+    omega = std::sqrt(-4.0 * (q * q * q * q * q) / (r5 + 9.0 * r4 - 34.0 * r3 + 6.0 * r2 - 15.0 * r + 1.0));
+  } else if (dk.time_kind != SEM2D_TIME_LEAPFROG) {
+    throw BuildError("TIME: unknown time scheme");
   }
   if (dt > 0.0) {
     courant = max_c_dx * dt;
@@ -786,10 +799,13 @@ void build_time(sem2d_problem &P, const sem2d_deck &dk) {
   P.nt = nsteps;
 }
 
-double coefA2V(const sem2d_problem &P) { return P.time_kind == SEM2D_TIME_NEWMARK ? P.gamma * P.dt : P.dt; }
-double coefA2D(const sem2d_problem &P) { return P.time_kind == SEM2D_TIME_NEWMARK ? P.beta * P.dt * P.dt : 0.0; }
+// TIME_getCoefA2V, TIME_getCoefA2D, TIME_getCoefA2Vrhs (time.f90:426-486);
+// alpha is 1 for Newmark
+bool newmark_like(const sem2d_problem &P) { return P.time_kind == SEM2D_TIME_NEWMARK || P.time_kind == SEM2D_TIME_HHT; }
+double coefA2V(const sem2d_problem &P) { return newmark_like(P) ? P.gamma * P.dt : P.dt; }
+double coefA2D(const sem2d_problem &P) { return newmark_like(P) ? P.beta * P.dt * P.dt : 0.0; }
 double coefA2Vrhs(const sem2d_problem &P) {
-  return P.time_kind == SEM2D_TIME_NEWMARK ? 1.0 * coefA2V(P) : 0.5 * coefA2V(P);
+  return newmark_like(P) ? P.alpha * coefA2V(P) : 0.5 * coefA2V(P);
 }
 
 // MAT_MASS_init (mat_mass.f90:29-61)
@@ -1314,6 +1330,7 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
   d->dt = P->dt;
   d->beta = P->beta;
   d->gamma = P->gamma;
+  d->alpha = P->alpha;
   d->nt = P->nt;
   d->nsrc = int(P->src_node.size());
   d->src_node = VPTR(P->src_node);

@@ -63,6 +63,7 @@ struct FaultParams {
   int scheme;
   double dt, cv, cpred, cd2;
   double cb;            // Newmark corrector beta dt^2
+  double tshift;        // time of the boundary terms minus it dt: (alpha-1) dt
   const unsigned char *dir_zero;  // [k] bits side*2+c: force zeroed after the fault, or null
   int *step;            // incremented by the last block (stand-alone kernel)
   unsigned int *done;   // block completion counter (reset by the last block)
@@ -127,9 +128,11 @@ struct BulkParams {
   const double *rec_w;        // [r*npts + q] weight
   double *sis;
   // time scheme
-  int scheme;             // 0 leapfrog, 1 Newmark (beta = 0)
+  int scheme;             // 0 leapfrog, 1 Newmark, 2 HHT-alpha
   real dt, cv, cpred, cd2;// cv: coef a->v, cpred: (1-gamma)dt, cd2: (0.5-beta)dt^2
   real cb;                // Newmark corrector beta dt^2 (0: leapfrog or beta = 0)
+  real cal, cpa;          // scheme 2 (HHT-alpha): 1 - alpha, and alpha (1 - gamma) dt, the
+                          // acceleration coefficient of v_alpha (cpred otherwise)
   int kd2;
   real width;             // 2.5D seismogenic width W, 0 for a 2D problem
   int nmat;               // material planes (node layout) or arrays (element layout)

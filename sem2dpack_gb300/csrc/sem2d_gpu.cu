@@ -48,8 +48,8 @@ struct sem2d_handle {
   int kd2 = 0;
   double width = 0;  // 2.5D seismogenic width, 0 = 2D
   FaultScalars fs;
-  int N = 0, ndof = 0, nelem = 0, npoin = 0, nt = 0, mixed = 0, scheme = 0;
-  double dt = 0, beta = 0, gamma = 0.5;
+  int N = 0, ndof = 0, nelem = 0, npoin = 0, nt = 0, mixed = 0, scheme = 0;  // scheme 2: HHT-alpha
+  double dt = 0, beta = 0, gamma = 0.5, alpha = 1.0;
   int nx = 0, nz = 0, LX = 0, LZ = 0, pitch = 0;
   long long plane = 0;
   std::vector<int> row0;             // [nz+1]
@@ -710,12 +710,13 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.nsamp = h->fnsamp;
   f.series = h->fd[F_SERIES];
   f.pot = h->potency ? h->fd[F_POT] : nullptr;
-  f.scheme = h->scheme;
+  f.scheme = h->scheme ? 1 : 0;  // the fault node update is the same for HHT-alpha
   f.dt = h->dt;
-  f.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
+  f.cv = h->scheme ? h->gamma * h->dt : h->dt;
   f.cpred = (1.0 - h->gamma) * h->dt;
   f.cd2 = (0.5 - h->beta) * h->dt * h->dt;
-  f.cb = h->scheme == 1 ? h->beta * h->dt * h->dt : 0.0;
+  f.cb = h->scheme ? h->beta * h->dt * h->dt : 0.0;
+  f.tshift = (h->alpha - 1.0) * h->dt;  // HHT-alpha boundary time (solver.f90:118-122)
   f.step = h->d_step;
   f.done = h->d_done;
   f.error = h->d_error;
@@ -803,10 +804,12 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   }
   bc.scheme = h->scheme;
   bc.dt = h->dt;
-  bc.cv = h->scheme == 1 ? h->gamma * h->dt : h->dt;
+  bc.cv = h->scheme ? h->gamma * h->dt : h->dt;
   bc.cpred = (1.0 - h->gamma) * h->dt;
   bc.cd2 = (0.5 - h->beta) * h->dt * h->dt;
-  bc.cb = h->scheme == 1 ? h->beta * h->dt * h->dt : 0.0;
+  bc.cb = h->scheme ? h->beta * h->dt * h->dt : 0.0;
+  bc.cal = 1.0 - h->alpha;
+  bc.cpa = h->alpha * ((1.0 - h->gamma) * h->dt);
   bc.kd2 = h->kd2;
   bc.width = h->width;
   bc.chunk_shift = h->fault_chunk;
@@ -1206,7 +1209,7 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
     // acceleration receivers there, and displacement ones when the Newmark
     // corrector adds beta dt^2 a, are sampled after it, by the receiver
     // kernel
-    const bool corrected = h->scheme == 1 && h->beta != 0.0;
+    const bool corrected = h->scheme == 2 || (h->scheme == 1 && h->beta != 0.0);
     for (size_t r = 0; r < rec_jn.size(); ++r)
       if ((h->rec_field != 'D' || corrected) && (rec_jn[r] == h->jf1 || rec_jn[r] == h->jf2))
         h->rec_separate = true;
@@ -1334,11 +1337,16 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
   h->npoin = d->npoin;
   h->nt = d->nt;
   h->mixed = d->precision == SEM2D_PRECISION_MIXED;
-  h->scheme = d->time_scheme == SEM2D_TIME_NEWMARK ? 1 : 0;
+  h->scheme = d->time_scheme == SEM2D_TIME_NEWMARK ? 1 : d->time_scheme == SEM2D_TIME_HHT ? 2 : 0;
+  if (d->time_scheme != SEM2D_TIME_LEAPFROG && !h->scheme) return set_err(h, SEM2D_E_ARG, "unknown time scheme");
   h->dt = d->dt;
   h->beta = d->beta;
   h->gamma = h->scheme ? d->gamma : 0.5;
-  h->keep_accel = h->scheme == 1 || d->rec_field == 'A';
+  h->alpha = h->scheme == 2 ? d->alpha : 1.0;
+  if (h->scheme == 2 && !(h->alpha >= 0.0 && h->alpha <= 1.0)) return set_err(h, SEM2D_E_ARG, "alpha out of [0,1]");
+  if (h->scheme == 2 && d->nstacey > 0)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey boundaries with HHT-alpha are not supported on the GPU path");
+  h->keep_accel = h->scheme != 0 || d->rec_field == 'A';
   if (shared) {
     h->stream = shared;
     h->owns_stream = false;
@@ -1410,7 +1418,8 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
       sJ[s] = int(h->glob2lat[p] / h->pitch);
       const double td = d->src_tdelay ? d->src_tdelay[s] : 0.0, rel = d->src_relamp ? d->src_relamp[s] : 1.0;
       for (int it = 1; it <= h->nt; ++it) {
-        const double t = it * d->dt;
+        // HHT-alpha adds the sources at t + (alpha-1) dt (solver.f90:116-117)
+        const double t = it * d->dt + (h->alpha - 1.0) * d->dt;
         double a = ricker(t - td, d->src_f0[s], d->src_t0[s], d->src_ampli[s]);
         a = a * rel;
         for (int c = 0; c < h->ndof; ++c)
@@ -1435,7 +1444,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     // corrector, which needs the new accelerations) reads nodes owned by
     // several CTAs: sampled by a separate kernel after the step; everything
     // else is sampled inside the bulk kernel by the CTA that owns the receiver
-    h->rec_separate = !d->rec_node && (h->rec_field != 'D' || (h->scheme == 1 && h->beta != 0.0));
+    h->rec_separate = !d->rec_node && (h->rec_field != 'D' || h->scheme == 2 || (h->scheme == 1 && h->beta != 0.0));
   }
   if ((st = dalloc(h, &h->sis, (size_t)std::max(h->rec_nsamp, 1) * std::max(h->nrec, 1) * h->ndof))) return st;
   std::vector<int> rec_ex, rec_ez, rec_jn;  // element owning each receiver (march units), node row
@@ -2289,7 +2298,7 @@ int sem2d_gpu_get_fields(sem2d_handle *h, double *displ, double *veloc, double *
     for (int c = 0; c < h->ndof; ++c)
       for (int p = 0; p < h->npoin; ++p) dst[k][p + (size_t)h->npoin * c] = tmp[c * h->plane + h->glob2lat[p]];
   }
-  if (displ && h->steps > 0 && h->scheme == 1 && h->beta != 0.0) {
+  if (displ && h->steps > 0 && h->scheme != 0 && h->beta != 0.0) {
     // the buffer holds the step's predictor: add the corrector beta dt^2 a^n
     // (solver.f90:82)
     const double cb = h->beta * h->dt * h->dt;
@@ -2326,7 +2335,7 @@ int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress)
   cudaMemcpy(dH, h->H.data(), sizeof(double) * NN, cudaMemcpyHostToDevice);
   const void *D = h->steps > 0 ? h->D[1 - h->cur] : h->D[h->cur];
   void *Dc = nullptr;
-  if (h->steps > 0 && h->scheme == 1 && h->beta != 0.0) {
+  if (h->steps > 0 && h->scheme != 0 && h->beta != 0.0) {
     // displacement d^n = the step's predictor + beta dt^2 a^n (solver.f90:82)
     const long long n = (long long)h->plane * h->ndof;
     const double cb = h->beta * h->dt * h->dt;

@@ -156,7 +156,8 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
   const int nm = MAT == kMatNode ? p.nmat : 0;
   const int pV = NDOF + nm, pA = pV + NDOF, pR = NP - 1;
   const bool iso = FAST || p.mat_iso;
-  const bool newmark = !FAST && p.scheme == 1;
+  const bool newmark = !FAST && p.scheme != 0;  // Newmark or HHT-alpha
+  const bool hht = !FAST && p.scheme == 2;
   const bool kv = !FAST && p.has_kv;
   const real width = FAST ? real(0) : p.width;
 
@@ -283,6 +284,18 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
     const real *sV = sg + size_t(pV) * PS;
     const real *sA = sg + size_t(pA) * PS;
     const real *sRm = sg + size_t(pR) * PS;
+    if (hht) {
+      // HHT-alpha: the forces see d_alpha = alpha d_pred + (1-alpha) d_n
+      // = d_pred - (1-alpha)(dt v_n + (1/2-beta) dt^2 a_n) (solver.f90:
+      // 106-113); the stage holds d_pred, v_n and a_n
+      real *sDw = const_cast<real *>(sD);
+      for (int q = tid; q < NDOF * PS; q += kStripThreads) {
+        const int c = q / PS, o = q - c * PS;
+        sDw[q] = sDw[q] - p.cal * (p.dt * sV[c * PS + o] + p.cd2 * sA[c * PS + o]);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // the stage is refilled by bulk copies
+      __syncthreads();
+    }
 
     // ---- element forces of the batch into the scratch areas ----
     {
@@ -331,7 +344,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           real u = sD[cc * PS + idx];
           if constexpr (KV) {
             real v = sV[cc * PS + idx];
-            if (newmark) v = v + p.cpred * sA[cc * PS + idx];
+            if (newmark) v = v + (hht ? p.cpa : p.cpred) * sA[cc * PS + idx];  // v_pred or v_alpha
             u = u + kve[i + N * j] * v;
           }
           return u;
@@ -608,12 +621,17 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
         for (int c = 0; c < NDOF; ++c) {
           real fc = f[c];
           real vp = sV[c * PS + sidx];
-          if (newmark) vp = vp + p.cpred * sA[c * PS + sidx];
+          real vd = vp;  // the dashpots' velocity: v_alpha under HHT-alpha (bc_gen.f90:295)
+          if (newmark) {
+            const real an = sA[c * PS + sidx];
+            vd = vp + (hht ? p.cpa : p.cpred) * an;
+            vp = vp + p.cpred * an;
+          }
           real rm;
           if (sp >= 0) {
             const int so = c * nslot + sp;
-            fc = fc - p.per_Ca[so] * vp;
-            fc = fc - p.per_Cb[so] * vp;
+            fc = fc - p.per_Ca[so] * vd;
+            fc = fc - p.per_Cb[so] * vd;
             if (p.per_kd) fc = fc - p.per_kd[so];
             if (p.per_dir && ((p.per_dir[sp] >> c) & 1)) fc = real(0);  // bc_dirneu.f90:155-167
             rm = p.per_rm[so];
@@ -626,7 +644,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           }
           const real a = rm * fc;
           const real vnew = vp + p.cv * a;
-          real dcur = sD[c * PS + sidx];
+          real dcur = hht ? p.Dcur[c * p.plane + g] : sD[c * PS + sidx];  // the stage holds d_alpha
           // Newmark corrector d += beta dt^2 a (solver.f90:81-82), then the
           // next step's predictor d + dt v + (1/2 - beta) dt^2 a (:59)
           if (newmark && p.cb != real(0)) dcur = dcur + p.cb * a;
@@ -665,11 +683,12 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           const int jj = J - Jlo;
           if (jj < 0 || jj >= nr || s_stat[jj] != 1) continue;
           // displacement after the step: the predictor plus the corrector
+          const real dp = hht ? p.Dcur[c * p.plane + (long long)J * p.pitch + I]
+                              : sD[c * PS + jj * TWp + xo + (I - Ia)];
           val = p.rec_field == 'D'
                     ? (newmark && p.cb != real(0)
-                           ? double(sD[c * PS + jj * TWp + xo + (I - Ia)] +
-                                    p.cb * p.Anext[c * p.plane + (long long)J * p.pitch + I])
-                           : double(sD[c * PS + jj * TWp + xo + (I - Ia)]))
+                           ? double(dp + p.cb * p.Anext[c * p.plane + (long long)J * p.pitch + I])
+                           : double(dp))
                 : p.rec_field == 'V' ? double(p.Vnext[c * p.plane + (long long)J * p.pitch + I])
                                      : double(p.Anext[c * p.plane + (long long)J * p.pitch + I]);
         } else {  // interpolated displacement over an element of this batch

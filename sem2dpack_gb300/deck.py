@@ -82,7 +82,7 @@ class Fault:
 
 @dataclass
 class Time:
-    """&TIME (+ &TIME_NEWMARK) (time.f90:122-315)."""
+    """&TIME (+ &TIME_NEWMARK or &TIME_HHTA) (time.f90:122-315)."""
     kind: str = "leapfrog"
     dt: float = 0.0
     courant: float = 0.5
@@ -90,6 +90,8 @@ class Time:
     nsteps: int = 0
     beta: float = 0.0
     gamma: float = 0.5
+    alpha: float = 0.5   # &TIME_HHTA (kind 'hht-alpha')
+    rho: float = 0.5
 
 
 @dataclass
@@ -234,7 +236,11 @@ class ParDeck:
                     keep.append(arr)
                     d.flt_array[i] = _dptr(arr)
         t = self.time
-        d.time_kind = abi.TIME_NEWMARK if t.kind.lower() == "newmark" else abi.TIME_LEAPFROG
+        kinds = {"leapfrog": abi.TIME_LEAPFROG, "newmark": abi.TIME_NEWMARK, "hht-alpha": abi.TIME_HHT}
+        if t.kind.lower() not in kinds:
+            raise ValueError("time scheme %s is not on the GPU path" % t.kind)
+        d.time_kind = kinds[t.kind.lower()]
+        d.hht_alpha, d.hht_rho = t.alpha, t.rho
         d.dt, d.courant, d.total_time, d.nsteps = t.dt, t.courant, t.total_time, t.nsteps
         d.beta, d.gamma = t.beta, t.gamma
         s = self.sources

@@ -194,7 +194,9 @@ def read_grid(path):
 def write_snapshot(path, solver, index, fields="V"):
     """The binary snapshot files of one output time for the SNAP_DEF
     `fields` letters D, V, A (node fields), E (strain) and S (stress);
-    `index` is the NNN of the file names.  The divergence and curl (d, c)
+    `index` is the NNN of the file names; A needs a handle that keeps the
+    accelerations (Newmark, HHT-alpha or 'A' receivers).  The divergence and
+    curl (d, c)
     are not written; nor is S for Kelvin-Voigt materials, whose snapshot
     stress the reference takes from d + eta v (MAT_stress_dv,
     mat_gen.f90:626-641) while the GPU getter gives the elastic stress of d."""

@@ -20,7 +20,7 @@ between blocks (``#`` comments, anything after the ``/``) is ignored.
                 kind 'DIRNEU' + &BC_DIRNEU h, v (bc_dirneu.f90:50-112),
                 kind 'DYNFLT' + &BC_DYNFLT / _SWF / _RSF / _TWF / _NOR with
                 scalar values (bc_dynflt*.f90)
-  &TIME         kind, Dt, Courant, TotalTime, NbSteps + &TIME_NEWMARK
+  &TIME         kind, Dt, Courant, TotalTime, NbSteps + &TIME_NEWMARK or &TIME_HHTA alpha, rho
                 beta, gamma (time.f90:122-315)
   &SRC_DEF      stf='RICKER', mechanism='FORCE', coord + &STF_RICKER f0,
                 onset, ampli + &SRC_FORCE angle (src_gen.f90, stf_ricker.f90)
@@ -49,7 +49,7 @@ from .distributions import Dist
 
 __all__ = ["read_namelists", "read_blocks", "deck_from_parinp", "load_parinp"]
 
-TIME_KINDS = ("leapfrog", "newmark")
+TIME_KINDS = ("leapfrog", "newmark", "hht-alpha")
 
 _TOKEN = re.compile(r"""'[^']*'|"[^"]*"|[&/=,]|[^\s&/=,'"]+""")
 
@@ -333,6 +333,9 @@ def deck_from_parinp(text, precision=None, base=None):
         elif name == "TIME_NEWMARK":
             time.beta = float(it.get("beta", 0.0))
             time.gamma = float(it.get("gamma", 0.5))
+        elif name == "TIME_HHTA":
+            time.alpha = float(it.get("alpha", 0.5))
+            time.rho = float(it.get("rho", 0.5))
         elif name == "SRC_DEF":
             if str(it.get("stf", "RICKER")).upper() != "RICKER" or \
                     str(it.get("mechanism", "FORCE")).upper() != "FORCE":

@@ -66,7 +66,9 @@ def test_snapshots_from_the_gpu(tmp_path):
     strain and stress records, against the FP64 oracle (FP32 files)."""
     from oracle import pyoracle as po
     from sem2dpack_gb300 import PRECISION_FP64, workloads
-    P = Problem(workloads.plain_psv(scale=0.1, nsteps=100))
+    dk = workloads.plain_psv(scale=0.1, nsteps=100)
+    dk.time.kind = "newmark"  # a handle keeps accelerations under Newmark (or for 'A' receivers)
+    P = Problem(dk)
     d = P.desc()
     d.precision = PRECISION_FP64
     g = Solver(d, owner=P)

@@ -118,3 +118,24 @@ def test_reference_warnings_abort():
     dk.sources.onset = 0.05  # onset < 1/f0 (stf_ricker.f90:63-68)
     with pytest.raises(Sem2dError):
         Problem(dk)
+
+
+def test_hht_alpha_problem_bit_exact():
+    """&TIME kind='HHT-alpha' + &TIME_HHTA (time.f90:222-240): gamma = 3/2 -
+    alpha, beta from alpha and rho, the absorbing fold with alpha gamma dt
+    (TIME_getCoefA2Vrhs, time.f90:467-486), on a fault deck."""
+    from sem2dpack_gb300.deck import Time
+    dk, g = workloads.sh_rupture(scale=0.1, nsteps=200)
+    dk.time = Time(kind="hht-alpha", nsteps=200, courant=0.5, alpha=0.7, rho=0.7)
+    P = Problem(dk, g)
+    O = po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    assert (a.alpha, a.beta, a.gamma) == (b.alpha, b.beta, b.gamma)
+    assert a.alpha == 0.7 and abs(a.gamma - 0.8) < 1e-15
+    r = 0.7
+    assert abs(a.beta - (1 - 0.7 - r * r * (r - 1) / (0.3 * (1 + r) ** 3))) < 1e-15
+    assert a.flt_coefA2D == a.beta * a.dt ** 2
+    dk.time.alpha = 1.5
+    with pytest.raises(Exception):
+        Problem(dk, g)

@@ -240,3 +240,8 @@ def test_snapshot_files(tmp_path):
             assert np.array_equal(raw[5], arr[:, :, k, 5].ravel(order="F").astype(np.float32))
     with pytest.raises(ValueError):
         outputs.write_snapshot(str(tmp_path), Run(), 4, "Vc")
+
+
+def test_hht_alpha_time_block():
+    d = deck_from_parinp("&TIME TotalTime=1d0, courant=0.3d0, kind='HHT-alpha' / &TIME_HHTA alpha=0.6d0, rho=0.9d0 /")
+    assert (d.time.kind, d.time.alpha, d.time.rho) == ("hht-alpha", 0.6, 0.9)
