@@ -166,7 +166,7 @@ def deck_from_parinp(text, precision=None, base=None):
                 continue
             want = "DIST_" + str(v).strip().upper()
             q = pos
-            while q < len(blocks3) and (q in consumed or blocks3[q][0] != want):
+            while q < len(blocks3) and blocks3[q][0] != want:
                 q += 1
             if q >= len(blocks3):
                 raise ValueError("&%s %sH='%s': no &%s block follows" % (blocks3[j][0], key, v, want))
@@ -218,13 +218,22 @@ def deck_from_parinp(text, precision=None, base=None):
             kinds = [s.upper() for s in kinds]
             if any(s not in ("ELAST", "KV") for s in kinds):
                 raise ValueError("material kind %s is not on the GPU path" % kinds)
-            j = k + 1
+            # MAT_read (mat_gen.f90:134-195): each kind's block is the first
+            # of its name after this &MATERIAL block (namelist reads search
+            # forward), so materials may share one &MAT_ELASTIC
             md = {}
-            while j < len(blocks) and (blocks[j][0] in ("MAT_ELASTIC", "MAT_KV") or j in consumed):
+            for kname in kinds:
+                want = "MAT_ELASTIC" if kname == "ELAST" else "MAT_KV"
+                j = k + 1
+                while j < len(blocks) and blocks[j][0] != want:
+                    j += 1
+                if j >= len(blocks):
+                    if kname == "ELAST":
+                        raise ValueError("&MATERIAL tag=%d: no &MAT_ELASTIC block follows" % m.tag)
+                    continue
                 bn, b = blocks[j]
-                if j in consumed:
-                    pass
-                elif bn == "MAT_ELASTIC":
+                consumed.add(j)
+                if bn == "MAT_ELASTIC":
                     # MAT_ELAST_read (mat_elastic.f90:102-135): rho, then cp, cs or the c_ij
                     aniso = any(c in b or c + "h" in b for c in ("c11", "c55"))
                     props = ("rho", "c11", "c13", "c33", "c55", "c66") if aniso else ("rho", "cp", "cs")
@@ -236,12 +245,9 @@ def deck_from_parinp(text, precision=None, base=None):
                     md.update(take_dists(j, b, [("eta", "kveta")]))
                     m.kv_eta = float(b.get("eta", 0.0))
                     m.kv_etaxdt = bool(b.get("etaxdt", True))
-                j += 1
             if md:
                 mat_dists[m.tag] = md
             mats.append(m)
-            k = j
-            continue
         elif name == "BC_DEF":
             kind = str(it.get("kind", "")).upper()
             tags = it.get("tags", it.get("tag"))

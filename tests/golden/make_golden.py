@@ -15,8 +15,14 @@ It reads the reference's own test data (nothing is written from memory):
                                               4, 18, 23, 46 (Anisotropic/write_seis.m)
   EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
   EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox,
-           TestFlt2D_SCEC_TPV3_inplane}/Par.inp
+           TestFlt2D_SCEC_TPV3_inplane,RateState}/Par.inp
                                               the input decks, as text (parinp_*)
+  EXAMPLES/RateState/{Ux,Vx,Tau}_{0,3,6,9}km_ascii
+                                              the reference's slip, slip rate and shear
+                                              stress change every step at x = 0, 3, 6,
+                                              9 km of its rate-and-state deck
+                                              (RateState/Par.inp; provenance of the
+                                              traces not recorded: a loose check)
   EXAMPLES/TestAbso/data_mat/{stacey,paraxial}_PSV.mat
                                               the reference's misfits of the direct
                                               P (errp) and S (errs) waves against
@@ -63,7 +69,11 @@ def main(ref):
         for key in ("theta", "errp", "errs"):
             out["abso_%s_%s" % (kind, key)] = np.asarray(m[key], dtype=np.float64).ravel()
 
-    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane"):
+    for q in ("Ux", "Vx", "Tau"):
+        out["ratestate_" + q] = np.stack([np.loadtxt(os.path.join(ex, "RateState", "%s_%dkm_ascii" % (q, x)))
+                                          for x in (0, 3, 6, 9)])
+
+    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
 
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")

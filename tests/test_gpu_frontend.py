@@ -86,3 +86,15 @@ def test_snapshots_from_the_gpu(tmp_path):
         raw = np.fromfile(tmp_path / ("%s12_001_sem2d.dat" % pre), dtype="<f4").reshape(d.nelem, -1)
         ref = np.transpose(arr[:, :, 2, :], (2, 1, 0)).reshape(d.nelem, -1)
         np.testing.assert_allclose(raw, ref, rtol=1e-6, atol=1e-6 * np.abs(ref).max())
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_ratestate_example_against_reference_traces(golden, precision):
+    from sem2dpack_gb300 import PRECISION_FP64
+    from test_ratestate_example import check_ratestate
+    P = Problem(deck_from_parinp(str(golden["parinp_RateState"])))
+    d = P.desc()
+    d.precision = PRECISION_FP64 if precision == 0 else PRECISION_MIXED
+    g = Solver(d, owner=P)
+    g.run()
+    check_ratestate(P, g.fault_series(), golden)
