@@ -206,6 +206,14 @@ typedef struct sem2d_problem_desc {
    * solver.f90:89-131); beta and gamma hold the Newmark parameters the
    * scheme derives from alpha and rho (time.f90:222-240).  1 otherwise. */
   double alpha;
+
+  /* ---- periodic sides (&BC_DEF kind='PERIOD', bc_periodic.f90:42-104):
+   * node pairs (master, slave) whose forces are summed before the other
+   * boundary terms and shared (BC_PERIO_set_field, :77-88); rmass already
+   * holds the summed mass. */
+  int nperio;
+  const int *perio_master; /* [nperio], 1-based                             */
+  const int *perio_slave;  /* [nperio], 1-based                             */
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;

@@ -57,6 +57,7 @@ typedef struct sem2d_material {
 #define SEM2D_BC_ABSORB 1
 #define SEM2D_BC_DYNFLT 2
 #define SEM2D_BC_DIRNEU 3
+#define SEM2D_BC_PERIOD 4 /* tag[0] master side, tag[1] slave side      */
 typedef struct sem2d_bc {
   int kind;
   int tag[2];

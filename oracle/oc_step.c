@@ -53,6 +53,8 @@ struct oc_sim {
   double *st_K;
   int ndir;
   int *dir_node, *dir_comp, *dir_after;
+  int nperio;
+  int *per_m, *per_s;
   int scheme;
   double dt, beta, gamma;
   int nt;
@@ -316,6 +318,18 @@ static void abso_apply(oc_sim *s, double *f, const double *v, const double *dsp)
       f[g + (size_t)s->npoin * c] -= s->st_K[t + (size_t)s->nstacey * c] * dd;
     }
   }
+}
+
+/* periodic sides: the forces of each node pair summed on the master and
+ * copied to the slave (bc_perio_apply = BC_PERIO_set_field,
+ * bc_periodic.f90:77-88), first of the boundary terms (bc_gen.f90:271-275) */
+static void perio_apply(oc_sim *s, double *f) {
+  for (int c = 0; c < s->ndof; c++)
+    for (int k = 0; k < s->nperio; k++) {
+      size_t m = (size_t)s->per_m[k] - 1 + (size_t)s->npoin * c, q = (size_t)s->per_s[k] - 1 + (size_t)s->npoin * c;
+      f[m] = f[m] + f[q];
+      f[q] = f[m];
+    }
 }
 
 /* zero-Dirichlet components of the &BC_DIRNEU sides that come before (after
@@ -725,6 +739,9 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
   s->dir_node = dupi(dd->dir_node, (size_t)dd->ndir);
   s->dir_comp = dupi(dd->dir_comp, (size_t)dd->ndir);
   s->dir_after = dupi(dd->dir_after_fault, (size_t)dd->ndir);
+  s->nperio = dd->nperio;
+  s->per_m = dupi(dd->perio_master, (size_t)dd->nperio);
+  s->per_s = dupi(dd->perio_slave, (size_t)dd->nperio);
   s->scheme = dd->time_scheme;
   s->alpha = dd->time_scheme == SEM2D_TIME_HHT ? dd->alpha : 1.0;
   s->dt = dd->dt;
@@ -885,6 +902,7 @@ int oc_sim_run(oc_sim *s, int nsteps) {
     s->tshift = hht ? (s->alpha - 1.0) * s->dt : 0.0;
     compute_fint(s, a, df, vf); /* f aliases accel */
     so_add(s, t, a);
+    perio_apply(s, a);
     abso_apply(s, a, vf, df);
     dirneu_apply(s, a, 0);
     if (s->nflt) dynflt_apply(s, a, v, d);
@@ -987,7 +1005,7 @@ void oc_sim_free(oc_sim *s) {
   if (!s) return;
   void *ptrs[] = {s->ibool, s->H, s->acoef, s->kveta, s->rmass, s->abs_node, s->abs_C,
                   s->st_node, s->st_k, s->st_edge, s->st_K, s->dir_node, s->dir_comp, s->dir_after,
-                  s->dal, s->val,
+                  s->dal, s->val, s->per_m, s->per_s,
                   s->src_node, s->src_dir, s->src_f0, s->src_t0, s->src_amp, s->src_rel,
                   s->src_tdelay, s->rec_node, s->rec_elem, s->rec_interp, s->sis, s->node1,
                   s->node2, s->n1, s->B, s->invM1, s->invM2, s->Z, s->T0, s->coh, s->swf_dc,

@@ -32,6 +32,7 @@ PRECISION_MIXED = 1
 BC_ABSORB = 1
 BC_DYNFLT = 2
 BC_DIRNEU = 3
+BC_PERIOD = 4
 
 MAX_DOMAINS = 64
 MAX_MATS = 64
@@ -97,6 +98,7 @@ class ProblemDesc(C.Structure):
         ("stacey_K", P_double),
         ("ndir", c_int), ("dir_node", P_int), ("dir_comp", P_int), ("dir_after_fault", P_int),
         ("alpha", c_double),
+        ("nperio", c_int), ("perio_master", P_int), ("perio_slave", P_int),
     ]
 
 

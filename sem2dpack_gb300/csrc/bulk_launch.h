@@ -33,6 +33,7 @@ struct BulkConfig {
   void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
   void *per_kd = nullptr;  // Stacey P3 forces [c*nslot + slot], or null
   const int *per_dir = nullptr;  // zero-Dirichlet bits c by perimeter slot, or null
+  void *perio_f = nullptr;       // raw forces of the periodic columns, or null
   int jf1 = -1, jf2 = -1;
   int has_fault = 0;
   const void *flt = nullptr;  // host FaultParams<real> of the problem's precision

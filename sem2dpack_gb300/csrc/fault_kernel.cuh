@@ -436,3 +436,88 @@ __global__ void receiver_kernel(RecParams<real> p) {
 }
 
 }  // namespace sem2d
+
+namespace sem2d {
+
+// Periodic columns (bc_perio_apply = BC_PERIO_set_field, bc_periodic.f90:
+// 77-88, applied first of the boundary terms, bc_gen.f90:271-275): the
+// raw forces the step kernel left for the nodes (0, J) and (LX-1, J) are
+// summed, each copy takes its dashpot and Dirichlet terms and is updated as
+// the step kernel updates a node; on the fault rows the sums go to the fault
+// node update of k = 0 and k = LX-1.  One thread per lattice row.
+template <typename real>
+struct PerioParams {
+  int LX, LZ, ndof, nslot, scheme;
+  long long plane, pitch;
+  const real *pf;
+  const real *Dcur, *Vcur, *Acur;
+  real *Dnext, *Vnext, *Anext;
+  const real *per_rm, *per_Ca, *per_Cb;
+  const int *per_dir;
+  real dt, cv, cpred, cpa, cd2, cb;
+  int jf1, jf2, has_fault, two;
+  const int *step;
+};
+
+template <typename real>
+__device__ __forceinline__ real perio_boundary(const PerioParams<real> &p, int I, int J, int c, real fc, real *vpred,
+                                               real *rm) {
+  const long long g = c * p.plane + (long long)J * p.pitch + I;
+  real vp = p.Vcur[g], vd = vp;
+  if (p.scheme != 0) {
+    const real an = p.Acur[g];
+    vd = vp + (p.scheme == 2 ? p.cpa : p.cpred) * an;
+    vp = vp + p.cpred * an;
+  }
+  const int sp = perimeter_slot(I, J, p.LX, p.LZ), so = c * p.nslot + sp;
+  fc = fc - p.per_Ca[so] * vd;
+  fc = fc - p.per_Cb[so] * vd;
+  if (p.per_dir && ((p.per_dir[sp] >> c) & 1)) fc = real(0);
+  *vpred = vp;
+  *rm = p.per_rm[so];
+  return fc;
+}
+
+template <typename real>
+__global__ void perio_kernel(const PerioParams<real> p, FaultParams<real> flt) {
+  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  if (J >= p.LZ) return;
+  const int it = *p.step;
+  if (p.has_fault && p.two && J == p.jf2) return;  // with the row jf1
+  if (p.has_fault && J == p.jf1) {
+    for (int e = 0; e < 2; ++e) {
+      const int I = e ? p.LX - 1 : 0;
+      double f1[2] = {0, 0}, f2[2] = {0, 0};
+      for (int c = 0; c < p.ndof; ++c) {
+        real vp, rm;
+        const real s1 = p.pf[(size_t(c) * p.LZ + p.jf1) * 2] + p.pf[(size_t(c) * p.LZ + p.jf1) * 2 + 1];
+        f1[c] = double(perio_boundary(p, I, p.jf1, c, s1, &vp, &rm));
+        if (p.two) {
+          const real s2 = p.pf[(size_t(c) * p.LZ + p.jf2) * 2] + p.pf[(size_t(c) * p.LZ + p.jf2) * 2 + 1];
+          f2[c] = double(perio_boundary(p, I, p.jf2, c, s2, &vp, &rm));
+        }
+      }
+      fault_node_update(flt, I, it, f1, f2);
+    }
+    return;
+  }
+  for (int e = 0; e < 2; ++e) {
+    const int I = e ? p.LX - 1 : 0;
+    for (int c = 0; c < p.ndof; ++c) {
+      const long long g = c * p.plane + (long long)J * p.pitch + I;
+      real vp, rm;
+      const real s = p.pf[(size_t(c) * p.LZ + J) * 2] + p.pf[(size_t(c) * p.LZ + J) * 2 + 1];
+      const real fc = perio_boundary(p, I, J, c, s, &vp, &rm);
+      const real a = rm * fc;
+      const real vnew = vp + p.cv * a;
+      real dcur = p.Dcur[g];
+      if (p.scheme != 0 && p.cb != real(0)) dcur = dcur + p.cb * a;
+      const real dnext = p.scheme != 0 ? (dcur + p.dt * vnew) + p.cd2 * a : dcur + p.dt * vnew;
+      p.Vnext[g] = vnew;
+      p.Dnext[g] = dnext;
+      if (p.Anext) p.Anext[g] = a;
+    }
+  }
+}
+
+}  // namespace sem2d

@@ -644,6 +644,8 @@ struct sem2d_problem {
   std::vector<double> st_K0, st_K1;
   // zero-Dirichlet components
   std::vector<int> dir_node, dir_comp, dir_after;
+  // periodic node pairs
+  std::vector<int> per_master, per_slave;
   // fault
   int nflt = 0;
   bool two = false;
@@ -832,7 +834,7 @@ void build_mass(sem2d_problem &P) {
 
 // BC_get_normal_and_weights (spec_grid.f90:961-1011)
 void normals(const sem2d_grid &g, const sem2d_grid::Boundary &b, std::vector<double> &nrm,
-             std::vector<double> &w) {
+             std::vector<double> &w, bool periodic = false) {
   const int N = g.ngll, np = int(b.node.size());
   nrm.assign(2 * size_t(np), 0.0);
   w.assign(np, 0.0);
@@ -856,6 +858,14 @@ void normals(const sem2d_grid &g, const sem2d_grid::Boundary &b, std::vector<dou
       w[bn] = w[bn] + g.gll.w[k] * j1;
     }
   }
+  if (periodic) {  // the two ends are one node (spec_grid.f90:998-1003)
+    for (int c = 0; c < 2; ++c) {
+      nrm[0 + size_t(np) * c] = nrm[0 + size_t(np) * c] + nrm[(np - 1) + size_t(np) * c];
+      nrm[(np - 1) + size_t(np) * c] = nrm[0 + size_t(np) * c];
+    }
+    w[0] = w[0] + w[np - 1];
+    w[np - 1] = w[0];
+  }
   for (size_t q = 0; q < b.elem.size(); ++q)
     for (int k : {0, N - 1}) {
       const int bn = b.ib[k + size_t(N) * q] - 1;
@@ -863,6 +873,45 @@ void normals(const sem2d_grid &g, const sem2d_grid::Boundary &b, std::vector<dou
       nrm[bn] = nrm[bn] / r;
       nrm[bn + np] = nrm[bn + np] / r;
     }
+}
+
+// BC_PERIO_intersects (bc_periodic.f90:108-121): both ends of the boundary
+// are periodic nodes
+bool perio_intersects(const sem2d_problem &P, const sem2d_grid::Boundary &b) {
+  if (P.per_master.empty() || b.node.empty()) return false;
+  auto on = [&](int n) {
+    for (size_t k = 0; k < P.per_master.size(); ++k)
+      if (P.per_master[k] == n || P.per_slave[k] == n) return true;
+    return false;
+  };
+  return on(b.node.front()) && on(b.node.back());
+}
+
+// BC_PERIO_init (bc_periodic.f90:42-72): pair the nodes of the two sides in
+// list order after checking they differ by one shift, then assemble the
+// mass on the master nodes and copy it to the slaves (BC_PERIO_set_field)
+void perio_init(sem2d_problem &P, const int tags[2]) {
+  const sem2d_grid &g = *P.g;
+  const sem2d_grid::Boundary *m = g.find(tags[0]), *s = g.find(tags[1]);
+  if (!m || !s) throw BuildError("bc_perio_init: boundary tag not found");
+  if (m->elem.size() != s->elem.size()) throw BuildError("bc_perio_init: number of boundary elements do not match");
+  if (m->node.size() != s->node.size()) throw BuildError("bc_perio_init: number of nodes on boundaries do not match");
+  const double *c0m = &g.coord[2 * size_t(m->node[0] - 1)], *c0s = &g.coord[2 * size_t(s->node[0] - 1)];
+  const double sh1 = c0m[0] - c0s[0], sh2 = c0m[1] - c0s[1];
+  for (size_t k = 0; k < m->node.size(); ++k) {
+    const double *cm = &g.coord[2 * size_t(m->node[k] - 1)], *cs = &g.coord[2 * size_t(s->node[k] - 1)];
+    if (std::fabs(cm[0] - cs[0] - sh1) > kTinyXabs || std::fabs(cm[1] - cs[1] - sh2) > kTinyXabs)
+      throw BuildError("bc_perio_init: coordinates on boundaries do not match properly");
+  }
+  for (int d = 0; d < P.ndof; ++d)
+    for (size_t k = 0; k < m->node.size(); ++k) {
+      double &a = P.mass[size_t(m->node[k] - 1) + size_t(g.npoin) * d];
+      double &b = P.mass[size_t(s->node[k] - 1) + size_t(g.npoin) * d];
+      a = a + b;
+      b = a;
+    }
+  P.per_master.insert(P.per_master.end(), m->node.begin(), m->node.end());
+  P.per_slave.insert(P.per_slave.end(), s->node.begin(), s->node.end());
 }
 
 // BC_ABSO_init (bc_abso.f90:115-266), Clayton-Engquist on flat sides, and
@@ -874,8 +923,9 @@ void abso_init(sem2d_problem &P, int tag, int stacey) {
   const sem2d_grid::Boundary *b = g.find(tag);
   if (!b) return;  // the reference ignores a BC whose tag is absent (bc_gen.f90:214-219)
   const int N = g.ngll, np = int(b->node.size()), nd = P.ndof;
+  const bool periodic = perio_intersects(P, *b);
   std::vector<double> nrm, w;
-  normals(g, *b, nrm, w);
+  normals(g, *b, nrm, w, periodic);
   bool horiz = true, vert = true;
   for (int k = 0; k < np; ++k) {
     horiz &= std::fabs(nrm[k]) < kTinyXabs;
@@ -918,6 +968,12 @@ void abso_init(sem2d_problem &P, int tag, int stacey) {
       }
     }
   }
+  if (periodic && stacey && nd == 2) throw BuildError("Stacey sides meeting periodic sides are not supported");
+  if (periodic)  // the two ends are one node (bc_abso.f90:227-231)
+    for (int d = 0; d < nd; ++d) {
+      Cb[0 + size_t(np) * d] = Cb[0 + size_t(np) * d] + Cb[(np - 1) + size_t(np) * d];
+      Cb[(np - 1) + size_t(np) * d] = Cb[0 + size_t(np) * d];
+    }
   const double cf = coefA2Vrhs(P);
   for (int d = 0; d < nd; ++d)
     for (int k = 0; k < np; ++k) {
@@ -970,7 +1026,7 @@ void dynflt_init(sem2d_problem &P, const sem2d_deck &dk, const int *tags) {
   if (P.two && (b1->elem.size() != b2->elem.size() || b2->node.size() != b1->node.size()))
     throw BuildError("bc_dynflt_init: boundaries do not match");
   std::vector<double> nrm, w;
-  normals(g, *b1, nrm, w);
+  normals(g, *b1, nrm, w, perio_intersects(P, *b1));
   for (int k = 0; k < nb; ++k) {
     if (P.two && b1->node[k] == b2->node[k]) continue;  // non-split nodes are dropped
     P.node1.push_back(b1->node[k]);
@@ -1259,6 +1315,12 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
       }
     }
     build_mass(*P);
+    // periodic sides first (bc_gen.f90:221-228)
+    for (int b = 0; b < deck->nbcs; ++b)
+      if (deck->bcs[b].kind == SEM2D_BC_PERIOD) {
+        if (!P->per_master.empty()) throw BuildError("more than one pair of periodic sides");
+        perio_init(*P, deck->bcs[b].tag);
+      }
     bool fault_seen = false;
     for (int b = 0; b < deck->nbcs; ++b) {
       const sem2d_bc &bc = deck->bcs[b];
@@ -1269,6 +1331,8 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
         fault_seen = true;
       } else if (bc.kind == SEM2D_BC_DIRNEU) {
         dirneu_init(*P, bc.tag[0], bc.dirichlet, fault_seen ? 1 : 0);
+      } else if (bc.kind == SEM2D_BC_PERIOD) {
+        continue;
       } else {
         throw BuildError("unsupported boundary condition kind");
       }
@@ -1326,6 +1390,9 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
   d->dir_node = VPTR(P->dir_node);
   d->dir_comp = VPTR(P->dir_comp);
   d->dir_after_fault = VPTR(P->dir_after);
+  d->nperio = int(P->per_master.size());
+  d->perio_master = VPTR(P->per_master);
+  d->perio_slave = VPTR(P->per_slave);
   d->time_scheme = P->time_kind;
   d->dt = P->dt;
   d->beta = P->beta;

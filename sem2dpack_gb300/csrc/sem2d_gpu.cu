@@ -76,6 +76,9 @@ struct sem2d_handle {
   int ndir = 0;
   int *per_dir = nullptr;
   unsigned char *d_fdir = nullptr;
+  // periodic columns I = 0 and LX-1: raw forces left by the step kernel
+  int nperio = 0;
+  void *perio_f = nullptr;
   int *d_row0 = nullptr, *d_step = nullptr, *d_error = nullptr;
   unsigned *d_done = nullptr;
   // sources
@@ -486,6 +489,29 @@ int upload_dirneu(sem2d_handle *h, const sem2d_problem_desc *d) {
   return SEM2D_OK;
 }
 
+// periodic node pairs: the lattice columns I = 0 and LX-1, row by row (the
+// Cartesian mesher's left and right sides); top/bottom periodic sides are
+// not supported
+int upload_perio(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int n = d->nperio, np = d->npoin;
+  if (n <= 0) return SEM2D_OK;
+  if (!d->perio_master || !d->perio_slave) return set_err(h, SEM2D_E_ARG, "periodic arrays missing");
+  if (h->st_nslot) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey sides with periodic sides");
+  if (n != h->LZ) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides other than left/right");
+  std::vector<int> seen(h->LZ, 0);
+  for (int k = 0; k < n; ++k) {
+    const int a = d->perio_master[k] - 1, b = d->perio_slave[k] - 1;
+    if (a < 0 || a >= np || b < 0 || b >= np) return set_err(h, SEM2D_E_ARG, "periodic node out of range");
+    const long long La = h->glob2lat[a], Lb = h->glob2lat[b];
+    const int Ia = int(La % h->pitch), Ja = int(La / h->pitch), Ib = int(Lb % h->pitch), Jb = int(Lb / h->pitch);
+    if (Ja != Jb || !((Ia == 0 && Ib == h->LX - 1) || (Ia == h->LX - 1 && Ib == 0)) || seen[Ja])
+      return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides other than left/right");
+    seen[Ja] = 1;
+  }
+  h->nperio = n;
+  return upload_real(h, &h->perio_f, std::vector<double>((size_t)2 * h->ndof * h->LZ, 0.0));
+}
+
 int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
   const int nd = d->ndof, np = d->npoin;
   const int nslot = perimeter_slots(h->LX, h->LZ);
@@ -521,7 +547,8 @@ int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
       (st = upload_real(h, &h->per_Ca, pca)) || (st = upload_real(h, &h->per_Cb, pcb)))
     return st;
   if ((st = upload_stacey(h, d))) return st;
-  return upload_dirneu(h, d);
+  if ((st = upload_dirneu(h, d))) return st;
+  return upload_perio(h, d);
 }
 
 int upload_fault(sem2d_handle *h, const sem2d_problem_desc *d) {
@@ -774,6 +801,7 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.per_Cb = h->per_Cb;
   bc.per_kd = h->per_kd;
   bc.per_dir = h->ndir ? h->per_dir : nullptr;
+  bc.perio_f = h->nperio ? h->perio_f : nullptr;
   bc.jf1 = h->nflt ? h->jf1 : -1;
   bc.jf2 = h->nflt ? h->jf2 : -1;
   bc.has_fault = h->nflt ? 1 : 0;
@@ -943,6 +971,41 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     if (launch_step_kernel(h, bc, rec))
       return set_err(h, SEM2D_E_CUDA, std::string("bulk launch: ") + bulk_last_error());
     h->launches++;
+    if (h->nperio) {
+      PerioParams<real> pp{};
+      pp.LX = h->LX;
+      pp.LZ = h->LZ;
+      pp.ndof = h->ndof;
+      pp.nslot = perimeter_slots(h->LX, h->LZ);
+      pp.scheme = h->scheme;
+      pp.plane = h->plane;
+      pp.pitch = h->pitch;
+      pp.pf = (const real *)h->perio_f;
+      pp.Dcur = (const real *)h->D[cur];
+      pp.Vcur = (const real *)h->V[cur];
+      pp.Acur = (const real *)h->A[cur];
+      pp.Dnext = (real *)h->D[1 - cur];
+      pp.Vnext = (real *)h->V[1 - cur];
+      pp.Anext = h->keep_accel ? (real *)h->A[1 - cur] : nullptr;
+      pp.per_rm = (const real *)h->per_rm;
+      pp.per_Ca = (const real *)h->per_Ca;
+      pp.per_Cb = (const real *)h->per_Cb;
+      pp.per_dir = h->ndir ? h->per_dir : nullptr;
+      pp.dt = real(bc.dt);
+      pp.cv = real(bc.cv);
+      pp.cpred = real(bc.cpred);
+      pp.cpa = real(bc.cpa);
+      pp.cd2 = real(bc.cd2);
+      pp.cb = real(bc.cb);
+      pp.jf1 = h->nflt ? h->jf1 : -1;
+      pp.jf2 = h->nflt ? h->jf2 : -1;
+      pp.has_fault = h->nflt ? 1 : 0;
+      pp.two = h->nflt ? h->two : 0;
+      pp.step = h->d_step;
+      perio_kernel<real><<<(h->LZ + 127) / 128, 128, 0, h->stream>>>(pp, f);
+      CK(cudaGetLastError());
+      h->launches++;
+    }
     if (ev) CK(cudaEventRecord(ev[1], h->stream));
     if (h->nflt && h->potency && launch_potency(h, h->stream, h->d_step)) return SEM2D_E_CUDA;
   }
@@ -1093,7 +1156,7 @@ int launch_steps(sem2d_handle *h, int n) {
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
   return 1 + (h->march && h->nflt ? (h->march_fused ? 1 : 2) : 0) + (h->nflt && h->potency ? 1 : 0) +
-         (h->nrec && h->rec_separate ? 1 : 0) + (h->st_nslot ? 1 : 0);
+         (h->nrec && h->rec_separate ? 1 : 0) + (h->st_nslot ? 1 : 0) + (h->nperio ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -1192,7 +1255,7 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   h->march = false;
   const char *env = std::getenv("SEM2D_MARCH");
   if (env && std::atoi(env) == 0) return SEM2D_OK;
-  if (h->st_nslot || h->ndir) return SEM2D_OK;  // Stacey or Dirichlet sides: the strip kernel
+  if (h->st_nslot || h->ndir || h->nperio) return SEM2D_OK;  // Stacey, Dirichlet or periodic sides: the strip kernel
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
@@ -1523,6 +1586,10 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
         rec_ez[r] = h->elem_ez[e];
       }
     }
+    // node receivers on periodic columns are sampled after the periodic pass
+    if (h->nperio && d->rec_node)
+      for (int r = 0; r < h->nrec; ++r)
+        if (rI[r] == 0 || rI[r] == h->LX - 1) h->rec_separate = true;
     std::vector<int> start(gx * gy + 1, 0), ids(h->nrec);
     for (int r = 0; r < h->nrec; ++r) start[owner[r] + 1]++;
     for (int k = 0; k < gx * gy; ++k) start[k + 1] += start[k];
@@ -1605,6 +1672,7 @@ int batch_close_impl(sem2d_handle *h) {
     if (m->potency) return set_err(h, SEM2D_E_UNSUPPORTED, "fault potency records in a batch");
     if (m->st_nslot) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey absorbing boundaries in a batch");
     if (m->ndir) return set_err(h, SEM2D_E_UNSUPPORTED, "Dirichlet sides in a batch");
+    if (m->nperio) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides in a batch");
   }
   h->N = a->N;
   h->ndof = a->ndof;
@@ -1957,7 +2025,7 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
   if (h->ckpt_every <= 0 || h->steps != h->nt || h->ckpt_saved != h->nt / h->ckpt_every)
     return set_err(h, SEM2D_E_STATE, "run all nt steps with checkpoints first (sem2d_gpu_checkpoint_every)");
   if (h->N != 5 || h->nflt || h->scheme != 0 || h->has_kv || h->width > 0 || !h->mat_iso ||
-      h->mat_elem != kMatNode || h->st_nslot || h->ndir)
+      h->mat_elem != kMatNode || h->st_nslot || h->ndir || h->nperio)
     return set_err(h, SEM2D_E_UNSUPPORTED,
                    "the adjoint covers NGLL=5, isotropic node material, leapfrog, no fault, KV, 2.5D, Stacey "
                    "or Dirichlet sides");

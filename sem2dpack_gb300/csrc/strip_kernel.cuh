@@ -612,6 +612,11 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
             for (int c = 0; c < NDOF; ++c)
               f[c] = f[c] + real(p.src_amp[((long long)s * NDOF + c) * (p.nt + 1) + it]);
         }
+        if (p.perio_f && (I == 0 || I == p.LX - 1)) {  // periodic columns: summed and finished after the step
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) p.perio_f[(size_t(c) * p.LZ + J) * 2 + (I == 0 ? 0 : 1)] = f[c];
+          continue;
+        }
         const int sidx = jj * TWp + xo + ii;
         const bool edge = (J == 0 || J == p.LZ - 1 || I == 0 || I == p.LX - 1);
         const int sp = edge ? perimeter_slot(I, J, p.LX, p.LZ) : -1;
@@ -660,6 +665,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
     // ---- the fault, once its last row is complete (FP64) ----
     if (jflast >= Jlo && jflast < Jlo + nr && s_stat[jflast - Jlo] == 1) {
       for (int I = I0 + tid; I < I1; I += kStripThreads) {
+        if (p.perio_f && (I == 0 || I == p.LX - 1)) continue;  // the periodic pass updates these
         const int io = I - I0;
         double f1[2] = {0, 0}, f2[2] = {0, 0};
         for (int c = 0; c < NDOF; ++c) {

@@ -137,6 +137,8 @@ class ParDeck:
     # &BC_DEF kind='DIRNEU' + &BC_DIRNEU h, v: (tag, h, v, before_fault), h and
     # v 'N' or 'D'; before_fault when the block precedes the fault's in &BC_DEF
     dirneu: List[Tuple[int, str, str, bool]] = field(default_factory=list)
+    # &BC_DEF kind='PERIOD' tags=(master, slave)
+    periodic: Optional[Tuple[int, int]] = None
     fault: Optional[Fault] = None
     fault_first: bool = False  # &BC_DEF order: DYNFLT block before the ABSORB blocks
     time: Time = field(default_factory=Time)
@@ -188,6 +190,8 @@ class ParDeck:
                 raise ValueError("BC_DIRNEU h and v must be 'N' or 'D'")
             (pre if before else post).append((abi.BC_DIRNEU, (t, (h == "D") | ((v == "D") << 1))))
         absorb = [(abi.BC_ABSORB, (t, 0)) for t in self.absorbing]
+        if self.periodic is not None:
+            absorb = [(abi.BC_PERIOD, tuple(self.periodic))] + absorb
         if self.fault is None:
             bcs = absorb + pre + post
         elif self.fault_first:

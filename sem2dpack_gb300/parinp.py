@@ -18,6 +18,7 @@ between blocks (``#`` comments, anything after the ``/``) is ignored.
                 &MAT_KV eta, ETAxDT (mat_kelvin_voigt.f90)
   &BC_DEF       tag, kind 'ABSORB' + &BC_ABSORB stacey (bc_abso.f90),
                 kind 'DIRNEU' + &BC_DIRNEU h, v (bc_dirneu.f90:50-112),
+                kind 'PERIOD' tags (bc_periodic.f90),
                 kind 'DYNFLT' + &BC_DYNFLT / _SWF / _RSF / _TWF / _NOR with
                 scalar values (bc_dynflt*.f90)
   &TIME         kind, Dt, Courant, TotalTime, NbSteps + &TIME_NEWMARK or &TIME_HHTA alpha, rho
@@ -262,6 +263,10 @@ def deck_from_parinp(text, precision=None, base=None):
                 # a single tag is a one-sided fault: tags = (tag, 0) (bc_gen.f90:126-133)
                 fault.tags = (int(tags[0]), int(tags[1]) if len(tags) > 1 else 0)
                 deck.fault_first = not absorbing
+            elif kind == "PERIOD":
+                if len(tags) != 2:
+                    raise ValueError("&BC_DEF kind='PERIOD' needs two tags")
+                deck.periodic = (int(tags[0]), int(tags[1]))
             elif kind == "DIRNEU":
                 b = nxt[1] if nxt[0] == "BC_DIRNEU" else {}
                 extra = set(b) - {"h", "v"}

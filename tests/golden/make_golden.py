@@ -15,7 +15,8 @@ It reads the reference's own test data (nothing is written from memory):
                                               4, 18, 23, 46 (Anisotropic/write_seis.m)
   EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
   EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox,
-           TestFlt2D_SCEC_TPV3_inplane,RateState}/Par.inp
+           TestFlt2D_SCEC_TPV3_inplane,RateState,TestFlt1D,
+           Bimaterial_fault}/Par.inp
                                               the input decks, as text (parinp_*)
   EXAMPLES/RateState/{Ux,Vx,Tau}_{0,3,6,9}km_ascii
                                               the reference's slip, slip rate and shear
@@ -73,7 +74,8 @@ def main(ref):
         out["ratestate_" + q] = np.stack([np.loadtxt(os.path.join(ex, "RateState", "%s_%dkm_ascii" % (q, x)))
                                           for x in (0, 3, 6, 9)])
 
-    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState"):
+    for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState",
+                 "TestFlt1D", "Bimaterial_fault"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
 
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")

@@ -143,3 +143,68 @@ def test_dirneu_order_against_the_fault():
     assert set(zip(comp.tolist(), after.tolist())) == {(1, 0), (0, 1)}
     with pytest.raises(ValueError):
         deck_from_parinp(text.replace("&BC_DIRNEU h='D' /", "&BC_DIRNEU h='D', hsrc='RICKER' /"))
+
+
+def periodic_box(stacey=False):
+    """The corner box with its left and right sides periodic (tags 2 and 4),
+    absorbing at the bottom and top."""
+    dk = small_box(stacey)
+    dk.absorbing = [1, 3]
+    dk.stacey = [t for t in dk.stacey if t in (1, 3)]
+    dk.periodic = (2, 4)
+    return dk
+
+
+def test_periodic_pairs_and_mass():
+    Pp, P0 = Problem(periodic_box()), Problem(small_box(False))
+    d, d0 = Pp.desc(), P0.desc()
+    n = d.nperio
+    assert n == 15 * 4 + 1
+    m, s = arr(d, "perio_master", n), arr(d, "perio_slave", n)
+    xz = Pp.grid.coord()
+    assert np.allclose(xz[0, m - 1], 0.9e3) and np.allclose(xz[0, s - 1], -1.5e3)
+    assert np.allclose(xz[1, m - 1], xz[1, s - 1])
+    # BC_PERIO_init: the masses are summed and shared (bc_periodic.f90:77-88);
+    # absorbing dashpots are absent on the periodic sides
+    rm, rm0 = arr(d, "rmass", 2 * d.npoin), arr(d0, "rmass", 2 * d.npoin)
+    np.testing.assert_array_equal(rm[m - 1], rm[s - 1])
+    # away from the four sides nothing changes
+    z = xz[1]
+    inner = (np.abs(xz[0] + 1.5e3) > 1) & (np.abs(xz[0] - 0.9e3) > 1) & (np.abs(z + 1e3) > 1) & (np.abs(z - 0.5e3) > 1)
+    np.testing.assert_array_equal(rm[:d.npoin][inner], rm0[:d.npoin][inner])
+    with pytest.raises(Exception):
+        Problem(periodic_box(stacey=True))
+
+
+def test_oracle_periodic_copies_stay_equal():
+    P = Problem(periodic_box())
+    d = P.desc()
+    d.precision = PRECISION_FP64
+    o = po.OracleSim(d, owner=P)
+    o.run(200)
+    D, V, A = o.fields()
+    m, s = arr(d, "perio_master", d.nperio) - 1, arr(d, "perio_slave", d.nperio) - 1
+    assert np.abs(D[m]).max() > 0
+    np.testing.assert_array_equal(D[m], D[s])
+    np.testing.assert_array_equal(V[m], V[s])
+
+
+def test_testflt1d_steady_slip_rate(golden):
+    """EXAMPLES/TestFlt1D (periodic sides, split fault, slip weakening,
+    HHT-alpha): after the slip passes Dc the 1-D fault slides at the
+    steady rate 2 (Tt - MuD |Tn|) / (rho cs) = 2.2 under the stress
+    MuD |Tn| (the check named for this example); from t = 2.5 s on the
+    oracle's rate averages it to 0.5 % and rings within 3 % of it."""
+    dk = deck_from_parinp(str(golden["parinp_TestFlt1D"]))
+    assert dk.periodic == (2, 4) and dk.time.kind == "hht-alpha"
+    P = Problem(dk)
+    d = P.desc()
+    d.precision = PRECISION_FP64
+    o = po.OracleSim(d, owner=P)
+    o.run(d.nt)
+    f = o.fault_series()
+    t = np.arange(f.shape[2]) * d.flt_oitd * d.dt
+    late = t >= 2.5
+    assert abs(f[0, 1, late].mean() / 2.2 - 1) < 5e-3
+    np.testing.assert_allclose(f[0, 1, late], 2.2, rtol=0.03)
+    np.testing.assert_allclose(f[0, 2, late], -1.1, rtol=1e-9)

@@ -1,0 +1,86 @@
+"""Periodic left/right sides (&BC_DEF kind='PERIOD', bc_periodic.f90) on the
+GPU against the FP64 oracle: FP64 <= 1e-10, mixed <= 1e-4 relative L2.
+The step kernel leaves the raw forces of the columns I = 0 and LX-1 and a
+second pass sums each pair, adds the boundary terms and updates both
+copies (on fault rows through the fault node update)."""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as po
+from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Problem, Solver, workloads
+from sem2dpack_gb300.parinp import deck_from_parinp
+
+from test_boundaries import periodic_box
+
+pytestmark = pytest.mark.gpu
+
+TOL = {PRECISION_FP64: 1e-10, PRECISION_MIXED: 1e-4}
+
+
+def rel_l2(a, b):
+    nb = np.linalg.norm(b)
+    return np.linalg.norm(a - b) / (nb if nb > 0 else 1.0)
+
+
+def run_both(deck_or_pair, nsteps, precision):
+    P = workloads.build(deck_or_pair)
+    d = P.desc()
+    d.precision = precision
+    g = Solver(d, owner=P)
+    g.step(nsteps)
+    o = po.OracleSim(d, owner=P)
+    o.run(nsteps)
+    return P, d, g, o
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+@pytest.mark.parametrize("scheme", ["leapfrog", "newmark"])
+def test_box(precision, scheme):
+    dk = periodic_box()
+    dk.time.kind = scheme
+    dk.receivers.first, dk.receivers.last = (-1.5e3, -600.0), (0.9e3, -600.0)  # both periodic columns
+    P, d, g, o = run_both(dk, 200, precision)
+    assert rel_l2(g.seismograms(), o.seismograms()) <= TOL[precision]
+    dg, vg = g.fields()
+    do, vo, _ = o.fields()
+    assert rel_l2(dg, do) <= TOL[precision] and rel_l2(vg, vo) <= TOL[precision]
+    m = np.ctypeslib.as_array(d.perio_master, shape=(d.nperio,)) - 1
+    s = np.ctypeslib.as_array(d.perio_slave, shape=(d.nperio,)) - 1
+    assert np.array_equal(dg[m], dg[s]) and np.array_equal(vg[m], vg[s])  # the copies stay one node
+    assert np.abs(dg[m]).max() > 0
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+def test_testflt1d_deck(golden, precision):
+    """EXAMPLES/TestFlt1D as written: periodic sides crossed by a split
+    slip-weakening fault, HHT-alpha, 40 receivers; and the 1-D steady slip
+    rate 2.2 on the GPU.  The whole 568-step run of steady sliding is
+    compared, so the mixed path's bound is 3e-4 here."""
+    P = Problem(deck_from_parinp(str(golden["parinp_TestFlt1D"])))
+    d = P.desc()
+    d.precision = precision
+    g = Solver(d, owner=P)
+    g.run()
+    o = po.OracleSim(d, owner=P)
+    o.run(d.nt)
+    fg, fo = g.fault_series(), o.fault_series()
+    tol = TOL[precision] if precision == PRECISION_FP64 else 3e-4
+    for rec in (0, 1, 2, 4):
+        assert rel_l2(fg[:, rec, :], fo[:, rec, :]) <= tol, rec
+    assert rel_l2(g.seismograms(), o.seismograms()) <= tol
+    t = np.arange(fg.shape[2]) * d.flt_oitd * d.dt
+    assert abs(fg[0, 1, t >= 2.5].mean() / 2.2 - 1) < 5e-3
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+def test_split_fault_across_periodic_sides(precision):
+    """SH rupture on a split fault whose ends are a periodic pair."""
+    deck, grid = workloads.sh_rupture(scale=0.1, nsteps=300)
+    deck.absorbing = [1, 3]
+    deck.periodic = (2, 4)
+    P, d, g, o = run_both((deck, grid), 300, precision)
+    fg, fo = g.fault_series(), o.fault_series()
+    assert fo[:, 0, -1].max() > 0.1
+    for rec in (0, 1, 2, 4):
+        assert rel_l2(fg[:, rec, :], fo[:, rec, :]) <= TOL[precision], rec
+    assert rel_l2(g.seismograms(), o.seismograms()) <= TOL[precision]

@@ -65,7 +65,7 @@ def test_namelist_reader():
 
 @pytest.mark.parametrize("bad", [
     "&MESH_DEF method='MESH2D' /",
-    "&BC_DEF tags=1,3, kind='PERIOD' /",
+    "&BC_DEF tags=1,3, kind='KINFLT' /",
     "&TIME kind='hhta' /",
     "&SRC_DEF stf='RICKER', coord=0,0, mechanism='WAVE' /",
     "&MATERIAL tag=1, kind='PLAST' /",
