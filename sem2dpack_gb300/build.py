@@ -14,7 +14,7 @@ CSRC = os.path.join(HERE, "csrc")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsem2d_gb300.so")
-CU_SOURCES = ["sem2d_gpu.cu", "bulk_launch.cu", "bulk_n5.cu", "bulk_n6.cu", "bulk_n9.cu", "noalloc.cu",
+CU_SOURCES = ["sem2d_gpu.cu", "bulk_launch.cu", "bulk_n3.cu", "bulk_n5.cu", "bulk_n6.cu", "bulk_n9.cu", "noalloc.cu",
               "adjoint.cu", "march.cu"]
 CPP_SOURCES = ["host_builder.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

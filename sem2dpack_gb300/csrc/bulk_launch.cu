@@ -17,6 +17,7 @@ int launch_bulk(const BulkConfig &c) {
   switch (c.N) {
     case 5: return launch_bulk_n5(c);
     case 6: return launch_bulk_n6(c);
+    case 3: return launch_bulk_n3(c);
     case 9: return launch_bulk_n9(c);
     default: g_bulk_err = "NGLL not compiled"; return 1;
   }
@@ -26,6 +27,7 @@ int configure_bulk(const BulkConfig &c) {
   switch (c.N) {
     case 5: return configure_bulk_n5(c);
     case 6: return configure_bulk_n6(c);
+    case 3: return configure_bulk_n3(c);
     case 9: return configure_bulk_n9(c);
     default: g_bulk_err = "NGLL not compiled"; return 1;
   }
@@ -35,6 +37,7 @@ int occupancy_bulk(const BulkConfig &c) {
   switch (c.N) {
     case 5: return occupancy_bulk_n5(c);
     case 6: return occupancy_bulk_n6(c);
+    case 3: return occupancy_bulk_n3(c);
     case 9: return occupancy_bulk_n9(c);
     default: return 0;
   }
@@ -44,6 +47,7 @@ size_t bulk_smem(int N, int ndof, int mixed, int nplanes) {
   switch (N) {
     case 5: return bulk_smem_n5(ndof, mixed, nplanes);
     case 6: return bulk_smem_n6(ndof, mixed, nplanes);
+    case 3: return bulk_smem_n3(ndof, mixed, nplanes);
     case 9: return bulk_smem_n9(ndof, mixed, nplanes);
     default: return size_t(-1);
   }
@@ -53,6 +57,7 @@ int launch_batch(const BulkConfig &c, const BatchLaunch &b) {
   switch (c.N) {
     case 5: return launch_batch_n5(c, b);
     case 6: return launch_batch_n6(c, b);
+    case 3: return launch_batch_n3(c, b);
     case 9: return launch_batch_n9(c, b);
     default: g_bulk_err = "NGLL not compiled"; return 1;
   }
@@ -62,6 +67,7 @@ size_t params_bytes(int N, int mixed) {
   switch (N) {
     case 5: return params_bytes_n5(mixed);
     case 6: return params_bytes_n6(mixed);
+    case 3: return params_bytes_n3(mixed);
     case 9: return params_bytes_n9(mixed);
     default: return 0;
   }
@@ -71,6 +77,7 @@ int fill_params_block(const BulkConfig &c, void *out) {
   switch (c.N) {
     case 5: fill_params_n5(c, out); return 0;
     case 6: fill_params_n6(c, out); return 0;
+    case 3: fill_params_n3(c, out); return 0;
     case 9: fill_params_n9(c, out); return 0;
     default: g_bulk_err = "NGLL not compiled"; return 1;
   }
@@ -80,6 +87,7 @@ int strip_batch_rows(int N) {
   switch (N) {
     case 5: return strip_batch_rows_n5();
     case 6: return strip_batch_rows_n6();
+    case 3: return strip_batch_rows_n3();
     case 9: return strip_batch_rows_n9();
     default: return 1;
   }
@@ -89,6 +97,7 @@ int strip_width(int N) {
   switch (N) {
     case 5: return strip_width_n5();
     case 6: return strip_width_n6();
+    case 3: return strip_width_n3();
     case 9: return strip_width_n9();
     default: return 0;
   }

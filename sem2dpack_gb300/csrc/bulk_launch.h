@@ -142,26 +142,33 @@ int choose_tiles(const BulkConfig &c, const int *row0, int *TZ);
 int launch_bulk_n5(const BulkConfig &c);
 int launch_bulk_n6(const BulkConfig &c);
 int launch_bulk_n9(const BulkConfig &c);
+int launch_bulk_n3(const BulkConfig &c);
 int configure_bulk_n5(const BulkConfig &c);
 int configure_bulk_n6(const BulkConfig &c);
 int configure_bulk_n9(const BulkConfig &c);
+int configure_bulk_n3(const BulkConfig &c);
 int occupancy_bulk_n5(const BulkConfig &c);
 int occupancy_bulk_n6(const BulkConfig &c);
 int occupancy_bulk_n9(const BulkConfig &c);
+int occupancy_bulk_n3(const BulkConfig &c);
 // resident CTAs per SM for the configuration's shared memory (0 if none)
 int occupancy_bulk(const BulkConfig &c);
 size_t bulk_smem_n5(int ndof, int mixed, int nplanes);
 size_t bulk_smem_n6(int ndof, int mixed, int nplanes);
 size_t bulk_smem_n9(int ndof, int mixed, int nplanes);
+size_t bulk_smem_n3(int ndof, int mixed, int nplanes);
 int strip_width_n5();
 int strip_width_n6();
 int strip_width_n9();
+int strip_width_n3();
 int strip_batch_rows_n5();
 int strip_batch_rows_n6();
 int strip_batch_rows_n9();
+int strip_batch_rows_n3();
 int launch_batch_n5(const BulkConfig &c, const BatchLaunch &b);
 int launch_batch_n6(const BulkConfig &c, const BatchLaunch &b);
 int launch_batch_n9(const BulkConfig &c, const BatchLaunch &b);
+int launch_batch_n3(const BulkConfig &c, const BatchLaunch &b);
 // The FP32 NGLL=5 fast path with one element per thread (march_kernel.cuh).
 // Units are MarchUnit records {problem, strip, z0, z1, rec0, rec1}.
 constexpr int kMarchColsHost = 31;   // element columns owned by one unit
@@ -214,8 +221,10 @@ int march_warps_per_sm(const BulkConfig &c);
 size_t params_bytes_n5(int mixed);
 size_t params_bytes_n6(int mixed);
 size_t params_bytes_n9(int mixed);
+size_t params_bytes_n3(int mixed);
 void fill_params_n5(const BulkConfig &c, void *out);
 void fill_params_n6(const BulkConfig &c, void *out);
 void fill_params_n9(const BulkConfig &c, void *out);
+void fill_params_n3(const BulkConfig &c, void *out);
 
 }  // namespace sem2d

@@ -1385,8 +1385,8 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
 
 int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t shared = nullptr,
                 int force_tz = 0) {
-  if (d->ngll != 5 && d->ngll != 6 && d->ngll != 9)
-    return set_err(h, SEM2D_E_UNSUPPORTED, "GPU kernels are compiled for ngll in {5, 6, 9}");
+  if (d->ngll != 3 && d->ngll != 5 && d->ngll != 6 && d->ngll != 9)
+    return set_err(h, SEM2D_E_UNSUPPORTED, "GPU kernels are compiled for ngll in {3, 5, 6, 9}");
   if (d->ndof != 1 && d->ndof != 2) return set_err(h, SEM2D_E_ARG, "ndof must be 1 or 2");
   if (d->nelem <= 0 || d->npoin <= 0 || !d->ibool || !d->coord || !d->hprime || !d->wgll || !d->rmass ||
       !d->Kx || !d->Kz || !d->la || !d->mu || !d->mux)

@@ -84,3 +84,17 @@ def test_split_fault_across_periodic_sides(precision):
     for rec in (0, 1, 2, 4):
         assert rel_l2(fg[:, rec, :], fo[:, rec, :]) <= TOL[precision], rec
     assert rel_l2(g.seismograms(), o.seismograms()) <= TOL[precision]
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+def test_bimaterial_fault_deck(golden, precision):
+    """EXAMPLES/Bimaterial_fault as written (NGLL 3, two Kelvin-Voigt
+    layers along a fault between two materials, Prakash-Clifton normal
+    stress, periodic sides crossed by the fault), 200 steps."""
+    dk = deck_from_parinp(str(golden["parinp_Bimaterial_fault"]))
+    assert dk.ngll == 3 and dk.periodic == (2, 4) and dk.fault.normal_kind == 2
+    P, d, g, o = run_both(dk, 200, precision)
+    fg, fo = g.fault_series(), o.fault_series()
+    assert fo[:, 1, :].max() > 1.0  # sliding at m/s
+    for rec in (0, 1, 2, 3, 4):
+        assert rel_l2(fg[:, rec, :201], fo[:, rec, :201]) <= TOL[precision], rec
