@@ -853,20 +853,24 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
 // component): the sum over the slot's terms t of K(t,c) times the derivative
 // of D(:,c) along the element edge, sum_l hprime(l,k_t) D(edge node l, c).
 // The step kernel subtracts it at the slot together with the dashpots.
+// Under HHT-alpha (cal = 1 - alpha != 0) the displacement is d_alpha =
+// d_pred - (1-alpha)(dt v + (1/2-beta) dt^2 a) (displ_alpha, solver.f90:
+// 106-113, bc_gen.f90:295).
 template <typename real>
-__global__ void stacey_kernel(real *per_kd, const real *D, int nused, const int *slot, const int *ptr,
-                              const int *kk, const int *lat, const real *K, const real *H, int N, int nterm,
-                              int nslot, long long plane) {
+__global__ void stacey_kernel(real *per_kd, const real *D, const real *V, const real *A, real cal, real dt, real cd2,
+                              int nused, const int *slot, const int *ptr, const int *kk, const int *lat,
+                              const real *K, const real *H, int N, int nterm, int nslot, long long plane) {
   const int q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= 2 * nused) return;
   const int i = q % nused, c = q / nused;
-  const real *Dc = D + c * plane;
+  const real *Dc = D + c * plane, *Vc = V + c * plane, *Ac = A ? A + c * plane : nullptr;
+  auto dval = [&](int l) { return cal != real(0) ? Dc[l] - cal * (dt * Vc[l] + cd2 * Ac[l]) : Dc[l]; };
   real acc = real(0);
   for (int t = ptr[i]; t < ptr[i + 1]; ++t) {
     const int k = kk[t];
     const int *L = lat + (size_t)t * N;
-    real dd = H[N * k] * Dc[L[0]];
-    for (int l = 1; l < N; ++l) dd = dd + H[l + N * k] * Dc[L[l]];
+    real dd = H[N * k] * dval(L[0]);
+    for (int l = 1; l < N; ++l) dd = dd + H[l + N * k] * dval(L[l]);
     acc = acc + K[t + (size_t)nterm * c] * dd;
   }
   per_kd[(size_t)c * nslot + slot[i]] = acc;
@@ -961,9 +965,10 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
     if (h->st_nslot) {
       const int nthr = 2 * h->st_nslot;
       stacey_kernel<real><<<(nthr + 127) / 128, 128, 0, h->stream>>>(
-          (real *)h->per_kd, (const real *)h->D[cur], h->st_nslot, h->d_st_slot, h->d_st_ptr, h->d_st_k,
-          h->d_st_lat, (const real *)h->d_st_K, (const real *)h->d_st_H, h->N, h->st_nterm,
-          perimeter_slots(h->LX, h->LZ), h->plane);
+          (real *)h->per_kd, (const real *)h->D[cur], (const real *)h->V[cur],
+          h->scheme == 2 ? (const real *)h->A[cur] : nullptr, real(bc.cal), real(bc.dt), real(bc.cd2), h->st_nslot,
+          h->d_st_slot, h->d_st_ptr, h->d_st_k, h->d_st_lat, (const real *)h->d_st_K, (const real *)h->d_st_H,
+          h->N, h->st_nterm, perimeter_slots(h->LX, h->LZ), h->plane);
       CK(cudaGetLastError());
       h->launches++;
     }
@@ -1407,8 +1412,6 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
   h->gamma = h->scheme ? d->gamma : 0.5;
   h->alpha = h->scheme == 2 ? d->alpha : 1.0;
   if (h->scheme == 2 && !(h->alpha >= 0.0 && h->alpha <= 1.0)) return set_err(h, SEM2D_E_ARG, "alpha out of [0,1]");
-  if (h->scheme == 2 && d->nstacey > 0)
-    return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey boundaries with HHT-alpha are not supported on the GPU path");
   h->keep_accel = h->scheme != 0 || d->rec_field == 'A';
   if (shared) {
     h->stream = shared;

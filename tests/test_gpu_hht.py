@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle as po
-from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Sem2dError, Solver, workloads
+from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Solver, workloads
 from sem2dpack_gb300.deck import Time
 
 from test_gpu_newmark import box
@@ -95,9 +95,15 @@ def test_fault(precision):
     assert rel_l2(g.fault_potency(), o.fault_potency()) <= TOL[precision]
 
 
-def test_stacey_refused():
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+def test_stacey(precision):
+    """Stacey P3 sides under HHT-alpha take d_alpha (displ_alpha,
+    bc_gen.f90:295)."""
     dk = hht_box("V")
     dk.stacey = list(dk.absorbing)
-    P = workloads.build(dk)
-    with pytest.raises(Sem2dError):
-        Solver(P)
+    P, g, o = run_both(dk, 200, precision)
+    assert P.desc().nstacey > 0
+    assert rel_l2(g.seismograms(), o.seismograms()) <= TOL[precision]
+    dg, vg = g.fields()
+    do, vo, _ = o.fields()
+    assert rel_l2(dg, do) <= TOL[precision]
