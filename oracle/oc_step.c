@@ -956,15 +956,23 @@ void oc_sim_strain_stress(const oc_sim *s, double *eo, double *so) {
   double Ht[400], dl[400], gx[400], ge[400];
   for (int j = 0; j < n; j++)
     for (int i = 0; i < n; i++) Ht[i + n * j] = s->H[j + n * i];
+  /* the stress of a Kelvin-Voigt element is that of d + eta v
+   * (MAT_stress_dv, mat_gen.f90:626-641; MAT_KV_add_etav) */
   for (int e = 0; e < s->nelem; e++) {
-    double g[2][2][400];
-    for (int c = 0; c < nd; c++) {
-      for (int q = 0; q < n2; q++) dl[q] = s->d[(size_t)(s->ibool[q + (size_t)n2 * e] - 1) + (size_t)s->npoin * c];
-      mxm(Ht, dl, gx, n);
-      mxm(dl, s->H, ge, n);
-      memcpy(g[c][0], gx, sizeof(double) * n2);
-      memcpy(g[c][1], ge, sizeof(double) * n2);
-    }
+    double g[2][2][400], gk[2][2][400];
+    const double *eta = s->kveta ? s->kveta + (size_t)n2 * e : NULL;
+    for (int k = 0; k < (eta ? 2 : 1); k++)
+      for (int c = 0; c < nd; c++) {
+        for (int q = 0; q < n2; q++) {
+          size_t gq = (size_t)(s->ibool[q + (size_t)n2 * e] - 1) + (size_t)s->npoin * c;
+          dl[q] = k == 0 ? s->d[gq] : s->d[gq] + eta[q] * s->v[gq];
+        }
+        mxm(Ht, dl, gx, n);
+        mxm(dl, s->H, ge, n);
+        memcpy(k == 0 ? g[c][0] : gk[c][0], gx, sizeof(double) * n2);
+        memcpy(k == 0 ? g[c][1] : gk[c][1], ge, sizeof(double) * n2);
+      }
+    if (!eta) memcpy(gk, g, sizeof(g));
     for (int q = 0; q < n2; q++) {
       size_t p = q + (size_t)n2 * e;
       double *ev = eo + q + (size_t)n2 * nc * e, *sv = so + q + (size_t)n2 * nc * e;
@@ -972,15 +980,16 @@ void oc_sim_strain_stress(const oc_sim *s, double *eo, double *so) {
       if (nd == 1) {
         ev[0] = 0.5 * (g[0][0][q] * dx);
         ev[n2] = 0.5 * (g[0][1][q] * dz);
-        sv[0] = 2.0 * s->mmu[p] * ev[0];
-        sv[n2] = 2.0 * s->mmu[p] * ev[n2];
+        sv[0] = 2.0 * s->mmu[p] * (0.5 * (gk[0][0][q] * dx));
+        sv[n2] = 2.0 * s->mmu[p] * (0.5 * (gk[0][1][q] * dz));
       } else {
         ev[0] = g[0][0][q] * dx;
         ev[n2] = g[1][1][q] * dz;
         ev[2 * n2] = 0.5 * (g[0][1][q] * dz + g[1][0][q] * dx);
-        sv[0] = s->mKx[p] * ev[0] + s->mla[p] * ev[n2];
-        sv[n2] = s->mla[p] * ev[0] + s->mKz[p] * ev[n2];
-        sv[2 * n2] = 2.0 * s->mmu[p] * ev[2 * n2];
+        double k0 = gk[0][0][q] * dx, k1 = gk[1][1][q] * dz, k2 = 0.5 * (gk[0][1][q] * dz + gk[1][0][q] * dx);
+        sv[0] = s->mKx[p] * k0 + s->mla[p] * k1;
+        sv[n2] = s->mla[p] * k0 + s->mKz[p] * k1;
+        sv[2 * n2] = 2.0 * s->mmu[p] * k2;
       }
     }
   }

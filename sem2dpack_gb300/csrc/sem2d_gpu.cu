@@ -1772,7 +1772,7 @@ template <typename real>
 __global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int nz, int pitch, long long plane,
                                      const int *row0, const real *xix, const real *etaz, const double *H,
                                      int mat_elem, int iso, const real *m0, const real *m1, const real *m2,
-                                     const real *m3, double *eo, double *so) {
+                                     const real *m3, const real *V, const real *kveta, double *eo, double *so) {
   const long long npt = (long long)nx * nz * N * N;
   for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < npt;
        q += (long long)gridDim.x * blockDim.x) {
@@ -1781,7 +1781,10 @@ __global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int
     const int i = pt % N, j = pt / N, ex = int(el % nx), ez = int(el / nx);
     const long long base = (long long)row0[ez] * pitch + (long long)ex * (N - 1);
     const double dxi = double(xix[ex]), deta = double(etaz[ez]);
-    double gx[2] = {0, 0}, ge[2] = {0, 0};
+    double gx[2] = {0, 0}, ge[2] = {0, 0}, kx[2] = {0, 0}, ke[2] = {0, 0};
+    // the stress of a Kelvin-Voigt element is that of d + eta v
+    // (MAT_stress_dv, mat_gen.f90:626-641)
+    const real *eta = kveta ? kveta + el * N * N : nullptr;
     for (int c = 0; c < ndof; ++c) {
       const real *u = D + c * plane + base;
       double a = H[0 + N * i] * double(u[(long long)j * pitch + 0]);
@@ -1790,6 +1793,19 @@ __global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int
       for (int k = 1; k < N; ++k) b = b + double(u[(long long)k * pitch + i]) * H[k + N * j];
       gx[c] = a;
       ge[c] = b;
+      kx[c] = a;
+      ke[c] = b;
+      if (eta) {
+        const real *w = V + c * plane + base;
+        auto uk = [&](int ii, int jj) {
+          return double(u[(long long)jj * pitch + ii]) + double(eta[ii + N * jj]) * double(w[(long long)jj * pitch + ii]);
+        };
+        double ak = H[0 + N * i] * uk(0, j), bk = uk(i, 0) * H[0 + N * j];
+        for (int k = 1; k < N; ++k) ak = ak + H[k + N * i] * uk(k, j);
+        for (int k = 1; k < N; ++k) bk = bk + uk(i, k) * H[k + N * j];
+        kx[c] = ak;
+        ke[c] = bk;
+      }
     }
     auto mat = [&](const real *m) -> double {
       if (!m) return 0.0;
@@ -1802,8 +1818,8 @@ __global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int
       const double mu = mat(m0);  // SH: mu (the reference has no anisotropic SH stress)
       e[0] = 0.5 * (gx[0] * dxi);
       e[1] = 0.5 * (ge[0] * deta);
-      s[0] = 2.0 * mu * e[0];
-      s[1] = 2.0 * mu * e[1];
+      s[0] = 2.0 * mu * (0.5 * (kx[0] * dxi));
+      s[1] = 2.0 * mu * (0.5 * (ke[0] * deta));
     } else {
       double Kx, Kz, la, mu;
       if (iso) {
@@ -1820,9 +1836,10 @@ __global__ void strain_stress_kernel(const real *D, int ndof, int N, int nx, int
       e[0] = gx[0] * dxi;
       e[1] = ge[1] * deta;
       e[2] = 0.5 * (ge[0] * deta + gx[1] * dxi);
-      s[0] = Kx * e[0] + la * e[1];
-      s[1] = la * e[0] + Kz * e[1];
-      s[2] = 2.0 * mu * e[2];
+      const double k0 = kx[0] * dxi, k1 = ke[1] * deta, k2 = 0.5 * (ke[0] * deta + kx[1] * dxi);
+      s[0] = Kx * k0 + la * k1;
+      s[1] = la * k0 + Kz * k1;
+      s[2] = 2.0 * mu * k2;
     }
   }
 }
@@ -2429,12 +2446,14 @@ int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress)
     sem2d_detail::strain_stress_kernel<float><<<blocks, 256, 0, h->stream>>>(
         (const float *)D, h->ndof, N, h->nx, h->nz, h->pitch, h->plane, h->d_row0, (const float *)h->geo[0],
         (const float *)h->geo[1], dH, h->mat_elem, h->mat_iso, (const float *)h->mat[0], (const float *)h->mat[1],
-        (const float *)h->mat[2], (const float *)h->mat[3], dev, dev + npt * nc);
+        (const float *)h->mat[2], (const float *)h->mat[3], (const float *)h->V[h->cur],
+        h->has_kv ? (const float *)h->kveta : nullptr, dev, dev + npt * nc);
   else
     sem2d_detail::strain_stress_kernel<double><<<blocks, 256, 0, h->stream>>>(
         (const double *)D, h->ndof, N, h->nx, h->nz, h->pitch, h->plane, h->d_row0, (const double *)h->geo[0],
         (const double *)h->geo[1], dH, h->mat_elem, h->mat_iso, (const double *)h->mat[0],
-        (const double *)h->mat[1], (const double *)h->mat[2], (const double *)h->mat[3], dev, dev + npt * nc);
+        (const double *)h->mat[1], (const double *)h->mat[2], (const double *)h->mat[3],
+        (const double *)h->V[h->cur], h->has_kv ? (const double *)h->kveta : nullptr, dev, dev + npt * nc);
   std::vector<double> host((size_t)npt * nc * 2);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(host.data(), dev, sizeof(double) * host.size(), cudaMemcpyDeviceToHost, h->stream);

@@ -195,18 +195,15 @@ def write_snapshot(path, solver, index, fields="V"):
     """The binary snapshot files of one output time for the SNAP_DEF
     `fields` letters D, V, A (node fields), E (strain) and S (stress);
     `index` is the NNN of the file names; A needs a handle that keeps the
-    accelerations (Newmark, HHT-alpha or 'A' receivers).  The divergence and
-    curl (d, c)
-    are not written; nor is S for Kelvin-Voigt materials, whose snapshot
-    stress the reference takes from d + eta v (MAT_stress_dv,
-    mat_gen.f90:626-641) while the GPU getter gives the elastic stress of d."""
+    accelerations (Newmark, HHT-alpha or 'A' receivers).  S of a
+    Kelvin-Voigt material is the stress of d + eta v, as the reference's
+    (MAT_stress_dv, mat_gen.f90:626-641).  The divergence and curl (d, c)
+    are not written."""
     d = solver.desc
     fields = str(fields)
     bad = set(fields) - set("DVAES")
     if bad:
         raise ValueError("snapshot fields %s are not written" % sorted(bad))
-    if "S" in fields and d.kv_eta:
-        raise ValueError("snapshot stress of a Kelvin-Voigt material is not written")
     os.makedirs(path, exist_ok=True)
     tag = "%03d" % int(index)
     comps = ["y"] if d.ndof == 1 else ["x", "z"]

@@ -21,7 +21,16 @@ CASES = {
     "sh_rupture": lambda: workloads.sh_rupture(scale=0.1, nsteps=150),
     "psv_rsf": lambda: workloads.psv_rsf(scale=0.05, nsteps=150),
     "anisotropic": lambda: decks.anisotropic(),
+    "kelvin_voigt": lambda: _kv(),
 }
+
+
+def _kv():
+    """Kelvin-Voigt material: the stress is that of d + eta v (MAT_stress_dv,
+    mat_gen.f90:626-641), the strain that of d."""
+    dk = workloads.plain_psv(scale=0.2, nsteps=150)
+    dk.materials[0].kv_eta = 0.3
+    return dk
 
 
 @pytest.mark.parametrize("name", list(CASES))
@@ -42,3 +51,7 @@ def test_strain_stress_match_oracle(name, precision):
     tol = 1e-10 if precision == PRECISION_FP64 else 1e-4
     assert rel_l2(eg, eo) <= tol
     assert rel_l2(sg, so) <= tol
+    if name == "kelvin_voigt":  # the viscous part is present
+        m = case.materials[0]
+        mu = m.rho * m.cs ** 2
+        assert rel_l2(sg[:, :, 2, :], 2 * mu * eo[:, :, 2, :]) > 1e-3
