@@ -16,7 +16,9 @@ It reads the reference's own test data (nothing is written from memory):
   EXAMPLES/InaBox/info                        check-mode log: npoin, dt, nt
   EXAMPLES/{LambsProblem,TestSH,Anisotropic,InaBox,
            TestFlt2D_SCEC_TPV3_inplane,RateState,TestFlt1D,
-           Bimaterial_fault}/Par.inp
+           Bimaterial_fault,2.5D_V-shape_rate-and-state,2.5D_inplane,
+           2D_roughness_drag_approximation,Kelvin_Visco_FZ,
+           Velocity_weakening}/Par.inp
                                               the input decks, as text (parinp_*)
   EXAMPLES/RateState/{Ux,Vx,Tau}_{0,3,6,9}km_ascii
                                               the reference's slip, slip rate and shear
@@ -75,7 +77,8 @@ def main(ref):
                                           for x in (0, 3, 6, 9)])
 
     for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState",
-                 "TestFlt1D", "Bimaterial_fault"):
+                 "TestFlt1D", "Bimaterial_fault", "2.5D_V-shape_rate-and-state", "2.5D_inplane",
+                 "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
 
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
