@@ -26,6 +26,8 @@ It reads the reference's own test data (nothing is written from memory):
                                               9 km of its rate-and-state deck
                                               (RateState/Par.inp; provenance of the
                                               traces not recorded: a loose check)
+  EXAMPLES/**/Par*.inp (the others)           the decks the front end refuses, as text
+                                              (refused_*)
   EXAMPLES/TestAbso/data_mat/{stacey,paraxial}_PSV.mat
                                               the reference's misfits of the direct
                                               P (errp) and S (errs) waves against
@@ -80,6 +82,16 @@ def main(ref):
                  "TestFlt1D", "Bimaterial_fault", "2.5D_V-shape_rate-and-state", "2.5D_inplane",
                  "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
+
+    # the other example decks, which the front end refuses (off the GPU path)
+    import glob
+    for f in sorted(glob.glob(os.path.join(ex, "**", "Par*.inp"), recursive=True)):
+        rel = os.path.relpath(f, ex)
+        key = "parinp_" + os.path.dirname(rel).replace("/", "__").replace("+", "_")
+        if os.path.basename(rel) != "Par.inp":
+            key += "__" + os.path.splitext(os.path.basename(rel))[0]
+        if key not in out:
+            out["refused_" + key[len("parinp_"):]] = np.array(open(f).read())
 
     dst = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden.npz")
     np.savez_compressed(dst, **out)

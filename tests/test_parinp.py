@@ -245,3 +245,18 @@ def test_snapshot_files(tmp_path):
 def test_hht_alpha_time_block():
     d = deck_from_parinp("&TIME TotalTime=1d0, courant=0.3d0, kind='HHT-alpha' / &TIME_HHTA alpha=0.6d0, rho=0.9d0 /")
     assert (d.time.kind, d.time.alpha, d.time.rho) == ("hht-alpha", 0.6, 0.9)
+
+
+def test_every_example_deck_is_taken_or_refused(golden):
+    """Each of the reference's example decks either builds (13, run on the
+    GPU by test_gpu_examples.py) or is refused with a ValueError naming the
+    block off the GPU path (17)."""
+    taken = [k for k in golden.files if k.startswith("parinp_")]
+    refused = [k for k in golden.files if k.startswith("refused_")]
+    assert len(taken) == 13 and len(refused) == 17
+    for k in taken:
+        P = Problem(deck_from_parinp(str(golden[k])))
+        assert P.desc().npoin > 0, k
+    for k in refused:
+        with pytest.raises(ValueError):
+            deck_from_parinp(str(golden[k]))
