@@ -23,9 +23,9 @@ between blocks (``#`` comments, anything after the ``/``) is ignored.
                 scalar values (bc_dynflt*.f90)
   &TIME         kind, Dt, Courant, TotalTime, NbSteps + &TIME_NEWMARK or &TIME_HHTA alpha, rho
                 beta, gamma (time.f90:122-315)
-  &SRC_DEF      stf='RICKER', mechanism='FORCE', coord + &STF_RICKER f0,
+  &SRC_DEF      stf='RICKER', mechanism='FORCE', coord or file + &STF_RICKER f0,
                 onset, ampli + &SRC_FORCE angle (src_gen.f90, stf_ricker.f90)
-  &REC_LINE     number, first, last, field, isamp, AtNode (receivers.f90)
+  &REC_LINE     number, first, last or file, field, isamp, AtNode (receivers.f90)
 
 and names the blocks it skips in ``deck.skipped``: plots, snapshots,
 energies, and the option blocks the reference would not read for this deck
@@ -351,9 +351,27 @@ def deck_from_parinp(text, precision=None, base=None):
             if str(it.get("stf", "RICKER")).upper() != "RICKER" or \
                     str(it.get("mechanism", "FORCE")).upper() != "FORCE":
                 raise ValueError("only RICKER force sources are on the GPU path")
-            c = it["coord"]
             src = src or Sources(coords=[])
-            src.coords = list(src.coords) + [(float(c[0]), float(c[1]))]
+            f = str(it.get("file", "")).strip()
+            if f and f.lower() != "none":
+                # one source per line: x, z [, time delay [, relative amplitude]]
+                # (SO_read, src_gen.f90:70-79)
+                t = np.loadtxt(os.path.join(base or ".", f), ndmin=2)
+                n0 = len(src.coords)
+                src.coords = list(src.coords) + [(float(r[0]), float(r[1])) for r in t]
+                if t.shape[1] > 2 or src.tdelay is not None:
+                    td = list(src.tdelay) if src.tdelay is not None else [0.0] * n0
+                    src.tdelay = td + [float(r[2]) if t.shape[1] > 2 else 0.0 for r in t]
+                if t.shape[1] > 3 or src.relamp is not None:
+                    ra = list(src.relamp) if src.relamp is not None else [1.0] * n0
+                    src.relamp = ra + [float(r[3]) if t.shape[1] > 3 else 1.0 for r in t]
+            else:
+                c = it["coord"]
+                src.coords = list(src.coords) + [(float(c[0]), float(c[1]))]
+                if src.tdelay is not None:
+                    src.tdelay = list(src.tdelay) + [0.0]
+                if src.relamp is not None:
+                    src.relamp = list(src.relamp) + [1.0]
         elif name == "STF_RICKER":
             src = src or Sources(coords=[])
             src.f0 = float(it.get("f0", src.f0))
@@ -364,6 +382,11 @@ def deck_from_parinp(text, precision=None, base=None):
             src.angle = float(it.get("angle", 0.0))
         elif name == "REC_LINE":
             rec = Receivers(number=int(it.get("number", 0)))
+            f = str(it.get("file", "")).strip()
+            if f and f.lower() != "none":
+                # station positions, two columns x z (REC_read, receivers.f90:43-44)
+                rec.coords = np.loadtxt(os.path.join(base or ".", f), ndmin=2)[:, :2].copy()  # (n, 2)
+                rec.number = rec.coords.shape[0]
             if "first" in it:
                 rec.first = _pair(it["first"])
             if "last" in it:

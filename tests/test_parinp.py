@@ -260,3 +260,33 @@ def test_every_example_deck_is_taken_or_refused(golden):
     for k in refused:
         with pytest.raises(ValueError):
             deck_from_parinp(str(golden[k]))
+
+
+def test_source_and_receiver_files(tmp_path):
+    """&SRC_DEF file (x, z [, delay [, relative amplitude]] per line,
+    src_gen.f90:70-79) and &REC_LINE file (x z per line, receivers.f90:
+    43-44), read relative to the Par.inp."""
+    (tmp_path / "src.tab").write_text("1000 1000 0.0 1.0\n3000 1200 0.05 0.5\n")
+    (tmp_path / "rec.tab").write_text("500 1500\n1500 1500\n2500 1500\n")
+    text = """
+&GENERAL ngll=5, fmax=10d0, ndof=2 /
+&MESH_DEF method='CARTESIAN' /
+&MESH_CART xlim=0d0,4d3, zlim=0d0,2d3, nelem=40,20 /
+&MATERIAL tag=1, kind='ELAST' /
+&MAT_ELASTIC rho=2670d0, cp=6000d0, cs=3464d0 /
+&TIME TotalTime=0.2d0, courant=0.5d0 /
+&SRC_DEF stf='RICKER', mechanism='FORCE', file='src.tab' /
+&STF_RICKER f0=10d0, onset=0.1d0, ampli=1d0 /
+&SRC_FORCE angle=0d0 /
+&REC_LINE file='rec.tab', field='D' /
+"""
+    (tmp_path / "Par.inp").write_text(text)
+    from sem2dpack_gb300.parinp import load_parinp
+    d = load_parinp(str(tmp_path / "Par.inp"))
+    assert d.sources.coords == [(1000.0, 1000.0), (3000.0, 1200.0)]
+    assert d.sources.tdelay == [0.0, 0.05] and d.sources.relamp == [1.0, 0.5]
+    assert d.receivers.number == 3 and d.receivers.coords.shape == (3, 2)
+    P = Problem(d)
+    desc = P.desc()
+    assert desc.nsrc == 2 and desc.nrec == 3
+    np.testing.assert_allclose(P.rec_coord()[0], [500.0, 1500.0, 2500.0])
