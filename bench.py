@@ -53,7 +53,7 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--workload", default="sh_rupture",
-                   choices=["sh_rupture", "plain_psv", "psv_rsf", "batch_shots", "gradient_shots"])
+                   choices=["sh_rupture", "plain_psv", "psv_rsf", "batch_shots", "gradient_shots", "tpv3_inplane"])
     p.add_argument("--nsim", type=int, default=256, help="problems of the batch_shots workload")
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
@@ -73,6 +73,11 @@ def make_workload(args):
     elif args.workload == "psv_rsf":
         pair = workloads.psv_rsf(scale=args.scale, precision=prec)
         name = "P-SV rate-and-state rupture (aging), von Karman medium, 1024x512 elements, NGLL=5"
+    elif args.workload == "tpv3_inplane":
+        # the reference's TPV3 in-plane example refined 8x in each direction
+        pair = workloads.tpv3_inplane(scale=8.0 * args.scale, precision=prec)
+        name = ("SCEC TPV3 in-plane example refined 8x: 560x320 elements, NGLL=6, Newmark, Kelvin-Voigt band, "
+                "one-sided SWF fault, Dirichlet side, 16 s")
     else:
         pair = workloads.plain_psv(scale=args.scale, precision=prec)
         name = "plain P-SV elastic, 100x100 elements of 100 m, NGLL=5, 2000 steps"
@@ -490,6 +495,9 @@ def main():
     kms = sim.step_timed(nt)
     bulk_ms = kms[0] / nt
     bpn = BYTES_PER_NODE_STEP[(ndof, dtype)]
+    if args.workload == "tpv3_inplane":
+        # Newmark: + read/write of the accelerations; Kelvin-Voigt: + eta
+        bpn = (4 if dtype == "f32" else 8) * (4 + 4 + 4 + 1 + 2 + 1)
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
     kernel = "march_step_kernel" if sim.tile[0] == MARCH_TX else "strip_step_kernel"

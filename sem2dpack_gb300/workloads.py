@@ -267,3 +267,42 @@ def build(deck_or_pair):
         deck, grid = deck_or_pair
         return Problem(deck, grid)
     return Problem(deck_or_pair)
+
+
+def tpv3_inplane(scale=1.0, nsteps=None, precision=abi.PRECISION_MIXED):
+    """The reference's SCEC TPV3 in-plane example (EXAMPLES/
+    TestFlt2D_SCEC_TPV3_inplane/Par.inp) with its element count multiplied
+    by `scale` in each direction (the domain stays 35 x 20 km): NGLL=6,
+    Newmark, a Kelvin-Voigt band eta = 0.1 exp(-(z/282.094 m)^2) (x dt)
+    along a one-sided slip-weakening fault on the bottom side (shear stress
+    81.6 MPa within 1.5 km of x = 0, 70 MPa beyond; static friction 0.677
+    within 15 km, 1e4 beyond), v = 'D' on the left side, absorbing right and
+    top sides.  16 s of simulated time unless `nsteps` is given."""
+    from .distributions import Dist
+    nx, nz = max(4, int(round(70 * scale))), max(4, int(round(40 * scale)))
+    deck = ParDeck(
+        ngll=6, ndof=2, fmax=3.0, xlim=(0.0, 35.0e3), zlim=(0.0, 20.0e3), nelem=(nx, nz),
+        materials=[Material(tag=1, rho=2670.0, cp=6000.0, cs=3464.0, kv_eta=0.0)],
+        absorbing=[2, 3], dirneu=[(4, "N", "D", False)],
+        fault=Fault(tags=(1, 0), friction="SWF", swf_kind=1, normal_kind=1, opening=True),
+        time=Time(kind="newmark", courant=0.55, total_time=0.0 if nsteps else 16.0, nsteps=nsteps or 0),
+        receivers=Receivers(number=10, first=(0.0, 500.0), last=(15.0e3, 500.0), isamp=20, atnode=False,
+                            field="V"),
+        precision=precision,
+    )
+    grid = Grid(deck)
+    xz = grid.coord()
+    n1, _ = grid.fault_nodes()
+    x, z = xz[0, n1 - 1], xz[1, n1 - 1]
+    tt = Dist("PWCONR", {"num": 2}, [1.5e3, 81.6e6, 70.0e6])
+    mus = Dist("PWCONR", {"num": 2}, [15.0e3, 0.677, 1.0e4])
+    deck.fault.values = {"Tn": -120.0e6, "Tt": tt(x, z), "swf_mus": mus(x, z), "swf_mud": 0.525, "swf_dc": 0.4}
+    deck.fault.oxi = (1, 65, 4)
+    ib = grid.ibool() - 1
+    px, pz = xz[0][ib], xz[1][ib]
+    eta = Dist("GAUSSIAN", {"length": [1.0e6, 282.094], "ampli": 0.1}, [])
+    shape = ib.shape
+    deck.hetero = {"rho": np.full(shape, 2670.0), "cp": np.full(shape, 6000.0), "cs": np.full(shape, 3464.0),
+                   "kveta": eta(px.ravel(), pz.ravel()).reshape(shape)}
+    deck.materials[0].hetero = True
+    return deck, grid
