@@ -290,3 +290,17 @@ def test_source_and_receiver_files(tmp_path):
     desc = P.desc()
     assert desc.nsrc == 2 and desc.nrec == 3
     np.testing.assert_allclose(P.rec_coord()[0], [500.0, 1500.0, 2500.0])
+
+
+def test_tpv3_workload_restates_the_example(golden):
+    """workloads.tpv3_inplane(scale=1) builds the same problem as the
+    reference's TPV3 in-plane deck parsed from its Par.inp."""
+    a = Problem(deck_from_parinp(str(golden["parinp_TestFlt2D_SCEC_TPV3_inplane"])))
+    b = workloads.build(workloads.tpv3_inplane(1.0))
+    da, db = a.desc(), b.desc()
+    assert (da.npoin, da.nt, da.dt, da.nflt, da.nrec, da.ndir) == (db.npoin, db.nt, db.dt, db.nflt, db.nrec, db.ndir)
+    for name, n in (("rmass", 2 * da.npoin), ("kv_eta", 36 * da.nelem), ("flt_T0", 2 * da.nflt),
+                    ("swf_mus", da.nflt), ("rec_interp", 36 * da.nrec)):
+        x = np.ctypeslib.as_array(getattr(da, name), shape=(n,))
+        y = np.ctypeslib.as_array(getattr(db, name), shape=(n,))
+        assert np.array_equal(x, y), name
