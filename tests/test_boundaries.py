@@ -208,3 +208,22 @@ def test_testflt1d_steady_slip_rate(golden):
     assert abs(f[0, 1, late].mean() / 2.2 - 1) < 5e-3
     np.testing.assert_allclose(f[0, 1, late], 2.2, rtol=0.03)
     np.testing.assert_allclose(f[0, 2, late], -1.1, rtol=1e-9)
+
+
+def test_oracle_hht_alpha_one_is_newmark():
+    """HHT-alpha with alpha = 1 is the explicit Newmark scheme (beta = 0,
+    gamma = 1/2; time.f90:230-236): the oracle's two paths agree bit for
+    bit, and alpha = 0.5 differs."""
+    from sem2dpack_gb300.deck import Time
+    out = []
+    for kind, alpha in (("newmark", 1.0), ("hht-alpha", 1.0), ("hht-alpha", 0.5)):
+        dk = small_box(False)
+        dk.time = Time(kind=kind, nsteps=150, courant=0.3, alpha=alpha, rho=0.5)
+        P = Problem(dk)
+        d = P.desc()
+        d.precision = PRECISION_FP64
+        o = po.OracleSim(d, owner=P)
+        o.run(150)
+        out.append(o.seismograms())
+    assert np.array_equal(out[0], out[1])
+    assert np.linalg.norm(out[2] - out[0]) > 1e-6 * np.linalg.norm(out[0])
