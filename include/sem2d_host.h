@@ -153,6 +153,12 @@ typedef struct sem2d_deck {
   /* 1: record the fault potency every step (the FltXX_potency_sem2d.tab
    * file of the reference, bc_dynflt.f90:436,757)                        */
   int flt_potency;
+  /* &SRC_DEF mechanism (src_moment.f90:27-110): 0 FORCE, 1 EXPLOSION,
+   * 2 DOUBLE_COUPLE (&SRC_DOUBLE_COUPLE dip, degrees), 3 MOMENT
+   * (&SRC_MOMENT Mxx, Mxz, Mzx, Mzz; SH: Myx, Myz in src_M[0], src_M[1]) */
+  int src_mech;
+  double src_M[4];
+  double src_dip;
 } sem2d_deck;
 
 typedef struct sem2d_grid sem2d_grid;

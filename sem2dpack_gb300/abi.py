@@ -152,6 +152,7 @@ class Deck(C.Structure):
         ("twf_X", c_double), ("twf_Z", c_double), ("twf_V", c_double), ("twf_L", c_double),
         ("twf_T", c_double), ("twf_Dc", c_double),
         ("flt_potency", c_int),
+        ("src_mech", c_int), ("src_M", c_double * 4), ("src_dip", c_double),
     ]
 
 

@@ -1215,15 +1215,107 @@ void src_init(sem2d_problem &P, const sem2d_deck &dk) {
   if (f0 <= 0.0f) throw BuildError("RICKER_read: f0 must be positive");
   if (onset < 1.0f / f0) throw BuildError("warning: RICKER_read: Onset time too small");
   const double ang = dk.force_angle * kPi / 180.0;
-  for (int k = 0; k < ns; ++k) {
-    P.src_node.push_back(nearest_node(*P.g, dk.src_coord + 2 * k));
-    P.src_dir.push_back(-std::sin(ang));
-    P.src_dir.push_back(std::cos(ang));
+  auto push = [&](int node, double dx, double dz, double rel, double td) {
+    P.src_node.push_back(node);
+    P.src_dir.push_back(dx);
+    P.src_dir.push_back(dz);
     P.src_f0.push_back(double(f0));
     P.src_t0.push_back(double(onset));
     P.src_amp.push_back(double(amp));
-    P.src_rel.push_back(dk.src_ampli ? dk.src_ampli[k] : 1.0);
-    P.src_tdelay.push_back(dk.src_tdelay ? dk.src_tdelay[k] : 0.0);
+    P.src_rel.push_back(rel);
+    P.src_tdelay.push_back(td);
+  };
+  if (dk.src_mech == 0) {
+    for (int k = 0; k < ns; ++k)
+      push(nearest_node(*P.g, dk.src_coord + 2 * k), -std::sin(ang), std::cos(ang),
+           dk.src_ampli ? dk.src_ampli[k] : 1.0, dk.src_tdelay ? dk.src_tdelay[k] : 0.0);
+    return;
+  }
+  // SRC_MOMENT_read (src_moment.f90:27-110): the tensor M(2,ndof)
+  const int nd = P.ndof;
+  double M[2][2] = {{0, 0}, {0, 0}};
+  if (dk.src_mech == 1) {
+    if (nd != 2) throw BuildError("SRC_MOMENT_read: explosion only allowed in PSV (ndof=2)");
+    M[0][0] = 1.0;
+    M[1][1] = 1.0;
+  } else if (dk.src_mech == 2) {
+    const double dip = dk.src_dip * kPi / 180.0, n0 = std::sin(dip), n1 = std::cos(dip);
+    if (nd == 2) {
+      const double r0 = -std::cos(dip), r1 = std::sin(dip);
+      M[0][0] = 2.0 * r0 * n0;
+      M[0][1] = r0 * n1 + r1 * n0;
+      M[1][0] = M[0][1];
+      M[1][1] = 2.0 * r1 * n1;
+    } else {
+      M[0][0] = n0;
+      M[1][0] = n1;
+    }
+  } else if (dk.src_mech == 3) {
+    if (nd == 2) {
+      M[0][0] = dk.src_M[0];
+      M[0][1] = dk.src_M[1];
+      M[1][0] = dk.src_M[2];
+      M[1][1] = dk.src_M[3];
+    } else {
+      M[0][0] = dk.src_M[0];
+      M[1][0] = dk.src_M[1];
+    }
+  } else {
+    throw BuildError("unknown source mechanism");
+  }
+  // SRC_MOMENT_init / SRC_MOMENT_add (src_moment.f90:118-175): in every
+  // element holding the source node (i, j), the row of nodes (:, j) gets
+  // G(c,1) h'_l(xi_i) and the column (i, :) G(c,2) h'_l(eta_j), with
+  // G = M jac_inv^T (SH: G = jac_inv M(:,1)); here the coefficients are
+  // summed per node into point forces of the same time function
+  const sem2d_grid &g = *P.g;
+  const int N = g.ngll;
+  for (int k = 0; k < ns; ++k) {
+    const int node = nearest_node(g, dk.src_coord + 2 * k);
+    const double rel = dk.src_ampli ? dk.src_ampli[k] : 1.0, td = dk.src_tdelay ? dk.src_tdelay[k] : 0.0;
+    std::vector<int> nodes;
+    std::vector<double> F;  // 2 per node
+    auto add = [&](int n, double fx, double fz) {
+      for (size_t q = 0; q < nodes.size(); ++q)
+        if (nodes[q] == n) {
+          F[2 * q] += fx;
+          F[2 * q + 1] += fz;
+          return;
+        }
+      nodes.push_back(n);
+      F.push_back(fx);
+      F.push_back(fz);
+    };
+    for (int e = 0; e < g.nelem; ++e)
+      for (int j = 0; j < N; ++j)
+        for (int i = 0; i < N; ++i) {
+          if (g.ibool[i + N * (j + size_t(N) * e)] != node) continue;
+          double c8[8], J[4];
+          g.corners(e, c8);
+          jacobian(c8, g.gll.x[i], g.gll.x[j], J);
+          const double det = J[0] * J[3] - J[2] * J[1];
+          const double inv[2][2] = {{J[3] / det, -J[2] / det}, {-J[1] / det, J[0] / det}};  // d(xi,eta)/d(x,z)
+          double G[2][2];
+          if (nd == 2) {
+            for (int a = 0; a < 2; ++a)
+              for (int b = 0; b < 2; ++b) G[a][b] = M[a][0] * inv[b][0] + M[a][1] * inv[b][1];
+          } else {
+            G[0][0] = inv[0][0] * M[0][0] + inv[0][1] * M[1][0];
+            G[0][1] = inv[1][0] * M[0][0] + inv[1][1] * M[1][0];
+            G[1][0] = G[1][1] = 0.0;
+          }
+          for (int l = 0; l < N; ++l) {
+            const double hx = g.gll.H[l + N * i], he = g.gll.H[l + N * j];
+            add(g.ibool[l + N * (j + size_t(N) * e)], G[0][0] * hx, G[1][0] * hx);
+            add(g.ibool[i + N * (l + size_t(N) * e)], G[0][1] * he, G[1][1] * he);
+          }
+        }
+    for (size_t q = 0; q < nodes.size(); ++q) {
+      if (nd == 2)
+        push(nodes[q], F[2 * q], F[2 * q + 1], rel, td);
+      else  // SH: the force is the amplitude itself
+        push(nodes[q], 1.0, 0.0, rel * F[2 * q], td);
+    }
   }
 }
 

@@ -104,6 +104,11 @@ class Sources:
     angle: float = 0.0
     tdelay: Optional[Sequence[float]] = None
     relamp: Optional[Sequence[float]] = None
+    # mechanism (src_moment.f90): FORCE (angle), EXPLOSION, DOUBLE_COUPLE
+    # (dip, degrees) or MOMENT (M = Mxx, Mxz, Mzx, Mzz; SH: Myx, Myz)
+    mechanism: str = "FORCE"
+    dip: float = 90.0
+    M: Tuple[float, float, float, float] = (0.0, 0.0, 0.0, 0.0)
 
 
 @dataclass
@@ -260,6 +265,12 @@ class ParDeck:
                     setattr(d, attr, _dptr(arr))
             d.ricker_f0, d.ricker_onset, d.ricker_ampli = s.f0, s.onset, s.ampli
             d.force_angle = s.angle
+            mechs = {"FORCE": 0, "EXPLOSION": 1, "DOUBLE_COUPLE": 2, "MOMENT": 3}
+            if s.mechanism.upper() not in mechs:
+                raise ValueError("source mechanism %s is not on the GPU path" % s.mechanism)
+            d.src_mech = mechs[s.mechanism.upper()]
+            d.src_M[:] = [float(v) for v in s.M]
+            d.src_dip = s.dip
         r = self.receivers
         if r is not None:
             if r.coords is not None:

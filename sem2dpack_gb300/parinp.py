@@ -348,10 +348,12 @@ def deck_from_parinp(text, precision=None, base=None):
             time.alpha = float(it.get("alpha", 0.5))
             time.rho = float(it.get("rho", 0.5))
         elif name == "SRC_DEF":
+            mech = str(it.get("mechanism", "FORCE")).upper()
             if str(it.get("stf", "RICKER")).upper() != "RICKER" or \
-                    str(it.get("mechanism", "FORCE")).upper() != "FORCE":
-                raise ValueError("only RICKER force sources are on the GPU path")
+                    mech not in ("FORCE", "EXPLOSION", "DOUBLE_COUPLE", "MOMENT"):
+                raise ValueError("only RICKER force and moment sources are on the GPU path")
             src = src or Sources(coords=[])
+            src.mechanism = mech
             f = str(it.get("file", "")).strip()
             if f and f.lower() != "none":
                 # one source per line: x, z [, time delay [, relative amplitude]]
@@ -377,6 +379,15 @@ def deck_from_parinp(text, precision=None, base=None):
             src.f0 = float(it.get("f0", src.f0))
             src.onset = float(it.get("onset", src.onset))
             src.ampli = float(it.get("ampli", src.ampli))
+        elif name == "SRC_MOMENT":
+            src = src or Sources(coords=[])
+            if "myx" in it or "myz" in it:
+                src.M = (float(it.get("myx", 0.0)), float(it.get("myz", 0.0)), 0.0, 0.0)
+            else:
+                src.M = tuple(float(it.get(k, 0.0)) for k in ("mxx", "mxz", "mzx", "mzz"))
+        elif name == "SRC_DOUBLE_COUPLE":
+            src = src or Sources(coords=[])
+            src.dip = float(it.get("dip", 90.0))
         elif name == "SRC_FORCE":
             src = src or Sources(coords=[])
             src.angle = float(it.get("angle", 0.0))

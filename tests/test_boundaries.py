@@ -227,3 +227,57 @@ def test_oracle_hht_alpha_one_is_newmark():
         out.append(o.seismograms())
     assert np.array_equal(out[0], out[1])
     assert np.linalg.norm(out[2] - out[0]) > 1e-6 * np.linalg.norm(out[0])
+
+
+@pytest.mark.parametrize("mech", ["EXPLOSION", "DOUBLE_COUPLE", "MOMENT"])
+def test_moment_source_point_forces(mech):
+    """Moment sources (SRC_MOMENT_init/add, src_moment.f90:118-175) become
+    point forces on the rows and columns through the source node of every
+    element holding it: they sum to zero and their first moment is
+    (elements holding the node) x M, since sum_l x_l h'_l = dx/dxi."""
+    dk = small_box(False)
+    dk.sources.mechanism = mech
+    dk.sources.dip = 60.0
+    dk.sources.M = (1.0, 0.3, 0.3, -0.5)
+    dk.sources.coords = [(-1100.0, -700.0)]  # a node shared by four elements
+    P = Problem(dk)
+    d = P.desc()
+    n = d.nsrc
+    node = arr(d, "src_node", n) - 1
+    F = arr(d, "src_dir", 2 * n).reshape(n, 2)
+    xz = P.grid.coord()
+    np.testing.assert_allclose(F.sum(axis=0), 0.0, atol=1e-15)
+    first = np.array([[np.sum(F[:, c] * xz[dd, node]) for dd in range(2)] for c in range(2)])
+    if mech == "EXPLOSION":
+        M = np.eye(2)
+    elif mech == "DOUBLE_COUPLE":
+        dip = np.radians(60.0)
+        nv, r = np.array([np.sin(dip), np.cos(dip)]), np.array([-np.cos(dip), np.sin(dip)])
+        M = np.outer(r, nv) + np.outer(nv, r)
+    else:
+        M = np.array([[1.0, 0.3], [0.3, -0.5]])
+    np.testing.assert_allclose(first, 4 * M, rtol=1e-12, atol=1e-12)
+    d.precision = PRECISION_FP64
+    o = po.OracleSim(d, owner=P)
+    o.run(100)
+    assert np.isfinite(o.seismograms()).all() and np.abs(o.seismograms()).max() > 0
+
+
+def test_moment_source_parinp():
+    text = """
+&GENERAL ngll=5, fmax=10d0, ndof=2 /
+&MESH_DEF method='CARTESIAN' /
+&MESH_CART xlim=0d0,4d3, zlim=0d0,2d3, nelem=40,20 /
+&MATERIAL tag=1, kind='ELAST' /
+&MAT_ELASTIC rho=2670d0, cp=6000d0, cs=3464d0 /
+&TIME TotalTime=0.2d0, courant=0.5d0 /
+&SRC_DEF stf='RICKER', mechanism='MOMENT', coord=2d3,1d3 /
+&STF_RICKER f0=10d0, onset=0.1d0, ampli=1d0 /
+&SRC_MOMENT Mxx=1d0, Mxz=0d0, Mzx=0d0, Mzz=-1d0 /
+"""
+    d = deck_from_parinp(text)
+    assert d.sources.mechanism == "MOMENT" and d.sources.M == (1.0, 0.0, 0.0, -1.0)
+    P = Problem(d)
+    # the element corner at the source: a 9-node line across two elements in
+    # x and one in z, sharing the node
+    assert P.desc().nsrc == 9 + 9 - 1

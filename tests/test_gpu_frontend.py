@@ -98,3 +98,27 @@ def test_ratestate_example_against_reference_traces(golden, precision):
     g = Solver(d, owner=P)
     g.run()
     check_ratestate(P, g.fault_series(), golden)
+
+
+@pytest.mark.parametrize("mech", ["EXPLOSION", "DOUBLE_COUPLE", "MOMENT"])
+@pytest.mark.parametrize("ndof", [1, 2])
+def test_moment_sources_against_oracle(mech, ndof):
+    """Explosion, double-couple and moment-tensor sources (point forces on
+    the lines through the source node, src_moment.f90:118-175), FP64."""
+    from oracle import pyoracle as po
+    from sem2dpack_gb300 import PRECISION_FP64, workloads
+    if mech == "EXPLOSION" and ndof == 1:
+        pytest.skip("explosions are P-SV only (src_moment.f90:56-57)")
+    dk = workloads.plain_psv(scale=0.2, nsteps=200)
+    dk.ndof = ndof
+    dk.sources.mechanism, dk.sources.dip, dk.sources.M = mech, 30.0, (1.0, 0.4, 0.4, -0.7)
+    P = Problem(dk)
+    d = P.desc()
+    d.precision = PRECISION_FP64
+    g = Solver(d, owner=P)
+    g.step(200)
+    o = po.OracleSim(d, owner=P)
+    o.run(200)
+    s_g, s_o = g.seismograms(), o.seismograms()
+    assert np.abs(s_o).max() > 0
+    assert np.linalg.norm(s_g - s_o) / np.linalg.norm(s_o) <= 1e-10
