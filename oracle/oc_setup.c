@@ -50,6 +50,11 @@ struct oc_setup {
   int nabs;
   int *abs_node;
   double *abs_C;     /* (nabs,ndof) */
+  /* Stacey P3 terms, one per (boundary element, edge point) */
+  int nst;
+  int *st_node, *st_k, *st_edge;
+  double *st_K;      /* (nst,2) once the build ends; K(:,1) then K(:,2) while it grows */
+  double *st_K1;
   /* fault */
   int nflt, two_sides;
   int *node1, *node2;
@@ -858,7 +863,23 @@ static void build_mass(oc_setup *s) {
 }
 
 /* BC_ABSO_init (bc_abso.f90:115-266) */
-static int abso_init(oc_setup *s, int tag, char *err, int el) {
+/* append one Stacey P3 term (BC_ABSO_init, bc_abso.f90:174-218) */
+static void st_push(oc_setup *s, int node, int k, const int *edge, double K0, double K1) {
+  int n = s->ngll, m = s->nst + 1;
+  s->st_node = realloc(s->st_node, (size_t)m * sizeof(int));
+  s->st_k = realloc(s->st_k, (size_t)m * sizeof(int));
+  s->st_edge = realloc(s->st_edge, (size_t)m * n * sizeof(int));
+  s->st_K = realloc(s->st_K, (size_t)m * sizeof(double));
+  s->st_K1 = realloc(s->st_K1, (size_t)m * sizeof(double));
+  s->st_node[s->nst] = node;
+  s->st_k[s->nst] = k;
+  memcpy(s->st_edge + (size_t)s->nst * n, edge, (size_t)n * sizeof(int));
+  s->st_K[s->nst] = K0;
+  s->st_K1[s->nst] = K1;
+  s->nst = m;
+}
+
+static int abso_init(oc_setup *s, int tag, int stacey, char *err, int el) {
   oc_bnd *bd = find_bnd(s, tag);
   if (!bd) return 0;
   int n = s->ngll, nd = s->ndof, np = bd->npoin;
@@ -899,6 +920,16 @@ static int abso_init(oc_setup *s, int tag, char *err, int el) {
       } else {
         C[bk] = C[bk] + rho * c[0] * ci;
         C[bk + np] = C[bk + np] + rho * c[1] * ci;
+      }
+      if (stacey && nd == 2) {
+        /* K(k,1,e) = CoefIntegr dloc_t/dx_t rho cs (2 cs - cp); K(:,2) = K(:,1);
+         * the tangential component negated */
+        double det = jac[0] * jac[3] - jac[2] * jac[1];
+        double inv[2][2] = {{jac[3] / det, -jac[2] / det}, {-jac[1] / det, jac[0] / det}};
+        double K0 = ci * inv[ldim][gtan] * (rho * c[gtan] * (2.0 * c[gtan] - c[gnor]));
+        int edge[32];
+        for (int l = 0; l < n; l++) edge[l] = bd->node[bd->ibool[l + n * q] - 1];
+        st_push(s, bd->node[bk], k, edge, gtan == 0 ? -K0 : K0, gtan == 1 ? -K0 : K0);
       }
     }
   }
@@ -1238,12 +1269,16 @@ oc_setup *oc_setup_build(const sem2d_deck *dk, char *err, int el) {
   for (int b = 0; b < dk->nbcs; b++) {
     const sem2d_bc *bc = &dk->bcs[b];
     if (bc->kind == SEM2D_BC_ABSORB) {
-      if (abso_init(s, bc->tag[0], err, el)) goto fail;
+      if (abso_init(s, bc->tag[0], bc->stacey, err, el)) goto fail;
     } else if (bc->kind == SEM2D_BC_DYNFLT) {
       if (dynflt_init(s, dk, bc->tag, err, el)) goto fail;
     }
   }
   if (rec_init(s, dk, err, el) || src_init(s, dk, err, el)) goto fail;
+  if (s->nst) {  /* Stacey K(nst,2): the first components, then the second */
+    s->st_K = realloc(s->st_K, 2 * (size_t)s->nst * sizeof(double));
+    memcpy(s->st_K + s->nst, s->st_K1, (size_t)s->nst * sizeof(double));
+  }
   /* invert the mass matrix (init.f90:112-116) */
   for (size_t q = 0; q < (size_t)s->npoin * s->ndof; q++) s->rmass[q] = 1.0 / s->rmass[q];
   return s;
@@ -1262,6 +1297,7 @@ void oc_setup_free(oc_setup *s) {
   free(s->ibool); free(s->coord);
   free(s->rho); free(s->cp); free(s->cs); free(s->Kx); free(s->Kz); free(s->la); free(s->mu);
   free(s->mux); free(s->kveta); free(s->rmass); free(s->abs_node); free(s->abs_C);
+  free(s->st_node); free(s->st_k); free(s->st_edge); free(s->st_K); free(s->st_K1);
   free(s->node1); free(s->node2); free(s->fcoord); free(s->n1); free(s->B); free(s->invM1);
   free(s->invM2); free(s->Z); free(s->T0); free(s->coh);
   for (int q = 0; q < SEM2D_FP_NPARAM; q++) free(s->prm[q]);
@@ -1326,6 +1362,11 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
   d->nabs = s->nabs;
   d->abs_node = s->abs_node;
   d->abs_C = s->abs_C;
+  d->nstacey = s->nst;
+  d->stacey_node = s->st_node;
+  d->stacey_k = s->st_k;
+  d->stacey_edge = s->st_edge;
+  d->stacey_K = s->st_K;
   d->time_scheme = s->time_kind;
   d->dt = s->dt;
   d->beta = s->beta;

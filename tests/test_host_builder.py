@@ -139,3 +139,22 @@ def test_hht_alpha_problem_bit_exact():
     dk.time.alpha = 1.5
     with pytest.raises(Exception):
         Problem(dk, g)
+
+
+def test_stacey_problem_bit_exact():
+    """The Stacey P3 terms (BC_ABSO_init, bc_abso.f90:174-218): the product
+    builder and the oracle's restated setup agree bit for bit."""
+    dk = decks.test_abso(-1.0e3, 12, True)
+    dk.ngll, dk.fmax, dk.nelem = 5, 20.0, (24, 15)
+    dk.xlim, dk.zlim = (-1.5e3, 0.9e3), (-1.0e3, 0.5e3)
+    dk.sources.coords = [(-1100.0, -700.0)]
+    dk.sources.f0, dk.sources.onset = 10.0, 0.1
+    dk.receivers.first, dk.receivers.last = (-1500.0, -1000.0), (900.0, -1000.0)
+    dk.receivers.number = 25
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    n = a.nstacey
+    assert n == b.nstacey == (2 * 24 + 2 * 15) * 5
+    for name, m in (("stacey_node", n), ("stacey_k", n), ("stacey_edge", 5 * n), ("stacey_K", 2 * n)):
+        assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
