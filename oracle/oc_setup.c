@@ -55,6 +55,11 @@ struct oc_setup {
   int *st_node, *st_k, *st_edge;
   double *st_K;      /* (nst,2) once the build ends; K(:,1) then K(:,2) while it grows */
   double *st_K1;
+  /* periodic node pairs and zero-Dirichlet components */
+  int nper;
+  int *per_m, *per_s;
+  int ndir;
+  int *dir_node, *dir_comp, *dir_after;
   /* fault */
   int nflt, two_sides;
   int *node1, *node2;
@@ -639,7 +644,7 @@ static oc_bnd *find_bnd(oc_setup *s, int tag) {
 }
 
 /* BC_get_normal_and_weights (spec_grid.f90:961-1011) */
-static void normal_and_weights(oc_setup *s, oc_bnd *bd, double *norm /* (np,2) */, double *w) {
+static void normal_and_weights(oc_setup *s, oc_bnd *bd, double *norm /* (np,2) */, double *w, int periodic) {
   int n = s->ngll, np = bd->npoin;
   int it[32], jt[32];
   for (int k = 0; k < 2 * np; k++) norm[k] = 0.0;
@@ -662,6 +667,14 @@ static void normal_and_weights(oc_setup *s, oc_bnd *bd, double *norm /* (np,2) *
       norm[bn + np] = norm[bn + np] + (-tx);
       w[bn] = w[bn] + s->wgll[k] * j1;
     }
+  }
+  if (periodic) { /* the two ends are one node (spec_grid.f90:998-1003) */
+    for (int c = 0; c < 2; c++) {
+      norm[0 + np * c] = norm[0 + np * c] + norm[(np - 1) + np * c];
+      norm[(np - 1) + np * c] = norm[0 + np * c];
+    }
+    w[0] = w[0] + w[np - 1];
+    w[np - 1] = w[0];
   }
   for (int q = 0; q < bd->nelem; q++) {
     int ends[2] = {bd->ibool[0 + n * q] - 1, bd->ibool[(n - 1) + n * q] - 1};
@@ -879,12 +892,82 @@ static void st_push(oc_setup *s, int node, int k, const int *edge, double K0, do
   s->nst = m;
 }
 
+/* BC_PERIO_intersects (bc_periodic.f90:108-121) */
+static int perio_intersects(const oc_setup *s, const oc_bnd *bd) {
+  int first = 0, last = 0;
+  for (int k = 0; k < s->nper; k++) {
+    if (s->per_m[k] == bd->node[0] || s->per_s[k] == bd->node[0]) first = 1;
+    if (s->per_m[k] == bd->node[bd->npoin - 1] || s->per_s[k] == bd->node[bd->npoin - 1]) last = 1;
+  }
+  return s->nper > 0 && bd->npoin > 0 && first && last;
+}
+
+/* BC_PERIO_init (bc_periodic.f90:42-72): pair the two sides' nodes in list
+ * order, check the shift, sum the mass on the master and copy it */
+static int perio_init(oc_setup *s, const int *tags, char *err, int el) {
+  oc_bnd *m = find_bnd(s, tags[0]), *q = find_bnd(s, tags[1]);
+  if (!m || !q) return seterr(err, el, "bc_perio_init: boundary tag not found"), -1;
+  if (m->nelem != q->nelem) return seterr(err, el, "bc_perio_init: number of boundary elements do not match"), -1;
+  if (m->npoin != q->npoin) return seterr(err, el, "bc_perio_init: number of nodes on boundaries do not match"), -1;
+  const double *c0m = s->coord + 2 * (size_t)(m->node[0] - 1), *c0s = s->coord + 2 * (size_t)(q->node[0] - 1);
+  double sh1 = c0m[0] - c0s[0], sh2 = c0m[1] - c0s[1];
+  for (int k = 0; k < m->npoin; k++) {
+    const double *cm = s->coord + 2 * (size_t)(m->node[k] - 1), *cs = s->coord + 2 * (size_t)(q->node[k] - 1);
+    if (fabs(cm[0] - cs[0] - sh1) > TINY_XABS || fabs(cm[1] - cs[1] - sh2) > TINY_XABS)
+      return seterr(err, el, "bc_perio_init: coordinates on boundaries do not match properly"), -1;
+  }
+  for (int d = 0; d < s->ndof; d++)
+    for (int k = 0; k < m->npoin; k++) {
+      double *a = &s->rmass[(size_t)(m->node[k] - 1) + (size_t)s->npoin * d];
+      double *b = &s->rmass[(size_t)(q->node[k] - 1) + (size_t)s->npoin * d];
+      *a = *a + *b;
+      *b = *a;
+    }
+  s->nper = m->npoin;
+  s->per_m = xcalloc((size_t)s->nper, sizeof(int));
+  s->per_s = xcalloc((size_t)s->nper, sizeof(int));
+  memcpy(s->per_m, m->node, (size_t)s->nper * sizeof(int));
+  memcpy(s->per_s, q->node, (size_t)s->nper * sizeof(int));
+  return 0;
+}
+
+/* BC_DIRNEU_init (bc_dirneu.f90:117-143): the components flagged 'D' */
+static int dirneu_init(oc_setup *s, int tag, int mask, int after, char *err, int el) {
+  oc_bnd *bd = find_bnd(s, tag);
+  if (!bd) return 0;
+  int np = bd->npoin;
+  double *norm = xcalloc(2 * (size_t)np, sizeof(double)), *w = xcalloc((size_t)np, sizeof(double));
+  normal_and_weights(s, bd, norm, w, perio_intersects(s, bd));
+  int horiz = 1, vert = 1;
+  for (int k = 0; k < np; k++) {
+    if (!(fabs(norm[k]) < TINY_XABS)) horiz = 0;
+    if (!(fabs(norm[k + np]) < TINY_XABS)) vert = 0;
+  }
+  free(norm); free(w);
+  if (!horiz && !vert) return seterr(err, el, "BC_DIRNEU_init: boundary is not vertical or horizontal"), -1;
+  for (int c = 0; c < s->ndof; c++) {
+    if (!((mask >> c) & 1)) continue;
+    int m = s->ndir + np;
+    s->dir_node = realloc(s->dir_node, (size_t)m * sizeof(int));
+    s->dir_comp = realloc(s->dir_comp, (size_t)m * sizeof(int));
+    s->dir_after = realloc(s->dir_after, (size_t)m * sizeof(int));
+    for (int k = 0; k < np; k++) {
+      s->dir_node[s->ndir + k] = bd->node[k];
+      s->dir_comp[s->ndir + k] = c;
+      s->dir_after[s->ndir + k] = after;
+    }
+    s->ndir = m;
+  }
+  return 0;
+}
+
 static int abso_init(oc_setup *s, int tag, int stacey, char *err, int el) {
   oc_bnd *bd = find_bnd(s, tag);
   if (!bd) return 0;
   int n = s->ngll, nd = s->ndof, np = bd->npoin;
+  const int periodic = perio_intersects(s, bd);
   double *norm = xcalloc(2 * (size_t)np, sizeof(double)), *w = xcalloc((size_t)np, sizeof(double));
-  normal_and_weights(s, bd, norm, w);
+  normal_and_weights(s, bd, norm, w, periodic);
   int flat = 1, gtan = 0, gnor = 1;
   int horiz = 1, vert = 1;
   for (int k = 0; k < np; k++) {
@@ -933,6 +1016,15 @@ static int abso_init(oc_setup *s, int tag, int stacey, char *err, int el) {
       }
     }
   }
+  if (periodic && stacey && nd == 2) {
+    free(norm); free(w); free(C);
+    return seterr(err, el, "Stacey sides meeting periodic sides are not supported"), -1;
+  }
+  if (periodic) /* the two ends are one node (bc_abso.f90:227-231) */
+    for (int d = 0; d < nd; d++) {
+      C[0 + np * d] = C[0 + np * d] + C[(np - 1) + np * d];
+      C[(np - 1) + np * d] = C[0 + np * d];
+    }
   double cf = coefA2Vrhs(s);
   for (int d = 0; d < nd; d++)
     for (int k = 0; k < np; k++) {
@@ -980,7 +1072,7 @@ static int dynflt_init(oc_setup *s, const sem2d_deck *dk, const int *tags, char 
   s->node1 = xcalloc((size_t)np, sizeof(int));
   s->node2 = xcalloc((size_t)np, sizeof(int));
   double *tn = xcalloc(2 * (size_t)b1->npoin, sizeof(double)), *tb = xcalloc((size_t)b1->npoin, sizeof(double));
-  normal_and_weights(s, b1, tn, tb);
+  normal_and_weights(s, b1, tn, tb, perio_intersects(s, b1));
   s->n1 = xcalloc(2 * (size_t)np, sizeof(double));
   s->B = xcalloc((size_t)np, sizeof(double));
   int j = 0;
@@ -1265,13 +1357,26 @@ oc_setup *oc_setup_build(const sem2d_deck *dk, char *err, int el) {
     }
   }
   build_mass(s);
-  /* BC_init: the &BC_DEF order decides the mass snapshot of the fault */
+  /* BC_init: periodic sides first (bc_gen.f90:221-228), then the &BC_DEF
+   * order, which decides the mass snapshot of the fault */
+  for (int b = 0; b < dk->nbcs; b++)
+    if (dk->bcs[b].kind == SEM2D_BC_PERIOD) {
+      if (s->nper) {
+        seterr(err, el, "more than one pair of periodic sides");
+        goto fail;
+      }
+      if (perio_init(s, dk->bcs[b].tag, err, el)) goto fail;
+    }
+  int fault_seen = 0;
   for (int b = 0; b < dk->nbcs; b++) {
     const sem2d_bc *bc = &dk->bcs[b];
     if (bc->kind == SEM2D_BC_ABSORB) {
       if (abso_init(s, bc->tag[0], bc->stacey, err, el)) goto fail;
     } else if (bc->kind == SEM2D_BC_DYNFLT) {
       if (dynflt_init(s, dk, bc->tag, err, el)) goto fail;
+      fault_seen = 1;
+    } else if (bc->kind == SEM2D_BC_DIRNEU) {
+      if (dirneu_init(s, bc->tag[0], bc->dirichlet, fault_seen, err, el)) goto fail;
     }
   }
   if (rec_init(s, dk, err, el) || src_init(s, dk, err, el)) goto fail;
@@ -1298,6 +1403,7 @@ void oc_setup_free(oc_setup *s) {
   free(s->rho); free(s->cp); free(s->cs); free(s->Kx); free(s->Kz); free(s->la); free(s->mu);
   free(s->mux); free(s->kveta); free(s->rmass); free(s->abs_node); free(s->abs_C);
   free(s->st_node); free(s->st_k); free(s->st_edge); free(s->st_K); free(s->st_K1);
+  free(s->per_m); free(s->per_s); free(s->dir_node); free(s->dir_comp); free(s->dir_after);
   free(s->node1); free(s->node2); free(s->fcoord); free(s->n1); free(s->B); free(s->invM1);
   free(s->invM2); free(s->Z); free(s->T0); free(s->coh);
   for (int q = 0; q < SEM2D_FP_NPARAM; q++) free(s->prm[q]);
@@ -1367,6 +1473,13 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
   d->stacey_k = s->st_k;
   d->stacey_edge = s->st_edge;
   d->stacey_K = s->st_K;
+  d->nperio = s->nper;
+  d->perio_master = s->per_m;
+  d->perio_slave = s->per_s;
+  d->ndir = s->ndir;
+  d->dir_node = s->dir_node;
+  d->dir_comp = s->dir_comp;
+  d->dir_after_fault = s->dir_after;
   d->time_scheme = s->time_kind;
   d->dt = s->dt;
   d->beta = s->beta;

@@ -158,3 +158,32 @@ def test_stacey_problem_bit_exact():
     assert n == b.nstacey == (2 * 24 + 2 * 15) * 5
     for name, m in (("stacey_node", n), ("stacey_k", n), ("stacey_edge", 5 * n), ("stacey_K", 2 * n)):
         assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
+
+
+@pytest.mark.parametrize("case", ["periodic", "periodic_fault", "dirneu"])
+def test_periodic_and_dirichlet_bit_exact(case):
+    """BC_PERIO_init (summed mass, boundary weights and dashpots at the ends
+    of crossing sides) and BC_DIRNEU_init: the product builder and the
+    oracle's restated setup agree bit for bit."""
+    if case == "periodic_fault":
+        dk, _ = workloads.sh_rupture(scale=0.1, nsteps=50)
+        dk.absorbing = [1, 3]
+        dk.periodic = (2, 4)
+    else:
+        dk = decks.inabox()
+        dk.time.total_time, dk.time.nsteps = 0.0, 50
+        if case == "periodic":
+            dk.absorbing = [1, 3]
+            dk.periodic = (2, 4)
+        else:
+            dk.absorbing = [1, 2, 3]
+            dk.dirneu = [(4, "N", "D", True)]
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    assert (a.nperio, a.ndir) == (b.nperio, b.ndir)
+    for name, m in (("perio_master", a.nperio), ("perio_slave", a.nperio), ("dir_node", a.ndir),
+                    ("dir_comp", a.ndir), ("dir_after_fault", a.ndir)):
+        if m:
+            assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
+    assert (a.nperio > 0) == (case != "dirneu") and (a.ndir > 0) == (case == "dirneu")
