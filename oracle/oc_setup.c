@@ -1297,6 +1297,109 @@ static int rec_init(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
 
 /* SO_read + RICKER_read + FORCE_read + SO_init (src_gen.f90:83-262,
  * stf_ricker.f90:46-80, src_force.f90:36-63) */
+/* SRC_MOMENT_read / SRC_MOMENT_init / SRC_MOMENT_add (src_moment.f90:27-175):
+ * in every element holding the source node (i, j) the row of nodes (:, j)
+ * gets G(c,1) h'_l(xi_i) and the column (i, :) gets G(c,2) h'_l(eta_j),
+ * G = M jac_inv^T (SH: G = jac_inv M(:,1)); the coefficients are summed per
+ * node (in order of first appearance) into point forces */
+static int moment_init(oc_setup *s, const sem2d_deck *dk, float f0, float onset, float amp, char *err, int el) {
+  int nd = s->ndof, n = s->ngll, ns = dk->nsrc;
+  double M[2][2] = {{0, 0}, {0, 0}};
+  if (dk->src_mech == 1) {
+    if (nd != 2) return seterr(err, el, "SRC_MOMENT_read: explosion only allowed in PSV (ndof=2)"), -1;
+    M[0][0] = 1.0;
+    M[1][1] = 1.0;
+  } else if (dk->src_mech == 2) {
+    double dip = dk->src_dip * PI_REF / 180.0, n0 = sin(dip), n1 = cos(dip);
+    if (nd == 2) {
+      double r0 = -cos(dip), r1 = sin(dip);
+      M[0][0] = 2.0 * r0 * n0;
+      M[0][1] = r0 * n1 + r1 * n0;
+      M[1][0] = M[0][1];
+      M[1][1] = 2.0 * r1 * n1;
+    } else {
+      M[0][0] = n0;
+      M[1][0] = n1;
+    }
+  } else if (dk->src_mech == 3) {
+    if (nd == 2) {
+      M[0][0] = dk->src_M[0]; M[0][1] = dk->src_M[1]; M[1][0] = dk->src_M[2]; M[1][1] = dk->src_M[3];
+    } else {
+      M[0][0] = dk->src_M[0];
+      M[1][0] = dk->src_M[1];
+    }
+  } else {
+    return seterr(err, el, "unknown source mechanism"), -1;
+  }
+  int cap = 4 * 2 * n * ns + 1, cnt = 0;
+  int *node = xcalloc((size_t)cap, sizeof(int));
+  double *F = xcalloc(2 * (size_t)cap, sizeof(double)), *rel = xcalloc((size_t)cap, sizeof(double)),
+         *td = xcalloc((size_t)cap, sizeof(double));
+  for (int k = 0; k < ns; k++) {
+    int src = nearest_node(s, dk->src_coord + 2 * k, NULL), first = cnt;
+    for (int e = 0; e < s->nelem; e++)
+      for (int j = 0; j < n; j++)
+        for (int i = 0; i < n; i++) {
+          if (s->ibool[i + n * (j + (size_t)n * e)] != src) continue;
+          double c8[8], J[4];
+          elem_coorg(s, e, c8);
+          jacobian(s, c8, i, j, J);
+          double det = J[0] * J[3] - J[2] * J[1];
+          double inv[2][2] = {{J[3] / det, -J[2] / det}, {-J[1] / det, J[0] / det}};
+          double G[2][2];
+          if (nd == 2) {
+            for (int a = 0; a < 2; a++)
+              for (int b = 0; b < 2; b++) G[a][b] = M[a][0] * inv[b][0] + M[a][1] * inv[b][1];
+          } else {
+            G[0][0] = inv[0][0] * M[0][0] + inv[0][1] * M[1][0];
+            G[0][1] = inv[1][0] * M[0][0] + inv[1][1] * M[1][0];
+            G[1][0] = G[1][1] = 0.0;
+          }
+          for (int l = 0; l < n; l++) {
+            double hx = s->H[l + n * i], he = s->H[l + n * j];
+            int nodes2[2] = {s->ibool[l + n * (j + (size_t)n * e)], s->ibool[i + n * (l + (size_t)n * e)]};
+            double fx[2] = {G[0][0] * hx, G[0][1] * he}, fz[2] = {G[1][0] * hx, G[1][1] * he};
+            for (int t = 0; t < 2; t++) {
+              int q = first;
+              while (q < cnt && node[q] != nodes2[t]) q++;
+              if (q == cnt) {
+                node[cnt] = nodes2[t];
+                F[2 * cnt] = 0.0;
+                F[2 * cnt + 1] = 0.0;
+                rel[cnt] = dk->src_ampli ? dk->src_ampli[k] : 1.0;
+                td[cnt] = dk->src_tdelay ? dk->src_tdelay[k] : 0.0;
+                cnt++;
+              }
+              F[2 * q] += fx[t];
+              F[2 * q + 1] += fz[t];
+            }
+          }
+        }
+  }
+  s->nsrc = cnt;
+  s->src_node = node;
+  s->src_dir = xcalloc(2 * (size_t)cnt, sizeof(double));
+  s->src_f0 = xcalloc((size_t)cnt, sizeof(double));
+  s->src_t0 = xcalloc((size_t)cnt, sizeof(double));
+  s->src_amp = xcalloc((size_t)cnt, sizeof(double));
+  s->src_rel = rel;
+  s->src_tdelay = td;
+  for (int q = 0; q < cnt; q++) {
+    if (nd == 2) {
+      s->src_dir[2 * q] = F[2 * q];
+      s->src_dir[2 * q + 1] = F[2 * q + 1];
+    } else { /* SH: the force is the amplitude itself */
+      s->src_dir[2 * q] = 1.0;
+      s->src_rel[q] = s->src_rel[q] * F[2 * q];
+    }
+    s->src_f0[q] = (double)f0;
+    s->src_t0[q] = (double)onset;
+    s->src_amp[q] = (double)amp;
+  }
+  free(F);
+  return 0;
+}
+
 static int src_init(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   int ns = dk->nsrc;
   if (ns <= 0) return 0;
@@ -1305,6 +1408,7 @@ static int src_init(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   if (f0 <= 0.0f) return seterr(err, el, "RICKER_read: f0 must be positive"), -1;
   if (onset < 1.0f / f0) return seterr(err, el, "warning: RICKER_read: Onset time too small"), -1;
   double ang = dk->force_angle * PI_REF / 180.0;
+  if (dk->src_mech != 0) return moment_init(s, dk, f0, onset, amp, err, el);
   s->nsrc = ns;
   s->src_node = xcalloc((size_t)ns, sizeof(int));
   s->src_dir = xcalloc(2 * (size_t)ns, sizeof(double));

@@ -187,3 +187,19 @@ def test_periodic_and_dirichlet_bit_exact(case):
         if m:
             assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
     assert (a.nperio > 0) == (case != "dirneu") and (a.ndir > 0) == (case == "dirneu")
+
+
+@pytest.mark.parametrize("mech,ndof", [("EXPLOSION", 2), ("DOUBLE_COUPLE", 2), ("MOMENT", 2), ("MOMENT", 1),
+                                       ("DOUBLE_COUPLE", 1)])
+def test_moment_sources_bit_exact(mech, ndof):
+    """Moment sources as point forces (src_moment.f90:27-175): builder and
+    the oracle's restated setup agree bit for bit."""
+    dk = decks.inabox()
+    dk.ndof = ndof
+    dk.time.total_time, dk.time.nsteps = 0.0, 50
+    dk.sources.mechanism, dk.sources.dip, dk.sources.M = mech, 35.0, (1.0, 0.2, 0.3, -0.6)
+    dk.sources.coords = [(0.0, 0.0), (125.0, -310.0)]
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert a.nsrc == b.nsrc > 2
+    assert_same_desc(a, b)
