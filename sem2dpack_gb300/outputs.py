@@ -31,7 +31,9 @@ JUPYTER/POST scripts of SEM2DPACK, Seismic Unix) read a GPU run unchanged.
                 stdio.f90:113-139); e11/e22/e12 (SH e13/e23) and s11/s22/s12
                 (SH s13/s23)_NNN_sem2d.dat: direct access, record e = the
                 NGLL x NGLL values of element e in FP32 (plot_gen.f90:
-                220-300).  NNN = (it - it1) / itd, three digits
+                220-300); div/curl_NNN_sem2d.dat: divergence and curl
+                of the velocity (P-SV), same records.  NNN = (it - it1) /
+                itd, three digits
 
 Values are written little-endian, as the reference built with gfortran on
 x86 or Arm writes them.
@@ -191,17 +193,18 @@ def read_grid(path):
     return sizes, np.transpose(ib, (2, 1, 0)), xz.T
 
 
-def write_snapshot(path, solver, index, fields="V"):
+def write_snapshot(path, solver, index, fields="V", grid=None):
     """The binary snapshot files of one output time for the SNAP_DEF
     `fields` letters D, V, A (node fields), E (strain) and S (stress);
     `index` is the NNN of the file names; A needs a handle that keeps the
     accelerations (Newmark, HHT-alpha or 'A' receivers).  S of a
     Kelvin-Voigt material is the stress of d + eta v, as the reference's
-    (MAT_stress_dv, mat_gen.f90:626-641).  The divergence and curl (d, c)
-    are not written."""
+    (MAT_stress_dv, mat_gen.f90:626-641).  The divergence and curl of the
+    velocity (d, c; P-SV only, MAT_divcurl_PSV, mat_gen.f90:802-825) need
+    the Grid of the problem."""
     d = solver.desc
     fields = str(fields)
-    bad = set(fields) - set("DVAES")
+    bad = set(fields) - set("DVAESdc")
     if bad:
         raise ValueError("snapshot fields %s are not written" % sorted(bad))
     os.makedirs(path, exist_ok=True)
@@ -217,6 +220,10 @@ def write_snapshot(path, solver, index, fields="V"):
             for k, comp in enumerate(comps):
                 np.ascontiguousarray(byname[c][:, k], dtype="<f4").tofile(
                     os.path.join(path, "%s%s_%s_sem2d.dat" % (c.lower(), comp, tag)))
+    if "d" in fields or "c" in fields:
+        if d.ndof != 2 or grid is None:
+            raise ValueError("div/curl snapshots need a P-SV problem and its Grid")
+        _write_divcurl(path, tag, solver.fields()[1], grid, fields)
     if "E" in fields or "S" in fields:
         strain, stress = solver.strain_stress()  # (ngll, ngll, ndof+1, nelem)
         names = (("13", "23") if d.ndof == 1 else ("11", "22", "12"))
@@ -226,6 +233,28 @@ def write_snapshot(path, solver, index, fields="V"):
             for k, nm in enumerate(names):
                 rec = np.transpose(arr[:, :, k, :], (2, 1, 0))  # record e, i fastest
                 np.ascontiguousarray(rec, dtype="<f4").tofile(os.path.join(path, "%s%s_%s_sem2d.dat" % (pre, nm, tag)))
+
+
+def _write_divcurl(path, tag, v, grid, fields):
+    """div v = dvx/dx + dvz/dz and curl v = dvx/dz - dvz/dx at the element
+    GLL points of the Cartesian mesher's rectangular elements (dxi/dz =
+    deta/dx = 0), records as for the strain."""
+    ib = grid.ibool() - 1  # (ngll, ngll, nelem)
+    xz = grid.coord()
+    _, _, H = grid.gll()  # H[k, i] = h'_k(x_i)
+    N = ib.shape[0]
+    vx, vz = v[:, 0][ib], v[:, 1][ib]
+    dxi_dx = 2.0 / (xz[0][ib[N - 1, 0, :]] - xz[0][ib[0, 0, :]])
+    deta_dz = 2.0 / (xz[1][ib[0, N - 1, :]] - xz[1][ib[0, 0, :]])
+    dxi = lambda u: np.einsum("ki,kje->ije", H, u)   # Ht . u
+    deta = lambda u: np.einsum("ike,kj->ije", u, H)  # u . H
+    out = {"d": ("div", dxi(vx) * dxi_dx + deta(vz) * deta_dz),
+           "c": ("curl", deta(vx) * deta_dz - dxi(vz) * dxi_dx)}
+    for letter in "dc":
+        if letter in fields:
+            name, arr = out[letter]
+            rec = np.transpose(arr, (2, 1, 0))  # record e, i fastest
+            np.ascontiguousarray(rec, dtype="<f4").tofile(os.path.join(path, "%s_%s_sem2d.dat" % (name, tag)))
 
 
 def write_run(path, solver, problem):

@@ -239,7 +239,32 @@ def test_snapshot_files(tmp_path):
             raw = np.fromfile(tmp_path / ("%s%s_003_sem2d.dat" % (pre, nm)), dtype="<f4").reshape(ne, N * N)
             assert np.array_equal(raw[5], arr[:, :, k, 5].ravel(order="F").astype(np.float32))
     with pytest.raises(ValueError):
-        outputs.write_snapshot(str(tmp_path), Run(), 4, "Vc")
+        outputs.write_snapshot(str(tmp_path), Run(), 4, "Vc")  # div/curl need the grid
+    with pytest.raises(ValueError):
+        outputs.write_snapshot(str(tmp_path), Run(), 4, "Vx")
+
+
+def test_divcurl_snapshot_of_a_linear_velocity(tmp_path):
+    """div and curl of v = (a x + b z, c x + e z) are a + e and b - c at
+    every GLL point (MAT_divcurl_PSV, mat_gen.f90:802-825)."""
+    P = Problem(workloads.plain_psv(scale=0.05, nsteps=10))
+    d = P.desc()
+    xz = P.grid.coord()
+    a, b, c, e = 1.5e-3, -0.7e-3, 0.4e-3, 2.1e-3
+    v = np.stack([a * xz[0] + b * xz[1], c * xz[0] + e * xz[1]], axis=1)
+
+    class Run:
+        desc = d
+
+        def fields(self, accel=False):
+            return np.zeros_like(v), v
+
+    outputs.write_snapshot(str(tmp_path), Run(), 2, "dc", grid=P.grid)
+    div = np.fromfile(tmp_path / "div_002_sem2d.dat", dtype="<f4")
+    curl = np.fromfile(tmp_path / "curl_002_sem2d.dat", dtype="<f4")
+    assert div.size == curl.size == d.ngll ** 2 * d.nelem
+    np.testing.assert_allclose(div, a + e, rtol=1e-5)
+    np.testing.assert_allclose(curl, b - c, rtol=1e-5)
 
 
 def test_hht_alpha_time_block():
