@@ -214,6 +214,19 @@ typedef struct sem2d_problem_desc {
   int nperio;
   const int *perio_master; /* [nperio], 1-based                             */
   const int *perio_slave;  /* [nperio], 1-based                             */
+
+  /* ---- run-time checks ----
+   * Iteration cap of the rate-and-state Newton solver (nr_solver,
+   * bc_dynflt_rsf.f90:372 uses 200); 0 selects 200.  A node that exceeds it
+   * makes the run fail with SEM2D_E_NR where the reference calls IO_abort
+   * (bc_dynflt_rsf.f90:461-466). */
+  int flt_nr_maxit;
+  /* Every info_every steps (&GENERAL itInfo, default 100: input.f90:95,122)
+   * the library takes max|veloc| and max|displ| over the nodes, as the
+   * reference prints them (main.f90:73-76), and fails the run with
+   * SEM2D_E_NAN when either is not finite; 0 selects 100, a negative value
+   * switches the check off.  sem2d_gpu_get_info returns the last values. */
+  int info_every;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;
@@ -323,6 +336,13 @@ int sem2d_gpu_get_fault_potency(sem2d_handle *h, double *out);
  * (a batch member reads its own). */
 int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress);
 
+/* The progress information of main.f90:73-76: *vmax = max|veloc| and
+ * *dmax = max|displ| over all nodes and components at the last multiple
+ * of info_every steps (step 0 before the first), and *step = that step.
+ * A batch returns the maxima over its members.  Either pointer may be
+ * NULL. */
+int sem2d_gpu_get_info(sem2d_handle *h, int *step, double *vmax, double *dmax);
+
 /* Current fault state D(nflt,ndof), V(nflt,ndof), T(nflt,2), MU(nflt),
  * state variable theta(nflt) (RSF, else zeros); any pointer may be NULL. */
 int sem2d_gpu_get_fault_state(sem2d_handle *h, double *D, double *V,
@@ -350,8 +370,8 @@ int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz);
 /* Releases device memory; h becomes invalid. */
 int sem2d_gpu_destroy(sem2d_handle *h);
 
-/* Message of the last failed call on h (or of the last failed create when
- * h is NULL). */
+/* Message of the last failed call on h (or, when h is NULL, of the last
+ * failed create or sem2d_gpu_step_noalloc). */
 const char *sem2d_gpu_last_error(sem2d_handle *h);
 
 /* ---- stepping caller-owned device arrays without allocating ----------
@@ -391,6 +411,13 @@ typedef struct sem2d_lattice_args {
   int step0;                  /* steps already done before this call         */
   double dt;
   int kd2_form;
+  int *status;                /* device int or NULL: a step that fails on the
+                                 device (a bounded wait for its shared-memory
+                                 copies that ran out: SEM2D_E_TIMEOUT) stores
+                                 its SEM2D_E_* code here; the library never
+                                 clears it.  Read it once the stream has
+                                 finished.  With NULL such failures go
+                                 unreported.                                 */
 } sem2d_lattice_args;
 
 /* Advances nsteps leapfrog steps of the elastic bulk (element forces,
@@ -410,7 +437,10 @@ typedef struct sem2d_lattice_args {
  * with SEM2D_E_ARG.  The first call on a device looks up that array's
  * address, so make it before any stream capture.  All calls share the one
  * array: calls that overlap on the GPU (other streams, other threads) race
- * and must be ordered by the caller. */
+ * and must be ordered by the caller.  NGLL 3, 5, 6 and 9 are taken.  The
+ * return value covers the arguments and the launches; failures inside the
+ * kernels reach the caller only through a->status.  Messages of rejected
+ * calls: sem2d_gpu_last_error(NULL). */
 #define SEM2D_NOALLOC_SCRATCH_BYTES (8u << 20)
 int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, void *stream);
 

@@ -215,3 +215,18 @@ def run_deck(deck, nsteps=None):
     sim = OracleSim(s.desc(), owner=s)
     sim.run(s.time()[1] if nsteps is None else nsteps)
     return s, sim
+
+
+def rupture_time(v, dt, v_crit=1.0e-3):
+    """Rupture time per node, restating the loop of the reference's
+    post-processing (POST/python/post-process-fault.py:53-62) on a slip-rate
+    array v[i, x] (sample i, node x): the first i in 0 .. nt-3 with
+    v[i, x] < V_critical <= v[i+1, x] gives Rup_t[x] = i*dt; otherwise 0."""
+    nt, nx = v.shape
+    rup = np.zeros(nx)
+    for x in range(nx):
+        for i in range(nt - 2):
+            if v[i, x] < v_crit and v[i + 1, x] >= v_crit:
+                rup[x] = i * dt
+                break
+    return rup

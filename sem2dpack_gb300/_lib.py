@@ -37,6 +37,7 @@ PROTOTYPES = [
     ("sem2d_gpu_get_fault_potency", C.c_int, [vp, dp]),
     ("sem2d_gpu_get_strain_stress", C.c_int, [vp, dp, dp]),
     ("sem2d_gpu_get_fault_state", C.c_int, [vp, dp, dp, dp, dp, dp]),
+    ("sem2d_gpu_get_info", C.c_int, [vp, ip, dp, dp]),
     ("sem2d_gpu_reset", C.c_int, [vp]),
     ("sem2d_gpu_kernel_launches", C.c_longlong, [vp]),
     ("sem2d_gpu_tile_shape", C.c_int, [vp, ip, ip]),

@@ -99,6 +99,7 @@ class ProblemDesc(C.Structure):
         ("ndir", c_int), ("dir_node", P_int), ("dir_comp", P_int), ("dir_after_fault", P_int),
         ("alpha", c_double),
         ("nperio", c_int), ("perio_master", P_int), ("perio_slave", P_int),
+        ("flt_nr_maxit", c_int), ("info_every", c_int),
     ]
 
 
@@ -168,4 +169,5 @@ class LatticeArgs(C.Structure):
         ("xix", C.c_void_p), ("etaz", C.c_void_p), ("dxdxi", C.c_void_p), ("dzdeta", C.c_void_p),
         ("nsrc", c_int), ("src_I", C.c_void_p), ("src_J", C.c_void_p), ("src_amp", C.c_void_p),
         ("nt", c_int), ("step0", c_int), ("dt", c_double), ("kd2_form", c_int),
+        ("status", C.c_void_p),
     ]

@@ -83,6 +83,7 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.has_kv = c.has_kv;
   p.nplanes = c.nplanes;
   p.error = c.error;
+  p.spin_limit = c.spin_limit;
   p.chunk_shift = c.chunk_shift;
 }
 

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <string>
 #include <vector>
 
 namespace sem2d {
@@ -54,7 +55,9 @@ struct BulkConfig {
   double cal = 0, cpa = 0;  // HHT-alpha: 1 - alpha; alpha (1 - gamma) dt
   double width = 0;  // 2.5D seismogenic width, 0 = 2D
   int *error = nullptr;  // device error flag
+  int spin_limit = 1 << 22;  // polls of a stage's mbarrier before giving up
   int chunk_shift = 0;   // chunk scheduled first (the fault's)
+  int march_stage = 1;   // march kernels: rows staged through shared memory (1) or loaded directly (0)
   cudaStream_t stream = nullptr;
 };
 
@@ -120,6 +123,8 @@ int fill_params_block(const BulkConfig &c, void *out);
 // any launch or stream capture)
 int configure_bulk(const BulkConfig &c);
 const char *bulk_last_error();
+// the message sem2d_gpu_last_error(NULL) returns
+void set_library_error(const std::string &msg);
 
 // element columns per strip and element rows per batch for NGLL N
 int strip_width(int N);
@@ -215,7 +220,8 @@ struct MarchAdjConfig {
   cudaStream_t stream = nullptr;
 };
 int launch_march_adjoint(const MarchAdjConfig &c);
-// resident warps per SM of the march kernel for the configuration
+// resident warps per SM of the march kernel for the configuration; also
+// sets the kernels' shared-memory limit (call before any launch or capture)
 int march_warps_per_sm(const BulkConfig &c);
 
 size_t params_bytes_n5(int mixed);

@@ -20,7 +20,7 @@
 
 namespace sem2d {
 
-constexpr int kNrMaxIt = 200;       // bc_dynflt_rsf.f90:372
+constexpr int kNrMaxIt = 200;       // bc_dynflt_rsf.f90:372 (default of FaultParams::nr_maxit)
 constexpr int kNrMaxBracket = 200;  // bound for the loop at bc_dynflt_rsf.f90:393-398
 constexpr int kErrNR = -4;          // SEM2D_E_NR
 
@@ -121,7 +121,7 @@ __device__ double nr_solve(const FaultParams<real> &p, int k, double xL, double 
   double xlow = flo < 0 ? xl : xr, xhigh = flo < 0 ? xr : xl;
   double xest = 0.5 * (xl + xr), dxold = fabs(xr - xl), dx = dxold, fx;
   nr_func(rf, sa, xest, ts, Z, fx, dfn, v);
-  for (int is = 0; is < kNrMaxIt; ++is) {
+  for (int is = 0; is < p.nr_maxit; ++is) {
     if (((xest - xhigh) * dfn - fx) * ((xest - xlow) * dfn - fx) > 0 ||
         fabs(2 * fx) > fabs(dxold * dfn)) {
       dxold = dx;

@@ -17,13 +17,32 @@ namespace {
 constexpr int kThreads = 32 * kMarchWarps;
 static_assert(kMarchWarpsHost == kMarchWarps, "host and device CTA shapes");
 
-template <int NDOF, int MAT>
+template <int NDOF, int MAT, bool STG>
+constexpr size_t ring_bytes() {
+  return STG ? MarchStage<NDOF, MAT>::kCtaBytes : 0;
+}
+
+template <int NDOF, int MAT, bool STG>
+int configure_typed() {
+  cudaError_t e = cudaFuncSetAttribute(march_step_kernel<NDOF, MAT, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       int(ring_bytes<NDOF, MAT, STG>()));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(march_batch_kernel<NDOF, MAT, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             int(ring_bytes<NDOF, MAT, STG>()));
+  if (e != cudaSuccess) {
+    g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
+}
+
+template <int NDOF, int MAT, bool STG>
 int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
   const int grid = std::max(1, (m.nunits + kMarchWarps - 1) / kMarchWarps);  // an empty set still counts the step
-  march_step_kernel<NDOF, MAT><<<grid, kThreads, 0, c.stream>>>(p, static_cast<const MarchUnit *>(m.units),
-                                                                m.nunits);
+  march_step_kernel<NDOF, MAT, STG><<<grid, kThreads, ring_bytes<NDOF, MAT, STG>(), c.stream>>>(
+      p, static_cast<const MarchUnit *>(m.units), m.nunits);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -32,7 +51,7 @@ int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   return 0;
 }
 
-template <int NDOF, int MAT>
+template <int NDOF, int MAT, bool STG>
 int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   MarchBatch b{};
   for (int k = 0; k < 25; ++k) b.H[k] = float(c.H[k]);
@@ -43,7 +62,7 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   b.step = m.step;
   b.done = m.done;
   const int grid = std::max(1, (m.nunits + kMarchWarps - 1) / kMarchWarps);  // an empty set still counts the step
-  march_batch_kernel<NDOF, MAT><<<grid, kThreads, 0, c.stream>>>(b);
+  march_batch_kernel<NDOF, MAT, STG><<<grid, kThreads, ring_bytes<NDOF, MAT, STG>(), c.stream>>>(b);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -52,13 +71,39 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   return 0;
 }
 
-template <int NDOF, int MAT>
+template <int NDOF, int MAT, bool STG>
 int occupancy_one() {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT>, kThreads, 0) != cudaSuccess)
+  if (configure_typed<NDOF, MAT, STG>()) return 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, STG>, kThreads,
+                                                    ring_bytes<NDOF, MAT, STG>()) != cudaSuccess)
     return 0;
   return nb * kMarchWarps;
 }
+
+// the instantiation for (ndof, material layout, staging) of c
+template <template <int, int, bool> class F, typename... A>
+int dispatch(const BulkConfig &c, A &&...a) {
+  const bool s = c.march_stage != 0;
+  if (c.ndof == 1) {
+    if (c.mat_elem == kMatNode) return s ? F<1, kMatNode, true>::run(a...) : F<1, kMatNode, false>::run(a...);
+    return s ? F<1, kMatElement, true>::run(a...) : F<1, kMatElement, false>::run(a...);
+  }
+  if (c.mat_elem == kMatNode) return s ? F<2, kMatNode, true>::run(a...) : F<2, kMatNode, false>::run(a...);
+  return s ? F<2, kMatElement, true>::run(a...) : F<2, kMatElement, false>::run(a...);
+}
+template <int NDOF, int MAT, bool STG>
+struct LaunchOne {
+  static int run(const BulkConfig &c, const MarchLaunch &m) { return launch_one<NDOF, MAT, STG>(c, m); }
+};
+template <int NDOF, int MAT, bool STG>
+struct LaunchMany {
+  static int run(const BulkConfig &c, const MarchLaunch &m) { return launch_many<NDOF, MAT, STG>(c, m); }
+};
+template <int NDOF, int MAT, bool STG>
+struct Occupancy {
+  static int run() { return occupancy_one<NDOF, MAT, STG>(); }
+};
 
 }  // namespace
 
@@ -67,17 +112,9 @@ bool march_supported(const BulkConfig &c) {
          (c.ndof == 1 || c.ndof == 2) && c.pitch % 4 == 0 && c.plane % 4 == 0;
 }
 
-int launch_march(const BulkConfig &c, const MarchLaunch &m) {
-  if (c.ndof == 1)
-    return c.mat_elem == kMatNode ? launch_one<1, kMatNode>(c, m) : launch_one<1, kMatElement>(c, m);
-  return c.mat_elem == kMatNode ? launch_one<2, kMatNode>(c, m) : launch_one<2, kMatElement>(c, m);
-}
+int launch_march(const BulkConfig &c, const MarchLaunch &m) { return dispatch<LaunchOne>(c, c, m); }
 
-int launch_march_batch(const BulkConfig &c, const MarchLaunch &m) {
-  if (c.ndof == 1)
-    return c.mat_elem == kMatNode ? launch_many<1, kMatNode>(c, m) : launch_many<1, kMatElement>(c, m);
-  return c.mat_elem == kMatNode ? launch_many<2, kMatNode>(c, m) : launch_many<2, kMatElement>(c, m);
-}
+int launch_march_batch(const BulkConfig &c, const MarchLaunch &m) { return dispatch<LaunchMany>(c, c, m); }
 
 int launch_march_fault_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
   BulkParams<float, 5> p;
@@ -171,9 +208,6 @@ int launch_march_adjoint(const MarchAdjConfig &c) {
   return 0;
 }
 
-int march_warps_per_sm(const BulkConfig &c) {
-  if (c.ndof == 1) return c.mat_elem == kMatNode ? occupancy_one<1, kMatNode>() : occupancy_one<1, kMatElement>();
-  return c.mat_elem == kMatNode ? occupancy_one<2, kMatNode>() : occupancy_one<2, kMatElement>();
-}
+int march_warps_per_sm(const BulkConfig &c) { return dispatch<Occupancy>(c); }
 
 }  // namespace sem2d

@@ -27,10 +27,23 @@
 // element before right, so both kernels assemble identically.
 //
 // Memory.  A lane reads the 4 node columns it owns of each node row as one
-// 16-byte load (the warp reads 512 contiguous bytes) and gets the fifth
+// 16-byte piece (the warp reads 512 contiguous bytes) and gets the fifth
 // column from the next lane; fields, inverse mass and node material are
-// read this way, written the same way.  Nothing is staged: the latency of
-// a row's loads is covered by the other resident warps.
+// read this way, written the same way.  Two variants move the rows:
+//  * direct (STG = false): 16-byte global loads; the latency of a row's
+//    loads is covered by the other resident warps only;
+//  * staged (STG = true): each warp owns a ring of 10 node-row slots in
+//    shared memory.  The rows of element row ez+1 (displacement, velocity,
+//    inverse mass, and for SH the node material) are copied in by
+//    cp.async (16 bytes per lane, one commit group per element row) while
+//    element row ez computes, so the element and node-update phases read
+//    shared memory only; the warp waits for a group with cp.async.wait_group,
+//    a hardware wait on its own copies (no polling).  Slot of node row J:
+//    J mod 10, enough for the rows of two consecutive element rows, a fault
+//    split included; a slot is refilled only after the element row that
+//    read it has finished (a __syncwarp orders the lanes).
+// Both variants do the same arithmetic in the same order: their results are
+// bitwise identical.
 //
 // Fault.  The complete forces of the split node rows jf1 (top of the
 // elements below the fault) and jf2 (bottom of the elements above),
@@ -56,11 +69,41 @@ constexpr int kMarchWarps = 4;     // warps per CTA
 constexpr int kMarchCols = 31;     // element columns owned by a warp
 // resident CTAs per SM the register budget allows: 102 registers per
 // thread for SH (20 warps per SM), 168 for P-SV (12 warps; fewer registers
-// spill the node-material variant)
-template <int NDOF>
+// spill the node-material variant).  The staged variant is bounded by its
+// shared memory instead (see MarchStage): 3 CTAs per SM for SH, 2 for P-SV.
+template <int NDOF, bool STG = false>
 struct MarchOcc {
-  static constexpr int kMinBlocks = NDOF == 1 ? 5 : 3;
+  static constexpr int kMinBlocks = STG ? (NDOF == 1 ? 3 : 2) : (NDOF == 1 ? 5 : 3);
 };
+
+// Staging ring of one warp: kRingSlots node-row slots, each holding the
+// staged fields of one lattice row over the warp's 132 columns (33 pieces
+// of 16 bytes: lane k's 4 columns, and the column right of lane 31)
+constexpr int kRingSlots = 10;
+constexpr int kRowF = 132;  // floats per staged field row
+template <int NDOF, int MAT>
+struct MarchStage {
+  // node material is staged for SH only (P-SV: two more planes would halve
+  // the resident warps; its rows are read from global memory)
+  static constexpr bool kStageMat = MAT == kMatNode && NDOF == 1;
+  // fields of a slot: displacement c, velocity c, inverse mass, material
+  static constexpr int kD = 0, kV = NDOF, kRm = 2 * NDOF, kM = 2 * NDOF + 1;
+  static constexpr int kFields = 2 * NDOF + 1 + (kStageMat ? NDOF : 0);
+  static constexpr int kSlot = kFields * kRowF;
+  static constexpr int kWarpFloats = kRingSlots * kSlot;
+  static constexpr size_t kCtaBytes = size_t(kMarchWarps) * kWarpFloats * sizeof(float);
+};
+
+__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
+               "l"(src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int K>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory");
+}
 
 // one unit of work: a strip of element columns and a chunk of element rows
 // of one problem, with its receivers rec_ids[rec0 .. rec1)
@@ -79,10 +122,11 @@ struct MarchBatch {
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-// one unit of one problem
-template <int NDOF, int MAT>
+// one unit of one problem (ring: this warp's staging slots when STG)
+template <int NDOF, int MAT, bool STG = false>
 __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const float *H, const float *w,
-                                           const MarchUnit &u, int it) {
+                                           const MarchUnit &u, int it, float *ring = nullptr) {
+  using Stg = MarchStage<NDOF, MAT>;
   constexpr int N = 5;
   const int lane = threadIdx.x & 31;
   const int ex = kMarchCols * u.strip - 1 + lane;
@@ -109,6 +153,40 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   int zs = u.z0;
   if (u.z0 > 0 && p.row0[u.z0] == p.row0[u.z0 - 1] + (N - 1)) zs = u.z0 - 1;
 
+  // staging: lane k's piece of a node row starts at column cs + 4k (I0 for
+  // the lanes that load), lane 31 also copies the piece at cs + 128; pieces
+  // outside the row (left of strip 0, right of the pitch) are not copied
+  // and never read
+  const int cs = 4 * (kMarchCols * u.strip - 1);
+  const bool pc_ok = cs + 4 * lane >= 0 && cs + 4 * lane < p.pitch;
+  const bool pc32_ok = lane == 31 && cs + 128 < p.pitch;
+  auto slot_of = [&](int J) -> float * { return ring + (J % kRingSlots) * Stg::kSlot; };
+  auto stage_row = [&](int J) {
+    float *sl = slot_of(J);
+    const long long ro = (long long)J * p.pitch + cs;
+#pragma unroll
+    for (int f = 0; f < Stg::kFields; ++f) {
+      const float *b = f < NDOF           ? p.Dcur + f * pl
+                       : f < 2 * NDOF     ? p.Vcur + (f - NDOF) * pl
+                       : f == 2 * NDOF    ? p.rmass
+                                          : p.mat[f - 2 * NDOF - 1];
+      if (pc_ok) cp_async16(sl + f * kRowF + 4 * lane, b + ro + 4 * lane);
+      if (pc32_ok) cp_async16(sl + f * kRowF + 128, b + ro + 128);
+    }
+  };
+  // the node rows of element row ezn not staged with the row below it
+  auto stage_elem_row = [&](int ezn, bool first) {
+    const int Ja = p.row0[ezn];
+    const int j0 = (!first && Ja == p.row0[ezn - 1] + (N - 1)) ? 1 : 0;
+    for (int j = j0; j < N; ++j) stage_row(Ja + j);
+  };
+  if constexpr (STG) {
+    stage_elem_row(zs, true);
+    cp_async_commit();
+    if (zs + 1 < u.z1) stage_elem_row(zs + 1, false);
+    cp_async_commit();
+  }
+
   float carry[NDOF][N];  // forces on the node row shared with the next element row
 #pragma unroll
   for (int c = 0; c < NDOF; ++c)
@@ -121,23 +199,35 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   // (shuffled or, for lane 31, loaded) when the row starts
   // (P-SV: requested at the row start instead; carrying them through the
   // node update costs more registers than P-SV has)
-  constexpr bool kPrefetch = NDOF == 1;
+  // (staged: read from the ring when the row starts)
+  constexpr bool kPrefetch = NDOF == 1 && !STG;
   float4 nq[NDOF][N];
   float n5[NDOF][N];
   auto fetch_u = [&](int ezn) {
-    const long long o = (long long)p.row0[ezn] * p.pitch;
+    const int Ja = p.row0[ezn];
+    const long long o = (long long)Ja * p.pitch;
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        const float *b = p.Dcur + c * pl + o + (long long)j * p.pitch + I0;
-        nq[c][j] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
-        n5[c][j] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
+        if constexpr (STG) {
+          const float *sr = slot_of(Ja + j) + (Stg::kD + c) * kRowF;
+          nq[c][j] = ld ? *reinterpret_cast<const float4 *>(sr + 4 * lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+          n5[c][j] = (lane == 31 && act) ? sr[128] : 0.f;
+        } else {
+          const float *b = p.Dcur + c * pl + o + (long long)j * p.pitch + I0;
+          nq[c][j] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
+          n5[c][j] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
+        }
       }
   };
   if (kPrefetch) fetch_u(zs);
 
   for (int ez = zs; ez < u.z1; ++ez) {
+    if constexpr (STG) {
+      cp_async_wait<1>();  // this element row's group has landed
+      __syncwarp();        // and the other lanes' pieces are visible
+    }
     const bool halo = ez < u.z0;
     const int J0 = p.row0[ez];
     const float etaz = act ? p.etaz[ez] : 0.f;
@@ -201,9 +291,15 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
       if (MAT != kMatNode) return;
 #pragma unroll
       for (int m = 0; m < NDOF; ++m) {
-        const float *b = p.mat[m] + (long long)(J0 + j) * p.pitch + I0;
-        mq[slot][m] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
-        m5[slot][m] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
+        if constexpr (STG && Stg::kStageMat) {
+          const float *sr = slot_of(J0 + j) + (Stg::kM + m) * kRowF;
+          mq[slot][m] = ld ? *reinterpret_cast<const float4 *>(sr + 4 * lane) : make_float4(0.f, 0.f, 0.f, 0.f);
+          m5[slot][m] = (lane == 31 && act) ? sr[128] : 0.f;
+        } else {
+          const float *b = p.mat[m] + (long long)(J0 + j) * p.pitch + I0;
+          mq[slot][m] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
+          m5[slot][m] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
+        }
       }
     };
     fetch_m(0, 0);
@@ -350,23 +446,27 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           }
         }
         if (!own) continue;
+        // this node row's staged fields (STG)
+        const float *sl = STG ? slot_of(J) + 4 * lane : nullptr;
         float vv[NDOF][N], rmv[N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = ldg4(Vc + c * pl + g);
+          const float *src = STG ? sl + (Stg::kV + c) * kRowF : Vc + c * pl + g;
+          const float4 q = STG ? *reinterpret_cast<const float4 *>(src) : ldg4(src);
           vv[c][0] = q.x;
           vv[c][1] = q.y;
           vv[c][2] = q.z;
           vv[c][3] = q.w;
-          vv[c][4] = last_col ? __ldg(Vc + c * pl + g + 4) : 0.f;
+          vv[c][4] = last_col ? (STG ? src[4] : __ldg(src + 4)) : 0.f;
         }
         {
-          const float4 q = ldg4(Rm + g);
+          const float *src = STG ? sl + Stg::kRm * kRowF : Rm + g;
+          const float4 q = STG ? *reinterpret_cast<const float4 *>(src) : ldg4(src);
           rmv[0] = q.x;
           rmv[1] = q.y;
           rmv[2] = q.z;
           rmv[3] = q.w;
-          rmv[4] = last_col ? __ldg(Rm + g + 4) : 0.f;
+          rmv[4] = last_col ? (STG ? src[4] : __ldg(src + 4)) : 0.f;
         }
         // dashpots and the perimeter inverse mass
 #pragma unroll
@@ -398,12 +498,13 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float dv[NDOF][N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = ldg4(Dc + c * pl + g);
+          const float *src = STG ? sl + (Stg::kD + c) * kRowF : Dc + c * pl + g;
+          const float4 q = STG ? *reinterpret_cast<const float4 *>(src) : ldg4(src);
           dv[c][0] = q.x;
           dv[c][1] = q.y;
           dv[c][2] = q.z;
           dv[c][3] = q.w;
-          dv[c][4] = last_col ? __ldg(Dc + c * pl + g + 4) : 0.f;
+          dv[c][4] = last_col ? (STG ? src[4] : __ldg(src + 4)) : 0.f;
         }
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
@@ -432,7 +533,15 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     }
     if (halo) set_carry();
     have_carry = top_shared;
+    if constexpr (STG) {
+      // every lane is done with this element row's slots: refill them with
+      // the rows of element row ez+2 (an empty group keeps the count)
+      __syncwarp();
+      if (ez + 2 < u.z1) stage_elem_row(ez + 2, false);
+      cp_async_commit();
+    }
   }
+  if constexpr (STG) cp_async_wait<0>();
 
   // ---- receivers of this unit ----
   if (p.rec_ids && u.rec1 > u.rec0 && it % p.rec_isamp == 0 && it / p.rec_isamp < p.rec_nsamp) {
@@ -472,30 +581,33 @@ __device__ __forceinline__ void march_done(int *step, unsigned *done, int it) {
   }
 }
 
-// one problem: warp w of CTA b walks unit kMarchWarps*b + w
-template <int NDOF, int MAT>
-__global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
+// one problem: warp w of CTA b walks unit kMarchWarps*b + w (STG: with
+// its ring in the CTA's dynamic shared memory, MarchStage::kCtaBytes)
+template <int NDOF, int MAT, bool STG>
+__global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBlocks))
     march_step_kernel(const __grid_constant__ BulkParams<float, 5> p, const MarchUnit *units, int nunits) {
+  extern __shared__ __align__(16) float march_ring[];
   const int warp = threadIdx.x >> 5;
   const int it = *p.step + 1;
   const int uid = blockIdx.x * kMarchWarps + warp;
   if (uid < nunits) {
     const MarchUnit u = units[uid];
-    march_unit<NDOF, MAT>(p, p.H, p.w, u, it);
+    march_unit<NDOF, MAT, STG>(p, p.H, p.w, u, it, march_ring + warp * MarchStage<NDOF, MAT>::kWarpFloats);
   }
   march_done(p.step, p.done, it);
 }
 
 // many problems: the units of all problems, each with its parameter block
-template <int NDOF, int MAT>
-__global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
+template <int NDOF, int MAT, bool STG>
+__global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBlocks))
     march_batch_kernel(const __grid_constant__ MarchBatch b) {
+  extern __shared__ __align__(16) float march_ring[];
   const int warp = threadIdx.x >> 5;
   const int it = *b.step + 1;
   const int uid = blockIdx.x * kMarchWarps + warp;
   if (uid < b.nunits) {
     const MarchUnit u = b.units[uid];
-    march_unit<NDOF, MAT>(b.sims[u.prob], b.H, b.w, u, it);
+    march_unit<NDOF, MAT, STG>(b.sims[u.prob], b.H, b.w, u, it, march_ring + warp * MarchStage<NDOF, MAT>::kWarpFloats);
   }
   march_done(b.step, b.done, it);
 }

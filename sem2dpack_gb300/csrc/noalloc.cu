@@ -4,7 +4,7 @@
 // The handle-based path allocates the partner buffers of its double-buffered
 // update and two counters with cudaMalloc.  Here they live in g_scratch:
 //   [0, 64)         step counter (int), CTA completion counter (unsigned),
-//                   device error flag (int)
+//                   the error flag of calls without a status pointer (int)
 //   [64, 16384)     tile-row boundaries, nz+1 ints
 //   [16384, ...)    partner displacement plane(s), then partner velocity
 // Host code never dereferences g_scratch: its device address is looked up
@@ -13,7 +13,9 @@
 
 #include <algorithm>
 #include <cstdint>
+#include <cstdlib>
 #include <mutex>
+#include <string>
 
 #include "../../include/sem2d_gpu.h"
 #include "bulk_launch.h"
@@ -29,27 +31,32 @@ __device__ __align__(256) unsigned char g_scratch[SEM2D_NOALLOC_SCRATCH_BYTES];
 std::mutex g_mutex;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 
-// step counter = step0, completion counter = 0, uniform tile rows of TZ
+// step counter = step0, completion counter = 0, uniform tile rows of TZ;
+// the error flag is left as it is (the caller's status is never cleared)
 __global__ void noalloc_setup_kernel(unsigned char *scratch, int step0, int nz, int TZ) {
   int *step = reinterpret_cast<int *>(scratch);
   unsigned *done = reinterpret_cast<unsigned *>(scratch + 4);
   int *ztile = reinterpret_cast<int *>(scratch + kHeaderBytes);
   *step = step0;
   *done = 0u;
-  *reinterpret_cast<int *>(scratch + 8) = 0;
   int k = 0;
   for (int z = 0; z < nz; z += TZ) ztile[k++] = z;
   ztile[k] = nz;
 }
 
-int fail(int code, const char *) { return code; }
+// the message of a rejected call, returned by sem2d_gpu_last_error(NULL)
+int fail(int code, const std::string &msg) {
+  sem2d::set_library_error("sem2d_gpu_step_noalloc: " + msg);
+  return code;
+}
 
 }  // namespace
 
 extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, void *stream) {
   using namespace sem2d;
   if (!a || nsteps < 0) return fail(SEM2D_E_ARG, "null arguments or negative step count");
-  if (a->ngll != 5 && a->ngll != 6 && a->ngll != 9) return fail(SEM2D_E_UNSUPPORTED, "ngll must be 5, 6 or 9");
+  if (a->ngll != 3 && a->ngll != 5 && a->ngll != 6 && a->ngll != 9)
+    return fail(SEM2D_E_UNSUPPORTED, "ngll must be 3, 5, 6 or 9");
   if (a->ndof != 1 && a->ndof != 2) return fail(SEM2D_E_ARG, "ndof must be 1 or 2");
   if (a->precision != SEM2D_PRECISION_FP64 && a->precision != SEM2D_PRECISION_MIXED)
     return fail(SEM2D_E_ARG, "unknown precision");
@@ -88,7 +95,7 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
     if (!g_scratch_addr[dev]) {
       void *p = nullptr;
       const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
-      if (e != cudaSuccess) return fail(SEM2D_E_CUDA, cudaGetErrorString(e));
+      if (e != cudaSuccess) return fail(SEM2D_E_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
       g_scratch_addr[dev] = p;
     }
     scratch = static_cast<unsigned char *>(g_scratch_addr[dev]);
@@ -111,7 +118,7 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
   c.nplanes = strip_plane_count(c.ndof, c.nmat, 0, 0);
   if (bulk_smem(N, c.ndof, c.mixed, c.nplanes) > 227 * 1024)
     return fail(SEM2D_E_UNSUPPORTED, "the stage buffers do not fit in shared memory");
-  if (configure_bulk(c)) return fail(SEM2D_E_CUDA, bulk_last_error());
+  if (configure_bulk(c)) return fail(SEM2D_E_CUDA, std::string("configure: ") + bulk_last_error());
   c.grid_x = (a->nx + TX - 1) / TX;
   c.grid_y = (a->nz + TZ - 1) / TZ;
   c.LX = a->LX;
@@ -141,14 +148,16 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
   c.nt = a->nt;
   c.step = reinterpret_cast<int *>(scratch);
   c.done = reinterpret_cast<unsigned *>(scratch + 4);
-  c.error = reinterpret_cast<int *>(scratch + 8);
+  c.error = a->status ? a->status : reinterpret_cast<int *>(scratch + 8);
+  if (const char *e = std::getenv("SEM2D_SPIN_LIMIT")) c.spin_limit = std::max(0, std::atoi(e));
   c.scheme = 0;
   c.dt = a->dt;
   c.cv = a->dt;
   c.kd2 = a->kd2_form ? 1 : 0;
   c.stream = st;
   noalloc_setup_kernel<<<1, 1, 0, st>>>(scratch, a->step0, a->nz, TZ);
-  if (cudaGetLastError() != cudaSuccess) return fail(SEM2D_E_CUDA, "setup launch failed");
+  if (const cudaError_t e = cudaGetLastError(); e != cudaSuccess)
+    return fail(SEM2D_E_CUDA, std::string("setup launch: ") + cudaGetErrorString(e));
   void *pd = scratch + kFieldOffset, *pv = scratch + kFieldOffset + field_bytes;
   void *bufD[2] = {a->d, pd}, *bufV[2] = {a->v, pv};
   int cur = 0;
@@ -157,7 +166,7 @@ extern "C" int sem2d_gpu_step_noalloc(const sem2d_lattice_args *a, int nsteps, v
     c.Dnext = bufD[1 - cur];
     c.Vcur = bufV[cur];
     c.Vnext = bufV[1 - cur];
-    if (launch_bulk(c)) return fail(SEM2D_E_CUDA, bulk_last_error());
+    if (launch_bulk(c)) return fail(SEM2D_E_CUDA, std::string("launch: ") + bulk_last_error());
     cur = 1 - cur;
   }
   if (cur == 1) {  // the state ended in the scratch: copy it back to the caller

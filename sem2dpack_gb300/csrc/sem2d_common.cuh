@@ -68,6 +68,7 @@ struct FaultParams {
   int *step;            // incremented by the last block (stand-alone kernel)
   unsigned int *done;   // block completion counter (reset by the last block)
   int *error;           // sticky device error flag (SEM2D_E_*)
+  int nr_maxit;         // iteration cap of the rate-and-state Newton solver
 };
 
 // Parameters of the fused element-force + assembly + update kernel.
@@ -140,6 +141,7 @@ struct BulkParams {
   int has_kv;             // Kelvin-Voigt viscosity present
   int nplanes;            // lattice planes staged per batch (strip_planes)
   int *error;             // sticky device error flag (SEM2D_E_*)
+  int spin_limit;         // polls of a stage's mbarrier before the step gives up
   int chunk_shift;        // chunk of CTA row y is (y + chunk_shift) % rows: the
                           // fault's chunk (long FP64 work) is scheduled first
 };

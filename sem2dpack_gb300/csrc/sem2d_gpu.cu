@@ -33,6 +33,8 @@ constexpr int kGraphPairs = 8;  // a captured graph covers 16 steps
 
 }  // namespace
 
+void sem2d::set_library_error(const std::string &msg) { g_create_err = msg; }
+
 struct FaultScalars {
   double coefA2V = 0, coefA2D = 0, normal_V = 0, normal_T = 1, normal_L = 1;
   int opening = 0, swf_kind = 1, swf_healing = 0, rsf_kind = 1, normal_kind = 1;
@@ -100,6 +102,12 @@ struct sem2d_handle {
   // time stepping
   int cur = 0;       // ping-pong index of the current displacement predictor
   int steps = 0;     // steps queued
+  // run-time checks: polls of an mbarrier before a step gives up
+  // (SEM2D_SPIN_LIMIT), Newton iteration cap, and the max|v|, max|d|
+  // watchdog every info_every steps (<= 0: off) into d_info
+  int spin_limit = 1 << 22, nr_maxit = 200, info_every = 100;
+  double *d_info = nullptr;  // [2]: max|v|, max|d| of the last check
+  int info_step = 0;         // step of the last check
   long long launches = 0;
   cudaGraphExec_t graph_exec = nullptr;
   std::string err;
@@ -114,6 +122,7 @@ struct sem2d_handle {
   // the one-element-per-thread kernel (FP32, NGLL = 5 fast path): work
   // units (strip, chunk) and the receivers each unit samples
   bool march = false;
+  int march_stage = 1;  // rows staged through shared memory (SEM2D_MARCH_STAGE=0: direct loads)
   int march_cz = 0, march_nunits = 0;
   void *d_march_units = nullptr;
   int *d_march_rec = nullptr;
@@ -747,6 +756,7 @@ FaultParams<real> fault_params(sem2d_handle *h, int cur) {
   f.step = h->d_step;
   f.done = h->d_done;
   f.error = h->d_error;
+  f.nr_maxit = h->nr_maxit;
   return f;
 }
 
@@ -775,6 +785,8 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.mat_iso = h->mat_iso;
   bc.fast = fast_path(h);
   bc.error = h->d_error;
+  bc.spin_limit = h->spin_limit;
+  bc.march_stage = h->march_stage;
   bc.grid_x = (h->nx + h->TX - 1) / h->TX;
   bc.grid_y = int(h->ztile.size()) - 1;
   bc.LX = h->LX;
@@ -894,6 +906,57 @@ __global__ void potency_kernel(const double *pot, int nflt, double *series, cons
   }
   const int it = *step;
   if (t < 6 && it >= 0 && it < rows) series[(size_t)6 * it + t] = part[t][0];
+}
+
+// The progress check of main.f90:73-76: max|v| and max|d| over n values
+// of each field into info[0], info[1] (atomic max on the bit patterns,
+// which order like the values for non-negative doubles); a value that is
+// not finite sets the device error flag to SEM2D_E_NAN.
+template <typename real>
+__global__ void watch_kernel(const real *V, const real *D, long long n, double *info, int *error) {
+  double vm = 0.0, dm = 0.0;
+  bool bad = false;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const double v = fabs(double(V[q])), d = fabs(double(D[q]));
+    bad = bad || !isfinite(v) || !isfinite(d);
+    vm = v > vm ? v : vm;
+    dm = d > dm ? d : dm;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+    dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(reinterpret_cast<unsigned long long *>(info), __double_as_longlong(vm));
+    atomicMax(reinterpret_cast<unsigned long long *>(info + 1), __double_as_longlong(dm));
+    if (bad) atomicCAS(error, 0, SEM2D_E_NAN);
+  }
+}
+
+// the check after the step just queued, over the problem or every member
+// of a batch (their maxima combined)
+int launch_watch(sem2d_handle *h) {
+  CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(double), h->stream));
+  std::vector<sem2d_handle *> probs = h->subs;
+  if (probs.empty()) probs.push_back(h);
+  for (sem2d_handle *m : probs) {
+    // after a step the displacement d^n is the buffer that is not current
+    const void *D = h->steps > 0 ? m->D[1 - h->cur] : m->D[h->cur];
+    const void *V = m->V[h->cur];
+    const long long n = (long long)m->plane * m->ndof;
+    const int grid = int(std::min<long long>((n + 255) / 256, 4 * 152));
+    if (h->mixed)
+      watch_kernel<float><<<grid, 256, 0, h->stream>>>(static_cast<const float *>(V), static_cast<const float *>(D), n,
+                                                      h->d_info, h->d_error);
+    else
+      watch_kernel<double><<<grid, 256, 0, h->stream>>>(static_cast<const double *>(V), static_cast<const double *>(D),
+                                                       n, h->d_info, h->d_error);
+    CK(cudaGetLastError());
+    h->launches++;
+  }
+  h->info_step = h->steps;
+  return SEM2D_OK;
 }
 
 int launch_potency(sem2d_handle *h, cudaStream_t s, const int *step) {
@@ -1192,6 +1255,8 @@ int reset_state(sem2d_handle *h) {
     CK(cudaMemsetAsync(h->d_step, 0, sizeof(int), h->stream));
     CK(cudaMemsetAsync(h->d_done, 0, sizeof(unsigned), h->stream));
     CK(cudaMemsetAsync(h->d_error, 0, sizeof(int), h->stream));
+    CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(double), h->stream));
+    h->info_step = 0;
     h->cur = 0;
     h->steps = 0;
     sync_members(h);
@@ -1206,6 +1271,8 @@ int reset_state(sem2d_handle *h) {
   CK(cudaMemsetAsync(h->d_step, 0, sizeof(int), h->stream));
   CK(cudaMemsetAsync(h->d_done, 0, sizeof(unsigned), h->stream));
   CK(cudaMemsetAsync(h->d_error, 0, sizeof(int), h->stream));
+  CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(double), h->stream));
+  h->info_step = 0;
   if (h->d_step_c) CK(cudaMemsetAsync(h->d_step_c, 0, sizeof(int), h->stream));
   if (h->d_done_c) CK(cudaMemsetAsync(h->d_done_c, 0, sizeof(unsigned), h->stream));
   if (h->sis) CK(cudaMemsetAsync(h->sis, 0, sizeof(double) * (size_t)h->rec_nsamp * h->nrec * h->ndof, h->stream));
@@ -1237,6 +1304,8 @@ int check_device_error(sem2d_handle *h) {
   CK(cudaMemcpy(&e, h->d_error, sizeof(int), cudaMemcpyDeviceToHost));
   if (e == SEM2D_E_NR) return set_err(h, SEM2D_E_NR, "rate-and-state Newton solver did not converge");
   if (e == SEM2D_E_TIMEOUT) return set_err(h, SEM2D_E_TIMEOUT, "a bounded wait for shared-memory copies expired");
+  if (e == SEM2D_E_NAN)
+    return set_err(h, SEM2D_E_NAN, "non-finite velocity or displacement found by the check every info_every steps");
   if (e) return set_err(h, e, "device error");
   return SEM2D_OK;
 }
@@ -1271,6 +1340,11 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   bc.pitch = h->pitch;
   bc.plane = h->plane;
   if (!march_supported(bc)) return SEM2D_OK;
+  if (const char *e = std::getenv("SEM2D_MARCH_STAGE")) h->march_stage = std::atoi(e) != 0;
+  bc.march_stage = h->march_stage;
+  // resident warps per SM; also sets the kernels' shared-memory limit
+  const int warps_per_sm = march_warps_per_sm(bc);
+  if (warps_per_sm <= 0) return set_err(h, SEM2D_E_CUDA, std::string("march kernel: ") + bulk_last_error());
   int st;
   if (h->nflt) {
     // the fault kernel finishes the fault rows after the step: velocity or
@@ -1291,7 +1365,7 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
     int dev = 0, nsm = 0;
     CK(cudaGetDevice(&dev));
     CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const long long target = 2LL * nsm * std::max(march_warps_per_sm(bc), 1);
+    const long long target = 2LL * nsm * warps_per_sm;
     cz = int(((long long)nstrips * h->nz + target - 1) / target);
   }
   cz = std::max(1, std::min(cz, h->nz));
@@ -1413,6 +1487,9 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
   h->alpha = h->scheme == 2 ? d->alpha : 1.0;
   if (h->scheme == 2 && !(h->alpha >= 0.0 && h->alpha <= 1.0)) return set_err(h, SEM2D_E_ARG, "alpha out of [0,1]");
   h->keep_accel = h->scheme != 0 || d->rec_field == 'A';
+  h->nr_maxit = d->flt_nr_maxit > 0 ? d->flt_nr_maxit : 200;
+  h->info_every = d->info_every == 0 ? 100 : d->info_every;
+  if (const char *e = std::getenv("SEM2D_SPIN_LIMIT")) h->spin_limit = std::max(0, std::atoi(e));
   if (shared) {
     h->stream = shared;
     h->owns_stream = false;
@@ -1465,7 +1542,8 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     }
   }
   if ((st = dupload(h, &h->d_row0, h->row0))) return st;
-  if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)))
+  if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)) ||
+      (st = dalloc(h, &h->d_info, 2)))
     return st;
   h->H.assign(d->hprime, d->hprime + h->N * h->N);
   h->w.assign(d->wgll, d->wgll + h->N);
@@ -1689,7 +1767,8 @@ int batch_close_impl(sem2d_handle *h) {
   h->march = true;
   for (const sem2d_handle *m : h->subs) h->march = h->march && m->march && !m->nflt;
   int st;
-  if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)))
+  if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)) ||
+      (st = dalloc(h, &h->d_info, 2)))
     return st;
   // parameter blocks of every member for both buffer parities
   const size_t pb = params_bytes(h->N, h->mixed);
@@ -2002,17 +2081,34 @@ int sem2d_gpu_step(sem2d_handle *h, int nsteps) {
   if (h->batch_open) return set_err(h, SEM2D_E_STATE, "the batch is still open");
   if (nsteps < 0) return set_err(h, SEM2D_E_ARG, "negative step count");
   if (h->steps + nsteps > h->nt) return set_err(h, SEM2D_E_ARG, "stepping beyond nt");
-  if (h->ckpt_every <= 0) return step_impl(h, nsteps);
-  // keep the state of every ckpt_every-th step for the adjoint
+  // runs of steps end at every checkpoint (the state of every
+  // ckpt_every-th step is kept for the adjoint) and at every check of
+  // max|v|, max|d| (every info_every steps)
+  const int ie = h->subs.empty() ? h->info_every : h->subs[0]->info_every;
   int st, left = nsteps;
-  if (h->steps == 0 && (st = save_checkpoint(h, 0))) return st;
+  if (h->ckpt_every > 0 && h->steps == 0 && (st = save_checkpoint(h, 0))) return st;
   while (left > 0) {
-    const int to_next = h->ckpt_every - h->steps % h->ckpt_every;
-    const int n = std::min(left, to_next);
+    int n = left;
+    if (h->ckpt_every > 0) n = std::min(n, h->ckpt_every - h->steps % h->ckpt_every);
+    if (ie > 0) n = std::min(n, ie - h->steps % ie);
     if ((st = step_impl(h, n))) return st;
     left -= n;
-    if (h->steps % h->ckpt_every == 0 && (st = save_checkpoint(h, h->steps / h->ckpt_every))) return st;
+    if (h->ckpt_every > 0 && h->steps % h->ckpt_every == 0 && (st = save_checkpoint(h, h->steps / h->ckpt_every)))
+      return st;
+    if (ie > 0 && h->steps % ie == 0 && (st = launch_watch(h))) return st;
   }
+  return SEM2D_OK;
+}
+
+int sem2d_gpu_get_info(sem2d_handle *h, int *step, double *vmax, double *dmax) {
+  if (!h) return SEM2D_E_ARG;
+  sem2d_handle *b = h->owner ? h->owner : h;
+  double v[2] = {0.0, 0.0};
+  CK(cudaStreamSynchronize(b->stream));
+  CK(cudaMemcpy(v, b->d_info, sizeof(v), cudaMemcpyDeviceToHost));
+  if (step) *step = b->info_step;
+  if (vmax) *vmax = v[0];
+  if (dmax) *dmax = v[1];
   return SEM2D_OK;
 }
 

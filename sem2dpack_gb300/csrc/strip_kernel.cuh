@@ -262,7 +262,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
       else if (eb1 < ez1 && rw(eb1) == J) fate = 2;
       s_stat[jj] = fate;
     }
-    if (!mbar_wait(&bar[st], ph[st])) atomicOr(&s_err, 1);
+    if (!mbar_wait(&bar[st], ph[st], p.spin_limit)) atomicOr(&s_err, 1);
     ph[st] ^= 1u;
     __syncthreads();
     if (s_err) {

@@ -4,8 +4,9 @@
 // A batch of lattice rows is brought from global into shared memory with
 // one cp.async.bulk per (row, plane); the copies signal an mbarrier with
 // their byte counts (complete_tx) and the consumers wait on its phase.
-// Every wait is bounded: after kSpinLimit polls the caller gets `false`
-// and reports an error instead of spinning forever.
+// Every wait is bounded: after `limit` polls (kSpinLimit unless the step
+// parameters give another) the caller gets `false` and reports an error
+// instead of spinning forever.
 #pragma once
 
 #include <cstdint>
@@ -45,9 +46,10 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait for the phase with the given parity to complete
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-  for (int k = 0; k < kSpinLimit; ++k)
+// bounded wait for the phase with the given parity to complete: at most
+// `limit` polls (0: give up at once)
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int limit = kSpinLimit) {
+  for (int k = 0; k < limit; ++k)
     if (mbar_try_wait(bar, parity)) return true;
   return false;
 }

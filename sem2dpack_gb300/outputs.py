@@ -43,7 +43,30 @@ import os
 import numpy as np
 
 __all__ = ["write_seismograms", "read_seismograms", "write_fault", "read_fault", "write_potency", "write_run",
-           "write_fault_init", "write_grid", "read_grid", "write_snapshot"]
+           "write_fault_init", "write_grid", "read_grid", "write_snapshot", "rupture_time"]
+
+V_CRITICAL = 1.0e-3  # slip rate (m/s) that marks rupture (post-process-fault.py:53)
+
+
+def rupture_time(slip_rate, odt, v_crit=V_CRITICAL):
+    """Rupture time of every fault node from its slip-rate series.
+
+    slip_rate is (onx, nsamp), the second record of the fault series
+    (Solver.fault_series()[:, 1, :]) sampled every odt seconds.  The
+    reference's post-processing (POST/python/post-process-fault.py:55-62)
+    takes, per node, the first sample i (i = 0 .. nsamp-3) with v[i] < v_crit
+    and v[i+1] >= v_crit and returns i*odt; a node whose slip rate never
+    crosses v_crit gets 0.  Returns (times (onx,), sample index (onx,), with
+    -1 where there is no crossing).
+    """
+    v = np.asarray(slip_rate, dtype=np.float64)
+    onx, ns = v.shape
+    if ns < 3:
+        return np.zeros(onx), np.full(onx, -1, dtype=np.int64)
+    cross = (v[:, : ns - 2] < v_crit) & (v[:, 1: ns - 1] >= v_crit)
+    hit = cross.any(axis=1)
+    idx = np.where(hit, np.argmax(cross, axis=1), -1).astype(np.int64)
+    return np.where(hit, idx * float(odt), 0.0), idx
 
 
 def _fmt_list(*vals):

@@ -157,6 +157,36 @@ def test_noalloc_matches_handle_path(precision):
     assert np.linalg.norm(dn - pred) / np.linalg.norm(pred) <= TOL[precision]
 
 
+def test_noalloc_reports_device_failures_through_status(monkeypatch):
+    """A step whose bounded wait runs out (no polls allowed: SEM2D_SPIN_LIMIT
+    = 0) stores SEM2D_E_TIMEOUT in the caller's status int; the library
+    never clears it, and a later call with the normal limit leaves it set
+    until the caller resets it."""
+    torch = pytest.importorskip("torch")
+    P = workloads.build(workloads.plain_psv(scale=0.2, nsteps=20))
+    d = P.desc()
+    d.precision = PRECISION_FP64
+    L = lattice_arrays(d)
+    args, dev = make_args(d, L, torch, PRECISION_FP64)
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    args.status = C.c_void_p(status.data_ptr())
+    monkeypatch.setenv("SEM2D_SPIN_LIMIT", "0")
+    assert lib().sem2d_gpu_step_noalloc(C.byref(args), 2, None) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == abi.SEM2D_E_TIMEOUT
+    monkeypatch.delenv("SEM2D_SPIN_LIMIT")
+    args.step0 = 0
+    assert lib().sem2d_gpu_step_noalloc(C.byref(args), 2, None) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == abi.SEM2D_E_TIMEOUT  # sticky
+    status.zero_()
+    dev["d"].zero_()
+    dev["v"].zero_()
+    assert lib().sem2d_gpu_step_noalloc(C.byref(args), 2, None) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+
+
 def test_noalloc_rejects_oversized_problems():
     """Partner buffers beyond SEM2D_NOALLOC_SCRATCH_BYTES are refused before
     any device work."""
@@ -172,3 +202,4 @@ def test_noalloc_rejects_oversized_problems():
     args.hprime, args.wgll = C.cast(w, abi.P_double), C.cast(w, abi.P_double)
     args.nt = 10
     assert lib().sem2d_gpu_step_noalloc(C.byref(args), 1, None) == abi.SEM2D_E_ARG
+    assert b"too large" in lib().sem2d_gpu_last_error(None)
