@@ -1,29 +1,39 @@
 """Benchmark of the GB300 spectral-element time step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload sh_rupture|plain_psv|psv_rsf|batch_shots]
+                    [--workload batch_shots|sh_rupture|plain_psv|psv_rsf|...]
 
-A benchmark step is one complete solve of the workload (all its time steps,
-fields reset and L2 flushed before it; for batch_shots, 200 of the 3000 time
-steps of all 256 problems, one launch per time step for the whole batch).  The default workload is the SH
-dynamic rupture (400 x 200 elements, NGLL=5, 6000 steps, FP32 fields with
-FP64 fault state).  The metric is GLL node-steps per second.
+The default workload is the batched-shot configuration: 256 independent
+P-SV problems of uneven size (64^2..512^2 elements, NGLL=5, layered media,
+423 M GLL nodes in all, FP32 fields), one launch per time step for the whole
+batch, 3000 time steps.  The K benchmark steps are K consecutive parts of
+one complete 3000-step solve of every shot from rest, so the timed region is
+the whole solve; the W warm-up steps run before it on the same batch, which
+is then reset.  The metric is GLL node-steps per second.
+
+For the other workloads a benchmark step is one complete solve of the
+workload (all its time steps, fields reset and a 512 MB buffer written
+before it).
 
 Reported on one JSON line (rank 0):
-  value      node-steps/s of the solves, device-timed with CUDA events on the
-             solver's own stream, inputs resident on the device
-  e2e        the same metric through the C-ABI from host arrays: create
-             (host->device copies), all steps, seismograms and fault series
-             back to the host, destroy
+  value      node-steps/s of the timed solve, device-timed with CUDA events
+             on the solver's own stream, inputs resident on the device
+  e2e        the same metric through the C-ABI from host arrays: the
+             uploads of every problem, one complete solve, the seismograms
+             (and fault series) back to the host, destroy
   roofline   the bulk kernel: algorithmic bytes per launch / average launch
-             duration (CUDA events around every launch, a second pass)
-  cpu_baseline  the FP64 oracle (CPU port of the reference path, 1 thread)
-             on a bounded sample of the same workload
+             duration (CUDA events around every launch)
+  cpu_baseline  the FP64 oracle (CPU restatement of the reference path) on
+             a bounded sample of the same workload; for the batch, the
+             smallest shots run to the end, one per host thread, and the
+             GPU seismograms of those shots are compared with it
+  fp64_plain the FP64 GPU path on the plain P-SV box (batch workload)
 
 --impl reference times the CPU restatement of the reference path (the
-reference itself is Fortran and cannot be built here) on the same workload.
-Under torchrun every rank runs its own replica (no data exchange); rank 0
-prints the line and `value` is the sum over ranks of work / the slowest rank.
+reference itself is Fortran and cannot be built here) on the same workload,
+set up by the oracle's own restated init.  Under torchrun every rank runs
+its own replica (no data exchange); rank 0 prints the line and `value` is
+the sum over ranks of work / the slowest rank.
 """
 import argparse
 import json
@@ -31,6 +41,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -52,30 +63,61 @@ def parse():
     p.add_argument("--steps", type=int, default=5)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    p.add_argument("--workload", default="sh_rupture",
+    p.add_argument("--workload", default="batch_shots",
                    choices=["sh_rupture", "plain_psv", "psv_rsf", "batch_shots", "gradient_shots", "tpv3_inplane"])
     p.add_argument("--nsim", type=int, default=256, help="problems of the batch_shots workload")
     p.add_argument("--scale", type=float, default=1.0)
     p.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     p.add_argument("--cpu-seconds", type=float, default=15.0)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-fp64-plain", action="store_true")
     p.add_argument("--time-steps", type=int, default=0,
-                   help="time steps per solve (default: all of the workload, 200 for batch_shots)")
+                   help="time steps per solve (default: all of the workload)")
     return p.parse_args()
 
 
-def make_workload(args):
+class OracleGrid:
+    """The mesh and spectral grid from the oracle's restated setup, with the
+    Grid methods the workload builders use (so that the reference arm loads
+    no product library)."""
+
+    def __init__(self, deck):
+        from oracle import pyoracle as po
+        self.deck = deck
+        self.S = po.OracleSetup(deck, grid_only=True)
+
+    def coord(self):
+        return self.S.coord()
+
+    def ibool(self):
+        return self.S.ibool()
+
+    def fault_nodes(self, tags=None):
+        t1, t2 = tags or (self.deck.fault.tags if self.deck.fault else (5, 6))
+        n1 = self.S.boundary(t1)
+        if t2 <= 0:
+            return n1, None
+        n2 = self.S.boundary(t2)
+        keep = n1 != n2
+        return n1[keep], n2[keep]
+
+
+def workload_deck(args, grid_cls=None):
+    """(deck or (deck, grid), name) of a single-problem workload; grid_cls builds the grid
+    the builders evaluate their distributions on (the product's Grid by
+    default)."""
     from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, workloads
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    kw = {"grid_cls": grid_cls} if grid_cls else {}
     if args.workload == "sh_rupture":
-        pair = workloads.sh_rupture(scale=args.scale, precision=prec)
+        pair = workloads.sh_rupture(scale=args.scale, precision=prec, **kw)
         name = "SH antiplane rupture, SWF, 400x200 elements of 100 m, NGLL=5, 6000 steps"
     elif args.workload == "psv_rsf":
-        pair = workloads.psv_rsf(scale=args.scale, precision=prec)
+        pair = workloads.psv_rsf(scale=args.scale, precision=prec, **kw)
         name = "P-SV rate-and-state rupture (aging), von Karman medium, 1024x512 elements, NGLL=5"
     elif args.workload == "tpv3_inplane":
         # the reference's TPV3 in-plane example refined 8x in each direction
-        pair = workloads.tpv3_inplane(scale=8.0 * args.scale, precision=prec)
+        pair = workloads.tpv3_inplane(scale=8.0 * args.scale, precision=prec, **kw)
         name = ("SCEC TPV3 in-plane example refined 8x: 560x320 elements, NGLL=6, Newmark, Kelvin-Voigt band, "
                 "one-sided SWF fault, Dirichlet side, 16 s")
     else:
@@ -83,6 +125,12 @@ def make_workload(args):
         name = "plain P-SV elastic, 100x100 elements of 100 m, NGLL=5, 2000 steps"
     if args.scale != 1.0:
         name += " (scale %.3g)" % args.scale
+    return pair, name
+
+
+def make_workload(args):
+    from sem2dpack_gb300 import workloads
+    pair, name = workload_deck(args)
     return workloads.build(pair), name
 
 
@@ -109,12 +157,12 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % index)
+        self.path = None
 
     def start(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.f = open(self.path, "w")
+            fd, self.path = tempfile.mkstemp(prefix="sem2d_clocks_rank%d_" % self.index, suffix=".csv")
+            self.f = os.fdopen(fd, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.QUERY,
                                           "--format=csv,noheader,nounits", "-lms", "200"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
@@ -144,6 +192,10 @@ class ClockSampler:
             for n, v in zip(names, parts[5:9]):
                 if v.lower() == "active":
                     reasons.add(n)
+        try:
+            os.unlink(self.path)
+        except OSError:
+            pass
         if not sm:
             return None
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
@@ -191,144 +243,287 @@ def cpu_baseline(desc, owner, npoin, seconds):
 
 
 def run_reference(args, rank):
+    """The reference's CPU path (its FP64 restatement: the reference is
+    Fortran and no Fortran compiler exists here) on the workload of the
+    GB300 arm, set up by the oracle's own restated init (no product library
+    is loaded).  Each benchmark step is a bounded sample of the workload's
+    time steps; independent problems run one per host thread."""
     if rank != 0:
         return
+    from concurrent.futures import ThreadPoolExecutor
+
     from oracle import pyoracle as po
-    prob, name = make_workload(args)
-    d = prob.desc()
-    d.precision = 0
-    sim = po.OracleSim(d, owner=prob)
+    from sem2dpack_gb300 import workloads
+    threads = 1
+    if args.workload == "batch_shots":
+        decks = workloads.batch_shots(nsim=args.nsim, scale=args.scale, nsteps=3000)
+        sizes = [(dk.nelem[0] * 4 + 1) * (dk.nelem[1] * 4 + 1) for dk in decks]
+        name = batch_name(len(decks), sum(sizes), args.scale)
+        threads = max(1, min(os.cpu_count() or 1, 16))
+        # a seeded sample of the shots, one per host thread
+        import numpy as np
+        pick = np.random.default_rng(20261203).choice(len(decks), size=min(threads, len(decks)), replace=False)
+        setups = [po.OracleSetup(decks[int(i)]) for i in pick]
+        what = "%d of the %d shots (seeded sample), one per host thread" % (len(setups), len(decks))
+        nprob = len(decks)
+    else:
+        pair, name = workload_deck(args, grid_cls=OracleGrid)
+        setups = [po.OracleSetup(pair[0] if isinstance(pair, tuple) else pair)]
+        what = name
+        nprob = 1
+    sims = []
+    for S in setups:
+        d = S.desc()
+        d.precision = 0
+        sims.append((po.OracleSim(d, owner=S), d.npoin, d.nt))
     t0 = time.perf_counter()
-    sim.run(2)
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda s: s[0].run(2), sims))
     rate = 2 / max(time.perf_counter() - t0, 1e-9)
-    # one benchmark step = a bounded sample of the workload's time steps
-    per = max(1, min(int(rate * 2.0), (d.nt - 2) // max(1, args.steps + args.warmup)))
+    nt_min = min(s[2] for s in sims)
+    per = max(1, min(int(rate * 2.0), (nt_min - 2) // max(1, args.steps + args.warmup)))
+
+    def bench_step():
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda s: s[0].run(per), sims))
+
     for _ in range(args.warmup):
-        sim.run(per)
+        bench_step()
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        sim.run(per)
+        bench_step()
     el = time.perf_counter() - t0
-    value = d.npoin * per * args.steps / el
-    sample = "%d time steps per benchmark step of %s (%d GLL nodes), FP64, 1 thread" % (per, name, d.npoin)
+    value = sum(n for _, n, _ in sims) * per * args.steps / el
+    sample = "%d time steps per benchmark step of %s, FP64, %d thread(s)" % (per, what, threads)
     print(json.dumps({
         "impl": "reference", "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1000 * el / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": name, "global_batch": 1, "seq_len": 0, "parallelism": "replicas",
-                   "reference_build": "CPU restatement (oracle); the Fortran reference needs a Fortran compiler"},
-        "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": 1, "kind": "port",
+        "config": {"workload": name, "global_batch": len(sims), "seq_len": 0, "parallelism": "replicas",
+                   "reference_build": "CPU restatement of the reference's step (oracle), set up by its own "
+                                      "restated init; the Fortran reference needs a Fortran compiler"},
+        "cpu_baseline": {"value": value, "unit": "node-steps/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "node-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
 
-def run_batch(args, rank, world, local, torch, dist, barrier):
-    """The batched-shot configuration: many uneven P-SV problems stepped by
-    one launch per time step (sem2d_gpu_create_batch path)."""
-    from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, BatchSolver, workloads
-    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
-    nt_full = 3000
-    nt = args.time_steps or 200
-    decks = workloads.batch_shots(nsim=args.nsim, scale=args.scale, nsteps=nt_full, precision=prec)
-    sizes = {"npoin": 0, "h2d": 0, "d2h": 0}
+def batch_parts(nt, k):
+    """Time steps of each of the k benchmark steps that together make one
+    complete nt-step solve."""
+    k = max(1, min(k, nt))
+    return [nt // k + (1 if i < nt % k else 0) for i in range(k)]
 
-    def problems():
-        for dk in decks:
-            P = workloads.build(dk)
-            d = P.desc()
-            sizes["npoin"] += d.npoin
-            sizes["h2d"] += desc_bytes(d)
-            sizes["d2h"] += 8 * d.rec_nsamp * d.nrec * d.ndof
-            yield d
+
+def built_problems(decks, workers):
+    """Problems of the decks, built by `workers` host threads (the C++
+    builder releases the interpreter lock) with a bounded look-ahead, in
+    deck order."""
+    from collections import deque
+    from concurrent.futures import ThreadPoolExecutor
+
+    from sem2dpack_gb300 import workloads
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        it = iter(decks)
+        futs = deque(ex.submit(workloads.build, dk) for _, dk in zip(range(2 * workers), it))
+        while futs:
+            P = futs.popleft().result()
+            nxt = next(it, None)
+            if nxt is not None:
+                futs.append(ex.submit(workloads.build, nxt))
+            yield P
             del P
 
-    sim = BatchSolver(problems())
-    npoin = sizes["npoin"]
+
+def oracle_sample(decks, nsteps_of, threads):
+    """Runs the FP64 oracle (CPU restatement of the reference's step, one
+    problem per host thread, as independent reference runs would) on the
+    given decks; returns (node-steps, wall seconds, [seismograms])."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import pyoracle as po
+    sims = []
+    for dk in decks:
+        S = po.OracleSetup(dk)
+        d = S.desc()
+        d.precision = 0
+        sims.append((po.OracleSim(d, owner=S), d.npoin, nsteps_of(d)))
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        list(ex.map(lambda s: s[0].run(s[2]), sims))
+    wall = time.perf_counter() - t0
+    return sum(n * k for _, n, k in sims), wall, [s[0].seismograms() for s in sims]
+
+
+def batch_name(nsim, npoin, scale):
+    name = ("batched P-SV shots: %d problems of 64^2..512^2 elements (25 m), NGLL=5, 3-8 layer media, "
+            "Ricker force, 32 receivers, 3000 steps, %d GLL nodes in total" % (nsim, npoin))
+    if scale != 1.0:
+        name += " (scale %.3g)" % scale
+    return name
+
+
+def run_batch(args, rank, world, local, torch, dist, barrier):
+    """The batched-shot configuration: 256 uneven P-SV problems stepped by
+    one launch per time step (sem2d_gpu_batch_* path), all 3000 time steps
+    of the solve timed: the K benchmark steps are consecutive parts of one
+    complete solve from rest."""
+    import numpy as np
+
+    from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, BatchSolver, workloads
+    prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
+    decks = workloads.batch_shots(nsim=args.nsim, scale=args.scale, nsteps=3000, precision=prec)
+    nt = min(args.time_steps or 3000, 3000)
+    workers = max(1, min(16, os.cpu_count() or 1))
+    t0 = time.perf_counter()
+    sim = BatchSolver(built_problems(decks, workers))
+    setup_s = time.perf_counter() - t0
+    descs = [m.desc for m in sim.members]
+    npoin = sum(d.npoin for d in descs)
+    h2d = sum(desc_bytes(d) for d in descs)
+    d2h = sum(8 * d.rec_nsamp * d.nrec * d.ndof for d in descs)
     dtype = "f32" if prec == PRECISION_MIXED else "f64"
-    name = ("batched P-SV shots: %d problems of 64^2..512^2 elements (25 m), NGLL=5, layered media, "
-            "%d GLL nodes in total" % (len(sim), npoin))
-    if args.scale != 1.0:
-        name += " (scale %.3g)" % args.scale
+    name = batch_name(len(sim), npoin, args.scale)
     stream = torch.cuda.ExternalStream(sim.stream)
 
-    def one_solve(timed):
-        sim.reset()
-        barrier()
-        if not timed:
-            sim.step(nt)
-            sim.sync()
-            return 0.0
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        sim.step(nt)
-        e1.record(stream)
-        e1.synchronize()
-        sim.sync()
-        return e0.elapsed_time(e1)
+    # end to end through the C-ABI from host arrays: the uploads made while
+    # the batch was built (sem2d_gpu_batch_add / close), one complete solve,
+    # every member's seismograms back, and (below) the destroy
+    barrier()
+    t0 = time.perf_counter()
+    sim.step(nt)
+    sis_gpu = [m.seismograms() for m in sim.members]
+    t_run = time.perf_counter() - t0
 
+    # device-resident: warm-up parts, then one complete solve from rest in
+    # K parts, events around each part and around every kernel launch
+    parts = batch_parts(nt, args.steps)
+    sim.reset()
+    left = nt
     for _ in range(args.warmup):
-        one_solve(False)
+        if left < parts[0]:
+            sim.reset()
+            left = nt
+        sim.step(parts[0])
+        left -= parts[0]
+    sim.sync()
+    sim.reset()
+    barrier()
     clocks = ClockSampler(local)
     clocks.start()
     l0 = sim.launches
-    ms = [one_solve(True) for _ in range(args.steps)]
+    ms, bulk = [], 0.0
+    for n in parts:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        kms = sim.step_timed(n)
+        e1.record(stream)
+        e1.synchronize()
+        ms.append(e0.elapsed_time(e1))
+        bulk += kms[0]
     launches = sim.launches - l0
+    barrier()
     clk = clocks.stop()
     total = sum(ms)
     if dist is not None:
         t = torch.tensor([total], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         total = float(t.item())
-    value = world * npoin * nt * args.steps / (total / 1000.0)
-    sim.reset()
-    kms = sim.step_timed(nt)
-    bulk_ms = kms[0] / nt
+    value = world * npoin * nt / (total / 1000.0)
+    bulk_ms = bulk / nt
     bpn = BYTES_PER_NODE_STEP[(2, dtype)]
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
-    # the one-element-per-thread kernel covers FP32 NGLL=5 isotropic problems
     kernel = "march_batch_kernel" if sim.tile[0] == MARCH_TX else "strip_batch_kernel"
     traffic = ncu_traffic(kernel, "batch_shots", npoin)
-    # end to end: uploads of every problem (the host arrays of the
-    # descriptors), the time steps, all seismograms back, destroy
-    barrier()
-    t0 = time.perf_counter()
-    sim.reset()
-    sim.step(nt)
-    for m in sim.members:
-        m.seismograms()
-    t_run = time.perf_counter() - t0
     t0 = time.perf_counter()
     sim.close()
     t_close = time.perf_counter() - t0
     e2e_value = world * npoin * nt / (sim.upload_seconds + t_run + t_close)
+
+    base = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # the smallest shots, all their time steps, one per host thread
+        order = np.argsort([d.npoin for d in descs])
+        threads = max(1, min(os.cpu_count() or 1, 16))
+        pick = [int(i) for i in order[:threads]]
+        ns, wall, sis_ref = oracle_sample([decks[i] for i in pick], lambda d: nt, threads)
+        err = max(float(np.linalg.norm(sis_gpu[i] - r) / np.linalg.norm(r)) for i, r in zip(pick, sis_ref))
+        base = {"value": ns / wall, "unit": "node-steps/s", "cores": threads, "kind": "port",
+                "sample": "the %d smallest of the %d shots (%d GLL nodes), all %d time steps each, FP64, "
+                          "one shot per host thread" % (len(pick), len(descs), sum(descs[i].npoin for i in pick), nt),
+                "sample_seconds": wall,
+                "seismogram_rel_l2_max": err,
+                "seismogram_rel_l2_note": "GPU mixed-precision seismograms of the sampled shots against this FP64 "
+                                          "oracle run, all time steps"}
+
+    fp64 = None
+    if rank == 0 and not args.no_fp64_plain:
+        fp64 = fp64_plain_record(torch, barrier)
+
     if rank == 0:
         print(json.dumps({
             "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / args.steps,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total / len(parts),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": dtype,
             "data": "synthetic",
-            "config": {"workload": name, "global_batch": len(sim.members), "seq_len": 0,
-                       "parallelism": "replicas", "npoin": npoin, "time_steps_per_step": nt,
+            "config": {"workload": name, "global_batch": len(descs), "seq_len": 0,
+                       "parallelism": "replicas", "npoin": npoin,
+                       "time_steps_timed": nt, "time_steps_per_step": nt / len(parts),
+                       "timed_region": "one complete %d-step solve of every shot from rest, in %d consecutive "
+                                       "benchmark steps" % (nt, len(parts)),
                        "precision": "FP32 fields" if dtype == "f32" else "FP64",
-                       "l2": "inputs larger than L2 (the batch's fields are %.1f GB)"
-                             % (npoin * bpn / 1e9)},
+                       "l2": "inputs larger than L2 (the batch's fields are %.1f GB)" % (npoin * bpn / 1e9),
+                       "host_setup_s": setup_s},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
                          "traffic": traffic, "peak_kind": peak_kind,
                          "kernel": kernel, "bytes_per_node_step": bpn,
-                         "bulk_ms_per_launch": bulk_ms},
-            "cpu_baseline": None,
-            "e2e": {"value": e2e_value, "unit": "node-steps/s", "h2d_bytes_per_step": sizes["h2d"],
-                    "d2h_bytes_per_step": sizes["d2h"],
-                    "upload_s": sim.upload_seconds, "run_s": t_run},
+                         "bulk_ms_per_launch": bulk_ms,
+                         "launch_timing": "CUDA events around every launch of the timed solve"},
+            "cpu_baseline": base,
+            "e2e": {"value": e2e_value, "unit": "node-steps/s",
+                    "h2d_bytes_per_step": h2d / len(parts), "d2h_bytes_per_step": d2h / len(parts),
+                    "h2d_bytes_per_solve": h2d, "d2h_bytes_per_solve": d2h,
+                    "upload_s": sim.upload_seconds, "run_s": t_run, "destroy_s": t_close,
+                    "path": "BatchSolver through the C-ABI: batch_add of every shot from host arrays, "
+                            "one complete solve, all seismograms back, destroy"},
+            "fp64_plain": fp64,
             "clocks": clk,
             "gpu_launches": launches,
         }), flush=True)
     if dist is not None:
         dist.destroy_process_group()
+
+
+def fp64_plain_record(torch, barrier):
+    """The plain FP64 P-SV box (100 x 100 elements, NGLL=5, 2000 steps):
+    the FP64 GPU path beside the mixed-precision headline."""
+    from sem2dpack_gb300 import PRECISION_FP64, Solver, workloads
+    P = workloads.build(workloads.plain_psv(precision=PRECISION_FP64))
+    d = P.desc()
+    sim = Solver(d, owner=P)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    ms = []
+    for k in range(4):
+        sim.reset()
+        flush.fill_(1.0)
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        sim.step(d.nt)
+        e1.record(stream)
+        e1.synchronize()
+        if k:
+            ms.append(e0.elapsed_time(e1))
+    sim.sync()
+    sim.close()
+    best = min(ms)
+    return {"workload": "plain P-SV elastic, 100x100 elements of 100 m, NGLL=5, 2000 steps, FP64",
+            "value": d.npoin * d.nt / (best / 1000.0), "unit": "node-steps/s", "ms_per_solve": best,
+            "npoin": d.npoin, "solves_timed": len(ms)}
 
 
 def run_gradient(args, rank, world, local, torch, dist, barrier):

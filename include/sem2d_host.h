@@ -200,6 +200,12 @@ const char *sem2d_host_last_error(void);
  * foreign-language bindings can check their struct layouts. */
 int sem2d_abi_struct_sizes(int *desc_size, int *deck_size);
 
+/* Offsets (bytes) of every member of a C-ABI structure as compiled, in
+ * declaration order: which = 0 sem2d_problem_desc, 1 sem2d_deck,
+ * 2 sem2d_lattice_args.  Writes min(n, count) offsets when offsets is not
+ * NULL and returns the member count (SEM2D_E_ARG for an unknown which). */
+int sem2d_abi_field_offsets(int which, long long *offsets, int n);
+
 #ifdef __cplusplus
 }
 #endif

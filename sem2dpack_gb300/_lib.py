@@ -61,6 +61,7 @@ PROTOTYPES = [
     ("sem2d_problem_destroy", None, [vp]),
     ("sem2d_host_last_error", C.c_char_p, []),
     ("sem2d_abi_struct_sizes", C.c_int, [ip, ip]),
+    ("sem2d_abi_field_offsets", C.c_int, [C.c_int, C.POINTER(C.c_longlong), C.c_int]),
 ]
 
 

@@ -84,6 +84,7 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.nplanes = c.nplanes;
   p.error = c.error;
   p.spin_limit = c.spin_limit;
+  p.march_pf = c.march_pf;
   p.chunk_shift = c.chunk_shift;
 }
 

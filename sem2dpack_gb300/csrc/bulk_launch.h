@@ -58,6 +58,8 @@ struct BulkConfig {
   int spin_limit = 1 << 22;  // polls of a stage's mbarrier before giving up
   int chunk_shift = 0;   // chunk scheduled first (the fault's)
   int march_stage = 1;   // march kernels: rows staged through shared memory (1) or loaded directly (0)
+  int march_warps = 4;   // march kernels: warps per CTA (1, 2 or 4)
+  int march_pf = 0;      // march kernels, direct loads: L2 prefetch of the next element row
   cudaStream_t stream = nullptr;
 };
 

@@ -17,9 +17,11 @@ namespace {
 constexpr int kThreads = 32 * kMarchWarps;
 static_assert(kMarchWarpsHost == kMarchWarps, "host and device CTA shapes");
 
+// warps per CTA of a launch (1, 2 or 4) and the shared memory it needs
+int cta_warps(const BulkConfig &c) { return c.march_warps == 1 || c.march_warps == 2 ? c.march_warps : kMarchWarps; }
 template <int NDOF, int MAT, bool STG>
-constexpr size_t ring_bytes() {
-  return STG ? MarchStage<NDOF, MAT>::kCtaBytes : 0;
+constexpr size_t ring_bytes(int warps = kMarchWarps) {
+  return STG ? warps * MarchStage<NDOF, MAT>::kWarpBytes : 0;
 }
 
 template <int NDOF, int MAT, bool STG>
@@ -40,8 +42,9 @@ template <int NDOF, int MAT, bool STG>
 int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
-  const int grid = std::max(1, (m.nunits + kMarchWarps - 1) / kMarchWarps);  // an empty set still counts the step
-  march_step_kernel<NDOF, MAT, STG><<<grid, kThreads, ring_bytes<NDOF, MAT, STG>(), c.stream>>>(
+  const int wpc = cta_warps(c);
+  const int grid = std::max(1, (m.nunits + wpc - 1) / wpc);  // an empty set still counts the step
+  march_step_kernel<NDOF, MAT, STG><<<grid, 32 * wpc, ring_bytes<NDOF, MAT, STG>(wpc), c.stream>>>(
       p, static_cast<const MarchUnit *>(m.units), m.nunits);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -61,8 +64,9 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   b.nunits = m.nunits;
   b.step = m.step;
   b.done = m.done;
-  const int grid = std::max(1, (m.nunits + kMarchWarps - 1) / kMarchWarps);  // an empty set still counts the step
-  march_batch_kernel<NDOF, MAT, STG><<<grid, kThreads, ring_bytes<NDOF, MAT, STG>(), c.stream>>>(b);
+  const int wpc = cta_warps(c);
+  const int grid = std::max(1, (m.nunits + wpc - 1) / wpc);  // an empty set still counts the step
+  march_batch_kernel<NDOF, MAT, STG><<<grid, 32 * wpc, ring_bytes<NDOF, MAT, STG>(wpc), c.stream>>>(b);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -72,13 +76,13 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
 }
 
 template <int NDOF, int MAT, bool STG>
-int occupancy_one() {
+int occupancy_one(int wpc) {
   int nb = 0;
   if (configure_typed<NDOF, MAT, STG>()) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, STG>, kThreads,
-                                                    ring_bytes<NDOF, MAT, STG>()) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, STG>, 32 * wpc,
+                                                    ring_bytes<NDOF, MAT, STG>(wpc)) != cudaSuccess)
     return 0;
-  return nb * kMarchWarps;
+  return nb * wpc;
 }
 
 // the instantiation for (ndof, material layout, staging) of c
@@ -102,7 +106,7 @@ struct LaunchMany {
 };
 template <int NDOF, int MAT, bool STG>
 struct Occupancy {
-  static int run() { return occupancy_one<NDOF, MAT, STG>(); }
+  static int run(int wpc) { return occupancy_one<NDOF, MAT, STG>(wpc); }
 };
 
 }  // namespace
@@ -208,6 +212,6 @@ int launch_march_adjoint(const MarchAdjConfig &c) {
   return 0;
 }
 
-int march_warps_per_sm(const BulkConfig &c) { return dispatch<Occupancy>(c); }
+int march_warps_per_sm(const BulkConfig &c) { return dispatch<Occupancy>(c, cta_warps(c)); }
 
 }  // namespace sem2d

@@ -65,7 +65,7 @@
 
 namespace sem2d {
 
-constexpr int kMarchWarps = 4;     // warps per CTA
+constexpr int kMarchWarps = 4;     // warps per CTA at most (the launch picks 1, 2 or 4)
 constexpr int kMarchCols = 31;     // element columns owned by a warp
 // resident CTAs per SM the register budget allows: 102 registers per
 // thread for SH (20 warps per SM), 168 for P-SV (12 warps; fewer registers
@@ -91,7 +91,7 @@ struct MarchStage {
   static constexpr int kFields = 2 * NDOF + 1 + (kStageMat ? NDOF : 0);
   static constexpr int kSlot = kFields * kRowF;
   static constexpr int kWarpFloats = kRingSlots * kSlot;
-  static constexpr size_t kCtaBytes = size_t(kMarchWarps) * kWarpFloats * sizeof(float);
+  static constexpr size_t kWarpBytes = size_t(kWarpFloats) * sizeof(float);
 };
 
 __device__ __forceinline__ void cp_async16(float *dst, const float *src) {
@@ -100,6 +100,11 @@ __device__ __forceinline__ void cp_async16(float *dst, const float *src) {
                : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// asks the TMA engine to bring `bytes` (a multiple of 16) at a 16-byte
+// aligned address into L2; no completion to wait for
+__device__ __forceinline__ void prefetch_l2(const float *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
 template <int K>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory");
@@ -186,6 +191,22 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     if (zs + 1 < u.z1) stage_elem_row(zs + 1, false);
     cp_async_commit();
   }
+  // direct loads with p.march_pf: the rows of element row ezn (fields as
+  // staged, plus the node material) are prefetched into L2, one bulk
+  // prefetch of the warp's row segment per lane, while the row below computes
+  constexpr int kPfFields = 2 * NDOF + 1 + (MAT == kMatNode ? NDOF : 0);
+  auto prefetch_elem_row = [&](int ezn) {
+    const int Ja = p.row0[ezn];
+    const int c0 = cs < 0 ? 0 : cs, c1 = cs + 132 < p.pitch ? cs + 132 : p.pitch;
+    for (int q = lane; q < N * kPfFields; q += 32) {
+      const int j = q / kPfFields, f = q - j * kPfFields;
+      const float *b = f < NDOF           ? p.Dcur + f * pl
+                       : f < 2 * NDOF     ? p.Vcur + (f - NDOF) * pl
+                       : f == 2 * NDOF    ? p.rmass
+                                          : p.mat[f - 2 * NDOF - 1];
+      if (c1 > c0) prefetch_l2(b + (long long)(Ja + j) * p.pitch + c0, uint32_t(c1 - c0) * 4u);
+    }
+  };
 
   float carry[NDOF][N];  // forces on the node row shared with the next element row
 #pragma unroll
@@ -227,6 +248,8 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     if constexpr (STG) {
       cp_async_wait<1>();  // this element row's group has landed
       __syncwarp();        // and the other lanes' pieces are visible
+    } else {
+      if (p.march_pf && ez + 1 < u.z1) prefetch_elem_row(ez + 1);
     }
     const bool halo = ez < u.z0;
     const int J0 = p.row0[ez];
@@ -581,15 +604,17 @@ __device__ __forceinline__ void march_done(int *step, unsigned *done, int it) {
   }
 }
 
-// one problem: warp w of CTA b walks unit kMarchWarps*b + w (STG: with
-// its ring in the CTA's dynamic shared memory, MarchStage::kCtaBytes)
+// one problem: warp w of CTA b walks unit (warps per CTA)*b + w (STG: with
+// its ring in the CTA's dynamic shared memory, MarchStage::kWarpBytes per
+// warp).  The launch picks 1, 2 or 4 warps per CTA: with one, a warp that
+// finishes its unit frees its slot at once.
 template <int NDOF, int MAT, bool STG>
 __global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBlocks))
     march_step_kernel(const __grid_constant__ BulkParams<float, 5> p, const MarchUnit *units, int nunits) {
   extern __shared__ __align__(16) float march_ring[];
   const int warp = threadIdx.x >> 5;
   const int it = *p.step + 1;
-  const int uid = blockIdx.x * kMarchWarps + warp;
+  const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (uid < nunits) {
     const MarchUnit u = units[uid];
     march_unit<NDOF, MAT, STG>(p, p.H, p.w, u, it, march_ring + warp * MarchStage<NDOF, MAT>::kWarpFloats);
@@ -604,7 +629,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBl
   extern __shared__ __align__(16) float march_ring[];
   const int warp = threadIdx.x >> 5;
   const int it = *b.step + 1;
-  const int uid = blockIdx.x * kMarchWarps + warp;
+  const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (uid < b.nunits) {
     const MarchUnit u = b.units[uid];
     march_unit<NDOF, MAT, STG>(b.sims[u.prob], b.H, b.w, u, it, march_ring + warp * MarchStage<NDOF, MAT>::kWarpFloats);

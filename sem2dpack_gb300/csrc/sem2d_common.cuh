@@ -142,6 +142,7 @@ struct BulkParams {
   int nplanes;            // lattice planes staged per batch (strip_planes)
   int *error;             // sticky device error flag (SEM2D_E_*)
   int spin_limit;         // polls of a stage's mbarrier before the step gives up
+  int march_pf;           // march kernel: prefetch the next element row into L2
   int chunk_shift;        // chunk of CTA row y is (y + chunk_shift) % rows: the
                           // fault's chunk (long FP64 work) is scheduled first
 };

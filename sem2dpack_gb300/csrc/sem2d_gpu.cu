@@ -122,7 +122,9 @@ struct sem2d_handle {
   // the one-element-per-thread kernel (FP32, NGLL = 5 fast path): work
   // units (strip, chunk) and the receivers each unit samples
   bool march = false;
-  int march_stage = 1;  // rows staged through shared memory (SEM2D_MARCH_STAGE=0: direct loads)
+  int march_stage = 0;  // rows staged through shared memory (SEM2D_MARCH_STAGE=1) or loaded directly
+  int march_warps = 4;  // warps per CTA (SEM2D_MARCH_WARPS)
+  int march_pf = 0;     // direct loads: L2 prefetch of the next element row (SEM2D_MARCH_PREFETCH)
   int march_cz = 0, march_nunits = 0;
   void *d_march_units = nullptr;
   int *d_march_rec = nullptr;
@@ -787,6 +789,8 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.error = h->d_error;
   bc.spin_limit = h->spin_limit;
   bc.march_stage = h->march_stage;
+  bc.march_warps = h->march_warps;
+  bc.march_pf = h->march_pf;
   bc.grid_x = (h->nx + h->TX - 1) / h->TX;
   bc.grid_y = int(h->ztile.size()) - 1;
   bc.LX = h->LX;
@@ -1341,7 +1345,10 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   bc.plane = h->plane;
   if (!march_supported(bc)) return SEM2D_OK;
   if (const char *e = std::getenv("SEM2D_MARCH_STAGE")) h->march_stage = std::atoi(e) != 0;
+  if (const char *e = std::getenv("SEM2D_MARCH_WARPS")) h->march_warps = std::atoi(e);
+  if (const char *e = std::getenv("SEM2D_MARCH_PREFETCH")) h->march_pf = std::atoi(e) != 0;
   bc.march_stage = h->march_stage;
+  bc.march_warps = h->march_warps;
   // resident warps per SM; also sets the kernels' shared-memory limit
   const int warps_per_sm = march_warps_per_sm(bc);
   if (warps_per_sm <= 0) return set_err(h, SEM2D_E_CUDA, std::string("march kernel: ") + bulk_last_error());
@@ -2410,6 +2417,8 @@ int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms) {
   constexpr int kBatch = 64;
   std::vector<cudaEvent_t> ev(4 * kBatch);
   for (auto &e : ev) CK(cudaEventCreate(&e));
+  // the same max|v|, max|d| checks as sem2d_gpu_step (outside the events)
+  const int ie = h->subs.empty() ? h->info_every : h->subs[0]->info_every;
   int st = SEM2D_OK;
   for (int done = 0; done < nsteps && !st;) {
     const int nb = std::min(kBatch, nsteps - done);
@@ -2421,6 +2430,10 @@ int sem2d_gpu_step_timed(sem2d_handle *h, int nsteps, double *ms) {
                       : launch_one_step<double>(h, h->cur, &ev[4 * k]);
       h->cur = 1 - h->cur;
       h->steps++;
+      if (!st && ie > 0 && h->steps % ie == 0) {
+        sync_members(h);
+        st = launch_watch(h);
+      }
     }
     sync_members(h);
     if (st) break;

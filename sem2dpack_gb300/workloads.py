@@ -71,7 +71,7 @@ def _correlated_noise(rng, x, corr, amp, dx=25.0):
     return vals * (amp / np.max(np.abs(vals)))
 
 
-def sh_rupture(scale=1.0, nsteps=6000, precision=abi.PRECISION_MIXED, out_every=10):
+def sh_rupture(scale=1.0, nsteps=6000, precision=abi.PRECISION_MIXED, out_every=10, grid_cls=Grid):
     """SH antiplane rupture on a split-node fault with slip weakening.
 
     The nucleation patch (81 MPa) must exceed the static strength to start
@@ -93,7 +93,7 @@ def sh_rupture(scale=1.0, nsteps=6000, precision=abi.PRECISION_MIXED, out_every=
                             last=(0.9 * Lx, 0.5 * Lz + 2000.0 * min(scale * 4, 1.0)), field="V"),
         precision=precision,
     )
-    grid = Grid(deck)
+    grid = grid_cls(deck)
     n1, _ = grid.fault_nodes()
     x = grid.coord()[0, n1 - 1]
     xc = 0.5 * Lx
@@ -135,7 +135,7 @@ def _bilinear(field, x0, z0, dx, x, z):
             + (1 - tx) * tz * field[j + 1, i] + tx * tz * field[j + 1, i + 1])
 
 
-def psv_rsf(scale=1.0, nsteps=10000, precision=abi.PRECISION_MIXED, rsf_kind=2, out_every=10):
+def psv_rsf(scale=1.0, nsteps=10000, precision=abi.PRECISION_MIXED, rsf_kind=2, out_every=10, grid_cls=Grid):
     """In-plane rupture with rate-and-state friction in a random medium.
 
     Background vp/vs/rho 6000/3464/2670 perturbed by one von Karman field
@@ -159,7 +159,7 @@ def psv_rsf(scale=1.0, nsteps=10000, precision=abi.PRECISION_MIXED, rsf_kind=2, 
                             last=(0.9 * Lx, 0.5 * Lz + 1500.0), field="V"),
         precision=precision,
     )
-    grid = Grid(deck)
+    grid = grid_cls(deck)
     rng = _rng(2)
     dxg = 25.0
     gx, gz = int(Lx / dxg) + 2, int(Lz / dxg) + 2
@@ -269,7 +269,7 @@ def build(deck_or_pair):
     return Problem(deck_or_pair)
 
 
-def tpv3_inplane(scale=1.0, nsteps=None, precision=abi.PRECISION_MIXED):
+def tpv3_inplane(scale=1.0, nsteps=None, precision=abi.PRECISION_MIXED, grid_cls=Grid):
     """The reference's SCEC TPV3 in-plane example (EXAMPLES/
     TestFlt2D_SCEC_TPV3_inplane/Par.inp) with its element count multiplied
     by `scale` in each direction (the domain stays 35 x 20 km): NGLL=6,
@@ -290,7 +290,7 @@ def tpv3_inplane(scale=1.0, nsteps=None, precision=abi.PRECISION_MIXED):
                             field="V"),
         precision=precision,
     )
-    grid = Grid(deck)
+    grid = grid_cls(deck)
     xz = grid.coord()
     n1, _ = grid.fault_nodes()
     x, z = xz[0, n1 - 1], xz[1, n1 - 1]

@@ -25,3 +25,10 @@ def has_gpu():
 def golden():
     import numpy as np
     return np.load(os.path.join(ROOT, "tests", "golden", "golden.npz"))
+
+
+def watch_launches(nsteps, members=1, every=100):
+    """Launches of the max|v|, max|d| check in a run of nsteps steps from
+    step 0 (one kernel per problem every `every` steps, the default
+    info_every)."""
+    return members * (nsteps // every)

@@ -10,6 +10,7 @@ depend on the work decomposition).
 """
 import numpy as np
 import pytest
+from conftest import watch_launches
 
 from oracle import pyoracle as po
 from sem2dpack_gb300 import PRECISION_MIXED, Solver, workloads
@@ -121,7 +122,7 @@ def test_march_receivers(field, atnode, monkeypatch):
     o.run(150)
     assert rel_l2(g.seismograms(), o.seismograms()) <= 1e-4
     # interpolated velocity is sampled by the separate kernel after the step
-    assert g.launches == 150 * (2 if (field != "D" and not atnode) else 1)
+    assert g.launches == 150 * (2 if (field != "D" and not atnode) else 1) + watch_launches(150)
 
 
 def test_fused_fault_side_equals_separate_kernels(monkeypatch):
@@ -134,7 +135,7 @@ def test_fused_fault_side_equals_separate_kernels(monkeypatch):
     lg, lh = g.launches, h.launches
     g.step(nt)
     h.step(nt)
-    assert g.launches - lg == 2 * nt and h.launches - lh == 3 * nt
+    assert g.launches - lg == 2 * nt + watch_launches(nt) and h.launches - lh == 3 * nt + watch_launches(nt)
     a, b = outputs(g, True), outputs(h, True)
     for k in a:
         assert np.array_equal(a[k], b[k]), k
