@@ -206,6 +206,37 @@ int sem2d_abi_struct_sizes(int *desc_size, int *deck_size);
  * NULL and returns the member count (SEM2D_E_ARG for an unknown which). */
 int sem2d_abi_field_offsets(int which, long long *offsets, int n);
 
+/* ---- tuning cache of the one-element-per-thread kernel's launch shape
+ * (no counterpart in the reference, which is serial).  The first handle of
+ * a class of problems times candidate shapes on the device and records the
+ * fastest; later handles of the class read it.  The cache is a text file of
+ * one JSON object per line (see autotune.cpp); its path is SEM2D_TUNE_CACHE,
+ * else $XDG_CACHE_HOME/sem2dpack_gb300/tune.json, else
+ * $HOME/.cache/sem2dpack_gb300/tune.json.  SEM2D_AUTOTUNE=0 switches the
+ * timing off (the analytic shape is used). */
+typedef struct sem2d_tune_entry {
+  int chunk_rows;     /* element rows per work unit                       */
+  int warps_per_cta;  /* 1, 2 or 4                                        */
+  int l2_prefetch;    /* 1: the next element row is prefetched into L2    */
+  int staged;         /* 1: rows staged through shared memory (cp.async)  */
+  double ms_per_step; /* measured                                         */
+} sem2d_tune_entry;
+/* The cache path into buf (n bytes); returns 0, or the bytes needed when
+ * buf is NULL or too small, or SEM2D_E_STATE when no location is known. */
+int sem2d_tune_cache_path(char *buf, int n);
+/* The key of a class: dof count, material layout (0 node planes, 2 one
+ * value per element), node count and member count (0: a single problem)
+ * to a power of two, SM count. */
+int sem2d_tune_key(int ndof, int mat_layout, long long nodes, int members, int nsm, char *buf, int n);
+/* 1 and *out when the cache holds key, 0 when it does not. */
+int sem2d_tune_lookup(const char *path, const char *key, sem2d_tune_entry *out);
+/* Records (or replaces) the entry of key; the file is rewritten atomically. */
+int sem2d_tune_record(const char *path, const char *key, const sem2d_tune_entry *e);
+/* Index of the fastest of n timed candidates; candidate 0 (the analytic
+ * shape) is kept unless another is faster by more than keep_margin (a
+ * fraction of its time). */
+int sem2d_tune_select(const sem2d_tune_entry *cands, int n, double keep_margin);
+
 #ifdef __cplusplus
 }
 #endif

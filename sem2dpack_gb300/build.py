@@ -16,7 +16,7 @@ OUT_DIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(OUT_DIR, "libsem2d_gb300.so")
 CU_SOURCES = ["sem2d_gpu.cu", "bulk_launch.cu", "bulk_n3.cu", "bulk_n5.cu", "bulk_n6.cu", "bulk_n9.cu", "noalloc.cu",
               "adjoint.cu", "march.cu"]
-CPP_SOURCES = ["host_builder.cpp", "abi_layout.cpp"]
+CPP_SOURCES = ["host_builder.cpp", "abi_layout.cpp", "autotune.cpp"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

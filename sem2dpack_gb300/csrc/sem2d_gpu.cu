@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/sem2d_gpu.h"
+#include "../../include/sem2d_host.h"
 #include "bulk_launch.h"
 #include "fault_kernel.cuh"
 #include "sem2d_common.cuh"
@@ -125,10 +126,12 @@ struct sem2d_handle {
   int march_stage = 0;  // rows staged through shared memory (SEM2D_MARCH_STAGE=1) or loaded directly
   int march_warps = 4;  // warps per CTA (SEM2D_MARCH_WARPS)
   int march_pf = 0;     // direct loads: L2 prefetch of the next element row (SEM2D_MARCH_PREFETCH)
+  int tune_source = 0;  // launch shape: 0 analytic, 1 timed at create, 2 from the tuning cache
   int march_cz = 0, march_nunits = 0;
   void *d_march_units = nullptr;
   int *d_march_rec = nullptr;
   std::vector<int> march_units_host;
+  std::vector<int> march_rec_ex, march_rec_ez;  // element of every receiver (units are rebuilt by the tuner)
   float *d_fault_force = nullptr;
   // with a fault: the first march_fault_units units are the fault chunk's,
   // launched as their own kernel with their own step/done counters; the
@@ -1323,59 +1326,24 @@ int owner_row(const sem2d_handle *h, int J) {
   return std::max(0, std::min(ez, h->nz - 1));
 }
 
-// Work units of the march kernel: strips of 31 element columns by chunks of
-// element rows.  The chunk height gives about two units per resident warp
-// (SEM2D_MARCH_CZ overrides it); a two-sided fault's rows stay in one chunk,
-// whose units come first (their FP64 fault work is the longest).
-// SEM2D_MARCH=0 keeps the strip kernel.
-int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vector<int> &rec_ez,
-                const std::vector<int> &rec_jn, int force_cz) {
-  h->march = false;
-  const char *env = std::getenv("SEM2D_MARCH");
-  if (env && std::atoi(env) == 0) return SEM2D_OK;
-  if (h->st_nslot || h->ndir || h->nperio) return SEM2D_OK;  // Stacey, Dirichlet or periodic sides: the strip kernel
-  BulkConfig bc;
-  bc.N = h->N;
-  bc.ndof = h->ndof;
-  bc.mixed = h->mixed;
-  bc.fast = fast_path(h);
-  bc.mat_iso = h->mat_iso;
-  bc.mat_elem = h->mat_elem;
-  bc.pitch = h->pitch;
-  bc.plane = h->plane;
-  if (!march_supported(bc)) return SEM2D_OK;
-  if (const char *e = std::getenv("SEM2D_MARCH_STAGE")) h->march_stage = std::atoi(e) != 0;
-  if (const char *e = std::getenv("SEM2D_MARCH_WARPS")) h->march_warps = std::atoi(e);
-  if (const char *e = std::getenv("SEM2D_MARCH_PREFETCH")) h->march_pf = std::atoi(e) != 0;
-  bc.march_stage = h->march_stage;
-  bc.march_warps = h->march_warps;
-  // resident warps per SM; also sets the kernels' shared-memory limit
-  const int warps_per_sm = march_warps_per_sm(bc);
-  if (warps_per_sm <= 0) return set_err(h, SEM2D_E_CUDA, std::string("march kernel: ") + bulk_last_error());
-  int st;
-  if (h->nflt) {
-    // the fault kernel finishes the fault rows after the step: velocity or
-    // acceleration receivers there, and displacement ones when the Newmark
-    // corrector adds beta dt^2 a, are sampled after it, by the receiver
-    // kernel
-    const bool corrected = h->scheme == 2 || (h->scheme == 1 && h->beta != 0.0);
-    for (size_t r = 0; r < rec_jn.size(); ++r)
-      if ((h->rec_field != 'D' || corrected) && (rec_jn[r] == h->jf1 || rec_jn[r] == h->jf2))
-        h->rec_separate = true;
-    if ((st = dalloc(h, &h->d_fault_force, (size_t)2 * h->ndof * h->nflt))) return st;
-  }
+// frees a device buffer allocated with dalloc/dupload before destroy
+void dfree(sem2d_handle *h, void *p) {
+  if (!p) return;
+  cudaFree(p);
+  h->allocs.erase(std::remove(h->allocs.begin(), h->allocs.end(), p), h->allocs.end());
+}
+
+// Work units of the march kernel for chunk height cz (element rows): the
+// element rows reading a fault row (those touching one and the row above
+// them, which reads the upper fault row as its halo) are chunks of one row
+// each and come first, with no chunk boundary inside or right above them,
+// so that only the fault chunk reads fault rows; the others are cut every
+// cz rows.  Receivers sampled inside the kernel are grouped by unit.
+// Replaces the units of an earlier call.
+int build_march_units(sem2d_handle *h, int cz) {
   const int nstrips = (h->nx + kMarchColsHost - 1) / kMarchColsHost;
-  int cz = 0;
-  if (const char *e = std::getenv("SEM2D_MARCH_CZ")) cz = std::atoi(e);
-  if (cz <= 0) cz = force_cz;
-  if (cz <= 0) {
-    int dev = 0, nsm = 0;
-    CK(cudaGetDevice(&dev));
-    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    const long long target = 2LL * nsm * warps_per_sm;
-    cz = int(((long long)nstrips * h->nz + target - 1) / target);
-  }
   cz = std::max(1, std::min(cz, h->nz));
+  const std::vector<int> &rec_ex = h->march_rec_ex, &rec_ez = h->march_rec_ez;
   // element rows touching a fault row; no chunk boundary inside them or
   // right above them, so that only the fault chunk reads fault rows
   int t0 = h->nz, t1 = -1;
@@ -1441,17 +1409,81 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
       U[4] = cnt[u];
       U[5] = cnt[u + 1];
     }
-  int *du = nullptr;
+  dfree(h, h->d_march_units);
+  dfree(h, h->d_march_rec);
+  h->d_march_units = nullptr;
+  h->d_march_rec = nullptr;
+  int *du = nullptr, st;
   if ((st = dupload(h, &du, units)) || (st = dupload(h, &h->d_march_rec, ids))) return st;
   h->d_march_units = du;
   h->march_units_host = units;
   h->march_nunits = nu;
   h->march_cz = cz;
+  h->march_nstrips = nstrips;
+  h->march_nfch = nfch;
+  h->march_fault_units = nfch * nstrips;
+  return SEM2D_OK;
+}
+
+
+// Work units of the march kernel: strips of 31 element columns by chunks of
+// element rows.  The chunk height gives about two units per resident warp
+// (SEM2D_MARCH_CZ overrides it); a two-sided fault's rows stay in one chunk,
+// whose units come first (their FP64 fault work is the longest).
+// SEM2D_MARCH=0 keeps the strip kernel.
+int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vector<int> &rec_ez,
+                const std::vector<int> &rec_jn, int force_cz) {
+  h->march = false;
+  const char *env = std::getenv("SEM2D_MARCH");
+  if (env && std::atoi(env) == 0) return SEM2D_OK;
+  if (h->st_nslot || h->ndir || h->nperio) return SEM2D_OK;  // Stacey, Dirichlet or periodic sides: the strip kernel
+  BulkConfig bc;
+  bc.N = h->N;
+  bc.ndof = h->ndof;
+  bc.mixed = h->mixed;
+  bc.fast = fast_path(h);
+  bc.mat_iso = h->mat_iso;
+  bc.mat_elem = h->mat_elem;
+  bc.pitch = h->pitch;
+  bc.plane = h->plane;
+  if (!march_supported(bc)) return SEM2D_OK;
+  if (const char *e = std::getenv("SEM2D_MARCH_STAGE")) h->march_stage = std::atoi(e) != 0;
+  if (const char *e = std::getenv("SEM2D_MARCH_WARPS")) h->march_warps = std::atoi(e);
+  if (const char *e = std::getenv("SEM2D_MARCH_PREFETCH")) h->march_pf = std::atoi(e) != 0;
+  bc.march_stage = h->march_stage;
+  bc.march_warps = h->march_warps;
+  // resident warps per SM; also sets the kernels' shared-memory limit
+  const int warps_per_sm = march_warps_per_sm(bc);
+  if (warps_per_sm <= 0) return set_err(h, SEM2D_E_CUDA, std::string("march kernel: ") + bulk_last_error());
+  int st;
+  if (h->nflt) {
+    // the fault kernel finishes the fault rows after the step: velocity or
+    // acceleration receivers there, and displacement ones when the Newmark
+    // corrector adds beta dt^2 a, are sampled after it, by the receiver
+    // kernel
+    const bool corrected = h->scheme == 2 || (h->scheme == 1 && h->beta != 0.0);
+    for (size_t r = 0; r < rec_jn.size(); ++r)
+      if ((h->rec_field != 'D' || corrected) && (rec_jn[r] == h->jf1 || rec_jn[r] == h->jf2))
+        h->rec_separate = true;
+    if ((st = dalloc(h, &h->d_fault_force, (size_t)2 * h->ndof * h->nflt))) return st;
+  }
+  const int nstrips = (h->nx + kMarchColsHost - 1) / kMarchColsHost;
+  int cz = 0;
+  if (const char *e = std::getenv("SEM2D_MARCH_CZ")) cz = std::atoi(e);
+  if (cz <= 0) cz = force_cz;
+  if (cz <= 0) {
+    int dev = 0, nsm = 0;
+    CK(cudaGetDevice(&dev));
+    CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    const long long target = 2LL * nsm * warps_per_sm;
+    cz = int(((long long)nstrips * h->nz + target - 1) / target);
+  }
+  h->march_rec_ex = rec_ex;
+  h->march_rec_ez = rec_ez;
+  if ((st = build_march_units(h, cz))) return st;
   h->march = true;
+  const int nfch = h->march_nfch;
   if (nfch > 0) {
-    h->march_fault_units = nfch * nstrips;
-    h->march_nstrips = nstrips;
-    h->march_nfch = nfch;
     const char *fu = std::getenv("SEM2D_FUSED_FAULT");
     h->march_fused = nfch <= kMarchWarpsHost && h->friction != SEM2D_FRICTION_RSF && !(fu && std::atoi(fu) == 0);
     if ((st = dalloc(h, &h->d_step_c, 1)) || (st = dalloc(h, &h->d_done_c, 1))) return st;
@@ -1466,6 +1498,109 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
       CK(cudaEventCreateWithFlags(&h->ev_f, cudaEventDisableTiming));
     }
   }
+  return SEM2D_OK;
+}
+
+int build_batch_tables(sem2d_handle *h);
+
+// ---- the autotuner of the march kernels' launch shape ----------------
+// The first handle of a class of problems (dof count, material layout,
+// node count and member count to a power of two, SM count) times candidate
+// shapes -- chunk height, warps per CTA, L2 prefetch of the next element
+// row -- over a few steps with CUDA events, keeps the fastest (the analytic
+// default unless another is faster by more than 2 %) and records it in the
+// tuning cache (autotune.cpp); later handles of the class read it.  The
+// shapes give bitwise identical results (the per-node summation order does
+// not depend on them), and the state is reset after the trial steps.
+// SEM2D_AUTOTUNE=0, or any of SEM2D_MARCH_CZ / _WARPS / _PREFETCH / _STAGE,
+// keeps the analytic shape.
+struct MarchShape {
+  int cz, warps, pf;
+};
+
+bool tune_disabled() {
+  const char *t = std::getenv("SEM2D_AUTOTUNE");
+  if (t && std::atoi(t) == 0) return true;
+  for (const char *v : {"SEM2D_MARCH_CZ", "SEM2D_MARCH_WARPS", "SEM2D_MARCH_PREFETCH", "SEM2D_MARCH_STAGE"})
+    if (std::getenv(v)) return true;
+  return false;
+}
+
+int apply_shape(sem2d_handle *h, const MarchShape &s) {
+  int st;
+  std::vector<sem2d_handle *> probs = h->subs;
+  if (probs.empty()) probs.push_back(h);
+  for (sem2d_handle *m : probs) {
+    if (s.cz != m->march_cz && (st = build_march_units(m, s.cz))) return st;
+    m->march_warps = s.warps;
+    m->march_pf = s.pf;
+  }
+  if (!h->subs.empty() && (st = build_batch_tables(h))) return st;
+  h->march_warps = s.warps;
+  h->march_pf = s.pf;
+  if (h->graph_exec) {  // a captured graph holds the old units
+    cudaGraphExecDestroy(h->graph_exec);
+    h->graph_exec = nullptr;
+  }
+  return SEM2D_OK;
+}
+
+// milliseconds per step of n steps after nwarm warm-up steps (direct launches)
+int time_shape(sem2d_handle *h, int nwarm, int n, double *ms) {
+  int st;
+  if ((st = launch_steps(h, nwarm))) return st;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, h->stream));
+  st = launch_steps(h, n);
+  CK(cudaEventRecord(e1, h->stream));
+  CK(cudaEventSynchronize(e1));
+  float t = 0.f;
+  cudaEventElapsedTime(&t, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *ms = double(t) / n;
+  return st;
+}
+
+int tune_march(sem2d_handle *h) {
+  if (!h->march || tune_disabled()) return SEM2D_OK;
+  const sem2d_handle *a = h->subs.empty() ? h : h->subs[0];
+  long long nodes = 0;
+  if (h->subs.empty()) nodes = h->npoin;
+  for (const sem2d_handle *m : h->subs) nodes += m->npoin;
+  int dev = 0, nsm = 1;
+  CK(cudaGetDevice(&dev));
+  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  char key[160], path[1024];
+  if (sem2d_tune_key(a->ndof, a->mat_elem, nodes, int(h->subs.size()), nsm, key, sizeof(key)) != SEM2D_OK)
+    return SEM2D_OK;
+  const bool have_path = sem2d_tune_cache_path(path, sizeof(path)) == SEM2D_OK;
+  sem2d_tune_entry e;
+  if (have_path && sem2d_tune_lookup(path, key, &e) == 1) {
+    h->tune_source = 2;
+    return apply_shape(h, MarchShape{e.chunk_rows, e.warps_per_cta, e.l2_prefetch});
+  }
+  const int nwarm = 2, n = std::min(32, h->nt - nwarm);
+  if (n < 4) return SEM2D_OK;  // too few steps to time: the analytic shape
+  const int cz0 = a->march_cz;
+  const MarchShape cands[] = {{cz0, a->march_warps, 0}, {cz0, 1, 0}, {2 * cz0, a->march_warps, 0},
+                              {std::max(1, cz0 / 2), a->march_warps, 0}, {cz0, a->march_warps, 1}};
+  const int nc = int(sizeof(cands) / sizeof(cands[0]));
+  std::vector<sem2d_tune_entry> res(nc);
+  const long long l0 = h->launches;
+  int st;
+  for (int k = 0; k < nc; ++k) {
+    double ms = 0;
+    if ((st = apply_shape(h, cands[k])) || (st = time_shape(h, nwarm, n, &ms)) || (st = reset_state(h))) return st;
+    res[k] = sem2d_tune_entry{std::max(1, std::min(cands[k].cz, a->nz)), cands[k].warps, cands[k].pf, 0, ms};
+  }
+  const int best = sem2d_tune_select(res.data(), nc, 0.02);
+  if ((st = apply_shape(h, cands[best]))) return st;
+  h->launches = l0;
+  h->tune_source = 1;
+  if (have_path) sem2d_tune_record(path, key, &res[best]);  // a cache that cannot be written is not an error
   return SEM2D_OK;
 }
 
@@ -1703,6 +1838,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
   }
   if ((st = setup_march(h, rec_ex, rec_ez, rec_jn, force_tz))) return st;
   if ((st = reset_state(h))) return st;
+  if (!shared && (st = tune_march(h))) return st;  // batch members are tuned with their batch
   CK(cudaStreamSynchronize(h->stream));
   return SEM2D_OK;
 }
@@ -1744,6 +1880,52 @@ int batch_add_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
   return SEM2D_OK;
 }
 
+// The parameter blocks of every member of a batch for both buffer
+// parities and the batch's list of march units (member by member); replaces
+// those of an earlier call (the tuner rebuilds them for each shape).
+int build_batch_tables(sem2d_handle *h) {
+  const int nsim = int(h->subs.size());
+  int st;
+  const size_t pb = params_bytes(h->N, h->mixed);
+  for (int cur = 0; cur < 2; ++cur) {
+    std::vector<unsigned char> blk(pb * nsim);
+    for (int i = 0; i < nsim; ++i) {
+      sem2d_handle *m = h->subs[i];
+      if (h->mixed) {
+        FaultParams<float> f;
+        BulkConfig bc = make_config<float>(m, cur, f);
+        if (h->march) bc.rec_ids = m->nrec ? m->d_march_rec : nullptr;
+        fill_params_block(bc, blk.data() + pb * i);
+      } else {
+        FaultParams<double> f;
+        BulkConfig bc = make_config<double>(m, cur, f);
+        fill_params_block(bc, blk.data() + pb * i);
+      }
+    }
+    dfree(h, h->d_params[cur]);
+    h->d_params[cur] = nullptr;
+    if ((st = dupload(h, reinterpret_cast<unsigned char **>(&h->d_params[cur]), blk))) return st;
+  }
+  if (h->march) {
+    std::vector<int> mu;
+    for (int i = 0; i < nsim; ++i) {
+      const std::vector<int> &src = h->subs[i]->march_units_host;
+      for (size_t k = 0; k < src.size(); k += kMarchUnitInts) {
+        mu.insert(mu.end(), src.begin() + k, src.begin() + k + kMarchUnitInts);
+        mu[mu.size() - kMarchUnitInts] = i;
+      }
+    }
+    h->march_nunits = int(mu.size() / kMarchUnitInts);
+    dfree(h, h->d_march_units);
+    h->d_march_units = nullptr;
+    int *du = nullptr;
+    if ((st = dupload(h, &du, mu))) return st;
+    h->d_march_units = du;
+    h->march_cz = h->subs[0]->march_cz;
+  }
+  return SEM2D_OK;
+}
+
 int batch_close_impl(sem2d_handle *h) {
   const int nsim = int(h->subs.size());
   if (nsim <= 0) return set_err(h, SEM2D_E_ARG, "empty batch");
@@ -1777,26 +1959,8 @@ int batch_close_impl(sem2d_handle *h) {
   if ((st = dalloc(h, &h->d_step, 1)) || (st = dalloc(h, &h->d_error, 1)) || (st = dalloc(h, &h->d_done, 1)) ||
       (st = dalloc(h, &h->d_info, 2)))
     return st;
-  // parameter blocks of every member for both buffer parities
-  const size_t pb = params_bytes(h->N, h->mixed);
-  for (int cur = 0; cur < 2; ++cur) {
-    std::vector<unsigned char> blk(pb * nsim);
-    for (int i = 0; i < nsim; ++i) {
-      sem2d_handle *m = h->subs[i];
-      if (h->mixed) {
-        FaultParams<float> f;
-        BulkConfig bc = make_config<float>(m, cur, f);
-        if (h->march) bc.rec_ids = m->nrec ? m->d_march_rec : nullptr;
-        fill_params_block(bc, blk.data() + pb * i);
-      } else {
-        FaultParams<double> f;
-        BulkConfig bc = make_config<double>(m, cur, f);
-        fill_params_block(bc, blk.data() + pb * i);
-      }
-    }
-    if ((st = dupload(h, reinterpret_cast<unsigned char **>(&h->d_params[cur]), blk))) return st;
-  }
-  // work units, member by member
+  if ((st = build_batch_tables(h))) return st;
+  // work units of the strip kernel, member by member
   std::vector<int> units;
   for (int i = 0; i < nsim; ++i) {
     const sem2d_handle *m = h->subs[i];
@@ -1808,21 +1972,6 @@ int batch_close_impl(sem2d_handle *h) {
   }
   h->nunits = int(units.size() / 4);
   if ((st = dupload(h, reinterpret_cast<int **>(&h->d_units), units))) return st;
-  if (h->march) {
-    std::vector<int> mu;
-    for (int i = 0; i < nsim; ++i) {
-      const std::vector<int> &src = h->subs[i]->march_units_host;
-      for (size_t k = 0; k < src.size(); k += kMarchUnitInts) {
-        mu.insert(mu.end(), src.begin() + k, src.begin() + k + kMarchUnitInts);
-        mu[mu.size() - kMarchUnitInts] = i;
-      }
-    }
-    h->march_nunits = int(mu.size() / kMarchUnitInts);
-    int *du = nullptr;
-    if ((st = dupload(h, &du, mu))) return st;
-    h->d_march_units = du;
-    h->march_cz = a->march_cz;
-  }
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
@@ -1840,6 +1989,7 @@ int batch_close_impl(sem2d_handle *h) {
   CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   h->batch_grid = std::min(h->nunits, per_sm * nsm);
   if ((st = reset_state(h))) return st;
+  if ((st = tune_march(h))) return st;
   CK(cudaStreamSynchronize(h->stream));
   h->batch_open = false;
   return SEM2D_OK;
