@@ -217,8 +217,6 @@ int sem2d_abi_field_offsets(int which, long long *offsets, int n);
 typedef struct sem2d_tune_entry {
   int chunk_rows;     /* element rows per work unit                       */
   int warps_per_cta;  /* 1, 2 or 4                                        */
-  int l2_prefetch;    /* 1: the next element row is prefetched into L2    */
-  int staged;         /* 1: rows staged through shared memory (cp.async)  */
   double ms_per_step; /* measured                                         */
 } sem2d_tune_entry;
 /* The cache path into buf (n bytes); returns 0, or the bytes needed when

@@ -159,8 +159,7 @@ class Deck(C.Structure):
 
 class TuneEntry(C.Structure):
     """sem2d_tune_entry: a launch shape of the march kernels and its time."""
-    _fields_ = [("chunk_rows", c_int), ("warps_per_cta", c_int), ("l2_prefetch", c_int), ("staged", c_int),
-                ("ms_per_step", c_double)]
+    _fields_ = [("chunk_rows", c_int), ("warps_per_cta", c_int), ("ms_per_step", c_double)]
 
 
 class LatticeArgs(C.Structure):

@@ -8,7 +8,7 @@
 //
 // The cache is a text file of JSON objects, one per line:
 //   {"key": "march ndof=2 mat=2 nodes=2^28 members=2^8 sm=152", "chunk_rows": 32,
-//    "warps_per_cta": 1, "l2_prefetch": 1, "staged": 0, "ms_per_step": 4.52}
+//    "warps_per_cta": 1, "ms_per_step": 4.52}
 // A later line with the same key replaces an earlier one.  Writes go to a
 // temporary file renamed over the cache, so readers never see half a file.
 #include <cerrno>
@@ -47,14 +47,12 @@ bool key_of(const std::string &line, std::string *key) {
 }
 
 bool parse_entry(const std::string &line, std::string *key, sem2d_tune_entry *e) {
-  double cz, w, pf, st, ms;
+  double cz, w, ms;
   if (!key_of(line, key) || !field(line, "chunk_rows", &cz) || !field(line, "warps_per_cta", &w) ||
-      !field(line, "l2_prefetch", &pf) || !field(line, "staged", &st) || !field(line, "ms_per_step", &ms))
+      !field(line, "ms_per_step", &ms))
     return false;
   e->chunk_rows = int(cz);
   e->warps_per_cta = int(w);
-  e->l2_prefetch = int(pf);
-  e->staged = int(st);
   e->ms_per_step = ms;
   return e->chunk_rows > 0 && (e->warps_per_cta == 1 || e->warps_per_cta == 2 || e->warps_per_cta == 4);
 }
@@ -135,10 +133,8 @@ int sem2d_tune_record(const char *path, const char *key, const sem2d_tune_entry 
   if (!f) return SEM2D_E_STATE;
   for (const auto &kv : all)
     std::fprintf(f,
-                 "{\"key\": \"%s\", \"chunk_rows\": %d, \"warps_per_cta\": %d, \"l2_prefetch\": %d, \"staged\": %d, "
-                 "\"ms_per_step\": %.6g}\n",
-                 kv.first.c_str(), kv.second.chunk_rows, kv.second.warps_per_cta, kv.second.l2_prefetch,
-                 kv.second.staged, kv.second.ms_per_step);
+                 "{\"key\": \"%s\", \"chunk_rows\": %d, \"warps_per_cta\": %d, \"ms_per_step\": %.6g}\n",
+                 kv.first.c_str(), kv.second.chunk_rows, kv.second.warps_per_cta, kv.second.ms_per_step);
   const bool ok = std::fclose(f) == 0;
   if (!ok || std::rename(tmp.c_str(), p.c_str()) != 0) {
     std::remove(tmp.c_str());

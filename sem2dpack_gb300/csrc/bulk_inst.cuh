@@ -25,12 +25,15 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.ztile = c.ztile;
   for (int k = 0; k < N * N; ++k) p.H[k] = real(c.H[k]);
   for (int k = 0; k < N; ++k) p.w[k] = real(c.w[k]);
+  for (int k = 0; k < N * N; ++k) p.Hw[k] = real(c.H[k] * c.w[k / N]);
   p.Dcur = static_cast<const real *>(c.Dcur);
   p.Dnext = static_cast<real *>(c.Dnext);
   p.Vcur = static_cast<const real *>(c.Vcur);
   p.Vnext = static_cast<real *>(c.Vnext);
   p.Acur = static_cast<const real *>(c.Acur);
   p.Anext = static_cast<real *>(c.Anext);
+  p.Fcur = static_cast<const real *>(c.Fcur);
+  p.Fnext = static_cast<real *>(c.Fnext);
   p.mat_iso = c.mat_iso;
   for (int m = 0; m < 4; ++m) p.mat[m] = static_cast<const real *>(c.mat[m]);
   p.mat_elem = c.mat_elem;
@@ -84,7 +87,6 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.nplanes = c.nplanes;
   p.error = c.error;
   p.spin_limit = c.spin_limit;
-  p.march_pf = c.march_pf;
   p.chunk_shift = c.chunk_shift;
 }
 

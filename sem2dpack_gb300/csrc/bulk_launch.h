@@ -28,6 +28,7 @@ struct BulkConfig {
   const double *H = nullptr, *w = nullptr;  // host arrays
   void *Dcur = nullptr, *Dnext = nullptr, *Vcur = nullptr, *Vnext = nullptr;
   void *Acur = nullptr, *Anext = nullptr;
+  void *Fcur = nullptr, *Fnext = nullptr;  // force state planes (march kernel)
   void *mat[4] = {nullptr, nullptr, nullptr, nullptr};
   void *kveta = nullptr, *rmass = nullptr;
   void *geo[4] = {nullptr, nullptr, nullptr, nullptr};  // xix, etaz, dxdxi, dzdeta
@@ -57,9 +58,8 @@ struct BulkConfig {
   int *error = nullptr;  // device error flag
   int spin_limit = 1 << 22;  // polls of a stage's mbarrier before giving up
   int chunk_shift = 0;   // chunk scheduled first (the fault's)
-  int march_stage = 1;   // march kernels: rows staged through shared memory (1) or loaded directly (0)
   int march_warps = 4;   // march kernels: warps per CTA (1, 2 or 4)
-  int march_pf = 0;      // march kernels, direct loads: L2 prefetch of the next element row
+  int march_fst = 0;     // march kernels: force state (1) or displacement state (0)
   cudaStream_t stream = nullptr;
 };
 

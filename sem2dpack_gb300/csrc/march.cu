@@ -17,35 +17,17 @@ namespace {
 constexpr int kThreads = 32 * kMarchWarps;
 static_assert(kMarchWarpsHost == kMarchWarps, "host and device CTA shapes");
 
-// warps per CTA of a launch (1, 2 or 4) and the shared memory it needs
+// warps per CTA of a launch (1, 2 or 4)
 int cta_warps(const BulkConfig &c) { return c.march_warps == 1 || c.march_warps == 2 ? c.march_warps : kMarchWarps; }
-template <int NDOF, int MAT, bool STG>
-constexpr size_t ring_bytes(int warps = kMarchWarps) {
-  return STG ? warps * MarchStage<NDOF, MAT>::kWarpBytes : 0;
-}
 
-template <int NDOF, int MAT, bool STG>
-int configure_typed() {
-  cudaError_t e = cudaFuncSetAttribute(march_step_kernel<NDOF, MAT, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(ring_bytes<NDOF, MAT, STG>()));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(march_batch_kernel<NDOF, MAT, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(ring_bytes<NDOF, MAT, STG>()));
-  if (e != cudaSuccess) {
-    g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
-    return 1;
-  }
-  return 0;
-}
-
-template <int NDOF, int MAT, bool STG>
+template <int NDOF, int MAT, bool FST>
 int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
   const int wpc = cta_warps(c);
   const int grid = std::max(1, (m.nunits + wpc - 1) / wpc);  // an empty set still counts the step
-  march_step_kernel<NDOF, MAT, STG><<<grid, 32 * wpc, ring_bytes<NDOF, MAT, STG>(wpc), c.stream>>>(
-      p, static_cast<const MarchUnit *>(m.units), m.nunits);
+  march_step_kernel<NDOF, MAT, FST><<<grid, 32 * wpc, 0, c.stream>>>(p, static_cast<const MarchUnit *>(m.units),
+                                                                      m.nunits);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -54,11 +36,12 @@ int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   return 0;
 }
 
-template <int NDOF, int MAT, bool STG>
+template <int NDOF, int MAT, bool FST>
 int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   MarchBatch b{};
   for (int k = 0; k < 25; ++k) b.H[k] = float(c.H[k]);
   for (int k = 0; k < 5; ++k) b.w[k] = float(c.w[k]);
+  for (int k = 0; k < 25; ++k) b.Hw[k] = float(c.H[k] * c.w[k / 5]);
   b.sims = static_cast<const BulkParams<float, 5> *>(m.sims);
   b.units = static_cast<const MarchUnit *>(m.units);
   b.nunits = m.nunits;
@@ -66,7 +49,7 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   b.done = m.done;
   const int wpc = cta_warps(c);
   const int grid = std::max(1, (m.nunits + wpc - 1) / wpc);  // an empty set still counts the step
-  march_batch_kernel<NDOF, MAT, STG><<<grid, 32 * wpc, ring_bytes<NDOF, MAT, STG>(wpc), c.stream>>>(b);
+  march_batch_kernel<NDOF, MAT><<<grid, 32 * wpc, 0, c.stream>>>(b);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -75,20 +58,33 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   return 0;
 }
 
-template <int NDOF, int MAT, bool STG>
+template <int NDOF, int MAT, bool FST>
+int launch_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
+  BulkParams<float, 5> p;
+  fill_params<float, 5>(c, p);
+  march_fault_side_kernel<NDOF, MAT, FST><<<nstrips, kThreads, 0, c.stream>>>(
+      p, static_cast<const MarchUnit *>(m.units), nstrips, nrows);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_bulk_err = cudaGetErrorString(e);
+    return 1;
+  }
+  return 0;
+}
+
+template <int NDOF, int MAT, bool FST>
 int occupancy_one(int wpc) {
   int nb = 0;
-  if (configure_typed<NDOF, MAT, STG>()) return 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, STG>, 32 * wpc,
-                                                    ring_bytes<NDOF, MAT, STG>(wpc)) != cudaSuccess)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, FST>, 32 * wpc, 0) !=
+      cudaSuccess)
     return 0;
   return nb * wpc;
 }
 
-// the instantiation for (ndof, material layout, staging) of c
+// the instantiation for (ndof, material layout, state formulation) of c
 template <template <int, int, bool> class F, typename... A>
 int dispatch(const BulkConfig &c, A &&...a) {
-  const bool s = c.march_stage != 0;
+  const bool s = c.march_fst != 0;
   if (c.ndof == 1) {
     if (c.mat_elem == kMatNode) return s ? F<1, kMatNode, true>::run(a...) : F<1, kMatNode, false>::run(a...);
     return s ? F<1, kMatElement, true>::run(a...) : F<1, kMatElement, false>::run(a...);
@@ -96,17 +92,23 @@ int dispatch(const BulkConfig &c, A &&...a) {
   if (c.mat_elem == kMatNode) return s ? F<2, kMatNode, true>::run(a...) : F<2, kMatNode, false>::run(a...);
   return s ? F<2, kMatElement, true>::run(a...) : F<2, kMatElement, false>::run(a...);
 }
-template <int NDOF, int MAT, bool STG>
+template <int NDOF, int MAT, bool FST>
 struct LaunchOne {
-  static int run(const BulkConfig &c, const MarchLaunch &m) { return launch_one<NDOF, MAT, STG>(c, m); }
+  static int run(const BulkConfig &c, const MarchLaunch &m) { return launch_one<NDOF, MAT, FST>(c, m); }
 };
-template <int NDOF, int MAT, bool STG>
+template <int NDOF, int MAT, bool FST>
 struct LaunchMany {
-  static int run(const BulkConfig &c, const MarchLaunch &m) { return launch_many<NDOF, MAT, STG>(c, m); }
+  static int run(const BulkConfig &c, const MarchLaunch &m) { return launch_many<NDOF, MAT, FST>(c, m); }
 };
-template <int NDOF, int MAT, bool STG>
+template <int NDOF, int MAT, bool FST>
+struct LaunchSide {
+  static int run(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
+    return launch_side<NDOF, MAT, FST>(c, m, nstrips, nrows);
+  }
+};
+template <int NDOF, int MAT, bool FST>
 struct Occupancy {
-  static int run(int wpc) { return occupancy_one<NDOF, MAT, STG>(wpc); }
+  static int run(int wpc) { return occupancy_one<NDOF, MAT, FST>(wpc); }
 };
 
 }  // namespace
@@ -118,25 +120,14 @@ bool march_supported(const BulkConfig &c) {
 
 int launch_march(const BulkConfig &c, const MarchLaunch &m) { return dispatch<LaunchOne>(c, c, m); }
 
-int launch_march_batch(const BulkConfig &c, const MarchLaunch &m) { return dispatch<LaunchMany>(c, c, m); }
+int launch_march_batch(const BulkConfig &c, const MarchLaunch &m) {
+  BulkConfig b = c;
+  b.march_fst = 0;  // batches hold no fault: the displacement state
+  return dispatch<LaunchMany>(b, b, m);
+}
 
 int launch_march_fault_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
-  BulkParams<float, 5> p;
-  fill_params<float, 5>(c, p);
-  const MarchUnit *u = static_cast<const MarchUnit *>(m.units);
-  if (c.ndof == 1) {
-    if (c.mat_elem == kMatNode) march_fault_side_kernel<1, kMatNode><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
-    else march_fault_side_kernel<1, kMatElement><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
-  } else {
-    if (c.mat_elem == kMatNode) march_fault_side_kernel<2, kMatNode><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
-    else march_fault_side_kernel<2, kMatElement><<<nstrips, kThreads, 0, c.stream>>>(p, u, nstrips, nrows);
-  }
-  const cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) {
-    g_bulk_err = cudaGetErrorString(e);
-    return 1;
-  }
-  return 0;
+  return dispatch<LaunchSide>(c, c, m, nstrips, nrows);
 }
 
 int launch_march_fault(const BulkConfig &c) {

@@ -27,23 +27,28 @@
 // element before right, so both kernels assemble identically.
 //
 // Memory.  A lane reads the 4 node columns it owns of each node row as one
-// 16-byte piece (the warp reads 512 contiguous bytes) and gets the fifth
+// 16-byte load (the warp reads 512 contiguous bytes) and gets the fifth
 // column from the next lane; fields, inverse mass and node material are
-// read this way, written the same way.  Two variants move the rows:
-//  * direct (STG = false): 16-byte global loads; the latency of a row's
-//    loads is covered by the other resident warps only;
-//  * staged (STG = true): each warp owns a ring of 10 node-row slots in
-//    shared memory.  The rows of element row ez+1 (displacement, velocity,
-//    inverse mass, and for SH the node material) are copied in by
-//    cp.async (16 bytes per lane, one commit group per element row) while
-//    element row ez computes, so the element and node-update phases read
-//    shared memory only; the warp waits for a group with cp.async.wait_group,
-//    a hardware wait on its own copies (no polling).  Slot of node row J:
-//    J mod 10, enough for the rows of two consecutive element rows, a fault
-//    split included; a slot is refilled only after the element row that
-//    read it has finished (a __syncwarp orders the lanes).
-// Both variants do the same arithmetic in the same order: their results are
-// bitwise identical.
+// read this way, written the same way.  Nothing is staged: the latency of
+// a row's loads is covered by the other resident warps.
+//
+// State.  Two formulations of the leapfrog state (FST):
+//  * displacement state (FST = false): the element pass applies the
+//    stiffness to the displacement predictor d, f = -K d, as the reference
+//    does (solver.f90:140-161);
+//  * force state (FST = true, problems with a fault): the elastic force is
+//    carried from step to step, f_el(n) = f_el(n-1) + dt (-K v), and the
+//    element pass applies the stiffness to the velocity.  The two agree in
+//    exact arithmetic (K is linear and d(n) = d(n-1) + dt v).  In FP32 the
+//    displacement next to a fault that has slipped metres is quantised to
+//    its ulp (5e-7 m at 5 m), which is the size of the node-to-node
+//    differences that carry the dynamic stress: its stiffness products
+//    lose about 3 digits and the slip rate and seismograms drift from the
+//    FP64 result by parts per thousand over thousands of steps.  The
+//    velocity and the net elastic force carry no static offset, so they
+//    keep FP32's relative precision.  The displacement is still integrated
+//    (d += dt v) for the outputs; the force state costs one more plane
+//    read and written per dof.
 //
 // Fault.  The complete forces of the split node rows jf1 (top of the
 // elements below the fault) and jf2 (bottom of the elements above),
@@ -69,46 +74,11 @@ constexpr int kMarchWarps = 4;     // warps per CTA at most (the launch picks 1,
 constexpr int kMarchCols = 31;     // element columns owned by a warp
 // resident CTAs per SM the register budget allows: 102 registers per
 // thread for SH (20 warps per SM), 168 for P-SV (12 warps; fewer registers
-// spill the node-material variant).  The staged variant is bounded by its
-// shared memory instead (see MarchStage): 3 CTAs per SM for SH, 2 for P-SV.
-template <int NDOF, bool STG = false>
+// spill the node-material variant)
+template <int NDOF>
 struct MarchOcc {
-  static constexpr int kMinBlocks = STG ? (NDOF == 1 ? 3 : 2) : (NDOF == 1 ? 5 : 3);
+  static constexpr int kMinBlocks = NDOF == 1 ? 5 : 3;
 };
-
-// Staging ring of one warp: kRingSlots node-row slots, each holding the
-// staged fields of one lattice row over the warp's 132 columns (33 pieces
-// of 16 bytes: lane k's 4 columns, and the column right of lane 31)
-constexpr int kRingSlots = 10;
-constexpr int kRowF = 132;  // floats per staged field row
-template <int NDOF, int MAT>
-struct MarchStage {
-  // node material is staged for SH only (P-SV: two more planes would halve
-  // the resident warps; its rows are read from global memory)
-  static constexpr bool kStageMat = MAT == kMatNode && NDOF == 1;
-  // fields of a slot: displacement c, velocity c, inverse mass, material
-  static constexpr int kD = 0, kV = NDOF, kRm = 2 * NDOF, kM = 2 * NDOF + 1;
-  static constexpr int kFields = 2 * NDOF + 1 + (kStageMat ? NDOF : 0);
-  static constexpr int kSlot = kFields * kRowF;
-  static constexpr int kWarpFloats = kRingSlots * kSlot;
-  static constexpr size_t kWarpBytes = size_t(kWarpFloats) * sizeof(float);
-};
-
-__device__ __forceinline__ void cp_async16(float *dst, const float *src) {
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(dst))),
-               "l"(src)
-               : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-// asks the TMA engine to bring `bytes` (a multiple of 16) at a 16-byte
-// aligned address into L2; no completion to wait for
-__device__ __forceinline__ void prefetch_l2(const float *src, uint32_t bytes) {
-  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
-}
-template <int K>
-__device__ __forceinline__ void cp_async_wait() {
-  asm volatile("cp.async.wait_group %0;" ::"n"(K) : "memory");
-}
 
 // one unit of work: a strip of element columns and a chunk of element rows
 // of one problem, with its receivers rec_ids[rec0 .. rec1)
@@ -118,6 +88,7 @@ struct MarchUnit {
 
 struct MarchBatch {
   float H[25], w[5];                 // GLL operator (the same for every problem)
+  float Hw[25];                      // Hw[i + 5q] = H[i + 5q] w[q]
   const BulkParams<float, 5> *sims;  // per problem
   const MarchUnit *units;
   int nunits;
@@ -127,11 +98,10 @@ struct MarchBatch {
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-// one unit of one problem (ring: this warp's staging slots when STG)
-template <int NDOF, int MAT, bool STG = false>
+// one unit of one problem (FST: the force-state formulation)
+template <int NDOF, int MAT, bool FST>
 __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const float *H, const float *w,
-                                           const MarchUnit &u, int it, float *ring = nullptr) {
-  using Stg = MarchStage<NDOF, MAT>;
+                                           const float *Hw, const MarchUnit &u, int it) {
   constexpr int N = 5;
   const int lane = threadIdx.x & 31;
   const int ex = kMarchCols * u.strip - 1 + lane;
@@ -153,60 +123,15 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   float *__restrict__ Vn = p.Vnext;
   float *__restrict__ Dn = p.Dnext;
   float *__restrict__ An = p.Anext;
+  // force state: the elastic force of the step before, and of this step
+  const float *__restrict__ Fc = p.Fcur;
+  float *__restrict__ Fn = p.Fnext;
+  // the field the stiffness is applied to
+  const float *__restrict__ Ue = FST ? p.Vcur : p.Dcur;
 
   // first element row walked: one below the chunk when they share nodes
   int zs = u.z0;
   if (u.z0 > 0 && p.row0[u.z0] == p.row0[u.z0 - 1] + (N - 1)) zs = u.z0 - 1;
-
-  // staging: lane k's piece of a node row starts at column cs + 4k (I0 for
-  // the lanes that load), lane 31 also copies the piece at cs + 128; pieces
-  // outside the row (left of strip 0, right of the pitch) are not copied
-  // and never read
-  const int cs = 4 * (kMarchCols * u.strip - 1);
-  const bool pc_ok = cs + 4 * lane >= 0 && cs + 4 * lane < p.pitch;
-  const bool pc32_ok = lane == 31 && cs + 128 < p.pitch;
-  auto slot_of = [&](int J) -> float * { return ring + (J % kRingSlots) * Stg::kSlot; };
-  auto stage_row = [&](int J) {
-    float *sl = slot_of(J);
-    const long long ro = (long long)J * p.pitch + cs;
-#pragma unroll
-    for (int f = 0; f < Stg::kFields; ++f) {
-      const float *b = f < NDOF           ? p.Dcur + f * pl
-                       : f < 2 * NDOF     ? p.Vcur + (f - NDOF) * pl
-                       : f == 2 * NDOF    ? p.rmass
-                                          : p.mat[f - 2 * NDOF - 1];
-      if (pc_ok) cp_async16(sl + f * kRowF + 4 * lane, b + ro + 4 * lane);
-      if (pc32_ok) cp_async16(sl + f * kRowF + 128, b + ro + 128);
-    }
-  };
-  // the node rows of element row ezn not staged with the row below it
-  auto stage_elem_row = [&](int ezn, bool first) {
-    const int Ja = p.row0[ezn];
-    const int j0 = (!first && Ja == p.row0[ezn - 1] + (N - 1)) ? 1 : 0;
-    for (int j = j0; j < N; ++j) stage_row(Ja + j);
-  };
-  if constexpr (STG) {
-    stage_elem_row(zs, true);
-    cp_async_commit();
-    if (zs + 1 < u.z1) stage_elem_row(zs + 1, false);
-    cp_async_commit();
-  }
-  // direct loads with p.march_pf: the rows of element row ezn (fields as
-  // staged, plus the node material) are prefetched into L2, one bulk
-  // prefetch of the warp's row segment per lane, while the row below computes
-  constexpr int kPfFields = 2 * NDOF + 1 + (MAT == kMatNode ? NDOF : 0);
-  auto prefetch_elem_row = [&](int ezn) {
-    const int Ja = p.row0[ezn];
-    const int c0 = cs < 0 ? 0 : cs, c1 = cs + 132 < p.pitch ? cs + 132 : p.pitch;
-    for (int q = lane; q < N * kPfFields; q += 32) {
-      const int j = q / kPfFields, f = q - j * kPfFields;
-      const float *b = f < NDOF           ? p.Dcur + f * pl
-                       : f < 2 * NDOF     ? p.Vcur + (f - NDOF) * pl
-                       : f == 2 * NDOF    ? p.rmass
-                                          : p.mat[f - 2 * NDOF - 1];
-      if (c1 > c0) prefetch_l2(b + (long long)(Ja + j) * p.pitch + c0, uint32_t(c1 - c0) * 4u);
-    }
-  };
 
   float carry[NDOF][N];  // forces on the node row shared with the next element row
 #pragma unroll
@@ -215,49 +140,35 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     for (int i = 0; i < N; ++i) carry[c][i] = 0.f;
   bool have_carry = false;
 
-  // the displacement rows of the next element row are requested while the
-  // current row's nodes are updated: 16-byte parts here, the fifth column
+  // the rows of the next element row are requested while the current
+  // row's nodes are updated: 16-byte parts here, the fifth column
   // (shuffled or, for lane 31, loaded) when the row starts
   // (P-SV: requested at the row start instead; carrying them through the
   // node update costs more registers than P-SV has)
-  // (staged: read from the ring when the row starts)
-  constexpr bool kPrefetch = NDOF == 1 && !STG;
+  constexpr bool kPrefetch = NDOF == 1;
   float4 nq[NDOF][N];
   float n5[NDOF][N];
   auto fetch_u = [&](int ezn) {
-    const int Ja = p.row0[ezn];
-    const long long o = (long long)Ja * p.pitch;
+    const long long o = (long long)p.row0[ezn] * p.pitch;
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
 #pragma unroll
       for (int j = 0; j < N; ++j) {
-        if constexpr (STG) {
-          const float *sr = slot_of(Ja + j) + (Stg::kD + c) * kRowF;
-          nq[c][j] = ld ? *reinterpret_cast<const float4 *>(sr + 4 * lane) : make_float4(0.f, 0.f, 0.f, 0.f);
-          n5[c][j] = (lane == 31 && act) ? sr[128] : 0.f;
-        } else {
-          const float *b = p.Dcur + c * pl + o + (long long)j * p.pitch + I0;
-          nq[c][j] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
-          n5[c][j] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
-        }
+        const float *b = Ue + c * pl + o + (long long)j * p.pitch + I0;
+        nq[c][j] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
+        n5[c][j] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
       }
   };
   if (kPrefetch) fetch_u(zs);
 
   for (int ez = zs; ez < u.z1; ++ez) {
-    if constexpr (STG) {
-      cp_async_wait<1>();  // this element row's group has landed
-      __syncwarp();        // and the other lanes' pieces are visible
-    } else {
-      if (p.march_pf && ez + 1 < u.z1) prefetch_elem_row(ez + 1);
-    }
     const bool halo = ez < u.z0;
     const int J0 = p.row0[ez];
     const float etaz = act ? p.etaz[ez] : 0.f;
     const float det = dxdxi * (act ? p.dzdeta[ez] : 0.f);
     const long long eidx = (long long)ez * p.nx + (ex < 0 ? 0 : ex);
 
-    // ---- element forces: A holds u, then d/deta; B holds d/dxi ----
+    // ---- element forces: A holds u (d, or v with FST), then d/deta; B holds d/dxi ----
     float A[NDOF][N][N], B[NDOF][N][N];
     if (!kPrefetch) fetch_u(ez);
 #pragma unroll
@@ -299,13 +210,23 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
 #pragma unroll
         for (int j = 0; j < N; ++j) A[c][j][i] = t[j];
       }
-    // stress terms at every point: column part (weights -W xix) into B,
-    // row part (weights -W etaz) into A
+    // stress terms at every point: column part into B, row part into A.
+    // The GLL weight of the contracted index is in the Hw table of the
+    // divergence below, so B(i,j) carries the weight w_j of its row and
+    // A(i,j) the weight w_i of its column: with det = dx/dxi dz/deta,
+    //   B = -det w_j xix (stress . x),  A = -det w_i etaz (stress . z)
+    // (the a-coefficients of MAT_ELAST_init_a, mat_elastic.f90:323-358,
+    // factored); per element the moduli are folded into four coefficients.
     float em0 = 0.f, em1 = 0.f;
     if (MAT == kMatElement && act) {
       em0 = p.mat[0][eidx];
       if (NDOF == 2) em1 = p.mat[1][eidx];
     }
+    const float sxz = kd2 ? etaz : xix;  // KD2 uses a4 for both shear derivatives
+    // element material: mu xix, mu etaz, mu sxz, la xix, la etaz, K xix, K etaz
+    const float eK = em0 + 2.f * em1;
+    const float cMx = em1 * xix, cMz = em1 * etaz, cMs = em1 * sxz;
+    const float cLx = em0 * xix, cLz = em0 * etaz, cKx = eK * xix, cKz = eK * etaz;
     // node material: the 16-byte parts of row j+1 are requested before row
     // j is used
     float4 mq[2][2];
@@ -314,15 +235,9 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
       if (MAT != kMatNode) return;
 #pragma unroll
       for (int m = 0; m < NDOF; ++m) {
-        if constexpr (STG && Stg::kStageMat) {
-          const float *sr = slot_of(J0 + j) + (Stg::kM + m) * kRowF;
-          mq[slot][m] = ld ? *reinterpret_cast<const float4 *>(sr + 4 * lane) : make_float4(0.f, 0.f, 0.f, 0.f);
-          m5[slot][m] = (lane == 31 && act) ? sr[128] : 0.f;
-        } else {
-          const float *b = p.mat[m] + (long long)(J0 + j) * p.pitch + I0;
-          mq[slot][m] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
-          m5[slot][m] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
-        }
+        const float *b = p.mat[m] + (long long)(J0 + j) * p.pitch + I0;
+        mq[slot][m] = ld ? ldg4(b) : make_float4(0.f, 0.f, 0.f, 0.f);
+        m5[slot][m] = (lane == 31 && act) ? __ldg(b + 4) : 0.f;
       }
     };
     fetch_m(0, 0);
@@ -342,39 +257,54 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           const float nx4 = __shfl_down_sync(0xffffffffu, q.x, 1);
           v[4] = lane < 31 ? nx4 : m5[j & 1][m];
         }
-      } else {
+      }
+      const float rB = -(det * w[j]) * xix;  // row factor of the column part
+      if (NDOF == 1) {
+        // SH: mu = m0 (node) or em0 (element)
+        const float rr = rB * xix;
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          m0[i] = em0;
-          m1[i] = em1;
+          const float cc = -(det * w[i]) * etaz * etaz;  // column factor of the row part
+          if (MAT == kMatNode) {
+            B[0][j][i] = rr * (m0[i] * B[0][j][i]);
+            A[0][j][i] = cc * (m0[i] * A[0][j][i]);
+          } else {
+            B[0][j][i] = (rr * em0) * B[0][j][i];
+            A[0][j][i] = (cc * em0) * A[0][j][i];
+          }
         }
-      }
-      const float wdtj = det * w[j];
+      } else if (MAT == kMatNode) {
+        // P-SV, la = m0, mu = m1 at each point
+        const float xr = rB * xix, er = rB * etaz;
 #pragma unroll
-      for (int i = 0; i < N; ++i) {
-        const float wdti = det * w[i];
-        if (NDOF == 1) {
-          // SH: mu = m0
-          const float cxx = -(wdtj * xix) * xix, czz = -(wdti * etaz) * etaz;
-          B[0][j][i] = (cxx * w[i]) * (m0[i] * B[0][j][i]);
-          A[0][j][i] = (czz * w[j]) * (m0[i] * A[0][j][i]);
-        } else {
-          // P-SV: la = m0, mu = m1
+        for (int i = 0; i < N; ++i) {
           const float la = m0[i], mu = m1[i];
           const float K = la + 2.f * mu;
           const float gxx = B[0][j][i], gxz = B[1][j][i], gex = A[0][j][i], gez = A[1][j][i];
-          const float dxux = xix * gxx, dxuz = xix * gxz, dzux = etaz * gex, dzuz = etaz * gez;
-          const float wc = -(wdtj * xix) * w[i];
-          const float wr = -(wdti * etaz) * w[j];
-          const float sxz = kd2 ? etaz : xix;
-          B[0][j][i] = wc * (K * dxux + la * dzuz);
-          B[1][j][i] = wc * (mu * (dzux + dxuz));
-          A[0][j][i] = wr * (mu * (dzux + sxz * gxz));
-          A[1][j][i] = wr * (la * dxux + K * dzuz);
+          const float cA = -(det * w[i]) * etaz;
+          const float xc = cA * xix, ec = cA * etaz, sc = cA * sxz;
+          B[0][j][i] = (xr * K) * gxx + (er * la) * gez;
+          B[1][j][i] = mu * (er * gex + xr * gxz);
+          A[0][j][i] = mu * (ec * gex + sc * gxz);
+          A[1][j][i] = (xc * la) * gxx + (ec * K) * gez;
+        }
+      } else {
+        // P-SV, moduli constant over the element: row-folded coefficients
+        const float b0x = rB * cKx, b0z = rB * cLz, b1e = rB * cMz, b1x = rB * cMx;
+#pragma unroll
+        for (int i = 0; i < N; ++i) {
+          const float gxx = B[0][j][i], gxz = B[1][j][i], gex = A[0][j][i], gez = A[1][j][i];
+          const float cA = -(det * w[i]) * etaz;
+          B[0][j][i] = b0x * gxx + b0z * gez;
+          B[1][j][i] = b1e * gex + b1x * gxz;
+          A[0][j][i] = cA * (cMz * gex + cMs * gxz);
+          A[1][j][i] = cA * (cLx * gxx + cKz * gez);
         }
       }
     }
-    // divergence: column part sum_q H[i + N q] B(q,j) row by row in place
+    // divergence, both parts in one chain: F(i,j) = sum_q Hw[i + N q] B(q,j)
+    // + sum_q A(i,q) Hw[j + N q]; row by row into B (row j of A is not read
+    // after row j of B is written: the row part reads A only)
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
 #pragma unroll
@@ -382,26 +312,16 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float t[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          float a = H[i + N * 0] * B[c][j][0];
+          float a = Hw[i + N * 0] * B[c][j][0];
 #pragma unroll
-          for (int q = 1; q < N; ++q) a = a + H[i + N * q] * B[c][j][q];
+          for (int q = 1; q < N; ++q) a = a + Hw[i + N * q] * B[c][j][q];
+#pragma unroll
+          for (int q = 0; q < N; ++q) a = a + A[c][q][i] * Hw[j + N * q];
           t[i] = a;
         }
 #pragma unroll
         for (int i = 0; i < N; ++i) B[c][j][i] = t[i];
       }
-    // plus the row part sum_q A(i,q) H[j + N q]: nodal forces into B
-#pragma unroll
-    for (int c = 0; c < NDOF; ++c)
-#pragma unroll
-      for (int i = 0; i < N; ++i)
-#pragma unroll
-        for (int j = 0; j < N; ++j) {
-          float a = A[c][0][i] * H[j + N * 0];
-#pragma unroll
-          for (int q = 1; q < N; ++q) a = a + A[c][q][i] * H[j + N * q];
-          B[c][j][i] = B[c][j][i] + a;
-        }
 
     // ---- assembly: forces of the left element on column 0 ----
     float L[NDOF][N];
@@ -454,6 +374,18 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         for (int c = 0; c < NDOF; ++c)
 #pragma unroll
           for (int i = 0; i < N; ++i) f[c][i] = fsum(c, j, i);
+        if (FST && own) {
+          // the elastic force of this step: the previous one plus dt (-K v)
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) {
+            const float4 q = ldg4(Fc + c * pl + g);
+            const float fp[N] = {q.x, q.y, q.z, q.w, last_col ? __ldg(Fc + c * pl + g + 4) : 0.f};
+#pragma unroll
+            for (int i = 0; i < N; ++i) f[c][i] = fp[i] + dt * f[c][i];
+            *reinterpret_cast<float4 *>(Fn + c * pl + g) = make_float4(f[c][0], f[c][1], f[c][2], f[c][3]);
+            if (last_col) Fn[c * pl + g + 4] = f[c][4];
+          }
+        }
         if (src_on) {
           for (int s = 0; s < p.nsrc; ++s) {
             const int sI = p.src_I[s], sJ = p.src_J[s];
@@ -469,33 +401,31 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           }
         }
         if (!own) continue;
-        // this node row's staged fields (STG)
-        const float *sl = STG ? slot_of(J) + 4 * lane : nullptr;
         float vv[NDOF][N], rmv[N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float *src = STG ? sl + (Stg::kV + c) * kRowF : Vc + c * pl + g;
-          const float4 q = STG ? *reinterpret_cast<const float4 *>(src) : ldg4(src);
+          const float4 q = ldg4(Vc + c * pl + g);
           vv[c][0] = q.x;
           vv[c][1] = q.y;
           vv[c][2] = q.z;
           vv[c][3] = q.w;
-          vv[c][4] = last_col ? (STG ? src[4] : __ldg(src + 4)) : 0.f;
+          vv[c][4] = last_col ? __ldg(Vc + c * pl + g + 4) : 0.f;
         }
         {
-          const float *src = STG ? sl + Stg::kRm * kRowF : Rm + g;
-          const float4 q = STG ? *reinterpret_cast<const float4 *>(src) : ldg4(src);
+          const float4 q = ldg4(Rm + g);
           rmv[0] = q.x;
           rmv[1] = q.y;
           rmv[2] = q.z;
           rmv[3] = q.w;
-          rmv[4] = last_col ? (STG ? src[4] : __ldg(src + 4)) : 0.f;
+          rmv[4] = last_col ? __ldg(Rm + g + 4) : 0.f;
         }
-        // dashpots and the perimeter inverse mass
+        // dashpots and the perimeter inverse mass (only lanes with a node on
+        // the perimeter in this row look at the table)
+        const bool per_row = edgeJ || I0 == 0 || (last_col && I0 + N - 1 == p.LX - 1);
 #pragma unroll
         for (int i = 0; i < N; ++i) {
           const int I = I0 + i;
-          if (i == N - 1 && !last_col) continue;
+          if (!per_row || (i == N - 1 && !last_col)) continue;
           if (edgeJ || I == 0 || I == p.LX - 1) {
             const int sp = perimeter_slot(I, J, p.LX, p.LZ);
 #pragma unroll
@@ -521,13 +451,12 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float dv[NDOF][N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float *src = STG ? sl + (Stg::kD + c) * kRowF : Dc + c * pl + g;
-          const float4 q = STG ? *reinterpret_cast<const float4 *>(src) : ldg4(src);
+          const float4 q = ldg4(Dc + c * pl + g);
           dv[c][0] = q.x;
           dv[c][1] = q.y;
           dv[c][2] = q.z;
           dv[c][3] = q.w;
-          dv[c][4] = last_col ? (STG ? src[4] : __ldg(src + 4)) : 0.f;
+          dv[c][4] = last_col ? __ldg(Dc + c * pl + g + 4) : 0.f;
         }
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
@@ -536,7 +465,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           for (int i = 0; i < N; ++i) {
             float rm = rmv[i];
             const int I = I0 + i;
-            if (c == 1 && (edgeJ || I == 0 || I == p.LX - 1) && (i < N - 1 || last_col))
+            if (c == 1 && per_row && (edgeJ || I == 0 || I == p.LX - 1) && (i < N - 1 || last_col))
               rm = p.per_rm[nslot + perimeter_slot(I, J, p.LX, p.LZ)];
             const float a = rm * f[c][i];
             an[i] = a;
@@ -556,15 +485,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     }
     if (halo) set_carry();
     have_carry = top_shared;
-    if constexpr (STG) {
-      // every lane is done with this element row's slots: refill them with
-      // the rows of element row ez+2 (an empty group keeps the count)
-      __syncwarp();
-      if (ez + 2 < u.z1) stage_elem_row(ez + 2, false);
-      cp_async_commit();
-    }
   }
-  if constexpr (STG) cp_async_wait<0>();
 
   // ---- receivers of this unit ----
   if (p.rec_ids && u.rec1 > u.rec0 && it % p.rec_isamp == 0 && it / p.rec_isamp < p.rec_nsamp) {
@@ -604,35 +525,33 @@ __device__ __forceinline__ void march_done(int *step, unsigned *done, int it) {
   }
 }
 
-// one problem: warp w of CTA b walks unit (warps per CTA)*b + w (STG: with
-// its ring in the CTA's dynamic shared memory, MarchStage::kWarpBytes per
-// warp).  The launch picks 1, 2 or 4 warps per CTA: with one, a warp that
-// finishes its unit frees its slot at once.
-template <int NDOF, int MAT, bool STG>
-__global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBlocks))
+// one problem: warp w of CTA b walks unit (warps per CTA)*b + w; the launch
+// picks 1, 2 or 4 warps per CTA (with one, a warp that finishes its unit
+// frees its slot at once)
+template <int NDOF, int MAT, bool FST>
+__global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
     march_step_kernel(const __grid_constant__ BulkParams<float, 5> p, const MarchUnit *units, int nunits) {
-  extern __shared__ __align__(16) float march_ring[];
   const int warp = threadIdx.x >> 5;
   const int it = *p.step + 1;
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (uid < nunits) {
     const MarchUnit u = units[uid];
-    march_unit<NDOF, MAT, STG>(p, p.H, p.w, u, it, march_ring + warp * MarchStage<NDOF, MAT>::kWarpFloats);
+    march_unit<NDOF, MAT, FST>(p, p.H, p.w, p.Hw, u, it);
   }
   march_done(p.step, p.done, it);
 }
 
-// many problems: the units of all problems, each with its parameter block
-template <int NDOF, int MAT, bool STG>
-__global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBlocks))
+// many problems (without faults: the displacement state): the units of all
+// problems, each with its parameter block
+template <int NDOF, int MAT>
+__global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
     march_batch_kernel(const __grid_constant__ MarchBatch b) {
-  extern __shared__ __align__(16) float march_ring[];
   const int warp = threadIdx.x >> 5;
   const int it = *b.step + 1;
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (uid < b.nunits) {
     const MarchUnit u = b.units[uid];
-    march_unit<NDOF, MAT, STG>(b.sims[u.prob], b.H, b.w, u, it, march_ring + warp * MarchStage<NDOF, MAT>::kWarpFloats);
+    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, b.Hw, u, it);
   }
   march_done(b.step, b.done, it);
 }
@@ -642,13 +561,13 @@ __global__ void __launch_bounds__(32 * kMarchWarps, (MarchOcc<NDOF, STG>::kMinBl
 // on warp w, w < nrows), then its threads finish the strip's fault node
 // pairs (columns 124 s .. 124 s + 123, and the last column on the last
 // strip) from the forces its warps wrote; the last CTA bumps the counter.
-template <int NDOF, int MAT>
+template <int NDOF, int MAT, bool FST>
 __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
     march_fault_side_kernel(const __grid_constant__ BulkParams<float, 5> p, const MarchUnit *units, int nstrips,
                             int nrows) {
   const int warp = threadIdx.x >> 5, s = blockIdx.x;
   const int it = *p.step + 1;
-  if (warp < nrows) march_unit<NDOF, MAT>(p, p.H, p.w, units[warp * nstrips + s], it);
+  if (warp < nrows) march_unit<NDOF, MAT, FST>(p, p.H, p.w, p.Hw, units[warp * nstrips + s], it);
   __syncthreads();  // the strip's fault-row forces are written (global memory, this block)
   const int t = threadIdx.x, I = 4 * kMarchCols * s + t;
   const bool mine = (t < 4 * kMarchCols && I < p.LX) || (t == 4 * kMarchCols && I == p.LX - 1);

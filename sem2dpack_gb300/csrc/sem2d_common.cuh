@@ -84,6 +84,7 @@ struct BulkParams {
   // GLL operator
   real H[N * N];    // H(i,j) = h'_i(x_j), column-major
   real w[N];
+  real Hw[N * N];   // Hw[i + N q] = H[i + N q] w[q] (the march kernel's divergence)
   // state (ping-pong buffers chosen by the host)
   const real *Dcur;
   real *Dnext;
@@ -91,6 +92,8 @@ struct BulkParams {
   real *Vnext;
   const real *Acur;
   real *Anext;      // null unless accelerations are kept
+  const real *Fcur; // march kernel, force state: elastic force of the step before
+  real *Fnext;      //   and of this step (null with the displacement state)
   // material
   int mat_iso;      // isotropic: planes (la, mu) [P-SV] or (mu) [SH]
   const real *mat[4];
@@ -142,7 +145,6 @@ struct BulkParams {
   int nplanes;            // lattice planes staged per batch (strip_planes)
   int *error;             // sticky device error flag (SEM2D_E_*)
   int spin_limit;         // polls of a stage's mbarrier before the step gives up
-  int march_pf;           // march kernel: prefetch the next element row into L2
   int chunk_shift;        // chunk of CTA row y is (y + chunk_shift) % rows: the
                           // fault's chunk (long FP64 work) is scheduled first
 };

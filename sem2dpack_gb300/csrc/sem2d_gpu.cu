@@ -123,9 +123,9 @@ struct sem2d_handle {
   // the one-element-per-thread kernel (FP32, NGLL = 5 fast path): work
   // units (strip, chunk) and the receivers each unit samples
   bool march = false;
-  int march_stage = 0;  // rows staged through shared memory (SEM2D_MARCH_STAGE=1) or loaded directly
   int march_warps = 4;  // warps per CTA (SEM2D_MARCH_WARPS)
-  int march_pf = 0;     // direct loads: L2 prefetch of the next element row (SEM2D_MARCH_PREFETCH)
+  int march_fst = 0;    // force state (problems with a fault; SEM2D_FORCE_STATE=0 keeps the displacement state)
+  void *F[2] = {nullptr, nullptr};  // force state planes, ping-pong like D and V
   int tune_source = 0;  // launch shape: 0 analytic, 1 timed at create, 2 from the tuning cache
   int march_cz = 0, march_nunits = 0;
   void *d_march_units = nullptr;
@@ -791,9 +791,10 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.fast = fast_path(h);
   bc.error = h->d_error;
   bc.spin_limit = h->spin_limit;
-  bc.march_stage = h->march_stage;
   bc.march_warps = h->march_warps;
-  bc.march_pf = h->march_pf;
+  bc.march_fst = h->march_fst;
+  bc.Fcur = h->F[cur];
+  bc.Fnext = h->F[1 - cur];
   bc.grid_x = (h->nx + h->TX - 1) / h->TX;
   bc.grid_y = int(h->ztile.size()) - 1;
   bc.LX = h->LX;
@@ -1273,6 +1274,7 @@ int reset_state(sem2d_handle *h) {
   for (int b = 0; b < 2; ++b) {
     CK(cudaMemsetAsync(h->D[b], 0, rs * h->plane * h->ndof, h->stream));
     CK(cudaMemsetAsync(h->V[b], 0, rs * h->plane * h->ndof, h->stream));
+    if (h->F[b]) CK(cudaMemsetAsync(h->F[b], 0, rs * h->plane * h->ndof, h->stream));
     if (h->A[b]) CK(cudaMemsetAsync(h->A[b], 0, rs * h->plane * h->ndof, h->stream));
   }
   CK(cudaMemsetAsync(h->d_step, 0, sizeof(int), h->stream));
@@ -1447,12 +1449,14 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   bc.pitch = h->pitch;
   bc.plane = h->plane;
   if (!march_supported(bc)) return SEM2D_OK;
-  if (const char *e = std::getenv("SEM2D_MARCH_STAGE")) h->march_stage = std::atoi(e) != 0;
   if (const char *e = std::getenv("SEM2D_MARCH_WARPS")) h->march_warps = std::atoi(e);
-  if (const char *e = std::getenv("SEM2D_MARCH_PREFETCH")) h->march_pf = std::atoi(e) != 0;
-  bc.march_stage = h->march_stage;
+  // with a fault the elastic force is the state: the displacement next to
+  // a slipped fault is too large for FP32 to resolve the dynamic stress
+  const char *fs = std::getenv("SEM2D_FORCE_STATE");
+  h->march_fst = h->nflt > 0 && !(fs && std::atoi(fs) == 0);
   bc.march_warps = h->march_warps;
-  // resident warps per SM; also sets the kernels' shared-memory limit
+  bc.march_fst = h->march_fst;
+  // resident warps per SM
   const int warps_per_sm = march_warps_per_sm(bc);
   if (warps_per_sm <= 0) return set_err(h, SEM2D_E_CUDA, std::string("march kernel: ") + bulk_last_error());
   int st;
@@ -1467,6 +1471,12 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
         h->rec_separate = true;
     if ((st = dalloc(h, &h->d_fault_force, (size_t)2 * h->ndof * h->nflt))) return st;
   }
+  if (h->march_fst)
+    for (int b = 0; b < 2; ++b) {
+      float *q = nullptr;
+      if ((st = dalloc(h, &q, (size_t)h->plane * h->ndof))) return st;
+      h->F[b] = q;
+    }
   const int nstrips = (h->nx + kMarchColsHost - 1) / kMarchColsHost;
   int cz = 0;
   if (const char *e = std::getenv("SEM2D_MARCH_CZ")) cz = std::atoi(e);
@@ -1506,22 +1516,22 @@ int build_batch_tables(sem2d_handle *h);
 // ---- the autotuner of the march kernels' launch shape ----------------
 // The first handle of a class of problems (dof count, material layout,
 // node count and member count to a power of two, SM count) times candidate
-// shapes -- chunk height, warps per CTA, L2 prefetch of the next element
-// row -- over a few steps with CUDA events, keeps the fastest (the analytic
+// shapes -- chunk height and warps per CTA -- over a few steps with CUDA
+// events, keeps the fastest (the analytic
 // default unless another is faster by more than 2 %) and records it in the
 // tuning cache (autotune.cpp); later handles of the class read it.  The
 // shapes give bitwise identical results (the per-node summation order does
 // not depend on them), and the state is reset after the trial steps.
-// SEM2D_AUTOTUNE=0, or any of SEM2D_MARCH_CZ / _WARPS / _PREFETCH / _STAGE,
-// keeps the analytic shape.
+// SEM2D_AUTOTUNE=0, or SEM2D_MARCH_CZ / SEM2D_MARCH_WARPS, keeps the
+// analytic shape.
 struct MarchShape {
-  int cz, warps, pf;
+  int cz, warps;
 };
 
 bool tune_disabled() {
   const char *t = std::getenv("SEM2D_AUTOTUNE");
   if (t && std::atoi(t) == 0) return true;
-  for (const char *v : {"SEM2D_MARCH_CZ", "SEM2D_MARCH_WARPS", "SEM2D_MARCH_PREFETCH", "SEM2D_MARCH_STAGE"})
+  for (const char *v : {"SEM2D_MARCH_CZ", "SEM2D_MARCH_WARPS"})
     if (std::getenv(v)) return true;
   return false;
 }
@@ -1533,11 +1543,9 @@ int apply_shape(sem2d_handle *h, const MarchShape &s) {
   for (sem2d_handle *m : probs) {
     if (s.cz != m->march_cz && (st = build_march_units(m, s.cz))) return st;
     m->march_warps = s.warps;
-    m->march_pf = s.pf;
   }
   if (!h->subs.empty() && (st = build_batch_tables(h))) return st;
   h->march_warps = s.warps;
-  h->march_pf = s.pf;
   if (h->graph_exec) {  // a captured graph holds the old units
     cudaGraphExecDestroy(h->graph_exec);
     h->graph_exec = nullptr;
@@ -1580,13 +1588,13 @@ int tune_march(sem2d_handle *h) {
   sem2d_tune_entry e;
   if (have_path && sem2d_tune_lookup(path, key, &e) == 1) {
     h->tune_source = 2;
-    return apply_shape(h, MarchShape{e.chunk_rows, e.warps_per_cta, e.l2_prefetch});
+    return apply_shape(h, MarchShape{e.chunk_rows, e.warps_per_cta});
   }
   const int nwarm = 2, n = std::min(32, h->nt - nwarm);
   if (n < 4) return SEM2D_OK;  // too few steps to time: the analytic shape
   const int cz0 = a->march_cz;
-  const MarchShape cands[] = {{cz0, a->march_warps, 0}, {cz0, 1, 0}, {2 * cz0, a->march_warps, 0},
-                              {std::max(1, cz0 / 2), a->march_warps, 0}, {cz0, a->march_warps, 1}};
+  const MarchShape cands[] = {{cz0, a->march_warps}, {cz0, 1}, {2 * cz0, a->march_warps},
+                              {std::max(1, cz0 / 2), a->march_warps}, {2 * cz0, 1}};
   const int nc = int(sizeof(cands) / sizeof(cands[0]));
   std::vector<sem2d_tune_entry> res(nc);
   const long long l0 = h->launches;
@@ -1594,7 +1602,7 @@ int tune_march(sem2d_handle *h) {
   for (int k = 0; k < nc; ++k) {
     double ms = 0;
     if ((st = apply_shape(h, cands[k])) || (st = time_shape(h, nwarm, n, &ms)) || (st = reset_state(h))) return st;
-    res[k] = sem2d_tune_entry{std::max(1, std::min(cands[k].cz, a->nz)), cands[k].warps, cands[k].pf, 0, ms};
+    res[k] = sem2d_tune_entry{std::max(1, std::min(cands[k].cz, a->nz)), cands[k].warps, ms};
   }
   const int best = sem2d_tune_select(res.data(), nc, 0.02);
   if ((st = apply_shape(h, cands[best]))) return st;

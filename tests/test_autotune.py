@@ -13,8 +13,8 @@ def key(ndof, mat, nodes, members, nsm):
     return buf.value
 
 
-def entry(cz, warps, pf, ms, staged=0):
-    return abi.TuneEntry(cz, warps, pf, staged, ms)
+def entry(cz, warps, ms):
+    return abi.TuneEntry(cz, warps, ms)
 
 
 def test_keys_bucket_by_powers_of_two():
@@ -35,15 +35,15 @@ def test_record_and_lookup(tmp_path):
     k1, k2 = key(2, 2, 1 << 20, 0, 152), key(1, 2, 1 << 20, 0, 152)
     out = abi.TuneEntry()
     assert L.sem2d_tune_lookup(path, k1, C.byref(out)) == 0  # no file yet
-    assert L.sem2d_tune_record(path, k1, C.byref(entry(32, 1, 0, 4.5))) == 0
-    assert L.sem2d_tune_record(path, k2, C.byref(entry(16, 4, 1, 0.02))) == 0
+    assert L.sem2d_tune_record(path, k1, C.byref(entry(32, 1, 4.5))) == 0
+    assert L.sem2d_tune_record(path, k2, C.byref(entry(16, 4, 0.02))) == 0
     assert L.sem2d_tune_lookup(path, k1, C.byref(out)) == 1
-    assert (out.chunk_rows, out.warps_per_cta, out.l2_prefetch, out.staged) == (32, 1, 0, 0)
+    assert (out.chunk_rows, out.warps_per_cta) == (32, 1)
     assert abs(out.ms_per_step - 4.5) < 1e-9
     # a new record replaces the old one
-    assert L.sem2d_tune_record(path, k1, C.byref(entry(8, 4, 1, 3.0))) == 0
+    assert L.sem2d_tune_record(path, k1, C.byref(entry(8, 4, 3.0))) == 0
     assert L.sem2d_tune_lookup(path, k1, C.byref(out)) == 1
-    assert (out.chunk_rows, out.warps_per_cta, out.l2_prefetch) == (8, 4, 1)
+    assert (out.chunk_rows, out.warps_per_cta) == (8, 4)
     lines = (tmp_path / "sub" / "tune.json").read_text().splitlines()
     assert len(lines) == 2
     recs = {json.loads(x)["key"]: json.loads(x) for x in lines}
@@ -51,17 +51,15 @@ def test_record_and_lookup(tmp_path):
     # unreadable lines are skipped, the others still read
     with open(path, "a") as f:
         f.write('{"key": "broken", "chunk_rows": \n')
-        f.write('{"key": "bad warps", "chunk_rows": 4, "warps_per_cta": 3, "l2_prefetch": 0, "staged": 0, '
-                '"ms_per_step": 1}\n')
+        f.write('{"key": "bad warps", "chunk_rows": 4, "warps_per_cta": 3, "ms_per_step": 1}\n')
     assert L.sem2d_tune_lookup(path, k2, C.byref(out)) == 1
     assert L.sem2d_tune_lookup(path, b"bad warps", C.byref(out)) == 0
-    assert L.sem2d_tune_record(path, b'quote"inside', C.byref(entry(1, 1, 0, 1.0))) == abi.SEM2D_E_ARG
+    assert L.sem2d_tune_record(path, b'quote"inside', C.byref(entry(1, 1, 1.0))) == abi.SEM2D_E_ARG
 
 
 def test_selection_keeps_the_default_within_the_margin():
     L = _lib.lib()
-    arr = (abi.TuneEntry * 4)(entry(16, 4, 0, 1.00), entry(16, 1, 0, 0.99), entry(32, 4, 0, 1.20),
-                              entry(8, 4, 0, 0.0))
+    arr = (abi.TuneEntry * 4)(entry(16, 4, 1.00), entry(16, 1, 0.99), entry(32, 4, 1.20), entry(8, 4, 0.0))
     assert L.sem2d_tune_select(arr, 4, 0.02) == 0  # 1 % faster: noise
     arr[1].ms_per_step = 0.95
     assert L.sem2d_tune_select(arr, 4, 0.02) == 1  # 5 % faster

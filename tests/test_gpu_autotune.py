@@ -41,7 +41,7 @@ def test_single_problem_tuned_then_cached(monkeypatch, tmp_path):
     assert launches == h.launches  # trial launches are not counted
     monkeypatch.delenv("SEM2D_AUTOTUNE")
     # a later handle reads the cache: an entry edited by hand is taken as is
-    recs[0].update(chunk_rows=3, warps_per_cta=1, l2_prefetch=0)
+    recs[0].update(chunk_rows=3, warps_per_cta=1)
     cache.write_text(json.dumps(recs[0]) + "\n")
     k = Solver(d, owner=P)
     assert k.tile == (MARCH_TX, 3)

@@ -82,6 +82,10 @@ def test_march_against_oracle(name, monkeypatch):
 
 @pytest.mark.parametrize("name", ["plain_psv_45", "sh_rupture", "psv_rsf"])
 def test_march_against_strip_kernel(name, monkeypatch):
+    """Same formulas in FP32.  With a fault the march kernel carries the
+    force state and the strip kernel the displacement state, whose FP32
+    displacement next to the slipped fault is the coarser of the two: there
+    the two agree to the mixed tolerance (1e-4)."""
     build, nt = CASES[name]
     case = build()
     P, d, g = make(case, monkeypatch)
@@ -91,7 +95,7 @@ def test_march_against_strip_kernel(name, monkeypatch):
     h.step(nt)
     a, b = outputs(g, d.nflt), outputs(h, d.nflt)
     for k in a:
-        assert rel_l2(a[k], b[k]) <= 2e-5, k
+        assert rel_l2(a[k], b[k]) <= (1e-4 if d.nflt else 2e-5), k
 
 
 @pytest.mark.parametrize("name", ["plain_psv_45", "sh_rupture", "psv_rsf"])
@@ -139,3 +143,26 @@ def test_fused_fault_side_equals_separate_kernels(monkeypatch):
     a, b = outputs(g, True), outputs(h, True)
     for k in a:
         assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("name", ["sh_rupture", "psv_rsf"])
+def test_force_state_is_closer_to_fp64(name, monkeypatch):
+    """Problems with a fault carry the elastic force as the state (the
+    element pass applies the stiffness to the velocity); in exact arithmetic
+    it equals the displacement state, which SEM2D_FORCE_STATE=0 selects.
+    In FP32 it is the closer of the two to the FP64 oracle: the displacement
+    next to the slipped fault loses the digits of the dynamic stress."""
+    build, nt = CASES[name]
+    case = build()
+    P, d, g = make(case, monkeypatch)
+    _, _, h = make(case, monkeypatch, {"SEM2D_FORCE_STATE": 0})
+    g.step(nt)
+    h.step(nt)
+    o = po.OracleSim(d, owner=P)
+    o.run(nt)
+    s_o, f_o = o.seismograms(), o.fault_series()[:, 1, :]
+    e_force = rel_l2(g.seismograms(), s_o) + rel_l2(g.fault_series()[:, 1, :], f_o)
+    e_displ = rel_l2(h.seismograms(), s_o) + rel_l2(h.fault_series()[:, 1, :], f_o)
+    assert e_force <= 1e-4 and e_displ <= 1e-4
+    if name == "sh_rupture":  # slip of a metre within the run
+        assert e_force < 0.5 * e_displ, (e_force, e_displ)
