@@ -536,11 +536,12 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
     from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Solver, workloads
     from sem2dpack_gb300._lib import lib
     prec = PRECISION_MIXED if args.precision == "mixed" else PRECISION_FP64
-    nt = args.time_steps or 400
+    nt = args.time_steps or 4000
     models, start, true = workloads.gradient_shots(scale=args.scale, nsteps=nt, precision=prec)
     every = max(1, int(round(np.sqrt(nt))))
     pp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
     sims, obs = [], []
+    t_create, h2d = 0.0, 0
     for m in models:
         Pt = workloads.build(m.deck_for(*true))
         st = Solver(Pt)
@@ -551,7 +552,10 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
         d = P.desc()
         d.precision = prec
         d.adjoint = 1
+        t0 = time.perf_counter()
         sims.append((Solver(d, owner=P), d))
+        t_create += time.perf_counter() - t0
+        h2d += desc_bytes(d)
     npoin = sims[0][1].npoin
     grads = [np.zeros(npoin) for _ in range(3)]
 
@@ -579,6 +583,17 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
             s._check(lib().sem2d_gpu_adjoint(s.h, pp(r), pp(grads[0]), pp(grads[1]), pp(grads[2])))
         return time.perf_counter() - t0
 
+    # end to end: the uploads (timed at creation), one forward solve of every
+    # shot, the seismograms back
+    barrier()
+    t0 = time.perf_counter()
+    for s, _ in sims:
+        s.reset()
+        s.step(nt)
+    for s, _ in sims:
+        s.seismograms()
+    e2e_value = world * len(sims) * sims[0][1].npoin * nt / (t_create + time.perf_counter() - t0)
+    d2h = sum(8 * d.rec_nsamp * d.nrec * d.ndof for _, d in sims)
     for _ in range(max(1, args.warmup)):
         forward_only()
         gradient()
@@ -593,6 +608,10 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
     value = len(sims) * npoin * nt / fwd
     name = ("gradient workflow: %d P-SV shots on %dx%d elements of 25 m, NGLL=5, %d of 4000 steps, "
             "checkpoint every %d steps" % (len(sims), models[0].deck.nelem[0], models[0].deck.nelem[1], nt, every))
+    # the bound from the bytes a step moves per node (P-SV FP32): forward 44,
+    # recomputed forward with its ring of d, v, a 68, reverse step 96
+    # (forces pass 60, moduli pass 36)
+    bound = (44 + 68 + 96) / 44
     if rank == 0:
         print(json.dumps({
             "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s", "n_gpus": world,
@@ -602,10 +621,15 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
             "config": {"workload": name, "global_batch": len(sims), "seq_len": 0, "parallelism": "replicas",
                        "npoin": npoin, "time_steps_per_step": nt},
             "gradient_cost": {"forward_s": fwd, "forward_and_adjoint_s": grd, "ratio": grd / fwd,
+                              "bytes_bound": bound,
                               "note": "forward with checkpoints + segment recomputation + adjoint, "
-                                      "over the plain forward solves of the same shots"},
+                                      "over the plain forward solves of the same shots; bytes_bound: the "
+                                      "ratio of the bytes per node the three phases move to a forward step's"},
             "roofline": None, "cpu_baseline": None,
-            "e2e": None, "clocks": clk, "gpu_launches": l0,
+            "e2e": {"value": e2e_value, "unit": "node-steps/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h, "path": "Solver creation of every shot from host arrays, one "
+                                                       "forward solve each, seismograms back"},
+            "clocks": clk, "gpu_launches": l0,
         }), flush=True)
     for s, _ in sims:
         s.close()

@@ -25,7 +25,6 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.ztile = c.ztile;
   for (int k = 0; k < N * N; ++k) p.H[k] = real(c.H[k]);
   for (int k = 0; k < N; ++k) p.w[k] = real(c.w[k]);
-  for (int k = 0; k < N * N; ++k) p.Hw[k] = real(c.H[k] * c.w[k / N]);
   p.Dcur = static_cast<const real *>(c.Dcur);
   p.Dnext = static_cast<real *>(c.Dnext);
   p.Vcur = static_cast<const real *>(c.Vcur);

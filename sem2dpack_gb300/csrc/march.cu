@@ -41,7 +41,6 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   MarchBatch b{};
   for (int k = 0; k < 25; ++k) b.H[k] = float(c.H[k]);
   for (int k = 0; k < 5; ++k) b.w[k] = float(c.w[k]);
-  for (int k = 0; k < 25; ++k) b.Hw[k] = float(c.H[k] * c.w[k / 5]);
   b.sims = static_cast<const BulkParams<float, 5> *>(m.sims);
   b.units = static_cast<const MarchUnit *>(m.units);
   b.nunits = m.nunits;

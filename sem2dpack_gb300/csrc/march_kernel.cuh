@@ -88,7 +88,6 @@ struct MarchUnit {
 
 struct MarchBatch {
   float H[25], w[5];                 // GLL operator (the same for every problem)
-  float Hw[25];                      // Hw[i + 5q] = H[i + 5q] w[q]
   const BulkParams<float, 5> *sims;  // per problem
   const MarchUnit *units;
   int nunits;
@@ -101,7 +100,7 @@ __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpre
 // one unit of one problem (FST: the force-state formulation)
 template <int NDOF, int MAT, bool FST>
 __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const float *H, const float *w,
-                                           const float *Hw, const MarchUnit &u, int it) {
+                                           const MarchUnit &u, int it) {
   constexpr int N = 5;
   const int lane = threadIdx.x & 31;
   const int ex = kMarchCols * u.strip - 1 + lane;
@@ -210,23 +209,13 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
 #pragma unroll
         for (int j = 0; j < N; ++j) A[c][j][i] = t[j];
       }
-    // stress terms at every point: column part into B, row part into A.
-    // The GLL weight of the contracted index is in the Hw table of the
-    // divergence below, so B(i,j) carries the weight w_j of its row and
-    // A(i,j) the weight w_i of its column: with det = dx/dxi dz/deta,
-    //   B = -det w_j xix (stress . x),  A = -det w_i etaz (stress . z)
-    // (the a-coefficients of MAT_ELAST_init_a, mat_elastic.f90:323-358,
-    // factored); per element the moduli are folded into four coefficients.
+    // stress terms at every point: column part (weights -W xix) into B,
+    // row part (weights -W etaz) into A
     float em0 = 0.f, em1 = 0.f;
     if (MAT == kMatElement && act) {
       em0 = p.mat[0][eidx];
       if (NDOF == 2) em1 = p.mat[1][eidx];
     }
-    const float sxz = kd2 ? etaz : xix;  // KD2 uses a4 for both shear derivatives
-    // element material: mu xix, mu etaz, mu sxz, la xix, la etaz, K xix, K etaz
-    const float eK = em0 + 2.f * em1;
-    const float cMx = em1 * xix, cMz = em1 * etaz, cMs = em1 * sxz;
-    const float cLx = em0 * xix, cLz = em0 * etaz, cKx = eK * xix, cKz = eK * etaz;
     // node material: the 16-byte parts of row j+1 are requested before row
     // j is used
     float4 mq[2][2];
@@ -257,54 +246,39 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           const float nx4 = __shfl_down_sync(0xffffffffu, q.x, 1);
           v[4] = lane < 31 ? nx4 : m5[j & 1][m];
         }
-      }
-      const float rB = -(det * w[j]) * xix;  // row factor of the column part
-      if (NDOF == 1) {
-        // SH: mu = m0 (node) or em0 (element)
-        const float rr = rB * xix;
+      } else {
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          const float cc = -(det * w[i]) * etaz * etaz;  // column factor of the row part
-          if (MAT == kMatNode) {
-            B[0][j][i] = rr * (m0[i] * B[0][j][i]);
-            A[0][j][i] = cc * (m0[i] * A[0][j][i]);
-          } else {
-            B[0][j][i] = (rr * em0) * B[0][j][i];
-            A[0][j][i] = (cc * em0) * A[0][j][i];
-          }
+          m0[i] = em0;
+          m1[i] = em1;
         }
-      } else if (MAT == kMatNode) {
-        // P-SV, la = m0, mu = m1 at each point
-        const float xr = rB * xix, er = rB * etaz;
+      }
+      const float wdtj = det * w[j];
 #pragma unroll
-        for (int i = 0; i < N; ++i) {
+      for (int i = 0; i < N; ++i) {
+        const float wdti = det * w[i];
+        if (NDOF == 1) {
+          // SH: mu = m0
+          const float cxx = -(wdtj * xix) * xix, czz = -(wdti * etaz) * etaz;
+          B[0][j][i] = (cxx * w[i]) * (m0[i] * B[0][j][i]);
+          A[0][j][i] = (czz * w[j]) * (m0[i] * A[0][j][i]);
+        } else {
+          // P-SV: la = m0, mu = m1
           const float la = m0[i], mu = m1[i];
           const float K = la + 2.f * mu;
           const float gxx = B[0][j][i], gxz = B[1][j][i], gex = A[0][j][i], gez = A[1][j][i];
-          const float cA = -(det * w[i]) * etaz;
-          const float xc = cA * xix, ec = cA * etaz, sc = cA * sxz;
-          B[0][j][i] = (xr * K) * gxx + (er * la) * gez;
-          B[1][j][i] = mu * (er * gex + xr * gxz);
-          A[0][j][i] = mu * (ec * gex + sc * gxz);
-          A[1][j][i] = (xc * la) * gxx + (ec * K) * gez;
-        }
-      } else {
-        // P-SV, moduli constant over the element: row-folded coefficients
-        const float b0x = rB * cKx, b0z = rB * cLz, b1e = rB * cMz, b1x = rB * cMx;
-#pragma unroll
-        for (int i = 0; i < N; ++i) {
-          const float gxx = B[0][j][i], gxz = B[1][j][i], gex = A[0][j][i], gez = A[1][j][i];
-          const float cA = -(det * w[i]) * etaz;
-          B[0][j][i] = b0x * gxx + b0z * gez;
-          B[1][j][i] = b1e * gex + b1x * gxz;
-          A[0][j][i] = cA * (cMz * gex + cMs * gxz);
-          A[1][j][i] = cA * (cLx * gxx + cKz * gez);
+          const float dxux = xix * gxx, dxuz = xix * gxz, dzux = etaz * gex, dzuz = etaz * gez;
+          const float wc = -(wdtj * xix) * w[i];
+          const float wr = -(wdti * etaz) * w[j];
+          const float sxz = kd2 ? etaz : xix;
+          B[0][j][i] = wc * (K * dxux + la * dzuz);
+          B[1][j][i] = wc * (mu * (dzux + dxuz));
+          A[0][j][i] = wr * (mu * (dzux + sxz * gxz));
+          A[1][j][i] = wr * (la * dxux + K * dzuz);
         }
       }
     }
-    // divergence, both parts in one chain: F(i,j) = sum_q Hw[i + N q] B(q,j)
-    // + sum_q A(i,q) Hw[j + N q]; row by row into B (row j of A is not read
-    // after row j of B is written: the row part reads A only)
+    // divergence: column part sum_q H[i + N q] B(q,j) row by row in place
 #pragma unroll
     for (int c = 0; c < NDOF; ++c)
 #pragma unroll
@@ -312,16 +286,26 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float t[N];
 #pragma unroll
         for (int i = 0; i < N; ++i) {
-          float a = Hw[i + N * 0] * B[c][j][0];
+          float a = H[i + N * 0] * B[c][j][0];
 #pragma unroll
-          for (int q = 1; q < N; ++q) a = a + Hw[i + N * q] * B[c][j][q];
-#pragma unroll
-          for (int q = 0; q < N; ++q) a = a + A[c][q][i] * Hw[j + N * q];
+          for (int q = 1; q < N; ++q) a = a + H[i + N * q] * B[c][j][q];
           t[i] = a;
         }
 #pragma unroll
         for (int i = 0; i < N; ++i) B[c][j][i] = t[i];
       }
+    // plus the row part sum_q A(i,q) H[j + N q]: nodal forces into B
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c)
+#pragma unroll
+      for (int i = 0; i < N; ++i)
+#pragma unroll
+        for (int j = 0; j < N; ++j) {
+          float a = A[c][0][i] * H[j + N * 0];
+#pragma unroll
+          for (int q = 1; q < N; ++q) a = a + A[c][q][i] * H[j + N * q];
+          B[c][j][i] = B[c][j][i] + a;
+        }
 
     // ---- assembly: forces of the left element on column 0 ----
     float L[NDOF][N];
@@ -425,7 +409,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
 #pragma unroll
         for (int i = 0; i < N; ++i) {
           const int I = I0 + i;
-          if (!per_row || (i == N - 1 && !last_col)) continue;
+          if (i == N - 1 && !last_col) continue;
           if (edgeJ || I == 0 || I == p.LX - 1) {
             const int sp = perimeter_slot(I, J, p.LX, p.LZ);
 #pragma unroll
@@ -465,7 +449,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           for (int i = 0; i < N; ++i) {
             float rm = rmv[i];
             const int I = I0 + i;
-            if (c == 1 && per_row && (edgeJ || I == 0 || I == p.LX - 1) && (i < N - 1 || last_col))
+            if (c == 1 && (edgeJ || I == 0 || I == p.LX - 1) && (i < N - 1 || last_col))
               rm = p.per_rm[nslot + perimeter_slot(I, J, p.LX, p.LZ)];
             const float a = rm * f[c][i];
             an[i] = a;
@@ -536,7 +520,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (uid < nunits) {
     const MarchUnit u = units[uid];
-    march_unit<NDOF, MAT, FST>(p, p.H, p.w, p.Hw, u, it);
+    march_unit<NDOF, MAT, FST>(p, p.H, p.w, u, it);
   }
   march_done(p.step, p.done, it);
 }
@@ -551,7 +535,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   if (uid < b.nunits) {
     const MarchUnit u = b.units[uid];
-    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, b.Hw, u, it);
+    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, u, it);
   }
   march_done(b.step, b.done, it);
 }
@@ -567,7 +551,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
                             int nrows) {
   const int warp = threadIdx.x >> 5, s = blockIdx.x;
   const int it = *p.step + 1;
-  if (warp < nrows) march_unit<NDOF, MAT, FST>(p, p.H, p.w, p.Hw, units[warp * nstrips + s], it);
+  if (warp < nrows) march_unit<NDOF, MAT, FST>(p, p.H, p.w, units[warp * nstrips + s], it);
   __syncthreads();  // the strip's fault-row forces are written (global memory, this block)
   const int t = threadIdx.x, I = 4 * kMarchCols * s + t;
   const bool mine = (t < 4 * kMarchCols && I < p.LX) || (t == 4 * kMarchCols && I == p.LX - 1);

@@ -84,7 +84,6 @@ struct BulkParams {
   // GLL operator
   real H[N * N];    // H(i,j) = h'_i(x_j), column-major
   real w[N];
-  real Hw[N * N];   // Hw[i + N q] = H[i + N q] w[q] (the march kernel's divergence)
   // state (ping-pong buffers chosen by the host)
   const real *Dcur;
   real *Dnext;

@@ -89,7 +89,11 @@ try:
         """sis = F(rho, vp, vs) on the GPU; backward = the discrete adjoint.
 
         Inputs are (LZ, LX) FP64 tensors on any device; the output is the
-        (rec_nsamp, nrec, ndof) seismogram tensor (FP64, CPU).
+        (rec_nsamp, nrec, ndof) seismogram tensor (FP64, CPU).  The forward
+        keeps its GPU handle (with the checkpoints) in the autograd graph
+        until the backward, which releases it: each forward supports one
+        backward, and a forward without backward holds the handle until the
+        graph is freed.
         """
 
         @staticmethod
@@ -112,12 +116,19 @@ try:
 
         @staticmethod
         def backward(ctx, grad_sis):
-            resid = np.asfortranarray(grad_sis.detach().cpu().numpy(), dtype=np.float64)
+            # the adjoint consumes the handle's checkpoints: one backward per
+            # forward (retain_graph does not make a second one possible)
+            if ctx.sim is None:
+                raise RuntimeError("SeismogramFunction supports one backward per forward: its GPU state "
+                                   "was released by the first")
             g = [np.zeros(ctx.npoin) for _ in range(3)]
             pp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
             sim = ctx.sim
-            sim._check(lib().sem2d_gpu_adjoint(sim.h, pp(resid), pp(g[0]), pp(g[1]), pp(g[2])))
-            sim.close()
+            try:
+                sim._check(lib().sem2d_gpu_adjoint(sim.h, pp(resid), pp(g[0]), pp(g[1]), pp(g[2])))
+            finally:
+                sim.close()
+                ctx.sim = None
             out = [torch.from_numpy(ctx.model.to_lattice(x)).to(ctx.device) for x in g]
             return out[0], out[1], out[2], None, None, None
 

@@ -223,8 +223,8 @@ def write_snapshot(path, solver, index, fields="V", grid=None):
     accelerations (Newmark, HHT-alpha or 'A' receivers).  S of a
     Kelvin-Voigt material is the stress of d + eta v, as the reference's
     (MAT_stress_dv, mat_gen.f90:626-641).  The divergence and curl of the
-    velocity (d, c; P-SV only, MAT_divcurl_PSV, mat_gen.f90:802-825) need
-    the Grid of the problem."""
+    velocity (d, c; MAT_divcurl_PSV, mat_gen.f90:802-825) need the Grid of
+    a P-SV problem and are skipped for SH, as the reference skips them."""
     d = solver.desc
     fields = str(fields)
     bad = set(fields) - set("DVAESdc")
@@ -243,9 +243,11 @@ def write_snapshot(path, solver, index, fields="V", grid=None):
             for k, comp in enumerate(comps):
                 np.ascontiguousarray(byname[c][:, k], dtype="<f4").tofile(
                     os.path.join(path, "%s%s_%s_sem2d.dat" % (c.lower(), comp, tag)))
-    if "d" in fields or "c" in fields:
-        if d.ndof != 2 or grid is None:
-            raise ValueError("div/curl snapshots need a P-SV problem and its Grid")
+    if ("d" in fields or "c" in fields) and d.ndof == 2:
+        # an SH problem has no divergence or curl: the reference drops them
+        # (plot_gen.f90:100), and so does this writer
+        if grid is None:
+            raise ValueError("div/curl snapshots of a P-SV problem need its Grid")
         _write_divcurl(path, tag, solver.fields()[1], grid, fields)
     if "E" in fields or "S" in fields:
         strain, stress = solver.strain_stress()  # (ngll, ngll, ndof+1, nelem)

@@ -267,6 +267,25 @@ def test_divcurl_snapshot_of_a_linear_velocity(tmp_path):
     np.testing.assert_allclose(curl, b - c, rtol=1e-5)
 
 
+def test_sh_snapshot_skips_div_curl(tmp_path):
+    """An SH problem has no divergence or curl: asked for them, the writer
+    skips them as the reference does (plot_gen.f90:100) and writes the rest."""
+    P = Problem(workloads.sh_rupture(scale=0.05, nsteps=10)[0])
+    d = P.desc()
+    v = np.ones((d.npoin, 1))
+
+    class Run:
+        desc = d
+
+        def fields(self, accel=False):
+            return np.zeros_like(v), v
+
+    outputs.write_snapshot(str(tmp_path), Run(), 1, "Vdc")
+    assert (tmp_path / "vy_001_sem2d.dat").exists()
+    assert not (tmp_path / "div_001_sem2d.dat").exists()
+    assert not (tmp_path / "curl_001_sem2d.dat").exists()
+
+
 def test_hht_alpha_time_block():
     d = deck_from_parinp("&TIME TotalTime=1d0, courant=0.3d0, kind='HHT-alpha' / &TIME_HHTA alpha=0.6d0, rho=0.9d0 /")
     assert (d.time.kind, d.time.alpha, d.time.rho) == ("hht-alpha", 0.6, 0.9)
