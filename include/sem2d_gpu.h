@@ -57,6 +57,43 @@ extern "C" {
 #define SEM2D_PRECISION_FP64 0  /* everything in FP64                       */
 #define SEM2D_PRECISION_MIXED 1 /* FP32 fields/forces, FP64 fault state     */
 
+/* source time functions, numbered as stf_gen.f90:23-29 (the reference's
+ * BUTTERWORTH aborts as not implemented, butterworth_filter.f90:27-43,
+ * and has no number here) */
+#define SEM2D_STF_NONE 0
+#define SEM2D_STF_RICKER 1
+#define SEM2D_STF_TAB 3
+#define SEM2D_STF_HARMONIC 4
+#define SEM2D_STF_BRUNE 5
+#define SEM2D_STF_GAUSSIAN 6
+#define SEM2D_STF_USER 7
+
+/* incident plane wave phases (&SRC_WAVE phase, src_wave.f90:56-110) */
+#define SEM2D_WAVE_NONE 0
+#define SEM2D_WAVE_P 1
+#define SEM2D_WAVE_S 2 /* also the SH wave of ndof = 1                  */
+
+/* A source time function (STF_get, stf_gen.f90:99-121), with the values
+ * as the reference holds them (the parameters that &STF_GAUSSIAN,
+ * &STF_HARMONIC and &STF_USER read into REAL variables are already
+ * rounded to FP32 by the caller):
+ *   RICKER    -ampli (1 - 2 a) exp(-a), a = (pi f0 (t - onset))^2
+ *             (stf_ricker.f90:89-103)
+ *   GAUSSIAN  ampli exp(-a)                         (stf_gaussian.f90:76-86)
+ *   BRUNE     ampli (1 - (1 + b) exp(-b)), b = 2 pi f0 max(t, 0)
+ *             (f0 is the corner frequency fc, stf_brune.f90:73-83)
+ *   HARMONIC  ampli sin(2 pi f0 t)                  (stf_harmonic.f90:68-77)
+ *   USER      ampli sin(t - onset) + par1 (t - onset)^2 (stf_user.f90:110-122)
+ *   TAB       cubic spline through (tab_t, tab_v) with zero end slopes,
+ *             t clamped to [tab_t[0], tab_t[ntab-1]]
+ *             (stf_tabulated.f90:52-95, utils.f90:652-734) */
+typedef struct sem2d_stf {
+  int kind; /* SEM2D_STF_*                                                */
+  int ntab; /* TAB: rows, >= 2, tab_t increasing                          */
+  double f0, onset, ampli, par1, par2;
+  const double *tab_t, *tab_v;
+} sem2d_stf;
+
 typedef struct sem2d_problem_desc {
   /* ---- sizes (spec_grid.f90:49-64, fields.f90:7-11) ---- */
   int ngll;  /* GLL nodes per element edge                        */
@@ -227,6 +264,45 @@ typedef struct sem2d_problem_desc {
    * SEM2D_E_NAN when either is not finite; 0 selects 100, a negative value
    * switches the check off.  sem2d_gpu_get_info returns the last values. */
   int info_every;
+
+  /* ---- time function of the point sources (SO_add, src_gen.f90:290-317):
+   * NULL keeps the Ricker of src_f0, src_t0, src_ampli; otherwise source s
+   * adds src_relamp[s] * STF_get(src_stf, t - src_tdelay[s]) and src_f0,
+   * src_t0, src_ampli are not read. */
+  const sem2d_stf *src_stf;
+
+  /* ---- incident plane wave (src_wave.f90:128-224, SO_WAVE_get_VT
+   * src_gen.f90:322-339), entering across the absorbing entries with
+   * abs_wave[k] = 1 (let_wave on a flat side, bc_abso.f90:245-256).  Entry k
+   * at node x receives (BC_ABSO_apply, bc_abso.f90:299-306)
+   *     + C_k Vin + B_k Tin,   Vin, Tin = STF_get(wave_stf, phase) (P, T(n_k))
+   * with phase = t - (x - wave_ref).k/c - wave_tdelay, k = (-sin a, cos a)
+   * for the angle a, c = wave_cp (P) or wave_cs (S, SH), the polarisation
+   * P = k (P), (cos a, sin a) (S), 1 (SH), and the traction per unit
+   * amplitude T(n) = -(lambda (k.P) n + mu ((P.n) k + (k.n) P)) / c
+   * (SH: -mu (k.n) / cs).  The material values are those of the reference
+   * point (WAVE_init, src_wave.f90:128-180). */
+  int wave_phase;         /* SEM2D_WAVE_*                                  */
+  double wave_angle;      /* degrees, in [-180, 180]                       */
+  double wave_ref[2];     /* reference point (x, z)                        */
+  double wave_cp, wave_cs, wave_mu, wave_lambda;
+  double wave_tdelay;
+  const sem2d_stf *wave_stf;
+  const double *abs_B;    /* [nabs] boundary weights w |J1D| (spec_grid.f90:961-1011) */
+  const double *abs_n;    /* abs_n(nabs,2) outward unit normal              */
+  const int *abs_wave;    /* [nabs] 1 where the wave enters, or NULL       */
+
+  /* ---- time-dependent Neumann tractions of &BC_DIRNEU hstf / vstf
+   * (bc_DIRNEU_apply, bc_dirneu.f90:148-169): force component neu_comp[k]
+   * at node neu_node[k] receives neu_B[k] * STF_get(neu_stfs[neu_stf[k]], t).
+   * A (node, component) may not also be a zero-Dirichlet entry. */
+  int nneu;
+  const int *neu_node;    /* [nneu], 1-based                                */
+  const int *neu_comp;    /* [nneu], 0 horizontal (SH: the only one), 1 vertical */
+  const double *neu_B;    /* [nneu] boundary weights                        */
+  const int *neu_stf;     /* [nneu] index into neu_stfs                     */
+  int nneu_stf;
+  const sem2d_stf *neu_stfs;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;

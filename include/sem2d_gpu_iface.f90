@@ -37,7 +37,30 @@ module sem2d_gpu_iface
   integer(c_int), parameter :: SEM2D_FRICTION_TWF = 3
   integer(c_int), parameter :: SEM2D_PRECISION_FP64 = 0
   integer(c_int), parameter :: SEM2D_PRECISION_MIXED = 1
+  integer(c_int), parameter :: SEM2D_STF_NONE = 0
+  integer(c_int), parameter :: SEM2D_STF_RICKER = 1
+  integer(c_int), parameter :: SEM2D_STF_TAB = 3
+  integer(c_int), parameter :: SEM2D_STF_HARMONIC = 4
+  integer(c_int), parameter :: SEM2D_STF_BRUNE = 5
+  integer(c_int), parameter :: SEM2D_STF_GAUSSIAN = 6
+  integer(c_int), parameter :: SEM2D_STF_USER = 7
+  integer(c_int), parameter :: SEM2D_WAVE_NONE = 0
+  integer(c_int), parameter :: SEM2D_WAVE_P = 1
+  integer(c_int), parameter :: SEM2D_WAVE_S = 2
   integer(c_int), parameter :: SEM2D_NOALLOC_SCRATCH_BYTES = 8388608
+
+  ! a source time function (STF_get, stf_gen.f90:99-121)
+  type, bind(C) :: sem2d_stf
+    integer(c_int)         :: kind
+    integer(c_int)         :: ntab
+    real(c_double)         :: f0
+    real(c_double)         :: onset
+    real(c_double)         :: ampli
+    real(c_double)         :: par1
+    real(c_double)         :: par2
+    type(c_ptr)            :: tab_t
+    type(c_ptr)            :: tab_v
+  end type sem2d_stf
 
   type, bind(C) :: sem2d_problem_desc
     integer(c_int)         :: ngll
@@ -149,6 +172,26 @@ module sem2d_gpu_iface
     type(c_ptr)            :: perio_slave
     integer(c_int)         :: flt_nr_maxit
     integer(c_int)         :: info_every
+    type(c_ptr)            :: src_stf
+    integer(c_int)         :: wave_phase
+    real(c_double)         :: wave_angle
+    real(c_double)         :: wave_ref(2)
+    real(c_double)         :: wave_cp
+    real(c_double)         :: wave_cs
+    real(c_double)         :: wave_mu
+    real(c_double)         :: wave_lambda
+    real(c_double)         :: wave_tdelay
+    type(c_ptr)            :: wave_stf
+    type(c_ptr)            :: abs_B
+    type(c_ptr)            :: abs_n
+    type(c_ptr)            :: abs_wave
+    integer(c_int)         :: nneu
+    type(c_ptr)            :: neu_node
+    type(c_ptr)            :: neu_comp
+    type(c_ptr)            :: neu_B
+    type(c_ptr)            :: neu_stf
+    integer(c_int)         :: nneu_stf
+    type(c_ptr)            :: neu_stfs
   end type sem2d_problem_desc
 
   type, bind(C) :: sem2d_lattice_args

@@ -63,6 +63,12 @@ typedef struct sem2d_bc {
   int tag[2];
   int stacey; /* &BC_ABSORB stacey (bc_abso.f90:55-100); P-SV only        */
   int dirichlet; /* &BC_DIRNEU: bit 0 h='D', bit 1 v='D' (bc_dirneu.f90:50-112) */
+  int let_wave;  /* &BC_ABSORB let_wave (default T): an incident wave of
+                  * the sources enters across this side                  */
+  /* &BC_DIRNEU hstf, vstf: time functions of the horizontal and vertical
+   * tractions of a Neumann component (kind SEM2D_STF_NONE: none; a
+   * Dirichlet component ignores its own, bc_dirneu.f90:70-101)          */
+  sem2d_stf hstf, vstf;
 } sem2d_bc;
 
 /* Per-node fault inputs of &BC_DYNFLT, &BC_DYNFLT_SWF and &BC_DYNFLT_RSF */
@@ -122,7 +128,7 @@ typedef struct sem2d_deck {
   double beta, gamma; /* &TIME_NEWMARK                                      */
   double hht_alpha, hht_rho; /* &TIME_HHTA alpha, rho (time.f90:222-240)     */
 
-  /* &SRC_DEF (FORCE mechanism, RICKER time function) */
+  /* &SRC_DEF (mechanism and time function: src_mech and stf below) */
   int nsrc;
   const double *src_coord;  /* (2,nsrc) requested positions                */
   const double *src_tdelay; /* [nsrc] or NULL                              */
@@ -159,6 +165,15 @@ typedef struct sem2d_deck {
   int src_mech;
   double src_M[4];
   double src_dip;
+  /* &SRC_DEF stf (stf_gen.f90:45-97): kind SEM2D_STF_NONE or RICKER uses
+   * ricker_f0, ricker_onset, ricker_ampli; the other kinds carry their
+   * &STF_* values as written in the input (the builder rounds the ones the
+   * reference reads as REAL) */
+  sem2d_stf stf;
+  /* &SRC_WAVE angle, phase (src_wave.f90:56-110) for src_mech = 4 (WAVE):
+   * phase SEM2D_WAVE_P or SEM2D_WAVE_S (ignored in SH) */
+  double wave_angle;
+  int wave_phase;
 } sem2d_deck;
 
 typedef struct sem2d_grid sem2d_grid;
@@ -202,7 +217,7 @@ int sem2d_abi_struct_sizes(int *desc_size, int *deck_size);
 
 /* Offsets (bytes) of every member of a C-ABI structure as compiled, in
  * declaration order: which = 0 sem2d_problem_desc, 1 sem2d_deck,
- * 2 sem2d_lattice_args.  Writes min(n, count) offsets when offsets is not
+ * 2 sem2d_lattice_args, 3 sem2d_stf.  Writes min(n, count) offsets when offsets is not
  * NULL and returns the member count (SEM2D_E_ARG for an unknown which). */
 int sem2d_abi_field_offsets(int which, long long *offsets, int n);
 

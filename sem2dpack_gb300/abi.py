@@ -29,6 +29,20 @@ FRICTION_TWF = 3
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
 
+STF_NONE = 0
+STF_RICKER = 1
+STF_TAB = 3
+STF_HARMONIC = 4
+STF_BRUNE = 5
+STF_GAUSSIAN = 6
+STF_USER = 7
+STF_KINDS = {"RICKER": STF_RICKER, "TAB": STF_TAB, "HARMONIC": STF_HARMONIC,
+             "BRUNE": STF_BRUNE, "GAUSSIAN": STF_GAUSSIAN, "USER": STF_USER}
+
+WAVE_NONE = 0
+WAVE_P = 1
+WAVE_S = 2
+
 BC_ABSORB = 1
 BC_DYNFLT = 2
 BC_DIRNEU = 3
@@ -51,6 +65,17 @@ FP_DEFAULTS = {"Tt": 0.0, "Tn": 0.0, "Sxx": 0.0, "Sxy": 0.0, "Sxz": 0.0, "Syz": 
                "swf_dc": 0.5, "swf_mus": 0.6, "swf_mud": 0.5, "swf_p": 3.0, "swf_alpha": 0.0,
                "rsf_dc": 0.5, "rsf_mus": 0.6, "rsf_a": 0.01, "rsf_b": 0.02, "rsf_vstar": 1.0,
                "rsf_theta": 0.0, "rsf_vc": 1e-6}
+
+
+class Stf(C.Structure):
+    """sem2d_stf: a source time function (STF_get, stf_gen.f90:99-121)."""
+    _fields_ = [("kind", c_int), ("ntab", c_int),
+                ("f0", c_double), ("onset", c_double), ("ampli", c_double),
+                ("par1", c_double), ("par2", c_double),
+                ("tab_t", P_double), ("tab_v", P_double)]
+
+
+P_Stf = C.POINTER(Stf)
 
 
 class ProblemDesc(C.Structure):
@@ -100,6 +125,13 @@ class ProblemDesc(C.Structure):
         ("alpha", c_double),
         ("nperio", c_int), ("perio_master", P_int), ("perio_slave", P_int),
         ("flt_nr_maxit", c_int), ("info_every", c_int),
+        ("src_stf", P_Stf),
+        ("wave_phase", c_int), ("wave_angle", c_double), ("wave_ref", c_double * 2),
+        ("wave_cp", c_double), ("wave_cs", c_double), ("wave_mu", c_double),
+        ("wave_lambda", c_double), ("wave_tdelay", c_double), ("wave_stf", P_Stf),
+        ("abs_B", P_double), ("abs_n", P_double), ("abs_wave", P_int),
+        ("nneu", c_int), ("neu_node", P_int), ("neu_comp", P_int), ("neu_B", P_double),
+        ("neu_stf", P_int), ("nneu_stf", c_int), ("neu_stfs", P_Stf),
     ]
 
 
@@ -116,7 +148,8 @@ class Material(C.Structure):
 
 
 class BC(C.Structure):
-    _fields_ = [("kind", c_int), ("tag", c_int * 2), ("stacey", c_int), ("dirichlet", c_int)]
+    _fields_ = [("kind", c_int), ("tag", c_int * 2), ("stacey", c_int), ("dirichlet", c_int),
+                ("let_wave", c_int), ("hstf", Stf), ("vstf", Stf)]
 
 
 class Deck(C.Structure):
@@ -154,6 +187,7 @@ class Deck(C.Structure):
         ("twf_T", c_double), ("twf_Dc", c_double),
         ("flt_potency", c_int),
         ("src_mech", c_int), ("src_M", c_double * 4), ("src_dip", c_double),
+        ("stf", Stf), ("wave_angle", c_double), ("wave_phase", c_int),
     ]
 
 

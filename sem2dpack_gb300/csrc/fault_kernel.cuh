@@ -454,6 +454,7 @@ struct PerioParams {
   real *Dnext, *Vnext, *Anext;
   const real *per_rm, *per_Ca, *per_Cb;
   const int *per_dir;
+  BoundaryForces bf;
   real dt, cv, cpred, cpa, cd2, cb;
   int jf1, jf2, has_fault, two;
   const int *step;
@@ -461,7 +462,7 @@ struct PerioParams {
 
 template <typename real>
 __device__ __forceinline__ real perio_boundary(const PerioParams<real> &p, int I, int J, int c, real fc, real *vpred,
-                                               real *rm) {
+                                               real *rm, int it) {
   const long long g = c * p.plane + (long long)J * p.pitch + I;
   real vp = p.Vcur[g], vd = vp;
   if (p.scheme != 0) {
@@ -472,6 +473,7 @@ __device__ __forceinline__ real perio_boundary(const PerioParams<real> &p, int I
   const int sp = perimeter_slot(I, J, p.LX, p.LZ), so = c * p.nslot + sp;
   fc = fc - p.per_Ca[so] * vd;
   fc = fc - p.per_Cb[so] * vd;
+  if (p.bf.W) fc = fc + real(boundary_force(p.bf, p.ndof, p.nslot, sp, c, it));
   if (p.per_dir && ((p.per_dir[sp] >> c) & 1)) fc = real(0);
   *vpred = vp;
   *rm = p.per_rm[so];
@@ -491,10 +493,10 @@ __global__ void perio_kernel(const PerioParams<real> p, FaultParams<real> flt) {
       for (int c = 0; c < p.ndof; ++c) {
         real vp, rm;
         const real s1 = p.pf[(size_t(c) * p.LZ + p.jf1) * 2] + p.pf[(size_t(c) * p.LZ + p.jf1) * 2 + 1];
-        f1[c] = double(perio_boundary(p, I, p.jf1, c, s1, &vp, &rm));
+        f1[c] = double(perio_boundary(p, I, p.jf1, c, s1, &vp, &rm, it));
         if (p.two) {
           const real s2 = p.pf[(size_t(c) * p.LZ + p.jf2) * 2] + p.pf[(size_t(c) * p.LZ + p.jf2) * 2 + 1];
-          f2[c] = double(perio_boundary(p, I, p.jf2, c, s2, &vp, &rm));
+          f2[c] = double(perio_boundary(p, I, p.jf2, c, s2, &vp, &rm, it));
         }
       }
       fault_node_update(flt, I, it, f1, f2);
@@ -507,7 +509,7 @@ __global__ void perio_kernel(const PerioParams<real> p, FaultParams<real> flt) {
       const long long g = c * p.plane + (long long)J * p.pitch + I;
       real vp, rm;
       const real s = p.pf[(size_t(c) * p.LZ + J) * 2] + p.pf[(size_t(c) * p.LZ + J) * 2 + 1];
-      const real fc = perio_boundary(p, I, J, c, s, &vp, &rm);
+      const real fc = perio_boundary(p, I, J, c, s, &vp, &rm, it);
       const real a = rm * fc;
       const real vnew = vp + p.cv * a;
       real dcur = p.Dcur[g];

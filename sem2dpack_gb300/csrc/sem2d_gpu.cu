@@ -82,6 +82,9 @@ struct sem2d_handle {
   // periodic columns I = 0 and LX-1: raw forces left by the step kernel
   int nperio = 0;
   void *perio_f = nullptr;
+  // perimeter forces with their own time functions: the incident plane
+  // wave and the time-dependent Neumann tractions (bf.W null: none)
+  BoundaryForces bf;
   int *d_row0 = nullptr, *d_step = nullptr, *d_error = nullptr;
   unsigned *d_done = nullptr;
   // sources
@@ -526,6 +529,158 @@ int upload_perio(sem2d_handle *h, const sem2d_problem_desc *d) {
   return upload_real(h, &h->perio_f, std::vector<double>((size_t)2 * h->ndof * h->LZ, 0.0));
 }
 
+// A time function on the device: the TAB rows and their spline second
+// derivatives are copied; host_v2 (optional) receives the derivatives for
+// an evaluation on the host.
+int upload_stf(sem2d_handle *h, const sem2d_stf &s, StfDev *out, std::vector<double> *host_v2 = nullptr) {
+  if (const char *m = stf_check(s)) return set_err(h, SEM2D_E_ARG, m);
+  StfDev q{};
+  q.kind = s.kind;
+  q.ntab = s.ntab;
+  q.f0 = s.f0;
+  q.onset = s.onset;
+  q.ampli = s.ampli;
+  q.par1 = s.par1;
+  q.par2 = s.par2;
+  if (s.kind == SEM2D_STF_TAB) {
+    const std::vector<double> t(s.tab_t, s.tab_t + s.ntab), v(s.tab_v, s.tab_v + s.ntab);
+    const std::vector<double> v2 = stf_spline_d2(s.tab_t, s.tab_v, s.ntab);
+    double *dt_ = nullptr, *dv = nullptr, *dv2 = nullptr;
+    int st;
+    if ((st = dupload(h, &dt_, t)) || (st = dupload(h, &dv, v)) || (st = dupload(h, &dv2, v2))) return st;
+    q.t = dt_;
+    q.v = dv;
+    q.v2 = dv2;
+    if (host_v2) *host_v2 = v2;
+  }
+  *out = q;
+  return SEM2D_OK;
+}
+
+// The incident plane wave (SRC_WAVE_get_VT src_wave.f90:190-224, phase
+// :181-187, SO_WAVE_get_VT src_gen.f90:322-339) and the Neumann tractions
+// (bc_DIRNEU_apply bc_dirneu.f90:157-167) as perimeter entries: weight,
+// time function and time shift per (slot, entry, component).
+int upload_boundary_forces(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const bool wave = d->wave_phase != SEM2D_WAVE_NONE && d->nabs > 0 && d->abs_wave;
+  if (!wave && d->nneu <= 0) return SEM2D_OK;
+  const int nd = h->ndof, np = d->npoin, nslot = perimeter_slots(h->LX, h->LZ);
+  std::vector<double> W((size_t)2 * nd * nslot, 0.0), phi((size_t)2 * nslot, 0.0);
+  std::vector<signed char> fn((size_t)2 * nd * nslot, -1);
+  std::vector<int> used(nslot, 0);
+  std::vector<StfDev> stfs;
+  auto slot_of = [&](int node1) {
+    const int p = node1 - 1;
+    if (p < 0 || p >= np) return -2;
+    const long long L = h->glob2lat[p];
+    return perimeter_slot(int(L % h->pitch), int(L / h->pitch), h->LX, h->LZ);
+  };
+  if (wave) {
+    if (d->wave_phase != SEM2D_WAVE_P && d->wave_phase != SEM2D_WAVE_S)
+      return set_err(h, SEM2D_E_ARG, "wave_phase must be SEM2D_WAVE_P or SEM2D_WAVE_S");
+    if (!d->wave_stf || !d->abs_B || !d->abs_n) return set_err(h, SEM2D_E_ARG, "incident wave without wave_stf, abs_B or abs_n");
+    if (!(d->wave_cp > 0) || !(d->wave_cs > 0)) return set_err(h, SEM2D_E_ARG, "incident wave needs cp > 0 and cs > 0");
+    if (!d->coord) return set_err(h, SEM2D_E_ARG, "incident wave without node coordinates");
+    StfDev q;
+    int st = upload_stf(h, *d->wave_stf, &q);
+    if (st) return st;
+    const signed char qi = (signed char)stfs.size();
+    stfs.push_back(q);
+    const double kPi = 3.141592653589793, a = kPi * d->wave_angle / 180.0;
+    const double k0 = -std::sin(a), k1 = std::cos(a);  // WAVE_init, src_wave.f90:163-172
+    const bool P = d->wave_phase == SEM2D_WAVE_P;
+    const double p0 = P ? -std::sin(a) : std::cos(a), p1 = P ? std::cos(a) : std::sin(a);
+    const double c = P ? d->wave_cp : d->wave_cs;
+    const double s0 = k0 / c, s1 = k1 / c;
+    const double mu = d->wave_mu, lam = d->wave_lambda, cp = d->wave_cp, cs = d->wave_cs;
+    for (int k = 0; k < d->nabs; ++k) {
+      if (!d->abs_wave[k]) continue;
+      const int sp = slot_of(d->abs_node[k]);
+      if (sp < 0) return set_err(h, SEM2D_E_ARG, "absorbing node out of range");
+      if (used[sp] >= 2) return set_err(h, SEM2D_E_UNSUPPORTED, "more than two boundary forces at a node");
+      const int e = used[sp]++;
+      const double n0 = d->abs_n[k], n1 = d->abs_n[k + d->nabs], B = d->abs_B[k];
+      const double KN = k0 * n0 + k1 * n1;
+      double V[2], T[2];
+      if (nd == 1) {
+        V[0] = 1.0;
+        T[0] = -mu / cs * KN;
+      } else {
+        V[0] = p0;
+        V[1] = p1;
+        if (P) {
+          T[0] = -1.0 / cp * (lam * n0 + 2.0 * mu * KN * k0);
+          T[1] = -1.0 / cp * (lam * n1 + 2.0 * mu * KN * k1);
+        } else {
+          const double PN = p0 * n0 + p1 * n1;
+          T[0] = -mu / cs * (PN * k0 + KN * p0);
+          T[1] = -mu / cs * (PN * k1 + KN * p1);
+        }
+      }
+      for (int cc = 0; cc < nd; ++cc) {
+        const size_t ei = ((size_t)e * nd + cc) * nslot + sp;
+        W[ei] = d->abs_C[k + (size_t)d->nabs * cc] * V[cc] + B * T[cc];
+        fn[ei] = qi;
+      }
+      const int pn = d->abs_node[k] - 1;
+      phi[(size_t)e * nslot + sp] =
+          (d->coord[2 * (size_t)pn] - d->wave_ref[0]) * s0 + (d->coord[2 * (size_t)pn + 1] - d->wave_ref[1]) * s1 +
+          d->wave_tdelay;
+    }
+  }
+  if (d->nneu > 0) {
+    if (!d->neu_node || !d->neu_comp || !d->neu_B || !d->neu_stf || !d->neu_stfs || d->nneu_stf <= 0)
+      return set_err(h, SEM2D_E_ARG, "incomplete Neumann traction arrays");
+    if (d->nneu_stf > 100) return set_err(h, SEM2D_E_UNSUPPORTED, "too many traction time functions");
+    const signed char q0 = (signed char)stfs.size();
+    for (int k = 0; k < d->nneu_stf; ++k) {
+      StfDev q;
+      int st = upload_stf(h, d->neu_stfs[k], &q);
+      if (st) return st;
+      stfs.push_back(q);
+    }
+    for (int k = 0; k < d->nneu; ++k) {
+      const int sp = slot_of(d->neu_node[k]);
+      if (sp == -2) return set_err(h, SEM2D_E_ARG, "traction node out of range");
+      if (sp < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "traction node inside the domain");
+      const int cc = d->neu_comp[k], qk = d->neu_stf[k];
+      if (cc < 0 || cc >= nd) return set_err(h, SEM2D_E_ARG, "traction component out of range");
+      if (qk < 0 || qk >= d->nneu_stf) return set_err(h, SEM2D_E_ARG, "traction time function out of range");
+      for (int j = 0; j < d->ndir; ++j)
+        if (d->dir_node && d->dir_comp && d->dir_node[j] == d->neu_node[k] && d->dir_comp[j] == cc)
+          return set_err(h, SEM2D_E_UNSUPPORTED, "a Neumann traction on a zero-Dirichlet component");
+      const long long L = h->glob2lat[d->neu_node[k] - 1];
+      if (h->nflt && (L / h->pitch == h->jf1 || L / h->pitch == h->jf2))
+        return set_err(h, SEM2D_E_UNSUPPORTED, "a Neumann traction on a fault node");
+      // an entry of the slot without time shift and free for this component
+      int e = -1;
+      for (int j = 0; j < used[sp]; ++j)
+        if (phi[(size_t)j * nslot + sp] == 0.0 && fn[((size_t)j * nd + cc) * nslot + sp] < 0) e = j;
+      if (e < 0) {
+        if (used[sp] >= 2) return set_err(h, SEM2D_E_UNSUPPORTED, "more than two boundary forces at a node");
+        e = used[sp]++;
+      }
+      const size_t ei = ((size_t)e * nd + cc) * nslot + sp;
+      W[ei] = d->neu_B[k];
+      fn[ei] = (signed char)(q0 + qk);
+    }
+  }
+  double *dW = nullptr, *dphi = nullptr;
+  signed char *dfn = nullptr;
+  StfDev *dstf = nullptr;
+  int st;
+  if ((st = dupload(h, &dW, W)) || (st = dupload(h, &dphi, phi)) || (st = dupload(h, &dfn, fn)) ||
+      (st = dupload(h, &dstf, stfs)))
+    return st;
+  h->bf.W = dW;
+  h->bf.fn = dfn;
+  h->bf.phi = dphi;
+  h->bf.stf = dstf;
+  h->bf.dt = h->dt;
+  h->bf.tshift = (h->alpha - 1.0) * h->dt;
+  return SEM2D_OK;
+}
+
 int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
   const int nd = d->ndof, np = d->npoin;
   const int nslot = perimeter_slots(h->LX, h->LZ);
@@ -562,6 +717,7 @@ int upload_mass_and_boundaries(sem2d_handle *h, const sem2d_problem_desc *d) {
     return st;
   if ((st = upload_stacey(h, d))) return st;
   if ((st = upload_dirneu(h, d))) return st;
+  if ((st = upload_boundary_forces(h, d))) return st;
   return upload_perio(h, d);
 }
 
@@ -822,6 +978,7 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.per_kd = h->per_kd;
   bc.per_dir = h->ndir ? h->per_dir : nullptr;
   bc.perio_f = h->nperio ? h->perio_f : nullptr;
+  bc.bf = h->bf;
   bc.jf1 = h->nflt ? h->jf1 : -1;
   bc.jf2 = h->nflt ? h->jf2 : -1;
   bc.has_fault = h->nflt ? 1 : 0;
@@ -1067,6 +1224,7 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
       pp.per_Ca = (const real *)h->per_Ca;
       pp.per_Cb = (const real *)h->per_Cb;
       pp.per_dir = h->ndir ? h->per_dir : nullptr;
+      pp.bf = h->bf;
       pp.dt = real(bc.dt);
       pp.cv = real(bc.cv);
       pp.cpred = real(bc.cpred);
@@ -1705,6 +1863,18 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
   if (h->nsrc) {
     std::vector<int> sI(h->nsrc), sJ(h->nsrc);
     std::vector<double> amp((size_t)h->nsrc * h->ndof * (h->nt + 1), 0.0);
+    // a time function other than Ricker, evaluated on the host
+    StfDev hs{};
+    std::vector<double> hv2;
+    if (d->src_stf) {
+      if (const char *m = stf_check(*d->src_stf)) return set_err(h, SEM2D_E_ARG, m);
+      const sem2d_stf &q = *d->src_stf;
+      hs = StfDev{q.kind, q.ntab, q.f0, q.onset, q.ampli, q.par1, q.par2, q.tab_t, q.tab_v, nullptr};
+      if (q.kind == SEM2D_STF_TAB) {
+        hv2 = stf_spline_d2(q.tab_t, q.tab_v, q.ntab);
+        hs.v2 = hv2.data();
+      }
+    }
     for (int s = 0; s < h->nsrc; ++s) {
       const int p = d->src_node[s] - 1;
       if (p < 0 || p >= d->npoin) return set_err(h, SEM2D_E_ARG, "source node out of range");
@@ -1714,7 +1884,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
       for (int it = 1; it <= h->nt; ++it) {
         // HHT-alpha adds the sources at t + (alpha-1) dt (solver.f90:116-117)
         const double t = it * d->dt + (h->alpha - 1.0) * d->dt;
-        double a = ricker(t - td, d->src_f0[s], d->src_t0[s], d->src_ampli[s]);
+        double a = d->src_stf ? stf_value(hs, t - td) : ricker(t - td, d->src_f0[s], d->src_t0[s], d->src_ampli[s]);
         a = a * rel;
         for (int c = 0; c < h->ndof; ++c)
           amp[((size_t)s * h->ndof + c) * (h->nt + 1) + it] = h->ndof == 1 ? a : d->src_dir[2 * s + c] * a;
@@ -1951,6 +2121,7 @@ int batch_close_impl(sem2d_handle *h) {
     if (m->st_nslot) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey absorbing boundaries in a batch");
     if (m->ndir) return set_err(h, SEM2D_E_UNSUPPORTED, "Dirichlet sides in a batch");
     if (m->nperio) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides in a batch");
+    if (m->bf.W) return set_err(h, SEM2D_E_UNSUPPORTED, "incident waves or Neumann tractions in a batch");
   }
   h->N = a->N;
   h->ndof = a->ndof;
@@ -2306,10 +2477,10 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
   if (h->ckpt_every <= 0 || h->steps != h->nt || h->ckpt_saved != h->nt / h->ckpt_every)
     return set_err(h, SEM2D_E_STATE, "run all nt steps with checkpoints first (sem2d_gpu_checkpoint_every)");
   if (h->N != 5 || h->nflt || h->scheme != 0 || h->has_kv || h->width > 0 || !h->mat_iso ||
-      h->mat_elem != kMatNode || h->st_nslot || h->ndir || h->nperio)
+      h->mat_elem != kMatNode || h->st_nslot || h->ndir || h->nperio || h->bf.W)
     return set_err(h, SEM2D_E_UNSUPPORTED,
                    "the adjoint covers NGLL=5, isotropic node material, leapfrog, no fault, KV, 2.5D, Stacey "
-                   "or Dirichlet sides");
+                   "or Dirichlet sides, incident wave or Neumann traction");
   if (h->nrec && (h->rec_npts != 1 || (h->rec_field != 'V' && h->rec_field != 'D')))
     return set_err(h, SEM2D_E_UNSUPPORTED, "the adjoint needs receivers at nodes recording V or D");
   int st = check_device_error(h);

@@ -637,6 +637,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
             const int so = c * nslot + sp;
             fc = fc - p.per_Ca[so] * vd;
             fc = fc - p.per_Cb[so] * vd;
+            if (p.bf.W) fc = fc + real(boundary_force(p.bf, NDOF, nslot, sp, c, it));
             if (p.per_kd) fc = fc - p.per_kd[so];
             if (p.per_dir && ((p.per_dir[sp] >> c) & 1)) fc = real(0);  // bc_dirneu.f90:155-167
             rm = p.per_rm[so];

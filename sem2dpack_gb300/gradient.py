@@ -121,6 +121,7 @@ try:
             if ctx.sim is None:
                 raise RuntimeError("SeismogramFunction supports one backward per forward: its GPU state "
                                    "was released by the first")
+            resid = np.asfortranarray(grad_sis.detach().cpu().numpy(), dtype=np.float64)
             g = [np.zeros(ctx.npoin) for _ in range(3)]
             pp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
             sim = ctx.sim

@@ -94,7 +94,7 @@ def test_every_member_offset_matches():
     fail here."""
     structs = {**c_structs("sem2d_gpu.h"), **c_structs("sem2d_host.h")}
     for which, (cname, py) in enumerate([("sem2d_problem_desc", abi.ProblemDesc), ("sem2d_deck", abi.Deck),
-                                         ("sem2d_lattice_args", abi.LatticeArgs)]):
+                                         ("sem2d_lattice_args", abi.LatticeArgs), ("sem2d_stf", abi.Stf)]):
         header = [f[0] for f in structs[cname]]
         mirror = [f[0] for f in py._fields_]
         assert header == mirror, cname
@@ -109,7 +109,7 @@ def test_fortran_types_repeat_the_header():
     structs = c_structs("sem2d_gpu.h")
     ftypes = fortran_types()
     kinds = {"int": "integer(c_int)", "double": "real(c_double)", "char": "character(kind=c_char)"}
-    for name in ("sem2d_problem_desc", "sem2d_lattice_args"):
+    for name in ("sem2d_stf", "sem2d_problem_desc", "sem2d_lattice_args"):
         c, f = structs[name], ftypes[name]
         assert [m[0] for m in c] == [m[0] for m in f], name
         for (cn, base, ptr, arr), (fn, ft, fdim) in zip(c, f):
