@@ -63,8 +63,9 @@ typedef struct sem2d_bc {
   int tag[2];
   int stacey; /* &BC_ABSORB stacey (bc_abso.f90:55-100); P-SV only        */
   int dirichlet; /* &BC_DIRNEU: bit 0 h='D', bit 1 v='D' (bc_dirneu.f90:50-112) */
-  int let_wave;  /* &BC_ABSORB let_wave (default T): an incident wave of
-                  * the sources enters across this side                  */
+  int no_wave;   /* &BC_ABSORB let_wave = F: the incident wave of the
+                  * sources does not enter across this side (0, the
+                  * reference's default let_wave = T, lets it in)        */
   /* &BC_DIRNEU hstf, vstf: time functions of the horizontal and vertical
    * tractions of a Neumann component (kind SEM2D_STF_NONE: none; a
    * Dirichlet component ignores its own, bc_dirneu.f90:70-101)          */
@@ -207,6 +208,11 @@ int sem2d_problem_time(const sem2d_problem *p, double *dt, int *nt,
 int sem2d_problem_rec_coord(const sem2d_problem *p, double *coord);
 int sem2d_problem_fault_coord(const sem2d_problem *p, double *coord);
 void sem2d_problem_destroy(sem2d_problem *p);
+
+/* Values of a time function at n times, as the library evaluates it for
+ * the point sources and the boundary forces (SEM2D_E_ARG for a bad
+ * description, message in sem2d_gpu_last_error(NULL)). */
+int sem2d_stf_eval(const sem2d_stf *stf, int n, const double *t, double *out);
 
 /* Message of the last failed builder call (thread local). */
 const char *sem2d_host_last_error(void);

@@ -50,6 +50,22 @@ struct oc_setup {
   int nabs;
   int *abs_node;
   double *abs_C;     /* (nabs,ndof) */
+  double *abs_B, *abs_nx, *abs_nz, *abs_n; /* weights, normals; abs_n (nabs,2) at export */
+  int *abs_wave;
+  /* time-dependent Neumann tractions of &BC_DIRNEU */
+  int nneu, nneu_stf;
+  int *neu_node, *neu_comp, *neu_stf;
+  double *neu_B;
+  sem2d_stf neu_stfs[2 * SEM2D_MAX_BCS];
+  /* time function of the sources other than Ricker, incident plane wave;
+   * TAB rows copied into tabs */
+  int has_src_stf;
+  sem2d_stf src_stf;
+  int wave_phase;
+  double wave_angle, wave_ref[2], wave_cp, wave_cs, wave_mu, wave_lambda, wave_tdelay;
+  sem2d_stf wave_stf;
+  int ntabs;
+  double *tabs[4 * SEM2D_MAX_BCS + 4];
   /* Stacey P3 terms, one per (boundary element, edge point) */
   int nst;
   int *st_node, *st_k, *st_edge;
@@ -931,8 +947,72 @@ static int perio_init(oc_setup *s, const int *tags, char *err, int el) {
   return 0;
 }
 
-/* BC_DIRNEU_init (bc_dirneu.f90:117-143): the components flagged 'D' */
-static int dirneu_init(oc_setup *s, int tag, int mask, int after, char *err, int el) {
+/* STF_read (stf_gen.f90:45-97) and the *_read checks; the REAL namelist
+ * variables of &STF_RICKER, &STF_GAUSSIAN, &STF_HARMONIC and &STF_USER
+ * hold FP32 values (stf_ricker.f90:51, stf_gaussian.f90:44,
+ * stf_harmonic.f90:41, stf_user.f90:46) */
+static int read_stf(oc_setup *s, const sem2d_stf *in, sem2d_stf *out, char *err, int el) {
+  *out = *in;
+  switch (in->kind) {
+    case SEM2D_STF_RICKER: {
+      float f0 = (float)in->f0, onset = (float)in->onset, ampli = (float)in->ampli;
+      if (f0 <= 0.0f) return seterr(err, el, "RICKER_read: f0 must be positive"), -1;
+      if (onset < 1.0f / f0) return seterr(err, el, "warning: RICKER_read: Onset time too small"), -1;
+      out->f0 = (double)f0;
+      out->onset = (double)onset;
+      out->ampli = (double)ampli;
+      return 0;
+    }
+    case SEM2D_STF_GAUSSIAN: {
+      float f0 = (float)in->f0, onset = (float)in->onset, ampli = (float)in->ampli;
+      if (f0 < 0.0f) return seterr(err, el, "STF_GAUSSIAN_read: f0 must be positive"), -1;
+      out->f0 = (double)f0;
+      out->onset = (double)onset;
+      out->ampli = (double)ampli;
+      return 0;
+    }
+    case SEM2D_STF_BRUNE:
+      if (in->f0 < 0.0) return seterr(err, el, "STF_BRUNE_read: fc must be positive"), -1;
+      return 0;
+    case SEM2D_STF_HARMONIC: {
+      float ampli = (float)in->ampli, f0 = (float)in->f0;
+      if (f0 <= 0.0f) return seterr(err, el, "STF_HARMONIC_read: f0 must be positive"), -1;
+      if (ampli == 0.0f) return seterr(err, el, "STF_HARMONIC_read: ampli must be non zero"), -1;
+      out->ampli = (double)ampli;
+      out->f0 = (double)f0;
+      return 0;
+    }
+    case SEM2D_STF_USER:
+      out->onset = (double)(float)in->onset;
+      out->ampli = (double)(float)in->ampli;
+      out->par1 = (double)(float)in->par1;
+      out->par2 = (double)(float)in->par2;
+      return 0;
+    case SEM2D_STF_TAB: {
+      int n = in->ntab;
+      if (n < 2 || !in->tab_t || !in->tab_v) return seterr(err, el, "STF_TAB_read: the table needs two rows or more"), -1;
+      if (s->ntabs + 2 > (int)(sizeof(s->tabs) / sizeof(s->tabs[0]))) return seterr(err, el, "too many tables"), -1;
+      double *t = xcalloc((size_t)n, sizeof(double)), *v = xcalloc((size_t)n, sizeof(double));
+      memcpy(t, in->tab_t, (size_t)n * sizeof(double));
+      memcpy(v, in->tab_v, (size_t)n * sizeof(double));
+      s->tabs[s->ntabs++] = t;
+      s->tabs[s->ntabs++] = v;
+      out->tab_t = t;
+      out->tab_v = v;
+      for (int k = 1; k < n; k++)
+        if (!(t[k] > t[k - 1])) return seterr(err, el, "STF_TAB_read: times must increase"), -1;
+      return 0;
+    }
+    default:
+      return seterr(err, el, "STF_read: unknown source time function "), -1;
+  }
+}
+
+/* BC_DIRNEU_init (bc_dirneu.f90:117-143): the components flagged 'D', and
+ * the time functions of the Neumann components (bc_DIRNEU_apply :157-167;
+ * a Dirichlet component drops its own, :70-101) */
+static int dirneu_init(oc_setup *s, const sem2d_bc *bc, int after, char *err, int el) {
+  const int tag = bc->tag[0], mask = bc->dirichlet;
   oc_bnd *bd = find_bnd(s, tag);
   if (!bd) return 0;
   int np = bd->npoin;
@@ -943,8 +1023,11 @@ static int dirneu_init(oc_setup *s, int tag, int mask, int after, char *err, int
     if (!(fabs(norm[k]) < TINY_XABS)) horiz = 0;
     if (!(fabs(norm[k + np]) < TINY_XABS)) vert = 0;
   }
-  free(norm); free(w);
-  if (!horiz && !vert) return seterr(err, el, "BC_DIRNEU_init: boundary is not vertical or horizontal"), -1;
+  free(norm);
+  if (!horiz && !vert) {
+    free(w);
+    return seterr(err, el, "BC_DIRNEU_init: boundary is not vertical or horizontal"), -1;
+  }
   for (int c = 0; c < s->ndof; c++) {
     if (!((mask >> c) & 1)) continue;
     int m = s->ndir + np;
@@ -958,10 +1041,33 @@ static int dirneu_init(oc_setup *s, int tag, int mask, int after, char *err, int
     }
     s->ndir = m;
   }
+  for (int c = 0; c < s->ndof; c++) {
+    const sem2d_stf *in = c == 0 ? &bc->hstf : &bc->vstf;
+    if (((mask >> c) & 1) || in->kind == SEM2D_STF_NONE) continue;
+    int q = s->nneu_stf;
+    if (read_stf(s, in, &s->neu_stfs[q], err, el)) {
+      free(w);
+      return -1;
+    }
+    s->nneu_stf = q + 1;
+    int m = s->nneu + np;
+    s->neu_node = realloc(s->neu_node, (size_t)m * sizeof(int));
+    s->neu_comp = realloc(s->neu_comp, (size_t)m * sizeof(int));
+    s->neu_stf = realloc(s->neu_stf, (size_t)m * sizeof(int));
+    s->neu_B = realloc(s->neu_B, (size_t)m * sizeof(double));
+    for (int k = 0; k < np; k++) {
+      s->neu_node[s->nneu + k] = bd->node[k];
+      s->neu_comp[s->nneu + k] = c;
+      s->neu_stf[s->nneu + k] = q;
+      s->neu_B[s->nneu + k] = w[k];
+    }
+    s->nneu = m;
+  }
+  free(w);
   return 0;
 }
 
-static int abso_init(oc_setup *s, int tag, int stacey, char *err, int el) {
+static int abso_init(oc_setup *s, int tag, int stacey, int wave, char *err, int el) {
   oc_bnd *bd = find_bnd(s, tag);
   if (!bd) return 0;
   int n = s->ngll, nd = s->ndof, np = bd->npoin;
@@ -1016,10 +1122,6 @@ static int abso_init(oc_setup *s, int tag, int stacey, char *err, int el) {
       }
     }
   }
-  if (periodic && stacey && nd == 2) {
-    free(norm); free(w); free(C);
-    return seterr(err, el, "Stacey sides meeting periodic sides are not supported"), -1;
-  }
   if (periodic) /* the two ends are one node (bc_abso.f90:227-231) */
     for (int d = 0; d < nd; d++) {
       C[0 + np * d] = C[0 + np * d] + C[(np - 1) + np * d];
@@ -1031,9 +1133,20 @@ static int abso_init(oc_setup *s, int tag, int stacey, char *err, int el) {
       int p = bd->node[k] - 1;
       s->rmass[p + (size_t)s->npoin * d] = s->rmass[p + (size_t)s->npoin * d] + cf * C[k + np * d];
     }
-  /* append to the absorbing entry list */
+  /* append to the absorbing entry list, with B, the normal and whether the
+   * wave source enters (let_wave on a flat side, bc_abso.f90:245-256) */
   int na = s->nabs + np;
   s->abs_node = realloc(s->abs_node, (size_t)na * sizeof(int));
+  s->abs_B = realloc(s->abs_B, (size_t)na * sizeof(double));
+  s->abs_nx = realloc(s->abs_nx, (size_t)na * sizeof(double));
+  s->abs_nz = realloc(s->abs_nz, (size_t)na * sizeof(double));
+  s->abs_wave = realloc(s->abs_wave, (size_t)na * sizeof(int));
+  for (int k = 0; k < np; k++) {
+    s->abs_B[s->nabs + k] = w[k];
+    s->abs_nx[s->nabs + k] = norm[k];
+    s->abs_nz[s->nabs + k] = norm[k + np];
+    s->abs_wave[s->nabs + k] = wave;
+  }
   double *nc = xcalloc((size_t)na * nd, sizeof(double));
   for (int d = 0; d < nd; d++)
     for (int k = 0; k < s->nabs; k++) nc[k + (size_t)na * d] = s->abs_C[k + (size_t)s->nabs * d];
@@ -1302,7 +1415,7 @@ static int rec_init(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
  * gets G(c,1) h'_l(xi_i) and the column (i, :) gets G(c,2) h'_l(eta_j),
  * G = M jac_inv^T (SH: G = jac_inv M(:,1)); the coefficients are summed per
  * node (in order of first appearance) into point forces */
-static int moment_init(oc_setup *s, const sem2d_deck *dk, float f0, float onset, float amp, char *err, int el) {
+static int moment_init(oc_setup *s, const sem2d_deck *dk, double f0, double onset, double amp, char *err, int el) {
   int nd = s->ndof, n = s->ngll, ns = dk->nsrc;
   double M[2][2] = {{0, 0}, {0, 0}};
   if (dk->src_mech == 1) {
@@ -1400,13 +1513,73 @@ static int moment_init(oc_setup *s, const sem2d_deck *dk, float f0, float onset,
   return 0;
 }
 
+/* WAVE_read + WAVE_init (src_wave.f90:78-180): the angle brought into
+ * [-180, 180], the reference point at the node nearest the domain corner
+ * the wave enters first, the material at the first element point of that
+ * node (SE_node_belongs_to, spec_grid.f90:441-456).  The reference
+ * computes that corner and then searches from wave%coord, which it never
+ * sets; the corner is what its comments and input documentation describe. */
+static int wave_init(oc_setup *s, const sem2d_deck *dk, const sem2d_stf *stf, char *err, int el) {
+  double angle = dk->wave_angle + 180.0;
+  angle = angle - floor(angle / 360.0) * 360.0 - 180.0;
+  if (dk->wave_phase != SEM2D_WAVE_P && dk->wave_phase != SEM2D_WAVE_S)
+    return seterr(err, el, "WAVE_read: phase must be S or P"), -1;
+  double xmin = s->coord[0], xmax = s->coord[0], zmin = s->coord[1], zmax = s->coord[1];
+  for (int p = 0; p < s->npoin; p++) {
+    double x = s->coord[2 * p], z = s->coord[2 * p + 1];
+    if (x < xmin) xmin = x;
+    if (x > xmax) xmax = x;
+    if (z < zmin) zmin = z;
+    if (z > zmax) zmax = z;
+  }
+  double corner[2];
+  corner[0] = angle >= 0.0 ? xmax : xmin;
+  corner[1] = fabs(angle) < 90.0 ? zmin : zmax;
+  int ig = nearest_node(s, corner, NULL), n = s->ngll;
+  size_t at = 0;
+  int found = 0;
+  for (int e = 0; e < s->nelem && !found; e++)
+    for (int j = 0; j < n && !found; j++)
+      for (int i = 0; i < n && !found; i++)
+        if (IB(s, i, j, e) == ig) {
+          at = i + n * (j + (size_t)n * e);
+          found = 1;
+        }
+  const sem2d_material *m = find_mat(dk, s->tag[at / ((size_t)n * n)]);
+  if (m && m->aniso) return seterr(err, el, "MAT_getProp: the incident wave needs mu and lambda of an isotropic material"), -1;
+  double rho = s->rho[at], cp = s->cp[at], cs = s->cs[at];
+  s->wave_phase = dk->wave_phase;
+  s->wave_angle = angle;
+  s->wave_ref[0] = s->coord[2 * (size_t)(ig - 1)];
+  s->wave_ref[1] = s->coord[2 * (size_t)(ig - 1) + 1];
+  s->wave_cp = cp;
+  s->wave_cs = cs;
+  s->wave_mu = rho * cs * cs;
+  s->wave_lambda = rho * (cp * cp - 2.0 * cs * cs);
+  s->wave_tdelay = dk->src_tdelay ? dk->src_tdelay[0] : 0.0;
+  s->wave_stf = *stf;
+  return 0;
+}
+
 static int src_init(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   int ns = dk->nsrc;
   if (ns <= 0) return 0;
-  /* &STF_RICKER values are REAL (single precision) in the reference */
-  float f0 = (float)dk->ricker_f0, onset = (float)dk->ricker_onset, amp = (float)dk->ricker_ampli;
-  if (f0 <= 0.0f) return seterr(err, el, "RICKER_read: f0 must be positive"), -1;
-  if (onset < 1.0f / f0) return seterr(err, el, "warning: RICKER_read: Onset time too small"), -1;
+  /* the time function all sources share (src_gen.f90:150-158) */
+  sem2d_stf in = dk->stf, stf;
+  if (in.kind == SEM2D_STF_NONE) {
+    in.kind = SEM2D_STF_RICKER;
+    in.f0 = dk->ricker_f0;
+    in.onset = dk->ricker_onset;
+    in.ampli = dk->ricker_ampli;
+  }
+  if (read_stf(s, &in, &stf, err, el)) return -1;
+  if (dk->src_mech == 4) return wave_init(s, dk, &stf, err, el);
+  if (stf.kind != SEM2D_STF_RICKER) {
+    s->has_src_stf = 1;
+    s->src_stf = stf;
+  }
+  /* the values of the time function as read (Ricker: already FP32) */
+  double f0 = stf.f0, onset = stf.onset, amp = stf.ampli;
   double ang = dk->force_angle * PI_REF / 180.0;
   if (dk->src_mech != 0) return moment_init(s, dk, f0, onset, amp, err, el);
   s->nsrc = ns;
@@ -1475,18 +1648,24 @@ oc_setup *oc_setup_build(const sem2d_deck *dk, char *err, int el) {
   for (int b = 0; b < dk->nbcs; b++) {
     const sem2d_bc *bc = &dk->bcs[b];
     if (bc->kind == SEM2D_BC_ABSORB) {
-      if (abso_init(s, bc->tag[0], bc->stacey, err, el)) goto fail;
+      if (abso_init(s, bc->tag[0], bc->stacey, !bc->no_wave && dk->nsrc > 0 && dk->src_mech == 4, err, el))
+        goto fail;
     } else if (bc->kind == SEM2D_BC_DYNFLT) {
       if (dynflt_init(s, dk, bc->tag, err, el)) goto fail;
       fault_seen = 1;
     } else if (bc->kind == SEM2D_BC_DIRNEU) {
-      if (dirneu_init(s, bc->tag[0], bc->dirichlet, fault_seen, err, el)) goto fail;
+      if (dirneu_init(s, bc, fault_seen, err, el)) goto fail;
     }
   }
   if (rec_init(s, dk, err, el) || src_init(s, dk, err, el)) goto fail;
   if (s->nst) {  /* Stacey K(nst,2): the first components, then the second */
     s->st_K = realloc(s->st_K, 2 * (size_t)s->nst * sizeof(double));
     memcpy(s->st_K + s->nst, s->st_K1, (size_t)s->nst * sizeof(double));
+  }
+  if (s->nabs) {
+    s->abs_n = xcalloc(2 * (size_t)s->nabs, sizeof(double));
+    memcpy(s->abs_n, s->abs_nx, (size_t)s->nabs * sizeof(double));
+    memcpy(s->abs_n + s->nabs, s->abs_nz, (size_t)s->nabs * sizeof(double));
   }
   /* invert the mass matrix (init.f90:112-116) */
   for (size_t q = 0; q < (size_t)s->npoin * s->ndof; q++) s->rmass[q] = 1.0 / s->rmass[q];
@@ -1514,6 +1693,9 @@ void oc_setup_free(oc_setup *s) {
   free(s->src_node); free(s->src_dir); free(s->src_f0); free(s->src_t0); free(s->src_amp);
   free(s->src_rel); free(s->src_tdelay); free(s->rec_node); free(s->rec_elem); free(s->rec_interp);
   free(s->rec_coord);
+  free(s->abs_B); free(s->abs_nx); free(s->abs_nz); free(s->abs_n); free(s->abs_wave);
+  free(s->neu_node); free(s->neu_comp); free(s->neu_stf); free(s->neu_B);
+  for (int q = 0; q < s->ntabs; q++) free(s->tabs[q]);
   free(s);
 }
 
@@ -1663,5 +1845,28 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
     d->twf_Dc = dk->twf_Dc;
     d->flt_potency = dk->flt_potency;
   }
+  d->src_stf = s->has_src_stf ? &s->src_stf : NULL;
+  d->wave_phase = s->wave_phase;
+  if (s->wave_phase) {
+    d->wave_angle = s->wave_angle;
+    d->wave_ref[0] = s->wave_ref[0];
+    d->wave_ref[1] = s->wave_ref[1];
+    d->wave_cp = s->wave_cp;
+    d->wave_cs = s->wave_cs;
+    d->wave_mu = s->wave_mu;
+    d->wave_lambda = s->wave_lambda;
+    d->wave_tdelay = s->wave_tdelay;
+    d->wave_stf = &s->wave_stf;
+    d->abs_wave = s->abs_wave;
+  }
+  d->abs_B = s->abs_B;
+  d->abs_n = s->abs_n;
+  d->nneu = s->nneu;
+  d->neu_node = s->neu_node;
+  d->neu_comp = s->neu_comp;
+  d->neu_B = s->neu_B;
+  d->neu_stf = s->neu_stf;
+  d->nneu_stf = s->nneu_stf;
+  d->neu_stfs = s->nneu_stf ? s->neu_stfs : NULL;
   return 0;
 }

@@ -11,7 +11,13 @@
  *   a coefficients (MAT_ELAST_init_a) mat_elastic.f90:290-360
  *   SO_add + FORCE_add + ricker       src_gen.f90:290-317,
  *                                     src_force.f90:77-92, stf_ricker.f90:89-103
- *   BC_ABSO_apply                     bc_abso.f90:286-336
+ *   STF_get (other time functions)    stf_gen.f90:99-121, stf_gaussian.f90:76-86,
+ *                                     stf_brune.f90:73-83, stf_harmonic.f90:68-77,
+ *                                     stf_user.f90:110-122, stf_tabulated.f90:83-95,
+ *                                     spline/splint/hunt utils.f90:596-734
+ *   BC_ABSO_apply (+ incident wave)   bc_abso.f90:286-336, SO_WAVE_get_VT
+ *                                     src_gen.f90:322-339, src_wave.f90:181-224
+ *   bc_DIRNEU_apply (tractions)       bc_dirneu.f90:148-169
  *   BC_DYNFLT_apply                   bc_dynflt.f90:569-739
  *   swf_*                             bc_dynflt_swf.f90:142-194
  *   rsf_*                             bc_dynflt_rsf.f90:165-568
@@ -35,8 +41,29 @@
 #define NR_MAXIT 200      /* bc_dynflt_rsf.f90:372 */
 #define NR_MAXBRACKET 200 /* the reference loop at :393-398 has no bound */
 
+/* a source time function with the spline second derivatives of a table
+ * and the bracket the last lookup found (splint keeps it, utils.f90:709) */
+typedef struct {
+  sem2d_stf s;
+  double *t, *v, *y2;
+  int klo;
+} oc_stf;
+
 struct oc_sim {
   int ngll, ndof, nelem, npoin, nelast, kd2;
+  double *coord; /* (2,npoin) node positions (incident wave phases) */
+  oc_stf *src_stf; /* NULL: the Ricker of src_f0, src_t0, src_amp */
+  /* incident plane wave across the absorbing entries with abs_wave */
+  int wave;
+  double wave_k[2], wave_p[2], wave_s[2], wave_ref[2], wave_cp, wave_cs, wave_mu, wave_lambda, wave_tdelay;
+  oc_stf *wave_stf;
+  double *abs_B, *abs_n;
+  int *abs_wave;
+  /* Neumann tractions of &BC_DIRNEU */
+  int nneu, nneu_stf;
+  int *neu_node, *neu_comp, *neu_stf;
+  double *neu_B;
+  oc_stf *neu_stfs;
   int *ibool;
   double *H;
   double *acoef; /* (ngll,ngll,nelast,nelem) */
@@ -51,6 +78,11 @@ struct oc_sim {
   int nstacey;
   int *st_node, *st_k, *st_edge;
   double *st_K;
+  /* KxD of BC_ABSO_apply: per node (npoin,2), the nodes it touches, and the
+   * periodic pairs at the ends of a side whose sums are shared */
+  double *st_f;
+  int nst_nodes, nst_pairs;
+  int *st_nodes, *st_pm, *st_ps;
   int ndir;
   int *dir_node, *dir_comp, *dir_after;
   int nperio;
@@ -282,9 +314,122 @@ static double ricker(double t, double f0, double t0, double ampli) {
   return -((ampli * (1.0 - 2.0 * arg)) * exp(-arg));
 }
 
+/* spline (utils.f90:652-691) with the end slopes STF_TAB_read gives, zero */
+static void stf_spline(const double *x, const double *y, int n, double *y2) {
+  double *u = xcalloc((size_t)n, sizeof(double));
+  double yp1 = 0.0, ypn = 0.0;
+  y2[0] = -0.5;
+  u[0] = (3.0 / (x[1] - x[0])) * ((y[1] - y[0]) / (x[1] - x[0]) - yp1);
+  for (int i = 1; i < n - 1; i++) {
+    double sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1]);
+    double p = sig * y2[i - 1] + 2.0;
+    y2[i] = (sig - 1.0) / p;
+    u[i] = (6.0 * ((y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1])) /
+                (x[i + 1] - x[i - 1]) -
+            sig * u[i - 1]) /
+           p;
+  }
+  double qn = 0.5, un = (3.0 / (x[n - 1] - x[n - 2])) * (ypn - (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]));
+  y2[n - 1] = (un - qn * u[n - 2]) / (qn * y2[n - 2] + 1.0);
+  for (int k = n - 2; k >= 0; k--) y2[k] = y2[k] * y2[k + 1] + u[k];
+  free(u);
+}
+
+static void stf_init(oc_stf *o, const sem2d_stf *in) {
+  memset(o, 0, sizeof(*o));
+  o->s = *in;
+  o->klo = 1;
+  if (in->kind == SEM2D_STF_TAB) {
+    int n = in->ntab;
+    o->t = dupd(in->tab_t, (size_t)n);
+    o->v = dupd(in->tab_v, (size_t)n);
+    o->y2 = xcalloc((size_t)n, sizeof(double));
+    stf_spline(o->t, o->v, n, o->y2);
+    o->s.tab_t = o->t;
+    o->s.tab_v = o->v;
+  }
+}
+static void stf_free(oc_stf *o) {
+  if (!o) return;
+  free(o->t); free(o->v); free(o->y2);
+}
+
+/* hunt (utils.f90:596-646), 1-based jlo in and out: the index before x */
+static int hunt(const double *xx, int n, double x, int jlo) {
+  int jhi, inc = 1;
+  const int ascnd = xx[n - 1] > xx[0];
+  if (jlo <= 0 || jlo > n) {
+    jlo = 0;
+    jhi = n + 1;
+  } else if ((x >= xx[jlo - 1]) == ascnd) {
+    for (;;) {
+      jhi = jlo + inc;
+      if (jhi > n) { jhi = n + 1; break; }
+      if ((x >= xx[jhi - 1]) == ascnd) { jlo = jhi; inc = inc + inc; }
+      else break;
+    }
+  } else {
+    jhi = jlo;
+    for (;;) {
+      jlo = jhi - inc;
+      if (jlo < 1) { jlo = 0; break; }
+      if ((x < xx[jlo - 1]) == ascnd) { jhi = jlo; inc = inc + inc; }
+      else break;
+    }
+  }
+  while (jhi - jlo != 1) {
+    int jm = (jhi + jlo) / 2;
+    if ((x > xx[jm - 1]) == ascnd) jlo = jm;
+    else jhi = jm;
+  }
+  return jlo;
+}
+
+/* STF_get (stf_gen.f90:99-121) */
+static double stf_get(oc_stf *o, double t) {
+  const sem2d_stf *s = &o->s;
+  double arg;
+  switch (s->kind) {
+    case SEM2D_STF_RICKER:
+      return ricker(t, s->f0, s->onset, s->ampli);
+    case SEM2D_STF_GAUSSIAN:
+      arg = PI_REF * s->f0 * (t - s->onset);
+      arg = arg * arg;
+      return s->ampli * exp(-arg);
+    case SEM2D_STF_BRUNE:
+      arg = 2 * PI_REF * s->f0 * (t > 0.0 ? t : 0.0);
+      return s->ampli * (1.0 - (1.0 + arg) * exp(-arg));
+    case SEM2D_STF_HARMONIC:
+      return s->ampli * sin(2.0 * PI_REF * t * s->f0);
+    case SEM2D_STF_USER:
+      arg = t - s->onset;
+      return s->ampli * sin(arg) + s->par1 * (arg * arg);
+    case SEM2D_STF_TAB: {
+      int n = s->ntab;
+      double tb = t > o->t[0] ? t : o->t[0];
+      tb = tb < o->t[n - 1] ? tb : o->t[n - 1];
+      /* splint (utils.f90:697-734) from the bracket of the last call; at
+       * the first abscissa hunt can return 0, an index before the table
+       * whose value at that abscissa is ya(1) all the same: kept in range */
+      int klo = hunt(o->t, n, tb, o->klo);
+      if (klo < 1) klo = 1;
+      if (klo > n - 1) klo = n - 1;
+      o->klo = klo;
+      int khi = klo + 1;
+      double h = o->t[khi - 1] - o->t[klo - 1];
+      double a = (o->t[khi - 1] - tb) / h, b = (tb - o->t[klo - 1]) / h;
+      return a * o->v[klo - 1] + b * o->v[khi - 1] +
+             ((a * a * a - a) * o->y2[klo - 1] + (b * b * b - b) * o->y2[khi - 1]) * (h * h) / 6.0;
+    }
+    default:
+      return 0.0;
+  }
+}
+
 static void so_add(oc_sim *s, double t, double *f) {
   for (int k = 0; k < s->nsrc; k++) {
-    double ampli = ricker(t - s->src_tdelay[k], s->src_f0[k], s->src_t0[k], s->src_amp[k]);
+    double ampli = s->src_stf ? stf_get(s->src_stf, t - s->src_tdelay[k])
+                              : ricker(t - s->src_tdelay[k], s->src_f0[k], s->src_t0[k], s->src_amp[k]);
     ampli = ampli * s->src_rel[k];
     size_t g = s->src_node[k] - 1;
     if (s->ndof == 1) {
@@ -296,28 +441,88 @@ static void so_add(oc_sim *s, double t, double *f) {
   }
 }
 
-static void abso_apply(oc_sim *s, double *f, const double *v, const double *dsp) {
+/* SO_WAVE_get_VT (src_gen.f90:322-339) for absorbing entry k: the
+ * incident velocity and traction, SRC_WAVE_get_VT (src_wave.f90:190-224)
+ * times STF_get at SRC_WAVE_get_phase (:181-187) minus the delay */
+static void wave_vt(oc_sim *s, int k, double time, double *Vin, double *Tin) {
+  double n0 = s->abs_n[k], n1 = s->abs_n[k + s->nabs];
+  double KN = s->wave_k[0] * n0 + s->wave_k[1] * n1;
+  if (s->ndof == 1) {
+    Vin[0] = 1.0;
+    Tin[0] = -s->wave_mu / s->wave_cs * KN;
+  } else {
+    Vin[0] = s->wave_p[0];
+    Vin[1] = s->wave_p[1];
+    if (s->wave == SEM2D_WAVE_P) {
+      Tin[0] = -1.0 / s->wave_cp * (s->wave_lambda * n0 + 2.0 * s->wave_mu * KN * s->wave_k[0]);
+      Tin[1] = -1.0 / s->wave_cp * (s->wave_lambda * n1 + 2.0 * s->wave_mu * KN * s->wave_k[1]);
+    } else {
+      double PN = s->wave_p[0] * n0 + s->wave_p[1] * n1;
+      Tin[0] = -s->wave_mu / s->wave_cs * (PN * s->wave_k[0] + KN * s->wave_p[0]);
+      Tin[1] = -s->wave_mu / s->wave_cs * (PN * s->wave_k[1] + KN * s->wave_p[1]);
+    }
+  }
+  const double *c = s->coord + 2 * (size_t)(s->abs_node[k] - 1);
+  double phase = time - (c[0] - s->wave_ref[0]) * s->wave_s[0] - (c[1] - s->wave_ref[1]) * s->wave_s[1];
+  phase = phase - s->wave_tdelay;
+  double ampli = stf_get(s->wave_stf, phase);
+  for (int d = 0; d < s->ndof; d++) {
+    Vin[d] = ampli * Vin[d];
+    Tin[d] = ampli * Tin[d];
+  }
+}
+
+static void abso_apply(oc_sim *s, double *f, const double *v, const double *dsp, double time) {
   for (int k = 0; k < s->nabs; k++) {
     size_t g = s->abs_node[k] - 1;
+    if (s->wave && s->abs_wave[k]) {
+      /* total field = incident + diffracted: T = T_i - C (V - V_i)
+       * (bc_abso.f90:279-306) */
+      double Vin[2], Tin[2];
+      wave_vt(s, k, time, Vin, Tin);
+      for (int d = 0; d < s->ndof; d++) {
+        size_t gg = g + (size_t)s->npoin * d;
+        f[gg] = f[gg] - s->abs_C[k + (size_t)s->nabs * d] * (v[gg] - Vin[d]) + s->abs_B[k] * Tin[d];
+      }
+      continue;
+    }
     for (int d = 0; d < s->ndof; d++) {
       size_t gg = g + (size_t)s->npoin * d;
       f[gg] = f[gg] - s->abs_C[k + (size_t)s->nabs * d] * v[gg];
     }
   }
-  /* Stacey P3 (BC_ABSO_apply, bc_abso.f90:321-334): for each boundary
-   * element edge point k, K(k,c,e) times the derivative of D(:,c) along
-   * the edge's traversal order, sum_l Ht(k,l) D(node_l, c) with
-   * Ht(k,l) = hprime(l,k) */
+  /* Stacey P3 (BC_ABSO_apply, bc_abso.f90:321-334): KxD accumulates, for
+   * each boundary element edge point k, K(k,c,e) times the derivative of
+   * D(:,c) along the edge's traversal order, sum_l Ht(k,l) D(node_l, c)
+   * with Ht(k,l) = hprime(l,k); a side that crosses periodic sides shares
+   * the sum of its two ends (:329-332); then MxA -= KxD */
+  if (!s->nstacey) return;
+  const size_t np = (size_t)s->npoin;
+  for (int u = 0; u < s->nst_nodes; u++) {
+    s->st_f[(size_t)s->st_nodes[u] - 1] = 0.0;
+    s->st_f[(size_t)s->st_nodes[u] - 1 + np] = 0.0;
+  }
   for (int t = 0; t < s->nstacey; t++) {
     const int n = s->ngll, k = s->st_k[t];
     const size_t g = (size_t)s->st_node[t] - 1;
     for (int c = 0; c < 2; c++) {
       double dd = 0.0;
       for (int l = 0; l < n; l++)
-        dd += s->H[l + (size_t)n * k] * dsp[(size_t)s->st_edge[l + (size_t)n * t] - 1 + (size_t)s->npoin * c];
-      f[g + (size_t)s->npoin * c] -= s->st_K[t + (size_t)s->nstacey * c] * dd;
+        dd += s->H[l + (size_t)n * k] * dsp[(size_t)s->st_edge[l + (size_t)n * t] - 1 + np * c];
+      s->st_f[g + np * c] = s->st_f[g + np * c] + s->st_K[t + (size_t)s->nstacey * c] * dd;
     }
   }
+  for (int q = 0; q < s->nst_pairs; q++)
+    for (int c = 0; c < 2; c++) {
+      size_t a = (size_t)s->st_pm[q] - 1 + np * c, b = (size_t)s->st_ps[q] - 1 + np * c;
+      s->st_f[a] = s->st_f[a] + s->st_f[b];
+      s->st_f[b] = s->st_f[a];
+    }
+  for (int u = 0; u < s->nst_nodes; u++)
+    for (int c = 0; c < 2; c++) {
+      size_t g = (size_t)s->st_nodes[u] - 1 + np * c;
+      f[g] = f[g] - s->st_f[g];
+    }
 }
 
 /* periodic sides: the forces of each node pair summed on the master and
@@ -339,6 +544,15 @@ static void dirneu_apply(oc_sim *s, double *f, int after) {
   for (int k = 0; k < s->ndir; k++)
     if (s->dir_after[k] == after)
       f[(size_t)s->dir_node[k] - 1 + (size_t)s->npoin * s->dir_comp[k]] = 0.0;
+}
+
+/* time-dependent Neumann tractions: field(node,c) += STF_get(stf, t) B
+ * (bc_DIRNEU_apply, bc_dirneu.f90:157-167) */
+static void neumann_apply(oc_sim *s, double *f, double time) {
+  for (int k = 0; k < s->nneu; k++) {
+    size_t g = (size_t)s->neu_node[k] - 1 + (size_t)s->npoin * s->neu_comp[k];
+    f[g] = f[g] + stf_get(&s->neu_stfs[s->neu_stf[k]], time) * s->neu_B[k];
+  }
 }
 
 /* ---------------- friction laws ---------------- */
@@ -735,6 +949,27 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
   s->st_k = dupi(dd->stacey_k, (size_t)dd->nstacey);
   s->st_edge = dupi(dd->stacey_edge, (size_t)dd->nstacey * n);
   s->st_K = dupd(dd->stacey_K, (size_t)dd->nstacey * 2);
+  if (dd->nstacey > 0) {
+    char *has = xcalloc((size_t)np, 1);
+    s->st_f = xcalloc(2 * (size_t)np, sizeof(double));
+    s->st_nodes = xcalloc((size_t)dd->nstacey, sizeof(int));
+    for (int t = 0; t < dd->nstacey; t++) {
+      int g = dd->stacey_node[t] - 1;
+      if (!has[g]) s->st_nodes[s->nst_nodes++] = g + 1;
+      has[g] = 1;
+    }
+    s->st_pm = xcalloc((size_t)dd->nperio + 1, sizeof(int));
+    s->st_ps = xcalloc((size_t)dd->nperio + 1, sizeof(int));
+    for (int q = 0; q < dd->nperio; q++) {
+      int a = dd->perio_master[q], b = dd->perio_slave[q];
+      if (has[a - 1] && has[b - 1]) {
+        s->st_pm[s->nst_pairs] = a;
+        s->st_ps[s->nst_pairs] = b;
+        s->nst_pairs++;
+      }
+    }
+    free(has);
+  }
   s->ndir = dd->ndir;
   s->dir_node = dupi(dd->dir_node, (size_t)dd->ndir);
   s->dir_comp = dupi(dd->dir_comp, (size_t)dd->ndir);
@@ -748,6 +983,50 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
   s->beta = dd->beta;
   s->gamma = dd->gamma;
   s->nt = dd->nt;
+  s->coord = dupd(dd->coord, 2 * (size_t)np);
+  if (dd->src_stf) {
+    s->src_stf = xcalloc(1, sizeof(oc_stf));
+    stf_init(s->src_stf, dd->src_stf);
+  }
+  if (dd->wave_phase != SEM2D_WAVE_NONE && dd->nabs > 0 && dd->abs_wave) {
+    /* WAVE_init (src_wave.f90:158-172): K, P and the slowness s = K/c */
+    double ang = PI_REF * dd->wave_angle / 180.0;
+    s->wave = dd->wave_phase;
+    s->wave_k[0] = -sin(ang);
+    s->wave_k[1] = cos(ang);
+    if (s->wave == SEM2D_WAVE_P) {
+      s->wave_p[0] = -sin(ang);
+      s->wave_p[1] = cos(ang);
+    } else {
+      s->wave_p[0] = cos(ang);
+      s->wave_p[1] = sin(ang);
+    }
+    double c = s->wave == SEM2D_WAVE_P ? dd->wave_cp : dd->wave_cs;
+    s->wave_s[0] = s->wave_k[0] / c;
+    s->wave_s[1] = s->wave_k[1] / c;
+    s->wave_ref[0] = dd->wave_ref[0];
+    s->wave_ref[1] = dd->wave_ref[1];
+    s->wave_cp = dd->wave_cp;
+    s->wave_cs = dd->wave_cs;
+    s->wave_mu = dd->wave_mu;
+    s->wave_lambda = dd->wave_lambda;
+    s->wave_tdelay = dd->wave_tdelay;
+    s->wave_stf = xcalloc(1, sizeof(oc_stf));
+    stf_init(s->wave_stf, dd->wave_stf);
+    s->abs_B = dupd(dd->abs_B, (size_t)dd->nabs);
+    s->abs_n = dupd(dd->abs_n, 2 * (size_t)dd->nabs);
+    s->abs_wave = dupi(dd->abs_wave, (size_t)dd->nabs);
+  }
+  if (dd->nneu > 0) {
+    s->nneu = dd->nneu;
+    s->neu_node = dupi(dd->neu_node, (size_t)dd->nneu);
+    s->neu_comp = dupi(dd->neu_comp, (size_t)dd->nneu);
+    s->neu_stf = dupi(dd->neu_stf, (size_t)dd->nneu);
+    s->neu_B = dupd(dd->neu_B, (size_t)dd->nneu);
+    s->nneu_stf = dd->nneu_stf;
+    s->neu_stfs = xcalloc((size_t)dd->nneu_stf, sizeof(oc_stf));
+    for (int q = 0; q < dd->nneu_stf; q++) stf_init(&s->neu_stfs[q], &dd->neu_stfs[q]);
+  }
   s->nsrc = dd->nsrc;
   s->src_node = dupi(dd->src_node, (size_t)dd->nsrc);
   s->src_dir = dupd(dd->src_dir, 2 * (size_t)dd->nsrc);
@@ -903,7 +1182,8 @@ int oc_sim_run(oc_sim *s, int nsteps) {
     compute_fint(s, a, df, vf); /* f aliases accel */
     so_add(s, t, a);
     perio_apply(s, a);
-    abso_apply(s, a, vf, df);
+    abso_apply(s, a, vf, df, t);
+    neumann_apply(s, a, t);
     dirneu_apply(s, a, 0);
     if (s->nflt) dynflt_apply(s, a, v, d);
     dirneu_apply(s, a, 1);
@@ -1010,8 +1290,23 @@ void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T, double
   if (theta) memcpy(theta, s->theta, (size_t)nf * sizeof(double));
 }
 
+int oc_stf_eval(const sem2d_stf *stf, int n, const double *t, double *out) {
+  oc_stf o;
+  stf_init(&o, stf);
+  for (int k = 0; k < n; k++) out[k] = stf_get(&o, t[k]);
+  stf_free(&o);
+  return 0;
+}
+
 void oc_sim_free(oc_sim *s) {
   if (!s) return;
+  stf_free(s->src_stf);
+  stf_free(s->wave_stf);
+  for (int q = 0; q < s->nneu_stf; q++) stf_free(&s->neu_stfs[q]);
+  free(s->src_stf); free(s->wave_stf); free(s->neu_stfs); free(s->coord);
+  free(s->abs_B); free(s->abs_n); free(s->abs_wave);
+  free(s->neu_node); free(s->neu_comp); free(s->neu_stf); free(s->neu_B);
+  free(s->st_f); free(s->st_nodes); free(s->st_pm); free(s->st_ps);
   void *ptrs[] = {s->ibool, s->H, s->acoef, s->kveta, s->rmass, s->abs_node, s->abs_C,
                   s->st_node, s->st_k, s->st_edge, s->st_K, s->dir_node, s->dir_comp, s->dir_after,
                   s->dal, s->val, s->per_m, s->per_s,

@@ -52,6 +52,7 @@ def lib():
         L.oc_sim_fault_state.argtypes = [vp, dp, dp, dp, dp, dp]
         L.oc_sim_free.argtypes = [vp]
         L.oc_gll_info.argtypes = [C.c_int, dp, dp, dp]
+        L.oc_stf_eval.argtypes = [C.POINTER(abi.Stf), C.c_int, dp, dp]
         _lib = L
     return _lib
 

@@ -68,6 +68,8 @@ void oc_sim_set_displacement(oc_sim *s, const double *d);
 void oc_sim_fault_state(const oc_sim *s, double *D, double *V, double *T,
                         double *MU, double *theta);
 void oc_sim_free(oc_sim *s);
+/* STF_get of a time function at n times (test hook) */
+int oc_stf_eval(const sem2d_stf *stf, int n, const double *t, double *out);
 
 #ifdef __cplusplus
 }

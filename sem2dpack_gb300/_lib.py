@@ -62,6 +62,7 @@ PROTOTYPES = [
     ("sem2d_host_last_error", C.c_char_p, []),
     ("sem2d_abi_struct_sizes", C.c_int, [ip, ip]),
     ("sem2d_abi_field_offsets", C.c_int, [C.c_int, C.POINTER(C.c_longlong), C.c_int]),
+    ("sem2d_stf_eval", C.c_int, [C.POINTER(abi.Stf), C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     ("sem2d_tune_cache_path", C.c_int, [C.c_char_p, C.c_int]),
     ("sem2d_tune_key", C.c_int, [C.c_int, C.c_int, C.c_longlong, C.c_int, C.c_int, C.c_char_p, C.c_int]),
     ("sem2d_tune_lookup", C.c_int, [C.c_char_p, C.c_char_p, C.POINTER(abi.TuneEntry)]),

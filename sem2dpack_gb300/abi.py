@@ -149,7 +149,7 @@ class Material(C.Structure):
 
 class BC(C.Structure):
     _fields_ = [("kind", c_int), ("tag", c_int * 2), ("stacey", c_int), ("dirichlet", c_int),
-                ("let_wave", c_int), ("hstf", Stf), ("vstf", Stf)]
+                ("no_wave", c_int), ("hstf", Stf), ("vstf", Stf)]
 
 
 class Deck(C.Structure):

@@ -48,7 +48,8 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.per_kd = static_cast<const real *>(c.per_kd);
   p.per_dir = c.per_dir;
   p.perio_f = static_cast<real *>(c.perio_f);
-  p.bf = c.bf;
+  p.perio_tb = c.perio_tb;
+  p.per_bf = static_cast<const real *>(c.per_bf);
   p.jf1 = c.jf1;
   p.jf2 = c.jf2;
   p.has_fault = c.has_fault;

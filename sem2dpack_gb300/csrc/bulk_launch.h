@@ -6,8 +6,6 @@
 #include <string>
 #include <vector>
 
-#include "stf.cuh"
-
 namespace sem2d {
 
 // largest chunk height the host picks (the kernel holds the row tables of
@@ -38,7 +36,8 @@ struct BulkConfig {
   void *per_kd = nullptr;  // Stacey P3 forces [c*nslot + slot], or null
   const int *per_dir = nullptr;  // zero-Dirichlet bits c by perimeter slot, or null
   void *perio_f = nullptr;       // raw forces of the periodic columns, or null
-  BoundaryForces bf;             // incident wave and Neumann tractions (W null: none)
+  int perio_tb = 0;              // the periodic sides are the bottom and top rows
+  void *per_bf = nullptr;        // incident wave and Neumann tractions of this step [c*nslot + slot], or null
   int jf1 = -1, jf2 = -1;
   int has_fault = 0;
   const void *flt = nullptr;  // host FaultParams<real> of the problem's precision

@@ -442,9 +442,11 @@ namespace sem2d {
 // Periodic columns (bc_perio_apply = BC_PERIO_set_field, bc_periodic.f90:
 // 77-88, applied first of the boundary terms, bc_gen.f90:271-275): the
 // raw forces the step kernel left for the nodes (0, J) and (LX-1, J) are
-// summed, each copy takes its dashpot and Dirichlet terms and is updated as
-// the step kernel updates a node; on the fault rows the sums go to the fault
-// node update of k = 0 and k = LX-1.  One thread per lattice row.
+// summed, each copy takes its dashpot, boundary-force, Stacey and Dirichlet
+// terms and is updated as the step kernel updates a node; on the fault rows
+// the sums go to the fault node update of k = 0 and k = LX-1.  One thread
+// per lattice row; with tb the rows J = 0 and LZ-1 instead, one thread per
+// lattice column (no fault).
 template <typename real>
 struct PerioParams {
   int LX, LZ, ndof, nslot, scheme;
@@ -454,7 +456,9 @@ struct PerioParams {
   real *Dnext, *Vnext, *Anext;
   const real *per_rm, *per_Ca, *per_Cb;
   const int *per_dir;
-  BoundaryForces bf;
+  const real *per_bf;  // incident wave and Neumann tractions of this step, or null
+  const real *per_kd;  // Stacey forces of this step, or null
+  int tb;              // bottom/top rows instead of left/right columns
   real dt, cv, cpred, cpa, cd2, cb;
   int jf1, jf2, has_fault, two;
   const int *step;
@@ -462,7 +466,7 @@ struct PerioParams {
 
 template <typename real>
 __device__ __forceinline__ real perio_boundary(const PerioParams<real> &p, int I, int J, int c, real fc, real *vpred,
-                                               real *rm, int it) {
+                                               real *rm) {
   const long long g = c * p.plane + (long long)J * p.pitch + I;
   real vp = p.Vcur[g], vd = vp;
   if (p.scheme != 0) {
@@ -473,7 +477,8 @@ __device__ __forceinline__ real perio_boundary(const PerioParams<real> &p, int I
   const int sp = perimeter_slot(I, J, p.LX, p.LZ), so = c * p.nslot + sp;
   fc = fc - p.per_Ca[so] * vd;
   fc = fc - p.per_Cb[so] * vd;
-  if (p.bf.W) fc = fc + real(boundary_force(p.bf, p.ndof, p.nslot, sp, c, it));
+  if (p.per_bf) fc = fc + p.per_bf[so];
+  if (p.per_kd) fc = fc - p.per_kd[so];
   if (p.per_dir && ((p.per_dir[sp] >> c) & 1)) fc = real(0);
   *vpred = vp;
   *rm = p.per_rm[so];
@@ -482,7 +487,29 @@ __device__ __forceinline__ real perio_boundary(const PerioParams<real> &p, int I
 
 template <typename real>
 __global__ void perio_kernel(const PerioParams<real> p, FaultParams<real> flt) {
-  const int J = blockIdx.x * blockDim.x + threadIdx.x;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p.tb) {  // the pair (I, 0), (I, LZ-1)
+    if (q >= p.LX) return;
+    for (int e = 0; e < 2; ++e) {
+      const int J = e ? p.LZ - 1 : 0;
+      for (int c = 0; c < p.ndof; ++c) {
+        const long long g = c * p.plane + (long long)J * p.pitch + q;
+        real vp, rm;
+        const real s = p.pf[(size_t(c) * p.LX + q) * 2] + p.pf[(size_t(c) * p.LX + q) * 2 + 1];
+        const real fc = perio_boundary(p, q, J, c, s, &vp, &rm);
+        const real a = rm * fc;
+        const real vnew = vp + p.cv * a;
+        real dcur = p.Dcur[g];
+        if (p.scheme != 0 && p.cb != real(0)) dcur = dcur + p.cb * a;
+        const real dnext = p.scheme != 0 ? (dcur + p.dt * vnew) + p.cd2 * a : dcur + p.dt * vnew;
+        p.Vnext[g] = vnew;
+        p.Dnext[g] = dnext;
+        if (p.Anext) p.Anext[g] = a;
+      }
+    }
+    return;
+  }
+  const int J = q;
   if (J >= p.LZ) return;
   const int it = *p.step;
   if (p.has_fault && p.two && J == p.jf2) return;  // with the row jf1
@@ -493,10 +520,10 @@ __global__ void perio_kernel(const PerioParams<real> p, FaultParams<real> flt) {
       for (int c = 0; c < p.ndof; ++c) {
         real vp, rm;
         const real s1 = p.pf[(size_t(c) * p.LZ + p.jf1) * 2] + p.pf[(size_t(c) * p.LZ + p.jf1) * 2 + 1];
-        f1[c] = double(perio_boundary(p, I, p.jf1, c, s1, &vp, &rm, it));
+        f1[c] = double(perio_boundary(p, I, p.jf1, c, s1, &vp, &rm));
         if (p.two) {
           const real s2 = p.pf[(size_t(c) * p.LZ + p.jf2) * 2] + p.pf[(size_t(c) * p.LZ + p.jf2) * 2 + 1];
-          f2[c] = double(perio_boundary(p, I, p.jf2, c, s2, &vp, &rm, it));
+          f2[c] = double(perio_boundary(p, I, p.jf2, c, s2, &vp, &rm));
         }
       }
       fault_node_update(flt, I, it, f1, f2);
@@ -509,7 +536,7 @@ __global__ void perio_kernel(const PerioParams<real> p, FaultParams<real> flt) {
       const long long g = c * p.plane + (long long)J * p.pitch + I;
       real vp, rm;
       const real s = p.pf[(size_t(c) * p.LZ + J) * 2] + p.pf[(size_t(c) * p.LZ + J) * 2 + 1];
-      const real fc = perio_boundary(p, I, J, c, s, &vp, &rm, it);
+      const real fc = perio_boundary(p, I, J, c, s, &vp, &rm);
       const real a = rm * fc;
       const real vnew = vp + p.cv * a;
       real dcur = p.Dcur[g];

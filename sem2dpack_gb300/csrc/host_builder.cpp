@@ -639,6 +639,23 @@ struct sem2d_problem {
   std::vector<int> abs_node;
   std::vector<double> abs_C;  // built per dof then transposed at export
   std::vector<std::vector<double>> abs_Cd;
+  // per absorbing entry: boundary weight, outward normal (n0 then n1 at
+  // export) and whether the incident wave enters there
+  std::vector<double> abs_B, abs_n0, abs_n1, abs_n;
+  std::vector<int> abs_wave;
+  // time-dependent Neumann tractions of &BC_DIRNEU
+  std::vector<int> neu_node, neu_comp, neu_stf;
+  std::vector<double> neu_B;
+  std::vector<sem2d_stf> neu_stfs;
+  // source time function other than Ricker and the incident plane wave;
+  // TAB rows are copied (tabs) so the descriptor outlives the deck
+  bool has_src_stf = false;
+  sem2d_stf src_stf{};
+  int wave_phase = 0;
+  double wave_angle = 0, wave_ref[2] = {0, 0}, wave_cp = 0, wave_cs = 0, wave_mu = 0, wave_lambda = 0,
+         wave_tdelay = 0;
+  sem2d_stf wave_stf{};
+  std::vector<std::unique_ptr<std::vector<double>>> tabs;
   // Stacey P3 terms, one per (boundary element, edge point)
   std::vector<int> st_node, st_k, st_edge;
   std::vector<double> st_K0, st_K1;
@@ -914,11 +931,65 @@ void perio_init(sem2d_problem &P, const int tags[2]) {
   P.per_slave.insert(P.per_slave.end(), s->node.begin(), s->node.end());
 }
 
+// STF_read (stf_gen.f90:45-97) of a deck value: the checks of the *_read
+// routines, the parameters that &STF_RICKER, &STF_GAUSSIAN, &STF_HARMONIC
+// and &STF_USER read into REAL variables rounded to FP32, the TAB rows
+// copied into the problem.  A deck kind NONE with ricker_* values is the
+// Ricker of &STF_RICKER.
+sem2d_stf read_stf(sem2d_problem &P, const sem2d_stf &in) {
+  sem2d_stf s = in;
+  auto r32 = [](double x) { return double(float(x)); };
+  switch (in.kind) {
+    case SEM2D_STF_RICKER:  // stf_ricker.f90:46-78
+      s.f0 = r32(in.f0);
+      s.onset = r32(in.onset);
+      s.ampli = r32(in.ampli);
+      if (s.f0 <= 0.0) throw BuildError("RICKER_read: f0 must be positive");
+      // a severe warning, fatal under the default abort_on_warnings (stdio.f90:13,218-227)
+      if (float(s.onset) < 1.0f / float(s.f0)) throw BuildError("warning: RICKER_read: Onset time too small");
+      break;
+    case SEM2D_STF_GAUSSIAN:  // stf_gaussian.f90:36-60
+      s.f0 = r32(in.f0);
+      s.onset = r32(in.onset);
+      s.ampli = r32(in.ampli);
+      if (s.f0 < 0.0) throw BuildError("STF_GAUSSIAN_read: f0 must be positive");
+      break;
+    case SEM2D_STF_BRUNE:  // stf_brune.f90:36-60 (double precision)
+      if (in.f0 < 0.0) throw BuildError("STF_BRUNE_read: fc must be positive");
+      break;
+    case SEM2D_STF_HARMONIC:  // stf_harmonic.f90:33-58
+      s.ampli = r32(in.ampli);
+      s.f0 = r32(in.f0);
+      if (s.f0 <= 0.0) throw BuildError("STF_HARMONIC_read: f0 must be positive");
+      if (s.ampli == 0.0) throw BuildError("STF_HARMONIC_read: ampli must be non zero");
+      break;
+    case SEM2D_STF_USER:  // stf_user.f90:38-80
+      s.onset = r32(in.onset);
+      s.ampli = r32(in.ampli);
+      s.par1 = r32(in.par1);
+      s.par2 = r32(in.par2);
+      break;
+    case SEM2D_STF_TAB: {  // stf_tabulated.f90:37-71
+      if (in.ntab < 2 || !in.tab_t || !in.tab_v) throw BuildError("STF_TAB_read: the table needs two rows or more");
+      P.tabs.emplace_back(new std::vector<double>(in.tab_t, in.tab_t + in.ntab));
+      s.tab_t = P.tabs.back()->data();
+      P.tabs.emplace_back(new std::vector<double>(in.tab_v, in.tab_v + in.ntab));
+      s.tab_v = P.tabs.back()->data();
+      for (int k = 1; k < in.ntab; ++k)
+        if (!(in.tab_t[k] > in.tab_t[k - 1])) throw BuildError("STF_TAB_read: times must increase");
+      break;
+    }
+    default:
+      throw BuildError("STF_read: unknown source time function ");
+  }
+  return s;
+}
+
 // BC_ABSO_init (bc_abso.f90:115-266), Clayton-Engquist on flat sides, and
 // the Stacey P3 coefficients of a P-SV side with stacey=T
 // (bc_abso.f90:174-218): K(k,c,e) = w_k |dx/dloc_t| dloc_t/dx_t
 // rho cs (2 cs - cp), negated for the tangential component
-void abso_init(sem2d_problem &P, int tag, int stacey) {
+void abso_init(sem2d_problem &P, int tag, int stacey, int let_wave, bool wave_source) {
   const sem2d_grid &g = *P.g;
   const sem2d_grid::Boundary *b = g.find(tag);
   if (!b) return;  // the reference ignores a BC whose tag is absent (bc_gen.f90:214-219)
@@ -968,7 +1039,6 @@ void abso_init(sem2d_problem &P, int tag, int stacey) {
       }
     }
   }
-  if (periodic && stacey && nd == 2) throw BuildError("Stacey sides meeting periodic sides are not supported");
   if (periodic)  // the two ends are one node (bc_abso.f90:227-231)
     for (int d = 0; d < nd; ++d) {
       Cb[0 + size_t(np) * d] = Cb[0 + size_t(np) * d] + Cb[(np - 1) + size_t(np) * d];
@@ -981,21 +1051,29 @@ void abso_init(sem2d_problem &P, int tag, int stacey) {
       P.mass[p] = P.mass[p] + cf * Cb[k + size_t(np) * d];
     }
   if (P.abs_Cd.empty()) P.abs_Cd.resize(nd);
+  // the first wave source found enters across a flat side with let_wave
+  // (bc_abso.f90:245-256); every side here is flat
+  const int wave = let_wave && wave_source ? 1 : 0;
   for (int k = 0; k < np; ++k) {
     P.abs_node.push_back(b->node[k]);
     for (int d = 0; d < nd; ++d) P.abs_Cd[d].push_back(Cb[k + size_t(np) * d]);
+    P.abs_B.push_back(w[k]);
+    P.abs_n0.push_back(nrm[k]);
+    P.abs_n1.push_back(nrm[k + np]);
+    P.abs_wave.push_back(wave);
   }
 }
 
 // BC_DIRNEU_init (bc_dirneu.f90:117-143): a flat side whose components
 // flagged 'D' have their force set to zero (bc_DIRNEU_apply, :148-169)
-void dirneu_init(sem2d_problem &P, int tag, int mask, int after_fault) {
+void dirneu_init(sem2d_problem &P, const sem2d_bc &bc, int after_fault) {
+  const int tag = bc.tag[0], mask = bc.dirichlet;
   const sem2d_grid &g = *P.g;
   const sem2d_grid::Boundary *b = g.find(tag);
   if (!b) return;
   const int np = int(b->node.size());
   std::vector<double> nrm, w;
-  normals(g, *b, nrm, w);
+  normals(g, *b, nrm, w, perio_intersects(P, *b));
   bool horiz = true, vert = true;
   for (int k = 0; k < np; ++k) {
     horiz &= std::fabs(nrm[k]) < kTinyXabs;
@@ -1008,6 +1086,21 @@ void dirneu_init(sem2d_problem &P, int tag, int mask, int after_fault) {
       P.dir_node.push_back(b->node[k]);
       P.dir_comp.push_back(c);
       P.dir_after.push_back(after_fault);
+    }
+  }
+  // a Neumann component with a time function: field += STF(t) B
+  // (bc_DIRNEU_apply, bc_dirneu.f90:157-167; a Dirichlet component's
+  // function is dropped, :70-101; SH has only the horizontal one)
+  for (int c = 0; c < P.ndof; ++c) {
+    const sem2d_stf &in = c == 0 ? bc.hstf : bc.vstf;
+    if (((mask >> c) & 1) || in.kind == SEM2D_STF_NONE) continue;
+    const int q = int(P.neu_stfs.size());
+    P.neu_stfs.push_back(read_stf(P, in));
+    for (int k = 0; k < np; ++k) {
+      P.neu_node.push_back(b->node[k]);
+      P.neu_comp.push_back(c);
+      P.neu_B.push_back(w[k]);
+      P.neu_stf.push_back(q);
     }
   }
 }
@@ -1207,21 +1300,84 @@ void rec_init(sem2d_problem &P, const sem2d_deck &dk) {
   P.rec_nsamp = P.nt / P.rec_isamp + 1;
 }
 
+// WAVE_read + WAVE_init (src_wave.f90:78-180) for the first wave source,
+// the one every absorbing side with let_wave takes (bc_abso.f90:245-256).
+// The reference point: the domain corner the wave enters first (maximum x
+// for angle >= 0, minimum z for |angle| < 90), moved to its nearest node;
+// the material values are those of the first element point at that node.
+// WAVE_init computes that corner but then searches from wave%coord, which
+// it never assigns, and leaves wave%coord unset for the phase
+// (src_wave.f90:133-157, 183-187); the corner is the reading its comments
+// and the input documentation give, and the C-ABI takes the point
+// explicitly (wave_ref) for a caller who wants another.
+void wave_init(sem2d_problem &P, const sem2d_deck &dk, const sem2d_stf &stf) {
+  const sem2d_grid &g = *P.g;
+  double angle = dk.wave_angle + 180.0;
+  angle = angle - std::floor(angle / 360.0) * 360.0 - 180.0;  // modulo(angle+180,360)-180
+  if (dk.wave_phase != SEM2D_WAVE_P && dk.wave_phase != SEM2D_WAVE_S)
+    throw BuildError("WAVE_read: phase must be S or P");
+  double xmin = g.coord[0], xmax = g.coord[0], zmin = g.coord[1], zmax = g.coord[1];
+  for (int p = 0; p < g.npoin; ++p) {
+    xmin = std::min(xmin, g.coord[2 * size_t(p)]);
+    xmax = std::max(xmax, g.coord[2 * size_t(p)]);
+    zmin = std::min(zmin, g.coord[2 * size_t(p) + 1]);
+    zmax = std::max(zmax, g.coord[2 * size_t(p) + 1]);
+  }
+  const double corner[2] = {angle >= 0.0 ? xmax : xmin, std::fabs(angle) < 90.0 ? zmin : zmax};
+  const int ig = nearest_node(g, corner);
+  const int N = g.ngll;
+  size_t at = 0;
+  bool found = false;
+  for (int e = 0; e < g.nelem && !found; ++e)  // SE_node_belongs_to_1, spec_grid.f90:441-456
+    for (int j = 0; j < N && !found; ++j)
+      for (int i = 0; i < N && !found; ++i)
+        if (g.ibool[i + N * (j + size_t(N) * e)] == ig) {
+          at = i + N * (j + size_t(N) * e);
+          found = true;
+        }
+  const sem2d_material *m = find_mat(dk, g.tag[at / (size_t(N) * N)]);
+  if (m && m->aniso) throw BuildError("MAT_getProp: the incident wave needs mu and lambda of an isotropic material");
+  P.wave_phase = dk.wave_phase;
+  P.wave_angle = angle;
+  P.wave_ref[0] = g.coord[2 * size_t(ig - 1)];
+  P.wave_ref[1] = g.coord[2 * size_t(ig - 1) + 1];
+  const double rho = P.rho[at], cp = P.cp[at], cs = P.cs[at];
+  P.wave_cp = cp;
+  P.wave_cs = cs;
+  P.wave_mu = rho * cs * cs;                      // mat_elastic.f90:214-215
+  P.wave_lambda = rho * (cp * cp - 2.0 * cs * cs);
+  P.wave_tdelay = dk.src_tdelay ? dk.src_tdelay[0] : 0.0;
+  P.wave_stf = stf;
+}
+
 void src_init(sem2d_problem &P, const sem2d_deck &dk) {
   const int ns = dk.nsrc;
   if (ns <= 0) return;
-  // &STF_RICKER reads f0, onset and ampli as REAL (stf_ricker.f90:49-51)
-  const float f0 = float(dk.ricker_f0), onset = float(dk.ricker_onset), amp = float(dk.ricker_ampli);
-  if (f0 <= 0.0f) throw BuildError("RICKER_read: f0 must be positive");
-  if (onset < 1.0f / f0) throw BuildError("warning: RICKER_read: Onset time too small");
+  // the time function all sources share (SO_read, src_gen.f90:150-158)
+  sem2d_stf in = dk.stf;
+  if (in.kind == SEM2D_STF_NONE) {
+    in.kind = SEM2D_STF_RICKER;
+    in.f0 = dk.ricker_f0;
+    in.onset = dk.ricker_onset;
+    in.ampli = dk.ricker_ampli;
+  }
+  const sem2d_stf stf = read_stf(P, in);
+  if (dk.src_mech == 4) {
+    wave_init(P, dk, stf);
+    return;
+  }
+  if (stf.kind != SEM2D_STF_RICKER) {
+    P.has_src_stf = true;
+    P.src_stf = stf;
+  }
   const double ang = dk.force_angle * kPi / 180.0;
   auto push = [&](int node, double dx, double dz, double rel, double td) {
     P.src_node.push_back(node);
     P.src_dir.push_back(dx);
     P.src_dir.push_back(dz);
-    P.src_f0.push_back(double(f0));
-    P.src_t0.push_back(double(onset));
-    P.src_amp.push_back(double(amp));
+    P.src_f0.push_back(stf.f0);
+    P.src_t0.push_back(stf.onset);
+    P.src_amp.push_back(stf.ampli);
     P.src_rel.push_back(rel);
     P.src_tdelay.push_back(td);
   };
@@ -1417,12 +1573,12 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
     for (int b = 0; b < deck->nbcs; ++b) {
       const sem2d_bc &bc = deck->bcs[b];
       if (bc.kind == SEM2D_BC_ABSORB) {
-        abso_init(*P, bc.tag[0], bc.stacey);
+        abso_init(*P, bc.tag[0], bc.stacey, !bc.no_wave, deck->nsrc > 0 && deck->src_mech == 4);
       } else if (bc.kind == SEM2D_BC_DYNFLT) {
         dynflt_init(*P, *deck, bc.tag);
         fault_seen = true;
       } else if (bc.kind == SEM2D_BC_DIRNEU) {
-        dirneu_init(*P, bc.tag[0], bc.dirichlet, fault_seen ? 1 : 0);
+        dirneu_init(*P, bc, fault_seen ? 1 : 0);
       } else if (bc.kind == SEM2D_BC_PERIOD) {
         continue;
       } else {
@@ -1437,6 +1593,8 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
     P->abs_C.resize(na * nd);
     for (int d = 0; d < nd && na; ++d)
       for (size_t k = 0; k < na; ++k) P->abs_C[k + na * d] = P->abs_Cd[d][k];
+    P->abs_n = P->abs_n0;
+    P->abs_n.insert(P->abs_n.end(), P->abs_n1.begin(), P->abs_n1.end());  // n(nabs, 2)
     P->st_K0.insert(P->st_K0.end(), P->st_K1.begin(), P->st_K1.end());  // K(nstacey, 2)
     *out = P.release();
     return SEM2D_OK;
@@ -1566,6 +1724,29 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
     d->twf_Dc = dk.twf_Dc;
     d->flt_potency = dk.flt_potency;
   }
+  d->src_stf = P->has_src_stf ? &P->src_stf : nullptr;
+  d->wave_phase = P->wave_phase;
+  if (P->wave_phase) {
+    d->wave_angle = P->wave_angle;
+    d->wave_ref[0] = P->wave_ref[0];
+    d->wave_ref[1] = P->wave_ref[1];
+    d->wave_cp = P->wave_cp;
+    d->wave_cs = P->wave_cs;
+    d->wave_mu = P->wave_mu;
+    d->wave_lambda = P->wave_lambda;
+    d->wave_tdelay = P->wave_tdelay;
+    d->wave_stf = &P->wave_stf;
+  }
+  d->abs_B = VPTR(P->abs_B);
+  d->abs_n = VPTR(P->abs_n);
+  d->abs_wave = P->wave_phase ? VPTR(P->abs_wave) : nullptr;
+  d->nneu = int(P->neu_node.size());
+  d->neu_node = VPTR(P->neu_node);
+  d->neu_comp = VPTR(P->neu_comp);
+  d->neu_B = VPTR(P->neu_B);
+  d->neu_stf = VPTR(P->neu_stf);
+  d->nneu_stf = int(P->neu_stfs.size());
+  d->neu_stfs = VPTR(P->neu_stfs);
   return SEM2D_OK;
 }
 

@@ -417,7 +417,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
               const int so = c * nslot + sp;
               f[c][i] = f[c][i] - p.per_Ca[so] * vv[c][i];
               f[c][i] = f[c][i] - p.per_Cb[so] * vv[c][i];
-              if (p.bf.W) f[c][i] = f[c][i] + float(boundary_force(p.bf, NDOF, nslot, sp, c, it));
+              if (p.per_bf) f[c][i] = f[c][i] + p.per_bf[so];
             }
             rmv[i] = p.per_rm[sp];  // dof 0 entry; dof 1 below
           }

@@ -14,8 +14,6 @@
 
 #include <cstdint>
 
-#include "stf.cuh"
-
 namespace sem2d {
 
 constexpr int kMaxN = 9;          // largest NGLL compiled
@@ -111,7 +109,8 @@ struct BulkParams {
   const real *per_kd;     // Stacey P3 forces [c*nslot + slot] of this step, or null
   const int *per_dir;     // zero-Dirichlet bits c by perimeter slot, or null
   real *perio_f;          // periodic columns I = 0, LX-1: raw forces [(c*LZ + J)*2 + side], or null
-  BoundaryForces bf;      // perimeter forces with their own time functions (bf.W null: none)
+  int perio_tb;           // periodic rows J = 0, LZ-1 instead: [(c*LX + I)*2 + side]
+  const real *per_bf;     // incident wave and Neumann tractions of this step [c*nslot + slot], or null
   // fault rows (lattice rows of side 1 and side 2, -1 if none); a tile row
   // always holds both rows, so the owning CTA finishes the fault nodes
   int jf1, jf2;

@@ -24,6 +24,7 @@
 #include "bulk_launch.h"
 #include "fault_kernel.cuh"
 #include "sem2d_common.cuh"
+#include "stf.cuh"
 
 using namespace sem2d;
 
@@ -80,11 +81,13 @@ struct sem2d_handle {
   int *per_dir = nullptr;
   unsigned char *d_fdir = nullptr;
   // periodic columns I = 0 and LX-1: raw forces left by the step kernel
-  int nperio = 0;
+  int nperio = 0, perio_tb = 0;  // perio_tb: the rows J = 0 and LZ-1 instead
   void *perio_f = nullptr;
   // perimeter forces with their own time functions: the incident plane
-  // wave and the time-dependent Neumann tractions (bf.W null: none)
+  // wave and the time-dependent Neumann tractions (bf.W null: none),
+  // evaluated into per_bf [c*nslot + slot] before every step
   BoundaryForces bf;
+  void *per_bf = nullptr;
   int *d_row0 = nullptr, *d_step = nullptr, *d_error = nullptr;
   unsigned *d_done = nullptr;
   // sources
@@ -447,6 +450,22 @@ int upload_stacey(sem2d_handle *h, const sem2d_problem_desc *d) {
     if (sl < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey node inside the domain");
     by_slot[sl].push_back(t);
   }
+  // a side that crosses periodic sides: the forces of its two ends, a
+  // periodic pair, are summed and shared (KxD, bc_abso.f90:329-332), so
+  // each end's slot lists the other's terms too
+  if (d->nperio > 0 && d->perio_master && d->perio_slave) {
+    std::vector<std::vector<int>> own = by_slot;
+    for (int k = 0; k < d->nperio; ++k) {
+      const int a = d->perio_master[k] - 1, b = d->perio_slave[k] - 1;
+      if (a < 0 || a >= np || b < 0 || b >= np) return set_err(h, SEM2D_E_ARG, "periodic node out of range");
+      const long long La = h->glob2lat[a], Lb = h->glob2lat[b];
+      const int sa = perimeter_slot(int(La % h->pitch), int(La / h->pitch), h->LX, h->LZ);
+      const int sb = perimeter_slot(int(Lb % h->pitch), int(Lb / h->pitch), h->LX, h->LZ);
+      if (sa < 0 || sb < 0 || own[sa].empty() || own[sb].empty()) continue;
+      by_slot[sa].insert(by_slot[sa].end(), own[sb].begin(), own[sb].end());
+      by_slot[sb].insert(by_slot[sb].end(), own[sa].begin(), own[sa].end());
+    }
+  }
   std::vector<int> slot, ptr(1, 0), kk, lat;
   std::vector<double> K0, K1;
   for (int sl = 0; sl < nslot; ++sl) {
@@ -467,7 +486,7 @@ int upload_stacey(sem2d_handle *h, const sem2d_problem_desc *d) {
   K0.insert(K0.end(), K1.begin(), K1.end());
   std::vector<double> H(d->hprime, d->hprime + (size_t)N * N);
   h->st_nslot = int(slot.size());
-  h->st_nterm = nt;
+  h->st_nterm = int(kk.size());
   int st;
   if ((st = dupload(h, &h->d_st_slot, slot)) || (st = dupload(h, &h->d_st_ptr, ptr)) ||
       (st = dupload(h, &h->d_st_k, kk)) || (st = dupload(h, &h->d_st_lat, lat)) ||
@@ -506,27 +525,42 @@ int upload_dirneu(sem2d_handle *h, const sem2d_problem_desc *d) {
   return SEM2D_OK;
 }
 
-// periodic node pairs: the lattice columns I = 0 and LX-1, row by row (the
-// Cartesian mesher's left and right sides); top/bottom periodic sides are
-// not supported
+// periodic node pairs: the lattice columns I = 0 and LX-1 row by row (the
+// Cartesian mesher's left and right sides) or the rows J = 0 and LZ-1
+// column by column (bottom and top)
 int upload_perio(sem2d_handle *h, const sem2d_problem_desc *d) {
   const int n = d->nperio, np = d->npoin;
   if (n <= 0) return SEM2D_OK;
   if (!d->perio_master || !d->perio_slave) return set_err(h, SEM2D_E_ARG, "periodic arrays missing");
-  if (h->st_nslot) return set_err(h, SEM2D_E_UNSUPPORTED, "Stacey sides with periodic sides");
-  if (n != h->LZ) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides other than left/right");
-  std::vector<int> seen(h->LZ, 0);
+  auto ij = [&](int node1, int &I, int &J) {
+    const long long L = h->glob2lat[node1 - 1];
+    I = int(L % h->pitch);
+    J = int(L / h->pitch);
+  };
   for (int k = 0; k < n; ++k) {
     const int a = d->perio_master[k] - 1, b = d->perio_slave[k] - 1;
     if (a < 0 || a >= np || b < 0 || b >= np) return set_err(h, SEM2D_E_ARG, "periodic node out of range");
-    const long long La = h->glob2lat[a], Lb = h->glob2lat[b];
-    const int Ia = int(La % h->pitch), Ja = int(La / h->pitch), Ib = int(Lb % h->pitch), Jb = int(Lb / h->pitch);
-    if (Ja != Jb || !((Ia == 0 && Ib == h->LX - 1) || (Ia == h->LX - 1 && Ib == 0)) || seen[Ja])
-      return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides other than left/right");
-    seen[Ja] = 1;
   }
+  int I0, J0, I1, J1;
+  ij(d->perio_master[0], I0, J0);
+  ij(d->perio_slave[0], I1, J1);
+  const bool tb = I0 == I1;
+  const int len = tb ? h->LX : h->LZ;
+  if (n != len) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides other than left/right or bottom/top");
+  std::vector<int> seen(len, 0);
+  for (int k = 0; k < n; ++k) {
+    int Ia, Ja, Ib, Jb;
+    ij(d->perio_master[k], Ia, Ja);
+    ij(d->perio_slave[k], Ib, Jb);
+    const bool ok = tb ? (Ia == Ib && ((Ja == 0 && Jb == h->LZ - 1) || (Ja == h->LZ - 1 && Jb == 0)) && !seen[Ia])
+                       : (Ja == Jb && ((Ia == 0 && Ib == h->LX - 1) || (Ia == h->LX - 1 && Ib == 0)) && !seen[Ja]);
+    if (!ok) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides other than left/right or bottom/top");
+    seen[tb ? Ia : Ja] = 1;
+  }
+  if (tb && h->nflt) return set_err(h, SEM2D_E_UNSUPPORTED, "bottom/top periodic sides with a fault");
   h->nperio = n;
-  return upload_real(h, &h->perio_f, std::vector<double>((size_t)2 * h->ndof * h->LZ, 0.0));
+  h->perio_tb = tb ? 1 : 0;
+  return upload_real(h, &h->perio_f, std::vector<double>((size_t)2 * h->ndof * len, 0.0));
 }
 
 // A time function on the device: the TAB rows and their spline second
@@ -672,6 +706,7 @@ int upload_boundary_forces(sem2d_handle *h, const sem2d_problem_desc *d) {
   if ((st = dupload(h, &dW, W)) || (st = dupload(h, &dphi, phi)) || (st = dupload(h, &dfn, fn)) ||
       (st = dupload(h, &dstf, stfs)))
     return st;
+  if ((st = upload_real(h, &h->per_bf, std::vector<double>((size_t)nd * nslot, 0.0)))) return st;
   h->bf.W = dW;
   h->bf.fn = dfn;
   h->bf.phi = dphi;
@@ -978,7 +1013,8 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.per_kd = h->per_kd;
   bc.per_dir = h->ndir ? h->per_dir : nullptr;
   bc.perio_f = h->nperio ? h->perio_f : nullptr;
-  bc.bf = h->bf;
+  bc.perio_tb = h->perio_tb;
+  bc.per_bf = h->bf.W ? h->per_bf : nullptr;
   bc.jf1 = h->nflt ? h->jf1 : -1;
   bc.jf2 = h->nflt ? h->jf2 : -1;
   bc.has_fault = h->nflt ? 1 : 0;
@@ -1033,6 +1069,16 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
 // Under HHT-alpha (cal = 1 - alpha != 0) the displacement is d_alpha =
 // d_pred - (1-alpha)(dt v + (1/2-beta) dt^2 a) (displ_alpha, solver.f90:
 // 106-113, bc_gen.f90:295).
+// The boundary forces of the step about to run (it = completed steps + 1),
+// one thread per perimeter slot: per_bf[c*nslot + s] (BoundaryForces).
+template <typename real>
+__global__ void boundary_force_kernel(const BoundaryForces bf, real *per_bf, int ndof, int nslot, const int *step) {
+  const int s = blockIdx.x * blockDim.x + threadIdx.x;
+  if (s >= nslot) return;
+  const int it = *step + 1;
+  for (int c = 0; c < ndof; ++c) per_bf[c * nslot + s] = real(boundary_force(bf, ndof, nslot, s, c, it));
+}
+
 template <typename real>
 __global__ void stacey_kernel(real *per_kd, const real *D, const real *V, const real *A, real cal, real dt, real cd2,
                               int nused, const int *slot, const int *ptr, const int *kk, const int *lat,
@@ -1161,6 +1207,13 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
   FaultParams<real> f;
   BulkConfig bc = make_config<real>(h, cur, f);
   const bool rec = h->nrec && !h->rec_separate;
+  if (h->bf.W) {
+    const int nslot = perimeter_slots(h->LX, h->LZ);
+    boundary_force_kernel<real><<<(nslot + 127) / 128, 128, 0, h->stream>>>(h->bf, (real *)h->per_bf, h->ndof,
+                                                                             nslot, h->d_step);
+    CK(cudaGetLastError());
+    h->launches++;
+  }
   if (h->march && h->march_fault_units) {
     // the units reading fault rows, then the others (the timed bulk), then
     // the fault kernel
@@ -1224,7 +1277,9 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
       pp.per_Ca = (const real *)h->per_Ca;
       pp.per_Cb = (const real *)h->per_Cb;
       pp.per_dir = h->ndir ? h->per_dir : nullptr;
-      pp.bf = h->bf;
+      pp.per_bf = h->bf.W ? (const real *)h->per_bf : nullptr;
+      pp.per_kd = h->st_nslot ? (const real *)h->per_kd : nullptr;
+      pp.tb = h->perio_tb;
       pp.dt = real(bc.dt);
       pp.cv = real(bc.cv);
       pp.cpred = real(bc.cpred);
@@ -1236,7 +1291,8 @@ int launch_one_step(sem2d_handle *h, int cur, cudaEvent_t *ev = nullptr) {
       pp.has_fault = h->nflt ? 1 : 0;
       pp.two = h->nflt ? h->two : 0;
       pp.step = h->d_step;
-      perio_kernel<real><<<(h->LZ + 127) / 128, 128, 0, h->stream>>>(pp, f);
+      const int nrow = h->perio_tb ? h->LX : h->LZ;
+      perio_kernel<real><<<(nrow + 127) / 128, 128, 0, h->stream>>>(pp, f);
       CK(cudaGetLastError());
       h->launches++;
     }
@@ -1390,7 +1446,7 @@ int launch_steps(sem2d_handle *h, int n) {
 int kernels_per_step(const sem2d_handle *h) {
   if (!h->subs.empty()) return 1;
   return 1 + (h->march && h->nflt ? (h->march_fused ? 1 : 2) : 0) + (h->nflt && h->potency ? 1 : 0) +
-         (h->nrec && h->rec_separate ? 1 : 0) + (h->st_nslot ? 1 : 0) + (h->nperio ? 1 : 0);
+         (h->nrec && h->rec_separate ? 1 : 0) + (h->st_nslot ? 1 : 0) + (h->nperio ? 1 : 0) + (h->bf.W ? 1 : 0);
 }
 
 int ensure_graph(sem2d_handle *h) {
@@ -1656,7 +1712,9 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
     h->march_fused = nfch <= kMarchWarpsHost && h->friction != SEM2D_FRICTION_RSF && !(fu && std::atoi(fu) == 0);
     if ((st = dalloc(h, &h->d_step_c, 1)) || (st = dalloc(h, &h->d_done_c, 1))) return st;
     const char *ov = std::getenv("SEM2D_OVERLAP");
-    h->march_overlap = !h->rec_separate && !(ov && std::atoi(ov) == 0);
+    // the boundary-force table of a step is written before the step on the
+    // main stream, which the two-stream schedule does not order
+    h->march_overlap = !h->rec_separate && !h->bf.W && !(ov && std::atoi(ov) == 0);
     if (h->march_overlap) {
       CK(cudaStreamCreateWithFlags(&h->fstream, cudaStreamNonBlocking));
       for (int q = 0; q < 2; ++q) {
@@ -1987,10 +2045,11 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
         rec_ez[r] = h->elem_ez[e];
       }
     }
-    // node receivers on periodic columns are sampled after the periodic pass
+    // node receivers on periodic columns (rows) are sampled after the periodic pass
     if (h->nperio && d->rec_node)
       for (int r = 0; r < h->nrec; ++r)
-        if (rI[r] == 0 || rI[r] == h->LX - 1) h->rec_separate = true;
+        if (h->perio_tb ? (rJ[r] == 0 || rJ[r] == h->LZ - 1) : (rI[r] == 0 || rI[r] == h->LX - 1))
+          h->rec_separate = true;
     std::vector<int> start(gx * gy + 1, 0), ids(h->nrec);
     for (int r = 0; r < h->nrec; ++r) start[owner[r] + 1]++;
     for (int k = 0; k < gx * gy; ++k) start[k + 1] += start[k];
@@ -2269,6 +2328,23 @@ __global__ void corrector_kernel(real *out, const real *d, const real *a, real c
 }  // namespace sem2d_detail
 
 extern "C" {
+
+int sem2d_stf_eval(const sem2d_stf *stf, int n, const double *t, double *out) {
+  if (!stf || n < 0 || (n > 0 && (!t || !out))) return SEM2D_E_ARG;
+  if (const char *m = stf_check(*stf)) {
+    sem2d::set_library_error(m);
+    return SEM2D_E_ARG;
+  }
+  StfDev hs{stf->kind, stf->ntab, stf->f0, stf->onset, stf->ampli, stf->par1, stf->par2, stf->tab_t, stf->tab_v,
+            nullptr};
+  std::vector<double> v2;
+  if (stf->kind == SEM2D_STF_TAB) {
+    v2 = stf_spline_d2(stf->tab_t, stf->tab_v, stf->ntab);
+    hs.v2 = v2.data();
+  }
+  for (int k = 0; k < n; ++k) out[k] = stf_value(hs, t[k]);
+  return SEM2D_OK;
+}
 
 int sem2d_gpu_version(void) { return SEM2D_GPU_ABI_VERSION; }
 

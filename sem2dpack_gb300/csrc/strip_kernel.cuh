@@ -612,9 +612,15 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
             for (int c = 0; c < NDOF; ++c)
               f[c] = f[c] + real(p.src_amp[((long long)s * NDOF + c) * (p.nt + 1) + it]);
         }
-        if (p.perio_f && (I == 0 || I == p.LX - 1)) {  // periodic columns: summed and finished after the step
+        if (p.perio_f && (p.perio_tb ? (J == 0 || J == p.LZ - 1) : (I == 0 || I == p.LX - 1))) {
+          // periodic columns (rows): summed and finished after the step
 #pragma unroll
-          for (int c = 0; c < NDOF; ++c) p.perio_f[(size_t(c) * p.LZ + J) * 2 + (I == 0 ? 0 : 1)] = f[c];
+          for (int c = 0; c < NDOF; ++c) {
+            if (p.perio_tb)
+              p.perio_f[(size_t(c) * p.LX + I) * 2 + (J == 0 ? 0 : 1)] = f[c];
+            else
+              p.perio_f[(size_t(c) * p.LZ + J) * 2 + (I == 0 ? 0 : 1)] = f[c];
+          }
           continue;
         }
         const int sidx = jj * TWp + xo + ii;
@@ -637,7 +643,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
             const int so = c * nslot + sp;
             fc = fc - p.per_Ca[so] * vd;
             fc = fc - p.per_Cb[so] * vd;
-            if (p.bf.W) fc = fc + real(boundary_force(p.bf, NDOF, nslot, sp, c, it));
+            if (p.per_bf) fc = fc + p.per_bf[so];
             if (p.per_kd) fc = fc - p.per_kd[so];
             if (p.per_dir && ((p.per_dir[sp] >> c) & 1)) fc = real(0);  // bc_dirneu.f90:155-167
             rm = p.per_rm[so];
@@ -666,7 +672,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
     // ---- the fault, once its last row is complete (FP64) ----
     if (jflast >= Jlo && jflast < Jlo + nr && s_stat[jflast - Jlo] == 1) {
       for (int I = I0 + tid; I < I1; I += kStripThreads) {
-        if (p.perio_f && (I == 0 || I == p.LX - 1)) continue;  // the periodic pass updates these
+        if (p.perio_f && !p.perio_tb && (I == 0 || I == p.LX - 1)) continue;  // the periodic pass updates these
         const int io = I - I0;
         double f1[2] = {0, 0}, f2[2] = {0, 0};
         for (int c = 0; c < NDOF; ++c) {

@@ -95,8 +95,49 @@ class Time:
 
 
 @dataclass
+class Stf:
+    """A source time function, &SRC_DEF stf= + its &STF_* block
+    (stf_gen.f90:45-97): kind 'RICKER', 'GAUSSIAN' (f0, onset, ampli),
+    'BRUNE' (f0 = the corner frequency fc, ampli), 'HARMONIC' (f0, ampli),
+    'USER' (onset, ampli, par1, par2) or 'TAB' (tab = (t, v) rows of the
+    reference's stf.tab file).  Values as written in the input."""
+    kind: str = "RICKER"
+    f0: float = 0.0
+    onset: float = 0.0
+    ampli: float = 1.0
+    par1: float = 0.0
+    par2: float = 0.0
+    tab: Optional[Tuple[Sequence[float], Sequence[float]]] = None
+
+    def to_c(self, keep):
+        s = abi.Stf()
+        kind = self.kind.upper()
+        if kind not in abi.STF_KINDS:
+            raise ValueError("source time function %s is not on the GPU path" % self.kind)
+        s.kind = abi.STF_KINDS[kind]
+        s.f0, s.onset, s.ampli = float(self.f0), float(self.onset), float(self.ampli)
+        s.par1, s.par2 = float(self.par1), float(self.par2)
+        if s.kind == abi.STF_TAB:
+            if self.tab is None:
+                raise ValueError("TAB time function without rows")
+            t = np.ascontiguousarray(np.asarray(self.tab[0], dtype=np.float64))
+            v = np.ascontiguousarray(np.asarray(self.tab[1], dtype=np.float64))
+            if t.shape != v.shape or t.ndim != 1:
+                raise ValueError("TAB time function: t and v must be 1-D of one length")
+            keep += [t, v]
+            s.ntab = t.size
+            s.tab_t, s.tab_v = _dptr(t), _dptr(v)
+        return s
+
+
+@dataclass
 class Sources:
-    """&SRC_DEF mechanism='FORCE' stf='RICKER' + &STF_RICKER + &SRC_FORCE."""
+    """&SRC_DEF + &STF_* + &SRC_FORCE / &SRC_MOMENT / &SRC_WAVE.
+
+    ``stf`` None is the Ricker of f0, onset, ampli (&STF_RICKER).  With
+    mechanism 'WAVE' the first source is an incident plane wave
+    (src_wave.f90): wave_angle in degrees counterclockwise from z up to the
+    wave vector, wave_phase 'P' or 'S' (ignored in SH)."""
     coords: Sequence[Sequence[float]] = ((0.0, 0.0),)
     f0: float = 1.0
     onset: float = 1.0
@@ -109,6 +150,9 @@ class Sources:
     mechanism: str = "FORCE"
     dip: float = 90.0
     M: Tuple[float, float, float, float] = (0.0, 0.0, 0.0, 0.0)
+    stf: Optional[Stf] = None
+    wave_angle: float = 0.0
+    wave_phase: str = "S"
 
 
 @dataclass
@@ -142,6 +186,11 @@ class ParDeck:
     # &BC_DEF kind='DIRNEU' + &BC_DIRNEU h, v: (tag, h, v, before_fault), h and
     # v 'N' or 'D'; before_fault when the block precedes the fault's in &BC_DEF
     dirneu: List[Tuple[int, str, str, bool]] = field(default_factory=list)
+    # &BC_DIRNEU hstf, vstf: tag -> (Stf or None, Stf or None), the time
+    # functions of the horizontal and vertical tractions of a Neumann side
+    dirneu_stf: Dict[int, Tuple[Optional[Stf], Optional[Stf]]] = field(default_factory=dict)
+    # absorbing tags with &BC_ABSORB let_wave=F
+    no_wave: List[int] = field(default_factory=list)
     # &BC_DEF kind='PERIOD' tags=(master, slave)
     periodic: Optional[Tuple[int, int]] = None
     fault: Optional[Fault] = None
@@ -206,14 +255,23 @@ class ParDeck:
         if len(bcs) > abi.MAX_BCS:
             raise ValueError("too many boundary conditions")
         d.nbcs = len(bcs)
+        for t in self.dirneu_stf:
+            if t not in [q[0] for q in self.dirneu]:
+                raise ValueError("traction time functions for tag %d, which is not a DIRNEU side" % t)
         for k, (kind, tags) in enumerate(bcs):
             d.bcs[k].kind = kind
             if kind == abi.BC_DIRNEU:
                 d.bcs[k].tag[:] = [int(tags[0]), 0]
                 d.bcs[k].dirichlet = int(tags[1])
+                hs, vs = self.dirneu_stf.get(int(tags[0]), (None, None))
+                if hs is not None:
+                    d.bcs[k].hstf = hs.to_c(keep)
+                if vs is not None:
+                    d.bcs[k].vstf = vs.to_c(keep)
                 continue
             d.bcs[k].tag[:] = [int(tags[0]), int(tags[1])]
             d.bcs[k].stacey = int(kind == abi.BC_ABSORB and tags[0] in self.stacey)
+            d.bcs[k].no_wave = int(kind == abi.BC_ABSORB and tags[0] in self.no_wave)
         f = self.fault
         for i, name in enumerate(abi.FP_NAMES):
             d.flt_value[i] = abi.FP_DEFAULTS[name]
@@ -265,12 +323,19 @@ class ParDeck:
                     setattr(d, attr, _dptr(arr))
             d.ricker_f0, d.ricker_onset, d.ricker_ampli = s.f0, s.onset, s.ampli
             d.force_angle = s.angle
-            mechs = {"FORCE": 0, "EXPLOSION": 1, "DOUBLE_COUPLE": 2, "MOMENT": 3}
+            mechs = {"FORCE": 0, "EXPLOSION": 1, "DOUBLE_COUPLE": 2, "MOMENT": 3, "WAVE": 4}
             if s.mechanism.upper() not in mechs:
                 raise ValueError("source mechanism %s is not on the GPU path" % s.mechanism)
             d.src_mech = mechs[s.mechanism.upper()]
             d.src_M[:] = [float(v) for v in s.M]
             d.src_dip = s.dip
+            if s.stf is not None:
+                d.stf = s.stf.to_c(keep)
+            d.wave_angle = float(s.wave_angle)
+            phases = {"P": abi.WAVE_P, "S": abi.WAVE_S}
+            if s.wave_phase.upper() not in phases:
+                raise ValueError("WAVE_read: phase must be S or P")
+            d.wave_phase = phases[s.wave_phase.upper()]
         r = self.receivers
         if r is not None:
             if r.coords is not None:

@@ -23,8 +23,11 @@ between blocks (``#`` comments, anything after the ``/``) is ignored.
                 scalar values (bc_dynflt*.f90)
   &TIME         kind, Dt, Courant, TotalTime, NbSteps + &TIME_NEWMARK or &TIME_HHTA alpha, rho
                 beta, gamma (time.f90:122-315)
-  &SRC_DEF      stf='RICKER', mechanism='FORCE', coord or file + &STF_RICKER f0,
-                onset, ampli + &SRC_FORCE angle (src_gen.f90, stf_ricker.f90)
+  &SRC_DEF      stf 'RICKER', 'GAUSSIAN', 'BRUNE', 'HARMONIC', 'TAB' or 'USER'
+                + its &STF_* block (stf_*.f90); mechanism 'FORCE' + &SRC_FORCE
+                angle, 'EXPLOSION', 'DOUBLE_COUPLE', 'MOMENT' (src_moment.f90) or
+                'WAVE' + &SRC_WAVE angle, phase (src_wave.f90); coord or file
+  &BC_ABSORB    stacey, let_wave; &BC_DIRNEU hstf, vstf + their &STF_* blocks
   &REC_LINE     number, first, last or file, field, isamp, AtNode (receivers.f90)
 
 and names the blocks it skips in ``deck.skipped``: plots, snapshots,
@@ -32,8 +35,8 @@ energies, and the option blocks the reference would not read for this deck
 (as it does, a &SRC_WAVE next to a mechanism='FORCE' source, or a
 &MESH_EMC2 under method='CARTESIAN', is ignored).  A selecting block that
 asks for something off the GPU path (another mesher, material kind,
-boundary kind, source mechanism or time scheme, a traction time function,
-a SPLINE or HETE1 distribution) raises ValueError.
+boundary kind, source mechanism, time function or time scheme, a SPLINE or
+HETE1 distribution) raises ValueError.
 
 Material and fault values given as distributions (rhoH, cpH, csH, etaH,
 TtH, TnH, MuSH, DcH, aH, ... followed by &DIST_* blocks) are evaluated on
@@ -176,6 +179,23 @@ def deck_from_parinp(text, precision=None, base=None):
             pos = q + 1
         return out
 
+    def take_stf(j, sname):
+        """Stf of the first &STF_<sname> block after block j (STF_read,
+        stf_gen.f90:45-97: the namelist read searches forward from the
+        block that names the function), and its index."""
+        sname = str(sname).strip().upper()
+        if sname not in ("RICKER", "GAUSSIAN", "BRUNE", "HARMONIC", "TAB", "USER"):
+            raise ValueError("source time function %s is not on the GPU path" % sname)
+        q = j + 1
+        while q < len(blocks) and blocks[q][0] != "STF_" + sname:
+            q += 1
+        if q >= len(blocks):
+            if sname == "TAB":  # &STF_TAB is optional: file = 'stf.tab'
+                return _stf_values(sname, {}, base), j
+            raise ValueError("%s: input block STF_%s not found" % (sname, sname))
+        consumed.add(q)
+        return _stf_values(sname, blocks[q][1], base), q
+
     kw = {}
     if precision is not None:
         kw["precision"] = precision
@@ -258,6 +278,8 @@ def deck_from_parinp(text, precision=None, base=None):
                 absorbing.extend(int(t) for t in tags)
                 if nxt[0] == "BC_ABSORB" and nxt[1].get("stacey", False):
                     deck.stacey.extend(int(t) for t in tags)
+                if nxt[0] == "BC_ABSORB" and not nxt[1].get("let_wave", True):
+                    deck.no_wave.extend(int(t) for t in tags)
             elif kind == "DYNFLT":
                 fault = fault or Fault()
                 # a single tag is a one-sided fault: tags = (tag, 0) (bc_gen.f90:126-133)
@@ -269,12 +291,23 @@ def deck_from_parinp(text, precision=None, base=None):
                 deck.periodic = (int(tags[0]), int(tags[1]))
             elif kind == "DIRNEU":
                 b = nxt[1] if nxt[0] == "BC_DIRNEU" else {}
-                extra = set(b) - {"h", "v"}
+                extra = set(b) - {"h", "v", "hstf", "vstf"}
                 if extra:
-                    raise ValueError("&BC_DIRNEU %s (traction time functions) is not on the GPU path"
-                                     % ", ".join(sorted(extra)))
+                    raise ValueError("&BC_DIRNEU %s is not on the GPU path" % ", ".join(sorted(extra)))
                 h, v = str(b.get("h", "N")).upper(), str(b.get("v", "N")).upper()
                 deck.dirneu.extend((int(t), h, v, fault is None) for t in tags)
+                # bc_DIRNEU_read (bc_dirneu.f90:50-112): the time function of a
+                # Neumann component reads the next &STF_* block, h then v; a
+                # Dirichlet component's name is reset to 'none'
+                pos, stfs = k + 1, [None, None]
+                for c, (key, bcc) in enumerate((("hstf", h), ("vstf", v))):
+                    name_c = str(b.get(key, "none")).strip()
+                    if bcc == "D" or name_c.lower() == "none":
+                        continue
+                    stfs[c], pos = take_stf(pos, name_c)
+                if stfs[0] is not None or stfs[1] is not None:
+                    for t in tags:
+                        deck.dirneu_stf[int(t)] = (stfs[0], stfs[1])
             else:
                 raise ValueError("boundary kind %s is not on the GPU path" % kind)
         elif name in ("BC_ABSORB", "BC_DIRNEU"):
@@ -349,11 +382,32 @@ def deck_from_parinp(text, precision=None, base=None):
             time.rho = float(it.get("rho", 0.5))
         elif name == "SRC_DEF":
             mech = str(it.get("mechanism", "FORCE")).upper()
-            if str(it.get("stf", "RICKER")).upper() != "RICKER" or \
-                    mech not in ("FORCE", "EXPLOSION", "DOUBLE_COUPLE", "MOMENT"):
-                raise ValueError("only RICKER force and moment sources are on the GPU path")
+            if mech not in ("FORCE", "EXPLOSION", "DOUBLE_COUPLE", "MOMENT", "WAVE"):
+                raise ValueError("source mechanism %s is not on the GPU path" % mech)
             src = src or Sources(coords=[])
             src.mechanism = mech
+            sname = str(it.get("stf", "RICKER")).strip().upper()
+            if sname == "RICKER":
+                q = k + 1
+                while q < len(blocks) and blocks[q][0] != "STF_RICKER":
+                    q += 1
+                if q < len(blocks):
+                    consumed.add(q)
+                    r = blocks[q][1]
+                    src.f0 = float(r.get("f0", 0.0))
+                    src.onset = float(r.get("onset", 0.0))
+                    src.ampli = float(r.get("ampli", 1.0))
+            else:
+                src.stf, _ = take_stf(k, sname)
+            if mech == "WAVE":
+                # WAVE_read reads the first &SRC_WAVE of the file (src_gen.f90:187-190)
+                w = next((b for n_, b in blocks if n_ == "SRC_WAVE"), None)
+                if w is None:
+                    raise ValueError("WAVE_read: SRC_WAVE input block not found")
+                src.wave_angle = float(w.get("angle", 0.0))
+                src.wave_phase = str(w.get("phase", "S")).strip().upper()
+                if src.wave_phase not in ("P", "S"):
+                    raise ValueError("WAVE_read: phase must be S or P")
             f = str(it.get("file", "")).strip()
             if f and f.lower() != "none":
                 # one source per line: x, z [, time delay [, relative amplitude]]
@@ -452,6 +506,29 @@ def _evaluate(deck, fault_dists, mat_dists):
                 const = m.kv_eta if name == "kveta" else getattr(m, name)
                 arr[sel] = md[name](px[sel], pz[sel]) if name in md else const
             m.hetero = True
+
+
+def _stf_values(sname, b, base):
+    """Stf of an &STF_<sname> block, with the reference's defaults
+    (stf_gaussian.f90:45-47, stf_brune.f90:43-44, stf_harmonic.f90:41-42,
+    stf_user.f90:47-52, stf_tabulated.f90:47-63)."""
+    from .deck import Stf
+    if sname == "RICKER":
+        return Stf("RICKER", f0=float(b.get("f0", 0.0)), onset=float(b.get("onset", 0.0)),
+                   ampli=float(b.get("ampli", 1.0)))
+    if sname == "GAUSSIAN":
+        return Stf("GAUSSIAN", f0=float(b.get("f0", 1.0)), onset=float(b.get("onset", 0.0)),
+                   ampli=float(b.get("ampli", 1.0)))
+    if sname == "BRUNE":
+        return Stf("BRUNE", f0=float(b.get("fc", 1.0)), ampli=float(b.get("ampli", 1.0)))
+    if sname == "HARMONIC":
+        return Stf("HARMONIC", f0=float(b.get("f0", 0.0)), ampli=float(b.get("ampli", 0.0)))
+    if sname == "USER":
+        return Stf("USER", onset=float(b.get("onset", 0.0)), ampli=float(b.get("ampli", 1.0)),
+                   par1=float(b.get("par1", 0.0)), par2=float(b.get("par2", 0.0)))
+    f = str(b.get("file", "stf.tab")).strip()
+    t = np.loadtxt(os.path.join(base or ".", f), ndmin=2)
+    return Stf("TAB", tab=(t[:, 0].copy(), t[:, 1].copy()))
 
 
 def load_parinp(path, precision=None):

@@ -82,3 +82,41 @@ def test_abso(zbottom, znel, stacey, ndof=2, total_time=1.5):
         sources=Sources(coords=[(0.0, 0.0)], f0=30.0, onset=0.05, ampli=1.0e9, angle=90.0),
         receivers=Receivers(number=91, first=(0.0, -1.0e3), last=(4.5e3, -1.0e3), isamp=1, field="V"),
     )
+
+
+def wave_box(ndof=2, phase="P", angle=0.0, stf=None, periodic=False, no_wave=(), tdelay=None):
+    """A 2 x 1 km box (NGLL 5, 20 x 10 elements, homogeneous) with absorbing
+    sides and an incident plane wave (&SRC_DEF mechanism='WAVE' + &SRC_WAVE
+    angle, phase, src_wave.f90) with a 10 Hz Ricker; `periodic` makes the
+    left and right sides periodic, so that a wave at normal incidence is
+    one-dimensional."""
+    from sem2dpack_gb300.deck import Stf  # noqa: F401
+    dk = ParDeck(
+        ngll=5, ndof=ndof, fmax=10.0, xlim=(0.0, 2000.0), zlim=(0.0, 1000.0), nelem=(20, 10),
+        materials=[Material(tag=1, rho=2500.0, cp=5000.0, cs=2887.0)],
+        absorbing=[1, 3] if periodic else [1, 2, 3, 4],
+        time=Time(kind="leapfrog", total_time=0.5, courant=0.5),
+        sources=Sources(coords=[(0.0, 0.0)], f0=10.0, onset=0.12, ampli=1.0, mechanism="WAVE",
+                        wave_angle=angle, wave_phase=phase, stf=stf,
+                        tdelay=None if tdelay is None else [tdelay]),
+        receivers=Receivers(number=9, first=(200.0, 500.0), last=(1800.0, 500.0), field="V", isamp=1),
+    )
+    if periodic:
+        dk.periodic = (2, 4)
+    dk.no_wave = list(no_wave)
+    return dk
+
+
+def traction_box(ndof=2, hstf=None, vstf=None, h="N", v="N", tag=3):
+    """A box with absorbing sides but one (&BC_DIRNEU with time-dependent
+    tractions, bc_dirneu.f90:50-169) and no source."""
+    absorbing = [t for t in (1, 2, 3, 4) if t != tag]
+    dk = ParDeck(
+        ngll=5, ndof=ndof, fmax=10.0, xlim=(0.0, 2000.0), zlim=(0.0, 1000.0), nelem=(20, 10),
+        materials=[Material(tag=1, rho=2500.0, cp=5000.0, cs=2887.0)],
+        absorbing=absorbing, dirneu=[(tag, h, v, True)],
+        time=Time(kind="leapfrog", total_time=0.3, courant=0.5),
+        receivers=Receivers(number=9, first=(200.0, 700.0), last=(1800.0, 300.0), field="V", isamp=1),
+    )
+    dk.dirneu_stf = {tag: (hstf, vstf)}
+    return dk

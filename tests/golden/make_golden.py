@@ -80,7 +80,7 @@ def main(ref):
 
     for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState",
                  "TestFlt1D", "Bimaterial_fault", "2.5D_V-shape_rate-and-state", "2.5D_inplane",
-                 "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening"):
+                 "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening", "TestAbso"):
         out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
 
     # the other example decks, which the front end refuses (off the GPU path)

@@ -1,4 +1,5 @@
-"""Every example deck of the reference that the Cartesian front end takes,
+"""Every example deck of the reference that the Cartesian front end takes
+(14),
 run as written through the GPU path for its first 30 steps against the FP64
 oracle (FP64 <= 1e-9 for the rate-and-state decks' Newton solves, 1e-10
 otherwise; mixed <= 1e-4): seismograms, and slip and slip rate on faults.
@@ -14,7 +15,7 @@ pytestmark = pytest.mark.gpu
 
 EXAMPLES = ["LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState",
             "TestFlt1D", "Bimaterial_fault", "2.5D_V-shape_rate-and-state", "2.5D_inplane",
-            "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening"]
+            "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening", "TestAbso"]
 
 
 def rel_l2(a, b):

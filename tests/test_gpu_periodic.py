@@ -98,3 +98,30 @@ def test_bimaterial_fault_deck(golden, precision):
     assert fo[:, 1, :].max() > 1.0  # sliding at m/s
     for rec in (0, 1, 2, 3, 4):
         assert rel_l2(fg[:, rec, :201], fo[:, rec, :201]) <= TOL[precision], rec
+
+
+@pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
+@pytest.mark.parametrize("sides", ["bottom_top", "bottom_top_stacey", "left_right_stacey"])
+def test_box_other_sides(sides, precision):
+    """Bottom/top periodic sides (the rows J = 0 and LZ-1 finished by the
+    periodic pass, as EXAMPLES/TestAbso/Par.inp has them) and Stacey sides
+    that cross periodic sides (the Stacey forces of a side's two ends, a
+    periodic pair, summed and shared: bc_abso.f90:329-332)."""
+    dk = periodic_box(stacey="stacey" in sides)
+    if sides.startswith("bottom_top"):
+        dk.absorbing, dk.periodic = [2, 4], (1, 3)
+        dk.stacey = [2, 4] if "stacey" in sides else []
+        dk.receivers.first, dk.receivers.last = (-1.2e3, -1.0e3), (0.6e3, -1.0e3)  # on the bottom row
+    else:
+        dk.stacey = [1, 3]
+        dk.receivers.first, dk.receivers.last = (-1.5e3, -600.0), (0.9e3, -600.0)
+    P, d, g, o = run_both(dk, 200, precision)
+    assert d.nstacey == (0 if sides == "bottom_top" else d.nstacey) and (d.nstacey > 0) == ("stacey" in sides)
+    assert rel_l2(g.seismograms(), o.seismograms()) <= TOL[precision]
+    dg, vg = g.fields()
+    do, vo, _ = o.fields()
+    assert rel_l2(dg, do) <= TOL[precision] and rel_l2(vg, vo) <= TOL[precision]
+    m = np.ctypeslib.as_array(d.perio_master, shape=(d.nperio,)) - 1
+    s = np.ctypeslib.as_array(d.perio_slave, shape=(d.nperio,)) - 1
+    assert np.array_equal(dg[m], dg[s]) and np.array_equal(vg[m], vg[s])
+    assert np.abs(dg[m]).max() > 0

@@ -9,7 +9,8 @@ import pytest
 
 import decks
 from oracle import pyoracle as po
-from sem2dpack_gb300 import Grid, Problem, workloads
+from sem2dpack_gb300 import Grid, Problem, abi, workloads
+from sem2dpack_gb300.deck import Stf
 
 INT_FIELDS = ["ibool", "abs_node", "src_node", "rec_node", "rec_elem", "flt_node1", "flt_node2"]
 
@@ -35,13 +36,35 @@ def _sizes(d):
             "flt_V0": d.nflt}
 
 
+def _stf_fields(p):
+    if not p:
+        return None
+    s = p.contents
+    out = [s.kind, s.ntab, s.f0, s.onset, s.ampli, s.par1, s.par2]
+    if s.ntab:
+        out += list(np.ctypeslib.as_array(s.tab_t, shape=(s.ntab,)))
+        out += list(np.ctypeslib.as_array(s.tab_v, shape=(s.ntab,)))
+    return out
+
+
 def assert_same_desc(a, b):
     for attr in ("ngll", "ndof", "nelem", "npoin", "nabs", "nt", "nsrc", "nrec", "rec_nsamp",
                  "rec_isamp", "nflt", "flt_nsamp", "flt_oit", "flt_oitd", "flt_oix1", "flt_oixn",
-                 "kd2_form", "time_scheme"):
+                 "kd2_form", "time_scheme", "wave_phase", "nneu", "nneu_stf"):
         assert getattr(a, attr) == getattr(b, attr), attr
     assert a.dt == b.dt and a.flt_coefA2V == b.flt_coefA2V
-    for name, n in _sizes(a).items():
+    for attr in ("wave_angle", "wave_cp", "wave_cs", "wave_mu", "wave_lambda", "wave_tdelay"):
+        assert getattr(a, attr) == getattr(b, attr), attr
+    assert list(a.wave_ref) == list(b.wave_ref)
+    assert _stf_fields(a.src_stf) == _stf_fields(b.src_stf)
+    assert _stf_fields(a.wave_stf) == _stf_fields(b.wave_stf)
+    for k in range(a.nneu_stf):
+        sa, sb = abi.P_Stf(a.neu_stfs[k]), abi.P_Stf(b.neu_stfs[k])
+        assert _stf_fields(sa) == _stf_fields(sb), k
+    sizes = _sizes(a)
+    sizes.update({"abs_B": a.nabs, "abs_n": 2 * a.nabs, "abs_wave": a.nabs, "neu_node": a.nneu,
+                  "neu_comp": a.nneu, "neu_B": a.nneu, "neu_stf": a.nneu})
+    for name, n in sizes.items():
         x, y = _arr(a, name, n), _arr(b, name, n)
         assert (x is None) == (y is None), name
         if x is not None:
@@ -160,7 +183,7 @@ def test_stacey_problem_bit_exact():
         assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
 
 
-@pytest.mark.parametrize("case", ["periodic", "periodic_fault", "dirneu"])
+@pytest.mark.parametrize("case", ["periodic", "periodic_fault", "dirneu", "periodic_bt_stacey", "periodic_lr_stacey"])
 def test_periodic_and_dirichlet_bit_exact(case):
     """BC_PERIO_init (summed mass, boundary weights and dashpots at the ends
     of crossing sides) and BC_DIRNEU_init: the product builder and the
@@ -175,6 +198,12 @@ def test_periodic_and_dirichlet_bit_exact(case):
         if case == "periodic":
             dk.absorbing = [1, 3]
             dk.periodic = (2, 4)
+        elif case == "periodic_bt_stacey":  # as EXAMPLES/TestAbso/Par.inp
+            dk.absorbing, dk.stacey = [2, 4], [2, 4]
+            dk.periodic = (1, 3)
+        elif case == "periodic_lr_stacey":
+            dk.absorbing, dk.stacey = [1, 3], [1, 3]
+            dk.periodic = (2, 4)
         else:
             dk.absorbing = [1, 2, 3]
             dk.dirneu = [(4, "N", "D", True)]
@@ -187,6 +216,10 @@ def test_periodic_and_dirichlet_bit_exact(case):
         if m:
             assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
     assert (a.nperio > 0) == (case != "dirneu") and (a.ndir > 0) == (case == "dirneu")
+    if "stacey" in case:
+        assert a.nstacey == b.nstacey > 0
+        for name, m in (("stacey_node", a.nstacey), ("stacey_k", a.nstacey), ("stacey_K", 2 * a.nstacey)):
+            assert np.array_equal(_arr(a, name, m), _arr(b, name, m)), name
 
 
 @pytest.mark.parametrize("mech,ndof", [("EXPLOSION", 2), ("DOUBLE_COUPLE", 2), ("MOMENT", 2), ("MOMENT", 1),
@@ -203,3 +236,79 @@ def test_moment_sources_bit_exact(mech, ndof):
     a, b = P.desc(), O.desc()
     assert a.nsrc == b.nsrc > 2
     assert_same_desc(a, b)
+
+
+@pytest.mark.parametrize("ndof,phase,angle", [(1, "S", 0.0), (1, "P", 30.0), (2, "P", 0.0), (2, "S", -45.0),
+                                              (2, "P", 150.0), (2, "S", 200.0)])
+def test_wave_problem_bit_exact(ndof, phase, angle):
+    """Incident plane wave (src_wave.f90): boundary weights, normals, the
+    entries it enters and its reference point and material, product
+    builder against the oracle's restatement."""
+    dk = decks.wave_box(ndof, phase, angle, tdelay=0.01)
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    assert a.nsrc == 0 and a.wave_phase == (abi.WAVE_P if phase == "P" else abi.WAVE_S)
+    assert -180.0 <= a.wave_angle <= 180.0 and a.wave_tdelay == 0.01
+    # the reference point: the corner the wave reaches first
+    ang = (angle + 180.0) % 360.0 - 180.0
+    assert list(a.wave_ref) == [2000.0 if ang >= 0 else 0.0, 0.0 if abs(ang) < 90 else 1000.0]
+    assert a.wave_mu == 2500.0 * 2887.0 ** 2
+    n = a.nabs
+    wave = np.ctypeslib.as_array(a.abs_wave, shape=(n,))
+    assert wave.all()
+    B = np.ctypeslib.as_array(a.abs_B, shape=(n,))
+    nrm = np.ctypeslib.as_array(a.abs_n, shape=(2 * n,)).reshape(2, n)
+    assert np.allclose(np.hypot(nrm[0], nrm[1]), 1.0)
+    # the weights of a side add up to its length
+    assert np.isclose(B.sum(), 2 * 2000.0 + 2 * 1000.0)
+
+
+def test_wave_let_wave_false_and_periodic():
+    dk = decks.wave_box(2, "P", 0.0, periodic=True, no_wave=[3])
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    n = a.nabs
+    wave = np.ctypeslib.as_array(a.abs_wave, shape=(n,))
+    xz = P.grid.coord()
+    node = np.ctypeslib.as_array(a.abs_node, shape=(n,)) - 1
+    assert wave[xz[1, node] < 1.0].all() and not wave[xz[1, node] > 999.0].any()
+
+
+@pytest.mark.parametrize("kind", ["GAUSSIAN", "BRUNE", "HARMONIC", "USER", "TAB"])
+def test_source_time_functions_bit_exact(kind):
+    dk = decks.lambs_problem()
+    dk.nelem, dk.fmax = (20, 10), 8.0
+    t = np.linspace(0.0, 0.5, 11)
+    dk.sources.stf = Stf(kind, f0=10.1, onset=0.15, ampli=1.3, par1=0.7, par2=0.2,
+                         tab=(t, np.sin(20 * t)) if kind == "TAB" else None)
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    s = a.src_stf.contents
+    assert s.kind == abi.STF_KINDS[kind]
+    # the REAL namelist variables of the reference hold FP32 values
+    if kind in ("GAUSSIAN", "HARMONIC"):
+        assert s.f0 == float(np.float32(10.1))
+    if kind == "BRUNE":
+        assert s.f0 == 10.1
+
+
+def test_traction_problem_bit_exact():
+    dk = decks.traction_box(2, hstf=Stf("GAUSSIAN", f0=8.0, onset=0.1, ampli=1e6),
+                            vstf=Stf("RICKER", f0=10.0, onset=0.12, ampli=2e6))
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    assert a.nneu_stf == 2 and a.nneu == 2 * (20 * 4 + 1)
+    comp = np.ctypeslib.as_array(a.neu_comp, shape=(a.nneu,))
+    B = np.ctypeslib.as_array(a.neu_B, shape=(a.nneu,))
+    assert np.isclose(B[comp == 0].sum(), 2000.0) and np.isclose(B[comp == 1].sum(), 2000.0)
+    # a Dirichlet component drops its time function (bc_dirneu.f90:70-101)
+    dk = decks.traction_box(2, hstf=Stf("GAUSSIAN", f0=8.0, onset=0.1, ampli=1e6),
+                            vstf=Stf("RICKER", f0=10.0, onset=0.12, ampli=2e6), v="D")
+    P, O = Problem(dk), po.OracleSetup(dk)
+    a, b = P.desc(), O.desc()
+    assert_same_desc(a, b)
+    assert a.nneu_stf == 1 and a.ndir == 20 * 4 + 1

@@ -67,7 +67,8 @@ def test_namelist_reader():
     "&MESH_DEF method='MESH2D' /",
     "&BC_DEF tags=1,3, kind='KINFLT' /",
     "&TIME kind='hhta' /",
-    "&SRC_DEF stf='RICKER', coord=0,0, mechanism='WAVE' /",
+    "&SRC_DEF stf='BUTTERWORTH', coord=0,0, mechanism='FORCE' /",
+    "&SRC_DEF stf='RICKER', coord=0,0, mechanism='WAVE' / &STF_RICKER f0=1, onset=2 /",
     "&MATERIAL tag=1, kind='PLAST' /",
     "&BC_DEF tags=5,6, kind='DYNFLT' / &BC_DYNFLT TtH='PWCONR' /",
     "&BC_DEF tags=5,6, kind='DYNFLT' / &BC_DYNFLT_SWF MuSH='LINEAR' /",
@@ -292,12 +293,12 @@ def test_hht_alpha_time_block():
 
 
 def test_every_example_deck_is_taken_or_refused(golden):
-    """Each of the reference's example decks either builds (13, run on the
+    """Each of the reference's example decks either builds (14, run on the
     GPU by test_gpu_examples.py) or is refused with a ValueError naming the
-    block off the GPU path (17)."""
+    block off the GPU path (16)."""
     taken = [k for k in golden.files if k.startswith("parinp_")]
     refused = [k for k in golden.files if k.startswith("refused_")]
-    assert len(taken) == 13 and len(refused) == 17
+    assert len(taken) == 14 and len(refused) == 16
     for k in taken:
         P = Problem(deck_from_parinp(str(golden[k])))
         assert P.desc().npoin > 0, k
@@ -348,3 +349,46 @@ def test_tpv3_workload_restates_the_example(golden):
         x = np.ctypeslib.as_array(getattr(da, name), shape=(n,))
         y = np.ctypeslib.as_array(getattr(db, name), shape=(n,))
         assert np.array_equal(x, y), name
+
+
+WAVE_PARINP = """
+&GENERAL ngll=5, fmax=10d0, ndof=2 /
+&MESH_DEF method='CARTESIAN' /
+&MESH_CART xlim=0d0,2d3, zlim=0d0,1d3, nelem=20,10 /
+&MATERIAL tag=1, kind='ELAST' /
+&MAT_ELASTIC rho=2500d0, cp=5000d0, cs=2887d0 /
+&BC_DEF tag=1, kind='ABSORB' /
+&BC_DEF tag=2, kind='ABSORB' /
+&BC_ABSORB stacey=F, let_wave=F /
+&BC_DEF tag=3, kind='DIRNEU' /
+&BC_DIRNEU h='N', v='N', hstf='GAUSSIAN', vstf='RICKER' /
+&STF_GAUSSIAN f0=8d0, onset=0.1d0, ampli=1d6 /
+&STF_RICKER f0=10d0, onset=0.12d0, ampli=2d6 /
+&BC_DEF tag=4, kind='ABSORB' /
+&TIME TotalTime=0.3d0, courant=0.5d0 /
+&SRC_DEF stf='BRUNE', coord=0d0,0d0, mechanism='WAVE' /
+&STF_BRUNE ampli=2d0, fc=3d0 /
+&SRC_WAVE angle=30d0, phase='P' /
+&REC_LINE number=5, first=200d0,500d0, last=1800d0,500d0 /
+"""
+
+
+def test_wave_traction_and_time_function_blocks():
+    """&SRC_DEF mechanism='WAVE' + &SRC_WAVE (src_wave.f90:56-110), a time
+    function other than Ricker read from the block after &SRC_DEF, let_wave
+    of &BC_ABSORB, and the hstf/vstf blocks that follow &BC_DIRNEU in order
+    (bc_dirneu.f90:50-112)."""
+    from sem2dpack_gb300 import Problem, abi
+    dk = deck_from_parinp(WAVE_PARINP)
+    s = dk.sources
+    assert s.mechanism == "WAVE" and s.wave_angle == 30.0 and s.wave_phase == "P"
+    assert s.stf.kind == "BRUNE" and s.stf.f0 == 3.0 and s.stf.ampli == 2.0
+    assert dk.no_wave == [2]
+    h, v = dk.dirneu_stf[3]
+    assert h.kind == "GAUSSIAN" and h.f0 == 8.0 and v.kind == "RICKER" and v.ampli == 2e6
+    P = Problem(dk)
+    d = P.desc()
+    assert d.wave_phase == abi.WAVE_P and d.nsrc == 0
+    assert d.nneu == 2 * 81 and d.nneu_stf == 2
+    wave = np.ctypeslib.as_array(d.abs_wave, shape=(d.nabs,))
+    assert wave.sum() == d.nabs - 41  # the right side (tag 2) has let_wave=F
