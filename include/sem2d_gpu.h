@@ -303,6 +303,17 @@ typedef struct sem2d_problem_desc {
   const int *neu_stf;     /* [nneu] index into neu_stfs                     */
   int nneu_stf;
   const sem2d_stf *neu_stfs;
+
+  /* ---- element geometry of a mesh that is not rectilinear (the
+   * reference's grid%flat = F, e.g. MESH_LAYERS_build, mesh_layers.f90:338):
+   * xjaci(2,2,ngll,ngll,nelem) = [dxi/dx dxi/dz; deta/dx deta/dz] at every
+   * element GLL point (SE_InverseJacobian, spec_grid.f90:621-643) and
+   * dvol(ngll,ngll,nelem) = wgll(i) wgll(j) det J (SE_VolumeWeights,
+   * :590-602).  The element forces then take the general coefficients
+   * (nelast = 10 in P-SV, 3 in SH: MAT_ELAST_init_a, mat_elastic.f90:
+   * 290-360, and ELAST_KD1/KD2, :464-518, 589-641).  NULL: a rectilinear
+   * mesh, whose geometry follows from coord (nelast = 6 or 2). */
+  const double *xjaci, *dvol;
 } sem2d_problem_desc;
 
 typedef struct sem2d_handle sem2d_handle;

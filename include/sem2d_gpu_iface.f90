@@ -192,6 +192,8 @@ module sem2d_gpu_iface
     type(c_ptr)            :: neu_stf
     integer(c_int)         :: nneu_stf
     type(c_ptr)            :: neu_stfs
+    type(c_ptr)            :: xjaci
+    type(c_ptr)            :: dvol
   end type sem2d_problem_desc
 
   type, bind(C) :: sem2d_lattice_args

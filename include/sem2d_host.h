@@ -33,6 +33,7 @@ extern "C" {
 #define SEM2D_MAX_DOMAINS 64
 #define SEM2D_MAX_MATS 64
 #define SEM2D_MAX_BCS 16
+#define SEM2D_MAX_LAYERS 32
 
 /* &MESH_CART_DOMAIN tag, ex, ez (mesh_cartesian.f90:64-79), 1-based */
 typedef struct sem2d_domain {
@@ -175,6 +176,22 @@ typedef struct sem2d_deck {
    * phase SEM2D_WAVE_P or SEM2D_WAVE_S (ignored in SH) */
   double wave_angle;
   int wave_phase;
+
+  /* &MESH_DEF method: 0 'CARTESIAN' (the &MESH_CART values above), 1
+   * 'LAYERED' (&MESH_LAYERED + &MESH_LAYER, mesh_layers.f90:120-300): xlim
+   * and nelem[0] (nx) above, zmin, and the layers from the bottom up, each
+   * with its element rows, material tag, control nodes (4: a flat or
+   * piecewise-linear top, 9: any other distribution) and its top boundary
+   * z at the nxp control abscissae xlim[0] + (xlim[1]-xlim[0]) i/(nxp-1),
+   * nxp = nx+1 when every layer has 4 control nodes, else 2 nx+1.  ezflt,
+   * fztag, fznz above apply to the layered mesh too. */
+  int mesh_method;
+  double zmin;
+  int nlayer;
+  int layer_nz[SEM2D_MAX_LAYERS];
+  int layer_tag[SEM2D_MAX_LAYERS];
+  int layer_ngnod[SEM2D_MAX_LAYERS];
+  const double *layer_top[SEM2D_MAX_LAYERS];
 } sem2d_deck;
 
 typedef struct sem2d_grid sem2d_grid;

@@ -29,7 +29,10 @@ struct oc_setup {
   /* control-node (Q4) mesh */
   int fem_npoin;
   double *fem_coord; /* (2,fem_npoin) */
-  int *knods;        /* (4,nelem) 1-based */
+  int ngnod;         /* control nodes per element: 4 (Q4) or 9 (Q9)        */
+  int flat;          /* grid%flat: rectangles (MESH_CART), not MESH_LAYERS  */
+  int *knods;        /* (ngnod,nelem) 1-based */
+  double *xjaci, *dvol; /* a grid that is not flat: SE_InverseJacobian, SE_VolumeWeights */
   int *tag;          /* [nelem] */
   int nbnds;
   oc_bnd bnds[8];
@@ -135,9 +138,55 @@ static void q4_dershape(double s, double t, double *d /* (4,2) */) {
   d[4 + 3] = -(0.25 * sm);
 }
 
-static void elem_coorg(const oc_setup *s, int e, double *c /* (2,4) */) {
-  for (int k = 0; k < 4; k++) {
-    int n = s->knods[k + 4 * e] - 1;
+/* Q9 shape functions and derivatives (elem_q9.f90:40-110) */
+static void q9_shape(double s, double t, double *sh) {
+  double sp = s + 1.0, sm = s - 1.0, tp = t + 1.0, tm = t - 1.0, ss = s * s, tt = t * t, st = s * t;
+  sh[0] = 0.25 * sm * st * tm;
+  sh[1] = 0.25 * sp * st * tm;
+  sh[2] = 0.25 * sp * st * tp;
+  sh[3] = 0.25 * sm * st * tp;
+  sh[4] = 0.5 * tm * t * (1.0 - ss);
+  sh[5] = 0.5 * sp * s * (1.0 - tt);
+  sh[6] = 0.5 * tp * t * (1.0 - ss);
+  sh[7] = 0.5 * sm * s * (1.0 - tt);
+  sh[8] = (1.0 - ss) * (1.0 - tt);
+}
+static void q9_dershape(double s, double t, double *d /* (9,2) */) {
+  double sp = s + 1.0, sm = s - 1.0, tp = t + 1.0, tm = t - 1.0, ss = s * s, tt = t * t, st = s * t;
+  double s2 = s * 2.0, t2 = t * 2.0;
+  d[0] = 0.25 * tm * t * (s2 - 1.0);
+  d[1] = 0.25 * tm * t * (s2 + 1.0);
+  d[2] = 0.25 * tp * t * (s2 + 1.0);
+  d[3] = 0.25 * tp * t * (s2 - 1.0);
+  d[9 + 0] = 0.25 * sm * s * (t2 - 1.0);
+  d[9 + 1] = 0.25 * sp * s * (t2 - 1.0);
+  d[9 + 2] = 0.25 * sp * s * (t2 + 1.0);
+  d[9 + 3] = 0.25 * sm * s * (t2 + 1.0);
+  d[4] = -1.0 * st * tm;
+  d[5] = 0.5 * (1.0 - tt) * (s2 + 1.0);
+  d[6] = -1.0 * st * tp;
+  d[7] = 0.5 * (1.0 - tt) * (s2 - 1.0);
+  d[9 + 4] = 0.5 * (1.0 - ss) * (t2 - 1.0);
+  d[9 + 5] = -1.0 * st * sp;
+  d[9 + 6] = 0.5 * (1.0 - ss) * (t2 + 1.0);
+  d[9 + 7] = -1.0 * st * sm;
+  d[8] = -1.0 * s2 * (1.0 - tt);
+  d[9 + 8] = -1.0 * t2 * (1.0 - ss);
+}
+/* FE_getshape / FE_getdershape (fem_grid.f90) for ngnod 4 or 9:
+ * d(k + ngnod*b) */
+static void shape_n(int ng, double s, double t, double *sh) {
+  if (ng == 9) q9_shape(s, t, sh);
+  else q4_shape(s, t, sh);
+}
+static void dershape_n(int ng, double s, double t, double *d) {
+  if (ng == 9) q9_dershape(s, t, d);
+  else q4_dershape(s, t, d);
+}
+
+static void elem_coorg(const oc_setup *s, int e, double *c /* (2,ngnod) */) {
+  for (int k = 0; k < s->ngnod; k++) {
+    int n = s->knods[k + s->ngnod * e] - 1;
     c[2 * k] = s->fem_coord[2 * n];
     c[2 * k + 1] = s->fem_coord[2 * n + 1];
   }
@@ -145,11 +194,12 @@ static void elem_coorg(const oc_setup *s, int e, double *c /* (2,4) */) {
 
 /* jac = matmul(coorg, dshape(:,:,i,j))  (spec_grid.f90:551-568) */
 static void jacobian(const oc_setup *s, const double *c, int i, int j, double *jac) {
-  const double *ds = s->dshape + 8 * (i + s->ngll * j);
+  int ng = s->ngnod;
+  const double *ds = s->dshape + 2 * ng * (i + s->ngll * j);
   for (int b = 0; b < 2; b++)
     for (int a = 0; a < 2; a++) {
-      double acc = c[a] * ds[0 + 4 * b];
-      for (int k = 1; k < 4; k++) acc = acc + c[a + 2 * k] * ds[k + 4 * b];
+      double acc = c[a] * ds[0 + ng * b];
+      for (int k = 1; k < ng; k++) acc = acc + c[a + 2 * k] * ds[k + ng * b];
       jac[a + 2 * b] = acc;
     }
 }
@@ -335,21 +385,117 @@ static void rank_stable(const double *key, int n, int *idx /* 0-based out */) {
 /* ------------------------------------------------------------------ */
 /* CART_read + CART_build + MESH_STRUCTURED_* (mesh_cartesian.f90:86-314,
  * mesh_structured.f90:12-269)                                          */
-static int build_mesh(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
-  int nx = dk->nelem[0], nz = dk->nelem[1];
-  if (nx <= 0 || nz <= 0) return seterr(err, el, "CART_read: nelem must be positive"), -1;
+/* MESH_LAYERS_build (mesh_layers.f90:331-449): control nodes row by row
+ * from zmin, each layer's rows between its bottom and its top boundary
+ * (given at the nxp control abscissae), the fault row duplicated; tags by
+ * layer, then the fault zone */
+static int layered_control(oc_setup *s, const sem2d_deck *dk, int *pnx, int *pnz, int *pezflt, int *pnxp,
+                           char *err, int el) {
+  int nx = dk->nelem[0], nl = dk->nlayer, ng = 4, nz = 0;
+  if (nx <= 0) return seterr(err, el, "MESH_LAYERS_read: nx must be positive"), -1;
+  if (nl <= 0 || nl > SEM2D_MAX_LAYERS) return seterr(err, el, "MESH_LAYERS_read: nlayer or file must be set"), -1;
+  for (int k = 0; k < nl; k++) {
+    if (dk->layer_nz[k] <= 0) return seterr(err, el, "MESH_LAYERS_read: nz null, negative or missing"), -1;
+    if (dk->layer_tag[k] < 1) return seterr(err, el, "MESH_LAYERS_read: tag null, negative or missing"), -1;
+    if (dk->layer_ngnod[k] != 4 && dk->layer_ngnod[k] != 9)
+      return seterr(err, el, "MESH_LAYERS_read: unsupported layer top"), -1;
+    if (dk->layer_ngnod[k] > ng) ng = dk->layer_ngnod[k];
+    nz += dk->layer_nz[k];
+  }
   int ezflt = dk->ezflt;
+  if (ezflt == -1) ezflt = nz / 2;
+  if (ezflt < -1) return seterr(err, el, "MESH_LAYERS_read: ezflt must be >= -1"), -1;
+  if (ezflt >= nz) return seterr(err, el, "MESH_LAYERS_read: ezflt must be < nz"), -1;
+  int d = ng == 9 ? 2 : 1, nxp = d * nx + 1, nzp = d * nz + 1 + (ezflt > 0 ? 1 : 0);
+  s->ngnod = ng;
+  s->flat = 0;
+  s->fem_npoin = nxp * nzp;
+  s->nelem = nx * nz;
+  s->fem_coord = xcalloc(2 * (size_t)s->fem_npoin, sizeof(double));
+  s->tag = xcalloc((size_t)s->nelem, sizeof(int));
+  double *x = xcalloc((size_t)nxp, sizeof(double)), *bot = xcalloc((size_t)nxp, sizeof(double));
+  for (int i = 0; i < nxp; i++) x[i] = dk->xlim[0] + (dk->xlim[1] - dk->xlim[0]) / (double)(nxp - 1) * (double)i;
+  for (int k = 0; k < nl; k++) {
+    if (!dk->layer_top[k]) {
+      free(x); free(bot);
+      return seterr(err, el, "MESH_LAYERS_build: layer top missing"), -1;
+    }
+    for (int i = 0; i < nxp; i++)
+      if (dk->layer_top[k][i] < dk->zmin) {
+        free(x); free(bot);
+        return seterr(err, el, "MESH_LAYERS_build: zmin in MESH_LAYERED should be deeper than all layer interfaces"), -1;
+      }
+  }
+  int row = 0;
+  for (int i = 0; i < nxp; i++) {
+    s->fem_coord[2 * i] = x[i];
+    s->fem_coord[2 * i + 1] = dk->zmin;
+    bot[i] = dk->zmin;
+  }
+  row = 1;
+  int jposlast = 1;
+  for (int k = 0; k < nl; k++) {
+    const double *top = dk->layer_top[k];
+    int nj = d * dk->layer_nz[k], jposflt = d * ezflt + 1 - jposlast;
+    for (int j = 1; j <= nj; j++) {
+      int reps = j == jposflt ? 2 : 1;
+      for (int r = 0; r < reps; r++, row++)
+        for (int i = 0; i < nxp; i++) {
+          double *c = s->fem_coord + 2 * ((size_t)row * nxp + i);
+          c[0] = x[i] + (double)j / (double)nj * (x[i] - x[i]);
+          c[1] = bot[i] + (double)j / (double)nj * (top[i] - bot[i]);
+        }
+    }
+    jposlast += nj;
+    for (int i = 0; i < nxp; i++) bot[i] = top[i];
+  }
+  free(x);
+  free(bot);
+  int jl = 0;
+  for (int k = 0; k < nl; k++)
+    for (int j = 0; j < dk->layer_nz[k]; j++, jl++)
+      for (int i = 0; i < nx; i++) s->tag[jl * nx + i] = dk->layer_tag[k];
+  if (dk->fztag > 0 && ezflt > 0) {
+    int fznz = dk->fznz > 0 ? dk->fznz : 1;
+    int j1 = ezflt + 1 - fznz > 1 ? ezflt + 1 - fznz : 1;
+    int j2 = ezflt + fznz < nz ? ezflt + fznz : nz;
+    for (int j = j1; j <= j2; j++)
+      for (int i = 1; i <= nx; i++) s->tag[(j - 1) * nx + (i - 1)] = dk->fztag;
+  }
+  for (int e = 0; e < s->nelem; e++)
+    if (s->tag[e] == 0) return seterr(err, el, "MESH_LAYERS_build: Domain tags not entirely set"), -1;
+  *pnx = nx;
+  *pnz = nz;
+  *pezflt = ezflt;
+  *pnxp = nxp;
+  return 0;
+}
+
+static int build_mesh(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
+  int nx, nz, ezflt, nxp;
+  s->ngnod = 4;
+  s->flat = 1;
+  if (dk->mesh_method == 1) {
+    if (layered_control(s, dk, &nx, &nz, &ezflt, &nxp, err, el)) return -1;
+    s->nx = nx;
+    s->nz = nz;
+    s->ezflt = ezflt;
+  } else {
+  nx = dk->nelem[0];
+  nz = dk->nelem[1];
+  if (nx <= 0 || nz <= 0) return seterr(err, el, "CART_read: nelem must be positive"), -1;
+  ezflt = dk->ezflt;
   if (ezflt >= nz) return seterr(err, el, "CART_read: ezflt must be < nelem(2)"), -1;
   if (ezflt == -1) ezflt = nz / 2;
   if (ezflt < -1) return seterr(err, el, "CART_read: ezflt must be >= -1"), -1;
   s->nx = nx;
   s->nz = nz;
   s->ezflt = ezflt;
-  int nxp = nx + 1, nzp = ezflt > 0 ? nz + 2 : nz + 1;
+  nxp = nx + 1;
+  int nzp = ezflt > 0 ? nz + 2 : nz + 1;
   s->fem_npoin = nxp * nzp;
   s->nelem = nx * nz;
   s->fem_coord = xcalloc(2 * (size_t)s->fem_npoin, sizeof(double));
-  s->knods = xcalloc(4 * (size_t)s->nelem, sizeof(int));
   s->tag = xcalloc((size_t)s->nelem, sizeof(int));
   double *x = xcalloc((size_t)nxp, sizeof(double)), *z = xcalloc((size_t)nzp, sizeof(double));
   double hx = (dk->xlim[1] - dk->xlim[0]) / (double)nx;
@@ -392,18 +538,39 @@ static int build_mesh(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   }
   for (int e = 0; e < s->nelem; e++)
     if (s->tag[e] == 0) return seterr(err, el, "CART_build: Domain tags not entirely set"), -1;
-  /* connectivity: elements numbered left to right, bottom to top */
+  }
+  /* MESH_STRUCTURED_connectivity (mesh_structured.f90:31-99): elements
+   * numbered left to right, bottom to top; Q9 nodes on the doubled grid */
+  int ng = s->ngnod;
+  s->knods = xcalloc((size_t)ng * s->nelem, sizeof(int));
   int k = 0;
-  for (int j = 1; j <= nz; j++)
-    for (int i = 1; i <= nx; i++, k++) {
-      s->knods[4 * k + 0] = (j - 1) * nxp + i;
-      s->knods[4 * k + 1] = (j - 1) * nxp + i + 1;
-      s->knods[4 * k + 2] = j * nxp + i + 1;
-      s->knods[4 * k + 3] = j * nxp + i;
+  for (int je = 1; je <= nz; je++)
+    for (int ie = 1; ie <= nx; ie++, k++) {
+      int *kn = s->knods + (size_t)ng * k;
+      if (ng == 4) {
+        int i = ie, j = je;
+        kn[0] = (j - 1) * nxp + i;
+        kn[1] = (j - 1) * nxp + i + 1;
+        kn[2] = j * nxp + i + 1;
+        kn[3] = j * nxp + i;
+      } else {
+        int i = 2 * (ie - 1) + 1, j = 2 * (je - 1) + 1;
+#define SUB2IND(ii, jj) (((jj) - 1) * nxp + (ii))
+        kn[0] = SUB2IND(i, j);
+        kn[1] = SUB2IND(i + 2, j);
+        kn[2] = SUB2IND(i + 2, j + 2);
+        kn[3] = SUB2IND(i, j + 2);
+        kn[4] = SUB2IND(i + 1, j);
+        kn[5] = SUB2IND(i + 2, j + 1);
+        kn[6] = SUB2IND(i + 1, j + 2);
+        kn[7] = SUB2IND(i, j + 1);
+        kn[8] = SUB2IND(i + 1, j + 1);
+#undef SUB2IND
+      }
     }
   if (ezflt > 0)
     for (int e = nx * ezflt; e < s->nelem; e++)
-      for (int c = 0; c < 4; c++) s->knods[4 * e + c] += nxp;
+      for (int c = 0; c < ng; c++) s->knods[(size_t)ng * e + c] += nxp;
   /* boundaries: bnds(1..4) = sides D,R,U,L; 5 = fault down, 6 = fault up */
   s->nbnds = ezflt > 0 ? 6 : 4;
   int cnt[6] = {nx, nz, nx, nz, nx, nx};
@@ -454,9 +621,9 @@ static int build_mesh(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   int *perm_inv = xcalloc((size_t)ne + 2, sizeof(int));
   for (int i = 1; i <= ne; i++) perm_inv[perm[i]] = i;
   /* FE_reorder (fem_grid.f90:505-520) */
-  int *kn2 = xcalloc(4 * (size_t)ne, sizeof(int)), *tg2 = xcalloc((size_t)ne, sizeof(int));
+  int *kn2 = xcalloc((size_t)ng * ne, sizeof(int)), *tg2 = xcalloc((size_t)ne, sizeof(int));
   for (int i = 1; i <= ne; i++) {
-    memcpy(kn2 + 4 * (i - 1), s->knods + 4 * (perm[i] - 1), 4 * sizeof(int));
+    memcpy(kn2 + (size_t)ng * (i - 1), s->knods + (size_t)ng * (perm[i] - 1), (size_t)ng * sizeof(int));
     tg2[i - 1] = s->tag[perm[i] - 1];
   }
   free(s->knods);
@@ -494,25 +661,26 @@ static int build_grid(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   s->wgll = xcalloc((size_t)n, sizeof(double));
   s->H = xcalloc((size_t)n * n, sizeof(double));
   oc_gll_info(n, s->xgll, s->wgll, s->H);
-  s->shape = xcalloc(4 * (size_t)n * n, sizeof(double));
-  s->dshape = xcalloc(8 * (size_t)n * n, sizeof(double));
+  int ng = s->ngnod;
+  s->shape = xcalloc((size_t)ng * n * n, sizeof(double));
+  s->dshape = xcalloc(2 * (size_t)ng * n * n, sizeof(double));
   for (int j = 0; j < n; j++)
     for (int i = 0; i < n; i++) {
-      q4_shape(s->xgll[i], s->xgll[j], s->shape + 4 * (i + n * j));
-      q4_dershape(s->xgll[i], s->xgll[j], s->dshape + 8 * (i + n * j));
+      shape_n(ng, s->xgll[i], s->xgll[j], s->shape + ng * (i + n * j));
+      dershape_n(ng, s->xgll[i], s->xgll[j], s->dshape + 2 * ng * (i + n * j));
     }
   /* FE_SetConnectivity: vertex lists in head-insertion order */
   int nv = s->fem_npoin, ne = s->nelem;
   int *vcnt = xcalloc((size_t)nv + 1, sizeof(int));
   for (int e = 0; e < ne; e++)
-    for (int c = 0; c < 4; c++) vcnt[s->knods[4 * e + c]]++;
+    for (int c = 0; c < 4; c++) vcnt[s->knods[s->ngnod * e + c]]++;
   int *vstart = xcalloc((size_t)nv + 2, sizeof(int));
   for (int k = 1; k <= nv; k++) vstart[k + 1] = vstart[k] + vcnt[k];
   int *velem = xcalloc(4 * (size_t)ne, sizeof(int)), *vnode = xcalloc(4 * (size_t)ne, sizeof(int));
   int *vfill = xcalloc((size_t)nv + 1, sizeof(int));
   for (int e = 0; e < ne; e++)
     for (int c = 0; c < 4; c++) {
-      int k = s->knods[4 * e + c];
+      int k = s->knods[s->ngnod * e + c];
       /* head insertion: the last inserted element comes first */
       int pos = vstart[k] + vcnt[k] - 1 - vfill[k]++;
       velem[pos] = e + 1;
@@ -523,8 +691,8 @@ static int build_grid(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   for (int e = 1; e <= ne; e++)
     for (int nn_ = 1; nn_ <= 4; nn_++) {
       if (econn_e[(nn_ - 1) + 4 * (e - 1)] > 0) continue;
-      int k1 = s->knods[(ek1[nn_ - 1] - 1) + 4 * (e - 1)];
-      int k2 = s->knods[(ek2[nn_ - 1] - 1) + 4 * (e - 1)];
+      int k1 = s->knods[(ek1[nn_ - 1] - 1) + s->ngnod * (e - 1)];
+      int k2 = s->knods[(ek2[nn_ - 1] - 1) + s->ngnod * (e - 1)];
       int found = 0;
       for (int p1 = vstart[k1]; p1 < vstart[k1 + 1] && !found; p1++) {
         int ee = velem[p1];
@@ -566,7 +734,7 @@ static int build_grid(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
     for (int c = 0; c < 4; c++) {
       if (IB(s, ivtx[c], jvtx[c], e) > 0) continue;
       npoin++;
-      int k = s->knods[c + 4 * e];
+      int k = s->knods[c + s->ngnod * e];
       for (int p = vstart[k]; p < vstart[k + 1]; p++) {
         int c2 = vnode[p] - 1;
         IB(s, ivtx[c2], jvtx[c2], velem[p] - 1) = npoin;
@@ -579,15 +747,15 @@ static int build_grid(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   /* SE_init_coord: coord = matmul(coorg, shape) */
   s->coord = xcalloc(2 * (size_t)npoin, sizeof(double));
   for (int e = 0; e < ne; e++) {
-    double c[8];
+    double c[18];
     elem_coorg(s, e, c);
     for (int j = 0; j < n; j++)
       for (int i = 0; i < n; i++) {
-        const double *sh = s->shape + 4 * (i + n * j);
+        const double *sh = s->shape + ng * (i + n * j);
         int p = IB(s, i, j, e) - 1;
         for (int a = 0; a < 2; a++) {
           double acc = c[a] * sh[0];
-          for (int k = 1; k < 4; k++) acc = acc + c[a + 2 * k] * sh[k];
+          for (int k = 1; k < ng; k++) acc = acc + c[a + 2 * k] * sh[k];
           s->coord[2 * p + a] = acc;
         }
       }
@@ -670,7 +838,7 @@ static void normal_and_weights(oc_setup *s, oc_bnd *bd, double *norm /* (np,2) *
     edge_ij(n, ed, it, jt);
     int ldim = (ed == 1 || ed == 3) ? 0 : 1;
     double sgn = (ed == 3 || ed == 4) ? -1.0 : 1.0;
-    double c[8];
+    double c[18];
     elem_coorg(s, e, c);
     for (int k = 0; k < n; k++) {
       double jac[4];
@@ -773,7 +941,7 @@ static int build_time(oc_setup *s, const sem2d_deck *dk, char *err, int el) {
   int n = s->ngll;
   double rlamdamin = 1e308, max_c_dx = 0.0;
   for (int e = 0; e < s->nelem; e++) {
-    double c[8];
+    double c[18];
     elem_coorg(s, e, c);
     double hsq[4];
     hsq[0] = (c[2] - c[0]) * (c[2] - c[0]) + (c[3] - c[1]) * (c[3] - c[1]);
@@ -874,7 +1042,7 @@ static void build_mass(oc_setup *s) {
   int n = s->ngll, nd = s->ndof;
   s->rmass = xcalloc((size_t)s->npoin * nd, sizeof(double));
   for (int e = 0; e < s->nelem; e++) {
-    double c[8];
+    double c[18];
     elem_coorg(s, e, c);
     for (int j = 0; j < n; j++)
       for (int i = 0; i < n; i++) {
@@ -906,6 +1074,34 @@ static void st_push(oc_setup *s, int node, int k, const int *edge, double K0, do
   s->st_K[s->nst] = K0;
   s->st_K1[s->nst] = K1;
   s->nst = m;
+}
+
+/* SE_InverseJacobian (invert2, utils.f90:88-110) and SE_VolumeWeights
+ * (spec_grid.f90:590-602) at every element GLL point of a grid that is not
+ * flat */
+static int build_general_geometry(oc_setup *s, char *err, int el) {
+  int n = s->ngll;
+  size_t npt = (size_t)n * n * s->nelem;
+  s->xjaci = xcalloc(4 * npt, sizeof(double));
+  s->dvol = xcalloc(npt, sizeof(double));
+  for (int e = 0; e < s->nelem; e++) {
+    double c[18];
+    elem_coorg(s, e, c);
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        double jac[4];
+        jacobian(s, c, i, j, jac);
+        double det = jac[0] * jac[3] - jac[2] * jac[1];
+        if (det <= 0.0) return seterr(err, el, "SE_InverseJacobian: undefined Jacobian"), -1;
+        size_t q = i + (size_t)n * j + (size_t)n * n * e;
+        s->xjaci[4 * q + 0] = jac[3] / det;
+        s->xjaci[4 * q + 1] = -jac[1] / det;
+        s->xjaci[4 * q + 2] = -jac[2] / det;
+        s->xjaci[4 * q + 3] = jac[0] / det;
+        s->dvol[q] = det * (s->wgll[i] * s->wgll[j]);
+      }
+  }
+  return 0;
 }
 
 /* BC_PERIO_intersects (bc_periodic.f90:108-121) */
@@ -1093,7 +1289,7 @@ static int abso_init(oc_setup *s, int tag, int stacey, int wave, char *err, int 
     int e = bd->elem[q] - 1, ed = bd->edge[q];
     edge_ij(n, ed, it, jt);
     int ldim = (ed == 1 || ed == 3) ? 0 : 1;
-    double c8[8];
+    double c8[18];
     elem_coorg(s, e, c8);
     for (int k = 0; k < n; k++) {
       size_t p = it[k] + n * jt[k] + (size_t)n * n * e;
@@ -1294,8 +1490,9 @@ static int find_point(const oc_setup *s, const double *xz, int *eout, double *xi
         if (IB(s, i, j, e) != ig) continue;
         /* first (e,i,j) holding the node: FE_find_point always reports
          * success because it tests the initial guess (fem_grid.f90:490) */
-        double c[8];
+        double c[18];
         elem_coorg(s, e, c);
+        int ng = s->ngnod;
         double x1 = c[0] - c[4], x2 = c[1] - c[5], y1 = c[2] - c[6], y2 = c[3] - c[7];
         double area = 0.5 * fabs(x1 * y2 - x2 * y1);
         double esize = sqrt(area / PI_REF);
@@ -1303,18 +1500,18 @@ static int find_point(const oc_setup *s, const double *xz, int *eout, double *xi
         double X[2] = {s->xgll[i], s->xgll[j]};
         int it;
         for (it = 1; it <= 100; it++) {
-          double sh[4], ds[8], fv[2], fj[4], fi[4];
-          q4_shape(X[0], X[1], sh);
+          double sh[9], ds[18], fv[2], fj[4], fi[4];
+          shape_n(ng, X[0], X[1], sh);
           for (int a = 0; a < 2; a++) {
             double acc = c[a] * sh[0];
-            for (int k = 1; k < 4; k++) acc = acc + c[a + 2 * k] * sh[k];
+            for (int k = 1; k < ng; k++) acc = acc + c[a + 2 * k] * sh[k];
             fv[a] = acc - xz[a];
           }
-          q4_dershape(X[0], X[1], ds);
+          dershape_n(ng, X[0], X[1], ds);
           for (int b = 0; b < 2; b++)
             for (int a = 0; a < 2; a++) {
-              double acc = c[a] * ds[4 * b];
-              for (int k = 1; k < 4; k++) acc = acc + c[a + 2 * k] * ds[k + 4 * b];
+              double acc = c[a] * ds[ng * b];
+              for (int k = 1; k < ng; k++) acc = acc + c[a + 2 * k] * ds[k + ng * b];
               fj[a + 2 * b] = acc;
             }
           if (fabs(fv[0]) + fabs(fv[1]) <= tolf) break;
@@ -1329,11 +1526,11 @@ static int find_point(const oc_setup *s, const double *xz, int *eout, double *xi
         *eout = e + 1;
         *xi = X[0];
         *eta = X[1];
-        double sh[4];
-        q4_shape(*xi, *eta, sh);
+        double sh[9];
+        shape_n(ng, *xi, *eta, sh);
         for (int a = 0; a < 2; a++) {
           double acc = c[a] * sh[0];
-          for (int k = 1; k < 4; k++) acc = acc + c[a + 2 * k] * sh[k];
+          for (int k = 1; k < ng; k++) acc = acc + c[a + 2 * k] * sh[k];
           newc[a] = acc;
         }
         return 0;
@@ -1454,7 +1651,7 @@ static int moment_init(oc_setup *s, const sem2d_deck *dk, double f0, double onse
       for (int j = 0; j < n; j++)
         for (int i = 0; i < n; i++) {
           if (s->ibool[i + n * (j + (size_t)n * e)] != src) continue;
-          double c8[8], J[4];
+          double c8[18], J[4];
           elem_coorg(s, e, c8);
           jacobian(s, c8, i, j, J);
           double det = J[0] * J[3] - J[2] * J[1];
@@ -1634,6 +1831,7 @@ oc_setup *oc_setup_build(const sem2d_deck *dk, char *err, int el) {
     }
   }
   build_mass(s);
+  if (!s->flat && build_general_geometry(s, err, el)) goto fail;
   /* BC_init: periodic sides first (bc_gen.f90:221-228), then the &BC_DEF
    * order, which decides the mass snapshot of the fault */
   for (int b = 0; b < dk->nbcs; b++)
@@ -1696,6 +1894,7 @@ void oc_setup_free(oc_setup *s) {
   free(s->abs_B); free(s->abs_nx); free(s->abs_nz); free(s->abs_n); free(s->abs_wave);
   free(s->neu_node); free(s->neu_comp); free(s->neu_stf); free(s->neu_B);
   for (int q = 0; q < s->ntabs; q++) free(s->tabs[q]);
+  free(s->xjaci); free(s->dvol);
   free(s);
 }
 
@@ -1709,7 +1908,9 @@ void oc_setup_ibool(const oc_setup *s, int *ib) {
 }
 void oc_setup_coord(const oc_setup *s, double *c) { memcpy(c, s->coord, 2 * (size_t)s->npoin * sizeof(double)); }
 void oc_setup_tags(const oc_setup *s, int *t) { memcpy(t, s->tag, (size_t)s->nelem * sizeof(int)); }
-void oc_setup_knods(const oc_setup *s, int *k) { memcpy(k, s->knods, 4 * (size_t)s->nelem * sizeof(int)); }
+void oc_setup_knods(const oc_setup *s, int *k) {
+  for (int e = 0; e < s->nelem; e++) memcpy(k + 4 * (size_t)e, s->knods + (size_t)s->ngnod * e, 4 * sizeof(int));
+}
 int oc_setup_boundary(const oc_setup *s, int tag, int *nodes) {
   for (int b = 0; b < s->nbnds; b++)
     if (s->bnds[b].tag == tag) {
@@ -1868,5 +2069,7 @@ int oc_setup_desc(const oc_setup *s, sem2d_problem_desc *d) {
   d->neu_stf = s->neu_stf;
   d->nneu_stf = s->nneu_stf;
   d->neu_stfs = s->nneu_stf ? s->neu_stfs : NULL;
+  d->xjaci = s->xjaci;
+  d->dvol = s->dvol;
   return 0;
 }

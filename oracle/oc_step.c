@@ -68,6 +68,7 @@ struct oc_sim {
   double *H;
   double *acoef; /* (ngll,ngll,nelast,nelem) */
   double *dxidx, *detadz;      /* (ngll,ngll,nelem) inverse Jacobian (flat elements) */
+  double *xjaci;               /* (2,2,ngll,ngll,nelem) inverse Jacobian of a grid that is not flat, or NULL */
   double *mKx, *mKz, *mla, *mmu; /* (ngll,ngll,nelem) moduli for MAT_ELAST_stress */
   double *beta25; /* (ngll,ngll,nelem) 2.5D coefficients or NULL */
   double *kveta;
@@ -149,6 +150,60 @@ static double *dupd_or(const double *src, size_t n, double fill) {
 }
 
 /* ------------------------------------------------------------------ */
+/* MAT_ELAST_init_a for a grid that is not flat (mat_elastic.f90:290-360,
+ * nelast 3 in SH, 10 in P-SV) from the inverse Jacobian and the weights the
+ * descriptor carries (SE_InverseJacobian, SE_VolumeWeights) */
+static void init_acoef_general(oc_sim *s, const sem2d_problem_desc *dd) {
+  int n = s->ngll, ne = s->nelem, na = s->nelast;
+  size_t st = (size_t)n * n;
+  s->xjaci = dupd(dd->xjaci, 4 * st * ne);
+  for (int e = 0; e < ne; e++)
+    for (int j = 0; j < n; j++)
+      for (int i = 0; i < n; i++) {
+        size_t p = i + (size_t)n * j + st * e;
+        const double *X = dd->xjaci + 4 * p;
+        double DxiDx = X[0], DetaDx = X[1], DxiDz = X[2], DetaDz = X[3];
+        double w = dd->dvol[p];
+        double Kx = dd->Kx[p], Kz = dd->Kz[p], la = dd->la[p], mu = dd->mu[p], mux = dd->mux[p];
+        double muz = mu;
+        double *A = s->acoef + st * na * e + i + n * j;
+        s->dxidx[p] = DxiDx;
+        s->detadz[p] = DetaDz;
+        s->mKx[p] = Kx;
+        s->mKz[p] = Kz;
+        s->mla[p] = la;
+        s->mmu[p] = mu;
+        if (s->beta25) {
+          double pw;
+          if (s->ndof == 1) {
+            pw = PI_REF / dd->width;
+          } else {
+            double nu = (la / (la + mu)) / 2.0;
+            pw = (PI_REF * (1.0 - nu)) / dd->width;
+          }
+          s->beta25[p] = (w * mu) * (pw * pw);
+        }
+        double a[10];
+        if (na == 3) {
+          a[0] = (mux * DxiDx) * DxiDx + (muz * DxiDz) * DxiDz;
+          a[1] = (mux * DetaDx) * DetaDx + (muz * DetaDz) * DetaDz;
+          a[2] = (mux * DxiDx) * DetaDx + (muz * DxiDz) * DetaDz;
+        } else {
+          a[0] = (Kx * DxiDx) * DxiDx + (mu * DxiDz) * DxiDz;
+          a[1] = (la * DxiDx) * DetaDz + (mu * DxiDz) * DetaDx;
+          a[2] = (Kz * DetaDz) * DetaDz + (mu * DetaDx) * DetaDx;
+          a[3] = (Kx * DetaDx) * DetaDx + (mu * DetaDz) * DetaDz;
+          a[4] = (la * DxiDz) * DetaDx + (mu * DxiDx) * DetaDz;
+          a[5] = (Kz * DxiDz) * DxiDz + (mu * DxiDx) * DxiDx;
+          a[6] = (Kx * DxiDx) * DetaDx + (mu * DxiDz) * DetaDz;
+          a[7] = ((la + mu) * DxiDx) * DxiDz;
+          a[8] = ((la + mu) * DetaDx) * DetaDz;
+          a[9] = (Kz * DxiDz) * DetaDz + (mu * DxiDx) * DetaDx;
+        }
+        for (int k = 0; k < na; k++) A[k * st] = -(w * a[k]);
+      }
+}
+
 /* MAT_ELAST_init_a for flat elements: Jacobian from the four corner
  * nodes (Q4, elem_q4.f90), inverse Jacobian by invert2 (utils.f90:92-114),
  * weights = det(J)*wgll(i)*wgll(j) (spec_grid.f90:590-602)             */
@@ -166,6 +221,12 @@ static void init_acoef(oc_sim *s, const sem2d_problem_desc *dd) {
   s->mla = xcalloc((size_t)n * n * ne, sizeof(double));
   s->mmu = xcalloc((size_t)n * n * ne, sizeof(double));
   s->beta25 = dd->width > 0.0 ? xcalloc((size_t)n * n * ne, sizeof(double)) : NULL;
+  if (dd->xjaci) {
+    init_acoef_general(s, dd);
+    free(xg);
+    free(wg);
+    return;
+  }
   for (int e = 0; e < ne; e++) {
     int cidx[4][2] = {{0, 0}, {n - 1, 0}, {n - 1, n - 1}, {0, n - 1}};
     double c[8];
@@ -246,6 +307,16 @@ static void elem_forces(const oc_sim *s, int e, const double *dl, double *fl) {
   for (int j = 0; j < n; j++)
     for (int i = 0; i < n; i++) Ht[i + n * j] = H[j + n * i];
   const double *A = s->acoef + (size_t)n2 * s->nelast * e;
+  if (s->ndof == 1 && s->nelast == 3) { /* ELAST_KD1_SH / KD2_SH, general grid */
+    mxm(Ht, dl, t1, n);
+    mxm(dl, H, t2, n);
+    for (int q = 0; q < n2; q++) tmp[q] = A[q] * t1[q] + A[2 * n2 + q] * t2[q];
+    mxm(H, tmp, fl, n);
+    for (int q = 0; q < n2; q++) tmp[q] = A[2 * n2 + q] * t1[q] + A[n2 + q] * t2[q];
+    mxm(tmp, Ht, tmp2, n);
+    for (int q = 0; q < n2; q++) fl[q] = fl[q] + tmp2[q];
+    return;
+  }
   if (s->ndof == 1) {
     mxm(Ht, dl, t1, n); /* dU_dxi  */
     mxm(dl, H, t2, n);  /* dU_deta */
@@ -264,6 +335,20 @@ static void elem_forces(const oc_sim *s, int e, const double *dl, double *fl) {
   mxm(uz, H, t4, n);  /* dUz_deta */
   const double *a1 = A, *a2 = A + n2, *a3 = A + 2 * n2, *a4 = A + 3 * n2, *a5 = A + 4 * n2,
                *a6 = A + 5 * n2;
+  if (s->nelast == 10) { /* ELAST_KD1_PSV / KD2_PSV, general grid (mat_elastic.f90:499-516, 620-636) */
+    const double *a7 = A + 6 * n2, *a8 = A + 7 * n2, *a9 = A + 8 * n2, *a10 = A + 9 * n2;
+    for (int q = 0; q < n2; q++) tmp[q] = a1[q] * t1[q] + a7[q] * t3[q] + a8[q] * t2[q] + a2[q] * t4[q];
+    mxm(H, tmp, fx, n);
+    for (int q = 0; q < n2; q++) tmp[q] = a7[q] * t1[q] + a4[q] * t3[q] + a5[q] * t2[q] + a9[q] * t4[q];
+    mxm(tmp, Ht, tmp2, n);
+    for (int q = 0; q < n2; q++) fx[q] = fx[q] + tmp2[q];
+    for (int q = 0; q < n2; q++) tmp[q] = a8[q] * t1[q] + a5[q] * t3[q] + a6[q] * t2[q] + a10[q] * t4[q];
+    mxm(H, tmp, fz, n);
+    for (int q = 0; q < n2; q++) tmp[q] = a2[q] * t1[q] + a9[q] * t3[q] + a10[q] * t2[q] + a3[q] * t4[q];
+    mxm(tmp, Ht, tmp2, n);
+    for (int q = 0; q < n2; q++) fz[q] = fz[q] + tmp2[q];
+    return;
+  }
   for (int q = 0; q < n2; q++) tmp[q] = a1[q] * t1[q] + a2[q] * t4[q];
   mxm(H, tmp, fx, n);
   if (s->kd2)
@@ -934,7 +1019,7 @@ oc_sim *oc_sim_create(const sem2d_problem_desc *dd, char *err, int el) {
   s->ndof = nd;
   s->nelem = ne;
   s->npoin = np;
-  s->nelast = nd == 1 ? 2 : 6;
+  s->nelast = dd->xjaci ? (nd == 1 ? 3 : 10) : (nd == 1 ? 2 : 6);
   s->kd2 = dd->kd2_form;
   s->ibool = dupi(dd->ibool, (size_t)n2 * ne);
   s->H = dupd(dd->hprime, (size_t)n2);
@@ -1257,6 +1342,26 @@ void oc_sim_strain_stress(const oc_sim *s, double *eo, double *so) {
       size_t p = q + (size_t)n2 * e;
       double *ev = eo + q + (size_t)n2 * nc * e, *sv = so + q + (size_t)n2 * nc * e;
       double dx = s->dxidx[p], dz = s->detadz[p];
+      if (s->xjaci) { /* MAT_strain_SH / _PSV on a grid that is not flat (mat_gen.f90:736-772) */
+        const double *X = s->xjaci + 4 * p;
+        double xx = X[0], ex = X[1], xz = X[2], ez = X[3];
+        if (nd == 1) {
+          ev[0] = 0.5 * (g[0][0][q] * xx + g[0][1][q] * ex);
+          ev[n2] = 0.5 * (g[0][0][q] * xz + g[0][1][q] * ez);
+          sv[0] = 2.0 * s->mmu[p] * (0.5 * (gk[0][0][q] * xx + gk[0][1][q] * ex));
+          sv[n2] = 2.0 * s->mmu[p] * (0.5 * (gk[0][0][q] * xz + gk[0][1][q] * ez));
+        } else {
+          ev[0] = g[0][0][q] * xx + g[0][1][q] * ex;
+          ev[n2] = g[1][0][q] * xz + g[1][1][q] * ez;
+          ev[2 * n2] = 0.5 * (g[0][0][q] * xz + g[0][1][q] * ez + g[1][0][q] * xx + g[1][1][q] * ex);
+          double k0 = gk[0][0][q] * xx + gk[0][1][q] * ex, k1 = gk[1][0][q] * xz + gk[1][1][q] * ez;
+          double k2 = 0.5 * (gk[0][0][q] * xz + gk[0][1][q] * ez + gk[1][0][q] * xx + gk[1][1][q] * ex);
+          sv[0] = s->mKx[p] * k0 + s->mla[p] * k1;
+          sv[n2] = s->mla[p] * k0 + s->mKz[p] * k1;
+          sv[2 * n2] = 2.0 * s->mmu[p] * k2;
+        }
+        continue;
+      }
       if (nd == 1) {
         ev[0] = 0.5 * (g[0][0][q] * dx);
         ev[n2] = 0.5 * (g[0][1][q] * dz);
@@ -1316,7 +1421,7 @@ void oc_sim_free(oc_sim *s) {
                   s->swf_mus, s->swf_mud, s->swf_p, s->swf_alpha, s->theta, s->rsf_dc,
                   s->rsf_mus, s->rsf_a, s->rsf_b, s->rsf_vstar, s->rsf_vc, s->rsf_Tc,
                   s->rsf_coeft, s->D, s->V, s->T, s->Tstick, s->MU, s->sigma, s->fseries,
-                  s->d, s->v, s->a, s->beta25, s->fcoord, s->pseries, s->dxidx, s->detadz,
+                  s->d, s->v, s->a, s->beta25, s->fcoord, s->pseries, s->dxidx, s->detadz, s->xjaci,
                   s->mKx, s->mKz, s->mla, s->mmu};
   for (size_t k = 0; k < sizeof(ptrs) / sizeof(ptrs[0]); k++) free(ptrs[k]);
   free(s);

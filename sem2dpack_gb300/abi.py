@@ -51,6 +51,7 @@ BC_PERIOD = 4
 MAX_DOMAINS = 64
 MAX_MATS = 64
 MAX_BCS = 16
+MAX_LAYERS = 32
 
 # per-node fault inputs (enum in sem2d_host.h)
 FP_NAMES = ["Tt", "Tn", "Sxx", "Sxy", "Sxz", "Syz", "Szz", "cohesion", "V",
@@ -132,6 +133,7 @@ class ProblemDesc(C.Structure):
         ("abs_B", P_double), ("abs_n", P_double), ("abs_wave", P_int),
         ("nneu", c_int), ("neu_node", P_int), ("neu_comp", P_int), ("neu_B", P_double),
         ("neu_stf", P_int), ("nneu_stf", c_int), ("neu_stfs", P_Stf),
+        ("xjaci", P_double), ("dvol", P_double),
     ]
 
 
@@ -188,6 +190,9 @@ class Deck(C.Structure):
         ("flt_potency", c_int),
         ("src_mech", c_int), ("src_M", c_double * 4), ("src_dip", c_double),
         ("stf", Stf), ("wave_angle", c_double), ("wave_phase", c_int),
+        ("mesh_method", c_int), ("zmin", c_double), ("nlayer", c_int),
+        ("layer_nz", c_int * MAX_LAYERS), ("layer_tag", c_int * MAX_LAYERS),
+        ("layer_ngnod", c_int * MAX_LAYERS), ("layer_top", P_double * MAX_LAYERS),
     ]
 
 

@@ -48,6 +48,8 @@ void fill_params(const BulkConfig &c, BulkParams<real, N> &p) {
   p.per_kd = static_cast<const real *>(c.per_kd);
   p.per_dir = c.per_dir;
   p.perio_f = static_cast<real *>(c.perio_f);
+  p.gen = static_cast<const real *>(c.gen);
+  p.gen_stride = c.gen_stride;
   p.perio_tb = c.perio_tb;
   p.per_bf = static_cast<const real *>(c.per_bf);
   p.jf1 = c.jf1;
@@ -96,9 +98,11 @@ int configure_typed(const BulkConfig &c) {
   const size_t smem = strip_smem_bytes<real, N, NDOF>(c.nplanes);
   cudaError_t e = cudaFuncSetAttribute(strip_step_kernel<real, N, NDOF, MAT, FAST>,
                                        cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(strip_batch_kernel<real, N, NDOF, MAT, FAST>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if constexpr (MAT != kMatGeneral) {
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(strip_batch_kernel<real, N, NDOF, MAT, FAST>,
+                               cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  }
   if (e != cudaSuccess) {
     g_bulk_err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e);
     return 1;
@@ -155,6 +159,7 @@ int occupancy_typed(const BulkConfig &c) {
 template <typename real, int N, int NDOF, typename F>
 int dispatch_m(const BulkConfig &c, F &&f) {
   const bool fast = N == 5 && c.fast;
+  if (c.mat_elem == kMatGeneral) return f.template operator()<real, N, NDOF, kMatGeneral, false>();
   if (c.mat_elem == kMatPoint)
     return fast ? f.template operator()<real, N, NDOF, kMatPoint, (N == 5)>()
                 : f.template operator()<real, N, NDOF, kMatPoint, false>();
@@ -190,7 +195,14 @@ struct BatchOp {
   const BulkConfig &c;
   const BatchLaunch &b;
   template <typename real, int N, int NDOF, int MAT, bool FAST>
-  int operator()() const { return launch_batch_typed<real, N, NDOF, MAT, FAST>(c, b); }
+  int operator()() const {
+    if constexpr (MAT == kMatGeneral) {
+      g_bulk_err = "batches of grids that are not flat are not supported";
+      return 1;
+    } else {
+      return launch_batch_typed<real, N, NDOF, MAT, FAST>(c, b);
+    }
+  }
 };
 
 template <int N>

@@ -30,6 +30,8 @@ struct BulkConfig {
   void *Acur = nullptr, *Anext = nullptr;
   void *Fcur = nullptr, *Fnext = nullptr;  // force state planes (march kernel)
   void *mat[4] = {nullptr, nullptr, nullptr, nullptr};
+  void *gen = nullptr;           // general coefficients (mat_elem == kMatGeneral)
+  long long gen_stride = 0;
   void *kveta = nullptr, *rmass = nullptr;
   void *geo[4] = {nullptr, nullptr, nullptr, nullptr};  // xix, etaz, dxdxi, dzdeta
   void *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;

@@ -411,7 +411,13 @@ std::vector<int> rcm_order(int nx, int nz) {
 struct sem2d_grid {
   int ngll = 0, ndof = 0, nx = 0, nz = 0, ezflt = 0, npoin = 0, nelem = 0;
   Gll gll;
-  std::vector<double> xc, zc;     // control-node coordinates
+  // control nodes on a structured grid of nxp columns (row by row, the split
+  // row of a fault duplicated): ngnod 4 (Q4) or 9 (Q9, every other control
+  // node a vertex); flat: rectangles, MESH_CART (grid%flat,
+  // mesh_cartesian.f90:238) -- MESH_LAYERS_build sets it false
+  int ngnod = 4, nxp = 0;
+  bool flat = true;
+  std::vector<double> cx, cz;
   std::vector<int> elem_ex, elem_ez;  // structured position of element e (RCM order)
   std::vector<int> tag;
   std::vector<int> ibool;         // (ngll,ngll,nelem), 1-based
@@ -437,14 +443,26 @@ struct sem2d_grid {
     const int J = row0[elem_ez[e]] + j;
     return size_t(J) * LX + I;
   }
-  // control-node corner coordinates of element e: (x1,z1,...,x4,z4), counterclockwise
+  // control nodes of element e in the order of knods
+  // (MESH_STRUCTURED_connectivity, mesh_structured.f90:31-99):
+  // (x1,z1,...), the four vertices counterclockwise first
+  void control(int e, double *c) const {
+    const int d = ngnod == 9 ? 2 : 1;
+    const int i = d * elem_ex[e];
+    const int j = d * elem_ez[e] + (ezflt > 0 && elem_ez[e] >= ezflt ? 1 : 0);  // control row, split shift
+    static const int di9[9] = {0, 2, 2, 0, 1, 2, 1, 0, 1}, dj9[9] = {0, 0, 2, 2, 0, 1, 2, 1, 1};
+    static const int di4[4] = {0, 1, 1, 0}, dj4[4] = {0, 0, 1, 1};
+    for (int k = 0; k < ngnod; ++k) {
+      const size_t q = size_t(j + (ngnod == 9 ? dj9[k] : dj4[k])) * nxp + (i + (ngnod == 9 ? di9[k] : di4[k]));
+      c[2 * k] = cx[q];
+      c[2 * k + 1] = cz[q];
+    }
+  }
+  // the four vertices
   void corners(int e, double *c) const {
-    const int i = elem_ex[e], j = elem_ez[e];
-    const int jr = j + (ezflt > 0 && j >= ezflt ? 1 : 0);  // control row with the split
-    c[0] = xc[i]; c[1] = zc[jr];
-    c[2] = xc[i + 1]; c[3] = zc[jr];
-    c[4] = xc[i + 1]; c[5] = zc[jr + 1];
-    c[6] = xc[i]; c[7] = zc[jr + 1];
+    double a[18];
+    control(e, a);
+    std::copy(a, a + 8, c);
   }
 };
 
@@ -463,18 +481,70 @@ inline void q4_dshape(double s, double t, double *d) {
   d[0] = 0.25 * tm; d[1] = -(0.25 * tm); d[2] = 0.25 * tp; d[3] = -(0.25 * tp);
   d[4] = 0.25 * sm; d[5] = -(0.25 * sp); d[6] = 0.25 * sp; d[7] = -(0.25 * sm);
 }
-inline double interp4(const double *c, int a, const double *w) {
+// Q9 shape functions and derivatives (elem_q9.f90:40-110)
+inline void q9_shape(double s, double t, double *sh) {
+  const double sp = s + 1.0, sm = s - 1.0, tp = t + 1.0, tm = t - 1.0, ss = s * s, tt = t * t, st = s * t;
+  sh[0] = 0.25 * sm * st * tm;
+  sh[1] = 0.25 * sp * st * tm;
+  sh[2] = 0.25 * sp * st * tp;
+  sh[3] = 0.25 * sm * st * tp;
+  sh[4] = 0.5 * tm * t * (1.0 - ss);
+  sh[5] = 0.5 * sp * s * (1.0 - tt);
+  sh[6] = 0.5 * tp * t * (1.0 - ss);
+  sh[7] = 0.5 * sm * s * (1.0 - tt);
+  sh[8] = (1.0 - ss) * (1.0 - tt);
+}
+inline void q9_dshape(double s, double t, double *d) {  // d[k] d/ds, d[9 + k] d/dt
+  const double sp = s + 1.0, sm = s - 1.0, tp = t + 1.0, tm = t - 1.0, ss = s * s, tt = t * t, st = s * t;
+  const double s2 = s * 2.0, t2 = t * 2.0;
+  d[0] = 0.25 * tm * t * (s2 - 1.0);
+  d[1] = 0.25 * tm * t * (s2 + 1.0);
+  d[2] = 0.25 * tp * t * (s2 + 1.0);
+  d[3] = 0.25 * tp * t * (s2 - 1.0);
+  d[9 + 0] = 0.25 * sm * s * (t2 - 1.0);
+  d[9 + 1] = 0.25 * sp * s * (t2 - 1.0);
+  d[9 + 2] = 0.25 * sp * s * (t2 + 1.0);
+  d[9 + 3] = 0.25 * sm * s * (t2 + 1.0);
+  d[4] = -1.0 * st * tm;
+  d[5] = 0.5 * (1.0 - tt) * (s2 + 1.0);
+  d[6] = -1.0 * st * tp;
+  d[7] = 0.5 * (1.0 - tt) * (s2 - 1.0);
+  d[9 + 4] = 0.5 * (1.0 - ss) * (t2 - 1.0);
+  d[9 + 5] = -1.0 * st * sp;
+  d[9 + 6] = 0.5 * (1.0 - ss) * (t2 + 1.0);
+  d[9 + 7] = -1.0 * st * sm;
+  d[8] = -1.0 * s2 * (1.0 - tt);
+  d[9 + 8] = -1.0 * t2 * (1.0 - ss);
+}
+inline void shape(int ngnod, double s, double t, double *sh) {
+  if (ngnod == 9) q9_shape(s, t, sh);
+  else q4_shape(s, t, sh);
+}
+// sum_k c(a,k) w(k) in increasing k (matmul(coorg, shape))
+inline double interp(const double *c, int ngnod, int a, const double *w) {
   double acc = c[a] * w[0];
-  for (int k = 1; k < 4; ++k) acc = acc + c[a + 2 * k] * w[k];
+  for (int k = 1; k < ngnod; ++k) acc = acc + c[a + 2 * k] * w[k];
   return acc;
 }
+inline double interp4(const double *c, int a, const double *w) { return interp(c, 4, a, w); }
 // Jacobian [dx/dxi dx/deta; dz/dxi dz/deta] at (s,t), column-major
-inline void jacobian(const double *c, double s, double t, double *J) {
-  double d[8];
-  q4_dshape(s, t, d);
+// (SE_Jacobian: matmul(coorg, dshape), spec_grid.f90:551-583)
+inline void jacobian(int ngnod, const double *c, double s, double t, double *J) {
+  double d[18];
+  if (ngnod == 9) {
+    q9_dshape(s, t, d);
+  } else {
+    double d4[8];
+    q4_dshape(s, t, d4);
+    for (int k = 0; k < 4; ++k) {
+      d[k] = d4[k];
+      d[9 + k] = d4[4 + k];
+    }
+  }
   for (int b = 0; b < 2; ++b)
-    for (int a = 0; a < 2; ++a) J[a + 2 * b] = interp4(c, a, d + 4 * b);
+    for (int a = 0; a < 2; ++a) J[a + 2 * b] = interp(c, ngnod, a, d + 9 * b);
 }
+inline void jacobian(const double *c, double s, double t, double *J) { jacobian(4, c, s, t, J); }
 
 void edge_ij(int n, int edge, int k, int &i, int &j) {
   switch (edge) {
@@ -485,7 +555,10 @@ void edge_ij(int n, int edge, int k, int &i, int &j) {
   }
 }
 
-void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
+void build_lattice(sem2d_grid &g, int ezflt, const std::vector<int> &tag_s);
+
+// MESH_CART_build (mesh_cartesian.f90:238-314)
+void build_cartesian(sem2d_grid &g, const sem2d_deck &dk) {
   const int nx = dk.nelem[0], nz = dk.nelem[1];
   if (nx <= 0 || nz <= 0) throw BuildError("CART_read: nelem must be positive");
   if (dk.ngll < 2 || dk.ngll > 20) throw BuildError("ngll out of range");
@@ -501,17 +574,23 @@ void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
   g.ezflt = ezflt;
   g.nelem = nx * nz;
   g.gll = make_gll(dk.ngll);
-  const int N = g.ngll;
   // control-node coordinates (mesh_cartesian.f90:248-263); the fault row is
   // duplicated in zc
   const double hx = (dk.xlim[1] - dk.xlim[0]) / double(nx);
   const double hz = (dk.zlim[1] - dk.zlim[0]) / double(nz);
-  g.xc.resize(nx + 1);
-  for (int i = 0; i <= nx; ++i) g.xc[i] = dk.xlim[0] + hx * double(i);
+  std::vector<double> xc(nx + 1), zc;
+  for (int i = 0; i <= nx; ++i) xc[i] = dk.xlim[0] + hx * double(i);
   for (int j = 0; j <= nz; ++j) {
-    g.zc.push_back(dk.zlim[0] + hz * double(j));
-    if (ezflt > 0 && j == ezflt) g.zc.push_back(dk.zlim[0] + hz * double(j));
+    zc.push_back(dk.zlim[0] + hz * double(j));
+    if (ezflt > 0 && j == ezflt) zc.push_back(dk.zlim[0] + hz * double(j));
   }
+  g.ngnod = 4;
+  g.nxp = nx + 1;
+  for (double z : zc)
+    for (double x : xc) {
+      g.cx.push_back(x);
+      g.cz.push_back(z);
+    }
   // domain tags in structured order
   std::vector<int> tag_s(size_t(nx) * nz, dk.ndomains == 0 ? 1 : 0);
   for (int d = 0; d < dk.ndomains; ++d) {
@@ -531,6 +610,96 @@ void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
   }
   for (int t : tag_s)
     if (t == 0) throw BuildError("CART_build: Domain tags not entirely set");
+  build_lattice(g, ezflt, tag_s);
+}
+
+// MESH_LAYERS_build (mesh_layers.f90:331-449): control rows from zmin up,
+// each layer's rows interpolated between its bottom and its top boundary
+// (layer_top at the nxp control abscissae), the row of the fault split
+// duplicated; Q4 when every top is flat or piecewise linear, Q9 otherwise
+void build_layered(sem2d_grid &g, const sem2d_deck &dk) {
+  const int nx = dk.nelem[0], nl = dk.nlayer;
+  if (nx <= 0) throw BuildError("MESH_LAYERS_read: nx must be positive");
+  if (nl <= 0 || nl > SEM2D_MAX_LAYERS) throw BuildError("MESH_LAYERS_read: nlayer or file must be set");
+  if (dk.ngll < 2 || dk.ngll > 20) throw BuildError("ngll out of range");
+  if (dk.ndof != 1 && dk.ndof != 2) throw BuildError("ndof must be 1 or 2");
+  int ngnod = 4, nz = 0;
+  for (int k = 0; k < nl; ++k) {
+    if (dk.layer_nz[k] <= 0) throw BuildError("MESH_LAYERS_read: nz null, negative or missing");
+    if (dk.layer_tag[k] < 1) throw BuildError("MESH_LAYERS_read: tag null, negative or missing");
+    if (dk.layer_ngnod[k] != 4 && dk.layer_ngnod[k] != 9) throw BuildError("MESH_LAYERS_read: unsupported layer top");
+    ngnod = std::max(ngnod, dk.layer_ngnod[k]);
+    nz += dk.layer_nz[k];
+  }
+  int ezflt = dk.ezflt;
+  if (ezflt == -1) ezflt = nz / 2;
+  if (ezflt < -1) throw BuildError("MESH_LAYERS_read: ezflt must be >= -1");
+  if (ezflt >= nz) throw BuildError("MESH_LAYERS_read: ezflt must be < nz");
+  const int d = ngnod == 9 ? 2 : 1, nxp = d * nx + 1;
+  g.ngll = dk.ngll;
+  g.ndof = dk.ndof;
+  g.nx = nx;
+  g.nz = nz;
+  g.ezflt = ezflt;
+  g.nelem = nx * nz;
+  g.gll = make_gll(dk.ngll);
+  g.ngnod = ngnod;
+  g.nxp = nxp;
+  g.flat = false;
+  std::vector<double> x(nxp);
+  for (int i = 0; i < nxp; ++i) x[i] = dk.xlim[0] + (dk.xlim[1] - dk.xlim[0]) / double(nxp - 1) * double(i);
+  for (int k = 0; k < nl; ++k) {
+    if (!dk.layer_top[k]) throw BuildError("MESH_LAYERS_build: layer top missing");
+    for (int i = 0; i < nxp; ++i)
+      if (dk.layer_top[k][i] < dk.zmin)
+        throw BuildError("MESH_LAYERS_build: zmin in MESH_LAYERED should be deeper than all layer interfaces");
+  }
+  auto row = [&](const std::vector<double> &zr) {
+    g.cx.insert(g.cx.end(), x.begin(), x.end());
+    g.cz.insert(g.cz.end(), zr.begin(), zr.end());
+  };
+  std::vector<double> bot(nxp, dk.zmin), xbot = x;
+  row(bot);
+  int jposlast = 1;
+  for (int k = 0; k < nl; ++k) {  // bottom to top
+    const double *top = dk.layer_top[k];
+    const int nj = d * dk.layer_nz[k];
+    const int jposflt = d * ezflt + 1 - jposlast;
+    for (int j = 1; j <= nj; ++j) {
+      std::vector<double> zr(nxp), xr(nxp);
+      for (int i = 0; i < nxp; ++i) {
+        xr[i] = xbot[i] + double(j) / double(nj) * (x[i] - xbot[i]);
+        zr[i] = bot[i] + double(j) / double(nj) * (top[i] - bot[i]);
+      }
+      const int reps = j == jposflt ? 2 : 1;
+      for (int r = 0; r < reps; ++r) {
+        g.cx.insert(g.cx.end(), xr.begin(), xr.end());
+        g.cz.insert(g.cz.end(), zr.begin(), zr.end());
+      }
+    }
+    jposlast += nj;
+    bot.assign(top, top + nxp);  // the next layer starts from this top (bot => top)
+    xbot = x;
+  }
+  // tags: layer tags, then the fault zone
+  std::vector<int> tag_s(size_t(nx) * nz, 0);
+  int jl = 0;
+  for (int k = 0; k < nl; ++k)
+    for (int j = 0; j < dk.layer_nz[k]; ++j, ++jl)
+      for (int i = 0; i < nx; ++i) tag_s[size_t(jl) * nx + i] = dk.layer_tag[k];
+  if (dk.fztag > 0 && ezflt > 0) {
+    const int fznz = dk.fznz > 0 ? dk.fznz : 1;
+    const int j1 = std::max(ezflt + 1 - fznz, 1), j2 = std::min(ezflt + fznz, nz);
+    for (int j = j1; j <= j2; ++j)
+      for (int i = 1; i <= nx; ++i) tag_s[size_t(j - 1) * nx + (i - 1)] = dk.fztag;
+  }
+  for (int t : tag_s)
+    if (t == 0) throw BuildError("MESH_LAYERS_build: Domain tags not entirely set");
+  build_lattice(g, ezflt, tag_s);
+}
+
+void build_lattice(sem2d_grid &g, int ezflt, const std::vector<int> &tag_s) {
+  const int nx = g.nx, nz = g.nz, N = g.ngll;
   // element order
   const std::vector<int> perm = rcm_order(nx, nz);
   std::vector<int> inv(perm.size());
@@ -576,17 +745,18 @@ void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
       for (int i = 0; i < N; ++i) g.ibool[i + N * (j + size_t(N) * e)] = g.lattice[g.lat(e, i, j)];
   // coordinates: the last element (in element order) writes a shared node
   g.coord.assign(2 * size_t(np), 0.0);
-  std::vector<double> shp(4 * size_t(N) * N);
+  const int ng = g.ngnod;
+  std::vector<double> shp(size_t(ng) * N * N);
   for (int j = 0; j < N; ++j)
-    for (int i = 0; i < N; ++i) q4_shape(g.gll.x[i], g.gll.x[j], &shp[4 * (i + N * j)]);
+    for (int i = 0; i < N; ++i) shape(ng, g.gll.x[i], g.gll.x[j], &shp[ng * (i + N * j)]);
   for (int e = 0; e < g.nelem; ++e) {
-    double c[8];
-    g.corners(e, c);
+    double c[18];
+    g.control(e, c);
     for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) {
         const int p = g.ibool[i + N * (j + size_t(N) * e)] - 1;
-        g.coord[2 * p] = interp4(c, 0, &shp[4 * (i + N * j)]);
-        g.coord[2 * p + 1] = interp4(c, 1, &shp[4 * (i + N * j)]);
+        g.coord[2 * p] = interp(c, ng, 0, &shp[ng * (i + N * j)]);
+        g.coord[2 * p + 1] = interp(c, ng, 1, &shp[ng * (i + N * j)]);
       }
   }
   // boundaries: tags 1..4 = bottom, right, top, left; 5/6 = fault sides
@@ -624,6 +794,11 @@ void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
     add_bnd(5, 3, [&](int q) { return (ezflt - 1) * nx + q; }, nx, true, g.row0[ezflt - 1] + N - 1);
     add_bnd(6, 1, [&](int q) { return ezflt * nx + q; }, nx, true, g.row0[ezflt]);
   }
+}
+
+void build_grid(sem2d_grid &g, const sem2d_deck &dk) {
+  if (dk.mesh_method == 1) build_layered(g, dk);
+  else build_cartesian(g, dk);
 }
 
 }  // namespace
@@ -679,6 +854,9 @@ struct sem2d_problem {
   std::vector<int> rec_node, rec_elem;
   std::vector<double> rec_interp, rec_coord;
   std::vector<double> H, w;
+  // a grid that is not flat: inverse Jacobian and weights at every element
+  // GLL point (SE_InverseJacobian, SE_VolumeWeights)
+  std::vector<double> xjaci, dvol;
   sem2d_deck deck{};
 };
 
@@ -827,18 +1005,45 @@ double coefA2Vrhs(const sem2d_problem &P) {
   return newmark_like(P) ? P.alpha * coefA2V(P) : 0.5 * coefA2V(P);
 }
 
+// SE_InverseJacobian (invert2, utils.f90:88-110) and SE_VolumeWeights
+// (spec_grid.f90:590-602) at every element GLL point
+void build_general_geometry(sem2d_problem &P) {
+  const sem2d_grid &g = *P.g;
+  const int N = g.ngll;
+  const size_t npt = size_t(N) * N * g.nelem;
+  P.xjaci.assign(4 * npt, 0.0);
+  P.dvol.assign(npt, 0.0);
+  for (int e = 0; e < g.nelem; ++e) {
+    double c[18];
+    g.control(e, c);
+    for (int j = 0; j < N; ++j)
+      for (int i = 0; i < N; ++i) {
+        double J[4];
+        jacobian(g.ngnod, c, g.gll.x[i], g.gll.x[j], J);
+        const double det = J[0] * J[3] - J[2] * J[1];
+        if (det <= 0.0) throw BuildError("SE_InverseJacobian: undefined Jacobian");
+        const size_t q = i + N * (j + size_t(N) * e);
+        P.xjaci[4 * q + 0] = J[3] / det;
+        P.xjaci[4 * q + 1] = -J[1] / det;
+        P.xjaci[4 * q + 2] = -J[2] / det;
+        P.xjaci[4 * q + 3] = J[0] / det;
+        P.dvol[q] = det * (g.gll.w[i] * g.gll.w[j]);
+      }
+  }
+}
+
 // MAT_MASS_init (mat_mass.f90:29-61)
 void build_mass(sem2d_problem &P) {
   const sem2d_grid &g = *P.g;
   const int N = g.ngll;
   P.mass.assign(size_t(g.npoin) * P.ndof, 0.0);
   for (int e = 0; e < g.nelem; ++e) {
-    double c[8];
-    g.corners(e, c);
+    double c[18];
+    g.control(e, c);
     for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) {
         double J[4];
-        jacobian(c, g.gll.x[i], g.gll.x[j], J);
+        jacobian(g.ngnod, c, g.gll.x[i], g.gll.x[j], J);
         double dvol = J[0] * J[3] - J[2] * J[1];
         dvol = dvol * (g.gll.w[i] * g.gll.w[j]);
         const size_t q = i + N * (j + size_t(N) * e);
@@ -859,13 +1064,13 @@ void normals(const sem2d_grid &g, const sem2d_grid::Boundary &b, std::vector<dou
     const int e = b.elem[q] - 1, ed = b.edge[q];
     const int ld = (ed == 1 || ed == 3) ? 0 : 1;
     const double sg = (ed == 3 || ed == 4) ? -1.0 : 1.0;
-    double c[8];
-    g.corners(e, c);
+    double c[18];
+    g.control(e, c);
     for (int k = 0; k < N; ++k) {
       int i, j;
       edge_ij(N, ed, k, i, j);
       double J[4];
-      jacobian(c, g.gll.x[i], g.gll.x[j], J);
+      jacobian(g.ngnod, c, g.gll.x[i], g.gll.x[j], J);
       const double dx = J[0 + 2 * ld], dz = J[1 + 2 * ld];
       const double j1 = std::sqrt(dx * dx + dz * dz);
       const double tx = sg * dx / j1, tz = sg * dz / j1;
@@ -1008,8 +1213,8 @@ void abso_init(sem2d_problem &P, int tag, int stacey, int let_wave, bool wave_so
   for (size_t q = 0; q < b->elem.size(); ++q) {
     const int e = b->elem[q] - 1, ed = b->edge[q];
     const int ld = (ed == 1 || ed == 3) ? 0 : 1;
-    double c8[8];
-    g.corners(e, c8);
+    double c8[18];
+    g.control(e, c8);
     for (int k = 0; k < N; ++k) {
       int i, j;
       edge_ij(N, ed, k, i, j);
@@ -1018,7 +1223,7 @@ void abso_init(sem2d_problem &P, int tag, int stacey, int let_wave, bool wave_so
       cv[gnor] = P.cp[p];
       cv[gtan] = P.cs[p];
       double J[4];
-      jacobian(c8, g.gll.x[i], g.gll.x[j], J);
+      jacobian(g.ngnod, c8, g.gll.x[i], g.gll.x[j], J);
       const double ci = g.gll.w[k] * std::sqrt(J[0 + 2 * ld] * J[0 + 2 * ld] + J[1 + 2 * ld] * J[1 + 2 * ld]);
       const int bk = b->ib[k + size_t(N) * q] - 1;
       if (nd == 1) {
@@ -1214,18 +1419,19 @@ void find_point(const sem2d_grid &g, const double *xz, int &e_out, double &xi, d
     for (int j = 0; j < N; ++j)
       for (int i = 0; i < N; ++i) {
         if (g.ibool[i + N * (j + size_t(N) * e)] != ig) continue;
-        double c[8];
-        g.corners(e, c);
+        double c[18];
+        g.control(e, c);
+        const int ng = g.ngnod;
         const double x1 = c[0] - c[4], x2 = c[1] - c[5], y1 = c[2] - c[6], y2 = c[3] - c[7];
         const double area = 0.5 * std::fabs(x1 * y2 - x2 * y1);
         const double tolf = kTinyXabs * std::sqrt(area / kPi), tolx = kTinyXabs;
         double X[2] = {g.gll.x[i], g.gll.x[j]};
         int it;
         for (it = 1; it <= 100; ++it) {
-          double sh[4], J[4];
-          q4_shape(X[0], X[1], sh);
-          const double f0 = interp4(c, 0, sh) - xz[0], f1 = interp4(c, 1, sh) - xz[1];
-          jacobian(c, X[0], X[1], J);
+          double sh[9], J[4];
+          shape(ng, X[0], X[1], sh);
+          const double f0 = interp(c, ng, 0, sh) - xz[0], f1 = interp(c, ng, 1, sh) - xz[1];
+          jacobian(ng, c, X[0], X[1], J);
           if (std::fabs(f0) + std::fabs(f1) <= tolf) break;
           const double det = J[0] * J[3] - J[2] * J[1];
           const double i00 = J[3] / det, i10 = -J[1] / det, i01 = -J[2] / det, i11 = J[0] / det;
@@ -1239,10 +1445,10 @@ void find_point(const sem2d_grid &g, const double *xz, int &e_out, double &xi, d
         e_out = e + 1;
         xi = X[0];
         eta = X[1];
-        double sh[4];
-        q4_shape(xi, eta, sh);
-        newc[0] = interp4(c, 0, sh);
-        newc[1] = interp4(c, 1, sh);
+        double sh[9];
+        shape(ng, xi, eta, sh);
+        newc[0] = interp(c, ng, 0, sh);
+        newc[1] = interp(c, ng, 1, sh);
         return;
       }
   throw BuildError("SE_find_point: point not found");
@@ -1446,9 +1652,9 @@ void src_init(sem2d_problem &P, const sem2d_deck &dk) {
       for (int j = 0; j < N; ++j)
         for (int i = 0; i < N; ++i) {
           if (g.ibool[i + N * (j + size_t(N) * e)] != node) continue;
-          double c8[8], J[4];
-          g.corners(e, c8);
-          jacobian(c8, g.gll.x[i], g.gll.x[j], J);
+          double c8[18], J[4];
+          g.control(e, c8);
+          jacobian(g.ngnod, c8, g.gll.x[i], g.gll.x[j], J);
           const double det = J[0] * J[3] - J[2] * J[1];
           const double inv[2][2] = {{J[3] / det, -J[2] / det}, {-J[1] / det, J[0] / det}};  // d(xi,eta)/d(x,z)
           double G[2][2];
@@ -1563,6 +1769,7 @@ int sem2d_problem_build(const sem2d_grid *g, const sem2d_deck *deck, sem2d_probl
       }
     }
     build_mass(*P);
+    if (!g->flat) build_general_geometry(*P);
     // periodic sides first (bc_gen.f90:221-228)
     for (int b = 0; b < deck->nbcs; ++b)
       if (deck->bcs[b].kind == SEM2D_BC_PERIOD) {
@@ -1747,6 +1954,8 @@ int sem2d_problem_get_desc(const sem2d_problem *P, sem2d_problem_desc *d) {
   d->neu_stf = VPTR(P->neu_stf);
   d->nneu_stf = int(P->neu_stfs.size());
   d->neu_stfs = VPTR(P->neu_stfs);
+  d->xjaci = VPTR(P->xjaci);
+  d->dvol = VPTR(P->dvol);
   return SEM2D_OK;
 }
 

@@ -25,6 +25,10 @@ constexpr int kMaxSrc = 64;
 constexpr int kMatNode = 0;
 constexpr int kMatPoint = 1;
 constexpr int kMatElement = 2;
+// a grid that is not flat: the element phase reads the general coefficients
+// a1..a10 (P-SV) or a1..a3 (SH) of every element GLL point (gen), which
+// hold the moduli, the inverse Jacobian and the weights together
+constexpr int kMatGeneral = 3;
 
 // Parameters of the per-node fault update (FP64 fault state).
 template <typename real>
@@ -96,7 +100,9 @@ struct BulkParams {
   // material
   int mat_iso;      // isotropic: planes (la, mu) [P-SV] or (mu) [SH]
   const real *mat[4];
-  int mat_elem;     // material layout: kMatNode, kMatPoint or kMatElement
+  int mat_elem;     // material layout: kMatNode, kMatPoint, kMatElement or kMatGeneral
+  const real *gen;  // kMatGeneral: a_k at [k*gen_stride + (ez*nx + ex)*N*N + i + N*j]
+  long long gen_stride;
   const real *kveta;// per element GLL point or null
   const real *rmass;// lattice plane (both dofs equal away from the perimeter)
   // element geometry (rectilinear): per column / per row

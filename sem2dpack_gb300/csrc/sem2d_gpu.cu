@@ -82,6 +82,9 @@ struct sem2d_handle {
   unsigned char *d_fdir = nullptr;
   // periodic columns I = 0 and LX-1: raw forces left by the step kernel
   int nperio = 0, perio_tb = 0;  // perio_tb: the rows J = 0 and LZ-1 instead
+  // a grid that is not flat: general coefficients a_k per element GLL point
+  int general = 0;
+  void *gen = nullptr;
   void *perio_f = nullptr;
   // perimeter forces with their own time functions: the incident plane
   // wave and the time-dependent Neumann tractions (bf.W null: none),
@@ -131,6 +134,10 @@ struct sem2d_handle {
   bool march = false;
   int march_warps = 4;  // warps per CTA (SEM2D_MARCH_WARPS)
   int march_fst = 0;    // force state (problems with a fault; SEM2D_FORCE_STATE=0 keeps the displacement state)
+  // a time function other than Ricker drives the sources or the boundary:
+  // its net impulse can leave a static displacement, which FP32 does not
+  // resolve against the dynamic one (the force state is used then too)
+  bool static_load = false;
   void *F[2] = {nullptr, nullptr};  // force state planes, ping-pong like D and V
   int tune_source = 0;  // launch shape: 0 analytic, 1 timed at create, 2 from the tuning cache
   int march_cz = 0, march_nunits = 0;
@@ -241,6 +248,80 @@ double ricker(double t, double f0, double t0, double ampli) {
 // ---------------------------------------------------------------------
 // Recover the lattice: element columns/rows from the element corner
 // coordinates, shared or split rows from ibool.
+// Element positions on a structured grid that is not flat, from the
+// connectivity: the right neighbour shares the right edge's corner nodes,
+// the upper one the top edge's, or, across a split (fault) row, has its
+// bottom corners at the same coordinates.
+int topology_positions(sem2d_handle *h, const sem2d_problem_desc *d, std::vector<int> &grid) {
+  const int N = d->ngll, ne = d->nelem, np = d->npoin;
+  auto ib = [&](int i, int j, int e) { return d->ibool[i + N * (j + (size_t)N * e)] - 1; };
+  std::vector<int> by00(np, -1);
+  for (int e = 0; e < ne; ++e) {
+    const int a = ib(0, 0, e);
+    if (by00[a] >= 0) return set_err(h, SEM2D_E_UNSUPPORTED, "two elements share a lower-left corner");
+    by00[a] = e;
+  }
+  auto same_xz = [&](int a, int b) {
+    return d->coord[2 * (size_t)a] == d->coord[2 * (size_t)b] && d->coord[2 * (size_t)a + 1] == d->coord[2 * (size_t)b + 1];
+  };
+  std::vector<std::pair<std::pair<double, double>, int>> c00;
+  for (int e = 0; e < ne; ++e) {
+    const int a = ib(0, 0, e);
+    c00.push_back({{d->coord[2 * (size_t)a], d->coord[2 * (size_t)a + 1]}, e});
+  }
+  std::sort(c00.begin(), c00.end());
+  std::vector<int> right(ne, -1), up(ne, -1), has_left(ne, 0), has_below(ne, 0);
+  for (int e = 0; e < ne; ++e) {
+    const int r = by00[ib(N - 1, 0, e)];
+    if (r >= 0 && ib(0, N - 1, r) == ib(N - 1, N - 1, e)) right[e] = r;
+    int u = by00[ib(0, N - 1, e)];
+    if (u >= 0 && ib(N - 1, 0, u) != ib(N - 1, N - 1, e)) u = -1;
+    if (u < 0) {  // a split row: the element whose bottom corners sit on this top edge
+      const int a = ib(0, N - 1, e);
+      const std::pair<double, double> key{d->coord[2 * (size_t)a], d->coord[2 * (size_t)a + 1]};
+      auto it = std::lower_bound(c00.begin(), c00.end(), std::make_pair(key, -1));
+      for (; it != c00.end() && it->first == key; ++it)
+        if (it->second != e && same_xz(ib(N - 1, 0, it->second), ib(N - 1, N - 1, e))) u = it->second;
+    }
+    up[e] = u;
+  }
+  for (int e = 0; e < ne; ++e) {
+    if (right[e] >= 0) has_left[right[e]]++;
+    if (up[e] >= 0) has_below[up[e]]++;
+  }
+  int origin = -1;
+  for (int e = 0; e < ne; ++e)
+    if (!has_left[e] && !has_below[e]) {
+      if (origin >= 0) return set_err(h, SEM2D_E_UNSUPPORTED, "mesh is not a structured grid of elements");
+      origin = e;
+    }
+  if (origin < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "mesh is not a structured grid of elements");
+  int nx = 0;
+  for (int e = origin; e >= 0; e = right[e]) ++nx;
+  if (nx <= 0 || ne % nx) return set_err(h, SEM2D_E_UNSUPPORTED, "mesh is not a structured grid of elements");
+  const int nz = ne / nx;
+  h->nx = nx;
+  h->nz = nz;
+  h->elem_ex.assign(ne, -1);
+  h->elem_ez.assign(ne, -1);
+  grid.assign((size_t)nx * nz, -1);
+  int start = origin;
+  for (int ez = 0; ez < nz; ++ez) {
+    if (start < 0) return set_err(h, SEM2D_E_UNSUPPORTED, "mesh is not a structured grid of elements");
+    int e = start;
+    for (int ex = 0; ex < nx; ++ex) {
+      if (e < 0 || h->elem_ex[e] >= 0) return set_err(h, SEM2D_E_UNSUPPORTED, "mesh is not a structured grid of elements");
+      h->elem_ex[e] = ex;
+      h->elem_ez[e] = ez;
+      grid[(size_t)ez * nx + ex] = e;
+      e = right[e];
+    }
+    if (e >= 0) return set_err(h, SEM2D_E_UNSUPPORTED, "element rows of unequal length");
+    start = up[start];
+  }
+  return SEM2D_OK;
+}
+
 int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
   const int N = d->ngll, ne = d->nelem;
   auto ib = [&](int i, int j, int e) { return d->ibool[i + N * (j + (size_t)N * e)] - 1; };
@@ -254,6 +335,12 @@ int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
     x1[e] = d->coord[2 * (size_t)b];
     z1[e] = d->coord[2 * (size_t)b + 1];
   }
+  std::vector<int> grid;
+  if (d->xjaci) {
+    if (!d->dvol) return set_err(h, SEM2D_E_ARG, "xjaci without dvol");
+    int st = topology_positions(h, d, grid);
+    if (st) return st;
+  } else {
   std::vector<double> xs(x0), zs(z0);
   std::sort(xs.begin(), xs.end());
   xs.erase(std::unique(xs.begin(), xs.end()), xs.end());
@@ -266,7 +353,7 @@ int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
   h->nz = nz;
   h->elem_ex.resize(ne);
   h->elem_ez.resize(ne);
-  std::vector<int> grid((size_t)nx * nz, -1);
+  grid.assign((size_t)nx * nz, -1);
   for (int e = 0; e < ne; ++e) {
     const int ex = int(std::lower_bound(xs.begin(), xs.end(), x0[e]) - xs.begin());
     const int ez = int(std::lower_bound(zs.begin(), zs.end(), z0[e]) - zs.begin());
@@ -276,6 +363,8 @@ int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
     h->elem_ex[e] = ex;
     h->elem_ez[e] = ez;
   }
+  }
+  const int nx = h->nx, nz = h->nz;
   // rows: shared (no fault) or split (fault) between consecutive element rows
   h->row0.assign(nz + 1, 0);
   for (int ez = 1; ez < nz; ++ez) {
@@ -310,6 +399,16 @@ int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
       }
   for (int p = 0; p < d->npoin; ++p)
     if (h->glob2lat[p] < 0) return set_err(h, SEM2D_E_ARG, "global node not referenced by ibool");
+  if (d->xjaci) {  // the element geometry is in the general coefficients
+    h->general = 1;
+    int st;
+    if ((st = upload_real(h, &h->geo[0], std::vector<double>(nx, 1.0))) ||
+        (st = upload_real(h, &h->geo[1], std::vector<double>(nz, 1.0))) ||
+        (st = upload_real(h, &h->geo[2], std::vector<double>(nx, 1.0))) ||
+        (st = upload_real(h, &h->geo[3], std::vector<double>(nz, 1.0))))
+      return st;
+    return SEM2D_OK;
+  }
   // rectilinear geometry: one width per column, one height per row
   std::vector<double> dxdxi(nx), dzdeta(nz);
   for (int e = 0; e < ne; ++e) {
@@ -331,7 +430,64 @@ int detect_lattice(sem2d_handle *h, const sem2d_problem_desc *d) {
   return SEM2D_OK;
 }
 
+int upload_kveta(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int N = d->ngll, NN = N * N, ne = d->nelem;
+  if (!d->kv_eta) return SEM2D_OK;
+  h->has_kv = 1;
+  std::vector<double> el((size_t)NN * ne);
+  for (int e = 0; e < ne; ++e) {
+    const size_t eo = ((size_t)h->elem_ez[e] * h->nx + h->elem_ex[e]) * NN;
+    for (int q = 0; q < NN; ++q) el[eo + q] = d->kv_eta[q + (size_t)NN * e];
+  }
+  return upload_real(h, &h->kveta, el);
+}
+
+// MAT_ELAST_init_a on a grid that is not flat (mat_elastic.f90:290-360):
+// a_k = -dvol (moduli x products of the inverse Jacobian), nelast 10 in
+// P-SV and 3 in SH, in the lattice element order [k][element][i + N j]
+int upload_general(sem2d_handle *h, const sem2d_problem_desc *d) {
+  const int N = d->ngll, NN = N * N, ne = d->nelem, na = d->ndof == 1 ? 3 : 10;
+  const size_t npt = (size_t)NN * ne;
+  if (d->width > 0) return set_err(h, SEM2D_E_UNSUPPORTED, "the 2.5D term on a grid that is not flat");
+  if (d->adjoint) return set_err(h, SEM2D_E_UNSUPPORTED, "the gradient workflow on a grid that is not flat");
+  std::vector<double> A((size_t)na * npt);
+  for (int e = 0; e < ne; ++e) {
+    const size_t eo = ((size_t)h->elem_ez[e] * h->nx + h->elem_ex[e]) * NN;
+    for (int q = 0; q < NN; ++q) {
+      const size_t p = q + (size_t)NN * e;
+      const double *X = d->xjaci + 4 * p;
+      const double DxiDx = X[0], DetaDx = X[1], DxiDz = X[2], DetaDz = X[3], w = d->dvol[p];
+      const double Kx = d->Kx[p], Kz = d->Kz[p], la = d->la[p], mu = d->mu[p], mux = d->mux[p], muz = mu;
+      double a[10];
+      if (na == 3) {
+        a[0] = (mux * DxiDx) * DxiDx + (muz * DxiDz) * DxiDz;
+        a[1] = (mux * DetaDx) * DetaDx + (muz * DetaDz) * DetaDz;
+        a[2] = (mux * DxiDx) * DetaDx + (muz * DxiDz) * DetaDz;
+      } else {
+        a[0] = (Kx * DxiDx) * DxiDx + (mu * DxiDz) * DxiDz;
+        a[1] = (la * DxiDx) * DetaDz + (mu * DxiDz) * DetaDx;
+        a[2] = (Kz * DetaDz) * DetaDz + (mu * DetaDx) * DetaDx;
+        a[3] = (Kx * DetaDx) * DetaDx + (mu * DetaDz) * DetaDz;
+        a[4] = (la * DxiDz) * DetaDx + (mu * DxiDx) * DetaDz;
+        a[5] = (Kz * DxiDz) * DxiDz + (mu * DxiDx) * DxiDx;
+        a[6] = (Kx * DxiDx) * DetaDx + (mu * DxiDz) * DetaDz;
+        a[7] = ((la + mu) * DxiDx) * DxiDz;
+        a[8] = ((la + mu) * DetaDx) * DetaDz;
+        a[9] = (Kz * DxiDz) * DetaDz + (mu * DxiDx) * DetaDx;
+      }
+      for (int k = 0; k < na; ++k) A[(size_t)k * npt + eo + q] = -(w * a[k]);
+    }
+  }
+  h->mat_elem = kMatGeneral;
+  h->nmat = 0;
+  h->mat_iso = 1;
+  int st = upload_real(h, &h->gen, A);
+  if (st) return st;
+  return upload_kveta(h, d);
+}
+
 int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
+  if (h->general) return upload_general(h, d);
   const int N = d->ngll, NN = N * N, ne = d->nelem;
   const size_t npt = (size_t)NN * ne;
   // isotropic?  Kx = Kz = la + 2 mu and mux = mu everywhere
@@ -419,16 +575,7 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
     }
     if (st) return st;
   }
-  if (d->kv_eta) {
-    h->has_kv = 1;
-    std::vector<double> el(npt);
-    for (int e = 0; e < ne; ++e) {
-      const size_t eo = ((size_t)h->elem_ez[e] * h->nx + h->elem_ex[e]) * NN;
-      for (int q = 0; q < NN; ++q) el[eo + q] = d->kv_eta[q + (size_t)NN * e];
-    }
-    if ((st = upload_real(h, &h->kveta, el))) return st;
-  }
-  return SEM2D_OK;
+  return upload_kveta(h, d);
 }
 
 // Stacey P3 terms (one per boundary element edge point) grouped by the
@@ -462,8 +609,11 @@ int upload_stacey(sem2d_handle *h, const sem2d_problem_desc *d) {
       const int sa = perimeter_slot(int(La % h->pitch), int(La / h->pitch), h->LX, h->LZ);
       const int sb = perimeter_slot(int(Lb % h->pitch), int(Lb / h->pitch), h->LX, h->LZ);
       if (sa < 0 || sb < 0 || own[sa].empty() || own[sb].empty()) continue;
-      by_slot[sa].insert(by_slot[sa].end(), own[sb].begin(), own[sb].end());
-      by_slot[sb].insert(by_slot[sb].end(), own[sa].begin(), own[sa].end());
+      // the same list, in the same order, for both ends: equal sums
+      std::vector<int> both = own[sa];
+      both.insert(both.end(), own[sb].begin(), own[sb].end());
+      by_slot[sa] = both;
+      by_slot[sb] = both;
     }
   }
   std::vector<int> slot, ptr(1, 0), kk, lat;
@@ -618,6 +768,7 @@ int upload_boundary_forces(sem2d_handle *h, const sem2d_problem_desc *d) {
     StfDev q;
     int st = upload_stf(h, *d->wave_stf, &q);
     if (st) return st;
+    h->static_load = h->static_load || d->wave_stf->kind != SEM2D_STF_RICKER;
     const signed char qi = (signed char)stfs.size();
     stfs.push_back(q);
     const double kPi = 3.141592653589793, a = kPi * d->wave_angle / 180.0;
@@ -671,6 +822,7 @@ int upload_boundary_forces(sem2d_handle *h, const sem2d_problem_desc *d) {
       StfDev q;
       int st = upload_stf(h, d->neu_stfs[k], &q);
       if (st) return st;
+      h->static_load = h->static_load || d->neu_stfs[k].kind != SEM2D_STF_RICKER;
       stfs.push_back(q);
     }
     for (int k = 0; k < d->nneu; ++k) {
@@ -1004,6 +1156,8 @@ BulkConfig make_config(sem2d_handle *h, int cur, FaultParams<real> &f) {
   bc.Acur = h->A[cur];
   bc.Anext = h->keep_accel ? h->A[1 - cur] : nullptr;
   for (int m = 0; m < 4; ++m) bc.mat[m] = h->mat[m];
+  bc.gen = h->gen;
+  bc.gen_stride = (long long)h->N * h->N * h->nx * h->nz;
   bc.kveta = h->kveta;
   bc.rmass = h->rmass;
   for (int g = 0; g < 4; ++g) bc.geo[g] = h->geo[g];
@@ -1652,7 +1806,8 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   h->march = false;
   const char *env = std::getenv("SEM2D_MARCH");
   if (env && std::atoi(env) == 0) return SEM2D_OK;
-  if (h->st_nslot || h->ndir || h->nperio) return SEM2D_OK;  // Stacey, Dirichlet or periodic sides: the strip kernel
+  // Stacey, Dirichlet or periodic sides, a grid that is not flat: the strip kernel
+  if (h->st_nslot || h->ndir || h->nperio || h->general) return SEM2D_OK;
   BulkConfig bc;
   bc.N = h->N;
   bc.ndof = h->ndof;
@@ -1667,7 +1822,7 @@ int setup_march(sem2d_handle *h, const std::vector<int> &rec_ex, const std::vect
   // with a fault the elastic force is the state: the displacement next to
   // a slipped fault is too large for FP32 to resolve the dynamic stress
   const char *fs = std::getenv("SEM2D_FORCE_STATE");
-  h->march_fst = h->nflt > 0 && !(fs && std::atoi(fs) == 0);
+  h->march_fst = (h->nflt > 0 || h->static_load) && !(fs && std::atoi(fs) == 0);
   bc.march_warps = h->march_warps;
   bc.march_fst = h->march_fst;
   // resident warps per SM
@@ -1926,6 +2081,7 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     std::vector<double> hv2;
     if (d->src_stf) {
       if (const char *m = stf_check(*d->src_stf)) return set_err(h, SEM2D_E_ARG, m);
+      h->static_load = h->static_load || d->src_stf->kind != SEM2D_STF_RICKER;
       const sem2d_stf &q = *d->src_stf;
       hs = StfDev{q.kind, q.ntab, q.f0, q.onset, q.ampli, q.par1, q.par2, q.tab_t, q.tab_v, nullptr};
       if (q.kind == SEM2D_STF_TAB) {
@@ -2181,6 +2337,7 @@ int batch_close_impl(sem2d_handle *h) {
     if (m->ndir) return set_err(h, SEM2D_E_UNSUPPORTED, "Dirichlet sides in a batch");
     if (m->nperio) return set_err(h, SEM2D_E_UNSUPPORTED, "periodic sides in a batch");
     if (m->bf.W) return set_err(h, SEM2D_E_UNSUPPORTED, "incident waves or Neumann tractions in a batch");
+    if (m->general) return set_err(h, SEM2D_E_UNSUPPORTED, "a grid that is not flat in a batch");
   }
   h->N = a->N;
   h->ndof = a->ndof;
@@ -2924,6 +3081,7 @@ int sem2d_gpu_get_strain_stress(sem2d_handle *h, double *strain, double *stress)
   if (!h) return SEM2D_E_ARG;
   if (!h->subs.empty()) return set_err(h, SEM2D_E_STATE, "outputs are read from the batch members");
   if (h->elem_ex.empty()) return set_err(h, SEM2D_E_STATE, "element numbering not kept (batch member)");
+  if (h->general) return set_err(h, SEM2D_E_UNSUPPORTED, "strain and stress on a grid that is not flat");
   int st = check_device_error(h);
   if (st) return st;
   const int N = h->N, NN = N * N, nc = h->ndof + 1;

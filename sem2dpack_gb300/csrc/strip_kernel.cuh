@@ -357,7 +357,72 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
             xline(sD + cc * PS, v);
           }
         };
-        if constexpr (NDOF == 1) {
+        if constexpr (NDOF == 1 && MAT == kMatGeneral) {
+          // a grid that is not flat (ELAST_KD1_SH / KD2_SH with nelast = 3,
+          // mat_elastic.f90:662-677): the line of point (q,t) is this
+          // thread's; dU/deta of (q,t) comes from thread q through the
+          // scratch area, as does the eta-part of (t,q)
+          real col[N], gxi[N], tA[N], rB[N];
+          xline_u(0, col);
+          if (act) {
+            real rowv[N];
+#pragma unroll
+            for (int q = 0; q < N; ++q) rowv[q] = uval(0, t, q);
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              real a = H[0 + N * i] * col[0];
+#pragma unroll
+              for (int q = 1; q < N; ++q) a = a + H[q + N * i] * col[q];
+              gxi[i] = a;
+            }
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+              real a = rowv[0] * H[0 + N * j];
+#pragma unroll
+              for (int q = 1; q < N; ++q) a = a + rowv[q] * H[q + N * j];
+              sc[t + N * j] = a;  // dU/deta at (t,j)
+            }
+          }
+          __syncwarp();
+          if (act) {
+            const real *g = p.gen + eoff;
+            const long long gs = p.gen_stride;
+#pragma unroll
+            for (int q = 0; q < N; ++q) {
+              const int k = q + N * t;
+              const real ge = sc[k];
+              const real a1 = g[k], a2 = g[gs + k], a3 = g[2 * gs + k];
+              tA[q] = a1 * gxi[q] + a3 * ge;
+              sc[k] = a3 * gxi[q] + a2 * ge;  // eta part at (q,t)
+            }
+          }
+          __syncwarp();
+          if (act) {
+#pragma unroll
+            for (int q = 0; q < N; ++q) rB[q] = sc[t + N * q];
+          }
+          __syncwarp();
+          if (act) {
+#pragma unroll
+            for (int i = 0; i < N; ++i) {
+              real a = H[i + N * 0] * tA[0];
+#pragma unroll
+              for (int q = 1; q < N; ++q) a = a + H[i + N * q] * tA[q];
+              sc[i + N * t] = a;  // xi part at (i,t)
+            }
+          }
+          __syncwarp();
+          if (act) {
+#pragma unroll
+            for (int j = 0; j < N; ++j) {
+              real a = rB[0] * H[j + N * 0];
+#pragma unroll
+              for (int q = 1; q < N; ++q) a = a + rB[q] * H[j + N * q];
+              sc[t + N * j] = sc[t + N * j] + a;  // nodal force of the element at (t,j)
+            }
+          }
+          __syncwarp();
+        } else if constexpr (NDOF == 1) {
           real col[N], row[N];
           xline_u(0, col);
           real mx[N];  // mu_x along the xi-line: mu (isotropic) or mux
@@ -457,7 +522,36 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           }
           __syncwarp();
           real cx[N], cz[N], rx[N], rz[N];
-          {
+          if constexpr (MAT == kMatGeneral) {
+            // a grid that is not flat (ELAST_KD1_PSV / KD2_PSV with nelast =
+            // 10, mat_elastic.f90:499-516, 620-636): the four products of the
+            // gradient at (q,t) with a1..a10, the eta parts handed over in
+            // the dU/deta areas
+            if (act) {
+              const real *g = p.gen + eoff;
+              const long long gs = p.gen_stride;
+#pragma unroll
+              for (int q = 0; q < N; ++q) {
+                const int k = q + N * t;
+                const real t1 = SXX[k], t2 = SXZ[k], t3 = SEX[k], t4 = SEZ[k];
+                const real a1 = g[k], a2 = g[gs + k], a3 = g[2 * gs + k], a4 = g[3 * gs + k],
+                           a5 = g[4 * gs + k], a6 = g[5 * gs + k], a7 = g[6 * gs + k], a8 = g[7 * gs + k],
+                           a9 = g[8 * gs + k], a10 = g[9 * gs + k];
+                cx[q] = a1 * t1 + a7 * t3 + a8 * t2 + a2 * t4;
+                cz[q] = a8 * t1 + a5 * t3 + a6 * t2 + a10 * t4;
+                SEX[k] = a7 * t1 + a4 * t3 + a5 * t2 + a9 * t4;
+                SEZ[k] = a2 * t1 + a9 * t3 + a10 * t2 + a3 * t4;
+              }
+            }
+            __syncwarp();
+            if (act) {
+#pragma unroll
+              for (int q = 0; q < N; ++q) {
+                rx[q] = SEX[t + N * q];
+                rz[q] = SEZ[t + N * q];
+              }
+            }
+          } else {
             // moduli along the xi-line at height t: (la, mu) or (Kx, la, mu)
             real m0[N], m1[N], m2[N];
             if (MAT == kMatNode && iso) {
@@ -491,32 +585,32 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
                 cz[q] = wq * (mu * (dzux + dxuz));
               }
             }
-          }
-          if (act) {
-            const real wrz = -(wdt * etaz);
-            const real sxz = p.kd2 ? etaz : xix;
+            if (act) {
+              const real wrz = -(wdt * etaz);
+              const real sxz = p.kd2 ? etaz : xix;
 #pragma unroll
-            for (int q = 0; q < N; ++q) {
-              // row part at point (t,q): -W etaz (sigma_xz, sigma_zz); the
-              // NGLL=5 kernel of the reference uses etaz for both shear
-              // terms (mat_elastic.f90:612)
-              real la, mu, Kz;
-              if (iso) {
-                la = matv(0, t, q);
-                mu = matv(1, t, q);
-                Kz = la + real(2) * mu;
-              } else {
-                Kz = matv(1, t, q);
-                la = matv(2, t, q);
-                mu = matv(3, t, q);
+              for (int q = 0; q < N; ++q) {
+                // row part at point (t,q): -W etaz (sigma_xz, sigma_zz); the
+                // NGLL=5 kernel of the reference uses etaz for both shear
+                // terms (mat_elastic.f90:612)
+                real la, mu, Kz;
+                if (iso) {
+                  la = matv(0, t, q);
+                  mu = matv(1, t, q);
+                  Kz = la + real(2) * mu;
+                } else {
+                  Kz = matv(1, t, q);
+                  la = matv(2, t, q);
+                  mu = matv(3, t, q);
+                }
+                const int k = t + N * q;
+                const real dzux = etaz * SEX[k], dzuz = etaz * SEZ[k];
+                const real wq = wrz * w[q];
+                rx[q] = wq * (mu * (dzux + sxz * SXZ[k]));
+                rz[q] = wq * (la * (xix * SXX[k]) + Kz * dzuz);
               }
-              const int k = t + N * q;
-              const real dzux = etaz * SEX[k], dzuz = etaz * SEZ[k];
-              const real wq = wrz * w[q];
-              rx[q] = wq * (mu * (dzux + sxz * SXZ[k]));
-              rz[q] = wq * (la * (xix * SXX[k]) + Kz * dzuz);
             }
-          }
+          }  // flat grid
           __syncwarp();
           if (act) {
 #pragma unroll
@@ -542,7 +636,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
                 b2 = b2 + rz[q] * H[j + N * q];
               }
               real flx = SXX[t + N * j] + a, flz = SXZ[t + N * j] + b2;
-              if (width > real(0)) {  // 2.5D term at point (t,j), isotropic
+              if (MAT != kMatGeneral && width > real(0)) {  // 2.5D term at point (t,j), isotropic
                 const real la = matv(0, t, j), mu = matv(1, t, j);
                 const real nu = (la / (la + mu)) / real(2);
                 const real pw = (real(3.141592653589793) * (real(1) - nu)) / width;

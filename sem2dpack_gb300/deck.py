@@ -156,6 +156,18 @@ class Sources:
 
 
 @dataclass
+class Layer:
+    """One layer of &MESH_DEF method='LAYERED' (&MESH_LAYER nz, ztop or
+    ztopH, tag; mesh_layers.f90:212-300): its element rows, material tag
+    and top boundary, a height or a distribution of x (a Dist evaluated at
+    z = 0).  `quadratic`: Q9 elements (a top other than flat or LINEAR)."""
+    nz: int = 1
+    tag: int = 1
+    ztop: Union[float, object] = 0.0
+    quadratic: bool = False
+
+
+@dataclass
 class Receivers:
     """&REC_LINE (receivers.f90:62-163)."""
     number: int = 0
@@ -203,6 +215,19 @@ class ParDeck:
     width: float = 0.0   # W of &GENERAL; 0 = 2D (the reference's huge)
     # per element GLL point arrays (ngll,ngll,nelem) for hetero materials
     hetero: Dict[str, np.ndarray] = field(default_factory=dict)
+    # &MESH_DEF method 'CARTESIAN' or 'LAYERED' (&MESH_LAYERED xlim, zmin,
+    # nx = nelem[0], ezflt, fztag, fznz; `layers` from the bottom up)
+    mesh: str = "CARTESIAN"
+    zmin: float = 0.0
+    layers: List[Layer] = field(default_factory=list)
+
+    def layer_abscissae(self):
+        """x of the control-node columns of a layered mesh (mesh_layers.f90:
+        357-361): nxp = nx+1 with Q4 elements, 2 nx+1 with Q9."""
+        d = 2 if any(layer.quadratic for layer in self.layers) else 1
+        nxp = d * int(self.nelem[0]) + 1
+        x0, x1 = float(self.xlim[0]), float(self.xlim[1])
+        return np.array([x0 + (x1 - x0) / float(nxp - 1) * float(i) for i in range(nxp)])
 
     def to_c(self):
         """Return (abi.Deck, keepalive) for the C builders."""
@@ -351,4 +376,21 @@ class ParDeck:
             d.rec_field = r.field.encode()[:1]
         d.precision, d.kd2_form = self.precision, self.kd2_form
         d.width = float(self.width)
+        if self.mesh.upper() == "LAYERED":
+            if not self.layers or len(self.layers) > abi.MAX_LAYERS:
+                raise ValueError("MESH_LAYERS_read: nlayer or file must be set")
+            d.mesh_method, d.zmin, d.nlayer = 1, float(self.zmin), len(self.layers)
+            x = self.layer_abscissae()
+            for k, layer in enumerate(self.layers):
+                d.layer_nz[k], d.layer_tag[k] = int(layer.nz), int(layer.tag)
+                d.layer_ngnod[k] = 9 if layer.quadratic else 4
+                if callable(layer.ztop):
+                    top = np.asarray(layer.ztop(x, np.zeros_like(x)), dtype=np.float64)
+                else:
+                    top = np.full(x.shape, float(layer.ztop))
+                top = np.ascontiguousarray(top)
+                keep.append(top)
+                d.layer_top[k] = _dptr(top)
+        elif self.mesh.upper() != "CARTESIAN":
+            raise ValueError("only the CARTESIAN and LAYERED meshers are on the GPU path")
         return d, keep

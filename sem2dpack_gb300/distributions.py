@@ -13,8 +13,12 @@ the element GLL points for material properties (MAT_setProp).
             of width `length` (distribution_linear.f90:60-188)
   GRADIENT  valref + grad (yref - y) in a frame rotated by `angle`, yref
             interpolated from a reference line (distribution_gradient.f90)
+  SPLINE    cubic spline with zero end slopes through a table sorted by x,
+            along x (dim=1) or z (dim=2) (distribution_spline.f90:34-109,
+            spline and splint utils.f90:652-734); a point outside the table
+            is refused (the reference reads outside its arrays there)
 
-SPLINE and HETE1 are refused.  Tables given by `file=` are read relative to
+HETE1 is refused.  Tables given by `file=` are read relative to
 the folder of the Par.inp.
 """
 import os
@@ -23,7 +27,46 @@ import numpy as np
 
 __all__ = ["Dist", "KINDS"]
 
-KINDS = ("PWCONR", "GAUSSIAN", "ORDER0", "LINEAR", "GRADIENT")
+KINDS = ("PWCONR", "GAUSSIAN", "ORDER0", "LINEAR", "GRADIENT", "SPLINE")
+
+
+def _spline_d2(x, y):
+    """spline (utils.f90:652-691) with yp1 = ypn = 0: the second
+    derivatives, in the reference's order of operations."""
+    n = len(x)
+    y2, u = [0.0] * n, [0.0] * n
+    y2[0] = -0.5
+    u[0] = (3.0 / (x[1] - x[0])) * ((y[1] - y[0]) / (x[1] - x[0]) - 0.0)
+    for i in range(1, n - 1):
+        sig = (x[i] - x[i - 1]) / (x[i + 1] - x[i - 1])
+        p = sig * y2[i - 1] + 2.0
+        y2[i] = (sig - 1.0) / p
+        u[i] = (6.0 * ((y[i + 1] - y[i]) / (x[i + 1] - x[i]) - (y[i] - y[i - 1]) / (x[i] - x[i - 1]))
+                / (x[i + 1] - x[i - 1]) - sig * u[i - 1]) / p
+    qn, un = 0.5, (3.0 / (x[n - 1] - x[n - 2])) * (0.0 - (y[n - 1] - y[n - 2]) / (x[n - 1] - x[n - 2]))
+    y2[n - 1] = (un - qn * u[n - 2]) / (qn * y2[n - 2] + 1.0)
+    for k in range(n - 2, -1, -1):
+        y2[k] = y2[k] * y2[k + 1] + u[k]
+    return y2
+
+
+def _splint(xa, ya, y2, x):
+    """splint (utils.f90:697-734) at each x: the bracket [klo, klo+1] with
+    xa[klo] < x <= xa[klo+1] (hunt's bisection, utils.f90:596-646)."""
+    out = []
+    n = len(xa)
+    for v in x:
+        lo, hi = 0, n - 1
+        while hi - lo > 1:
+            m = (lo + hi) // 2
+            if v > xa[m]:
+                lo = m
+            else:
+                hi = m
+        h = xa[hi] - xa[lo]
+        a, b = (xa[hi] - v) / h, (v - xa[lo]) / h
+        out.append(a * ya[lo] + b * ya[hi] + ((a ** 3 - a) * y2[lo] + (b ** 3 - b) * y2[hi]) * (h * h) / 6.0)
+    return np.array(out)
 
 
 def _interpol(xi, yi, xo):
@@ -112,6 +155,14 @@ class Dist:
                 if len(d) < 2 * n:
                     raise ValueError("DIST_LINEAR: %d (x, value) pairs expected" % n)
                 self.x, self.y = np.array(d[0:2 * n:2]), np.array(d[1:2 * n:2])
+        elif self.kind == "SPLINE":
+            self.dim = int(it.get("dim", 1))
+            if self.dim not in (1, 2):
+                raise ValueError("read_spline_dist: dim must be 1 or 2")
+            xs, ys = _table(os.path.join(self.base, str(it["file"]).strip()))
+            order = np.argsort(xs, kind="stable")  # dsort (utils.f90)
+            self.x, self.y = [float(v) for v in xs[order]], [float(v) for v in ys[order]]
+            self.y2 = _spline_d2(self.x, self.y)
         else:  # GRADIENT
             self.grad = abs(float(it["grad"]))
             self.angle = float(it.get("angle", 0.0)) * 3.141592653589793 / 180.0
@@ -141,6 +192,11 @@ class Dist:
             if self.length > 0:
                 return _smooth_interpol(self.x, self.y, c, self.length)
             return _interpol(self.x, self.y, c)
+        if self.kind == "SPLINE":
+            c = np.atleast_1d(x if self.dim == 1 else z)
+            if c.min() < self.x[0] or c.max() > self.x[-1]:
+                raise ValueError("DIST_SPLINE: a point lies outside the table")
+            return _splint(self.x, self.y, self.y2, c)
         ca, sa = np.cos(self.angle), np.sin(self.angle)
         xr, yr = ca * x + sa * z, -sa * x + ca * z
         if xr.min() < self.x[0] or xr.max() > self.x[-1]:

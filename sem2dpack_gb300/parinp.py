@@ -219,8 +219,59 @@ def deck_from_parinp(text, precision=None, base=None):
             if float(it.get("w", 0.0) or 0.0) > 0.0:
                 deck.width = float(it["w"])
         elif name == "MESH_DEF":
-            if str(it.get("method", "CARTESIAN")).upper() != "CARTESIAN":
-                raise ValueError("only &MESH_DEF method='CARTESIAN' is on the GPU path")
+            method = str(it.get("method", "CARTESIAN")).upper()
+            if method not in ("CARTESIAN", "LAYERED"):
+                raise ValueError("only &MESH_DEF method='CARTESIAN' or 'LAYERED' is on the GPU path")
+            deck.mesh = method
+        elif name == "MESH_LAYERED" and deck.mesh == "LAYERED":
+            # MESH_LAYERS_read (mesh_layers.f90:30-88): &MESH_LAYERED, then
+            # nlayer &MESH_LAYER blocks (each followed by its &DIST_* block
+            # when ztopH is set) or a file of "ztop nz tag" lines, listed from
+            # the top down; default tags 1 (top) to nlayer (bottom)
+            xl = it.get("xlim")
+            if xl is None or "zmin" not in it:
+                raise ValueError("MESH_LAYERS_read: you must set xlim and zmin")
+            deck.xlim = _pair(xl)
+            deck.zmin = float(it["zmin"])
+            nx = int(it.get("nx", 1))
+            deck.ezflt = int(it.get("ezflt", 0))
+            deck.fztag = int(it.get("fztag", 0)) if deck.ezflt != 0 else 0
+            deck.fznz = int(it.get("fznz", 1))
+            f = str(it.get("file", "")).strip()
+            from .deck import Layer
+            top_down = []
+            if f:
+                for row in np.loadtxt(os.path.join(base or ".", f), ndmin=2):
+                    top_down.append(Layer(nz=int(row[1]), tag=int(row[2]), ztop=float(row[0])))
+            else:
+                nl = int(it.get("nlayer", 0))
+                if nl <= 0:
+                    raise ValueError("MESH_LAYERS_read: nlayer or file must be set")
+                q = k + 1
+                for li in range(nl):
+                    while q < len(blocks) and blocks[q][0] != "MESH_LAYER":
+                        q += 1
+                    if q >= len(blocks):
+                        raise ValueError("MESH_LAYERS_read: %d &MESH_LAYER blocks expected" % nl)
+                    consumed.add(q)
+                    b = blocks[q][1]
+                    layer = Layer(nz=int(b.get("nz", 0)), tag=int(b.get("tag", li + 1)))
+                    zh = str(b.get("ztoph", "")).strip().upper()
+                    if zh in ("QSPLINE", "CSPLINE"):
+                        raise ValueError("&MESH_LAYER ztopH='%s' is not supported by the front end" % zh)
+                    if zh:
+                        dist = take_dists(q, {"ztoph": zh}, [("ztop", "ztop")])["ztop"]
+                        layer.ztop, layer.quadratic = dist, zh != "LINEAR"
+                    elif "ztop" in b:
+                        layer.ztop = float(b["ztop"])
+                    else:
+                        raise ValueError("MESH_LAYERS_read: ztop or ztopH must be set")
+                    top_down.append(layer)
+                    q += 1
+            if any(layer.nz <= 0 for layer in top_down):
+                raise ValueError("MESH_LAYERS_read: nz null, negative or missing")
+            deck.layers = top_down[::-1]
+            deck.nelem = (nx, sum(layer.nz for layer in top_down))
         elif name == "MESH_CART":
             deck.xlim = _pair(it["xlim"])
             deck.zlim = _pair(it["zlim"])

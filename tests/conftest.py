@@ -32,3 +32,15 @@ def watch_launches(nsteps, members=1, every=100):
     step 0 (one kernel per problem every `every` steps, the default
     info_every)."""
     return members * (nsteps // every)
+
+
+def example_deck(golden, name, folder):
+    """ParDeck of the example deck `name` of the fixtures, its tables
+    (file=...) written to `folder` first."""
+    from sem2dpack_gb300.parinp import deck_from_parinp
+    prefix = "exfile_%s__" % name
+    for k in golden.files:
+        if k.startswith(prefix):
+            with open(os.path.join(str(folder), k[len(prefix):]), "w") as f:
+                f.write(str(golden[k]))
+    return deck_from_parinp(str(golden["parinp_" + name]), base=str(folder))

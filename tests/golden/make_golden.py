@@ -80,8 +80,15 @@ def main(ref):
 
     for name in ("LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState",
                  "TestFlt1D", "Bimaterial_fault", "2.5D_V-shape_rate-and-state", "2.5D_inplane",
-                 "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening", "TestAbso"):
-        out["parinp_" + name] = np.array(open(os.path.join(ex, name, "Par.inp")).read())
+                 "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening", "TestAbso",
+                 "TestLayers", "TestLayers_2"):
+        text = open(os.path.join(ex, name, "Par.inp")).read()
+        out["parinp_" + name] = np.array(text)
+        # the tables the deck names (file='...'), as text
+        for fname in sorted(set(re.findall(r"""file\s*=\s*['"]([^'"]+)['"]""", text))):
+            path = os.path.join(ex, name, fname)
+            if os.path.exists(path):
+                out["exfile_%s__%s" % (name, fname)] = np.array(open(path).read())
 
     # the other example decks, which the front end refuses (off the GPU path)
     import glob

@@ -1,5 +1,5 @@
 """Every example deck of the reference that the Cartesian front end takes
-(14),
+(16),
 run as written through the GPU path for its first 30 steps against the FP64
 oracle (FP64 <= 1e-9 for the rate-and-state decks' Newton solves, 1e-10
 otherwise; mixed <= 1e-4): seismograms, and slip and slip rate on faults.
@@ -9,13 +9,14 @@ import pytest
 
 from oracle import pyoracle as po
 from sem2dpack_gb300 import PRECISION_FP64, PRECISION_MIXED, Problem, Solver
-from sem2dpack_gb300.parinp import deck_from_parinp
+from conftest import example_deck
 
 pytestmark = pytest.mark.gpu
 
 EXAMPLES = ["LambsProblem", "TestSH", "Anisotropic", "InaBox", "TestFlt2D_SCEC_TPV3_inplane", "RateState",
             "TestFlt1D", "Bimaterial_fault", "2.5D_V-shape_rate-and-state", "2.5D_inplane",
-            "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening", "TestAbso"]
+            "2D_roughness_drag_approximation", "Kelvin_Visco_FZ", "Velocity_weakening", "TestAbso", "TestLayers",
+            "TestLayers_2"]
 
 
 def rel_l2(a, b):
@@ -25,8 +26,8 @@ def rel_l2(a, b):
 
 @pytest.mark.parametrize("precision", [PRECISION_FP64, PRECISION_MIXED])
 @pytest.mark.parametrize("name", EXAMPLES)
-def test_example_deck(golden, name, precision):
-    dk = deck_from_parinp(str(golden["parinp_" + name]))
+def test_example_deck(golden, name, precision, tmp_path):
+    dk = example_deck(golden, name, tmp_path)
     P = Problem(dk)
     d = P.desc()
     d.precision = precision

@@ -63,7 +63,8 @@ def assert_same_desc(a, b):
         assert _stf_fields(sa) == _stf_fields(sb), k
     sizes = _sizes(a)
     sizes.update({"abs_B": a.nabs, "abs_n": 2 * a.nabs, "abs_wave": a.nabs, "neu_node": a.nneu,
-                  "neu_comp": a.nneu, "neu_B": a.nneu, "neu_stf": a.nneu})
+                  "neu_comp": a.nneu, "neu_B": a.nneu, "neu_stf": a.nneu,
+                  "xjaci": 4 * a.ngll * a.ngll * a.nelem, "dvol": a.ngll * a.ngll * a.nelem})
     for name, n in sizes.items():
         x, y = _arr(a, name, n), _arr(b, name, n)
         assert (x is None) == (y is None), name
