@@ -128,6 +128,7 @@ struct sem2d_handle {
   sem2d_handle *owner = nullptr;    // the batch a member belongs to
   bool owns_stream = true;
   void *d_params[2] = {nullptr, nullptr};
+  void *d_watch[2] = {nullptr, nullptr};  // batch: (V, D, n) of every member by buffer parity
   void *d_units = nullptr;
   // the one-element-per-thread kernel (FP32, NGLL = 5 fast path): work
   // units (strip, chunk) and the receivers each unit samples
@@ -1299,10 +1300,73 @@ __global__ void watch_kernel(const real *V, const real *D, long long n, double *
   }
 }
 
+// the fields of one batch member for the check
+struct WatchSeg {
+  const void *V, *D;
+  long long n;
+};
+
+// the check over every member of a batch in one launch: blockIdx.y is the
+// member, the blocks along x stride over its planes
+template <typename real>
+__global__ void watch_batch_kernel(const WatchSeg *segs, double *info, int *error) {
+  const WatchSeg sg = segs[blockIdx.y];
+  const real *V = static_cast<const real *>(sg.V), *D = static_cast<const real *>(sg.D);
+  double vm = 0.0, dm = 0.0;
+  bool bad = false;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < sg.n; q += (long long)gridDim.x * blockDim.x) {
+    const double v = fabs(double(V[q])), d = fabs(double(D[q]));
+    bad = bad || !isfinite(v) || !isfinite(d);
+    vm = v > vm ? v : vm;
+    dm = d > dm ? d : dm;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    vm = fmax(vm, __shfl_xor_sync(0xffffffffu, vm, o));
+    dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+  }
+  bad = __any_sync(0xffffffffu, bad);
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(reinterpret_cast<unsigned long long *>(info), __double_as_longlong(vm));
+    atomicMax(reinterpret_cast<unsigned long long *>(info + 1), __double_as_longlong(dm));
+    if (bad) atomicCAS(error, 0, SEM2D_E_NAN);
+  }
+}
+
 // the check after the step just queued, over the problem or every member
 // of a batch (their maxima combined)
 int launch_watch(sem2d_handle *h) {
   CK(cudaMemsetAsync(h->d_info, 0, 2 * sizeof(double), h->stream));
+  if (!h->subs.empty() && h->steps > 0 && h->subs.size() <= 65535) {
+    const int nsim = int(h->subs.size());
+    int per = 0;  // blocks per member: about four waves over the batch
+    long long nmax = 0;
+    for (sem2d_handle *m : h->subs) nmax = std::max(nmax, (long long)m->plane * m->ndof);
+    per = int(std::min<long long>((nmax + 255) / 256, std::max(1, 4 * 152 * 4 / nsim)));
+    if (!h->d_watch[0]) {
+      for (int par = 0; par < 2; ++par) {  // h->cur == par after the step
+        std::vector<WatchSeg> segs(nsim);
+        for (int i = 0; i < nsim; ++i) {
+          sem2d_handle *m = h->subs[i];
+          segs[i] = WatchSeg{m->V[par], m->D[1 - par], (long long)m->plane * m->ndof};
+        }
+        WatchSeg *d = nullptr;
+        int st = dupload(h, &d, segs);
+        if (st) return st;
+        h->d_watch[par] = d;
+      }
+    }
+    const dim3 grid(per, nsim);
+    if (h->mixed)
+      watch_batch_kernel<float><<<grid, 256, 0, h->stream>>>(static_cast<const WatchSeg *>(h->d_watch[h->cur]),
+                                                             h->d_info, h->d_error);
+    else
+      watch_batch_kernel<double><<<grid, 256, 0, h->stream>>>(static_cast<const WatchSeg *>(h->d_watch[h->cur]),
+                                                              h->d_info, h->d_error);
+    CK(cudaGetLastError());
+    h->launches++;
+    h->info_step = h->steps;
+    return SEM2D_OK;
+  }
   std::vector<sem2d_handle *> probs = h->subs;
   if (probs.empty()) probs.push_back(h);
   for (sem2d_handle *m : probs) {

@@ -29,9 +29,9 @@ def golden():
 
 def watch_launches(nsteps, members=1, every=100):
     """Launches of the max|v|, max|d| check in a run of nsteps steps from
-    step 0 (one kernel per problem every `every` steps, the default
-    info_every)."""
-    return members * (nsteps // every)
+    step 0 (one kernel every `every` steps, the default info_every; a batch
+    checks all its members in that one launch)."""
+    return nsteps // every
 
 
 def example_deck(golden, name, folder):
