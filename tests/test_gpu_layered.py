@@ -27,6 +27,7 @@ def run_both(dk, precision, nsteps):
     P = Problem(dk)
     d = P.desc()
     d.precision = precision
+    nsteps = min(nsteps, d.nt)
     g = Solver(d, owner=P)
     g.step(nsteps)
     o = po.OracleSim(d, owner=P)

@@ -87,16 +87,31 @@ def test_gpu_wave_is_the_analytic_plane_wave(ndof, phase):
         g.close()
 
 
-@BOTH
-@pytest.mark.parametrize("kind", ["GAUSSIAN", "BRUNE", "HARMONIC", "USER", "TAB"])
-def test_point_source_time_functions(kind, precision):
+def stf_deck(kind, ngll):
     dk = decks.lambs_problem()
-    dk.nelem, dk.fmax = (20, 10), 8.0
+    dk.nelem, dk.fmax, dk.ngll = (20, 10), 8.0 if ngll == 9 else 4.0, ngll
     t = np.linspace(0.0, 0.5, 11)
     dk.sources.stf = Stf(kind, f0=10.1, onset=0.15, ampli=1.3, par1=0.7,
                          tab=(t, np.sin(20 * t)) if kind == "TAB" else None)
-    d, g, o = run_both(dk, precision, nsteps=300)
+    return dk
+
+
+@BOTH
+@pytest.mark.parametrize("kind", ["GAUSSIAN", "BRUNE", "HARMONIC", "USER", "TAB"])
+def test_point_source_time_functions(kind, precision):
+    """NGLL 5: the one-element-per-thread kernel, which keeps the elastic
+    force as its state when a time function has a net impulse (a static
+    displacement that FP32 would not resolve against the dynamic one)."""
+    d, g, o = run_both(stf_deck(kind, 5), precision, nsteps=300)
     check(g, o, precision)
+
+
+@pytest.mark.parametrize("kind", ["GAUSSIAN", "TAB"])
+def test_point_source_time_functions_strip_fp64(kind):
+    """NGLL 9 (the strip kernel, which keeps the displacement state) in
+    FP64."""
+    d, g, o = run_both(stf_deck(kind, 9), PRECISION_FP64, nsteps=300)
+    check(g, o, PRECISION_FP64)
 
 
 @BOTH
