@@ -139,6 +139,10 @@ struct sem2d_handle {
   // its net impulse can leave a static displacement, which FP32 does not
   // resolve against the dynamic one (the force state is used then too)
   bool static_load = false;
+  // the strip kernel's force state (mixed precision, leapfrog, no
+  // Kelvin-Voigt, with a fault or a static load): F planes as for the march
+  // kernel
+  int strip_fst = 0;
   void *F[2] = {nullptr, nullptr};  // force state planes, ping-pong like D and V
   int tune_source = 0;  // launch shape: 0 analytic, 1 timed at create, 2 from the tuning cache
   int march_cz = 0, march_nunits = 0;
@@ -2294,6 +2298,18 @@ int create_impl(sem2d_handle *h, const sem2d_problem_desc *d, cudaStream_t share
     if (configure_bulk(bc)) return set_err(h, SEM2D_E_CUDA, bulk_last_error());
   }
   if ((st = setup_march(h, rec_ex, rec_ez, rec_jn, force_tz))) return st;
+  if (!h->march && !shared && h->mixed && (h->nflt > 0 || h->static_load) && h->scheme == 0 && !h->has_kv &&
+      !h->adjoint) {
+    const char *fs = std::getenv("SEM2D_FORCE_STATE");
+    if (!(fs && std::atoi(fs) == 0)) {
+      for (int b = 0; b < 2; ++b) {
+        float *q = nullptr;
+        if ((st = dalloc(h, &q, (size_t)h->plane * h->ndof))) return st;
+        h->F[b] = q;
+      }
+      h->strip_fst = 1;
+    }
+  }
   if ((st = reset_state(h))) return st;
   if (!shared && (st = tune_march(h))) return st;  // batch members are tuned with their batch
   CK(cudaStreamSynchronize(h->stream));

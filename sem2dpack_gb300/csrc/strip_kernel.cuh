@@ -280,6 +280,11 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
 
     const real *sg = stg + st * stage_sz;
     const real *sD = sg;
+    // force state (leapfrog, no Kelvin-Voigt; Fcur set by the host): the
+    // stiffness is applied to the velocity and the elastic force of the
+    // step is the previous one plus dt times that, so a large static
+    // displacement does not enter the FP32 force
+    const bool fst = p.Fcur != nullptr;
     const real *sM = sg + size_t(NDOF) * PS;
     const real *sV = sg + size_t(pV) * PS;
     const real *sA = sg + size_t(pA) * PS;
@@ -341,7 +346,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
         // displacement (+ eta v, mat_kelvin_voigt.f90:137-151) at (i,j)
         auto uval = [&](int cc, int i, int j) -> real {
           const int idx = eb + j * TWp + i;
-          real u = sD[cc * PS + idx];
+          real u = (fst ? sV : sD)[cc * PS + idx];
           if constexpr (KV) {
             real v = sV[cc * PS + idx];
             if (newmark) v = v + (hht ? p.cpa : p.cpred) * sA[cc * PS + idx];  // v_pred or v_alpha
@@ -354,7 +359,7 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
 #pragma unroll
             for (int q = 0; q < N; ++q) v[q] = act ? uval(cc, q, t) : real(0);
           } else {
-            xline(sD + cc * PS, v);
+            xline((fst ? sV : sD) + cc * PS, v);
           }
         };
         if constexpr (NDOF == 1 && MAT == kMatGeneral) {
@@ -699,6 +704,15 @@ __device__ __forceinline__ bool strip_unit(const BulkParams<real, N> &p, const r
           continue;
         }
         const int I = I0 + io;
+        if (fst) {  // the elastic force of this step: the previous one plus dt (-K v)
+          const long long gf = (long long)J * p.pitch + I;
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) {
+            const real fe = p.Fcur[c * p.plane + gf] + p.dt * f[c];
+            p.Fnext[c * p.plane + gf] = fe;
+            f[c] = fe;
+          }
+        }
         for (int k = 0; k < s_nsrc; ++k) {
           const int s = s_src[k];
           if (p.src_I[s] == I && p.src_J[s] == J)

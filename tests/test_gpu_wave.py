@@ -100,18 +100,20 @@ def stf_deck(kind, ngll):
 @pytest.mark.parametrize("kind", ["GAUSSIAN", "BRUNE", "HARMONIC", "USER", "TAB"])
 def test_point_source_time_functions(kind, precision):
     """NGLL 5: the one-element-per-thread kernel, which keeps the elastic
-    force as its state when a time function has a net impulse (a static
-    displacement that FP32 would not resolve against the dynamic one)."""
+    force as its state in mixed precision when a time function has a net
+    impulse (a static displacement that FP32 would not resolve against the
+    dynamic one)."""
     d, g, o = run_both(stf_deck(kind, 5), precision, nsteps=300)
     check(g, o, precision)
 
 
+@BOTH
 @pytest.mark.parametrize("kind", ["GAUSSIAN", "TAB"])
-def test_point_source_time_functions_strip_fp64(kind):
-    """NGLL 9 (the strip kernel, which keeps the displacement state) in
-    FP64."""
-    d, g, o = run_both(stf_deck(kind, 9), PRECISION_FP64, nsteps=300)
-    check(g, o, PRECISION_FP64)
+def test_point_source_time_functions_strip(kind, precision):
+    """NGLL 9: the strip kernel, which keeps the force state too under
+    leapfrog."""
+    d, g, o = run_both(stf_deck(kind, 9), precision, nsteps=300)
+    check(g, o, precision)
 
 
 @BOTH
