@@ -388,7 +388,7 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     stream = torch.cuda.ExternalStream(sim.stream)
 
     # end to end through the C-ABI from host arrays: the uploads made while
-    # the batch was built (sem2d_gpu_batch_add / close), one complete solve,
+    # the batch was built (sem2d_gpu_batch_add_many / close), one complete solve,
     # every member's seismograms back, and (below) the destroy
     barrier()
     t0 = time.perf_counter()
@@ -487,8 +487,9 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
                     "h2d_bytes_per_step": h2d / len(parts), "d2h_bytes_per_step": d2h / len(parts),
                     "h2d_bytes_per_solve": h2d, "d2h_bytes_per_solve": d2h,
                     "upload_s": sim.upload_seconds, "run_s": t_run, "destroy_s": t_close,
-                    "path": "BatchSolver through the C-ABI: batch_add of every shot from host arrays, "
-                            "one complete solve, all seismograms back, destroy"},
+                    "path": "BatchSolver through the C-ABI: batch_add_many of every shot from host arrays "
+                            "(16 shots per call, set up on host threads), one complete solve, all "
+                            "seismograms back, destroy"},
             "fp64_plain": fp64,
             "clocks": clk,
             "gpu_launches": launches,

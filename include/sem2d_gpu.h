@@ -343,6 +343,12 @@ int sem2d_gpu_create_batch(const sem2d_problem_desc *descs, int nsim, sem2d_hand
  * uploaded at once), close it (units and parameter blocks are built). */
 int sem2d_gpu_batch_open(sem2d_handle **out);
 int sem2d_gpu_batch_add(sem2d_handle *h, const sem2d_problem_desc *desc);
+/* n members at once, set up on up to SEM2D_HOST_THREADS host threads
+ * (default: the hardware threads, at most 16) and added in the order
+ * given; the descriptions are read during the call only.  On failure no
+ * member of the call is added.  sem2d_gpu_create_batch adds its members
+ * this way. */
+int sem2d_gpu_batch_add_many(sem2d_handle *h, const sem2d_problem_desc *descs, int n);
 int sem2d_gpu_batch_close(sem2d_handle *h);
 /* Number of members of a batch (0 for a single problem). */
 int sem2d_gpu_batch_size(sem2d_handle *h);

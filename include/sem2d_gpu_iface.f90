@@ -264,6 +264,13 @@ module sem2d_gpu_iface
       type(c_ptr), value :: h
       type(sem2d_problem_desc), intent(in) :: desc
     end function sem2d_gpu_batch_add
+    function sem2d_gpu_batch_add_many(h, descs, n) bind(C, name="sem2d_gpu_batch_add_many")
+      import :: c_int, c_double, c_long_long, c_ptr, sem2d_problem_desc, sem2d_lattice_args
+      integer(c_int) :: sem2d_gpu_batch_add_many
+      type(c_ptr), value :: h
+      type(sem2d_problem_desc), intent(in) :: descs(*)
+      integer(c_int), value :: n
+    end function sem2d_gpu_batch_add_many
     function sem2d_gpu_batch_close(h) bind(C, name="sem2d_gpu_batch_close")
       import :: c_int, c_double, c_long_long, c_ptr, sem2d_problem_desc, sem2d_lattice_args
       integer(c_int) :: sem2d_gpu_batch_close

@@ -21,6 +21,7 @@ PROTOTYPES = [
     ("sem2d_gpu_create_batch", C.c_int, [C.POINTER(abi.ProblemDesc), C.c_int, PP]),
     ("sem2d_gpu_batch_open", C.c_int, [PP]),
     ("sem2d_gpu_batch_add", C.c_int, [vp, C.POINTER(abi.ProblemDesc)]),
+    ("sem2d_gpu_batch_add_many", C.c_int, [vp, C.POINTER(abi.ProblemDesc), C.c_int]),
     ("sem2d_gpu_batch_close", C.c_int, [vp]),
     ("sem2d_gpu_batch_size", C.c_int, [vp]),
     ("sem2d_gpu_batch_member", C.c_void_p, [vp, C.c_int]),

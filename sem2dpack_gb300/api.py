@@ -10,6 +10,7 @@ There is no CPU execution path: Solver needs the compiled library and a
 CUDA device and raises Sem2dError otherwise.
 """
 import ctypes as C
+import os
 import time
 
 import numpy as np
@@ -267,40 +268,73 @@ class _Member(Solver):
 
 
 class BatchSolver:
-    """Independent problems advanced together by one launch per step
-    (sem2d_gpu_batch_open / add / close).  ``problems`` may be an iterator:
-    each Problem (or deck, or (deck, grid) pair) is built, uploaded and
-    released before the next one, so host memory holds one problem at a
-    time.  ``batch[i]`` reads the outputs of problem i."""
+    """Independent problems advanced together by one launch per step.
 
-    def __init__(self, problems, owners=None):
-        h = C.c_void_p()
-        st = lib().sem2d_gpu_batch_open(C.byref(h))
-        if st != 0:
-            raise Sem2dError(st, lib().sem2d_gpu_last_error(None).decode())
-        self.h = h
+    ``problems`` given as a list or tuple of problem descriptions
+    (ProblemDesc, whose arrays the caller keeps alive through ``owners``)
+    go through sem2d_gpu_create_batch.  Otherwise ``problems`` may be an
+    iterator of Problems (or decks, or (deck, grid) pairs, or descriptions)
+    taken ``group`` at a time (sem2d_gpu_batch_open / add_many / close):
+    a group is built, uploaded and released before the next one, so host
+    memory holds one group at a time.  Both calls set the members of a
+    group up on several host threads.  ``batch[i]`` reads the outputs of
+    problem i."""
+
+    def __init__(self, problems, owners=None, group=None):
+        self.h = None
         self._keep = list(owners or [])
-        self.upload_seconds = 0.0  # time spent in batch_add / batch_close
-        descs = []
-        try:
-            for p in problems:
-                if isinstance(p, abi.ProblemDesc):
-                    d = p
-                else:
-                    if not isinstance(p, Problem):
-                        p = Problem(*p) if isinstance(p, tuple) else Problem(p)
-                    d = p.desc()
-                t0 = time.perf_counter()
-                self._check(lib().sem2d_gpu_batch_add(h, C.byref(d)))
-                self.upload_seconds += time.perf_counter() - t0
-                # only the sizes of the description are used from now on
-                descs.append(abi.ProblemDesc.from_buffer_copy(d))
+        self.upload_seconds = 0.0  # time spent in the create / add / close calls
+        if isinstance(problems, (list, tuple)) and problems and all(
+                isinstance(p, abi.ProblemDesc) for p in problems):
+            arr = (abi.ProblemDesc * len(problems))(*problems)
+            h = C.c_void_p()
             t0 = time.perf_counter()
-            self._check(lib().sem2d_gpu_batch_close(h))
-            self.upload_seconds += time.perf_counter() - t0
-        except Exception:
-            self.close()
-            raise
+            st = lib().sem2d_gpu_create_batch(arr, len(problems), C.byref(h))
+            self.upload_seconds = time.perf_counter() - t0
+            if st != 0:
+                raise Sem2dError(st, lib().sem2d_gpu_last_error(None).decode())
+            self.h = h
+            descs = [abi.ProblemDesc.from_buffer_copy(d) for d in problems]
+        else:
+            h = C.c_void_p()
+            st = lib().sem2d_gpu_batch_open(C.byref(h))
+            if st != 0:
+                raise Sem2dError(st, lib().sem2d_gpu_last_error(None).decode())
+            self.h = h
+            descs = []
+            group = group or int(os.environ.get("SEM2D_HOST_THREADS", "0")) or min(16, os.cpu_count() or 1)
+            held = []  # the group's problems, alive until their upload returns
+
+            def flush():
+                if not held:
+                    return
+                arr = (abi.ProblemDesc * len(held))(*[d for d, _ in held])
+                t0 = time.perf_counter()
+                self._check(lib().sem2d_gpu_batch_add_many(h, arr, len(held)))
+                self.upload_seconds += time.perf_counter() - t0
+                # only the sizes of the descriptions are used from now on
+                descs.extend(abi.ProblemDesc.from_buffer_copy(d) for d, _ in held)
+                held.clear()
+
+            try:
+                for p in problems:
+                    if isinstance(p, abi.ProblemDesc):
+                        d = p
+                    else:
+                        if not isinstance(p, Problem):
+                            p = Problem(*p) if isinstance(p, tuple) else Problem(p)
+                        d = p.desc()
+                    held.append((d, p))
+                    del p
+                    if len(held) >= group:
+                        flush()
+                flush()
+                t0 = time.perf_counter()
+                self._check(lib().sem2d_gpu_batch_close(h))
+                self.upload_seconds += time.perf_counter() - t0
+            except Exception:
+                self.close()
+                raise
         self.members = [_Member(self, C.c_void_p(lib().sem2d_gpu_batch_member(h, i)), descs[i])
                         for i in range(len(descs))]
         self.nt = descs[0].nt

@@ -202,30 +202,25 @@ int launch_march_fault(const BulkConfig &c);
 // launch (a CTA per strip; nrows fault-side units per strip, at most 4)
 int launch_march_fault_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows);
 // one reverse step of the adjoint with the march kernels (FP32, NGLL=5,
-// isotropic node material): the forces pass, then the moduli pass
+// isotropic node material; march_adjoint.cuh): `bc` is the forward step's
+// configuration with (lambda^n, w^{n+1}) as (Dcur, Vcur) and (lambda^{n-1},
+// w^n) as (Dnext, Vnext), sources and receivers off; `c` the rest
 struct MarchAdjConfig {
-  int ndof = 0, LX = 0, LZ = 0, pitch = 0, nx = 0, nz = 0;
-  long long plane = 0;
-  const int *row0 = nullptr;
-  const double *H = nullptr, *w = nullptr;
-  const void *geo[4] = {nullptr, nullptr, nullptr, nullptr};
-  const void *mat[2] = {nullptr, nullptr};
-  const void *rmass = nullptr, *per_rm = nullptr, *per_Ca = nullptr, *per_Cb = nullptr;
-  const void *Db = nullptr, *Vb = nullptr;
-  void *Dbn = nullptr, *Vbn = nullptr;
-  const void *d = nullptr, *vprev = nullptr, *a = nullptr;
+  const void *a = nullptr, *vprev = nullptr;  // forward a^n, v^{n-1}
+  const void *d = nullptr;                    // forward d^n
   void *g_la = nullptr, *g_mu = nullptr, *g_M = nullptr, *g_C = nullptr;
   int nrec = 0, nsamp = 0, isamp = 1;
   char field = 'V';
-  const int *rec_I = nullptr, *rec_row = nullptr, *rec_ids_row = nullptr;
+  const int *rec_I = nullptr, *rec_J = nullptr;
   const double *resid = nullptr;
-  double dt = 0;
-  int kd2 = 0, it = 0;
+  int it = 0;
   const void *units = nullptr;
   int nunits = 0;
-  cudaStream_t stream = nullptr;
 };
-int launch_march_adjoint(const MarchAdjConfig &c);
+// reverse step c.it; *launches receives the number of kernels launched
+int launch_march_adjoint(const BulkConfig &bc, const MarchAdjConfig &c, int *launches);
+// lambda^{nt} from the velocity misfit of the last step (into Dcur of bc)
+int launch_march_adjoint_seed(const BulkConfig &bc, const MarchAdjConfig &c, int *launches);
 // resident warps per SM of the march kernel for the configuration; also
 // sets the kernels' shared-memory limit (call before any launch or capture)
 int march_warps_per_sm(const BulkConfig &c);

@@ -142,58 +142,74 @@ int launch_march_fault(const BulkConfig &c) {
   return 0;
 }
 
-int launch_march_adjoint(const MarchAdjConfig &c) {
-  MarchAdjParams p{};
-  p.LX = c.LX;
-  p.LZ = c.LZ;
-  p.pitch = c.pitch;
-  p.plane = c.plane;
-  p.nx = c.nx;
-  p.nz = c.nz;
-  p.row0 = c.row0;
-  for (int k = 0; k < 25; ++k) p.H[k] = float(c.H[k]);
-  for (int k = 0; k < 5; ++k) p.w[k] = float(c.w[k]);
-  p.xix = static_cast<const float *>(c.geo[0]);
-  p.etaz = static_cast<const float *>(c.geo[1]);
-  p.dxdxi = static_cast<const float *>(c.geo[2]);
-  p.dzdeta = static_cast<const float *>(c.geo[3]);
-  p.mat[0] = static_cast<const float *>(c.mat[0]);
-  p.mat[1] = static_cast<const float *>(c.mat[1]);
-  p.rmass = static_cast<const float *>(c.rmass);
-  p.per_rm = static_cast<const float *>(c.per_rm);
-  p.per_Ca = static_cast<const float *>(c.per_Ca);
-  p.per_Cb = static_cast<const float *>(c.per_Cb);
-  p.Db = static_cast<const float *>(c.Db);
-  p.Vb = static_cast<const float *>(c.Vb);
-  p.Dbn = static_cast<float *>(c.Dbn);
-  p.Vbn = static_cast<float *>(c.Vbn);
-  p.d = static_cast<const float *>(c.d);
-  p.vprev = static_cast<const float *>(c.vprev);
-  p.a = static_cast<const float *>(c.a);
-  p.g_la = static_cast<float *>(c.g_la);
-  p.g_mu = static_cast<float *>(c.g_mu);
-  p.g_M = static_cast<float *>(c.g_M);
-  p.g_C = static_cast<float *>(c.g_C);
-  p.nrec = c.nrec;
-  p.nsamp = c.nsamp;
-  p.isamp = c.isamp > 0 ? c.isamp : 1;
-  p.field = c.field;
-  p.rec_I = c.rec_I;
-  p.rec_row = c.rec_row;
-  p.rec_ids_row = c.rec_ids_row;
-  p.resid = c.resid;
-  p.dt = float(c.dt);
-  p.kd2 = c.kd2;
-  p.it = c.it;
+namespace {
+// the receivers' misfit derivatives of sample smp (march_adjoint_inject)
+int adjoint_inject(const BulkConfig &bc, const MarchAdjConfig &c, void *lam, void *wv, int smp, int disp) {
+  const int n = c.nrec * bc.ndof;
+  march_adjoint_inject<<<(n + 127) / 128, 128, 0, bc.stream>>>(
+      static_cast<float *>(lam), static_cast<float *>(wv), bc.plane, bc.pitch, bc.LX, bc.LZ,
+      static_cast<const float *>(bc.rmass), static_cast<const float *>(bc.per_rm), bc.ndof, c.nrec, c.nsamp, smp,
+      disp, c.rec_I, c.rec_J, c.resid, float(bc.dt));
+  return 1;
+}
+bool sampled(const MarchAdjConfig &c, int it) {
+  const int is = c.isamp > 0 ? c.isamp : 1;
+  return c.nrec > 0 && it > 0 && it % is == 0 && it / is < c.nsamp;
+}
+}  // namespace
+
+int launch_march_adjoint(const BulkConfig &bc, const MarchAdjConfig &c, int *launches) {
+  BulkParams<float, 5> p;
+  fill_params<float, 5>(bc, p);
+  MarchAdj x{};
+  x.a = static_cast<const float *>(c.a);
+  x.vprev = static_cast<const float *>(c.vprev);
+  x.g_M = static_cast<float *>(c.g_M);
+  x.g_C = static_cast<float *>(c.g_C);
+  MarchAdjParams m{};
+  m.LX = bc.LX;
+  m.LZ = bc.LZ;
+  m.pitch = bc.pitch;
+  m.plane = bc.plane;
+  m.nx = bc.nx;
+  m.nz = bc.nz;
+  m.row0 = bc.row0;
+  for (int k = 0; k < 25; ++k) m.H[k] = float(bc.H[k]);
+  for (int k = 0; k < 5; ++k) m.w[k] = float(bc.w[k]);
+  m.xix = static_cast<const float *>(bc.geo[0]);
+  m.etaz = static_cast<const float *>(bc.geo[1]);
+  m.dxdxi = static_cast<const float *>(bc.geo[2]);
+  m.dzdeta = static_cast<const float *>(bc.geo[3]);
+  m.lam = static_cast<const float *>(bc.Dcur);
+  m.d = static_cast<const float *>(c.d);
+  m.g_la = static_cast<float *>(c.g_la);
+  m.g_mu = static_cast<float *>(c.g_mu);
+  m.kd2 = bc.kd2;
   const MarchUnit *u = static_cast<const MarchUnit *>(c.units);
-  const int grid = std::max(1, (c.nunits + kMarchWarps - 1) / kMarchWarps);
-  if (c.ndof == 1) {
-    adj_march_forces<1><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
-    adj_march_moduli<1><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
-  } else {
-    adj_march_forces<2><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
-    adj_march_moduli<2><<<grid, kThreads, 0, c.stream>>>(p, u, c.nunits);
+  const int wpc = cta_warps(bc);
+  const int grid = std::max(1, (c.nunits + wpc - 1) / wpc);
+  const int mgrid = std::max(1, (c.nunits + kMarchWarps - 1) / kMarchWarps);
+  int n = 2;
+  if (bc.ndof == 1) march_adjoint_kernel<1><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+  else march_adjoint_kernel<2><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+  const int is = c.isamp > 0 ? c.isamp : 1;
+  if (c.field == 'D' && sampled(c, c.it)) n += adjoint_inject(bc, c, bc.Dnext, bc.Vnext, c.it / is, 1);
+  if (c.field != 'D' && sampled(c, c.it - 1)) n += adjoint_inject(bc, c, bc.Dnext, bc.Vnext, (c.it - 1) / is, 0);
+  if (bc.ndof == 1) adj_march_moduli<1><<<mgrid, kThreads, 0, bc.stream>>>(m, u, c.nunits);
+  else adj_march_moduli<2><<<mgrid, kThreads, 0, bc.stream>>>(m, u, c.nunits);
+  *launches = n;
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    g_bulk_err = cudaGetErrorString(e);
+    return 1;
   }
+  return 0;
+}
+
+int launch_march_adjoint_seed(const BulkConfig &bc, const MarchAdjConfig &c, int *launches) {
+  *launches = 0;
+  if (c.field == 'D' || !sampled(c, c.it)) return 0;
+  *launches = adjoint_inject(bc, c, bc.Dcur, bc.Vcur, c.it / (c.isamp > 0 ? c.isamp : 1), 0);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);

@@ -97,10 +97,20 @@ struct MarchBatch {
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-// one unit of one problem (FST: the force-state formulation)
-template <int NDOF, int MAT, bool FST>
+// What one reverse step of the discrete adjoint (ADJ, march_adjoint.cuh)
+// reads and writes beyond a forward step's planes: the forward a^n and
+// v^{n-1}, and the mass and dashpot gradient sums.
+struct MarchAdj {
+  const float *a, *vprev;
+  float *g_M;               // plane
+  float *g_C;               // [c * nslot + perimeter slot]
+};
+
+// one unit of one problem (FST: the force-state formulation; ADJ: a
+// reverse step of the adjoint, whose state (lambda, w) steps like (d, v))
+template <int NDOF, int MAT, bool FST, bool ADJ = false>
 __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const float *H, const float *w,
-                                           const MarchUnit &u, int it) {
+                                           const MarchUnit &u, int it, const MarchAdj *x = nullptr) {
   constexpr int N = 5;
   const int lane = threadIdx.x & 31;
   const int ex = kMarchCols * u.strip - 1 + lane;
@@ -370,7 +380,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
             if (last_col) Fn[c * pl + g + 4] = f[c][4];
           }
         }
-        if (src_on) {
+        if (!ADJ && src_on) {
           for (int s = 0; s < p.nsrc; ++s) {
             const int sI = p.src_I[s], sJ = p.src_J[s];
             if (sJ == J && own && sI >= I0 && sI < I0 + 4 + (last_col ? 1 : 0)) {
@@ -404,20 +414,22 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           rmv[4] = last_col ? __ldg(Rm + g + 4) : 0.f;
         }
         // dashpots and the perimeter inverse mass (only lanes with a node on
-        // the perimeter in this row look at the table)
-        const bool per_row = edgeJ || I0 == 0 || (last_col && I0 + N - 1 == p.LX - 1);
+        // the perimeter in this row look at the table; the adjoint applies
+        // the dashpots to its lambda update below)
 #pragma unroll
         for (int i = 0; i < N; ++i) {
           const int I = I0 + i;
           if (i == N - 1 && !last_col) continue;
           if (edgeJ || I == 0 || I == p.LX - 1) {
             const int sp = perimeter_slot(I, J, p.LX, p.LZ);
+            if (!ADJ) {
 #pragma unroll
-            for (int c = 0; c < NDOF; ++c) {
-              const int so = c * nslot + sp;
-              f[c][i] = f[c][i] - p.per_Ca[so] * vv[c][i];
-              f[c][i] = f[c][i] - p.per_Cb[so] * vv[c][i];
-              if (p.per_bf) f[c][i] = f[c][i] + p.per_bf[so];
+              for (int c = 0; c < NDOF; ++c) {
+                const int so = c * nslot + sp;
+                f[c][i] = f[c][i] - p.per_Ca[so] * vv[c][i];
+                f[c][i] = f[c][i] - p.per_Cb[so] * vv[c][i];
+                if (p.per_bf) f[c][i] = f[c][i] + p.per_bf[so];
+              }
             }
             rmv[i] = p.per_rm[sp];  // dof 0 entry; dof 1 below
           }
@@ -443,19 +455,49 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           dv[c][3] = q.w;
           dv[c][4] = last_col ? __ldg(Dc + c * pl + g + 4) : 0.f;
         }
+        float gm[N];
+#pragma unroll
+        for (int i = 0; i < N; ++i) gm[i] = 0.f;
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
           float vn[N], dn[N], an[N];
+          float aq[N];
+          if (ADJ) {
+            const float4 q = ldg4(x->a + c * pl + g);
+            aq[0] = q.x;
+            aq[1] = q.y;
+            aq[2] = q.z;
+            aq[3] = q.w;
+            aq[4] = last_col ? __ldg(x->a + c * pl + g + 4) : 0.f;
+          }
 #pragma unroll
           for (int i = 0; i < N; ++i) {
             float rm = rmv[i];
             const int I = I0 + i;
-            if (c == 1 && (edgeJ || I == 0 || I == p.LX - 1) && (i < N - 1 || last_col))
-              rm = p.per_rm[nslot + perimeter_slot(I, J, p.LX, p.LZ)];
-            const float a = rm * f[c][i];
-            an[i] = a;
-            vn[i] = vv[c][i] + cv * a;
-            dn[i] = dv[c][i] + dt * vn[i];
+            const bool edge = (edgeJ || I == 0 || I == p.LX - 1) && (i < N - 1 || last_col);
+            if (c == 1 && edge) rm = p.per_rm[nslot + perimeter_slot(I, J, p.LX, p.LZ)];
+            if (ADJ) {
+              // w^n = w^{n+1} + dt M^-1 F lambda^n;
+              // lambda^{n-1} = (1 - dt M^-1 C) lambda^n + dt w^n
+              // (the receivers' misfit derivatives are added after the launch)
+              const float a = rm * f[c][i];
+              an[i] = a;
+              vn[i] = vv[c][i] + cv * a;
+              float lam = dv[c][i];
+              gm[i] = gm[i] - lam * aq[i];  // mass term of the gradient with lambda^n
+              if (edge) {
+                const int so = c * nslot + perimeter_slot(I, J, p.LX, p.LZ);
+                lam = lam - (dt * rm) * ((p.per_Ca[so] + p.per_Cb[so]) * dv[c][i]);
+                // dashpot term
+                x->g_C[so] += -dv[c][i] * (x->vprev[c * pl + g + i] + (0.5f * dt) * aq[i]);
+              }
+              dn[i] = lam + dt * vn[i];
+            } else {
+              const float a = rm * f[c][i];
+              an[i] = a;
+              vn[i] = vv[c][i] + cv * a;
+              dn[i] = dv[c][i] + dt * vn[i];
+            }
           }
           *reinterpret_cast<float4 *>(Vn + c * pl + g) = make_float4(vn[0], vn[1], vn[2], vn[3]);
           *reinterpret_cast<float4 *>(Dn + c * pl + g) = make_float4(dn[0], dn[1], dn[2], dn[3]);
@@ -466,6 +508,15 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
             if (An) An[c * pl + g + 4] = an[4];
           }
         }
+        if (ADJ) {
+          float4 q = *reinterpret_cast<const float4 *>(x->g_M + g);
+          q.x = q.x + gm[0];
+          q.y = q.y + gm[1];
+          q.z = q.z + gm[2];
+          q.w = q.w + gm[3];
+          *reinterpret_cast<float4 *>(x->g_M + g) = q;
+          if (last_col) x->g_M[g + 4] = x->g_M[g + 4] + gm[4];
+        }
       }
     }
     if (halo) set_carry();
@@ -473,7 +524,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   }
 
   // ---- receivers of this unit ----
-  if (p.rec_ids && u.rec1 > u.rec0 && it % p.rec_isamp == 0 && it / p.rec_isamp < p.rec_nsamp) {
+  if (!ADJ && p.rec_ids && u.rec1 > u.rec0 && it % p.rec_isamp == 0 && it / p.rec_isamp < p.rec_nsamp) {
     __syncwarp();
     __threadfence_block();
     const int s = it / p.rec_isamp, nr = u.rec1 - u.rec0;

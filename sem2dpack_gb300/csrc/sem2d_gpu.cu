@@ -11,12 +11,15 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "../../include/sem2d_gpu.h"
@@ -2353,6 +2356,64 @@ int batch_add_impl(sem2d_handle *h, const sem2d_problem_desc *d) {
   return SEM2D_OK;
 }
 
+// Members added together: each is set up (lattice recovery, conversion of
+// the description's arrays to device planes, uploads) on one of up to
+// SEM2D_HOST_THREADS host threads (default: the hardware threads, at most
+// 16), all enqueueing on the batch's stream; the members join the batch in
+// the order given.  On failure nothing is added and the first failing
+// member is named.
+int batch_add_parallel(sem2d_handle *h, const sem2d_problem_desc *descs, int n) {
+  std::vector<sem2d_handle *> ms(n, nullptr);
+  for (int i = 0; i < n; ++i) {
+    ms[i] = new (std::nothrow) sem2d_handle();
+    if (!ms[i]) {
+      for (sem2d_handle *m : ms) delete m;
+      return set_err(h, SEM2D_E_NOMEM, "out of host memory");
+    }
+    ms[i]->owner = h;
+  }
+  std::vector<int> st(n, SEM2D_OK);
+  std::atomic<int> next{0};
+  auto work = [&]() {
+    for (int i; (i = next.fetch_add(1)) < n;) {
+      try {
+        st[i] = create_impl(ms[i], &descs[i], h->stream, kBatchChunk);
+      } catch (const std::bad_alloc &) {
+        ms[i]->err = "out of host memory";
+        st[i] = SEM2D_E_NOMEM;
+      }
+      if (!st[i]) {
+        std::vector<int>().swap(ms[i]->elem_ex);
+        std::vector<int>().swap(ms[i]->elem_ez);
+      }
+    }
+  };
+  int nthr = int(std::thread::hardware_concurrency());
+  if (const char *e = std::getenv("SEM2D_HOST_THREADS")) nthr = std::atoi(e);
+  nthr = std::max(1, std::min({nthr > 0 ? nthr : 1, 16, n}));
+  std::vector<std::thread> pool;
+  try {
+    for (int t = 1; t < nthr; ++t) pool.emplace_back(work);
+  } catch (const std::system_error &) {
+    // fewer threads than asked: the calling thread does the rest
+  }
+  work();
+  for (std::thread &t : pool) t.join();
+  int bad = -1;
+  for (int i = 0; i < n && bad < 0; ++i)
+    if (st[i]) bad = i;
+  if (bad >= 0) {
+    const std::string e = ms[bad]->err;
+    for (sem2d_handle *m : ms) {
+      m->owner = nullptr;
+      sem2d_gpu_destroy(m);
+    }
+    return set_err(h, st[bad], "problem " + std::to_string(h->subs.size() + bad) + ": " + e);
+  }
+  h->subs.insert(h->subs.end(), ms.begin(), ms.end());
+  return SEM2D_OK;
+}
+
 // The parameter blocks of every member of a batch for both buffer
 // parities and the batch's list of march units (member by member); replaces
 // those of an earlier call (the tuner rebuilds them for each shape).
@@ -2612,6 +2673,17 @@ int sem2d_gpu_batch_add(sem2d_handle *h, const sem2d_problem_desc *desc) {
   return batch_add_impl(h, desc);
 }
 
+int sem2d_gpu_batch_add_many(sem2d_handle *h, const sem2d_problem_desc *descs, int n) {
+  if (!h || (!descs && n > 0) || n < 0) return SEM2D_E_ARG;
+  if (!h->batch_open) return set_err(h, SEM2D_E_STATE, "not an open batch");
+  if (n == 0) return SEM2D_OK;
+  try {
+    return batch_add_parallel(h, descs, n);
+  } catch (const std::exception &) {
+    return set_err(h, SEM2D_E_NOMEM, "out of host resources");
+  }
+}
+
 int sem2d_gpu_batch_close(sem2d_handle *h) {
   if (!h) return SEM2D_E_ARG;
   if (!h->batch_open) return set_err(h, SEM2D_E_STATE, "not an open batch");
@@ -2631,7 +2703,11 @@ int sem2d_gpu_create_batch(const sem2d_problem_desc *descs, int nsim, sem2d_hand
   }
   int st = sem2d_gpu_batch_open(out);
   if (st) return st;
-  for (int i = 0; i < nsim && !st; ++i) st = sem2d_gpu_batch_add(*out, &descs[i]);
+  try {
+    st = batch_add_parallel(*out, descs, nsim);
+  } catch (const std::exception &) {
+    st = set_err(*out, SEM2D_E_NOMEM, "out of host resources");
+  }
   if (!st) st = sem2d_gpu_batch_close(*out);
   if (st) {
     g_create_err = (*out)->err;
@@ -2886,41 +2962,6 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
   // the march passes find the receivers of a lattice row through a CSR index
   MarchAdjConfig mc;
   if (h->march) {
-    std::vector<int> rI(std::max(h->nrec, 1)), rJ(std::max(h->nrec, 1));
-    if (h->nrec) {
-      CK(cudaMemcpy(rI.data(), h->rec_I, sizeof(int) * h->nrec, cudaMemcpyDeviceToHost));
-      CK(cudaMemcpy(rJ.data(), h->rec_J, sizeof(int) * h->nrec, cudaMemcpyDeviceToHost));
-    }
-    std::vector<int> row(h->LZ + 1, 0), ids(std::max(h->nrec, 1));
-    for (int r = 0; r < h->nrec; ++r) row[rJ[r] + 1]++;
-    for (int J = 0; J < h->LZ; ++J) row[J + 1] += row[J];
-    std::vector<int> fill(row.begin(), row.end() - 1);
-    for (int r = 0; r < h->nrec; ++r) ids[fill[rJ[r]]++] = r;
-    int *d_row = (int *)alloc(sizeof(int) * row.size()), *d_ids = (int *)alloc(sizeof(int) * ids.size());
-    if (!d_row || !d_ids) {
-      release();
-      return set_err(h, SEM2D_E_NOMEM, "no device memory for the adjoint");
-    }
-    CK(cudaMemcpyAsync(d_row, row.data(), sizeof(int) * row.size(), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaMemcpyAsync(d_ids, ids.data(), sizeof(int) * ids.size(), cudaMemcpyHostToDevice, h->stream));
-    CK(cudaStreamSynchronize(h->stream));
-    mc.ndof = nd;
-    mc.LX = h->LX;
-    mc.LZ = h->LZ;
-    mc.pitch = h->pitch;
-    mc.nx = h->nx;
-    mc.nz = h->nz;
-    mc.plane = h->plane;
-    mc.row0 = h->d_row0;
-    mc.H = h->H.data();
-    mc.w = h->w.data();
-    for (int q = 0; q < 4; ++q) mc.geo[q] = h->geo[q];
-    mc.mat[0] = h->mat[0];
-    mc.mat[1] = nd == 2 ? h->mat[1] : nullptr;
-    mc.rmass = h->rmass;
-    mc.per_rm = h->per_rm;
-    mc.per_Ca = h->per_Ca;
-    mc.per_Cb = h->per_Cb;
     mc.g_la = g_la;
     mc.g_mu = g_mu;
     mc.g_M = g_M;
@@ -2930,14 +2971,39 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
     mc.isamp = h->rec_isamp;
     mc.field = h->rec_field;
     mc.rec_I = h->rec_I;
-    mc.rec_row = d_row;
-    mc.rec_ids_row = d_ids;
+    mc.rec_J = h->rec_J;
     mc.resid = d_resid;
-    mc.dt = h->dt;
-    mc.kd2 = h->kd2;
     mc.units = h->d_march_units;
     mc.nunits = h->march_nunits;
-    mc.stream = h->stream;
+  }
+  // march path: the adjoint state (lambda, w) in (Dbar, Vbar); the step's
+  // configuration is the forward one on those planes, sources and
+  // receivers off
+  FaultParams<float> f_none;
+  auto adj_config = [&](int c) {
+    BulkConfig bc = make_config<float>(h, h->cur, f_none);
+    bc.Dcur = Dbar[c];
+    bc.Vcur = Vbar[c];
+    bc.Dnext = Dbar[1 - c];
+    bc.Vnext = Vbar[1 - c];
+    bc.Acur = bc.Anext = nullptr;
+    bc.Fcur = bc.Fnext = nullptr;
+    bc.march_fst = 0;
+    bc.nsrc = 0;
+    bc.rec_nrec = 0;
+    bc.rec_ids = nullptr;
+    bc.sis = nullptr;
+    bc.per_bf = nullptr;
+    bc.has_fault = 0;
+    bc.flt = nullptr;
+    return bc;
+  };
+  if (h->march) {
+    mc.it = h->nt;
+    int nl = 0;
+    if (launch_march_adjoint_seed(adj_config(0), mc, &nl))
+      st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
+    h->launches += nl;
   }
   int ca = 0;
   const int nseg = (h->nt + k - 1) / k;
@@ -2985,16 +3051,14 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
       ac.a = RA[j];
       ac.it = n;
       if (h->march) {
-        mc.Db = ac.Db;
-        mc.Vb = ac.Vb;
-        mc.Dbn = ac.Dbn;
-        mc.Vbn = ac.Vbn;
         mc.d = ac.d;
         mc.vprev = ac.vprev;
         mc.a = ac.a;
         mc.it = n;
-        if (launch_march_adjoint(mc)) st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
-        h->launches += 2;
+        int nl = 0;
+        if (launch_march_adjoint(adj_config(ca), mc, &nl))
+          st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
+        h->launches += nl;
       } else {
         if (launch_adjoint(ac)) st = set_err(h, SEM2D_E_CUDA, std::string("adjoint: ") + bulk_last_error());
         h->launches++;

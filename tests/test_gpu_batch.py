@@ -85,3 +85,26 @@ def test_batch_reset_and_errors():
     p2[1][1].nt = 50
     with pytest.raises(Sem2dError):
         BatchSolver([d for _, d in p2], owners=[P for P, _ in p2])
+
+
+def test_members_set_up_on_host_threads_equal_one_at_a_time(monkeypatch):
+    """sem2d_gpu_create_batch and batch_add_many set members up on several
+    host threads; the batch they build steps bit for bit like one built a
+    member at a time on one thread, in the order given.  A bad member in a
+    group is named and no member of that group joins the batch."""
+    probs = problems(6, PRECISION_MIXED, nsteps=80)
+    a = BatchSolver([d for _, d in probs], owners=[P for P, _ in probs])
+    monkeypatch.setenv("SEM2D_HOST_THREADS", "1")
+    b = BatchSolver(iter([d for _, d in probs]), owners=[P for P, _ in probs], group=1)
+    monkeypatch.setenv("SEM2D_HOST_THREADS", "4")
+    c = BatchSolver(iter([d for _, d in probs]), owners=[P for P, _ in probs], group=4)
+    for s in (a, b, c):
+        s.step(80)
+    for i, (_, d) in enumerate(probs):
+        assert a[i].desc.npoin == d.npoin
+        assert np.array_equal(a[i].seismograms(), b[i].seismograms()), i
+        assert np.array_equal(c[i].seismograms(), b[i].seismograms()), i
+    bad = problems(3, PRECISION_MIXED, nsteps=80)
+    bad[2][1].ndof = 3
+    with pytest.raises(Sem2dError, match="problem 2"):
+        BatchSolver([d for _, d in bad], owners=[P for P, _ in bad])

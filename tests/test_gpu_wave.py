@@ -87,6 +87,13 @@ def test_gpu_wave_is_the_analytic_plane_wave(ndof, phase):
         g.close()
 
 
+# the receivers are 700 and 1200 m from the source: the P wave of the pulse
+# centred at 0.15 s passes them by 0.55 s (1100 steps of 0.5 ms); before it
+# arrives they record only the tail of the discrete operator, a residue that
+# is no test of the precision
+STF_STEPS = 1100
+
+
 def stf_deck(kind, ngll):
     dk = decks.lambs_problem()
     dk.nelem, dk.fmax, dk.ngll = (20, 10), 8.0 if ngll == 9 else 4.0, ngll
@@ -103,7 +110,7 @@ def test_point_source_time_functions(kind, precision):
     force as its state in mixed precision when a time function has a net
     impulse (a static displacement that FP32 would not resolve against the
     dynamic one)."""
-    d, g, o = run_both(stf_deck(kind, 5), precision, nsteps=300)
+    d, g, o = run_both(stf_deck(kind, 5), precision, nsteps=STF_STEPS)
     check(g, o, precision)
 
 
@@ -112,7 +119,7 @@ def test_point_source_time_functions(kind, precision):
 def test_point_source_time_functions_strip(kind, precision):
     """NGLL 9: the strip kernel, which keeps the force state too under
     leapfrog."""
-    d, g, o = run_both(stf_deck(kind, 9), precision, nsteps=300)
+    d, g, o = run_both(stf_deck(kind, 9), precision, nsteps=STF_STEPS)
     check(g, o, precision)
 
 
