@@ -189,15 +189,36 @@ int launch_march_adjoint(const BulkConfig &bc, const MarchAdjConfig &c, int *lau
   const int wpc = cta_warps(bc);
   const int grid = std::max(1, (c.nunits + wpc - 1) / wpc);
   const int mgrid = std::max(1, (c.nunits + kMarchWarps - 1) / kMarchWarps);
-  int n = 2;
-  if (bc.ndof == 1) march_adjoint_kernel<1><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
-  else march_adjoint_kernel<2><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+  // the misfit derivatives of the step, by an extra CTA of the moduli launch
   const int is = c.isamp > 0 ? c.isamp : 1;
-  if (c.field == 'D' && sampled(c, c.it)) n += adjoint_inject(bc, c, bc.Dnext, bc.Vnext, c.it / is, 1);
-  if (c.field != 'D' && sampled(c, c.it - 1)) n += adjoint_inject(bc, c, bc.Dnext, bc.Vnext, (c.it - 1) / is, 0);
-  if (bc.ndof == 1) adj_march_moduli<1><<<mgrid, kThreads, 0, bc.stream>>>(m, u, c.nunits);
-  else adj_march_moduli<2><<<mgrid, kThreads, 0, bc.stream>>>(m, u, c.nunits);
-  *launches = n;
+  m.inj = -1;
+  if (c.field == 'D' && sampled(c, c.it)) {
+    m.inj = 1;
+    m.smp = c.it / is;
+  } else if (c.field != 'D' && sampled(c, c.it - 1)) {
+    m.inj = 0;
+    m.smp = (c.it - 1) / is;
+  }
+  m.ndof = bc.ndof;
+  m.nrec = c.nrec;
+  m.nsamp = c.nsamp;
+  m.lam_next = static_cast<float *>(bc.Dnext);
+  m.w_next = static_cast<float *>(bc.Vnext);
+  m.rmass = static_cast<const float *>(bc.rmass);
+  m.per_rm = static_cast<const float *>(bc.per_rm);
+  m.rec_I = c.rec_I;
+  m.rec_J = c.rec_J;
+  m.resid = c.resid;
+  m.dt = float(bc.dt);
+  const int mg = mgrid + (m.inj >= 0 ? 1 : 0);
+  if (bc.ndof == 1) {
+    march_adjoint_kernel<1><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+    adj_march_moduli<1><<<mg, kThreads, 0, bc.stream>>>(m, u, c.nunits);
+  } else {
+    march_adjoint_kernel<2><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+    adj_march_moduli<2><<<mg, kThreads, 0, bc.stream>>>(m, u, c.nunits);
+  }
+  *launches = 2;
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);

@@ -13,12 +13,11 @@
 // the leapfrog step of the forward march kernel with (lambda, w) in place
 // of (d, v) and the dashpots acting on the lambda update instead of the
 // force; the misfit derivatives are node-local additions at the receivers
-// (march_adjoint_inject).  Reverse step n reads (lambda^n, w^{n+1}) and
+// (adjoint_inject_one, by an extra CTA of the second launch).  Reverse step n reads (lambda^n, w^{n+1}) and
 // writes (lambda^{n-1}, w^n); it starts from lambda^{nt} = dt M^-1 g_v^{nt},
 // w^{nt+1} = 0.
 //
-// Two launches per reverse step (three at a sampled step), both walking
-// the forward's march units:
+// Two launches per reverse step, both walking the forward's march units:
 //   march_adjoint_kernel: march_unit<..., ADJ> (march_kernel.cuh): the
 //     step above, plus the mass term g_M += -lambda^n . a^n at every owned
 //     node and the dashpot term g_C += -lambda^n . (v^{n-1} + dt/2 a^n) on
@@ -47,6 +46,14 @@ struct MarchAdjParams {
   const float *d;    // forward d^n
   float *g_la, *g_mu;
   int kd2;
+  // the misfit derivatives of the step (march_adjoint_inject), added by the
+  // launch's last CTA when inj >= 0 (0: velocity, 1: displacement)
+  int inj, ndof, nrec, nsamp, smp;
+  float *lam_next, *w_next;  // lambda^{n-1}, w^n
+  const float *rmass, *per_rm;
+  const int *rec_I, *rec_J;
+  const double *resid;
+  float dt;
 };
 
 // one reverse step of lambda, w and the mass and dashpot sums
@@ -65,11 +72,10 @@ __global__ void __launch_bounds__(32 * kMarchWarps, NDOF == 1 ? 4 : 3)
 //     at the start, g_v^{nt} into lambda^{nt});
 //   displacement (disp = 1): w += dt M^-1 g and lambda += dt (dt M^-1 g)
 //     (g_d^n into w^n, and through it into lambda^{n-1} = ... + dt w^n).
-__global__ void march_adjoint_inject(float *lam, float *wv, long long plane, int pitch, int LX, int LZ,
-                                     const float *rmass, const float *per_rm, int ndof, int nrec, int nsamp, int smp,
-                                     int disp, const int *rec_I, const int *rec_J, const double *resid, float dt) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nrec * ndof) return;
+__device__ __forceinline__ void adjoint_inject_one(int k, float *lam, float *wv, long long plane, int pitch, int LX,
+                                                   int LZ, const float *rmass, const float *per_rm, int nrec,
+                                                   int nsamp, int smp, int disp, const int *rec_I, const int *rec_J,
+                                                   const double *resid, float dt) {
   const int r = k % nrec, c = k / nrec;
   const int I = rec_I[r], J = rec_J[r];
   float rm = rmass[(long long)J * pitch + I];
@@ -84,6 +90,15 @@ __global__ void march_adjoint_inject(float *lam, float *wv, long long plane, int
   } else {
     atomicAdd(lam + o, q);
   }
+}
+
+__global__ void march_adjoint_inject(float *lam, float *wv, long long plane, int pitch, int LX, int LZ,
+                                     const float *rmass, const float *per_rm, int ndof, int nrec, int nsamp, int smp,
+                                     int disp, const int *rec_I, const int *rec_J, const double *resid, float dt) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nrec * ndof)
+    adjoint_inject_one(k, lam, wv, plane, pitch, LX, LZ, rmass, per_rm, nrec, nsamp, smp, disp, rec_I, rec_J, resid,
+                       dt);
 }
 
 // ---------------------------------------------------------------------
@@ -233,6 +248,14 @@ __device__ __forceinline__ void adj_moduli_unit(const MarchAdjParams &p, const M
 template <int NDOF>
 __global__ void __launch_bounds__(32 * kMarchWarps, NDOF == 1 ? 4 : 3)
     adj_march_moduli(const __grid_constant__ MarchAdjParams p, const MarchUnit *units, int nunits) {
+  if (p.inj >= 0 && blockIdx.x == gridDim.x - 1) {
+    // the extra CTA: the misfit derivatives (lambda^{n-1} and w^n, which
+    // this launch does not read)
+    for (int k = threadIdx.x; k < p.nrec * p.ndof; k += blockDim.x)
+      adjoint_inject_one(k, p.lam_next, p.w_next, p.plane, p.pitch, p.LX, p.LZ, p.rmass, p.per_rm, p.nrec, p.nsamp,
+                         p.smp, p.inj, p.rec_I, p.rec_J, p.resid, p.dt);
+    return;
+  }
   const int uid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   if (uid < nunits) adj_moduli_unit<NDOF>(p, units[uid]);
 }

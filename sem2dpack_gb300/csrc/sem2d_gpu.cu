@@ -537,8 +537,12 @@ int upload_material(sem2d_handle *h, const sem2d_problem_desc *d) {
   }
   // node layout when every shared node carries one value
   bool node = !elem_const;
-  std::vector<std::vector<double>> planes(src.size(), std::vector<double>(h->plane, 0.0));
-  std::vector<char> seen(h->plane, 0);
+  std::vector<std::vector<double>> planes;
+  std::vector<char> seen;
+  if (node) {
+    planes.assign(src.size(), std::vector<double>(h->plane, 0.0));
+    seen.assign(h->plane, 0);
+  }
   for (int e = 0; e < ne && node; ++e)
     for (int q = 0; q < NN && node; ++q) {
       const long long L = h->glob2lat[d->ibool[q + (size_t)NN * e] - 1];
