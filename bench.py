@@ -316,26 +316,6 @@ def batch_parts(nt, k):
     return [nt // k + (1 if i < nt % k else 0) for i in range(k)]
 
 
-def built_problems(decks, workers):
-    """Problems of the decks, built by `workers` host threads (the C++
-    builder releases the interpreter lock) with a bounded look-ahead, in
-    deck order."""
-    from collections import deque
-    from concurrent.futures import ThreadPoolExecutor
-
-    from sem2dpack_gb300 import workloads
-    with ThreadPoolExecutor(max_workers=workers) as ex:
-        it = iter(decks)
-        futs = deque(ex.submit(workloads.build, dk) for _, dk in zip(range(2 * workers), it))
-        while futs:
-            P = futs.popleft().result()
-            nxt = next(it, None)
-            if nxt is not None:
-                futs.append(ex.submit(workloads.build, nxt))
-            yield P
-            del P
-
-
 def oracle_sample(decks, nsteps_of, threads):
     """Runs the FP64 oracle (CPU restatement of the reference's step, one
     problem per host thread, as independent reference runs would) on the
@@ -377,7 +357,16 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     nt = min(args.time_steps or 3000, 3000)
     workers = max(1, min(16, os.cpu_count() or 1))
     t0 = time.perf_counter()
-    sim = BatchSolver(built_problems(decks, workers))
+    # every problem built first on host threads (about 60 GB of host
+    # arrays for the 256 shots), then one create_batch call uploads them
+    # with the members set up on host threads; the arrays are released
+    # once the batch holds its device copies
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        probs = list(ex.map(workloads.build, decks))
+    build_s = time.perf_counter() - t0
+    sim = BatchSolver([P.desc() for P in probs])
+    del probs
     setup_s = time.perf_counter() - t0
     descs = [m.desc for m in sim.members]
     npoin = sum(d.npoin for d in descs)
@@ -387,8 +376,8 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     name = batch_name(len(sim), npoin, args.scale)
     stream = torch.cuda.ExternalStream(sim.stream)
 
-    # end to end through the C-ABI from host arrays: the uploads made while
-    # the batch was built (sem2d_gpu_batch_add_many / close), one complete solve,
+    # end to end through the C-ABI from host arrays: the upload
+    # (sem2d_gpu_create_batch), one complete solve,
     # every member's seismograms back, and (below) the destroy
     barrier()
     t0 = time.perf_counter()
@@ -475,7 +464,7 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
                                        "benchmark steps" % (nt, len(parts)),
                        "precision": "FP32 fields" if dtype == "f32" else "FP64",
                        "l2": "inputs larger than L2 (the batch's fields are %.1f GB)" % (npoin * bpn / 1e9),
-                       "host_setup_s": setup_s},
+                       "host_setup_s": setup_s, "host_build_s": build_s},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
                          "traffic": traffic, "peak_kind": peak_kind,
@@ -487,9 +476,9 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
                     "h2d_bytes_per_step": h2d / len(parts), "d2h_bytes_per_step": d2h / len(parts),
                     "h2d_bytes_per_solve": h2d, "d2h_bytes_per_solve": d2h,
                     "upload_s": sim.upload_seconds, "run_s": t_run, "destroy_s": t_close,
-                    "path": "BatchSolver through the C-ABI: batch_add_many of every shot from host arrays "
-                            "(16 shots per call, set up on host threads), one complete solve, all "
-                            "seismograms back, destroy"},
+                    "path": "BatchSolver through the C-ABI: sem2d_gpu_create_batch of every shot from host "
+                            "arrays (members set up on host threads), one complete solve, all seismograms "
+                            "back, destroy"},
             "fp64_plain": fp64,
             "clocks": clk,
             "gpu_launches": launches,

@@ -370,7 +370,10 @@ int sem2d_gpu_checkpoint_every(sem2d_handle *h, int every);
  * dashpot terms) with segment-wise recomputation from the checkpoints; the
  * gradient covers the moduli, the mass and the absorbing dashpots.  NGLL=5,
  * isotropic material continuous at nodes, leapfrog, no fault, Kelvin-Voigt
- * or 2.5D term, receivers at nodes recording V or D. */
+ * or 2.5D term, receivers at nodes recording V or D.  Device scratch of
+ * the call (3 x every + 8 lattice planes of ndof fields and a few more)
+ * comes from a stream-ordered pool of the library that keeps the memory
+ * reserved for later calls of the process. */
 int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, double *grad_vp,
                       double *grad_vs);
 

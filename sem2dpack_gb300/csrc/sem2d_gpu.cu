@@ -17,6 +17,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <system_error>
 #include <thread>
@@ -2863,6 +2864,28 @@ int sem2d_gpu_checkpoint_every(sem2d_handle *h, int every) {
   return SEM2D_OK;
 }
 
+// The library's pool for per-call device scratch (the adjoint): memory
+// freed into it stays reserved for the next call of the process.
+static cudaMemPool_t scratch_pool() {
+  static std::once_flag once;
+  static cudaMemPool_t pool = nullptr;
+  std::call_once(once, [] {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t p = nullptr;
+    if (cudaMemPoolCreate(&p, &props) != cudaSuccess) return;
+    unsigned long long keep = ~0ull;
+    cudaMemPoolSetAttribute(p, cudaMemPoolAttrReleaseThreshold, &keep);
+    pool = p;
+  });
+  return pool;
+}
+
 int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, double *grad_vp,
                       double *grad_vs) {
   if (!h || !resid) return SEM2D_E_ARG;
@@ -2881,26 +2904,34 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
   const size_t rs = h->mixed ? sizeof(float) : sizeof(double);
   const size_t fbytes = rs * (size_t)h->plane * h->ndof;
   const int k = h->ckpt_every, nd = h->ndof, nslot = perimeter_slots(h->LX, h->LZ);
+  // the call's device scratch comes from the library's stream-ordered pool,
+  // which keeps its memory between calls (the ring of one shot is several
+  // GB: cudaMalloc and cudaFree of it per call cost about a forward step
+  // per reverse segment on the 8-shot workload)
+  cudaMemPool_t pool = scratch_pool();
+  if (!pool) return set_err(h, SEM2D_E_CUDA, "no memory pool for the adjoint");
   std::vector<void *> tmp;
-  auto alloc = [&](size_t bytes) -> void * {
+  auto alloc_raw = [&](size_t bytes, bool zero) -> void * {
     void *q = nullptr;
-    if (cudaMalloc(&q, bytes) != cudaSuccess) return nullptr;
+    if (cudaMallocFromPoolAsync(&q, bytes, pool, h->stream) != cudaSuccess) return nullptr;
     tmp.push_back(q);
-    cudaMemsetAsync(q, 0, bytes, h->stream);
+    if (zero) cudaMemsetAsync(q, 0, bytes, h->stream);
     return q;
   };
+  auto alloc = [&](size_t bytes) { return alloc_raw(bytes, true); };
   auto release = [&]() {
+    for (void *q : tmp) cudaFreeAsync(q, h->stream);
     cudaStreamSynchronize(h->stream);
-    for (void *q : tmp) cudaFree(q);
     tmp.clear();
   };
   // ring of recomputed forward states: slot j holds (after step n0+j) the
-  // displacement predictor, velocity and acceleration
+  // displacement predictor, velocity and acceleration (written by the
+  // recomputation before any read)
   std::vector<void *> RD(k + 1), RV(k + 1), RA(k + 1);
   for (int j = 1; j <= k; ++j) {
-    RD[j] = alloc(fbytes);
-    RV[j] = alloc(fbytes);
-    RA[j] = alloc(fbytes);
+    RD[j] = alloc_raw(fbytes, false);
+    RV[j] = alloc_raw(fbytes, false);
+    RA[j] = alloc_raw(fbytes, false);
     if (!RD[j] || !RV[j] || !RA[j]) {
       release();
       return set_err(h, SEM2D_E_NOMEM, "no device memory for the recomputed segment");
