@@ -460,7 +460,12 @@ long long sem2d_gpu_kernel_launches(sem2d_handle *h);
  * (SEM2D_MARCH_CZ=TZ overrides its chunk height, SEM2D_MARCH=0 selects the
  * strip kernel).  Every other problem runs the strip kernel: a CTA per
  * unit (SEM2D_CHUNK=TZ overrides its chunk height).  The environment is
- * read at create time. */
+ * read at create time.  The march kernel's shape comes from the tuning
+ * cache (SEM2D_TUNE_CACHE) when it holds the class of the problem; else
+ * five shapes are timed on the first 85 steps of the first step call that
+ * runs at least 85 steps between checks (every shape gives the same
+ * results), and the fastest is kept and recorded (SEM2D_AUTOTUNE=0: the
+ * analytic shape). */
 int sem2d_gpu_tile_shape(sem2d_handle *h, int *tx, int *tz);
 
 /* Releases device memory; h becomes invalid. */

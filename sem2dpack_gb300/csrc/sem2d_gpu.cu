@@ -148,7 +148,8 @@ struct sem2d_handle {
   // kernel
   int strip_fst = 0;
   void *F[2] = {nullptr, nullptr};  // force state planes, ping-pong like D and V
-  int tune_source = 0;  // launch shape: 0 analytic, 1 timed at create, 2 from the tuning cache
+  int tune_source = 0;  // launch shape: 0 analytic, 1 timed on the first run, 2 from the tuning cache
+  int tune_pending = 0;  // the shape is timed on the next run of at least kTuneSteps steps
   int march_cz = 0, march_nunits = 0;
   void *d_march_units = nullptr;
   int *d_march_rec = nullptr;
@@ -2019,43 +2020,60 @@ int time_shape(sem2d_handle *h, int nwarm, int n, double *ms) {
   return st;
 }
 
-int tune_march(sem2d_handle *h) {
-  if (!h->march || tune_disabled()) return SEM2D_OK;
+// The launch shape of a class of problems: from the tuning cache when it
+// holds the class, else timed on the handle's first run of at least
+// kTuneSteps steps (tune_on_run).
+constexpr int kTuneWarm = 1, kTuneTimed = 16, kTuneShapes = 5;
+constexpr int kTuneSteps = kTuneShapes * (kTuneWarm + kTuneTimed);
+
+bool tune_key(const sem2d_handle *h, char *key, size_t n) {
   const sem2d_handle *a = h->subs.empty() ? h : h->subs[0];
   long long nodes = 0;
   if (h->subs.empty()) nodes = h->npoin;
   for (const sem2d_handle *m : h->subs) nodes += m->npoin;
   int dev = 0, nsm = 1;
-  CK(cudaGetDevice(&dev));
-  CK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return false;
+  return sem2d_tune_key(a->ndof, a->mat_elem, nodes, int(h->subs.size()), nsm, key, n) == SEM2D_OK;
+}
+
+int tune_march(sem2d_handle *h) {
+  if (!h->march || tune_disabled()) return SEM2D_OK;
   char key[160], path[1024];
-  if (sem2d_tune_key(a->ndof, a->mat_elem, nodes, int(h->subs.size()), nsm, key, sizeof(key)) != SEM2D_OK)
-    return SEM2D_OK;
-  const bool have_path = sem2d_tune_cache_path(path, sizeof(path)) == SEM2D_OK;
+  if (!tune_key(h, key, sizeof(key))) return SEM2D_OK;
   sem2d_tune_entry e;
-  if (have_path && sem2d_tune_lookup(path, key, &e) == 1) {
+  if (sem2d_tune_cache_path(path, sizeof(path)) == SEM2D_OK && sem2d_tune_lookup(path, key, &e) == 1) {
     h->tune_source = 2;
     return apply_shape(h, MarchShape{e.chunk_rows, e.warps_per_cta});
   }
-  const int nwarm = 2, n = std::min(32, h->nt - nwarm);
-  if (n < 4) return SEM2D_OK;  // too few steps to time: the analytic shape
+  h->tune_pending = 1;
+  return SEM2D_OK;
+}
+
+// Times the candidate shapes on the run's own first kTuneSteps steps (every
+// shape gives the same bits, so these are steps of the solution), keeps the
+// fastest unless the analytic one is within 2 %, and records it in the
+// tuning cache.
+int tune_on_run(sem2d_handle *h) {
+  h->tune_pending = 0;
+  const sem2d_handle *a = h->subs.empty() ? h : h->subs[0];
   const int cz0 = a->march_cz;
-  const MarchShape cands[] = {{cz0, a->march_warps}, {cz0, 1}, {2 * cz0, a->march_warps},
-                              {std::max(1, cz0 / 2), a->march_warps}, {2 * cz0, 1}};
-  const int nc = int(sizeof(cands) / sizeof(cands[0]));
-  std::vector<sem2d_tune_entry> res(nc);
-  const long long l0 = h->launches;
+  const MarchShape cands[kTuneShapes] = {{cz0, a->march_warps}, {cz0, 1}, {2 * cz0, a->march_warps},
+                                         {std::max(1, cz0 / 2), a->march_warps}, {2 * cz0, 1}};
+  std::vector<sem2d_tune_entry> res(kTuneShapes);
   int st;
-  for (int k = 0; k < nc; ++k) {
+  for (int k = 0; k < kTuneShapes; ++k) {
     double ms = 0;
-    if ((st = apply_shape(h, cands[k])) || (st = time_shape(h, nwarm, n, &ms)) || (st = reset_state(h))) return st;
+    if ((st = apply_shape(h, cands[k])) || (st = time_shape(h, kTuneWarm, kTuneTimed, &ms))) return st;
     res[k] = sem2d_tune_entry{std::max(1, std::min(cands[k].cz, a->nz)), cands[k].warps, ms};
   }
-  const int best = sem2d_tune_select(res.data(), nc, 0.02);
+  const int best = sem2d_tune_select(res.data(), kTuneShapes, 0.02);
   if ((st = apply_shape(h, cands[best]))) return st;
-  h->launches = l0;
   h->tune_source = 1;
-  if (have_path) sem2d_tune_record(path, key, &res[best]);  // a cache that cannot be written is not an error
+  char key[160], path[1024];
+  if (tune_key(h, key, sizeof(key)) && sem2d_tune_cache_path(path, sizeof(path)) == SEM2D_OK)
+    sem2d_tune_record(path, key, &res[best]);  // a cache that cannot be written is not an error
   return SEM2D_OK;
 }
 
@@ -2769,6 +2787,10 @@ namespace {
 int step_impl(sem2d_handle *h, int nsteps) {
   int st;
   int left = nsteps;
+  if (h->tune_pending && left >= kTuneSteps) {
+    if ((st = tune_on_run(h))) return st;
+    left -= kTuneSteps;
+  }
   const char *nog = std::getenv("SEM2D_NO_GRAPH");
   const bool use_graph = !(nog && nog[0] == '1');
   // align to even parity, then replay captured runs
