@@ -62,6 +62,7 @@ struct sem2d_handle {
   long long plane = 0;
   std::vector<int> row0;             // [nz+1]
   std::vector<long long> glob2lat;   // global node -> J*pitch + I
+  long long *d_glob2lat = nullptr;   // the same on the device (the adjoint's output), when needed
   std::vector<int> elem_ex, elem_ez; // reference element -> structured position
   int TX = 8, TZ = 8, nplanes = 0, nmat = 0, mat_iso = 0, mat_elem = 0, has_kv = 0;
   std::vector<int> ztile;            // chunk boundaries (element rows)
@@ -2886,6 +2887,15 @@ int sem2d_gpu_checkpoint_every(sem2d_handle *h, int every) {
   return SEM2D_OK;
 }
 
+// out[q * npoin + p] = lat[q * plane + g2l[p]] for the three gradients
+static __global__ void gather_nodes_kernel(const double *lat, long long plane, const long long *g2l, int npoin,
+                                           double *out) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= npoin) return;
+  const long long L = g2l[p];
+  for (int q = 0; q < 3; ++q) out[(size_t)q * npoin + p] = lat[q * plane + L];
+}
+
 // The library's pool for per-call device scratch (the adjoint): memory
 // freed into it stays reserved for the next call of the process.
 static cudaMemPool_t scratch_pool() {
@@ -3155,15 +3165,29 @@ int sem2d_gpu_adjoint(sem2d_handle *h, const double *resid, double *grad_rho, do
   }
   const int s_now = h->steps;
   if (!st) {
-    std::vector<double> hg(3 * (size_t)h->plane);
-    if (cudaMemcpyAsync(hg.data(), grads, 8 * hg.size(), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess ||
-        cudaMemcpyAsync(h->d_step, &s_now, sizeof(int), cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
-        cudaStreamSynchronize(h->stream) != cudaSuccess)
-      st = set_err(h, SEM2D_E_CUDA, "adjoint: copy back failed");
+    // the gradients in global node order on the device, copied straight
+    // into the caller's arrays
+    if (!h->d_glob2lat) {
+      if ((st = dupload(h, &h->d_glob2lat, h->glob2lat))) {
+        release();
+        return st;
+      }
+    }
+    double *nodes = (double *)alloc_raw(8 * 3 * (size_t)h->npoin, false);
+    if (!nodes) {
+      release();
+      return set_err(h, SEM2D_E_NOMEM, "no device memory for the adjoint");
+    }
+    gather_nodes_kernel<<<(h->npoin + 255) / 256, 256, 0, h->stream>>>(grads, h->plane, h->d_glob2lat, h->npoin,
+                                                                       nodes);
     double *out[3] = {grad_rho, grad_vp, grad_vs};
     for (int q = 0; q < 3 && !st; ++q)
-      if (out[q])
-        for (int pnode = 0; pnode < h->npoin; ++pnode) out[q][pnode] = hg[(size_t)q * h->plane + h->glob2lat[pnode]];
+      if (out[q] && cudaMemcpyAsync(out[q], nodes + (size_t)q * h->npoin, 8 * (size_t)h->npoin,
+                                    cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+        st = set_err(h, SEM2D_E_CUDA, "adjoint: copy back failed");
+    if (!st && (cudaMemcpyAsync(h->d_step, &s_now, sizeof(int), cudaMemcpyHostToDevice, h->stream) != cudaSuccess ||
+                cudaStreamSynchronize(h->stream) != cudaSuccess))
+      st = set_err(h, SEM2D_E_CUDA, "adjoint: copy back failed");
   }
   release();
   if (st) return st;
