@@ -26,8 +26,8 @@ int launch_one(const BulkConfig &c, const MarchLaunch &m) {
   fill_params<float, 5>(c, p);
   const int wpc = cta_warps(c);
   const int grid = std::max(1, (m.nunits + wpc - 1) / wpc);  // an empty set still counts the step
-  march_step_kernel<NDOF, MAT, FST><<<grid, 32 * wpc, 0, c.stream>>>(p, static_cast<const MarchUnit *>(m.units),
-                                                                      m.nunits);
+  march_step_kernel<NDOF, MAT, FST><<<grid, 32 * wpc, wpc * march_stage_bytes(NDOF, FST), c.stream>>>(
+      p, static_cast<const MarchUnit *>(m.units), m.nunits);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -48,7 +48,7 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
   b.done = m.done;
   const int wpc = cta_warps(c);
   const int grid = std::max(1, (m.nunits + wpc - 1) / wpc);  // an empty set still counts the step
-  march_batch_kernel<NDOF, MAT><<<grid, 32 * wpc, 0, c.stream>>>(b);
+  march_batch_kernel<NDOF, MAT><<<grid, 32 * wpc, wpc * march_stage_bytes(NDOF, false), c.stream>>>(b);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     g_bulk_err = cudaGetErrorString(e);
@@ -61,7 +61,7 @@ template <int NDOF, int MAT, bool FST>
 int launch_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
-  march_fault_side_kernel<NDOF, MAT, FST><<<nstrips, kThreads, 0, c.stream>>>(
+  march_fault_side_kernel<NDOF, MAT, FST><<<nstrips, kThreads, kMarchWarps * march_stage_bytes(NDOF, FST), c.stream>>>(
       p, static_cast<const MarchUnit *>(m.units), nstrips, nrows);
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
@@ -74,7 +74,8 @@ int launch_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrow
 template <int NDOF, int MAT, bool FST>
 int occupancy_one(int wpc) {
   int nb = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, FST>, 32 * wpc, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, FST>, 32 * wpc,
+                                                    wpc * march_stage_bytes(NDOF, FST)) !=
       cudaSuccess)
     return 0;
   return nb * wpc;
@@ -212,10 +213,10 @@ int launch_march_adjoint(const BulkConfig &bc, const MarchAdjConfig &c, int *lau
   m.dt = float(bc.dt);
   const int mg = mgrid + (m.inj >= 0 ? 1 : 0);
   if (bc.ndof == 1) {
-    march_adjoint_kernel<1><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+    march_adjoint_kernel<1><<<grid, 32 * wpc, wpc * march_stage_bytes(1, false), bc.stream>>>(p, x, c.it, u, c.nunits);
     adj_march_moduli<1><<<mg, kThreads, 0, bc.stream>>>(m, u, c.nunits);
   } else {
-    march_adjoint_kernel<2><<<grid, 32 * wpc, 0, bc.stream>>>(p, x, c.it, u, c.nunits);
+    march_adjoint_kernel<2><<<grid, 32 * wpc, wpc * march_stage_bytes(2, false), bc.stream>>>(p, x, c.it, u, c.nunits);
     adj_march_moduli<2><<<mg, kThreads, 0, bc.stream>>>(m, u, c.nunits);
   }
   *launches = 2;

@@ -61,8 +61,11 @@ template <int NDOF>
 __global__ void __launch_bounds__(32 * kMarchWarps, NDOF == 1 ? 4 : 3)
     march_adjoint_kernel(const __grid_constant__ BulkParams<float, 5> p, const __grid_constant__ MarchAdj x, int it,
                          const MarchUnit *units, int nunits) {
-  const int uid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (uid < nunits) march_unit<NDOF, kMatNode, false, true>(p, p.H, p.w, units[uid], it, &x);
+  const int warp = threadIdx.x >> 5;
+  const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
+  extern __shared__ float4 march_stage[];
+  if (uid < nunits)
+    march_unit<NDOF, kMatNode, false, true>(p, p.H, p.w, units[uid], it, march_stage + warp * march_stage_f4(NDOF), &x);
 }
 
 // The misfit derivatives g of sample smp at the receivers' nodes, thread k

@@ -97,6 +97,27 @@ struct MarchBatch {
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
+// P-SV in the displacement state (the batch kernel among them): the node
+// update's velocity and inverse-mass rows of an element row are staged in
+// shared memory by cp.async when the row starts, so that their loads fly
+// while the element forces are computed (3 % on the batched shots): per
+// warp, node rows j = 0..4, planes v (ndof) and inverse mass, 16 bytes per
+// lane; each lane reads back only what it copied.  (SH and the force state,
+// whose element pass has just read the velocity, load them directly: staged
+// they measured slower.)
+__host__ __device__ constexpr bool march_staged(int ndof, bool fst) { return ndof == 2 && !fst; }
+__host__ __device__ constexpr int march_stage_f4(int ndof) { return 5 * (ndof + 1) * 32; }
+__host__ __device__ constexpr int march_stage_bytes(int ndof, bool fst) {
+  return march_staged(ndof, fst) ? march_stage_f4(ndof) * 16 : 0;
+}
+
+__device__ __forceinline__ void cp_async16(float4 *dst, const float *src) {
+  const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 // What one reverse step of the discrete adjoint (ADJ, march_adjoint.cuh)
 // reads and writes beyond a forward step's planes: the forward a^n and
 // v^{n-1}, and the mass and dashpot gradient sums.
@@ -110,7 +131,8 @@ struct MarchAdj {
 // reverse step of the adjoint, whose state (lambda, w) steps like (d, v))
 template <int NDOF, int MAT, bool FST, bool ADJ = false>
 __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const float *H, const float *w,
-                                           const MarchUnit &u, int it, const MarchAdj *x = nullptr) {
+                                           const MarchUnit &u, int it, float4 *stage,
+                                           const MarchAdj *x = nullptr) {
   constexpr int N = 5;
   const int lane = threadIdx.x & 31;
   const int ex = kMarchCols * u.strip - 1 + lane;
@@ -170,12 +192,27 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   };
   if (kPrefetch) fetch_u(zs);
 
+  constexpr int NP = NDOF + 1;  // staged planes per node row
+  constexpr bool kStage = march_staged(NDOF, FST);
   for (int ez = zs; ez < u.z1; ++ez) {
     const bool halo = ez < u.z0;
     const int J0 = p.row0[ez];
     const float etaz = act ? p.etaz[ez] : 0.f;
     const float det = dxdxi * (act ? p.dzdeta[ez] : 0.f);
     const long long eidx = (long long)ez * p.nx + (ex < 0 ? 0 : ex);
+    // the node rows this element row updates (below), staged now
+    if (kStage && !halo && own) {
+      const int nrow = (ez == p.nz - 1 || (p.has_fault && J0 + N - 1 == p.jf1)) ? N : N - 1;
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        if (j < nrow) {
+          const long long g = (long long)(J0 + j) * p.pitch + I0;
+#pragma unroll
+          for (int c = 0; c < NDOF; ++c) cp_async16(stage + (j * NP + c) * 32 + lane, p.Vcur + c * pl + g);
+          cp_async16(stage + (j * NP + NDOF) * 32 + lane, p.rmass + g);
+        }
+      cp_async_commit();
+    }
 
     // ---- element forces: A holds u (d, or v with FST), then d/deta; B holds d/dxi ----
     float A[NDOF][N][N], B[NDOF][N][N];
@@ -354,6 +391,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     // the top row is not shared (lattice top or fault side 1) and this
     // chunk owns it
     if (!halo) {
+      if (kStage && own) cp_async_wait_all();
 #pragma unroll
       for (int j = 0; j < N; ++j) {
         if (j == 1) set_carry();
@@ -398,7 +436,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float vv[NDOF][N], rmv[N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = ldg4(Vc + c * pl + g);
+          const float4 q = kStage ? stage[(j * NP + c) * 32 + lane] : ldg4(Vc + c * pl + g);
           vv[c][0] = q.x;
           vv[c][1] = q.y;
           vv[c][2] = q.z;
@@ -406,7 +444,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           vv[c][4] = last_col ? __ldg(Vc + c * pl + g + 4) : 0.f;
         }
         {
-          const float4 q = ldg4(Rm + g);
+          const float4 q = kStage ? stage[(j * NP + NDOF) * 32 + lane] : ldg4(Rm + g);
           rmv[0] = q.x;
           rmv[1] = q.y;
           rmv[2] = q.z;
@@ -570,9 +608,10 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   const int warp = threadIdx.x >> 5;
   const int it = *p.step + 1;
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
+  extern __shared__ float4 march_stage[];
   if (uid < nunits) {
     const MarchUnit u = units[uid];
-    march_unit<NDOF, MAT, FST>(p, p.H, p.w, u, it);
+    march_unit<NDOF, MAT, FST>(p, p.H, p.w, u, it, march_stage + warp * march_stage_f4(NDOF));
   }
   march_done(p.step, p.done, it);
 }
@@ -585,9 +624,10 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   const int warp = threadIdx.x >> 5;
   const int it = *b.step + 1;
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
+  extern __shared__ float4 march_stage[];
   if (uid < b.nunits) {
     const MarchUnit u = b.units[uid];
-    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, u, it);
+    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, u, it, march_stage + warp * march_stage_f4(NDOF));
   }
   march_done(b.step, b.done, it);
 }
@@ -603,7 +643,9 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
                             int nrows) {
   const int warp = threadIdx.x >> 5, s = blockIdx.x;
   const int it = *p.step + 1;
-  if (warp < nrows) march_unit<NDOF, MAT, FST>(p, p.H, p.w, units[warp * nstrips + s], it);
+  extern __shared__ float4 march_stage[];
+  if (warp < nrows)
+    march_unit<NDOF, MAT, FST>(p, p.H, p.w, units[warp * nstrips + s], it, march_stage + warp * march_stage_f4(NDOF));
   __syncthreads();  // the strip's fault-row forces are written (global memory, this block)
   const int t = threadIdx.x, I = 4 * kMarchCols * s + t;
   const bool mine = (t < 4 * kMarchCols && I < p.LX) || (t == 4 * kMarchCols && I == p.LX - 1);
