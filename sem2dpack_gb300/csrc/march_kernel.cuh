@@ -200,6 +200,11 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
     const float etaz = act ? p.etaz[ez] : 0.f;
     const float det = dxdxi * (act ? p.dzdeta[ez] : 0.f);
     const long long eidx = (long long)ez * p.nx + (ex < 0 ? 0 : ex);
+    // a source in the node rows of this element row (the lanes test each
+    // row's sources only then)
+    bool src_row = false;
+    if (!ADJ && src_on && !halo)
+      for (int s = 0; s < p.nsrc; ++s) src_row = src_row || (p.src_J[s] >= J0 && p.src_J[s] < J0 + N);
     // the node rows this element row updates (below), staged now
     if (kStage && !halo && own) {
       const int nrow = (ez == p.nz - 1 || (p.has_fault && J0 + N - 1 == p.jf1)) ? N : N - 1;
@@ -418,7 +423,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
             if (last_col) Fn[c * pl + g + 4] = f[c][4];
           }
         }
-        if (!ADJ && src_on) {
+        if (!ADJ && src_row) {
           for (int s = 0; s < p.nsrc; ++s) {
             const int sI = p.src_I[s], sJ = p.src_J[s];
             if (sJ == J && own && sI >= I0 && sI < I0 + 4 + (last_col ? 1 : 0)) {
