@@ -20,8 +20,22 @@ static_assert(kMarchWarpsHost == kMarchWarps, "host and device CTA shapes");
 // warps per CTA of a launch (1, 2 or 4)
 int cta_warps(const BulkConfig &c) { return c.march_warps == 1 || c.march_warps == 2 ? c.march_warps : kMarchWarps; }
 
+// the staged rows of a 4-warp CTA may exceed the default 48 KB of dynamic
+// shared memory (P-SV force state: 51 KB); allowed once per kernel
+template <int NDOF, int MAT, bool FST>
+void allow_stage() {
+  static const bool done = [] {
+    const int b = kMarchWarps * march_stage_bytes(NDOF, FST);
+    cudaFuncSetAttribute(march_step_kernel<NDOF, MAT, FST>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    cudaFuncSetAttribute(march_fault_side_kernel<NDOF, MAT, FST>, cudaFuncAttributeMaxDynamicSharedMemorySize, b);
+    return true;
+  }();
+  (void)done;
+}
+
 template <int NDOF, int MAT, bool FST>
 int launch_one(const BulkConfig &c, const MarchLaunch &m) {
+  allow_stage<NDOF, MAT, FST>();
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
   const int wpc = cta_warps(c);
@@ -59,6 +73,7 @@ int launch_many(const BulkConfig &c, const MarchLaunch &m) {
 
 template <int NDOF, int MAT, bool FST>
 int launch_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrows) {
+  allow_stage<NDOF, MAT, FST>();
   BulkParams<float, 5> p;
   fill_params<float, 5>(c, p);
   march_fault_side_kernel<NDOF, MAT, FST><<<nstrips, kThreads, kMarchWarps * march_stage_bytes(NDOF, FST), c.stream>>>(
@@ -73,6 +88,7 @@ int launch_side(const BulkConfig &c, const MarchLaunch &m, int nstrips, int nrow
 
 template <int NDOF, int MAT, bool FST>
 int occupancy_one(int wpc) {
+  allow_stage<NDOF, MAT, FST>();
   int nb = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, march_step_kernel<NDOF, MAT, FST>, 32 * wpc,
                                                     wpc * march_stage_bytes(NDOF, FST)) !=
@@ -212,12 +228,22 @@ int launch_march_adjoint(const BulkConfig &bc, const MarchAdjConfig &c, int *lau
   m.resid = c.resid;
   m.dt = float(bc.dt);
   const int mg = mgrid + (m.inj >= 0 ? 1 : 0);
+  // the P-SV step stages six planes per node row: 7.5 KB per warp
+  const int sb1 = wpc * march_stage_bytes(1, false, true), sb2 = wpc * march_stage_bytes(2, false, true);
+  static const bool smem_set = [] {
+    cudaFuncSetAttribute(march_adjoint_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kMarchWarps * march_stage_bytes(1, false, true));
+    cudaFuncSetAttribute(march_adjoint_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         kMarchWarps * march_stage_bytes(2, false, true));
+    return true;
+  }();
+  (void)smem_set;
   if (bc.ndof == 1) {
-    march_adjoint_kernel<1><<<grid, 32 * wpc, wpc * march_stage_bytes(1, false), bc.stream>>>(p, x, c.it, u, c.nunits);
-    adj_march_moduli<1><<<mg, kThreads, 0, bc.stream>>>(m, u, c.nunits);
+    march_adjoint_kernel<1><<<grid, 32 * wpc, sb1, bc.stream>>>(p, x, c.it, u, c.nunits);
+    adj_march_moduli<1><<<mg, kThreads, kMarchWarps * adj_moduli_stage_f4(1) * 16, bc.stream>>>(m, u, c.nunits);
   } else {
-    march_adjoint_kernel<2><<<grid, 32 * wpc, wpc * march_stage_bytes(2, false), bc.stream>>>(p, x, c.it, u, c.nunits);
-    adj_march_moduli<2><<<mg, kThreads, 0, bc.stream>>>(m, u, c.nunits);
+    march_adjoint_kernel<2><<<grid, 32 * wpc, sb2, bc.stream>>>(p, x, c.it, u, c.nunits);
+    adj_march_moduli<2><<<mg, kThreads, kMarchWarps * adj_moduli_stage_f4(2) * 16, bc.stream>>>(m, u, c.nunits);
   }
   *launches = 2;
   const cudaError_t e = cudaGetLastError();

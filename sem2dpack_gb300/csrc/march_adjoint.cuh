@@ -65,7 +65,8 @@ __global__ void __launch_bounds__(32 * kMarchWarps, NDOF == 1 ? 4 : 3)
   const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
   extern __shared__ float4 march_stage[];
   if (uid < nunits)
-    march_unit<NDOF, kMatNode, false, true>(p, p.H, p.w, units[uid], it, march_stage + warp * march_stage_f4(NDOF), &x);
+    march_unit<NDOF, kMatNode, false, true>(p, p.H, p.w, units[uid], it,
+                                            march_stage + warp * march_stage_f4(NDOF, false, true), &x);
 }
 
 // The misfit derivatives g of sample smp at the receivers' nodes, thread k
@@ -106,8 +107,12 @@ __global__ void march_adjoint_inject(float *lam, float *wv, long long plane, int
 
 // ---------------------------------------------------------------------
 // the moduli products lambda^n . dF/dtheta d^n
+// the gradient sums' rows of an element row, staged by cp.async when the
+// row starts (per warp: node rows j = 0..4, NQ planes, 16 bytes per lane)
+__host__ __device__ constexpr int adj_moduli_stage_f4(int ndof) { return 5 * (ndof == 2 ? 2 : 1) * 32; }
+
 template <int NDOF>
-__device__ __forceinline__ void adj_moduli_unit(const MarchAdjParams &p, const MarchUnit &u) {
+__device__ __forceinline__ void adj_moduli_unit(const MarchAdjParams &p, const MarchUnit &u, float4 *stage) {
   constexpr int N = 5;
   constexpr int NQ = NDOF == 2 ? 2 : 1;  // d/dla, d/dmu (P-SV) or d/dmu (SH)
   const int lane = threadIdx.x & 31;
@@ -160,10 +165,22 @@ __device__ __forceinline__ void adj_moduli_unit(const MarchAdjParams &p, const M
     const float etaz = act ? p.etaz[ez] : 0.f;
     const float det = dxdxi * (act ? p.dzdeta[ez] : 0.f);
     const float sxz = p.kd2 ? etaz : xix;
+    const bool top_last = ez == p.nz - 1;
+    if (!halo && own) {
+      const int nrow = top_last ? N : N - 1;
+#pragma unroll
+      for (int j = 0; j < N; ++j)
+        if (j < nrow) {
+          const long long g = (long long)(J0 + j) * p.pitch + I0;
+#pragma unroll
+          for (int c = 0; c < NQ; ++c)
+            cp_async16(stage + (j * NQ + c) * 32 + lane, ((NDOF == 2 && c == 0) ? p.g_la : p.g_mu) + g);
+        }
+      cp_async_commit();
+    }
     float Lm[NDOF][N][N], Dm[NDOF][N][N];
     rows(p.lam, J0, Lm);
     rows(p.d, J0, Dm);
-    const bool top_last = ez == p.nz - 1;
     const bool top_shared = !top_last && p.row0[ez + 1] == J0 + N - 1;
     const bool bottom_carry = have_carry;
 #pragma unroll
@@ -222,6 +239,7 @@ __device__ __forceinline__ void adj_moduli_unit(const MarchAdjParams &p, const M
         continue;
       }
       if (halo || !own) continue;
+      if (j == 0) cp_async_wait_all();
       const long long g = (long long)J * p.pitch + I0;
       float sum[NQ][N];
 #pragma unroll
@@ -235,7 +253,7 @@ __device__ __forceinline__ void adj_moduli_unit(const MarchAdjParams &p, const M
 #pragma unroll
       for (int c = 0; c < NQ; ++c) {
         float *G = (NDOF == 2 && c == 0) ? p.g_la : p.g_mu;
-        float4 q = *reinterpret_cast<const float4 *>(G + g);
+        float4 q = stage[(j * NQ + c) * 32 + lane];
         q.x = q.x + sum[c][0];
         q.y = q.y + sum[c][1];
         q.z = q.z + sum[c][2];
@@ -259,8 +277,10 @@ __global__ void __launch_bounds__(32 * kMarchWarps, NDOF == 1 ? 4 : 3)
                          p.smp, p.inj, p.rec_I, p.rec_J, p.resid, p.dt);
     return;
   }
-  const int uid = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (uid < nunits) adj_moduli_unit<NDOF>(p, units[uid]);
+  const int warp = threadIdx.x >> 5;
+  const int uid = blockIdx.x * (blockDim.x >> 5) + warp;
+  extern __shared__ float4 moduli_stage[];
+  if (uid < nunits) adj_moduli_unit<NDOF>(p, units[uid], moduli_stage + warp * adj_moduli_stage_f4(NDOF));
 }
 
 }  // namespace sem2d

@@ -97,18 +97,23 @@ struct MarchBatch {
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-// P-SV in the displacement state (the batch kernel among them): the node
-// update's velocity and inverse-mass rows of an element row are staged in
+// P-SV: the node update's input rows of an element row are staged in
 // shared memory by cp.async when the row starts, so that their loads fly
-// while the element forces are computed (3 % on the batched shots): per
-// warp, node rows j = 0..4, planes v (ndof) and inverse mass, 16 bytes per
-// lane; each lane reads back only what it copied.  (SH and the force state,
-// whose element pass has just read the velocity, load them directly: staged
-// they measured slower.)
-__host__ __device__ constexpr bool march_staged(int ndof, bool fst) { return ndof == 2 && !fst; }
-__host__ __device__ constexpr int march_stage_f4(int ndof) { return 5 * (ndof + 1) * 32; }
-__host__ __device__ constexpr int march_stage_bytes(int ndof, bool fst) {
-  return march_staged(ndof, fst) ? march_stage_f4(ndof) * 16 : 0;
+// while the element forces are computed: per warp, node rows j = 0..4, 16
+// bytes per lane and plane, each lane reading back only what it copied.
+// The planes are those the element pass has not just read: in the
+// displacement state v and the inverse mass (the adjoint step also a^n and
+// the mass sum), in the force state the force and displacement and the
+// inverse mass.  (SH loads them directly: staged it measured slower.)
+__host__ __device__ constexpr bool march_staged(int ndof, bool fst) { return ndof == 2; }
+__host__ __device__ constexpr int march_stage_planes(int ndof, bool fst, bool adj) {
+  return fst ? 2 * ndof + 1 : (adj ? 2 * ndof + 2 : ndof + 1);
+}
+__host__ __device__ constexpr int march_stage_f4(int ndof, bool fst, bool adj = false) {
+  return 5 * march_stage_planes(ndof, fst, adj) * 32;
+}
+__host__ __device__ constexpr int march_stage_bytes(int ndof, bool fst, bool adj = false) {
+  return march_staged(ndof, fst) ? march_stage_f4(ndof, fst, adj) * 16 : 0;
 }
 
 __device__ __forceinline__ void cp_async16(float4 *dst, const float *src) {
@@ -192,8 +197,10 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
   };
   if (kPrefetch) fetch_u(zs);
 
-  constexpr int NP = NDOF + 1;  // staged planes per node row
+  constexpr int NP = march_stage_planes(NDOF, FST, ADJ);  // staged planes per node row
   constexpr bool kStage = march_staged(NDOF, FST);
+  // staged plane index: v (or, in the force state, F then d), inverse mass, a^n, mass sum
+  constexpr int PR = FST ? 2 * NDOF : NDOF, PA = NDOF + 1, PG = 2 * NDOF + 1;
   for (int ez = zs; ez < u.z1; ++ez) {
     const bool halo = ez < u.z0;
     const int J0 = p.row0[ez];
@@ -213,8 +220,20 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         if (j < nrow) {
           const long long g = (long long)(J0 + j) * p.pitch + I0;
 #pragma unroll
-          for (int c = 0; c < NDOF; ++c) cp_async16(stage + (j * NP + c) * 32 + lane, p.Vcur + c * pl + g);
-          cp_async16(stage + (j * NP + NDOF) * 32 + lane, p.rmass + g);
+          for (int c = 0; c < NDOF; ++c) {
+            if (FST) {
+              cp_async16(stage + (j * NP + c) * 32 + lane, p.Fcur + c * pl + g);
+              cp_async16(stage + (j * NP + NDOF + c) * 32 + lane, p.Dcur + c * pl + g);
+            } else {
+              cp_async16(stage + (j * NP + c) * 32 + lane, p.Vcur + c * pl + g);
+            }
+          }
+          cp_async16(stage + (j * NP + PR) * 32 + lane, p.rmass + g);
+          if (ADJ) {
+#pragma unroll
+            for (int c = 0; c < NDOF; ++c) cp_async16(stage + (j * NP + PA + c) * 32 + lane, x->a + c * pl + g);
+            cp_async16(stage + (j * NP + PG) * 32 + lane, x->g_M + g);
+          }
         }
       cp_async_commit();
     }
@@ -415,7 +434,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           // the elastic force of this step: the previous one plus dt (-K v)
 #pragma unroll
           for (int c = 0; c < NDOF; ++c) {
-            const float4 q = ldg4(Fc + c * pl + g);
+            const float4 q = kStage ? stage[(j * NP + c) * 32 + lane] : ldg4(Fc + c * pl + g);
             const float fp[N] = {q.x, q.y, q.z, q.w, last_col ? __ldg(Fc + c * pl + g + 4) : 0.f};
 #pragma unroll
             for (int i = 0; i < N; ++i) f[c][i] = fp[i] + dt * f[c][i];
@@ -441,7 +460,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float vv[NDOF][N], rmv[N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = kStage ? stage[(j * NP + c) * 32 + lane] : ldg4(Vc + c * pl + g);
+          const float4 q = (kStage && !FST) ? stage[(j * NP + c) * 32 + lane] : ldg4(Vc + c * pl + g);
           vv[c][0] = q.x;
           vv[c][1] = q.y;
           vv[c][2] = q.z;
@@ -449,7 +468,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           vv[c][4] = last_col ? __ldg(Vc + c * pl + g + 4) : 0.f;
         }
         {
-          const float4 q = kStage ? stage[(j * NP + NDOF) * 32 + lane] : ldg4(Rm + g);
+          const float4 q = kStage ? stage[(j * NP + PR) * 32 + lane] : ldg4(Rm + g);
           rmv[0] = q.x;
           rmv[1] = q.y;
           rmv[2] = q.z;
@@ -491,7 +510,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
         float dv[NDOF][N];
 #pragma unroll
         for (int c = 0; c < NDOF; ++c) {
-          const float4 q = ldg4(Dc + c * pl + g);
+          const float4 q = (kStage && FST) ? stage[(j * NP + NDOF + c) * 32 + lane] : ldg4(Dc + c * pl + g);
           dv[c][0] = q.x;
           dv[c][1] = q.y;
           dv[c][2] = q.z;
@@ -506,7 +525,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           float vn[N], dn[N], an[N];
           float aq[N];
           if (ADJ) {
-            const float4 q = ldg4(x->a + c * pl + g);
+            const float4 q = kStage ? stage[(j * NP + PA + c) * 32 + lane] : ldg4(x->a + c * pl + g);
             aq[0] = q.x;
             aq[1] = q.y;
             aq[2] = q.z;
@@ -552,7 +571,7 @@ __device__ __forceinline__ void march_unit(const BulkParams<float, 5> &p, const 
           }
         }
         if (ADJ) {
-          float4 q = *reinterpret_cast<const float4 *>(x->g_M + g);
+          float4 q = kStage ? stage[(j * NP + PG) * 32 + lane] : *reinterpret_cast<const float4 *>(x->g_M + g);
           q.x = q.x + gm[0];
           q.y = q.y + gm[1];
           q.z = q.z + gm[2];
@@ -616,7 +635,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   extern __shared__ float4 march_stage[];
   if (uid < nunits) {
     const MarchUnit u = units[uid];
-    march_unit<NDOF, MAT, FST>(p, p.H, p.w, u, it, march_stage + warp * march_stage_f4(NDOF));
+    march_unit<NDOF, MAT, FST>(p, p.H, p.w, u, it, march_stage + warp * march_stage_f4(NDOF, FST));
   }
   march_done(p.step, p.done, it);
 }
@@ -632,7 +651,7 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   extern __shared__ float4 march_stage[];
   if (uid < b.nunits) {
     const MarchUnit u = b.units[uid];
-    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, u, it, march_stage + warp * march_stage_f4(NDOF));
+    march_unit<NDOF, MAT, false>(b.sims[u.prob], b.H, b.w, u, it, march_stage + warp * march_stage_f4(NDOF, false));
   }
   march_done(b.step, b.done, it);
 }
@@ -650,7 +669,8 @@ __global__ void __launch_bounds__(32 * kMarchWarps, MarchOcc<NDOF>::kMinBlocks)
   const int it = *p.step + 1;
   extern __shared__ float4 march_stage[];
   if (warp < nrows)
-    march_unit<NDOF, MAT, FST>(p, p.H, p.w, units[warp * nstrips + s], it, march_stage + warp * march_stage_f4(NDOF));
+    march_unit<NDOF, MAT, FST>(p, p.H, p.w, units[warp * nstrips + s], it,
+                               march_stage + warp * march_stage_f4(NDOF, FST));
   __syncthreads();  // the strip's fault-row forces are written (global memory, this block)
   const int t = threadIdx.x, I = 4 * kMarchCols * s + t;
   const bool mine = (t < 4 * kMarchCols && I < p.LX) || (t == 4 * kMarchCols && I == p.LX - 1);
