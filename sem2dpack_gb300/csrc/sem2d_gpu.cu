@@ -2408,6 +2408,9 @@ int batch_add_parallel(sem2d_handle *h, const sem2d_problem_desc *descs, int n) 
       } catch (const std::bad_alloc &) {
         ms[i]->err = "out of host memory";
         st[i] = SEM2D_E_NOMEM;
+      } catch (...) {  // nothing may leave a worker thread
+        ms[i]->err = "host exception while setting the member up";
+        st[i] = SEM2D_E_NOMEM;
       }
       if (!st[i]) {
         std::vector<int>().swap(ms[i]->elem_ex);
