@@ -424,7 +424,8 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     bpn = BYTES_PER_NODE_STEP[(2, dtype)]
     achieved = npoin * bpn / (bulk_ms / 1000.0) / 1e9
     peaks, peak_kind = measured_peaks()
-    kernel = "march_batch_kernel" if sim.tile[0] == MARCH_TX else "strip_batch_kernel"
+    shape = sim.tile
+    kernel = "march_batch_kernel" if shape[0] == MARCH_TX else "strip_batch_kernel"
     traffic = ncu_traffic(kernel, "batch_shots", npoin)
     t0 = time.perf_counter()
     sim.close()
@@ -464,7 +465,8 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
                                        "benchmark steps" % (nt, len(parts)),
                        "precision": "FP32 fields" if dtype == "f32" else "FP64",
                        "l2": "inputs larger than L2 (the batch's fields are %.1f GB)" % (npoin * bpn / 1e9),
-                       "host_setup_s": setup_s, "host_build_s": build_s},
+                       "host_setup_s": setup_s, "host_build_s": build_s,
+                       "launch_shape": {"element_columns": shape[0], "chunk_rows": shape[1]}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peaks.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / peaks.get("hbm_gbs"),
                          "traffic": traffic, "peak_kind": peak_kind,

@@ -2064,7 +2064,7 @@ int tune_on_run(sem2d_handle *h) {
   const sem2d_handle *a = h->subs.empty() ? h : h->subs[0];
   const int cz0 = a->march_cz;
   const MarchShape cands[kTuneShapes] = {{cz0, a->march_warps}, {cz0, 1}, {2 * cz0, a->march_warps},
-                                         {std::max(1, cz0 / 2), a->march_warps}, {2 * cz0, 1}};
+                                         {std::max(1, cz0 / 2), a->march_warps}, {4 * cz0, a->march_warps}};
   std::vector<sem2d_tune_entry> res(kTuneShapes);
   int st;
   for (int k = 0; k < kTuneShapes; ++k) {
