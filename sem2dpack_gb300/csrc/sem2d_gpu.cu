@@ -2040,10 +2040,10 @@ bool tune_key(const sem2d_handle *h, char *key, size_t n) {
 }
 
 int tune_march(sem2d_handle *h) {
-  // a problem with a fault keeps the analytic shape: its step time is set
-  // as much by the fault side on the second stream, and timed shapes of
-  // the first steps (the fault at rest) picked slower ones
-  if (!h->march || tune_disabled() || h->nflt > 0) return SEM2D_OK;
+  // a rate-and-state fault keeps the analytic shape: its step time is set as
+  // much by the Newton solves on the second stream, and the shape timed on
+  // the first steps (the fault at rest) was slower over the run
+  if (!h->march || tune_disabled() || (h->nflt > 0 && h->friction == SEM2D_FRICTION_RSF)) return SEM2D_OK;
   char key[160], path[1024];
   if (!tune_key(h, key, sizeof(key))) return SEM2D_OK;
   sem2d_tune_entry e;
