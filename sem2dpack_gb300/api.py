@@ -302,7 +302,8 @@ class BatchSolver:
                 raise Sem2dError(st, lib().sem2d_gpu_last_error(None).decode())
             self.h = h
             descs = []
-            group = group or int(os.environ.get("SEM2D_HOST_THREADS", "0")) or min(16, os.cpu_count() or 1)
+            env = os.environ.get("SEM2D_HOST_THREADS", "")
+            group = group or (int(env) if env.isdigit() else 0) or min(16, os.cpu_count() or 1)
             held = []  # the group's problems, alive until their upload returns
 
             def flush():

@@ -2419,7 +2419,8 @@ int batch_add_parallel(sem2d_handle *h, const sem2d_problem_desc *descs, int n) 
     }
   };
   int nthr = int(std::thread::hardware_concurrency());
-  if (const char *e = std::getenv("SEM2D_HOST_THREADS")) nthr = std::atoi(e);
+  if (const char *e = std::getenv("SEM2D_HOST_THREADS"))
+    if (std::atoi(e) > 0) nthr = std::atoi(e);
   nthr = std::max(1, std::min({nthr > 0 ? nthr : 1, 16, n}));
   std::vector<std::thread> pool;
   try {
