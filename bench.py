@@ -605,6 +605,13 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
     # (lambda, w) step 60: lambda, w read and written, moduli, inverse mass,
     # a^n, the mass sum; the moduli pass 32: lambda^n, d^n, the two sums)
     bound = (44 + 68 + 60 + 32) / 44
+    # aggregate roofline of the forward solves: 44 B per node-step over
+    # their wall time, and of the whole gradient: the 204 B its three
+    # phases move per node-step over its wall time
+    peaks, peak_kind = measured_peaks()
+    hbm = peaks.get("hbm_gbs")
+    fwd_gbs = len(sims) * npoin * nt * 44 / fwd / 1e9
+    grd_gbs = len(sims) * npoin * nt * (44 + 68 + 60 + 32) / grd / 1e9
     if rank == 0:
         print(json.dumps({
             "metric": "GLL node-steps/s", "value": value, "unit": "node-steps/s", "n_gpus": world,
@@ -618,7 +625,12 @@ def run_gradient(args, rank, world, local, torch, dist, barrier):
                               "note": "forward with checkpoints + segment recomputation + adjoint, "
                                       "over the plain forward solves of the same shots; bytes_bound: the "
                                       "ratio of the bytes per node the three phases move to a forward step's"},
-            "roofline": None, "cpu_baseline": None,
+            "roofline": {"bound": "hbm", "achieved": fwd_gbs, "peak": hbm, "unit": "GB/s",
+                         "frac": fwd_gbs / hbm if hbm else None, "traffic": None, "peak_kind": peak_kind,
+                         "note": "forward solves of the 8 shots, 44 B per node-step over their wall time",
+                         "gradient_achieved": grd_gbs,
+                         "gradient_frac": grd_gbs / hbm if hbm else None},
+            "cpu_baseline": None,
             "e2e": {"value": e2e_value, "unit": "node-steps/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "path": "Solver creation of every shot from host arrays, one "
                                                        "forward solve each, seismograms back"},
