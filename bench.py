@@ -316,6 +316,29 @@ def batch_parts(nt, k):
     return [nt // k + (1 if i < nt % k else 0) for i in range(k)]
 
 
+# problems built and uploaded per group of the batched workload: the host
+# holds one group (about 11 GB of arrays for 64 shots) at a time
+BUILD_GROUP = 64
+
+
+def built_groups(decks, workers, group, build_s):
+    """Problems of the decks in order, built `group` at a time on `workers`
+    host threads; a group is built only when the previous one has been
+    taken (BatchSolver uploads each group with one batch_add_many call, so
+    building and uploading do not compete for the host threads).  The
+    building time is added to build_s[0]."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from sem2dpack_gb300 import workloads
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        for k in range(0, len(decks), group):
+            t0 = time.perf_counter()
+            probs = list(ex.map(workloads.build, decks[k:k + group]))
+            build_s[0] += time.perf_counter() - t0
+            while probs:
+                yield probs.pop(0)
+
+
 def oracle_sample(decks, nsteps_of, threads):
     """Runs the FP64 oracle (CPU restatement of the reference's step, one
     problem per host thread, as independent reference runs would) on the
@@ -357,17 +380,10 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     nt = min(args.time_steps or 3000, 3000)
     workers = max(1, min(16, os.cpu_count() or 1))
     t0 = time.perf_counter()
-    # every problem built first on host threads (about 60 GB of host
-    # arrays for the 256 shots), then one create_batch call uploads them
-    # with the members set up on host threads; the arrays are released
-    # once the batch holds its device copies
-    from concurrent.futures import ThreadPoolExecutor
-    with ThreadPoolExecutor(max_workers=workers) as ex:
-        probs = list(ex.map(workloads.build, decks))
-    build_s = time.perf_counter() - t0
-    sim = BatchSolver([P.desc() for P in probs])
-    del probs
+    build_s = [0.0]
+    sim = BatchSolver(built_groups(decks, workers, BUILD_GROUP, build_s), group=BUILD_GROUP)
     setup_s = time.perf_counter() - t0
+    build_s = build_s[0]
     descs = [m.desc for m in sim.members]
     npoin = sum(d.npoin for d in descs)
     h2d = sum(desc_bytes(d) for d in descs)
@@ -377,7 +393,7 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
     stream = torch.cuda.ExternalStream(sim.stream)
 
     # end to end through the C-ABI from host arrays: the upload
-    # (sem2d_gpu_create_batch), one complete solve,
+    # (sem2d_gpu_batch_add_many per group), one complete solve,
     # every member's seismograms back, and (below) the destroy
     barrier()
     t0 = time.perf_counter()
@@ -478,9 +494,9 @@ def run_batch(args, rank, world, local, torch, dist, barrier):
                     "h2d_bytes_per_step": h2d / len(parts), "d2h_bytes_per_step": d2h / len(parts),
                     "h2d_bytes_per_solve": h2d, "d2h_bytes_per_solve": d2h,
                     "upload_s": sim.upload_seconds, "run_s": t_run, "destroy_s": t_close,
-                    "path": "BatchSolver through the C-ABI: sem2d_gpu_create_batch of every shot from host "
-                            "arrays (members set up on host threads), one complete solve, all seismograms "
-                            "back, destroy"},
+                    "path": "BatchSolver through the C-ABI: sem2d_gpu_batch_add_many of every shot from host "
+                            "arrays in groups of %d (members set up on host threads), one complete solve, all "
+                            "seismograms back, destroy" % BUILD_GROUP},
             "fp64_plain": fp64,
             "clocks": clk,
             "gpu_launches": launches,
